@@ -1,0 +1,37 @@
+#!/bin/sh
+# Builds the REFERENCE's own hot-path routines, from the unmodified sources
+# where they lie, into oracle/_ref/ (git-ignored).  Used only to pin the
+# oracle and to generate golden fixtures; the reference tree is only present
+# on the development machine, so this is skipped elsewhere.
+#
+#   ref_harness       strict IEEE build (-O2 -ffp-contract=off, no fast-math):
+#                     bit-reproducible, used for golden vectors
+#   ref_harness_fast  the reference makefile's own flags (makefile:84-88:
+#                     -O3 -ffast-math -funroll-all-loops -std=c99), for timing
+#
+# Feature flags: -DNLIST -DEWALD -DSPME -DSTYPE.  FFTW3 is not installed, so
+# the five FFTW symbols come from oracle/fftw_shim (the oracle's own FFT).
+set -e
+REF=${REF:-/root/reference}
+HERE=$(cd "$(dirname "$0")" && pwd)
+OUT="$HERE/_ref"
+if [ ! -f "$REF/defines.h" ]; then
+  echo "build_ref: reference sources not present; skipped"
+  exit 0
+fi
+mkdir -p "$OUT"
+SRCS="nblist cnonbond_nblist pme_qgrid pme_spline pme_setup pme_calc forces
+      cbond cbend curey ctorsion cimproper integrate_vverlet pbc_all kinet
+      integrate_nhc setlj ewald"
+FEAT="-DNLIST -DEWALD -DSPME -DSTYPE"
+build() {
+  name=$1; shift
+  files=""
+  for s in $SRCS; do files="$files $REF/$s.c"; done
+  gcc "$@" $FEAT -I"$HERE/fftw_shim" -I"$REF" -w -o "$OUT/$name" \
+      "$HERE/ref_harness.c" $files "$HERE/fftw_shim/fftw_shim.c" \
+      "$HERE/fe_fft.c" -lm
+}
+build ref_harness -std=gnu99 -O2 -ffp-contract=off
+build ref_harness_fast -std=c99 -D_POSIX_C_SOURCE=200809L -O3 -ffast-math -funroll-all-loops
+echo "build_ref: built $OUT/ref_harness and $OUT/ref_harness_fast"

@@ -1,0 +1,327 @@
+"""ctypes front end of the CPU oracle (fe_oracle.c) -- TEST INFRASTRUCTURE.
+
+Only tests/, __graft_entry__.smoke() and bench.py's cpu_baseline / reference
+legs may import this module, and only as the checker or the timed CPU
+baseline.  The product path (thecodecombo_7_gb300) never imports it.
+
+Also writes the binary system file read by ref_harness.c (the driver of the
+reference's own routines) and reads its tagged output.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import struct
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "liboracle.so")
+SRC = [os.path.join(HERE, "fe_oracle.c"), os.path.join(HERE, "fe_fft.c")]
+REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
+REF_BIN_FAST = os.path.join(HERE, "_ref", "ref_harness_fast")
+
+# strict IEEE: no FMA contraction, no fast-math, so results are reproducible
+# on x86-64 and aarch64 alike and match a strict build of the reference
+CFLAGS = ["-O2", "-std=gnu99", "-fPIC", "-shared", "-ffp-contract=off",
+          "-fno-fast-math"]
+
+
+def build(force: bool = False) -> str:
+    newest = max(os.path.getmtime(p) for p in SRC + [os.path.join(HERE, "fe_oracle.h")])
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < newest:
+        tmp = LIB + ".tmp"
+        subprocess.check_call(["gcc", *CFLAGS, "-o", tmp, *SRC, "-lm"])
+        os.replace(tmp, LIB)
+    return LIB
+
+
+def build_reference() -> bool:
+    """Compile the reference's own routines into oracle/_ref (only where the
+    reference sources exist).  Returns True when the binary is available."""
+    script = os.path.join(HERE, "build_ref.sh")
+    if os.path.exists("/root/reference/defines.h"):
+        subprocess.check_call(["sh", script])
+    return os.path.exists(REF_BIN)
+
+
+class OrSystem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("ntypes", C.c_int), ("L", C.c_double * 3),
+        ("rc", C.c_double), ("rclist", C.c_double), ("rclist_ew", C.c_double),
+        ("kappa", C.c_double), ("epsRF", C.c_double), ("dt", C.c_double),
+        ("T", C.c_double), ("grid", C.c_int * 3), ("order", C.c_int),
+        ("r_switch", C.c_double),
+        ("q", C.c_void_p), ("mass", C.c_void_p), ("type", C.c_void_p),
+        ("lj_eps", C.c_void_p), ("lj_sig", C.c_void_p),
+        ("nbond", C.c_int), ("bond_ab", C.c_void_p), ("bond_req", C.c_void_p),
+        ("bond_k", C.c_void_p),
+        ("nbend", C.c_int), ("bend_abc", C.c_void_p),
+        ("bend_theta0", C.c_void_p), ("bend_k", C.c_void_p),
+        ("nexcl", C.c_int), ("excl_ab", C.c_void_p), ("excl_flag", C.c_void_p),
+    ]
+
+
+class OrEnergy(C.Structure):
+    _fields_ = [(k, C.c_double) for k in (
+        "bond", "bend", "nbond", "nbonds", "coulomb", "rewald", "rewalds",
+        "kewald", "sewald", "iewald", "tewald")]
+
+    def asdict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+EN_KEYS = ["kinet", "bond", "bend", "nbond", "nbonds", "coulomb", "rewald",
+           "rewalds", "kewald", "sewald", "iewald", "tewald"]
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+class Oracle:
+    """Holds one system's arrays alive and exposes the restated routines."""
+
+    def __init__(self, sysm):
+        self.lib = C.CDLL(build())
+        L = self.lib
+        L.or_nblist.restype = C.c_int64
+        L.or_ewald_self.restype = C.c_double
+        L.or_kinet.restype = C.c_double
+        L.or_cbond.restype = C.c_double
+        L.or_cbend.restype = C.c_double
+        L.or_run_md.restype = C.c_int
+        L.or_ewald_kspace_energy.restype = C.c_double
+        L.or_mc_delta_energy.restype = C.c_double
+        L.or_ewald_nk.restype = C.c_int
+        self.sysm = sysm
+        eps, sig = sysm.lj_tables()
+        self._keep = dict(
+            q=np.ascontiguousarray(sysm.q, np.float64),
+            mass=np.ascontiguousarray(sysm.mass, np.float64),
+            type=np.ascontiguousarray(sysm.type, np.int32),
+            eps=np.ascontiguousarray(eps), sig=np.ascontiguousarray(sig),
+            bond_ab=np.ascontiguousarray(sysm.bonds, np.int32),
+            bond_req=np.ascontiguousarray(sysm.bond_req, np.float64),
+            bond_k=np.ascontiguousarray(sysm.bond_k, np.float64),
+            bend_abc=np.ascontiguousarray(sysm.bends, np.int32),
+            bend_t0=np.ascontiguousarray(sysm.bend_theta0, np.float64),
+            bend_k=np.ascontiguousarray(sysm.bend_k, np.float64),
+            excl_ab=np.ascontiguousarray(sysm.excl, np.int32),
+            excl_flag=np.ascontiguousarray(sysm.excl_flag, np.int32),
+        )
+        k = self._keep
+        s = OrSystem()
+        s.n = sysm.n
+        s.ntypes = sysm.ntypes
+        s.L[:] = [float(x) for x in sysm.L]
+        s.rc, s.rclist, s.rclist_ew = sysm.rc, sysm.rclist, sysm.rclist_ew
+        s.kappa, s.epsRF, s.dt, s.T = sysm.kappa, sysm.epsRF, sysm.dt, sysm.T
+        s.grid[:] = list(sysm.grid)
+        s.order = sysm.order
+        s.r_switch = sysm.r_switch
+        s.q, s.mass, s.type = _p(k["q"]), _p(k["mass"]), _p(k["type"])
+        s.lj_eps, s.lj_sig = _p(k["eps"]), _p(k["sig"])
+        s.nbond = k["bond_ab"].shape[0]
+        s.bond_ab, s.bond_req, s.bond_k = _p(k["bond_ab"]), _p(k["bond_req"]), _p(k["bond_k"])
+        s.nbend = k["bend_abc"].shape[0]
+        s.bend_abc, s.bend_theta0, s.bend_k = _p(k["bend_abc"]), _p(k["bend_t0"]), _p(k["bend_k"])
+        s.nexcl = k["excl_ab"].shape[0]
+        s.excl_ab, s.excl_flag = _p(k["excl_ab"]), _p(k["excl_flag"])
+        self.s = s
+        self.sp = C.byref(s)
+
+    # ---- neighbour list ----
+    def nblist(self, pos, with_ew=False):
+        n = self.sysm.n
+        pos = np.ascontiguousarray(pos, np.float64)
+        cap = n * 800 + 64
+        cnt = np.zeros(n, np.int32)
+        idx = np.zeros(cap, np.int32)
+        flg = np.zeros(cap, np.int32)
+        if with_ew:
+            cnt_e = np.zeros(n, np.int32)
+            idx_e = np.zeros(cap, np.int32)
+            flg_e = np.zeros(cap, np.int32)
+            tot = self.lib.or_nblist(self.sp, _p(pos), _p(cnt), _p(idx), _p(flg), C.c_int64(cap),
+                                     _p(cnt_e), _p(idx_e), _p(flg_e), C.c_int64(cap))
+        else:
+            tot = self.lib.or_nblist(self.sp, _p(pos), _p(cnt), _p(idx), _p(flg), C.c_int64(cap),
+                                     None, None, None, C.c_int64(0))
+        if tot < 0:
+            raise RuntimeError("oracle neighbour list overflow")
+        out = (cnt, idx[:tot].copy(), flg[:tot].copy())
+        if with_ew:
+            te = int(cnt_e.sum())
+            out = out + (cnt_e, idx_e[:te].copy(), flg_e[:te].copy())
+        return out
+
+    # ---- forces ----
+    def forces(self, pos, lst=None):
+        pos = np.ascontiguousarray(pos, np.float64)
+        if lst is None:
+            lst = self.nblist(pos)
+        cnt, idx, flg = lst
+        ff = np.zeros((self.sysm.n, 3))
+        en = OrEnergy()
+        sew = self.lib.or_ewald_self(self.sp)
+        self.lib.or_forces(self.sp, _p(pos), _p(cnt), _p(idx), _p(flg), C.c_double(sew),
+                           _p(ff), C.byref(en))
+        return ff, en.asdict()
+
+    def pair_forces(self, pos, lst):
+        pos = np.ascontiguousarray(pos, np.float64)
+        cnt, idx, flg = lst
+        ff = np.zeros((self.sysm.n, 3))
+        e5 = np.zeros(5)
+        self.lib.or_cnonbond_pairs(self.sp, _p(pos), _p(cnt), _p(idx), _p(flg), _p(ff), _p(e5))
+        return ff, e5
+
+    def pme(self, pos):
+        pos = np.ascontiguousarray(pos, np.float64)
+        ff = np.zeros((self.sysm.n, 3))
+        e3 = np.zeros(3)
+        sew = self.lib.or_ewald_self(self.sp)
+        self.lib.or_pme_calc(self.sp, _p(pos), C.c_double(sew), _p(ff), _p(e3))
+        return ff, e3
+
+    def charge_grid(self, pos):
+        pos = np.ascontiguousarray(pos, np.float64)
+        g = np.zeros(int(np.prod(self.sysm.grid)))
+        self.lib.or_charge_grid(self.sp, _p(pos), _p(g))
+        return g.reshape(self.sysm.grid)
+
+    def bspline_moduli(self):
+        gx, gy, gz = self.sysm.grid
+        bx, by, bz = np.zeros(gx + 2), np.zeros(gy + 2), np.zeros(gz + 2)
+        self.lib.or_pme_bspline(self.sp, _p(bx), _p(by), _p(bz))
+        return bx[1:gx + 1], by[1:gy + 1], bz[1:gz + 1]
+
+    def bonded(self, pos):
+        pos = np.ascontiguousarray(pos, np.float64)
+        ff = np.zeros((self.sysm.n, 3))
+        eb = self.lib.or_cbond(self.sp, _p(pos), _p(ff))
+        ea = self.lib.or_cbend(self.sp, _p(pos), _p(ff))
+        return ff, eb, ea
+
+    def ewald_self(self):
+        return self.lib.or_ewald_self(self.sp)
+
+    def kinet(self, vv, uu=None):
+        vv = np.ascontiguousarray(vv, np.float64)
+        uu = vv if uu is None else np.ascontiguousarray(uu, np.float64)
+        ken = np.zeros(6)
+        k = self.lib.or_kinet(self.sp, _p(vv), _p(uu), _p(ken))
+        return k, ken
+
+    def integrate_nhc(self, vv, uu, zeta, M, Q, nfree=None):
+        vv = np.ascontiguousarray(vv, np.float64)
+        uu = np.ascontiguousarray(uu, np.float64)
+        zeta = np.ascontiguousarray(zeta, np.float64)
+        if nfree is None:
+            nfree = 3.0 * self.sysm.n - 3.0
+        self.lib.or_integrate_nhc(self.sp, C.c_double(self.sysm.dt), C.c_int(M),
+                                  C.c_double(Q), C.c_double(nfree), _p(zeta), _p(vv), _p(uu))
+        return vv, uu, zeta
+
+    def run_md(self, nsteps, use_nhc=False, pos=None, vel=None):
+        s = self.sysm
+        pos = np.ascontiguousarray(s.pos if pos is None else pos, np.float64).copy()
+        nop = pos.copy()
+        vv = np.ascontiguousarray(s.vel if vel is None else vel, np.float64).copy()
+        ff = np.zeros_like(pos)
+        M = s.nhc_M
+        zeta = np.zeros(3 * max(M, 1))
+        kT = 1.380662e-23 * s.T * 1e-4
+        for i in range(M - 1):  # read_config.c:369-370
+            zeta[3 * (i + 1) + 2] = (s.nhc_Q * zeta[3 * i + 1] ** 2 - kT) / s.nhc_Q
+        rec = np.zeros((nsteps + 1, 12))
+        rc = self.lib.or_run_md(self.sp, nsteps, s.nlist_freq, int(use_nhc), M,
+                                C.c_double(s.nhc_Q), _p(pos), _p(nop), _p(vv), _p(ff),
+                                _p(zeta), _p(rec))
+        if rc != 0:
+            raise RuntimeError("oracle md failed (list overflow)")
+        return dict(en=rec, pos=pos, pos_nopbc=nop, vel=vv, force=ff, zeta=zeta.reshape(-1, 3))
+
+    # ---- MC ----
+    def ewald_kspace_energy(self, pos, kmax=7, max_k_square=49):
+        pos = np.ascontiguousarray(pos, np.float64)
+        return self.lib.or_ewald_kspace_energy(self.sp, _p(pos), kmax, max_k_square)
+
+    def mc_delta_energy(self, pos, pos_new, lb, ub, kmax=7, max_k_square=49, rc_ew=None):
+        pos = np.ascontiguousarray(pos, np.float64)
+        pos_new = np.ascontiguousarray(pos_new, np.float64)
+        parts = np.zeros(3)
+        rc_ew = self.sysm.rc_ew if rc_ew is None else rc_ew
+        de = self.lib.or_mc_delta_energy(self.sp, _p(pos), _p(pos_new), lb, ub, kmax,
+                                         max_k_square, C.c_double(rc_ew), _p(parts))
+        return de, parts
+
+
+# ---------------------------------------------------------------------------
+# binary system file for ref_harness.c, and its tagged output
+
+def write_system_file(path, sysm):
+    n = sysm.n
+    hi = [n, sysm.ntypes, sysm.bonds.shape[0], sysm.bends.shape[0], sysm.excl.shape[0],
+          *sysm.grid, sysm.order, sysm.nhc_M, sysm.nlist_freq, 0]
+    hd = [*sysm.L, sysm.rc, sysm.rclist, sysm.rclist_ew, sysm.rc_ew, sysm.kappa,
+          sysm.epsRF, sysm.dt, sysm.T, sysm.nhc_Q]
+    with open(path, "wb") as f:
+        f.write(b"FESYS01\0")
+        f.write(struct.pack("<12i", *hi))
+        f.write(struct.pack("<12d", *hd))
+        for t in range(sysm.ntypes):
+            f.write(struct.pack("<2d", sysm.type_eps_kcal[t], sysm.type_rmin_half[t]))
+        rec = np.zeros(n, dtype=[("r", "<f8", 5), ("t", "<i4")])
+        rec["r"][:, :3] = sysm.pos
+        rec["r"][:, 3] = sysm.q
+        rec["r"][:, 4] = sysm.mass
+        rec["t"] = sysm.type
+        f.write(rec.tobytes())
+        f.write(np.ascontiguousarray(sysm.vel, "<f8").tobytes())
+        b = np.zeros(sysm.bonds.shape[0], dtype=[("ab", "<i4", 2), ("p", "<f8", 2)])
+        b["ab"] = sysm.bonds
+        b["p"][:, 0] = sysm.bond_req
+        b["p"][:, 1] = sysm.bond_k
+        f.write(b.tobytes())
+        a = np.zeros(sysm.bends.shape[0], dtype=[("abc", "<i4", 3), ("p", "<f8", 2)])
+        a["abc"] = sysm.bends
+        a["p"][:, 0] = sysm.bend_theta0
+        a["p"][:, 1] = sysm.bend_k
+        f.write(a.tobytes())
+        x = np.zeros((sysm.excl.shape[0], 3), "<i4")
+        x[:, :2] = sysm.excl
+        x[:, 2] = sysm.excl_flag
+        f.write(x.tobytes())
+
+
+def read_tagged(path):
+    out = {}
+    with open(path, "rb") as f:
+        data = f.read()
+    p = 0
+    while p < len(data):
+        tag = data[p:p + 16].split(b"\0", 1)[0].decode()
+        (nb,) = struct.unpack("<q", data[p + 16:p + 24])
+        p += 24
+        raw = data[p:p + nb]
+        p += nb
+        if tag.endswith(("_cnt", "_idx", "_flg")):
+            out[tag] = np.frombuffer(raw, "<i4").copy()
+        else:
+            out[tag] = np.frombuffer(raw, "<f8").copy()
+    return out
+
+
+def run_reference(mode, sysm, workdir, nsteps=None, fast=False):
+    """Run the reference's own routines (oracle/_ref) on sysm."""
+    binp = REF_BIN_FAST if fast else REF_BIN
+    os.makedirs(workdir, exist_ok=True)
+    sp = os.path.join(workdir, "system.bin")
+    op = os.path.join(workdir, f"out_{mode}.bin")
+    write_system_file(sp, sysm)
+    cmd = [binp, mode, sp, op] + ([str(nsteps)] if nsteps is not None else [])
+    subprocess.check_call(cmd)
+    return read_tagged(op)

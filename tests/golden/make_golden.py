@@ -1,0 +1,83 @@
+"""Generates the golden fixtures in this folder from the REFERENCE itself.
+
+The reference's own hot-path routines are compiled from its unmodified C
+sources (oracle/build_ref.sh -> oracle/_ref/ref_harness, strict IEEE build)
+and driven by oracle/ref_harness.c on seeded synthetic water boxes; their
+outputs are stored as compressed .npz files.  Needs the reference sources, so
+it runs on the development machine only:
+
+    python tests/golden/make_golden.py
+
+Fixtures:
+  water600.npz   600 sites, L = 25 A, SPME grid 24x25x27 (odd, non-cubic):
+                 full pair lists (nlist + nlist_ew with xflags), spread grid,
+                 force breakdown, energies, 12-step NVE and NHC trajectories
+                 (list rebuilt every 5 steps)
+  water4095.npz  the 4,095-site box at 0.1 sites/A^3 (L = 34.47 A, grid 32^3):
+                 per-atom list counts, a SHA-256 of the sorted pair list,
+                 forces and energies
+"""
+import hashlib
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from thecodecombo_7_gb300 import systems  # noqa: E402
+
+
+def sys_arrays(s):
+    return dict(L=s.L, pos=s.pos, vel=s.vel, q=s.q, mass=s.mass, type=s.type,
+                grid=np.array(s.grid), nlist_freq=np.array(s.nlist_freq))
+
+
+def pair_hash(cnt, idx):
+    rows = np.repeat(np.arange(cnt.shape[0], dtype=np.int64), cnt)
+    key = rows * (1 << 32) + idx.astype(np.int64)
+    return hashlib.sha256(np.sort(key).tobytes()).hexdigest()
+
+
+def main():
+    if not O.build_reference():
+        raise SystemExit("reference sources not available")
+    tmp = tempfile.mkdtemp(prefix="fe_golden_")
+    # ---- small system, full detail ----
+    s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27))
+    s.nlist_freq = 5
+    nb = O.run_reference("nblist", s, tmp)
+    fo = O.run_reference("forces", s, tmp)
+    nve = O.run_reference("nve", s, tmp, nsteps=12)
+    nhc = O.run_reference("nhc", s, tmp, nsteps=12)
+    out = sys_arrays(s)
+    for k, v in nb.items():
+        out["nblist_" + k] = v
+    for k, v in fo.items():
+        out["forces_" + k] = v
+    for k, v in nve.items():
+        out["nve_" + k] = v
+    for k, v in nhc.items():
+        out["nhc_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "water600.npz"), **out)
+    # ---- the 4,095-site box ----
+    s = systems.water_box(1365, density=0.1, seed=2024)
+    nb = O.run_reference("nblist", s, tmp)
+    fo = O.run_reference("forces", s, tmp)
+    out = sys_arrays(s)
+    out["nl_cnt"] = nb["nl_cnt"]
+    out["nl_hash"] = np.array(pair_hash(nb["nl_cnt"], nb["nl_idx"]))
+    out["nl_nflag"] = np.array([(nb["nl_flg"] == f).sum() for f in range(5)])
+    for k in ("f_total", "f_pme", "f_nonbond", "f_bonded", "e_pme", "e_nonbond",
+              "e_bonded", "en"):
+        out["forces_" + k] = fo[k]
+    np.savez_compressed(os.path.join(HERE, "water4095.npz"), **out)
+    print("golden fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,115 @@
+"""Pins the CPU oracle (oracle/fe_oracle.c) to the reference.
+
+(1) against golden fixtures made by running the reference's own routines
+    (tests/golden/make_golden.py) -- bit for bit;
+(2) against the reference built from source right now, when its sources are
+    present (development machine only);
+(3) the oracle's FFT against numpy's DFT.
+"""
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.helpers import system_from_golden
+
+
+def _pair_hash(cnt, idx):
+    rows = np.repeat(np.arange(cnt.shape[0], dtype=np.int64), cnt)
+    key = rows * (1 << 32) + idx.astype(np.int64)
+    return hashlib.sha256(np.sort(key).tobytes()).hexdigest()
+
+
+def test_oracle_lists_bit_exact(golden600):
+    s = system_from_golden(golden600, 200)
+    orc = O.Oracle(s)
+    cnt, idx, flg, ce, ie, fe = orc.nblist(s.pos, with_ew=True)
+    np.testing.assert_array_equal(cnt, golden600["nblist_nl_cnt"])
+    np.testing.assert_array_equal(idx, golden600["nblist_nl_idx"])
+    np.testing.assert_array_equal(flg, golden600["nblist_nl_flg"])
+    np.testing.assert_array_equal(ce, golden600["nblist_nlew_cnt"])
+    np.testing.assert_array_equal(ie, golden600["nblist_nlew_idx"])
+    np.testing.assert_array_equal(fe, golden600["nblist_nlew_flg"])
+
+
+def test_oracle_forces_bit_exact(golden600):
+    g = golden600
+    s = system_from_golden(g, 200)
+    orc = O.Oracle(s)
+    lst = orc.nblist(s.pos)
+    ff, en = orc.forces(s.pos, lst)
+    np.testing.assert_array_equal(ff.ravel(), g["forces_f_total"])
+    ref_en = dict(zip(O.EN_KEYS, g["forces_en"]))
+    for k, v in en.items():
+        assert v == ref_en[k], k
+    grid = orc.charge_grid(s.pos)
+    np.testing.assert_array_equal(grid.ravel(), g["forces_qgrid"])
+    fp, e3 = orc.pme(s.pos)
+    np.testing.assert_array_equal(fp.ravel(), g["forces_f_pme"])
+    np.testing.assert_array_equal(e3, g["forces_e_pme"])
+    fb, eb, ea = orc.bonded(s.pos)
+    np.testing.assert_array_equal(fb.ravel(), g["forces_f_bonded"])
+    assert (eb, ea) == tuple(g["forces_e_bonded"])
+
+
+@pytest.mark.parametrize("mode", ["nve", "nhc"])
+def test_oracle_trajectory_bit_exact(golden600, mode):
+    g = golden600
+    s = system_from_golden(g, 200)
+    orc = O.Oracle(s)
+    o = orc.run_md(12, use_nhc=(mode == "nhc"))
+    np.testing.assert_array_equal(o["en"].ravel(), g[mode + "_en_steps"])
+    np.testing.assert_array_equal(o["pos"].ravel(), g[mode + "_pos"])
+    np.testing.assert_array_equal(o["pos_nopbc"].ravel(), g[mode + "_pos_nopbc"])
+    np.testing.assert_array_equal(o["vel"].ravel(), g[mode + "_vel"])
+    np.testing.assert_array_equal(o["force"].ravel(), g[mode + "_force"])
+    if mode == "nhc":
+        np.testing.assert_array_equal(o["zeta"].ravel(), g["nhc_zeta"])
+
+
+def test_oracle_4095_box(golden4095):
+    g = golden4095
+    s = system_from_golden(g, 1365)
+    orc = O.Oracle(s)
+    cnt, idx, flg = orc.nblist(s.pos)
+    np.testing.assert_array_equal(cnt, g["nl_cnt"])
+    assert _pair_hash(cnt, idx) == str(g["nl_hash"])
+    np.testing.assert_array_equal([(flg == f).sum() for f in range(5)], g["nl_nflag"])
+    ff, en = orc.forces(s.pos, (cnt, idx, flg))
+    np.testing.assert_array_equal(ff.ravel(), g["forces_f_total"])
+    ref_en = dict(zip(O.EN_KEYS, g["forces_en"]))
+    for k, v in en.items():
+        assert v == ref_en[k], k
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/defines.h"),
+                    reason="reference sources not present")
+def test_oracle_against_live_reference(tmp_path):
+    from thecodecombo_7_gb300 import systems
+    assert O.build_reference()
+    s = systems.water_box(150, L=24.5, seed=99, grid=(20, 24, 30))
+    s.nlist_freq = 3
+    ref = O.run_reference("forces", s, str(tmp_path))
+    orc = O.Oracle(s)
+    ff, en = orc.forces(s.pos)
+    np.testing.assert_array_equal(ff.ravel(), ref["f_total"])
+    traj = O.run_reference("nhc", s, str(tmp_path), nsteps=7)
+    o = orc.run_md(7, use_nhc=True)
+    np.testing.assert_array_equal(o["en"].ravel(), traj["en_steps"])
+    np.testing.assert_array_equal(o["vel"].ravel(), traj["vel"])
+
+
+@pytest.mark.parametrize("shape", [(8, 9, 10), (24, 25, 27), (7, 1, 13)])
+def test_oracle_fft_matches_dft(shape):
+    import ctypes as C
+    lib = C.CDLL(O.build())
+    rng = np.random.default_rng(3)
+    x = rng.normal(size=shape) + 1j * rng.normal(size=shape)
+    for sign in (-1, 1):
+        buf = np.ascontiguousarray(np.stack([x.real, x.imag], -1))
+        lib.fe_fft3d(buf.ctypes.data_as(C.c_void_p), *shape, sign)
+        got = buf[..., 0] + 1j * buf[..., 1]
+        want = np.fft.fftn(x) if sign == -1 else np.fft.ifftn(x) * x.size
+        np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-11 * np.abs(want).max())

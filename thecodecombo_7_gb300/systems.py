@@ -1,0 +1,227 @@
+"""Synthetic systems in the reference's vocabulary (boxes of sites).
+
+The reference reads its systems from INPUT/ files (read_config.c,
+read_topology.c); the workloads here are generated instead, seeded, with the
+shapes the engine is measured on:
+
+* ``water_box`` -- rigid-geometry 3-site bent molecules (O, H, H) with charges
+  -0.8/+0.4/+0.4 e, O-H 1.0 A (k = 450 kcal/mol/A^2), H-O-H 104.5 deg
+  (k = 55 kcal/mol/rad^2), LJ on O only (eps = 0.15 kcal/mol, sigma = 3.15 A,
+  stored the reference's way as CHARMM eps < 0 and R_min/2), masses 16/1/1
+  amu; 1-2 pairs (xflag 1) and the 1-3 pair (xflag 2) excluded.  Molecule
+  centres are placed uniformly at random in a periodic cube at the requested
+  site density, rejecting any O-O distance below 2.6 A, with uniformly random
+  orientations, and Maxwell-Boltzmann velocities (net momentum removed).
+
+Units are the reference's internal ones (A, ps, amu, e, kJ/mol;
+defines.h:62-75, integrate_vverlet.c:56).
+"""
+from __future__ import annotations
+
+import dataclasses
+import math
+
+import numpy as np
+
+KB = 1.380662e-23  # defines.h:63
+AU = 1.6605655e-27  # defines.h:66
+KCAL = 4.184  # read_topology.c:212 (kcal -> kJ)
+
+
+@dataclasses.dataclass
+class System:
+    """One box: sites, topology and the run parameters of the hot path."""
+
+    L: np.ndarray  # (3,) box lengths
+    pos: np.ndarray  # (n, 3) float64, wrapped into [-L/2, L/2]
+    q: np.ndarray  # (n,)
+    mass: np.ndarray  # (n,)
+    type: np.ndarray  # (n,) int32 site type (atom[k][i].atomid)
+    vel: np.ndarray  # (n, 3) A/ps
+    type_eps_kcal: np.ndarray  # (ntypes,) CHARMM eps (<= 0)
+    type_rmin_half: np.ndarray  # (ntypes,) R_min/2
+    bonds: np.ndarray  # (nb, 2) int32
+    bond_req: np.ndarray
+    bond_k: np.ndarray  # kJ/mol/A^2, E = k (r - r0)^2
+    bends: np.ndarray  # (na, 3) int32 (a, b=apex, c)
+    bend_theta0: np.ndarray  # rad
+    bend_k: np.ndarray  # kJ/mol/rad^2, E = k (theta - theta0)^2
+    excl: np.ndarray  # (nx, 2) int32
+    excl_flag: np.ndarray  # (nx,) int32, 1 bond / 2 bend / 3 exNB / 4 1-4
+    rc: float = 10.0
+    rclist: float = 12.0
+    rclist_ew: float = 12.0
+    rc_ew: float = 10.0
+    kappa: float = 0.32
+    epsRF: float = 1.0
+    dt: float = 0.0005  # ps
+    T: float = 300.0
+    grid: tuple = (32, 32, 32)
+    order: int = 4
+    nlist_freq: int = 10
+    r_switch: float = 0.0  # 0 = no switch (the reference); 8.0 = CHARMM switch 8->rc
+    nhc_M: int = 3
+    nhc_Q: float = 1.0e-18
+    seed: int = 0
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    @property
+    def ntypes(self) -> int:
+        return int(self.type_eps_kcal.shape[0])
+
+    def lj_tables(self):
+        """Mixed (eps [kJ/mol], R_min [A]) per type pair, setlj.c:181-191."""
+        e = self.type_eps_kcal
+        s = self.type_rmin_half
+        eps = KCAL * np.sqrt(np.outer(e, e))
+        sig = 0.5 * (2.0 * s[:, None] + 2.0 * s[None, :])
+        return np.ascontiguousarray(eps), np.ascontiguousarray(sig)
+
+    def copy(self) -> "System":
+        return dataclasses.replace(
+            self, pos=self.pos.copy(), vel=self.vel.copy(), L=self.L.copy())
+
+
+def fft_friendly(n: int) -> int:
+    """Smallest m >= n whose prime factors are 2, 3 and 5."""
+    m = max(int(n), 1)
+    while True:
+        k = m
+        for p in (2, 3, 5):
+            while k % p == 0:
+                k //= p
+        if k == 1:
+            return m
+        m += 1
+
+
+def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
+    """Uniform random rotation matrices from unit quaternions."""
+    qv = rng.normal(size=(n, 4))
+    qv /= np.linalg.norm(qv, axis=1, keepdims=True)
+    w, x, y, z = qv.T
+    R = np.empty((n, 3, 3))
+    R[:, 0, 0] = 1 - 2 * (y * y + z * z)
+    R[:, 0, 1] = 2 * (x * y - z * w)
+    R[:, 0, 2] = 2 * (x * z + y * w)
+    R[:, 1, 0] = 2 * (x * y + z * w)
+    R[:, 1, 1] = 1 - 2 * (x * x + z * z)
+    R[:, 1, 2] = 2 * (y * z - x * w)
+    R[:, 2, 0] = 2 * (x * z - y * w)
+    R[:, 2, 1] = 2 * (y * z + x * w)
+    R[:, 2, 2] = 1 - 2 * (x * x + y * y)
+    return R
+
+
+def _place_centres(rng: np.random.Generator, n_mol: int, L: float,
+                   dmin: float, max_tries: int = 400) -> np.ndarray:
+    """Random sequential placement in a periodic cube with an O-O minimum.
+
+    A cell grid (cell >= dmin) keeps each trial O(1).  Candidates are drawn
+    in batches so the Python overhead stays per accepted molecule.
+    """
+    m = max(1, int(L // dmin))
+    cell = L / m
+    heads: dict = {}
+    out = np.empty((n_mol, 3))
+    d2 = dmin * dmin
+    count = 0
+    tries = 0
+    while count < n_mol:
+        cand = rng.uniform(-L / 2, L / 2, size=(4096, 3))
+        for c in cand:
+            tries += 1
+            ci = ((c + L / 2) / cell).astype(int) % m
+            ok = True
+            for ox in (-1, 0, 1):
+                for oy in (-1, 0, 1):
+                    for oz in (-1, 0, 1):
+                        key = ((ci[0] + ox) % m, (ci[1] + oy) % m, (ci[2] + oz) % m)
+                        lst = heads.get(key)
+                        if not lst:
+                            continue
+                        d = out[lst] - c
+                        d -= L * np.rint(d / L)
+                        if np.any(np.einsum("ij,ij->i", d, d) < d2):
+                            ok = False
+                            break
+                    if not ok:
+                        break
+                if not ok:
+                    break
+            if ok:
+                out[count] = c
+                heads.setdefault((ci[0], ci[1], ci[2]), []).append(count)
+                count += 1
+                if count == n_mol:
+                    break
+        if tries > max_tries * n_mol:
+            raise RuntimeError(
+                f"could not place {n_mol} molecules at L={L:.3f} with O-O >= {dmin}")
+    return out
+
+
+def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
+              grid=None, T: float = 300.0, L: float | None = None,
+              dmin: float = 2.6, **params) -> System:
+    """The 3-site bent-molecule box of the configured workloads.
+
+    ``density`` is sites per A^3 (0.1 gives L = 34.47 A at 1,365 molecules and
+    L = 98.65 A at 32,000).  ``grid`` defaults to about 1 point/A rounded up
+    to an FFT-friendly size (32^3 and 96^3 for the two sizes above).
+    """
+    rng = np.random.default_rng(seed)
+    n = 3 * n_mol
+    if L is None:
+        L = (n / density) ** (1.0 / 3.0)
+    if grid is None:
+        g = fft_friendly(int(math.ceil(L - 1e-9)))
+        grid = (g, g, g)
+    centres = _place_centres(rng, n_mol, L, dmin)
+    R = _random_rotations(rng, n_mol)
+    half = math.radians(104.5) / 2.0
+    body = np.array([[0.0, 0.0, 0.0],
+                     [math.sin(half), math.cos(half), 0.0],
+                     [-math.sin(half), math.cos(half), 0.0]])  # O-H = 1.0 A
+    pos = centres[:, None, :] + np.einsum("mij,kj->mki", R, body)
+    pos = pos.reshape(n, 3)
+    pos -= L * np.floor(pos / L + 0.5)  # wrap into [-L/2, L/2)
+    q = np.tile([-0.8, 0.4, 0.4], n_mol)
+    mass = np.tile([16.0, 1.0, 1.0], n_mol)
+    typ = np.tile(np.array([0, 1, 1], dtype=np.int32), n_mol)
+    # Maxwell-Boltzmann at T: sigma = sqrt(kT/m) m/s = 0.01 * that A/ps
+    sd = np.sqrt(KB * T / (mass * AU)) * 1.0e-2
+    vel = rng.normal(size=(n, 3)) * sd[:, None]
+    p = (vel * mass[:, None]).sum(0) / mass.sum()
+    vel -= p
+    base = 3 * np.arange(n_mol, dtype=np.int32)
+    bonds = np.stack([np.stack([base, base + 1], 1),
+                      np.stack([base, base + 2], 1)], 1).reshape(-1, 2)
+    bends = np.stack([base + 1, base, base + 2], 1)
+    excl = np.concatenate([np.stack([base, base + 1], 1),
+                           np.stack([base, base + 2], 1),
+                           np.stack([base + 1, base + 2], 1)], 0)
+    excl_flag = np.concatenate([np.ones(n_mol, np.int32), np.ones(n_mol, np.int32),
+                                2 * np.ones(n_mol, np.int32)])
+    rmin_half = 2.0 ** (1.0 / 6.0) * 3.15 / 2.0
+    sysm = System(
+        L=np.array([L, L, L], dtype=np.float64),
+        pos=np.ascontiguousarray(pos, dtype=np.float64),
+        q=q.astype(np.float64), mass=mass, type=typ,
+        vel=np.ascontiguousarray(vel),
+        type_eps_kcal=np.array([-0.15, 0.0]),
+        type_rmin_half=np.array([rmin_half, 0.0]),
+        bonds=bonds.astype(np.int32),
+        bond_req=np.full(bonds.shape[0], 1.0),
+        bond_k=np.full(bonds.shape[0], 450.0 * KCAL),
+        bends=bends.astype(np.int32),
+        bend_theta0=np.full(n_mol, math.radians(104.5)),
+        bend_k=np.full(n_mol, 55.0 * KCAL),
+        excl=excl.astype(np.int32), excl_flag=excl_flag,
+        T=T, grid=tuple(int(x) for x in grid), seed=seed)
+    for k, v in params.items():
+        setattr(sysm, k, v)
+    return sysm
