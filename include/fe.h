@@ -1,0 +1,206 @@
+/*
+ * fe.h -- C ABI of the GB300 force engine (libfe.so).
+ *
+ * One fe_box holds one simulation box of the reference (its `ibox`) resident
+ * in GPU memory: positions, velocities, forces, the Verlet list, the SPME
+ * grids and plans.  Every entry point below replaces one routine of the
+ * reference's hot path (file:line of the routine it replaces is on each);
+ * arguments are plain pointers and sizes, arrays on the host side use the
+ * reference's own layouts:
+ *   - `struct atoms` records (defines.h:307-317): x, y, z doubles at a byte
+ *     offset inside a record of `stride` bytes (64 / 16 with gcc LP64);
+ *   - `struct veloc` records (defines.h:508-512): 3 doubles, stride 24, which
+ *     is also a plain interleaved xyz array;
+ *   - energies as the reference's en[k] fields (FE_EN_* indices).
+ * Units are the reference's (A, ps, amu, e, kJ/mol).
+ *
+ * Errors: every call returns FE_OK (0) or an FE_ERR_* code; fe_last_error()
+ * gives the message.  Nothing falls back to the CPU: without a usable CUDA
+ * device fe_box_create fails with FE_ERR_CUDA.
+ *
+ * Threading: a box is used by one host thread at a time (the reference is
+ * single-threaded and loops boxes sequentially).  Work is issued on the box's
+ * stream (fe_box_set_stream); calls that return host data synchronise it.
+ */
+#ifndef FE_H
+#define FE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FE_ABI_VERSION 1
+
+enum {
+  FE_OK = 0,
+  FE_ERR_CUDA = 1,     /* CUDA / cuFFT failure or no device */
+  FE_ERR_ARG = 2,      /* invalid argument */
+  FE_ERR_OVERFLOW = 5, /* neighbour-list row over capacity (nblist.c:185-197 exit 5) */
+  FE_ERR_CHARGE = 20,  /* non-neutral box (ewald.c:185-194 exit 20) */
+  FE_ERR_STATE = 30,   /* call order (e.g. forces before a list exists) */
+  FE_ERR_DEVICE = 31,  /* a kernel reported an error status (bounded loop ran out, bad index) */
+  FE_ERR_SIZE = 32     /* request beyond a fixed maximum */
+};
+
+/* arithmetic of the pair / SPME kernels */
+enum {
+  FE_PREC_FP64 = 0, /* plain FP64: the drop-in (same arithmetic as the reference) */
+  FE_PREC_MIXED = 1 /* FP32 pair/PME math, 64-bit fixed-point force sums, FP64 integration */
+};
+
+/* en[k] fields, in this order, for every energy record */
+enum {
+  FE_EN_KINET = 0, FE_EN_BOND, FE_EN_BEND, FE_EN_NBOND, FE_EN_NBONDS,
+  FE_EN_COULOMB, FE_EN_REWALD, FE_EN_REWALDS, FE_EN_KEWALD, FE_EN_SEWALD,
+  FE_EN_IEWALD, FE_EN_TEWALD, FE_EN_COUNT
+};
+
+typedef struct fe_box fe_box;
+
+/* Box description: what read_sim.c / read_config.c / read_topology.c /
+ * setlj.c leave in sim, box[k], pott[k], ljset, bond[k], bend[k], xint[k]. */
+typedef struct {
+  int n;              /* box[k].boxns */
+  int ntypes;         /* NUM_ATOM (site types) */
+  double L[3];        /* box[k].lx, ly, lz */
+  double rc;          /* sim.rc */
+  double rclist;      /* sim.rclist */
+  double rclist_ew;   /* sim.rclist_ew */
+  double kappa;       /* sim.kappa[k] */
+  double epsRF;       /* sim.epsRF[k] */
+  double dt;          /* sim.dt [ps] */
+  double T;           /* sim.T[k] [K] */
+  int grid[3];        /* sim.grid */
+  int order;          /* sim.order (B-spline order, 3..8) */
+  double r_switch;    /* LJ switch start (CHARMM switch r_switch..rc); 0 = off (reference) */
+  int precision;      /* FE_PREC_* */
+  int max_neighbors;  /* capacity per list row; 0 = the reference's rule (allocate.c:321-322) */
+  int device;         /* CUDA device ordinal */
+  /* sites */
+  const double *q;    /* n  pott[k][i].qq */
+  const double *mass; /* n  pott[k][i].mas */
+  const int *type;    /* n  atom[k][i].atomid */
+  const double *lj_eps; /* ntypes*ntypes, ljset[ta][tb].eps [kJ/mol] */
+  const double *lj_sig; /* ntypes*ntypes, ljset[ta][tb].sig (R_min) [A] */
+  /* bonded terms of forces() (cbond.c, cbend.c) */
+  int nbond;
+  const int *bond_ab;        /* 2*nbond */
+  const double *bond_req;    /* nbond */
+  const double *bond_k;      /* nbond, E = k (r - req)^2 */
+  int nbend;
+  const int *bend_abc;       /* 3*nbend (apex in the middle) */
+  const double *bend_theta0; /* nbend [rad] */
+  const double *bend_k;      /* nbend, E = k (theta - theta0)^2 */
+  /* excluded / modified pairs (xint[k]): flag 1 bond, 2 bend, 3 exNB, 4 1-4 */
+  int nexcl;
+  const int *excl_ab;   /* 2*nexcl */
+  const int *excl_flag; /* nexcl */
+  /* Nose-Hoover chain (nhc[k], read_sim.c:537-561) */
+  int nhc_M;
+  double nhc_Q;
+  double nfree;       /* box[k].nfree; <= 0 means 3n - 3 (read_config.c:340-342) */
+} fe_box_params;
+
+/* ---- lifetime ---------------------------------------------------------- */
+
+/* Allocates the box on the device (the reference's allocate.c:312-505 and
+ * ewald_setup(), ewald.c:46-197: SPME setup, B-spline moduli, self energy,
+ * neutrality check).  Returns FE_ERR_CHARGE for a non-neutral box. */
+int fe_box_create(fe_box **out, const fe_box_params *p);
+/* Frees everything (pme_clean, pme_setup.c:249-257, and mem_free.c). */
+void fe_box_destroy(fe_box *box);
+/* Issue all work of this box on `stream` (a cudaStream_t); NULL = the box's own. */
+int fe_box_set_stream(fe_box *box, void *stream);
+const char *fe_last_error(void);
+int fe_abi_version(void);
+
+/* ---- state transfer (host <-> device) ----------------------------------- */
+
+/* Positions from `struct atoms`-like records: x at `off_x`, y, z following,
+ * `stride` bytes apart (atom[k]: stride 64, off_x 16).  Also sets the
+ * unwrapped copy (atnopbc) when `nopbc` is nonzero. */
+int fe_set_positions(fe_box *box, const void *atoms, size_t stride, size_t off_x, int nopbc);
+int fe_get_positions(fe_box *box, void *atoms, size_t stride, size_t off_x);
+int fe_set_positions_nopbc(fe_box *box, const void *atoms, size_t stride, size_t off_x);
+int fe_get_positions_nopbc(fe_box *box, void *atoms, size_t stride, size_t off_x);
+/* `struct veloc` arrays (vv[k], uu[k], ff[k]): n x 3 doubles */
+int fe_set_velocities(fe_box *box, const double *vv, const double *uu);
+int fe_get_velocities(fe_box *box, double *vv, double *uu);
+int fe_get_forces(fe_box *box, double *ff);
+/* NHC state nhc[k].zeta[j].{r,v,G}: 3*M doubles */
+int fe_set_nhc_state(fe_box *box, const double *zeta);
+int fe_get_nhc_state(fe_box *box, double *zeta);
+
+/* ---- hot path ------------------------------------------------------------ */
+
+/* nblist(ibox), nblist.c:32-592: half Verlet list b > a with the reference's
+ * distance test (components against rclist, dr2 < rclist^2 and
+ * dr2 < rclist_ew^2), built from a cell grid on the device.  Rows keep the
+ * reference's order (ascending b) and carry the xint flag. */
+int fe_nblist(fe_box *box);
+/* Copies the list to the host as CSR (count[n], idx/flag[<= cap]); returns
+ * FE_ERR_SIZE when cap is too small.  *total gets the number of entries. */
+int fe_nblist_download(fe_box *box, int *count, int *idx, int *flag, int64_t cap, int64_t *total);
+
+/* forces(ibox), forces.c:118-446: zero ff, cbond, cbend, cnonbondnl (pair
+ * loop + pme_calc).  `en` (may be NULL) gets FE_EN_COUNT values with
+ * FE_EN_KINET left as the last kinet() result. */
+int fe_forces(fe_box *box, double *en);
+/* cnonbondnl(ibox, energy), cnonbond_nblist.c:51-622: accumulates the pair
+ * and SPME forces into ff; energy[8] as the reference assembles it. */
+int fe_cnonbondnl(fe_box *box, double *energy8);
+/* pme_calc(k, energy), pme_calc.c:18-279 (charge_grid, FFTs, reciprocal
+ * sum, pme_force with mean-force removal): accumulates into ff. */
+int fe_pme_calc(fe_box *box, double *energy3);
+/* charge_grid(k), pme_qgrid.c:13-121: spread charges; fe_get_charge_grid
+ * copies the real grid (grid[0]*grid[1]*grid[2] doubles, x slowest). */
+int fe_charge_grid(fe_box *box);
+int fe_get_charge_grid(fe_box *box, double *grid);
+/* cbond + cbend energies into en2 (forces accumulated into ff). */
+int fe_bonded(fe_box *box, double *en2);
+/* zero ff (forces.c:126-130) */
+int fe_zero_forces(fe_box *box);
+
+/* pbc_all(ibox), pbc_all.c:23-88 */
+int fe_pbc_all(fe_box *box);
+/* kinet(ibox), kinet.c:18-68: ken[6] tensor and the scalar (may be NULL) */
+int fe_kinet(fe_box *box, double *ken6, double *kinet);
+/* integrate_vverlet(ibox, vscal), integrate_vverlet.c:36-103 (includes
+ * pbc_all and forces); `en` as for fe_forces, may be NULL. */
+int fe_integrate_vverlet(fe_box *box, double vscal, double *en);
+/* integrate_nhc(time_step, ibox), integrate_nhc.c:40-161 (Nc = Nys = 1) */
+int fe_integrate_nhc(fe_box *box, double time_step);
+
+/* The production step loop of nve_md.c:359-418 (use_nhc = 0) or nvt_md.c
+ * with ID2 == 4 (use_nhc = 1): for i = 1..nsteps { if i % nlist_freq == 0
+ * nblist; [nhc]; integrate_vverlet(1.0); [nhc]; kinet }, captured in a CUDA
+ * graph and replayed.  `rec` (may be NULL) gets FE_EN_COUNT doubles per step
+ * (nsteps records). `first_step` is the value of i for the first step. */
+int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_step, double *rec);
+
+/* ---- classic-Ewald Monte Carlo energy path (ewald_mc.c, enbnd_mc.c) --------- */
+
+/* Set up the k-vector table of ewald_setup (ewald.c:95-118) for kmax in
+ * each direction and max_k_square, and the structure factor S(k) of the
+ * current positions.  rc_ew is sim.rc_ew. */
+int fe_mc_setup(fe_box *box, int kmax, int max_k_square, double rc_ew);
+/* Energy change of moving sites [lb, ub) to new_pos (n_moved x 3 doubles):
+ * exact reciprocal part from the incremental structure-factor update plus
+ * real-space Ewald and shifted LJ over all pairs touching the moved sites
+ * (minimum image).  parts3 (may be NULL) = {dE_recip, dE_real, dE_lj}.
+ * Replaces forces_mc(lb,ub,0|1,k) old/new differencing (forces_mc.c:90-573). */
+int fe_mc_delta(fe_box *box, int lb, int ub, const double *new_pos, double *dE, double *parts3);
+/* Commit the last fe_mc_delta move (positions and S(k) update) -- the
+ * accepted branch of mcmove_trans.c:177; a rejected move needs no call
+ * (mcmove_rstr restores nothing on the device). */
+int fe_mc_accept(fe_box *box);
+/* Current k-space energy from the maintained S(k) (ewald_kspace_mc enkewald[0]). */
+int fe_mc_kspace_energy(fe_box *box, double *e);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,91 @@
+"""CPU-side checks of the C ABI and host logic (no GPU needed)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from thecodecombo_7_gb300 import build, engine
+    build.build()
+    return engine.load_library()
+
+
+def _declared(header):
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char \*)\s*\*?\s*(fe_\w+)\s*\(", txt, re.M)))
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from thecodecombo_7_gb300 import engine
+    declared = _declared("fe.h")
+    assert declared, "no declarations parsed"
+    for name in declared:
+        assert hasattr(lib, name), name
+    assert sorted(engine.EXPORTS) == declared
+    out = subprocess.run(["nm", "-D", "--defined-only", engine.LIB_PATH], capture_output=True,
+                         text=True).stdout
+    for name in declared:
+        assert re.search(rf"\bT {name}\b", out), name
+
+
+def test_abi_version(lib):
+    assert lib.fe_abi_version() == 1
+
+
+def test_non_neutral_box_is_rejected_with_code_20(lib):
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(20, L=12.0, seed=1, grid=(8, 8, 8))
+    s.q = s.q.copy()
+    s.q[0] += 0.01
+    with pytest.raises(engine.FeError) as ei:
+        engine.Box(s)
+    assert ei.value.code == engine.FE_ERR_CHARGE
+
+
+def test_bad_arguments_are_rejected(lib):
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(20, L=12.0, seed=1, grid=(8, 8, 8))
+    s.order = 2
+    with pytest.raises(engine.FeError) as ei:
+        engine.Box(s)
+    assert ei.value.code == engine.FE_ERR_ARG
+
+
+def test_no_cpu_fallback_without_device(lib):
+    """With no usable GPU the engine fails loudly instead of computing on the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(20, L=12.0, seed=1, grid=(8, 8, 8))
+    with pytest.raises(engine.FeError) as ei:
+        engine.Box(s)
+    assert ei.value.code == engine.FE_ERR_CUDA
+
+
+def test_water_box_recipe():
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(1365, density=0.1, seed=3)
+    assert s.n == 4095
+    assert abs(s.L[0] - 34.4683) < 1e-3 and s.grid == (32, 32, 32)
+    assert abs(s.q.sum()) < 1e-12
+    o = s.pos[0::3]
+    d = o[:, None, :] - o[None, :, :]
+    d -= s.L * np.rint(d / s.L)
+    r = np.sqrt((d ** 2).sum(-1)) + np.eye(len(o)) * 100
+    assert r.min() >= 2.6
+    oh = s.pos[1::3] - s.pos[0::3]
+    oh -= s.L * np.rint(oh / s.L)
+    np.testing.assert_allclose(np.linalg.norm(oh, axis=1), 1.0, atol=1e-12)
+    assert np.all(np.abs(s.pos) <= s.L / 2)
+    p = (s.vel * s.mass[:, None]).sum(0)
+    np.testing.assert_allclose(p, 0.0, atol=1e-9)
+    assert systems.fft_friendly(97) == 100 and systems.fft_friendly(96) == 96
+    assert systems.fft_friendly_below(99) == 96 and systems.fft_friendly_below(34) == 32

@@ -1,0 +1,656 @@
+// fe_api.cu -- the C ABI of libfe.so (include/fe.h): box lifetime, host <->
+// device transfers in the reference's layouts, and the drivers that chain the
+// kernels in the order of the reference's routines.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "fe_internal.h"
+
+namespace fe {
+
+static thread_local std::string g_err;
+
+void set_error(const std::string &msg) { g_err = msg; }
+
+int cuda_fail(cudaError_t e, const char *what) {
+  set_error(std::string("CUDA error in ") + what + ": " + cudaGetErrorString(e));
+  return FE_ERR_CUDA;
+}
+
+int cufft_fail(cufftResult r, const char *what) {
+  set_error(std::string("cuFFT error ") + std::to_string((int)r) + " in " + what);
+  return FE_ERR_CUDA;
+}
+
+int check_status(Box *b) {
+  int st = 0;
+  FE_CUDA(cudaMemcpyAsync(&st, b->status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  if (st == 0) return FE_OK;
+  FE_CUDA(cudaMemsetAsync(b->status, 0, sizeof(int), b->stream));
+  std::string m = "device status:";
+  if (st & ST_LIST_OVERFLOW)
+    m += " neighbour-list row over capacity (increase max_neighbors or check the density);";
+  if (st & ST_CELL_OVERFLOW) m += " cell bin over capacity;";
+  if (st & ST_PBC_LOOP) m += " periodic wrap did not converge (non-finite or runaway position);";
+  if (st & ST_GRID_OVERFLOW) m += " SPME bin over capacity;";
+  if (st & ST_BAD_INDEX) m += " index out of range skipped;";
+  set_error(m);
+  if (st & ST_LIST_OVERFLOW) return FE_ERR_OVERFLOW;
+  return FE_ERR_DEVICE;
+}
+
+template <class T>
+static int upload(T **dst, const T *src, size_t count) {
+  FE_CUDA(cudaMalloc(dst, sizeof(T) * (count ? count : 1)));
+  if (count) FE_CUDA(cudaMemcpy(*dst, src, sizeof(T) * count, cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+static int sync_scal(Box *b) {
+  FE_CUDA(cudaMemcpyAsync(b->host_scal, b->scal, sizeof(double) * SC_COUNT, cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return check_status(b);
+}
+
+// forces() on the device, forces.c:118-219
+static int forces_device(Box *b) {
+  if (!b->have_list) {
+    set_error("forces requested before a neighbour list was built (call nblist first)");
+    return FE_ERR_STATE;
+  }
+  int rc;
+  if ((rc = launch_zero_forces(b))) return rc;
+  if ((rc = launch_bonded64(b))) return rc;
+  if ((rc = launch_pair64(b))) return rc;
+  if ((rc = launch_pme64(b))) return rc;
+  if ((rc = launch_apply_pme(b))) return rc;
+  return launch_assemble_energies(b, 1);
+}
+
+static void free_box(Box *b) {
+  void *ptrs[] = {b->pos_q, b->pos_nopbc, b->vv, b->uu, b->ff, b->mass, b->type, b->lj_eps,
+                  b->lj_sig, b->x_start, b->x_partner, b->x_flag, b->bond_ab, b->bend_abc,
+                  b->bond_req, b->bond_k, b->bend_t0, b->bend_k, b->cell_count, b->cell_start,
+                  b->cell_fill, b->cell_atoms, b->cell_of, b->nl_count, b->nl_ent, b->eterm,
+                  b->kweight, b->grid, b->grid_k, b->spl_floor, b->spl_m, b->spl_d, b->fp,
+                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->zeta, b->rec,
+                  b->rec_counter};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  mc_free(b);
+  if (b->host_scal) cudaFreeHost(b->host_scal);
+  if (b->plans) {
+    cufftDestroy(b->plan_r2c);
+    cufftDestroy(b->plan_c2r);
+  }
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
+  if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+}
+
+static int create(Box *b, const fe_box_params *p) {
+  b->p = *p;
+  b->n = p->n;
+  b->nt = p->ntypes;
+  b->dev = p->device;
+  b->prec = p->precision;
+  if (p->n < 2 || p->ntypes < 1 || !p->q || !p->mass || !p->type || !p->lj_eps || !p->lj_sig) {
+    set_error("fe_box_create: n >= 2, ntypes >= 1 and q/mass/type/lj tables are required");
+    return FE_ERR_ARG;
+  }
+  if (p->order < 3 || p->order > 8) {
+    set_error("fe_box_create: SPME order must be in 3..8");
+    return FE_ERR_ARG;
+  }
+  for (int d = 0; d < 3; d++)
+    if (p->grid[d] < p->order || p->L[d] <= 0.0) {
+      set_error("fe_box_create: grid must be >= order and box lengths positive");
+      return FE_ERR_ARG;
+    }
+  if (p->rc <= 0.0 || p->rclist < p->rc || p->kappa <= 0.0 || p->epsRF == 0.0) {
+    set_error("fe_box_create: need rc > 0, rclist >= rc, kappa > 0, epsRF != 0");
+    return FE_ERR_ARG;
+  }
+  if (p->precision != FE_PREC_FP64 && p->precision != FE_PREC_MIXED) {
+    set_error("fe_box_create: unknown precision");
+    return FE_ERR_ARG;
+  }
+  for (int i = 0; i < p->n; i++)
+    if (p->type[i] < 0 || p->type[i] >= p->ntypes) {
+      set_error("fe_box_create: site type out of range");
+      return FE_ERR_ARG;
+    }
+  // ewald.c:185-194 neutrality (summed in site order)
+  double charge = 0.0;
+  for (int i = 0; i < p->n; i++) charge += p->q[i];
+  if (fabs(charge) > 0.000005) {
+    char m[160];
+    snprintf(m, sizeof m,
+             "The charge of the system is %f; Ewald summation needs a neutral system", charge);
+    set_error(m);
+    return FE_ERR_CHARGE;
+  }
+  int ndev = 0;
+  cudaError_t e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) {
+    set_error(std::string("no CUDA device available: ") +
+              (e != cudaSuccess ? cudaGetErrorString(e) : "0 devices"));
+    return FE_ERR_CUDA;
+  }
+  FE_CUDA(cudaSetDevice(p->device));
+  FE_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  b->own_stream = true;
+  int n = p->n;
+  std::vector<double4> pq(n);
+  for (int i = 0; i < n; i++) pq[i] = make_double4(0.0, 0.0, 0.0, p->q[i]);
+  int rc;
+  if ((rc = upload(&b->pos_q, pq.data(), n))) return rc;
+  FE_CUDA(cudaMalloc(&b->pos_nopbc, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMalloc(&b->vv, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMalloc(&b->uu, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMalloc(&b->ff, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMemset(b->pos_nopbc, 0, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMemset(b->vv, 0, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMemset(b->uu, 0, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMemset(b->ff, 0, sizeof(double) * 3 * n));
+  if ((rc = upload(&b->mass, p->mass, n))) return rc;
+  if ((rc = upload(&b->type, p->type, n))) return rc;
+  size_t nt2 = (size_t)p->ntypes * p->ntypes;
+  if ((rc = upload(&b->lj_eps, p->lj_eps, nt2))) return rc;
+  if ((rc = upload(&b->lj_sig, p->lj_sig, nt2))) return rc;
+  // exclusions: per site, both directions, xint order kept
+  b->nexcl = p->nexcl;
+  std::vector<int> xs(n + 1, 0), xp(2 * (size_t)p->nexcl + 1), xf(2 * (size_t)p->nexcl + 1);
+  for (int i = 0; i < p->nexcl; i++) {
+    int a = p->excl_ab[2 * i], c = p->excl_ab[2 * i + 1];
+    if (a < 0 || a >= n || c < 0 || c >= n) {
+      set_error("fe_box_create: exclusion index out of range");
+      return FE_ERR_ARG;
+    }
+    xs[a + 1]++;
+    xs[c + 1]++;
+  }
+  for (int i = 0; i < n; i++) xs[i + 1] += xs[i];
+  std::vector<int> fill(n, 0);
+  for (int i = 0; i < p->nexcl; i++) {
+    int a = p->excl_ab[2 * i], c = p->excl_ab[2 * i + 1];
+    int pa = xs[a] + fill[a]++;
+    xp[pa] = c;
+    xf[pa] = p->excl_flag[i];
+    int pc = xs[c] + fill[c]++;
+    xp[pc] = a;
+    xf[pc] = p->excl_flag[i];
+  }
+  if ((rc = upload(&b->x_start, xs.data(), xs.size()))) return rc;
+  if ((rc = upload(&b->x_partner, xp.data(), xp.size()))) return rc;
+  if ((rc = upload(&b->x_flag, xf.data(), xf.size()))) return rc;
+  // bonded
+  b->nbond = p->nbond;
+  b->nbend = p->nbend;
+  for (int i = 0; i < 2 * p->nbond; i++)
+    if (p->bond_ab[i] < 0 || p->bond_ab[i] >= n) {
+      set_error("fe_box_create: bond index out of range");
+      return FE_ERR_ARG;
+    }
+  for (int i = 0; i < 3 * p->nbend; i++)
+    if (p->bend_abc[i] < 0 || p->bend_abc[i] >= n) {
+      set_error("fe_box_create: bend index out of range");
+      return FE_ERR_ARG;
+    }
+  if ((rc = upload(&b->bond_ab, p->bond_ab, 2 * (size_t)p->nbond))) return rc;
+  if ((rc = upload(&b->bond_req, p->bond_req, (size_t)p->nbond))) return rc;
+  if ((rc = upload(&b->bond_k, p->bond_k, (size_t)p->nbond))) return rc;
+  if ((rc = upload(&b->bend_abc, p->bend_abc, 3 * (size_t)p->nbend))) return rc;
+  if ((rc = upload(&b->bend_t0, p->bend_theta0, (size_t)p->nbend))) return rc;
+  if ((rc = upload(&b->bend_k, p->bend_k, (size_t)p->nbend))) return rc;
+  // scalars, status
+  FE_CUDA(cudaMalloc(&b->partials, sizeof(double) * kMaxPartialBlocks * kPartialTerms));
+  FE_CUDA(cudaMalloc(&b->scal, sizeof(double) * SC_COUNT));
+  FE_CUDA(cudaMemset(b->scal, 0, sizeof(double) * SC_COUNT));
+  FE_CUDA(cudaMalloc(&b->status, sizeof(int)));
+  FE_CUDA(cudaMemset(b->status, 0, sizeof(int)));
+  FE_CUDA(cudaMallocHost(&b->host_scal, sizeof(double) * SC_COUNT));
+  FE_CUDA(cudaMalloc(&b->rec_counter, sizeof(int)));
+  // self energy, ewald.c:61,172-178
+  double fconv = (kELEC * kELEQ * kELEQ * kNA * 0.001) / p->epsRF;
+  double vs = 0.0;
+  for (int i = 0; i < n; i++) vs += p->q[i] * p->q[i];
+  vs *= p->kappa / sqrt(kPI);
+  b->sewald = vs * fconv;
+  // NHC state, read_config.c:358-370
+  b->nhc_M = p->nhc_M > 0 ? p->nhc_M : 1;
+  b->nhc_Q = p->nhc_Q != 0.0 ? p->nhc_Q : 1.0e-18;
+  b->nfree = p->nfree > 0.0 ? p->nfree : 3.0 * n - 3.0;
+  std::vector<double> z(3 * b->nhc_M, 0.0);
+  double kT = kKB * p->T * 1E-4;
+  for (int i = 0; i < b->nhc_M - 1; i++)
+    z[3 * (i + 1) + 2] = (b->nhc_Q * z[3 * i + 1] * z[3 * i + 1] - kT) / b->nhc_Q;
+  if ((rc = upload(&b->zeta, z.data(), z.size()))) return rc;
+  if ((rc = nblist_setup(b))) return rc;
+  if ((rc = spme_setup(b))) return rc;
+  FE_CUDA(cudaDeviceSynchronize());
+  return FE_OK;
+}
+
+static int stage_xyz_in(Box *b, const void *atoms, size_t stride, size_t off, std::vector<double> &v) {
+  if (!atoms || stride < 24) {
+    set_error("positions: null pointer or stride < 24");
+    return FE_ERR_ARG;
+  }
+  v.resize(3 * (size_t)b->n);
+  const char *base = (const char *)atoms + off;
+  for (int i = 0; i < b->n; i++) memcpy(&v[3 * (size_t)i], base + (size_t)i * stride, 24);
+  return FE_OK;
+}
+
+static void stage_xyz_out(Box *b, void *atoms, size_t stride, size_t off, const std::vector<double> &v) {
+  char *base = (char *)atoms + off;
+  for (int i = 0; i < b->n; i++) memcpy(base + (size_t)i * stride, &v[3 * (size_t)i], 24);
+}
+
+// one step of the production loop (graph body)
+static int step_body(Box *b, bool with_list, bool use_nhc) {
+  int rc;
+  if (with_list && (rc = launch_nblist(b))) return rc;
+  if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
+  if ((rc = launch_vv1(b, 1.0))) return rc;
+  if ((rc = forces_device(b))) return rc;
+  if ((rc = launch_vv2(b, 1.0))) return rc;
+  if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
+  if ((rc = launch_kinet(b))) return rc;
+  return launch_record(b);
+}
+
+static int capture(Box *b, bool with_list, bool use_nhc, cudaGraphExec_t *out) {
+  cudaGraph_t g;
+  FE_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = step_body(b, with_list, use_nhc);
+  cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+  e = cudaGraphInstantiate(out, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+  return FE_OK;
+}
+
+}  // namespace fe
+
+using namespace fe;
+
+extern "C" {
+
+int fe_abi_version(void) { return FE_ABI_VERSION; }
+
+const char *fe_last_error(void) { return g_err.c_str(); }
+
+int fe_box_create(fe_box **out, const fe_box_params *p) {
+  if (!out || !p) {
+    set_error("fe_box_create: null argument");
+    return FE_ERR_ARG;
+  }
+  *out = nullptr;
+  fe_box *fb = new fe_box();
+  int rc = create(&fb->b, p);
+  if (rc) {
+    free_box(&fb->b);
+    delete fb;
+    return rc;
+  }
+  *out = fb;
+  return FE_OK;
+}
+
+void fe_box_destroy(fe_box *box) {
+  if (!box) return;
+  cudaSetDevice(box->b.dev);
+  cudaStreamSynchronize(box->b.stream);
+  free_box(&box->b);
+  delete box;
+}
+
+int fe_box_set_stream(fe_box *box, void *stream) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  if (b->own_stream) cudaStreamDestroy(b->stream);
+  if (stream) {
+    b->stream = (cudaStream_t)stream;
+    b->own_stream = false;
+  } else {
+    FE_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    b->own_stream = true;
+  }
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
+  b->g_step = b->g_step_list = nullptr;
+  b->g_key = -1;
+  return FE_OK;
+}
+
+int fe_set_positions(fe_box *box, const void *atoms, size_t stride, size_t off_x, int nopbc) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  std::vector<double> v;
+  int rc = stage_xyz_in(b, atoms, stride, off_x, v);
+  if (rc) return rc;
+  std::vector<double4> pq(b->n);
+  for (int i = 0; i < b->n; i++) pq[i] = make_double4(v[3 * i], v[3 * i + 1], v[3 * i + 2], b->p.q[i]);
+  // keep q as uploaded at creation: only x, y, z change here
+  FE_CUDA(cudaMemcpy2DAsync(b->pos_q, sizeof(double4), pq.data(), sizeof(double4), 3 * sizeof(double),
+                            b->n, cudaMemcpyHostToDevice, b->stream));
+  if (nopbc)
+    FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, v.data(), sizeof(double) * 3 * b->n,
+                            cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_get_positions(fe_box *box, void *atoms, size_t stride, size_t off_x) {
+  if (!box || !atoms || stride < 24) return FE_ERR_ARG;
+  Box *b = &box->b;
+  std::vector<double4> pq(b->n);
+  FE_CUDA(cudaMemcpyAsync(pq.data(), b->pos_q, sizeof(double4) * b->n, cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  std::vector<double> v(3 * (size_t)b->n);
+  for (int i = 0; i < b->n; i++) {
+    v[3 * i] = pq[i].x;
+    v[3 * i + 1] = pq[i].y;
+    v[3 * i + 2] = pq[i].z;
+  }
+  stage_xyz_out(b, atoms, stride, off_x, v);
+  return FE_OK;
+}
+
+int fe_set_positions_nopbc(fe_box *box, const void *atoms, size_t stride, size_t off_x) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  std::vector<double> v;
+  int rc = stage_xyz_in(b, atoms, stride, off_x, v);
+  if (rc) return rc;
+  FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, v.data(), sizeof(double) * 3 * b->n, cudaMemcpyHostToDevice,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_get_positions_nopbc(fe_box *box, void *atoms, size_t stride, size_t off_x) {
+  if (!box || !atoms || stride < 24) return FE_ERR_ARG;
+  Box *b = &box->b;
+  std::vector<double> v(3 * (size_t)b->n);
+  FE_CUDA(cudaMemcpyAsync(v.data(), b->pos_nopbc, sizeof(double) * 3 * b->n, cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  stage_xyz_out(b, atoms, stride, off_x, v);
+  return FE_OK;
+}
+
+int fe_set_velocities(fe_box *box, const double *vv, const double *uu) {
+  if (!box || !vv) return FE_ERR_ARG;
+  Box *b = &box->b;
+  size_t bytes = sizeof(double) * 3 * b->n;
+  FE_CUDA(cudaMemcpyAsync(b->vv, vv, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaMemcpyAsync(b->uu, uu ? uu : vv, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_get_velocities(fe_box *box, double *vv, double *uu) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  size_t bytes = sizeof(double) * 3 * b->n;
+  if (vv) FE_CUDA(cudaMemcpyAsync(vv, b->vv, bytes, cudaMemcpyDeviceToHost, b->stream));
+  if (uu) FE_CUDA(cudaMemcpyAsync(uu, b->uu, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_get_forces(fe_box *box, double *ff) {
+  if (!box || !ff) return FE_ERR_ARG;
+  Box *b = &box->b;
+  FE_CUDA(cudaMemcpyAsync(ff, b->ff, sizeof(double) * 3 * b->n, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_set_nhc_state(fe_box *box, const double *zeta) {
+  if (!box || !zeta) return FE_ERR_ARG;
+  Box *b = &box->b;
+  FE_CUDA(cudaMemcpyAsync(b->zeta, zeta, sizeof(double) * 3 * b->nhc_M, cudaMemcpyHostToDevice,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_get_nhc_state(fe_box *box, double *zeta) {
+  if (!box || !zeta) return FE_ERR_ARG;
+  Box *b = &box->b;
+  FE_CUDA(cudaMemcpyAsync(zeta, b->zeta, sizeof(double) * 3 * b->nhc_M, cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_nblist(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  int rc = launch_nblist(&box->b);
+  if (rc) return rc;
+  return check_status(&box->b);
+}
+
+int fe_nblist_download(fe_box *box, int *count, int *idx, int *flag, int64_t cap, int64_t *total) {
+  if (!box || !count) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!b->have_list) {
+    set_error("no neighbour list built yet");
+    return FE_ERR_STATE;
+  }
+  std::vector<int> ent((size_t)b->n * b->max_nb);
+  FE_CUDA(cudaMemcpyAsync(count, b->nl_count, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(ent.data(), b->nl_ent, sizeof(int) * ent.size(), cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  int64_t tot = 0;
+  for (int i = 0; i < b->n; i++) tot += count[i];
+  if (total) *total = tot;
+  if (tot > cap || !idx) {
+    set_error("fe_nblist_download: capacity too small");
+    return idx ? FE_ERR_SIZE : FE_OK;
+  }
+  int64_t p = 0;
+  for (int i = 0; i < b->n; i++)
+    for (int j = 0; j < count[i]; j++) {
+      int e = ent[(size_t)i * b->max_nb + j];
+      idx[p] = e >> 3;
+      if (flag) flag[p] = e & 7;
+      p++;
+    }
+  return FE_OK;
+}
+
+int fe_zero_forces(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  int rc = launch_zero_forces(&box->b);
+  if (rc) return rc;
+  FE_CUDA(cudaStreamSynchronize(box->b.stream));
+  return FE_OK;
+}
+
+int fe_forces(fe_box *box, double *en) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = forces_device(b);
+  if (rc) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (en)
+    for (int i = 0; i < FE_EN_COUNT; i++) en[i] = b->host_scal[i];
+  return FE_OK;
+}
+
+int fe_cnonbondnl(fe_box *box, double *energy8) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!b->have_list) {
+    set_error("cnonbondnl requested before a neighbour list was built");
+    return FE_ERR_STATE;
+  }
+  int rc;
+  if ((rc = launch_pair64(b))) return rc;
+  if ((rc = launch_pme64(b))) return rc;
+  if ((rc = launch_apply_pme(b))) return rc;
+  if ((rc = launch_assemble_energies(b, 0))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (energy8)
+    for (int i = 0; i < 8; i++) energy8[i] = b->host_scal[SC_ENERGY8 + i];
+  return FE_OK;
+}
+
+int fe_pme_calc(fe_box *box, double *energy3) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc;
+  if ((rc = launch_pme64(b))) return rc;
+  if ((rc = launch_apply_pme(b))) return rc;
+  if ((rc = launch_assemble_energies(b, 0))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (energy3)
+    for (int i = 0; i < 3; i++) energy3[i] = b->host_scal[SC_ENERGY3 + i];
+  return FE_OK;
+}
+
+int fe_charge_grid(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  int rc = launch_charge_grid64(&box->b);
+  if (rc) return rc;
+  return check_status(&box->b);
+}
+
+int fe_get_charge_grid(fe_box *box, double *grid) {
+  if (!box || !grid) return FE_ERR_ARG;
+  Box *b = &box->b;
+  FE_CUDA(cudaMemcpyAsync(grid, b->grid, sizeof(double) * b->K, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_bonded(fe_box *box, double *en2) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = launch_bonded64(b);
+  if (rc) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (en2) {
+    en2[0] = b->host_scal[SC_BOND];
+    en2[1] = b->host_scal[SC_BEND];
+  }
+  return FE_OK;
+}
+
+int fe_pbc_all(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  int rc = launch_pbc(&box->b);
+  if (rc) return rc;
+  return check_status(&box->b);
+}
+
+int fe_kinet(fe_box *box, double *ken6, double *kinet) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = launch_kinet(b);
+  if (rc) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (ken6)
+    for (int i = 0; i < 6; i++) ken6[i] = b->host_scal[SC_KEN + i];
+  if (kinet) *kinet = b->host_scal[FE_EN_KINET];
+  return FE_OK;
+}
+
+int fe_integrate_vverlet(fe_box *box, double vscal, double *en) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc;
+  if ((rc = launch_vv1(b, vscal))) return rc;
+  if ((rc = forces_device(b))) return rc;
+  if ((rc = launch_vv2(b, vscal))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (en)
+    for (int i = 0; i < FE_EN_COUNT; i++) en[i] = b->host_scal[i];
+  return FE_OK;
+}
+
+int fe_integrate_nhc(fe_box *box, double time_step) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = launch_nhc(b, time_step);
+  if (rc) return rc;
+  return check_status(b);
+}
+
+int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_step, double *rec) {
+  if (!box || nsteps < 0 || nlist_freq <= 0) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!b->have_list) {
+    set_error("run_md requested before a neighbour list was built");
+    return FE_ERR_STATE;
+  }
+  if (nsteps == 0) return FE_OK;
+  if (b->rec_cap < nsteps) {
+    if (b->rec) cudaFree(b->rec);
+    b->rec = nullptr;
+    FE_CUDA(cudaMalloc(&b->rec, sizeof(double) * FE_EN_COUNT * (size_t)nsteps));
+    b->rec_cap = nsteps;
+    // the record kernel's capacity is baked into the graphs: recapture
+    if (b->g_step) cudaGraphExecDestroy(b->g_step);
+    if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
+    b->g_step = b->g_step_list = nullptr;
+    b->g_key = -1;
+  }
+  FE_CUDA(cudaMemsetAsync(b->rec_counter, 0, sizeof(int), b->stream));
+  int key = use_nhc ? 1 : 0;
+  int rc;
+  if (b->g_key != key) {
+    if (b->g_step) cudaGraphExecDestroy(b->g_step);
+    if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
+    b->g_step = b->g_step_list = nullptr;
+    if ((rc = capture(b, false, use_nhc != 0, &b->g_step))) return rc;
+    if ((rc = capture(b, true, use_nhc != 0, &b->g_step_list))) return rc;
+    b->g_key = key;
+  }
+  for (long i = first_step; i < first_step + nsteps; i++) {
+    cudaGraphExec_t g = (i % nlist_freq == 0) ? b->g_step_list : b->g_step;
+    FE_CUDA(cudaGraphLaunch(g, b->stream));
+  }
+  if (rec)
+    FE_CUDA(cudaMemcpyAsync(rec, b->rec, sizeof(double) * FE_EN_COUNT * (size_t)nsteps,
+                            cudaMemcpyDeviceToHost, b->stream));
+  if ((rc = sync_scal(b))) return rc;
+  return FE_OK;
+}
+
+int fe_mc_setup(fe_box *box, int kmax, int max_k_square, double rc_ew) {
+  if (!box || kmax < 1 || max_k_square < 1 || rc_ew <= 0.0) return FE_ERR_ARG;
+  return mc_setup(&box->b, kmax, max_k_square, rc_ew);
+}
+
+int fe_mc_delta(fe_box *box, int lb, int ub, const double *new_pos, double *dE, double *parts3) {
+  if (!box || !new_pos || lb < 0 || ub <= lb || ub > box->b.n) return FE_ERR_ARG;
+  return mc_delta(&box->b, lb, ub, new_pos, dE, parts3);
+}
+
+int fe_mc_accept(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  return mc_accept(&box->b);
+}
+
+int fe_mc_kspace_energy(fe_box *box, double *e) {
+  if (!box || !e) return FE_ERR_ARG;
+  return mc_kspace_energy(&box->b, e);
+}
+
+}  // extern "C"

@@ -1,0 +1,69 @@
+// fe_device.cuh -- device helpers shared by the FP64 kernels.
+//
+// The FP64 translation units are compiled with -fmad=false so that every
+// multiply and add rounds separately, as the reference's C does; the pair
+// set of the neighbour list then matches the reference bit for bit.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "fe_internal.h"
+
+namespace fe {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Deterministic block sum of up to kPartialTerms values; thread 0 writes
+// partials[blockIdx.x * kPartialTerms + t].  blockDim.x must be a multiple
+// of 32 and at most 1024.
+template <int NT>
+__device__ __forceinline__ void block_partials(double (&v)[NT], double *partials) {
+  __shared__ double sh[32][NT];
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int t = 0; t < NT; t++) {
+    double s = warp_sum(v[t]);
+    if (lane == 0) sh[wid][t] = s;
+  }
+  __syncthreads();
+  if (wid == 0) {
+    int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int t = 0; t < NT; t++) {
+      double s = lane < nw ? sh[lane][t] : 0.0;
+      s = warp_sum(s);
+      if (lane == 0) partials[blockIdx.x * kPartialTerms + t] = s;
+    }
+  }
+}
+
+// The reference's erfc (ewald.c:817-836): the Chebyshev fit "erfcc" of
+// Numerical Recipes (Press et al., 2nd ed., sec. 6.2), fractional error
+// below 1.2e-7, same evaluation order.  The exponential is CUDA's exp.
+__device__ __forceinline__ double ref_erfc(double x) {
+  double z = fabs(x);
+  double t = 1.0 / (1.0 + 0.5 * z);
+  double v = t * exp(-z * z + -1.26551223 +
+                     t * (1.00002368 +
+                     t * (0.37409196 +
+                     t * (0.09678418 +
+                     t * (-0.18628806 +
+                     t * (0.27886807 +
+                     t * (-1.13520398 +
+                     t * (1.48851587 +
+                     t * (-0.82215223 + t * 0.17087277)))))))));
+  if (x < 0) return 2.0 - v;
+  return v;
+}
+
+// qa * qb * QFACTOR in the reference's evaluation order (QFACTOR is an
+// unparenthesised macro, defines.h:71).
+__device__ __forceinline__ double qfactor_mul(double x) {
+  return ((((x * kELEC) * kELEQ) * kELEQ) * kNA) * 1.0E-3;
+}
+
+}  // namespace fe

@@ -1,0 +1,305 @@
+// k_integrate.cu -- FP64 per-site update kernels and the scalar bookkeeping of
+// forces(): deterministic partial-sum reduction, reciprocal-force mean
+// removal (pme_calc.c:268-277), energy assembly (cnonbond_nblist.c:613-620,
+// forces.c:204-219), velocity Verlet (integrate_vverlet.c:36-103) with
+// pbc_all (pbc_all.c:23-88), kinet (kinet.c:18-68) and the Nose-Hoover chain
+// (integrate_nhc.c:40-161).  Compiled with -fmad=false.
+#include "fe_device.cuh"
+
+namespace fe {
+
+// one block; sums partials[b * kPartialTerms + t] over b in a fixed order
+__global__ void k_reduce(const double *__restrict__ partials, int nblocks, int nterms,
+                         double *__restrict__ out, double scale) {
+  __shared__ double sh[256];
+  for (int t = 0; t < nterms; t++) {
+    double s = 0.0;
+    for (int bidx = threadIdx.x; bidx < nblocks; bidx += blockDim.x)
+      s += partials[bidx * kPartialTerms + t];
+    sh[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+      if (threadIdx.x < w) sh[threadIdx.x] += sh[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[t] = sh[0] * scale;
+    __syncthreads();
+  }
+}
+
+int launch_reduce(Box *b, const double *partials, int nblocks, int nterms, int slot, double scale) {
+  k_reduce<<<1, 256, 0, b->stream>>>(partials, nblocks, nterms, b->scal + slot, scale);
+  FE_LAUNCH_CHECK("k_reduce");
+  return FE_OK;
+}
+
+int launch_zero_forces(Box *b) {
+  FE_CUDA(cudaMemsetAsync(b->ff, 0, sizeof(double) * 3 * b->n, b->stream));
+  return FE_OK;
+}
+
+// ff += fp, then ff -= sum(fp)/n (pme_calc.c:198-200 and 268-277)
+__global__ void k_apply_pme(int n, const double *__restrict__ fp, const double *__restrict__ scal,
+                            double *__restrict__ ff) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * n) return;
+  int c = i % 3;
+  double mean = scal[SC_FMEAN + c] / (double)(n);
+  double v = ff[i] + fp[i];
+  ff[i] = v - mean;
+}
+
+int launch_apply_pme(Box *b) {
+  k_apply_pme<<<(3 * b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->fp, b->scal, b->ff);
+  FE_LAUNCH_CHECK("k_apply_pme");
+  return FE_OK;
+}
+
+// energy[8] of cnonbondnl and en[k] of forces()
+__global__ void k_assemble(double *__restrict__ s, double fan, double sewald, int with_bonded) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double ek0 = s[SC_ENREC] * fan;  // pme_calc.c:99-101
+  double ek1 = sewald;
+  double ek2 = ek0 - ek1;
+  s[SC_ENERGY3 + 0] = ek0;
+  s[SC_ENERGY3 + 1] = ek1;
+  s[SC_ENERGY3 + 2] = ek2;
+  double er0 = s[SC_REAL], er1 = s[SC_REAL] - s[SC_REALS], er2 = s[SC_INTRA];
+  double e[8];
+  e[0] = s[SC_LJ] + er0 - er2 + ek2;  // cnonbond_nblist.c:613-620
+  e[1] = e[0] - s[SC_LJS];
+  e[2] = er0 + ek2 - er2;
+  e[3] = er0 - er1;
+  e[4] = ek0;
+  e[5] = ek1;
+  e[6] = er2;
+  e[7] = er0;
+  for (int k = 0; k < 8; k++) s[SC_ENERGY8 + k] = e[k];
+  if (with_bonded) {
+    s[FE_EN_BOND] = s[SC_BOND];  // forces.c:172-219
+    s[FE_EN_BEND] = s[SC_BEND];
+    s[FE_EN_NBOND] = e[0];
+    s[FE_EN_NBONDS] = e[1];
+    s[FE_EN_COULOMB] = e[2];
+    s[FE_EN_TEWALD] = e[2];
+    s[FE_EN_REWALD] = e[7];
+    s[FE_EN_REWALDS] = e[3];
+    s[FE_EN_KEWALD] = e[4];
+    s[FE_EN_SEWALD] = e[5];
+    s[FE_EN_IEWALD] = e[6];
+  }
+}
+
+int launch_assemble_energies(Box *b, int with_bonded) {
+  double fan = 0.5 * kELEC * kELEQ * kELEQ * kNA * 1.0E-3 / b->p.epsRF;
+  k_assemble<<<1, 32, 0, b->stream>>>(b->scal, fan, b->sewald, with_bonded);
+  FE_LAUNCH_CHECK("k_assemble");
+  return FE_OK;
+}
+
+// pbc_all for one coordinate, bounded (the reference loops until inside)
+__device__ __forceinline__ double pbc_wrap(double d, double h, double l, int *bad) {
+  double pbc = 0.0;
+  int it = 0;
+  while (d < -h || d > h) {
+    if (d < -h) pbc = +l;
+    if (d > h) pbc = -l;
+    d += pbc;
+    if (++it > 64) {
+      *bad = 1;
+      break;
+    }
+  }
+  return d;
+}
+
+// integrate_vverlet.c:54-83: half kick, drift (atom and atnopbc), pbc_all
+__global__ void k_vv1(int n, double vscal, double dt, double dt_h, double3 L,
+                      const double *__restrict__ mass, const double *__restrict__ ff,
+                      double *__restrict__ vv, double4 *__restrict__ pos,
+                      double *__restrict__ nopbc, int *__restrict__ status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double imass = 100.0 / mass[i];
+  double v0 = vscal * (vv[3 * i] + dt_h * imass * ff[3 * i]);
+  double v1 = vscal * (vv[3 * i + 1] + dt_h * imass * ff[3 * i + 1]);
+  double v2 = vscal * (vv[3 * i + 2] + dt_h * imass * ff[3 * i + 2]);
+  vv[3 * i] = v0;
+  vv[3 * i + 1] = v1;
+  vv[3 * i + 2] = v2;
+  double ddx = dt * v0, ddy = dt * v1, ddz = dt * v2;
+  nopbc[3 * i] += ddx;
+  nopbc[3 * i + 1] += ddy;
+  nopbc[3 * i + 2] += ddz;
+  double4 p = pos[i];
+  p.x += ddx;
+  p.y += ddy;
+  p.z += ddz;
+  int bad = 0;
+  p.x = pbc_wrap(p.x, L.x / 2.0, L.x, &bad);
+  p.y = pbc_wrap(p.y, L.y / 2.0, L.y, &bad);
+  p.z = pbc_wrap(p.z, L.z / 2.0, L.z, &bad);
+  if (bad) atomicOr(status, ST_PBC_LOOP);
+  pos[i] = p;
+}
+
+int launch_vv1(Box *b, double vscal) {
+  double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
+  double dt = b->p.dt, dt_h = 0.5 * b->p.dt;
+  k_vv1<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal, dt, dt_h, L, b->mass, b->ff, b->vv,
+                                                   b->pos_q, b->pos_nopbc, b->status);
+  FE_LAUNCH_CHECK("k_vv1");
+  return FE_OK;
+}
+
+__global__ void k_pbc(int n, double3 L, double4 *__restrict__ pos, int *__restrict__ status) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4 p = pos[i];
+  int bad = 0;
+  p.x = pbc_wrap(p.x, L.x / 2.0, L.x, &bad);
+  p.y = pbc_wrap(p.y, L.y / 2.0, L.y, &bad);
+  p.z = pbc_wrap(p.z, L.z / 2.0, L.z, &bad);
+  if (bad) atomicOr(status, ST_PBC_LOOP);
+  pos[i] = p;
+}
+
+int launch_pbc(Box *b) {
+  double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
+  k_pbc<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, L, b->pos_q, b->status);
+  FE_LAUNCH_CHECK("k_pbc");
+  return FE_OK;
+}
+
+// integrate_vverlet.c:93-102: second half kick and uu = vv
+__global__ void k_vv2(int n, double vscal, double dt_h, const double *__restrict__ mass,
+                      const double *__restrict__ ff, double *__restrict__ vv,
+                      double *__restrict__ uu) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double imass = 100.0 / mass[i];
+  for (int c = 0; c < 3; c++) {
+    double v = (vv[3 * i + c] + vscal * dt_h * imass * ff[3 * i + c]);
+    vv[3 * i + c] = v;
+    uu[3 * i + c] = v;
+  }
+}
+
+int launch_vv2(Box *b, double vscal) {
+  double dt_h = 0.5 * b->p.dt;
+  k_vv2<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal, dt_h, b->mass, b->ff, b->vv, b->uu);
+  FE_LAUNCH_CHECK("k_vv2");
+  return FE_OK;
+}
+
+// kinet.c:31-43 partial sums of the kinetic tensor
+__global__ void k_kinet(int n, const double *__restrict__ mass, const double *__restrict__ vv,
+                        const double *__restrict__ uu, double *__restrict__ partials) {
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double fac = mass[i];
+    double sx = vv[3 * i] + uu[3 * i];
+    double sy = vv[3 * i + 1] + uu[3 * i + 1];
+    double sz = vv[3 * i + 2] + uu[3 * i + 2];
+    k[0] += fac * sx * sx;
+    k[1] += fac * sy * sx;
+    k[2] += fac * sy * sy;
+    k[3] += fac * sz * sx;
+    k[4] += fac * sz * sy;
+    k[5] += fac * sz * sz;
+  }
+  block_partials<6>(k, partials);
+}
+
+// kinet.c:50-65 unit conversion and the scalar
+__global__ void k_kinet_final(double *__restrict__ s) {
+  if (threadIdx.x != 0) return;
+  double f = (0.125) * (kNA * kAU * 10.0);
+  for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
+  s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
+}
+
+int launch_kinet(Box *b) {
+  int blocks = (b->n + 255) / 256;
+  if (blocks > 512) blocks = 512;
+  k_kinet<<<blocks, 256, 0, b->stream>>>(b->n, b->mass, b->vv, b->uu, b->partials);
+  FE_LAUNCH_CHECK("k_kinet");
+  int rc = launch_reduce(b, b->partials, blocks, 6, SC_KEN, 1.0);
+  if (rc) return rc;
+  k_kinet_final<<<1, 32, 0, b->stream>>>(b->scal);
+  FE_LAUNCH_CHECK("k_kinet_final");
+  return FE_OK;
+}
+
+// integrate_nhc.c:57-147 (Nc = Nys = 1, w[0] = 1): the chain, one thread
+__global__ void k_nhc_chain(int M, double Q, double nfree, double T, double time_step,
+                            double *__restrict__ zeta, double *__restrict__ s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+#define ZR(j) zeta[3 * (j)]
+#define ZV(j) zeta[3 * (j) + 1]
+#define ZG(j) zeta[3 * (j) + 2]
+  int M1 = M - 1, M2 = M - 2;
+  double NkT = nfree * kKB * T * 1E-4;
+  double kT = kKB * T * 1E-4;
+  double akin = 2.0 * s[FE_EN_KINET] * 1000.0 * 1E-4 / kNA;
+  double scale = 1.0;
+  double dt = time_step * 1.0 / (double)1;
+  double dt2 = dt / 2.0, dt4 = dt / 4.0, dt8 = dt / 8.0;
+  double AA;
+  ZG(0) = (akin - NkT) / Q;
+  ZV(M1) += ZG(M1) * dt4;
+  for (int j = 0; j < M1; j++) {
+    AA = exp(-dt8 * ZV(M1 - j));
+    ZV(M2 - j) = ZV(M2 - j) * AA * AA + dt4 * ZG(M2 - j) * AA;
+  }
+  AA = exp(-dt2 * ZV(0));
+  scale = scale * AA;
+  for (int j = 0; j < M; j++) ZR(j) += ZV(j) * dt2;
+  ZG(0) = (scale * scale * akin - NkT) / Q;
+  for (int j = 0; j < M - 1; j++) {
+    AA = exp(-dt8 * ZV(j + 1));
+    ZV(j) = ZV(j) * AA * AA + dt4 * ZG(j) * AA;
+    ZG(j + 1) = (Q * ZV(j) * ZV(j) - kT) / Q;
+  }
+  ZV(M - 1) += ZG(M - 1) * dt4;
+  s[SC_NHC_SCALE] = scale;
+#undef ZR
+#undef ZV
+#undef ZG
+}
+
+// integrate_nhc.c:152-159
+__global__ void k_nhc_scale(int n3, const double *__restrict__ s, double *__restrict__ vv,
+                            double *__restrict__ uu) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n3) return;
+  double scale = s[SC_NHC_SCALE];
+  vv[i] = vv[i] * scale;
+  uu[i] = uu[i] * scale;
+}
+
+int launch_nhc(Box *b, double time_step) {
+  int rc = launch_kinet(b);  // integrate_nhc.c:68
+  if (rc) return rc;
+  k_nhc_chain<<<1, 32, 0, b->stream>>>(b->nhc_M, b->nhc_Q, b->nfree, b->p.T, time_step, b->zeta,
+                                       b->scal);
+  k_nhc_scale<<<(3 * b->n + 255) / 256, 256, 0, b->stream>>>(3 * b->n, b->scal, b->vv, b->uu);
+  FE_LAUNCH_CHECK("k_nhc_scale");
+  return FE_OK;
+}
+
+__global__ void k_record(const double *__restrict__ s, double *__restrict__ rec, long cap,
+                         int *__restrict__ counter) {
+  int c = *counter;
+  if (threadIdx.x < FE_EN_COUNT && c < cap) rec[(long)c * FE_EN_COUNT + threadIdx.x] = s[threadIdx.x];
+  __syncthreads();
+  if (threadIdx.x == 0) *counter = c + 1;
+}
+
+int launch_record(Box *b) {
+  k_record<<<1, 32, 0, b->stream>>>(b->scal, b->rec, b->rec_cap, b->rec_counter);
+  FE_LAUNCH_CHECK("k_record");
+  return FE_OK;
+}
+
+}  // namespace fe

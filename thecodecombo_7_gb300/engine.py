@@ -1,0 +1,317 @@
+"""Host-side mirror of the reference's hot-path interface over libfe.so.
+
+``Box`` wraps one fe_box (the reference's ``ibox``) and exposes the
+reference's routine names -- nblist, forces, cnonbondnl, charge_grid,
+pme_calc, pbc_all, kinet, integrate_vverlet, integrate_nhc -- plus the
+production step loop (run_md) and the classic-Ewald MC energy path.  Every
+call goes through the C ABI of include/fe.h; there is no CPU fallback: without
+the compiled library or a CUDA device the constructor raises.
+
+Errors: the reference prints and exit()s (nblist.c:185-197 exit 5,
+ewald.c:185-194 exit 20); here the same conditions raise ``FeError`` carrying
+the same code.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libfe.so")
+
+FE_OK = 0
+FE_ERR_CUDA = 1
+FE_ERR_ARG = 2
+FE_ERR_OVERFLOW = 5
+FE_ERR_CHARGE = 20
+FE_ERR_STATE = 30
+FE_ERR_DEVICE = 31
+FE_ERR_SIZE = 32
+FE_PREC_FP64 = 0
+FE_PREC_MIXED = 1
+EN_KEYS = ["kinet", "bond", "bend", "nbond", "nbonds", "coulomb", "rewald", "rewalds",
+           "kewald", "sewald", "iewald", "tewald"]
+FE_EN_COUNT = len(EN_KEYS)
+
+# symbols of include/fe.h (checked by the tests against the built library)
+EXPORTS = [
+    "fe_box_create", "fe_box_destroy", "fe_box_set_stream", "fe_last_error", "fe_abi_version",
+    "fe_set_positions", "fe_get_positions", "fe_set_positions_nopbc", "fe_get_positions_nopbc",
+    "fe_set_velocities", "fe_get_velocities", "fe_get_forces", "fe_set_nhc_state",
+    "fe_get_nhc_state", "fe_nblist", "fe_nblist_download", "fe_forces", "fe_cnonbondnl",
+    "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
+    "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
+    "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
+]
+
+
+class FeError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"[fe error {code}] {msg}")
+        self.code = code
+
+
+class FeBoxParams(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("ntypes", C.c_int), ("L", C.c_double * 3), ("rc", C.c_double),
+        ("rclist", C.c_double), ("rclist_ew", C.c_double), ("kappa", C.c_double),
+        ("epsRF", C.c_double), ("dt", C.c_double), ("T", C.c_double), ("grid", C.c_int * 3),
+        ("order", C.c_int), ("r_switch", C.c_double), ("precision", C.c_int),
+        ("max_neighbors", C.c_int), ("device", C.c_int),
+        ("q", C.c_void_p), ("mass", C.c_void_p), ("type", C.c_void_p),
+        ("lj_eps", C.c_void_p), ("lj_sig", C.c_void_p),
+        ("nbond", C.c_int), ("bond_ab", C.c_void_p), ("bond_req", C.c_void_p),
+        ("bond_k", C.c_void_p),
+        ("nbend", C.c_int), ("bend_abc", C.c_void_p), ("bend_theta0", C.c_void_p),
+        ("bend_k", C.c_void_p),
+        ("nexcl", C.c_int), ("excl_ab", C.c_void_p), ("excl_flag", C.c_void_p),
+        ("nhc_M", C.c_int), ("nhc_Q", C.c_double), ("nfree", C.c_double),
+    ]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH) -> C.CDLL:
+    """Load libfe.so; raises if it has not been built (no CPU fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FeError(FE_ERR_CUDA, f"{path} not built: run __graft_entry__.build() "
+                      "or python -m thecodecombo_7_gb300.build")
+    lib = C.CDLL(path)
+    lib.fe_last_error.restype = C.c_char_p
+    lib.fe_box_create.argtypes = [C.POINTER(C.c_void_p), C.POINTER(FeBoxParams)]
+    lib.fe_box_destroy.argtypes = [C.c_void_p]
+    lib.fe_box_destroy.restype = None
+    for name in EXPORTS:
+        fn = getattr(lib, name)
+        if name not in ("fe_last_error", "fe_box_destroy", "fe_box_create"):
+            fn.restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p)
+
+
+def _c(a, dt):
+    return np.ascontiguousarray(a, dtype=dt)
+
+
+class Box:
+    """One simulation box resident on the GPU (the reference's ``ibox``)."""
+
+    def __init__(self, sysm, precision: int = FE_PREC_FP64, device: int = 0,
+                 max_neighbors: int = 0):
+        self.lib = load_library()
+        self.sysm = sysm
+        eps, sig = sysm.lj_tables()
+        k = dict(q=_c(sysm.q, np.float64), mass=_c(sysm.mass, np.float64),
+                 type=_c(sysm.type, np.int32), eps=_c(eps, np.float64), sig=_c(sig, np.float64),
+                 bond_ab=_c(sysm.bonds, np.int32), bond_req=_c(sysm.bond_req, np.float64),
+                 bond_k=_c(sysm.bond_k, np.float64), bend_abc=_c(sysm.bends, np.int32),
+                 bend_t0=_c(sysm.bend_theta0, np.float64), bend_k=_c(sysm.bend_k, np.float64),
+                 excl_ab=_c(sysm.excl, np.int32), excl_flag=_c(sysm.excl_flag, np.int32))
+        self._keep = k
+        p = FeBoxParams()
+        p.n = sysm.n
+        p.ntypes = sysm.ntypes
+        p.L[:] = [float(x) for x in sysm.L]
+        p.rc, p.rclist, p.rclist_ew = sysm.rc, sysm.rclist, sysm.rclist_ew
+        p.kappa, p.epsRF, p.dt, p.T = sysm.kappa, sysm.epsRF, sysm.dt, sysm.T
+        p.grid[:] = list(sysm.grid)
+        p.order = sysm.order
+        p.r_switch = sysm.r_switch
+        p.precision = precision
+        p.max_neighbors = max_neighbors
+        p.device = device
+        p.q, p.mass, p.type = _p(k["q"]), _p(k["mass"]), _p(k["type"])
+        p.lj_eps, p.lj_sig = _p(k["eps"]), _p(k["sig"])
+        p.nbond = k["bond_ab"].shape[0]
+        p.bond_ab, p.bond_req, p.bond_k = _p(k["bond_ab"]), _p(k["bond_req"]), _p(k["bond_k"])
+        p.nbend = k["bend_abc"].shape[0]
+        p.bend_abc, p.bend_theta0, p.bend_k = _p(k["bend_abc"]), _p(k["bend_t0"]), _p(k["bend_k"])
+        p.nexcl = k["excl_ab"].shape[0]
+        p.excl_ab, p.excl_flag = _p(k["excl_ab"]), _p(k["excl_flag"])
+        p.nhc_M = sysm.nhc_M
+        p.nhc_Q = sysm.nhc_Q
+        p.nfree = 0.0
+        self.params = p
+        h = C.c_void_p()
+        self._check(self.lib.fe_box_create(C.byref(h), C.byref(p)))
+        self.h = h
+        self.n = sysm.n
+        self.set_positions(sysm.pos, nopbc=True)
+        self.set_velocities(sysm.vel)
+
+    # ---- plumbing ----
+    def _check(self, rc):
+        if rc != FE_OK:
+            raise FeError(rc, self.lib.fe_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fe_box_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self.lib.fe_box_set_stream(self.h, C.c_void_p(stream_ptr or 0)))
+
+    # ---- state ----
+    def set_positions(self, pos, nopbc=False):
+        a = _c(pos, np.float64).reshape(-1, 3)
+        self._check(self.lib.fe_set_positions(self.h, _p(a), C.c_size_t(24), C.c_size_t(0),
+                                              int(nopbc)))
+
+    def set_positions_records(self, records: np.ndarray, stride: int, off_x: int, nopbc=False):
+        """Positions straight from reference-layout records (e.g. struct atoms)."""
+        self._check(self.lib.fe_set_positions(self.h, _p(records), C.c_size_t(stride),
+                                              C.c_size_t(off_x), int(nopbc)))
+
+    def get_positions(self):
+        out = np.empty((self.n, 3))
+        self._check(self.lib.fe_get_positions(self.h, _p(out), C.c_size_t(24), C.c_size_t(0)))
+        return out
+
+    def get_positions_records(self, records: np.ndarray, stride: int, off_x: int):
+        self._check(self.lib.fe_get_positions(self.h, _p(records), C.c_size_t(stride),
+                                              C.c_size_t(off_x)))
+
+    def get_positions_nopbc(self):
+        out = np.empty((self.n, 3))
+        self._check(self.lib.fe_get_positions_nopbc(self.h, _p(out), C.c_size_t(24),
+                                                    C.c_size_t(0)))
+        return out
+
+    def set_velocities(self, vv, uu=None):
+        v = _c(vv, np.float64).reshape(-1, 3)
+        u = v if uu is None else _c(uu, np.float64).reshape(-1, 3)
+        self._check(self.lib.fe_set_velocities(self.h, _p(v), _p(u)))
+
+    def get_velocities(self):
+        v = np.empty((self.n, 3))
+        u = np.empty((self.n, 3))
+        self._check(self.lib.fe_get_velocities(self.h, _p(v), _p(u)))
+        return v, u
+
+    def get_forces(self):
+        f = np.empty((self.n, 3))
+        self._check(self.lib.fe_get_forces(self.h, _p(f)))
+        return f
+
+    def get_nhc_state(self):
+        z = np.empty((max(self.sysm.nhc_M, 1), 3))
+        self._check(self.lib.fe_get_nhc_state(self.h, _p(z)))
+        return z
+
+    def set_nhc_state(self, zeta):
+        z = _c(zeta, np.float64)
+        self._check(self.lib.fe_set_nhc_state(self.h, _p(z)))
+
+    # ---- the reference's routines ----
+    def nblist(self):
+        self._check(self.lib.fe_nblist(self.h))
+
+    def nblist_download(self):
+        cnt = np.empty(self.n, np.int32)
+        tot = C.c_int64()
+        self._check(self.lib.fe_nblist_download(self.h, _p(cnt), None, None, C.c_int64(0),
+                                                C.byref(tot)))
+        idx = np.empty(max(tot.value, 1), np.int32)
+        flg = np.empty(max(tot.value, 1), np.int32)
+        self._check(self.lib.fe_nblist_download(self.h, _p(cnt), _p(idx), _p(flg),
+                                                C.c_int64(idx.size), C.byref(tot)))
+        return cnt, idx[:tot.value], flg[:tot.value]
+
+    def forces(self):
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_forces(self.h, _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
+
+    def cnonbondnl(self):
+        e = np.empty(8)
+        self._check(self.lib.fe_cnonbondnl(self.h, _p(e)))
+        return e
+
+    def pme_calc(self):
+        e = np.empty(3)
+        self._check(self.lib.fe_pme_calc(self.h, _p(e)))
+        return e
+
+    def charge_grid(self):
+        self._check(self.lib.fe_charge_grid(self.h))
+        g = np.empty(int(np.prod(self.sysm.grid)))
+        self._check(self.lib.fe_get_charge_grid(self.h, _p(g)))
+        return g.reshape(self.sysm.grid)
+
+    def bonded(self):
+        e = np.empty(2)
+        self._check(self.lib.fe_bonded(self.h, _p(e)))
+        return e
+
+    def zero_forces(self):
+        self._check(self.lib.fe_zero_forces(self.h))
+
+    def pbc_all(self):
+        self._check(self.lib.fe_pbc_all(self.h))
+
+    def kinet(self):
+        ken = np.empty(6)
+        k = C.c_double()
+        self._check(self.lib.fe_kinet(self.h, _p(ken), C.byref(k)))
+        return k.value, ken
+
+    def integrate_vverlet(self, vscal=1.0):
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_integrate_vverlet(self.h, C.c_double(vscal), _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
+
+    def integrate_nhc(self, time_step=None):
+        ts = self.sysm.dt if time_step is None else time_step
+        self._check(self.lib.fe_integrate_nhc(self.h, C.c_double(ts)))
+
+    def run_md(self, nsteps, nlist_freq=None, use_nhc=False, first_step=1, record=True):
+        nl = self.sysm.nlist_freq if nlist_freq is None else nlist_freq
+        rec = np.empty((max(nsteps, 1), FE_EN_COUNT)) if record else None
+        self._check(self.lib.fe_run_md(self.h, int(nsteps), int(nl), int(use_nhc),
+                                       C.c_long(first_step), _p(rec) if record else None))
+        return rec[:nsteps] if record else None
+
+    # ---- Monte Carlo energy path ----
+    def mc_setup(self, kmax=7, max_k_square=None, rc_ew=None):
+        mks = kmax * kmax if max_k_square is None else max_k_square
+        rc = self.sysm.rc_ew if rc_ew is None else rc_ew
+        self._check(self.lib.fe_mc_setup(self.h, int(kmax), int(mks), C.c_double(rc)))
+
+    def mc_delta(self, lb, ub, new_pos):
+        npos = _c(new_pos, np.float64).reshape(-1, 3)
+        de = C.c_double()
+        parts = np.empty(3)
+        self._check(self.lib.fe_mc_delta(self.h, int(lb), int(ub), _p(npos), C.byref(de),
+                                         _p(parts)))
+        return de.value, parts
+
+    def mc_accept(self):
+        self._check(self.lib.fe_mc_accept(self.h))
+
+    def mc_kspace_energy(self):
+        e = C.c_double()
+        self._check(self.lib.fe_mc_kspace_energy(self.h, C.byref(e)))
+        return e.value

@@ -98,6 +98,20 @@ def fft_friendly(n: int) -> int:
         m += 1
 
 
+def fft_friendly_below(n: int) -> int:
+    """Largest m <= n whose prime factors are 2, 3 and 5."""
+    m = max(int(n), 1)
+    while m > 1:
+        k = m
+        for p in (2, 3, 5):
+            while k % p == 0:
+                k //= p
+        if k == 1:
+            return m
+        m -= 1
+    return 1
+
+
 def _random_rotations(rng: np.random.Generator, n: int) -> np.ndarray:
     """Uniform random rotation matrices from unit quaternions."""
     qv = rng.normal(size=(n, 4))
@@ -170,15 +184,16 @@ def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
     """The 3-site bent-molecule box of the configured workloads.
 
     ``density`` is sites per A^3 (0.1 gives L = 34.47 A at 1,365 molecules and
-    L = 98.65 A at 32,000).  ``grid`` defaults to about 1 point/A rounded up
-    to an FFT-friendly size (32^3 and 96^3 for the two sizes above).
+    L = 98.65 A at 32,000).  ``grid`` defaults to about 1 point/A: round(L)
+    lowered to the nearest FFT-friendly size (32^3 and 96^3 for the two sizes
+    above).
     """
     rng = np.random.default_rng(seed)
     n = 3 * n_mol
     if L is None:
         L = (n / density) ** (1.0 / 3.0)
     if grid is None:
-        g = fft_friendly(int(math.ceil(L - 1e-9)))
+        g = fft_friendly_below(int(round(L)))
         grid = (g, g, g)
     centres = _place_centres(rng, n_mol, L, dmin)
     R = _random_rotations(rng, n_mol)
