@@ -1,0 +1,94 @@
+"""Mixed-precision path (FP32 pair/PME math, 64-bit fixed-point force sums,
+FP64 integration) against the FP64 CPU oracle.
+
+Bars: relative rms force error <= 1e-5 (forces summed over all terms);
+energies within 2e-6 relative of the force-field total; bitwise identical
+results on repeated evaluation (fixed-point sums are order independent)."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+RMS_TOL = 1e-5
+
+
+def _mixed(s):
+    from thecodecombo_7_gb300 import engine
+    return engine.Box(s, precision=engine.FE_PREC_MIXED)
+
+
+def _rms_rel(got, want):
+    return float(np.sqrt(((got - want) ** 2).sum() / (want ** 2).sum()))
+
+
+@pytest.fixture(scope="module", params=[(1365, None), (4000, None)], ids=["4095", "12000"])
+def case(request):
+    from thecodecombo_7_gb300 import systems
+    n_mol, _ = request.param
+    s = systems.water_box(n_mol, density=0.1, seed=77 + n_mol)
+    o = O.Oracle(s)
+    f_ref, en_ref = o.forces(s.pos)
+    return s, f_ref, en_ref
+
+
+def test_mixed_force_error(case):
+    s, f_ref, en_ref = case
+    with _mixed(s) as b:
+        b.nblist()
+        en = b.forces()
+        f = b.get_forces()
+    err = _rms_rel(f, f_ref)
+    assert err <= RMS_TOL, f"rms force error {err:.3e}"
+    pot_ref = en_ref["bond"] + en_ref["bend"] + en_ref["nbonds"]
+    scale = max(abs(en_ref["sewald"]), abs(pot_ref))
+    for k in ("bond", "bend", "nbond", "nbonds", "rewald", "kewald", "iewald", "tewald"):
+        assert abs(en[k] - en_ref[k]) <= 2e-6 * scale, (k, en[k], en_ref[k])
+
+
+def test_mixed_deterministic(case):
+    s, _, _ = case
+    with _mixed(s) as b:
+        b.nblist()
+        e1 = b.forces()
+        f1 = b.get_forces()
+        b.nblist()
+        e2 = b.forces()
+        f2 = b.get_forces()
+    assert np.array_equal(f1, f2)
+    assert e1 == e2
+
+
+def test_mixed_trajectory_tracks_fp64():
+    """20 NVE steps: the mixed trajectory stays within the FP32 error band of
+    the FP64 oracle trajectory."""
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(1365, density=0.1, seed=5)
+    o = O.Oracle(s)
+    md = o.run_md(20)
+    with _mixed(s) as b:
+        b.nblist()
+        b.forces()
+        b.kinet()
+        rec = b.run_md(20)
+        pos = b.get_positions()
+    d = pos - md["pos"]
+    d -= s.L * np.rint(d / s.L)
+    assert np.abs(d).max() < 1e-4
+    tot = rec[:, 0] + rec[:, 1] + rec[:, 2] + rec[:, 4]
+    tot_ref = (md["en"][1:, 0] + md["en"][1:, 1] + md["en"][1:, 2] + md["en"][1:, 4])
+    assert np.abs(tot - tot_ref).max() <= 1e-5 * np.abs(tot_ref).max()
+
+
+def test_mixed_switch_matches_oracle():
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(1365, density=0.1, seed=9, r_switch=8.0)
+    o = O.Oracle(s)
+    f_ref, en_ref = o.forces(s.pos)
+    with _mixed(s) as b:
+        b.nblist()
+        en = b.forces()
+        f = b.get_forces()
+    assert _rms_rel(f, f_ref) <= RMS_TOL
+    assert abs(en["nbond"] - en_ref["nbond"]) <= 2e-6 * abs(en_ref["sewald"])

@@ -20,6 +20,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libfe.so")
+HOSTLIB = os.path.join(HERE, "libfe_sysgen.so")
 ROOT = os.path.dirname(HERE)
 INCLUDE = os.path.join(ROOT, "include")
 
@@ -59,7 +60,19 @@ def _compile(src: str, obj: str, extra) -> str:
     return obj
 
 
+def build_host(force: bool = False) -> str:
+    """The workload generator's host helper (plain C, gcc)."""
+    src = os.path.join(CSRC, "sysgen.c")
+    if force or not os.path.exists(HOSTLIB) or os.path.getmtime(HOSTLIB) < os.path.getmtime(src):
+        tmp = HOSTLIB + ".tmp"
+        subprocess.check_call(["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared",
+                               "-ffp-contract=off", "-o", tmp, src, "-lm"])
+        os.replace(tmp, HOSTLIB)
+    return HOSTLIB
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
+    build_host(force)
     os.makedirs(BUILD, exist_ok=True)
     units = [u for u in UNITS if os.path.exists(os.path.join(CSRC, u))]
     hdr_time = max(os.path.getmtime(h) for h in _headers())

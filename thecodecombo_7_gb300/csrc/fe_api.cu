@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "fe_internal.h"
+#include "fe_mixed.h"
 
 namespace fe {
 
@@ -57,12 +58,18 @@ static int sync_scal(Box *b) {
   return check_status(b);
 }
 
+static int launch_list(Box *b) {
+  if (b->mx) return launch_mixed_list(b);
+  return launch_nblist(b);
+}
+
 // forces() on the device, forces.c:118-219
 static int forces_device(Box *b) {
   if (!b->have_list) {
     set_error("forces requested before a neighbour list was built (call nblist first)");
     return FE_ERR_STATE;
   }
+  if (b->mx) return forces_mixed(b);
   int rc;
   if ((rc = launch_zero_forces(b))) return rc;
   if ((rc = launch_bonded64(b))) return rc;
@@ -83,6 +90,7 @@ static void free_box(Box *b) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   mc_free(b);
+  mixed_free(b);
   if (b->host_scal) cudaFreeHost(b->host_scal);
   if (b->plans) {
     cufftDestroy(b->plan_r2c);
@@ -233,6 +241,16 @@ static int create(Box *b, const fe_box_params *p) {
   if ((rc = upload(&b->zeta, z.data(), z.size()))) return rc;
   if ((rc = nblist_setup(b))) return rc;
   if ((rc = spme_setup(b))) return rc;
+  if (p->precision == FE_PREC_MIXED) {
+    b->mx = new Mixed();
+    double kr = p->kappa * p->rc, z = fabs(kr), t = 1.0 / (1.0 + 0.5 * z);
+    double v = t * exp(-z * z + -1.26551223 +
+                       t * (1.00002368 + t * (0.37409196 + t * (0.09678418 +
+                       t * (-0.18628806 + t * (0.27886807 + t * (-1.13520398 +
+                       t * (1.48851587 + t * (-0.82215223 + t * 0.17087277)))))))));
+    b->mx->erfc_rc_over_rc = v / p->rc;  // ewald.c:817-836 at kappa*rc
+    if ((rc = mixed_setup(b))) return rc;
+  }
   FE_CUDA(cudaDeviceSynchronize());
   return FE_OK;
 }
@@ -256,7 +274,7 @@ static void stage_xyz_out(Box *b, void *atoms, size_t stride, size_t off, const 
 // one step of the production loop (graph body)
 static int step_body(Box *b, bool with_list, bool use_nhc) {
   int rc;
-  if (with_list && (rc = launch_nblist(b))) return rc;
+  if (with_list && (rc = launch_list(b))) return rc;
   if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
   if ((rc = launch_vv1(b, 1.0))) return rc;
   if ((rc = forces_device(b))) return rc;
@@ -439,7 +457,7 @@ int fe_get_nhc_state(fe_box *box, double *zeta) {
 
 int fe_nblist(fe_box *box) {
   if (!box) return FE_ERR_ARG;
-  int rc = launch_nblist(&box->b);
+  int rc = launch_list(&box->b);
   if (rc) return rc;
   return check_status(&box->b);
 }
@@ -447,8 +465,9 @@ int fe_nblist(fe_box *box) {
 int fe_nblist_download(fe_box *box, int *count, int *idx, int *flag, int64_t cap, int64_t *total) {
   if (!box || !count) return FE_ERR_ARG;
   Box *b = &box->b;
-  if (!b->have_list) {
-    set_error("no neighbour list built yet");
+  if (!b->have_list || b->mx) {
+    set_error(b->mx ? "list download is available for the FP64 drop-in list only"
+                    : "no neighbour list built yet");
     return FE_ERR_STATE;
   }
   std::vector<int> ent((size_t)b->n * b->max_nb);
@@ -500,6 +519,10 @@ int fe_cnonbondnl(fe_box *box, double *energy8) {
     set_error("cnonbondnl requested before a neighbour list was built");
     return FE_ERR_STATE;
   }
+  if (b->mx) {
+    set_error("fe_cnonbondnl is the FP64 drop-in entry; the mixed path evaluates fe_forces");
+    return FE_ERR_STATE;
+  }
   int rc;
   if ((rc = launch_pair64(b))) return rc;
   if ((rc = launch_pme64(b))) return rc;
@@ -514,6 +537,10 @@ int fe_cnonbondnl(fe_box *box, double *energy8) {
 int fe_pme_calc(fe_box *box, double *energy3) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;
+  if (b->mx) {
+    set_error("fe_pme_calc is the FP64 drop-in entry; the mixed path evaluates fe_forces");
+    return FE_ERR_STATE;
+  }
   int rc;
   if ((rc = launch_pme64(b))) return rc;
   if ((rc = launch_apply_pme(b))) return rc;

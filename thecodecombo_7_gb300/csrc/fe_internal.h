@@ -13,6 +13,8 @@
 
 namespace fe {
 
+struct Mixed;
+
 // Physical constants of the reference (defines.h:62-75).
 constexpr double kPI = 3.141592653589793238462643383;
 constexpr double kKB = 1.380662E-23;
@@ -46,7 +48,9 @@ enum : int {
   SC_NHC_SCALE = SC_KEN + 6,       // last NHC velocity scale
   SC_ENERGY8,                      // 8 slots: cnonbondnl energy[]
   SC_ENERGY3 = SC_ENERGY8 + 8,     // 3 slots: pme_calc energy[]
-  SC_COUNT = SC_ENERGY3 + 3
+  SC_MX_PAIR = SC_ENERGY3 + 3,     // 4 slots: mixed pair sums (lj, ljs, real, sum qq)
+  SC_MX_EXCL = SC_MX_PAIR + 4,     // 5 slots: mixed exclusion sums (.., intra)
+  SC_COUNT = SC_MX_EXCL + 5
 };
 
 // Largest number of blocks a partial-sum kernel may use.
@@ -137,6 +141,9 @@ struct Box {
   int mc_lb = 0, mc_ub = 0, mc_pending = 0;
   double *mc_part = nullptr;   // partial sums
   int mc_nmax = 0;             // capacity of a staged move
+
+  // mixed-precision path (k_mixed.cu); null in FP64 mode
+  Mixed *mx = nullptr;
 };
 
 // ---- error plumbing ----

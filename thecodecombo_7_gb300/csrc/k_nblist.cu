@@ -177,6 +177,10 @@ k_list(const double4 *__restrict__ pos, int n, double3 L, double rcut, double rc
   }
 }
 
+void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s) {
+  k_cell_scan<<<1, 1024, 0, s>>>(count, ncells, start, fill);
+}
+
 int nblist_setup(Box *b) {
   double cut = b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew;
   cut *= (1.0 + 1e-9);

@@ -22,6 +22,7 @@ import dataclasses
 import math
 
 import numpy as np
+from scipy.spatial import cKDTree
 
 KB = 1.380662e-23  # defines.h:63
 AU = 1.6605655e-27  # defines.h:66
@@ -134,48 +135,95 @@ def _place_centres(rng: np.random.Generator, n_mol: int, L: float,
                    dmin: float, max_tries: int = 400) -> np.ndarray:
     """Random sequential placement in a periodic cube with an O-O minimum.
 
-    A cell grid (cell >= dmin) keeps each trial O(1).  Candidates are drawn
-    in batches so the Python overhead stays per accepted molecule.
+    Candidates are drawn in batches of 4096; each batch is first screened in
+    one vectorised pass against the molecules accepted before it (a dense
+    cell grid, cell >= dmin, 8 slots per cell), then the survivors are taken
+    in order against the grid as it fills -- the same outcome as testing
+    every candidate sequentially against all earlier acceptances.
     """
     m = max(1, int(L // dmin))
     cell = L / m
-    heads: dict = {}
+    slots = 8
+    occ = np.full((m, m, m, slots, 3), np.nan)
+    nocc = np.zeros((m, m, m), dtype=np.int64)
     out = np.empty((n_mol, 3))
     d2 = dmin * dmin
+    offs = np.array([(a, b, c) for a in (-1, 0, 1) for b in (-1, 0, 1) for c in (-1, 0, 1)])
     count = 0
     tries = 0
+
+    def conflicts(cs, ci):
+        nb = (ci[:, None, :] + offs[None, :, :]) % m
+        pts = occ[nb[..., 0], nb[..., 1], nb[..., 2]]  # (B, 27, slots, 3)
+        d = pts - cs[:, None, None, :]
+        d -= L * np.rint(d / L)
+        r2 = np.einsum("bkst,bkst->bks", d, d)
+        return np.any(r2 < d2, axis=(1, 2))  # NaN slots compare False
+
     while count < n_mol:
         cand = rng.uniform(-L / 2, L / 2, size=(4096, 3))
-        for c in cand:
-            tries += 1
-            ci = ((c + L / 2) / cell).astype(int) % m
-            ok = True
-            for ox in (-1, 0, 1):
-                for oy in (-1, 0, 1):
-                    for oz in (-1, 0, 1):
-                        key = ((ci[0] + ox) % m, (ci[1] + oy) % m, (ci[2] + oz) % m)
-                        lst = heads.get(key)
-                        if not lst:
-                            continue
-                        d = out[lst] - c
-                        d -= L * np.rint(d / L)
-                        if np.any(np.einsum("ij,ij->i", d, d) < d2):
-                            ok = False
-                            break
-                    if not ok:
-                        break
-                if not ok:
-                    break
-            if ok:
-                out[count] = c
-                heads.setdefault((ci[0], ci[1], ci[2]), []).append(count)
-                count += 1
-                if count == n_mol:
-                    break
+        ci = ((cand + L / 2) / cell).astype(np.int64) % m
+        bad = conflicts(cand, ci)
+        surv = np.nonzero(~bad)[0]
+        keep = np.ones(surv.size, dtype=bool)
+        if surv.size > 1:
+            # conflicts among this batch's survivors: an earlier accepted one wins
+            tree = cKDTree(np.mod(cand[surv] + L / 2, L), boxsize=L)
+            pairs = tree.query_pairs(dmin, output_type="ndarray")
+            if len(pairs):
+                pairs = pairs[np.lexsort((pairs[:, 0], pairs[:, 1]))]
+                for i, j in pairs:
+                    if keep[i]:
+                        keep[j] = False
+        for k in surv[keep][: n_mol - count]:
+            cc = ci[k]
+            slot = nocc[cc[0], cc[1], cc[2]]
+            if slot >= slots:
+                raise RuntimeError("cell over capacity in the placement grid")
+            occ[cc[0], cc[1], cc[2], slot] = cand[k]
+            nocc[cc[0], cc[1], cc[2]] += 1
+            out[count] = cand[k]
+            count += 1
+        tries += 4096
         if tries > max_tries * n_mol:
             raise RuntimeError(
                 f"could not place {n_mol} molecules at L={L:.3f} with O-O >= {dmin}")
     return out
+
+
+def _place_centres_fast(rng: np.random.Generator, n_mol: int, L: float, dmin: float,
+                        max_tries: int = 400):
+    """Same placement as _place_centres (same candidate stream, same result)
+    through the C helper libfe_sysgen.so; None if the helper is not built."""
+    import ctypes as C
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "libfe_sysgen.so")
+    if not os.path.exists(path):
+        return None
+    lib = C.CDLL(path)
+    lib.fe_sysgen_place.restype = C.c_long
+    lib.fe_sysgen_place.argtypes = [C.c_void_p, C.c_long, C.c_double, C.c_double, C.c_long,
+                                    C.c_void_p, C.POINTER(C.c_long)]
+    out = np.zeros((n_mol, 3))
+    done = C.c_long(0)
+    drawn = 0
+    chunk = 4096 * 64
+    while True:
+        state = rng.bit_generator.state
+        cand = np.ascontiguousarray(rng.uniform(-L / 2, L / 2, size=(chunk, 3)))
+        used = lib.fe_sysgen_place(cand.ctypes.data, chunk, L, dmin, n_mol, out.ctypes.data,
+                                   C.byref(done))
+        if used == -2:
+            raise RuntimeError("cell over capacity in the placement grid")
+        if used > 0:
+            # advance the stream exactly as the batch-of-4096 version would
+            rng.bit_generator.state = state
+            rng.uniform(-L / 2, L / 2, size=(-(-used // 4096) * 4096, 3))
+            return out
+        drawn += chunk
+        if drawn > max_tries * n_mol:
+            raise RuntimeError(
+                f"could not place {n_mol} molecules at L={L:.3f} with O-O >= {dmin}")
 
 
 def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
@@ -195,7 +243,9 @@ def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
     if grid is None:
         g = fft_friendly_below(int(round(L)))
         grid = (g, g, g)
-    centres = _place_centres(rng, n_mol, L, dmin)
+    centres = _place_centres_fast(rng, n_mol, L, dmin)
+    if centres is None:
+        centres = _place_centres(rng, n_mol, L, dmin)
     R = _random_rotations(rng, n_mol)
     half = math.radians(104.5) / 2.0
     body = np.array([[0.0, 0.0, 0.0],
