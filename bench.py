@@ -1,0 +1,353 @@
+"""Throughput of the GB300 force engine on its headline workload.
+
+Workload (one step = one production MD step of nve_md.c:359-418): the 3-site
+water recipe scaled to 32,000 molecules (96,000 sites, L = 98.65 A, density
+0.1 sites/A^3), SPME 96^3 order 4, kappa 0.32, rc 10 A, Verlet list 12 A
+rebuilt every 10 steps, NVE velocity Verlet with dt = 0.5 fs, mixed
+precision (FP32 pair/PME math, 64-bit fixed-point force sums, FP64
+integration).  Synthetic seeded input (no dataset is involved).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line.  ``value`` is atom-steps/s with all state resident on
+the GPU (steps timed with CUDA events on the engine's stream); ``e2e`` is the
+same metric through the C ABI with host buffers (positions and velocities
+uploaded and positions, velocities and forces read back every step, as a
+drop-in integrate_vverlet called from the reference's host loop would).
+Under torchrun each rank runs its own replica (the single-box path does not
+shard: replicas only) and the slowest rank's time is used.
+``--impl reference`` times the reference's CPU implementation of the path
+(the pinned CPU restatement, built with the reference makefile's flags) on a
+bounded sample of the same workload, on rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_MOL = 32000
+SEED = 2025
+METRIC = "atom-steps/s"
+PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
+PROFILE = os.path.join(ROOT, "profiles", "k_mx_pair_water96k.md")
+WORKLOAD = ("water 3-site, 96,000 sites (32,000 molecules), L=98.65 A, SPME 96^3 order 4, "
+            "kappa 0.32, rc 10 A, list 12 A every 10 steps, NVE velocity Verlet dt 0.5 fs")
+
+
+def load_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d, "measured"
+    return PEAKS_FALLBACK, "fallback"
+
+
+def profile_traffic():
+    """dram read+write bytes per launch of the pair kernel from the committed
+    ncu summary (None if absent)."""
+    if not os.path.exists(PROFILE):
+        return None
+    with open(PROFILE) as f:
+        for line in f:
+            m = re.match(r"\s*traffic_bytes_per_launch:\s*([0-9.eE+]+)", line)
+            if m:
+                return float(m.group(1))
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.device)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            out, _ = self.proc.communicate(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+            out, _ = self.proc.communicate()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        import torch
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    return world, rank, local
+
+
+def allreduce_max(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def cpu_sample(sysm, nsteps_cap: int = 3):
+    """Times the CPU restatement of the path (reference makefile flags) on a
+    bounded sample: one O(N^2) list build and a few force+integration steps;
+    the per-step cost charges the list build once per nlist_freq steps as the
+    workload does."""
+    from oracle import oracle as orc
+    o = orc.Oracle(sysm, fast=True)
+    t0 = time.perf_counter()
+    o.nblist(sysm.pos)
+    t_list = time.perf_counter() - t0
+    ns = nsteps_cap
+    t0 = time.perf_counter()
+    o.run_md(ns - 1)  # list + forces, then ns-1 steps: ns force evaluations
+    t_md = time.perf_counter() - t0
+    t_step = (t_md - t_list) / ns
+    per_step = t_step + t_list / sysm.nlist_freq
+    return {
+        "value": sysm.n / per_step, "unit": METRIC, "cores": 1, "kind": "port",
+        "sample": (f"{sysm.n} sites: 1 O(N^2) list build ({t_list:.2f} s) + {ns} force/VV "
+                   f"evaluations ({t_step:.2f} s each); list charged every {sysm.nlist_freq} "
+                   "steps; single thread, reference makefile flags"),
+        "seconds": t_list + t_md,
+    }
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    from thecodecombo_7_gb300 import systems
+    sysm = systems.water_box(N_MOL, density=0.1, seed=SEED)
+    base = cpu_sample(sysm)
+    # --warmup/--steps map to bounded samples of the same workload
+    line = {
+        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": METRIC,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1000.0 * sysm.n / base["value"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "fp64 CPU (reference arithmetic)",
+                   "parallelism": "1 replica, 1 thread"},
+        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
+        "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    from thecodecombo_7_gb300 import build as fe_build
+    from thecodecombo_7_gb300 import engine, systems
+
+    if not os.path.exists(engine.LIB_PATH):
+        fe_build.build()
+    torch.cuda.set_device(local)
+    sysm = systems.water_box(N_MOL, density=0.1, seed=SEED + rank)
+    n = sysm.n
+    stream = torch.cuda.Stream(device=local)
+    box = engine.Box(sysm, precision=engine.FE_PREC_MIXED, device=local)
+    box.set_stream(stream.cuda_stream)
+    box.nblist()
+    box.forces()
+    box.kinet()
+    W = max(args.warmup, 3)
+    K = args.steps
+    box.run_md(W, first_step=1)
+    first = W + 1
+    nl = sysm.nlist_freq
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    box.run_md(K, nlist_freq=nl, first_step=first)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms_max = allreduce_max(ms, world)
+    value = world * n * K / (ms_max / 1000.0)
+    n_list_steps = sum(1 for i in range(first, first + K) if i % nl == 0)
+    lp, ll = box.step_launches(False)
+    launches = lp * (K - n_list_steps) + ll * n_list_steps
+    # dominant kernel: the pair loop, timed live on the same stream
+    pair_us = box.time_kernel(engine.FE_KERNEL_PAIR, reps=20)
+    entries, max_row = box.list_stats()
+    alg_bytes = 4.0 * entries + n * (16.0 + 4.0 + 4.0 + 24.0)
+    peaks, peak_kind = load_peaks()
+    achieved = alg_bytes / (pair_us * 1e-6) / 1e9
+    peak = float(peaks["hbm_gbs"])
+    traffic = profile_traffic()
+    # plain FP64 drop-in on the same workload (the 10x denominator), a few steps
+    fp64 = None
+    if rank == 0:
+        b64 = engine.Box(sysm, precision=engine.FE_PREC_FP64, device=local)
+        b64.set_stream(stream.cuda_stream)
+        b64.nblist()
+        b64.forces()
+        b64.kinet()
+        b64.run_md(3, first_step=1)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        k64 = 20
+        e0.record(stream)
+        b64.run_md(k64, first_step=4)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        fp64 = n * k64 / (e0.elapsed_time(e1) / 1000.0)
+        b64.close()
+    # end to end through the C ABI with host buffers (pinned)
+    ke = min(K, 30)
+    pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    nop_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    vv_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    uu_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    ff_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
+    pos_h[:] = box.get_positions()
+    nop_h[:] = box.get_positions_nopbc()
+    v, u = box.get_velocities()
+    vv_h[:] = v
+    uu_h[:] = u
+    lib = box.lib
+    import ctypes as C
+
+    def ptr(a):
+        return a.ctypes.data_as(C.c_void_p)
+
+    en = np.empty(engine.FE_EN_COUNT)
+    barrier(world)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for i in range(first + K, first + K + ke):
+        box._check(lib.fe_set_positions(box.h, ptr(pos_h), C.c_size_t(24), C.c_size_t(0), 0))
+        box._check(lib.fe_set_positions_nopbc(box.h, ptr(nop_h), C.c_size_t(24), C.c_size_t(0)))
+        box._check(lib.fe_set_velocities(box.h, ptr(vv_h), ptr(uu_h)))
+        if i % nl == 0:
+            box._check(lib.fe_nblist(box.h))
+        box._check(lib.fe_integrate_vverlet(box.h, C.c_double(1.0), ptr(en)))
+        box._check(lib.fe_kinet(box.h, None, None))
+        box._check(lib.fe_get_positions(box.h, ptr(pos_h), C.c_size_t(24), C.c_size_t(0)))
+        box._check(lib.fe_get_positions_nopbc(box.h, ptr(nop_h), C.c_size_t(24), C.c_size_t(0)))
+        box._check(lib.fe_get_velocities(box.h, ptr(vv_h), ptr(uu_h)))
+        box._check(lib.fe_get_forces(box.h, ptr(ff_h)))
+    torch.cuda.synchronize()
+    t_e2e = allreduce_max(time.perf_counter() - t0, world)
+    e2e = world * n * ke / t_e2e
+    h2d = 4 * 24 * n
+    d2h = 5 * 24 * n + 8 * engine.FE_EN_COUNT
+    box.close()
+    if rank != 0:
+        return
+    cpu = None
+    if world == 1:
+        try:
+            c = cpu_sample(sysm)
+            cpu = {k: c[k] for k in ("value", "unit", "cores", "kind", "sample")}
+        except Exception as exc:  # the GPU line must still print
+            cpu = {"value": None, "unit": METRIC, "cores": 1, "kind": "port",
+                   "sample": f"failed: {exc}"}
+    steps_per_s = K / (ms_max / 1000.0)
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
+        "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "precision": "mixed (FP32 pair/PME math, int64 "
+                   "fixed-point force sums, FP64 integration and energy sums)",
+                   "parallelism": f"replicas x{world}",
+                   "cache": "inputs larger than L2 (pair list ~280 MB read per step)",
+                   "ns_per_day": steps_per_s * 0.0005e-3 * 86400.0},
+        "roofline": {"kernel": "k_mx_pair", "bound": "hbm", "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
+                     "us_per_launch": pair_us, "list_entries": entries, "max_row": max_row},
+        "cpu_baseline": cpu,
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "steps": ke},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "fp64_drop_in": {"value": fp64, "unit": METRIC,
+                         "ratio": (value / world) / fp64 if fp64 else None},
+    }
+    print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    args = ap.parse_args()
+    world, rank, local = dist_setup() if args.impl == "ours" else (
+        int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1 and args.impl == "ours":
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -200,6 +200,20 @@ int fe_mc_accept(fe_box *box);
 /* Current k-space energy from the maintained S(k) (ewald_kspace_mc enkewald[0]). */
 int fe_mc_kspace_energy(fe_box *box, double *e);
 
+/* ---- instrumentation (no counterpart in the reference) ----------------- */
+
+enum { FE_KERNEL_PAIR = 0, FE_KERNEL_SPREAD = 1, FE_KERNEL_LIST = 2 };
+/* Re-launches one kernel of the force step on the current state `reps` times
+ * between CUDA events on the box's stream; *us = mean device time per launch.
+ * Scratch sums are overwritten; call fe_forces again before reading forces. */
+int fe_time_kernel(fe_box *box, int which, int reps, double *us);
+/* Number of this library's own kernel launches in one fe_run_md step without
+ * and with a list rebuild (cuFFT's kernels not included). */
+int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list);
+/* Entries of the current pair list (half list in FP64 mode, full list in
+ * mixed mode) and the longest row. */
+int fe_list_stats(fe_box *box, int64_t *entries, int *max_row);
+
 #ifdef __cplusplus
 }
 #endif

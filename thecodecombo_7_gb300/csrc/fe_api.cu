@@ -13,6 +13,7 @@
 namespace fe {
 
 static thread_local std::string g_err;
+thread_local long g_launches = 0;
 
 void set_error(const std::string &msg) { g_err = msg; }
 
@@ -92,6 +93,7 @@ static void free_box(Box *b) {
   mc_free(b);
   mixed_free(b);
   if (b->host_scal) cudaFreeHost(b->host_scal);
+  if (b->stage) cudaFreeHost(b->stage);
   if (b->plans) {
     cufftDestroy(b->plan_r2c);
     cufftDestroy(b->plan_c2r);
@@ -223,6 +225,7 @@ static int create(Box *b, const fe_box_params *p) {
   FE_CUDA(cudaMalloc(&b->status, sizeof(int)));
   FE_CUDA(cudaMemset(b->status, 0, sizeof(int)));
   FE_CUDA(cudaMallocHost(&b->host_scal, sizeof(double) * SC_COUNT));
+  FE_CUDA(cudaMallocHost(&b->stage, sizeof(double) * 4 * (size_t)n));
   FE_CUDA(cudaMalloc(&b->rec_counter, sizeof(int)));
   // self energy, ewald.c:61,172-178
   double fconv = (kELEC * kELEQ * kELEQ * kNA * 0.001) / p->epsRF;
@@ -284,10 +287,26 @@ static int step_body(Box *b, bool with_list, bool use_nhc) {
   return launch_record(b);
 }
 
+int relaunch_kernel(Box *b, int which) {
+  if (b->mx) {
+    if (which == FE_KERNEL_PAIR) return launch_mx_pair_only(b);
+    if (which == FE_KERNEL_SPREAD) return launch_mx_spread_only(b);
+    if (which == FE_KERNEL_LIST) return launch_mixed_list(b);
+  } else {
+    if (which == FE_KERNEL_PAIR) return launch_pair64(b);
+    if (which == FE_KERNEL_SPREAD) return launch_charge_grid64(b);
+    if (which == FE_KERNEL_LIST) return launch_nblist(b);
+  }
+  set_error("fe_time_kernel: unknown kernel id");
+  return FE_ERR_ARG;
+}
+
 static int capture(Box *b, bool with_list, bool use_nhc, cudaGraphExec_t *out) {
   cudaGraph_t g;
   FE_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  long l0 = g_launches;
   int rc = step_body(b, with_list, use_nhc);
+  (with_list ? b->launches_list : b->launches_plain) = (int)(g_launches - l0);
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
@@ -354,17 +373,19 @@ int fe_box_set_stream(fe_box *box, void *stream) {
 int fe_set_positions(fe_box *box, const void *atoms, size_t stride, size_t off_x, int nopbc) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;
-  std::vector<double> v;
-  int rc = stage_xyz_in(b, atoms, stride, off_x, v);
-  if (rc) return rc;
-  std::vector<double4> pq(b->n);
-  for (int i = 0; i < b->n; i++) pq[i] = make_double4(v[3 * i], v[3 * i + 1], v[3 * i + 2], b->p.q[i]);
-  // keep q as uploaded at creation: only x, y, z change here
-  FE_CUDA(cudaMemcpy2DAsync(b->pos_q, sizeof(double4), pq.data(), sizeof(double4), 3 * sizeof(double),
+  if (!atoms || stride < 24) {
+    set_error("positions: null pointer or stride < 24");
+    return FE_ERR_ARG;
+  }
+  // gather x, y, z into pinned staging laid out as double4 (q untouched on the device)
+  double *st = b->stage;
+  const char *base = (const char *)atoms + off_x;
+  for (int i = 0; i < b->n; i++) memcpy(st + 4 * (size_t)i, base + (size_t)i * stride, 24);
+  FE_CUDA(cudaMemcpy2DAsync(b->pos_q, sizeof(double4), st, sizeof(double4), 3 * sizeof(double),
                             b->n, cudaMemcpyHostToDevice, b->stream));
   if (nopbc)
-    FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, v.data(), sizeof(double) * 3 * b->n,
-                            cudaMemcpyHostToDevice, b->stream));
+    FE_CUDA(cudaMemcpy2DAsync(b->pos_nopbc, 3 * sizeof(double), st, sizeof(double4),
+                              3 * sizeof(double), b->n, cudaMemcpyHostToDevice, b->stream));
   FE_CUDA(cudaStreamSynchronize(b->stream));
   return FE_OK;
 }
@@ -372,17 +393,12 @@ int fe_set_positions(fe_box *box, const void *atoms, size_t stride, size_t off_x
 int fe_get_positions(fe_box *box, void *atoms, size_t stride, size_t off_x) {
   if (!box || !atoms || stride < 24) return FE_ERR_ARG;
   Box *b = &box->b;
-  std::vector<double4> pq(b->n);
-  FE_CUDA(cudaMemcpyAsync(pq.data(), b->pos_q, sizeof(double4) * b->n, cudaMemcpyDeviceToHost,
-                          b->stream));
+  double *st = b->stage;
+  FE_CUDA(cudaMemcpy2DAsync(st, 3 * sizeof(double), b->pos_q, sizeof(double4), 3 * sizeof(double),
+                            b->n, cudaMemcpyDeviceToHost, b->stream));
   FE_CUDA(cudaStreamSynchronize(b->stream));
-  std::vector<double> v(3 * (size_t)b->n);
-  for (int i = 0; i < b->n; i++) {
-    v[3 * i] = pq[i].x;
-    v[3 * i + 1] = pq[i].y;
-    v[3 * i + 2] = pq[i].z;
-  }
-  stage_xyz_out(b, atoms, stride, off_x, v);
+  char *base = (char *)atoms + off_x;
+  for (int i = 0; i < b->n; i++) memcpy(base + (size_t)i * stride, st + 3 * (size_t)i, 24);
   return FE_OK;
 }
 
@@ -657,6 +673,66 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
     FE_CUDA(cudaMemcpyAsync(rec, b->rec, sizeof(double) * FE_EN_COUNT * (size_t)nsteps,
                             cudaMemcpyDeviceToHost, b->stream));
   if ((rc = sync_scal(b))) return rc;
+  return FE_OK;
+}
+
+int fe_time_kernel(fe_box *box, int which, int reps, double *us) {
+  if (!box || reps < 1 || !us) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!b->have_list) {
+    set_error("fe_time_kernel needs a built list");
+    return FE_ERR_STATE;
+  }
+  cudaEvent_t e0, e1;
+  FE_CUDA(cudaEventCreate(&e0));
+  FE_CUDA(cudaEventCreate(&e1));
+  int rc = relaunch_kernel(b, which);  // warm
+  if (rc) return rc;
+  FE_CUDA(cudaEventRecord(e0, b->stream));
+  for (int r = 0; r < reps; r++)
+    if ((rc = relaunch_kernel(b, which))) return rc;
+  FE_CUDA(cudaEventRecord(e1, b->stream));
+  FE_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  FE_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *us = 1000.0 * ms / reps;
+  return check_status(b);
+}
+
+int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int key = use_nhc ? 1 : 0;
+  if (b->g_key != key) {
+    set_error("fe_step_launches: run fe_run_md with the same use_nhc first");
+    return FE_ERR_STATE;
+  }
+  if (plain) *plain = b->launches_plain;
+  if (with_list) *with_list = b->launches_list;
+  return FE_OK;
+}
+
+int fe_list_stats(fe_box *box, int64_t *entries, int *max_row) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!b->have_list) {
+    set_error("no list built yet");
+    return FE_ERR_STATE;
+  }
+  std::vector<int> c(b->n);
+  const int *src = b->mx ? mixed_counts(b) : b->nl_count;
+  FE_CUDA(cudaMemcpyAsync(c.data(), src, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  int64_t e = 0;
+  int m = 0;
+  for (int v : c) {
+    e += v;
+    if (v > m) m = v;
+  }
+  if (entries) *entries = e;
+  if (max_row) *max_row = m;
   return FE_OK;
 }
 

@@ -129,6 +129,8 @@ struct Box {
   int *rec_counter = nullptr;
   cudaGraphExec_t g_step = nullptr, g_step_list = nullptr;
   int g_key = -1;              // graph capture key (use_nhc)
+  int launches_plain = 0, launches_list = 0;  // own kernels per captured step
+  double *stage = nullptr;     // pinned host staging, 3n doubles
 
   // MC (classic Ewald)
   int mc_nk = 0, mc_kmax = 0, mc_mks = 0;
@@ -158,8 +160,12 @@ int check_status(Box *b);  // reads the device status word (synchronises)
     if (e_ != cudaSuccess) return ::fe::cuda_fail(e_, #call); \
   } while (0)
 
+// counts this library's kernel launches (one per FE_LAUNCH_CHECK)
+extern thread_local long g_launches;
+
 #define FE_LAUNCH_CHECK(what)                                 \
   do {                                                        \
+    ++::fe::g_launches;                                       \
     cudaError_t e_ = cudaGetLastError();                      \
     if (e_ != cudaSuccess) return ::fe::cuda_fail(e_, what);  \
   } while (0)
@@ -186,6 +192,8 @@ int launch_pbc(Box *b);
 int launch_kinet(Box *b);
 int launch_nhc(Box *b, double time_step);
 int launch_record(Box *b);
+// instrumentation: relaunch one kernel (FE_KERNEL_*) on the current state
+int relaunch_kernel(Box *b, int which);
 // k_mc.cu
 int mc_setup(Box *b, int kmax, int mks, double rc_ew);
 int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, double *parts);

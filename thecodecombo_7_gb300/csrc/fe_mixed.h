@@ -40,6 +40,9 @@ void mixed_free(Box *b);
 int launch_mixed_list(Box *b);
 int forces_mixed(Box *b);
 int launch_mixed_assemble(Box *b);
+int launch_mx_pair_only(Box *b);
+const int *mixed_counts(Box *b);    // device row counts of the full list    // the pair kernel alone (timing)
+int launch_mx_spread_only(Box *b);  // the spreading kernel alone (timing)
 void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s);
 
 }  // namespace fe

@@ -283,6 +283,7 @@ int launch_nhc(Box *b, double time_step) {
   if (rc) return rc;
   k_nhc_chain<<<1, 32, 0, b->stream>>>(b->nhc_M, b->nhc_Q, b->nfree, b->p.T, time_step, b->zeta,
                                        b->scal);
+  FE_LAUNCH_CHECK("k_nhc_chain");
   k_nhc_scale<<<(3 * b->n + 255) / 256, 256, 0, b->stream>>>(3 * b->n, b->scal, b->vv, b->uu);
   FE_LAUNCH_CHECK("k_nhc_scale");
   return FE_OK;

@@ -767,10 +767,14 @@ int launch_mixed_list(Box *b) {
   int3 nc = make_int3(M.nc[0], M.nc[1], M.nc[2]);
   FE_CUDA(cudaMemsetAsync(M.cell_count, 0, sizeof(int) * M.ncells, b->stream));
   k_mx_cell<<<(n + 255) / 256, 256, 0, b->stream>>>(n, b->pos_q, L, h, nc, M.cell_of, M.cell_count);
+  FE_LAUNCH_CHECK("k_mx_cell");
   k_cell_scan_ext(M.cell_count, M.ncells, M.cell_start, M.cell_fill, b->stream);
   k_mx_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.cell_of, M.cell_start, M.cell_fill, M.perm);
+  FE_LAUNCH_CHECK("k_mx_fill");
   k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s, b->status);
+  FE_LAUNCH_CHECK("k_mx_cellsort");
   k_mx_types<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.perm, b->type, M.type_s);
+  FE_LAUNCH_CHECK("k_mx_types");
   int rc = launch_convert(b);
   if (rc) return rc;
   float3 hf = make_float3((float)M.h[0], (float)M.h[1], (float)M.h[2]);
@@ -786,13 +790,16 @@ int launch_mixed_list(Box *b) {
   return FE_OK;
 }
 
-int forces_mixed(Box *b) {
+const int *mixed_counts(Box *b) { return b->mx->count; }
+
+static int pair_blocks(Box *b) {
+  int blocks = (b->n + kMxWarps - 1) / kMxWarps;
+  return blocks > 2048 ? 2048 : blocks;
+}
+
+int launch_mx_pair_only(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
-  int rc;
-  if ((rc = launch_convert(b))) return rc;
-  FE_CUDA(cudaMemsetAsync(M.fix, 0, sizeof(unsigned long long) * 3 * n, b->stream));
-  // pair loop
   MxPair P;
   P.n = n;
   P.nt = b->nt;
@@ -806,20 +813,40 @@ int forces_mixed(Box *b) {
   double rc2 = b->p.rc * b->p.rc;
   P.ron2 = (float)ron2;
   P.sw_den = ron2 > 0.0 ? (float)((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2)) : 0.f;
-  int blocks = (n + kMxWarps - 1) / kMxWarps;
-  if (blocks > 2048) blocks = 2048;
+  int blocks = pair_blocks(b);
   size_t shm = sizeof(float) * (kCodes * 6 + b->nt * b->nt * 3);
   k_mx_pair<<<blocks, kMxWarps * 32, shm, b->stream>>>(P, M.pos32, M.type_s, M.perm, M.count, M.ent,
                                                       M.shift_tab, M.lj_tab, M.fix, b->partials);
   FE_LAUNCH_CHECK("k_mx_pair");
-  if ((rc = launch_reduce(b, b->partials, blocks, 4, SC_MX_PAIR, 1.0))) return rc;
+  return FE_OK;
+}
+
+int launch_mx_spread_only(Box *b) {
+  Mixed &M = *b->mx;
+  int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
+  k_mx_spread<<<(unsigned)((b->K + 127) / 128), 128, 0, b->stream>>>(
+      b->order, G, M.pos32, M.sm, b->gcap, b->gbin_count, b->gbin_atoms, M.grid32);
+  FE_LAUNCH_CHECK("k_mx_spread");
+  return FE_OK;
+}
+
+int forces_mixed(Box *b) {
+  Mixed &M = *b->mx;
+  int n = b->n;
+  int rc;
+  if ((rc = launch_convert(b))) return rc;
+  FE_CUDA(cudaMemsetAsync(M.fix, 0, sizeof(unsigned long long) * 3 * n, b->stream));
+  if ((rc = launch_mx_pair_only(b))) return rc;
+  if ((rc = launch_reduce(b, b->partials, pair_blocks(b), 4, SC_MX_PAIR, 1.0))) return rc;
+  double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
   // exclusions
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   int xb = (M.nexcl + 255) / 256;
   if (xb > 1024) xb = 1024;
   if (xb < 1) xb = 1;
   k_mx_excl<<<xb, 256, 0, b->stream>>>(M.nexcl, M.excl_ab, M.excl_flag, b->pos_q, b->type, L, b->nt,
-                                       M.lj_tab, P.rc2, P.kappa, P.c2k, (float)qf,
+                                       M.lj_tab, (float)(b->p.rc * b->p.rc), (float)b->p.kappa,
+                                       (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
                                        (float)b->p.epsRF, M.fix, b->partials);
   FE_LAUNCH_CHECK("k_mx_excl");
   if ((rc = launch_reduce(b, b->partials, xb, 5, SC_MX_EXCL, 1.0))) return rc;
@@ -839,8 +866,10 @@ int forces_mixed(Box *b) {
   k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, L, b->pos_q, M.perm, M.floor3,
                                                        M.sm, M.sd, b->gcap, b->gbin_count,
                                                        b->gbin_atoms, b->status);
+  FE_LAUNCH_CHECK("k_mx_splines");
   k_mx_binsort<<<(unsigned)((b->K + 255) / 256), 256, 0, b->stream>>>(b->K, b->gcap, b->gbin_count,
                                                                      b->gbin_atoms);
+  FE_LAUNCH_CHECK("k_mx_binsort");
   k_mx_spread<<<(unsigned)((b->K + 127) / 128), 128, 0, b->stream>>>(
       b->order, G, M.pos32, M.sm, b->gcap, b->gbin_count, b->gbin_atoms, M.grid32);
   FE_LAUNCH_CHECK("k_mx_spread");
@@ -861,7 +890,8 @@ int forces_mixed(Box *b) {
                           (float)(b->G[2] / b->p.L[2]));
   int gb = (n + 127) / 128;
   if (gb > 1024) gb = 1024;
-  k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, P.qfe, M.pos32, M.perm, M.floor3, M.sm,
+  float qfe = (float)(qf / b->p.epsRF);
+  k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.pos32, M.perm, M.floor3, M.sm,
                                          M.sd, M.grid32, M.fix, b->partials);
   FE_LAUNCH_CHECK("k_mx_gather");
   if ((rc = launch_reduce(b, b->partials, gb, 3, SC_FMEAN, 1.0))) return rc;

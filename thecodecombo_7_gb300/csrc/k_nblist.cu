@@ -179,6 +179,7 @@ k_list(const double4 *__restrict__ pos, int n, double3 L, double rcut, double rc
 
 void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s) {
   k_cell_scan<<<1, 1024, 0, s>>>(count, ncells, start, fill);
+  ++g_launches;
 }
 
 int nblist_setup(Box *b) {
@@ -212,9 +213,12 @@ int launch_nblist(Box *b) {
   int3 nc = make_int3(b->nc[0], b->nc[1], b->nc[2]);
   FE_CUDA(cudaMemsetAsync(b->cell_count, 0, sizeof(int) * b->ncells, b->stream));
   k_cell_count<<<(n + 255) / 256, 256, 0, b->stream>>>(b->pos_q, n, L, nc, b->cell_of, b->cell_count);
+  FE_LAUNCH_CHECK("k_cell_count");
   k_cell_scan<<<1, 1024, 0, b->stream>>>(b->cell_count, b->ncells, b->cell_start, b->cell_fill);
+  FE_LAUNCH_CHECK("k_cell_scan");
   k_cell_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, b->cell_of, b->cell_start, b->cell_fill,
                                                       b->cell_atoms);
+  FE_LAUNCH_CHECK("k_cell_fill");
   double rcut = b->p.rclist;
   double rcut2 = b->p.rclist * b->p.rclist;
   double rcut2_ew = b->p.rclist_ew * b->p.rclist_ew;

@@ -302,8 +302,10 @@ int launch_charge_grid64(Box *b) {
   k_splines<<<(b->n + 127) / 128, 128, 0, b->stream>>>(b->n, b->order, G, L, b->pos_q, b->spl_floor,
                                                        b->spl_m, b->spl_d, b->gcap, b->gbin_count,
                                                        b->gbin_atoms, b->status);
+  FE_LAUNCH_CHECK("k_splines");
   k_bin_sort<<<(unsigned)((b->K + 255) / 256), 256, 0, b->stream>>>(b->K, b->gcap, b->gbin_count,
                                                                    b->gbin_atoms);
+  FE_LAUNCH_CHECK("k_bin_sort");
   k_spread<<<(unsigned)((b->K + 127) / 128), 128, 0, b->stream>>>(
       b->order, G, b->pos_q, b->spl_m, b->gcap, b->gbin_count, b->gbin_atoms, b->grid);
   FE_LAUNCH_CHECK("k_spread");

@@ -44,7 +44,11 @@ EXPORTS = [
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
+    "fe_time_kernel", "fe_step_launches", "fe_list_stats",
 ]
+FE_KERNEL_PAIR = 0
+FE_KERNEL_SPREAD = 1
+FE_KERNEL_LIST = 2
 
 
 class FeError(RuntimeError):
@@ -293,6 +297,22 @@ class Box:
         self._check(self.lib.fe_run_md(self.h, int(nsteps), int(nl), int(use_nhc),
                                        C.c_long(first_step), _p(rec) if record else None))
         return rec[:nsteps] if record else None
+
+    # ---- instrumentation ----
+    def time_kernel(self, which=FE_KERNEL_PAIR, reps=20):
+        us = C.c_double()
+        self._check(self.lib.fe_time_kernel(self.h, int(which), int(reps), C.byref(us)))
+        return us.value
+
+    def list_stats(self):
+        e, m = C.c_int64(), C.c_int()
+        self._check(self.lib.fe_list_stats(self.h, C.byref(e), C.byref(m)))
+        return e.value, m.value
+
+    def step_launches(self, use_nhc=False):
+        a, b = C.c_int(), C.c_int()
+        self._check(self.lib.fe_step_launches(self.h, int(use_nhc), C.byref(a), C.byref(b)))
+        return a.value, b.value
 
     # ---- Monte Carlo energy path ----
     def mc_setup(self, kmax=7, max_k_square=None, rc_ew=None):
