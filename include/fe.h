@@ -200,6 +200,25 @@ int fe_mc_accept(fe_box *box);
 /* Current k-space energy from the maintained S(k) (ewald_kspace_mc enkewald[0]). */
 int fe_mc_kspace_energy(fe_box *box, double *e);
 
+/* ---- allocation-free entry (no counterpart in the reference) ---------------
+ *
+ * For callers that may not allocate device memory themselves -- a plug-in
+ * inside a host program whose device memory all comes from that program's own
+ * allocator (a caching allocator or a pool reserved once under a fixed
+ * budget).  Computes the classic-Ewald reciprocal energy of ewald_kspace_mc
+ * (ewald_mc.c:186-287 with the k-vectors of ewald.c:104-118, in kJ/mol) of
+ * n sites given as device memory xyzq[4*i+0..3] = x, y, z, q, into the device
+ * double *energy, on `stream` (a cudaStream_t, NULL = the legacy default
+ * stream).  L is a host array of the 3 box lengths.  Allocates nothing: its
+ * only temporary is a fixed 64 KB array in device memory that each GPU using
+ * the library keeps until the process exits.  Limit: (kmax+1)*(2*kmax+1)^2 <=
+ * 8192 candidate k-vectors (kmax <= 12), else FE_ERR_SIZE.  The first call on
+ * a device looks up that array's device address, so make the first call on
+ * each device before any stream capture.  All calls share the array; calls
+ * whose kernels overlap on the GPU race and must be serialised. */
+int fe_ewald_kspace_energy_noalloc(const double *xyzq, int n, const double *L, double kappa,
+                                   int kmax, int max_k_square, double *energy, void *stream);
+
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 
 enum { FE_KERNEL_PAIR = 0, FE_KERNEL_SPREAD = 1, FE_KERNEL_LIST = 2 };

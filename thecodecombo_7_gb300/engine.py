@@ -45,6 +45,7 @@ EXPORTS = [
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats",
+    "fe_ewald_kspace_energy_noalloc",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
