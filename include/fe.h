@@ -130,6 +130,9 @@ int fe_get_positions_nopbc(fe_box *box, void *atoms, size_t stride, size_t off_x
 int fe_set_velocities(fe_box *box, const double *vv, const double *uu);
 int fe_get_velocities(fe_box *box, double *vv, double *uu);
 int fe_get_forces(fe_box *box, double *ff);
+/* ff[k] before routines that accumulate into it (cnonbondnl, pme_calc) or
+ * read it (the first half-kick of integrate_vverlet). */
+int fe_set_forces(fe_box *box, const double *ff);
 /* NHC state nhc[k].zeta[j].{r,v,G}: 3*M doubles */
 int fe_set_nhc_state(fe_box *box, const double *zeta);
 int fe_get_nhc_state(fe_box *box, double *zeta);

@@ -89,3 +89,23 @@ def test_water_box_recipe():
     np.testing.assert_allclose(p, 0.0, atol=1e-9)
     assert systems.fft_friendly(97) == 100 and systems.fft_friendly(96) == 96
     assert systems.fft_friendly_below(99) == 96 and systems.fft_friendly_below(34) == 32
+
+
+@pytest.mark.skipif(not os.path.exists("/root/reference/makefile"),
+                    reason="reference sources not present")
+def test_reference_program_links_against_the_engine(lib):
+    """The reference's own program, with the nine replaced routines taken out
+    of its SRCS and the drop-in shim added, compiles and links against
+    libfe.so; the replaced symbols resolve to the shim."""
+    script = os.path.join(ROOT, "thecodecombo_7_gb300", "dropin", "build_reference_with_engine.sh")
+    subprocess.check_call(["sh", script], stdout=subprocess.DEVNULL)
+    out = os.path.join(ROOT, "thecodecombo_7_gb300", "dropin", "_build")
+    assert os.path.exists(os.path.join(out, "spidey_gpu"))
+    syms = subprocess.run(["nm", "--defined-only", os.path.join(out, "fe_dropin.o")],
+                          capture_output=True, text=True).stdout
+    for name in ("nblist", "forces", "cnonbondnl", "pme_calc", "charge_grid",
+                 "integrate_vverlet", "integrate_nhc", "pbc_all", "kinet"):
+        assert re.search(rf"\bT {name}\b", syms), name
+    need = subprocess.run(["nm", "-u", os.path.join(out, "fe_dropin.o")], capture_output=True,
+                          text=True).stdout
+    assert "fe_forces" in need and "fe_box_create" in need

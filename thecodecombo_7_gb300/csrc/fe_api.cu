@@ -453,6 +453,14 @@ int fe_get_forces(fe_box *box, double *ff) {
   return FE_OK;
 }
 
+int fe_set_forces(fe_box *box, const double *ff) {
+  if (!box || !ff) return FE_ERR_ARG;
+  Box *b = &box->b;
+  FE_CUDA(cudaMemcpyAsync(b->ff, ff, sizeof(double) * 3 * b->n, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
 int fe_set_nhc_state(fe_box *box, const double *zeta) {
   if (!box || !zeta) return FE_ERR_ARG;
   Box *b = &box->b;

@@ -39,7 +39,7 @@ FE_EN_COUNT = len(EN_KEYS)
 EXPORTS = [
     "fe_box_create", "fe_box_destroy", "fe_box_set_stream", "fe_last_error", "fe_abi_version",
     "fe_set_positions", "fe_get_positions", "fe_set_positions_nopbc", "fe_get_positions_nopbc",
-    "fe_set_velocities", "fe_get_velocities", "fe_get_forces", "fe_set_nhc_state",
+    "fe_set_velocities", "fe_get_velocities", "fe_get_forces", "fe_set_forces", "fe_set_nhc_state",
     "fe_get_nhc_state", "fe_nblist", "fe_nblist_download", "fe_forces", "fe_cnonbondnl",
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
@@ -220,6 +220,10 @@ class Box:
         f = np.empty((self.n, 3))
         self._check(self.lib.fe_get_forces(self.h, _p(f)))
         return f
+
+    def set_forces(self, ff):
+        f = _c(ff, np.float64).reshape(-1, 3)
+        self._check(self.lib.fe_set_forces(self.h, _p(f)))
 
     def get_nhc_state(self):
         z = np.empty((max(self.sysm.nhc_M, 1), 3))
