@@ -86,7 +86,7 @@ static void free_box(Box *b) {
                   b->bond_req, b->bond_k, b->bend_t0, b->bend_k, b->cell_count, b->cell_start,
                   b->cell_fill, b->cell_atoms, b->cell_of, b->nl_count, b->nl_ent, b->eterm,
                   b->kweight, b->grid, b->grid_k, b->spl_floor, b->spl_m, b->spl_d, b->fp,
-                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->zeta, b->rec,
+                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->zeta, b->rec,
                   b->rec_counter};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -100,6 +100,7 @@ static void free_box(Box *b) {
   }
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
+  if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -224,6 +225,8 @@ static int create(Box *b, const fe_box_params *p) {
   FE_CUDA(cudaMemset(b->scal, 0, sizeof(double) * SC_COUNT));
   FE_CUDA(cudaMalloc(&b->status, sizeof(int)));
   FE_CUDA(cudaMemset(b->status, 0, sizeof(int)));
+  FE_CUDA(cudaMalloc(&b->ticket, sizeof(unsigned)));
+  FE_CUDA(cudaMemset(b->ticket, 0, sizeof(unsigned)));
   FE_CUDA(cudaMallocHost(&b->host_scal, sizeof(double) * SC_COUNT));
   FE_CUDA(cudaMallocHost(&b->stage, sizeof(double) * 4 * (size_t)n));
   FE_CUDA(cudaMalloc(&b->rec_counter, sizeof(int)));
@@ -274,16 +277,24 @@ static void stage_xyz_out(Box *b, void *atoms, size_t stride, size_t off, const 
   for (int i = 0; i < b->n; i++) memcpy(base + (size_t)i * stride, &v[3 * (size_t)i], 24);
 }
 
-// one step of the production loop (graph body)
-static int step_body(Box *b, bool with_list, bool use_nhc) {
+// one step of the production loop (graph body); `prune` refreshes the mixed
+// path's inner list inside the force evaluation
+static int step_body(Box *b, bool with_list, bool use_nhc, bool prune) {
   int rc;
   if (with_list && (rc = launch_list(b))) return rc;
+  if (b->mx) b->mx->do_prune = with_list || prune;
   if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
   if ((rc = launch_vv1(b, 1.0))) return rc;
   if ((rc = forces_device(b))) return rc;
-  if ((rc = launch_vv2(b, 1.0))) return rc;
-  if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
-  if ((rc = launch_kinet(b))) return rc;
+  if (use_nhc) {
+    if ((rc = launch_vv2(b, 1.0))) return rc;
+    if ((rc = launch_nhc(b, b->p.dt))) return rc;
+    if ((rc = launch_kinet(b))) return rc;
+  } else {
+    // kinet of the fresh velocities folded into the second half kick
+    if ((rc = launch_vv2_kinet(b, 1.0))) return rc;
+  }
+  if (b->mx) b->mx->do_prune = true;  // direct API calls always prune
   return launch_record(b);
 }
 
@@ -301,12 +312,15 @@ int relaunch_kernel(Box *b, int which) {
   return FE_ERR_ARG;
 }
 
-static int capture(Box *b, bool with_list, bool use_nhc, cudaGraphExec_t *out) {
+static int capture(Box *b, bool with_list, bool use_nhc, bool prune, cudaGraphExec_t *out) {
   cudaGraph_t g;
   FE_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   long l0 = g_launches;
-  int rc = step_body(b, with_list, use_nhc);
-  (with_list ? b->launches_list : b->launches_plain) = (int)(g_launches - l0);
+  int rc = step_body(b, with_list, use_nhc, prune);
+  int nl = (int)(g_launches - l0);
+  if (with_list) b->launches_list = nl;
+  else if (prune) b->launches_prune = nl;
+  else b->launches_plain = nl;
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
@@ -365,7 +379,8 @@ int fe_box_set_stream(fe_box *box, void *stream) {
   }
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-  b->g_step = b->g_step_list = nullptr;
+  if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
+  b->g_step = b->g_step_list = b->g_step_prune = nullptr;
   b->g_key = -1;
   return FE_OK;
 }
@@ -659,7 +674,8 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
     // the record kernel's capacity is baked into the graphs: recapture
     if (b->g_step) cudaGraphExecDestroy(b->g_step);
     if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-    b->g_step = b->g_step_list = nullptr;
+    if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
+    b->g_step = b->g_step_list = b->g_step_prune = nullptr;
     b->g_key = -1;
   }
   FE_CUDA(cudaMemsetAsync(b->rec_counter, 0, sizeof(int), b->stream));
@@ -668,13 +684,19 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
   if (b->g_key != key) {
     if (b->g_step) cudaGraphExecDestroy(b->g_step);
     if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-    b->g_step = b->g_step_list = nullptr;
-    if ((rc = capture(b, false, use_nhc != 0, &b->g_step))) return rc;
-    if ((rc = capture(b, true, use_nhc != 0, &b->g_step_list))) return rc;
+    if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
+    b->g_step = b->g_step_list = b->g_step_prune = nullptr;
+    if ((rc = capture(b, false, use_nhc != 0, false, &b->g_step))) return rc;
+    if ((rc = capture(b, true, use_nhc != 0, false, &b->g_step_list))) return rc;
+    if (b->mx && b->mx->use_inner &&
+        (rc = capture(b, false, use_nhc != 0, true, &b->g_step_prune)))
+      return rc;
     b->g_key = key;
   }
   for (long i = first_step; i < first_step + nsteps; i++) {
-    cudaGraphExec_t g = (i % nlist_freq == 0) ? b->g_step_list : b->g_step;
+    cudaGraphExec_t g = b->g_step;
+    if (i % nlist_freq == 0) g = b->g_step_list;
+    else if (b->g_step_prune && i % b->prune_every == 0) g = b->g_step_prune;
     FE_CUDA(cudaGraphLaunch(g, b->stream));
   }
   if (rec)
@@ -719,6 +741,7 @@ int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list) {
   }
   if (plain) *plain = b->launches_plain;
   if (with_list) *with_list = b->launches_list;
+  // a prune step launches exactly one kernel more than a plain step
   return FE_OK;
 }
 
@@ -729,10 +752,18 @@ int fe_list_stats(fe_box *box, int64_t *entries, int *max_row) {
     set_error("no list built yet");
     return FE_ERR_STATE;
   }
-  std::vector<int> c(b->n);
-  const int *src = b->mx ? mixed_counts(b) : b->nl_count;
-  FE_CUDA(cudaMemcpyAsync(c.data(), src, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  std::vector<int> c(b->n), c2(b->n, 0);
+  if (b->mx) {
+    const int *a = nullptr, *r = nullptr;
+    mixed_counts(b, &a, &r);
+    FE_CUDA(cudaMemcpyAsync(c.data(), a, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+    FE_CUDA(cudaMemcpyAsync(c2.data(), r, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  } else {
+    FE_CUDA(cudaMemcpyAsync(c.data(), b->nl_count, sizeof(int) * b->n, cudaMemcpyDeviceToHost,
+                            b->stream));
+  }
   FE_CUDA(cudaStreamSynchronize(b->stream));
+  for (int i = 0; i < b->n; i++) c[i] += c2[i];
   int64_t e = 0;
   int m = 0;
   for (int v : c) {

@@ -41,6 +41,41 @@ __device__ __forceinline__ void block_partials(double (&v)[NT], double *partials
   }
 }
 
+// Like block_partials, then the last block to finish sums every block's
+// partials in a fixed order into out[0..NT) (deterministic, one launch; the
+// threadfence/ticket pattern).  `ticket` is a device counter that is 0 on
+// entry and left 0 on exit.  blockDim.x <= 256.
+template <int NT>
+__device__ __forceinline__ bool block_partials_final(double (&v)[NT], double *partials,
+                                                     unsigned *ticket, double *out) {
+  block_partials<NT>(v, partials);  // thread 0 writes this block's partials
+  __shared__ bool last;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return false;
+  __threadfence();
+  __shared__ double red[256];
+  for (int t = 0; t < NT; t++) {
+    double s = 0.0;
+    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+      s += ((volatile double *)partials)[b * kPartialTerms + t];
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) red[i] = 0.0;
+    __syncthreads();
+    red[threadIdx.x] = s;
+    __syncthreads();
+    for (int w = 128; w > 0; w >>= 1) {
+      if (threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) out[t] = red[0];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+  return true;
+}
+
 // The reference's erfc (ewald.c:817-836): the Chebyshev fit "erfcc" of
 // Numerical Recipes (Press et al., 2nd ed., sec. 6.2), fractional error
 // below 1.2e-7, same evaluation order.  The exponential is CUDA's exp.

@@ -115,6 +115,7 @@ struct Box {
   double *partials = nullptr;  // kMaxPartialBlocks * kPartialTerms
   double *scal = nullptr;      // SC_COUNT
   int *status = nullptr;       // device status word
+  unsigned *ticket = nullptr;  // last-block counter of the fused reductions (0 between kernels)
   double *host_scal = nullptr; // pinned SC_COUNT
 
   // NHC
@@ -127,9 +128,10 @@ struct Box {
   double *rec = nullptr;       // device records
   long rec_cap = 0;
   int *rec_counter = nullptr;
-  cudaGraphExec_t g_step = nullptr, g_step_list = nullptr;
+  cudaGraphExec_t g_step = nullptr, g_step_list = nullptr, g_step_prune = nullptr;
   int g_key = -1;              // graph capture key (use_nhc)
-  int launches_plain = 0, launches_list = 0;  // own kernels per captured step
+  int launches_plain = 0, launches_list = 0, launches_prune = 0;  // own kernels per step
+  int prune_every = 2;         // mixed path: inner-list prune period in fe_run_md
   double *stage = nullptr;     // pinned host staging, 3n doubles
 
   // MC (classic Ewald)
@@ -190,6 +192,7 @@ int launch_vv1(Box *b, double vscal);  // half kick, drift, pbc_all
 int launch_vv2(Box *b, double vscal);  // half kick, uu = vv
 int launch_pbc(Box *b);
 int launch_kinet(Box *b);
+int launch_vv2_kinet(Box *b, double vscal);  // vv2 with the kinetic tensor folded in
 int launch_nhc(Box *b, double time_step);
 int launch_record(Box *b);
 // instrumentation: relaunch one kernel (FE_KERNEL_*) on the current state

@@ -9,20 +9,29 @@ namespace fe {
 struct Box;
 
 struct Mixed {
+  // cell grid (edge >= rlist / 2) used to sort sites and enumerate candidates
   int nc[3] = {1, 1, 1};
   double h[3] = {0, 0, 0};
   int ncells = 1;
   int *cell_count = nullptr, *cell_start = nullptr, *cell_fill = nullptr, *cell_of = nullptr;
-  int *perm = nullptr;    // sorted slot -> original site
-  int *iperm = nullptr;   // original site -> sorted slot
-  int *cell_s = nullptr;  // cell assigned to each sorted slot at the last rebuild
-  int *type_s = nullptr;  // site type per sorted slot
-  float4 *pos32 = nullptr;
-  int cap = 0;            // full-list row capacity
-  int *count = nullptr, *ent = nullptr;
+  int *perm = nullptr;            // sorted slot -> original site
+  int *iperm = nullptr;           // original site -> sorted slot
+  int *cell_s = nullptr;          // cell of each sorted slot at the last rebuild
+  unsigned char *cz_s = nullptr;  // z index of that cell (nc[2] <= 255)
+  int *type_s = nullptr;          // site type per sorted slot
+  int4 *posfx = nullptr;          // sorted x, y, z as 32-bit fractions of L; w = bits of (float)q
+  // outer list (rlist, rebuilt every nlist steps) and inner list (rc + skin,
+  // pruned from it every few steps); rows hold LJ pairs at the front and the
+  // rest at the back, entries are sorted-slot indices
+  int cap = 0;
+  int *cnt_lj = nullptr, *cnt_nl = nullptr, *ent = nullptr;
+  int *icnt_lj = nullptr, *icnt_nl = nullptr, *ient = nullptr;
+  double skin = 0.6;              // inner list radius = rc + skin
+  bool use_inner = false;         // pair kernel reads the inner list (pruning on)
+  bool do_prune = true;           // prune inside the next forces evaluation
   unsigned long long *fix = nullptr;  // 3n fixed-point forces (2^32 per kJ/mol/A)
-  float *shift_tab = nullptr;         // 343 x (hi xyz, lo xyz)
-  float *lj_tab = nullptr;            // nt*nt x (eps, sig^2, shift constant)
+  float *lj_tab = nullptr;        // nt*nt x (eps, sig^2, shift constant)
+  unsigned char *lj_on = nullptr; // nt*nt: pair type has an LJ term
   int nexcl = 0;
   int *excl_ab = nullptr, *excl_flag = nullptr;
   float *eterm32 = nullptr, *kw32 = nullptr;
@@ -37,12 +46,13 @@ struct Mixed {
 
 int mixed_setup(Box *b);
 void mixed_free(Box *b);
-int launch_mixed_list(Box *b);
+int launch_mixed_list(Box *b);      // sort + outer list + inner list
+int launch_mx_prune(Box *b);        // inner list from the outer list
 int forces_mixed(Box *b);
 int launch_mixed_assemble(Box *b);
-int launch_mx_pair_only(Box *b);
-const int *mixed_counts(Box *b);    // device row counts of the full list    // the pair kernel alone (timing)
+int launch_mx_pair_only(Box *b);    // the pair kernel alone (timing)
 int launch_mx_spread_only(Box *b);  // the spreading kernel alone (timing)
+void mixed_counts(Box *b, const int **lj, const int **rest);  // device row counts (outer)
 void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s);
 
 }  // namespace fe

@@ -192,6 +192,47 @@ int launch_vv2(Box *b, double vscal) {
   return FE_OK;
 }
 
+// integrate_vverlet.c:93-102 and kinet.c:31-65 in one pass: second half
+// kick, uu = vv, and the kinetic tensor of the new velocities
+__global__ void k_vv2_kinet(int n, double vscal, double dt_h, const double *__restrict__ mass,
+                            const double *__restrict__ ff, double *__restrict__ vv,
+                            double *__restrict__ uu, double *__restrict__ partials,
+                            unsigned *__restrict__ ticket, double *__restrict__ s) {
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double imass = 100.0 / mass[i];
+    double v[3];
+    for (int c = 0; c < 3; c++) {
+      v[c] = (vv[3 * i + c] + vscal * dt_h * imass * ff[3 * i + c]);
+      vv[3 * i + c] = v[c];
+      uu[3 * i + c] = v[c];
+    }
+    double fac = mass[i];
+    double sx = v[0] + v[0], sy = v[1] + v[1], sz = v[2] + v[2];
+    k[0] += fac * sx * sx;
+    k[1] += fac * sy * sx;
+    k[2] += fac * sy * sy;
+    k[3] += fac * sz * sx;
+    k[4] += fac * sz * sy;
+    k[5] += fac * sz * sz;
+  }
+  if (block_partials_final<6>(k, partials, ticket, s + SC_KEN) && threadIdx.x == 0) {
+    double f = (0.125) * (kNA * kAU * 10.0);  // kinet.c:50-65
+    for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
+    s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
+  }
+}
+
+int launch_vv2_kinet(Box *b, double vscal) {
+  double dt_h = 0.5 * b->p.dt;
+  int blocks = (b->n + 255) / 256;
+  if (blocks > 512) blocks = 512;
+  k_vv2_kinet<<<blocks, 256, 0, b->stream>>>(b->n, vscal, dt_h, b->mass, b->ff, b->vv, b->uu,
+                                             b->partials, b->ticket, b->scal);
+  FE_LAUNCH_CHECK("k_vv2_kinet");
+  return FE_OK;
+}
+
 // kinet.c:31-43 partial sums of the kinetic tensor
 __global__ void k_kinet(int n, const double *__restrict__ mass, const double *__restrict__ vv,
                         const double *__restrict__ uu, double *__restrict__ partials) {

@@ -1,19 +1,22 @@
 // k_mixed.cu -- the mixed-precision force engine: FP32 pair and SPME math,
-// 64-bit fixed-point force sums (exact, so the result does not depend on
-// summation order), FP64 integration and energy reductions.
+// 64-bit fixed-point force sums (exact, so the result does not depend on the
+// order of summation), FP64 integration and energy reductions.
 //
 // Layout (rebuilt with the list, every nlist steps):
 //   * sites are sorted by a cell grid of edge h >= rlist/2; perm[s] is the
-//     original index of sorted slot s, and each slot keeps the cell it was
-//     assigned to until the next rebuild;
-//   * every step, pos32[s] = (x - C_cell) wrapped to the nearest image, in
-//     FP32 (|.| ~ h/2, so FP32 rounding is ~2e-7 A), and q;
-//   * the list is FULL (both directions, no Newton-3 scatter, no atomics on
-//     the j side): row s holds entries (j << 9) | code for every non-excluded
-//     j within rlist, code = the integer image shift o in {-3..3}^3 such
-//     that d = (r_i - r_j) + o * h exactly; o*h is a hi+lo float pair in
-//     shared memory;
-//   * excluded / 1-4 pairs (xint) are handled by a separate kernel over the
+//     original index of sorted slot s;
+//   * every step, posfx[s] = (x, y, z) as unsigned 32-bit fractions of the box
+//     length (x/L + 1/2 scaled by 2^32) and the charge: the difference of two
+//     coordinates taken in 32-bit integer arithmetic wraps around, which IS the
+//     minimum image for |d| < L/2, and converts to FP32 with a relative error
+//     of 2^-24 (~2e-7 A at 3 A) -- no image shifts, no cell-relative frames;
+//   * the OUTER list is full (both directions, no Newton-3 scatter): row s
+//     holds every non-excluded j within rlist, pairs with an LJ term at the
+//     front and the rest at the back.  Optionally (use_inner) it is pruned
+//     every few steps into an INNER list (rc + skin) for the pair kernel; on
+//     this hardware the prune pass costs about what it saves, because both
+//     are bound by the same j-position gathers, so it is off by default;
+//   * excluded / 1-4 pairs (xint) are handled by their own kernel over the
 //     exclusion list (cnonbond_nblist.c:245-263, 416-437 semantics).
 // One warp per i site walks its row with coalesced entry loads; each lane
 // keeps an FP32 partial, converts it to fixed point (2^32 per kJ/mol/A) and
@@ -29,18 +32,30 @@ namespace fe {
 
 constexpr double kFixScale = 4294967296.0;  // 2^32
 constexpr float kFixScaleF = 4294967296.0f;
-constexpr int kMxWarps = 8;                 // warps per block in the pair kernel
+constexpr float kInvTwo32 = 2.3283064365386963e-10f;  // 2^-32
+constexpr int kMxWarps = 8;                 // warps per block (list, prune, pair)
 constexpr int kMxMaxCellAtoms = 2048;       // sites per cell a sort block handles
-constexpr int kCodes = 343;                 // 7^3 image shifts
+constexpr int kBrick = 8;                   // spreading brick edge (grid points)
+constexpr int kSp4Warps = 4;
+constexpr int kSp4MaxSites = 1024;
 
 __device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScaleF); }
 
-__device__ __forceinline__ int shift_code(int ox, int oy, int oz) {
-  return ((ox + 3) * 7 + (oy + 3)) * 7 + (oz + 3);
+// v in [-g, 2g) wrapped into [0, g) without a division
+__device__ __forceinline__ int wrap1(int v, int g) { return v < 0 ? v + g : (v >= g ? v - g : v); }
+
+__device__ __forceinline__ int wrapg32(int v, int g) {
+  v %= g;
+  return v < 0 ? v + g : v;
+}
+
+// minimum-image separation from 32-bit fractional coordinates
+__device__ __forceinline__ float fx_delta(unsigned a, unsigned b, float scale) {
+  return __int2float_rn((int)(a - b)) * scale;
 }
 
 // ---------------------------------------------------------------------------
-// list build
+// sorting by cells
 
 __global__ void k_mx_cell(int n, const double4 *__restrict__ pos, double3 L, double3 h, int3 nc,
                           int *__restrict__ cell_of, int *__restrict__ count) {
@@ -70,6 +85,8 @@ __global__ void k_mx_fill(int n, const int *__restrict__ cell_of, const int *__r
 // order each cell's sites by original index (deterministic layout)
 __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ perm,
                               int *__restrict__ iperm, int *__restrict__ cell_s,
+                              unsigned char *__restrict__ cz_s, int ncz,
+                              const int *__restrict__ type, int *__restrict__ type_s,
                               int *__restrict__ status) {
   __shared__ int buf[kMxMaxCellAtoms];
   int c = blockIdx.x;
@@ -98,31 +115,27 @@ __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ p
       }
       __syncthreads();
     }
+  int cz = c % ncz;
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     int o = buf[i];
     perm[s0 + i] = o;
     iperm[o] = s0 + i;
     cell_s[s0 + i] = c;
+    cz_s[s0 + i] = (unsigned char)cz;
+    type_s[s0 + i] = type[o];
   }
 }
 
-// per step: sorted FP32 cell-relative coordinates and charge
+// per step: sorted fixed-point coordinates and charge
 __global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *__restrict__ perm,
-                             const int *__restrict__ cell_s, double3 L, double3 h, int3 nc,
-                             float4 *__restrict__ pos32) {
+                             double3 invL, int4 *__restrict__ posfx) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  int i = perm[s];
-  int c = cell_s[s];
-  int cz = c % nc.z, cy = (c / nc.z) % nc.y, cx = c / (nc.z * nc.y);
-  double4 p = pos[i];
-  double rx = p.x - ((cx + 0.5) * h.x - 0.5 * L.x);
-  double ry = p.y - ((cy + 0.5) * h.y - 0.5 * L.y);
-  double rz = p.z - ((cz + 0.5) * h.z - 0.5 * L.z);
-  rx -= L.x * rint(rx / L.x);
-  ry -= L.y * rint(ry / L.y);
-  rz -= L.z * rint(rz / L.z);
-  pos32[s] = make_float4((float)rx, (float)ry, (float)rz, (float)p.w);
+  double4 p = pos[perm[s]];
+  unsigned ux = (unsigned)(unsigned long long)llrint((p.x * invL.x + 0.5) * kFixScale);
+  unsigned uy = (unsigned)(unsigned long long)llrint((p.y * invL.y + 0.5) * kFixScale);
+  unsigned uz = (unsigned)(unsigned long long)llrint((p.z * invL.z + 0.5) * kFixScale);
+  posfx[s] = make_int4((int)ux, (int)uy, (int)uz, __float_as_int((float)p.w));
 }
 
 __device__ __forceinline__ int mx_is_excluded(const int *__restrict__ xs, const int *__restrict__ xp,
@@ -132,66 +145,200 @@ __device__ __forceinline__ int mx_is_excluded(const int *__restrict__ xs, const 
   return 0;
 }
 
-// one warp per sorted site: all non-excluded j != i within rlist, in a fixed
-// (cell, slot) order -- no sort needed for a deterministic row
+// ---------------------------------------------------------------------------
+// lists
+
+// Appends the candidates that pass to a row: LJ pairs at the front
+// (ascending), the rest at the back (descending).
+struct RowCursor {
+  int nlj, nnl;
+};
+
+__device__ __forceinline__ void row_push(bool ok, bool lj, int entry, int lane, int cap,
+                                         int *__restrict__ row, RowCursor &rc) {
+  unsigned mlj = __ballot_sync(0xffffffffu, ok && lj);
+  unsigned mnl = __ballot_sync(0xffffffffu, ok && !lj);
+  unsigned lt = (1u << lane) - 1u;
+  if (ok) {
+    if (lj) {
+      int p = rc.nlj + __popc(mlj & lt);
+      if (p + rc.nnl < cap) row[p] = entry;
+    } else {
+      int p = rc.nnl + __popc(mnl & lt);
+      if (p + rc.nlj < cap) row[cap - 1 - p] = entry;
+    }
+  }
+  rc.nlj += __popc(mlj);
+  rc.nnl += __popc(mnl);
+}
+
+__device__ __forceinline__ void row_close(const RowCursor &rc, int cap, int s, int lane,
+                                          int *__restrict__ cnt_lj, int *__restrict__ cnt_nl,
+                                          int *__restrict__ status) {
+  if (lane != 0) return;
+  if (rc.nlj + rc.nnl > cap) {
+    atomicOr(status, ST_LIST_OVERFLOW);
+    int keep = min(rc.nlj, cap);
+    cnt_lj[s] = keep;
+    cnt_nl[s] = cap - keep;
+  } else {
+    cnt_lj[s] = rc.nlj;
+    cnt_nl[s] = rc.nnl;
+  }
+}
+
+// one candidate j of row s: fixed-point distance, exclusion, LJ class
+__device__ __forceinline__ void list_test(int j, int4 pi, int oi, int ti,
+                                          const int4 *__restrict__ posfx,
+                                          const int *__restrict__ perm,
+                                          const int *__restrict__ type_s, float3 sc, float rl2,
+                                          int nt, const unsigned char *__restrict__ lj_on,
+                                          const int *__restrict__ xs, const int *__restrict__ xp,
+                                          bool &ok, bool &lj) {
+  int4 pj = posfx[j];
+  float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, sc.x);
+  float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, sc.y);
+  float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, sc.z);
+  float r2 = dx * dx + dy * dy + dz * dz;
+  if (r2 < rl2 && !mx_is_excluded(xs, xp, oi, perm[j])) {
+    ok = true;
+    lj = lj_on[ti * nt + type_s[j]] != 0;
+  }
+}
+
+// gap along one axis between a site at fraction u and cell c (of nc), in A
+__device__ __forceinline__ float cell_gap(int c, int nc, float u, float L) {
+  float lo = (float)c / nc - u;
+  float g = fmaxf(fmaxf(lo, -(lo + 1.0f / nc)), 0.f) * L - 1e-3f;
+  return fmaxf(g, 0.f);
+}
+
+// Outer list: one warp per sorted site, every non-excluded j != i within
+// rlist.  With at least 5 cells per axis the 5x5x5 neighbourhood is walked as
+// (x, y) columns whose z cells within rlist of the site (box distance) form
+// one or two contiguous sorted ranges; smaller grids visit every cell.  Rows
+// come out in a fixed (column, slot) order: deterministic.
 __global__ void __launch_bounds__(kMxWarps * 32)
-k_mx_list(int n, const float4 *__restrict__ pos32, const int *__restrict__ perm,
-          const int *__restrict__ cell_s, const int *__restrict__ cstart, int3 nc, float3 hf,
-          float3 Lf, float rlist2, const int *__restrict__ xs, const int *__restrict__ xp,
-          int cap, int *__restrict__ count, int *__restrict__ ent, int *__restrict__ status) {
+k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
+          const int *__restrict__ cell_s, const int *__restrict__ type_s,
+          const int *__restrict__ cstart, int3 nc, float3 sc, float3 Lf, float rlist2, int nt,
+          const unsigned char *__restrict__ lj_on, const int *__restrict__ xs,
+          const int *__restrict__ xp, int cap, int *__restrict__ cnt_lj,
+          int *__restrict__ cnt_nl, int *__restrict__ ent, int *__restrict__ status) {
   int lane = threadIdx.x & 31;
-  int nx = nc.x >= 5 ? 5 : nc.x, ny = nc.y >= 5 ? 5 : nc.y, nz = nc.z >= 5 ? 5 : nc.z;
+  bool fast = nc.x >= 5 && nc.y >= 5 && nc.z >= 5;
   for (int s = blockIdx.x * kMxWarps + (threadIdx.x >> 5); s < n; s += gridDim.x * kMxWarps) {
-    float4 ri = pos32[s];
+    int4 pi = posfx[s];
     int c = cell_s[s];
     int cz = c % nc.z, cy = (c / nc.z) % nc.y, cx = c / (nc.z * nc.y);
     int oi = perm[s];
-    int cnt = 0;
+    int ti = type_s[s];
+    RowCursor rc = {0, 0};
     int *row = ent + (size_t)s * cap;
-    for (int ix = 0; ix < nx; ix++) {
-      int x = nc.x >= 5 ? (cx + ix - 2 + nc.x) % nc.x : ix;
-      for (int iy = 0; iy < ny; iy++) {
-        int y = nc.y >= 5 ? (cy + iy - 2 + nc.y) % nc.y : iy;
-        for (int iz = 0; iz < nz; iz++) {
-          int z = nc.z >= 5 ? (cz + iz - 2 + nc.z) % nc.z : iz;
-          int cj = (x * nc.y + y) * nc.z + z;
-          // raw cell offset and the image that brings the cell nearest
-          int dcx = cx - x, dcy = cy - y, dcz = cz - z;
-          int s0 = cstart[cj], s1 = cstart[cj + 1];
-          for (int base = s0; base < s1; base += 32) {
-            int j = base + lane;
-            bool ok = false;
-            int code = 0;
-            if (j < s1 && j != s) {
-              float4 rj = pos32[j];
-              float rx = ri.x - rj.x, ry = ri.y - rj.y, rz = ri.z - rj.z;
-              // d_raw = r_i - r_j + (c_i - c_j) h ; o = (c_i - c_j) - nc * k
-              float ddx = rx + dcx * hf.x, ddy = ry + dcy * hf.y, ddz = rz + dcz * hf.z;
-              int kx = (int)rintf(ddx / Lf.x), ky = (int)rintf(ddy / Lf.y), kz = (int)rintf(ddz / Lf.z);
-              int ox = dcx - kx * nc.x, oy = dcy - ky * nc.y, oz = dcz - kz * nc.z;
-              if (ox >= -3 && ox <= 3 && oy >= -3 && oy <= 3 && oz >= -3 && oz <= 3) {
-                float dx = rx + ox * hf.x, dy = ry + oy * hf.y, dz = rz + oz * hf.z;
-                float r2 = dx * dx + dy * dy + dz * dz;
-                if (r2 < rlist2) {
-                  ok = !mx_is_excluded(xs, xp, oi, perm[j]);
-                  code = shift_code(ox, oy, oz);
-                }
+    if (fast) {
+      float ux = (float)(unsigned)pi.x * kInvTwo32, uy = (float)(unsigned)pi.y * kInvTwo32,
+            uz = (float)(unsigned)pi.z * kInvTwo32;
+      for (int dcx = -2; dcx <= 2; dcx++) {
+        float gx = cell_gap(cx + dcx, nc.x, ux, Lf.x);
+        if (gx * gx >= rlist2) continue;
+        int x = wrap1(cx + dcx, nc.x);
+        for (int dcy = -2; dcy <= 2; dcy++) {
+          float gy = cell_gap(cy + dcy, nc.y, uy, Lf.y);
+          float gxy = gx * gx + gy * gy;
+          if (gxy >= rlist2) continue;
+          int y = wrap1(cy + dcy, nc.y);
+          int zlo = 3, zhi = -3;
+          for (int dcz = -2; dcz <= 2; dcz++) {
+            float gz = cell_gap(cz + dcz, nc.z, uz, Lf.z);
+            if (gxy + gz * gz < rlist2) {
+              zlo = min(zlo, dcz);
+              zhi = max(zhi, dcz);
+            }
+          }
+          if (zhi < zlo) continue;
+          int colbase = (x * nc.y + y) * nc.z;
+          int zs = cz + zlo, ze = cz + zhi;  // inclusive, may leave [0, nc.z)
+          for (int part = 0; part < 2; part++) {
+            int za, zb;
+            if (part == 0) {
+              za = max(zs, 0);
+              zb = min(ze, nc.z - 1);
+            } else {
+              if (zs >= 0 && ze < nc.z) break;
+              if (zs < 0) {
+                za = zs + nc.z;
+                zb = nc.z - 1;
+              } else {
+                za = 0;
+                zb = ze - nc.z;
               }
             }
-            unsigned m = __ballot_sync(0xffffffffu, ok);
-            if (ok) {
-              int p = cnt + __popc(m & ((1u << lane) - 1u));
-              if (p < cap) row[p] = (j << 9) | code;
+            if (za > zb) continue;
+            int j0 = cstart[colbase + za], j1 = cstart[colbase + zb + 1];
+            for (int base = j0; base < j1; base += 32) {
+              int j = base + lane;
+              bool ok = false, lj = false;
+              if (j < j1 && j != s)
+                list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ok,
+                          lj);
+              row_push(ok, lj, j, lane, cap, row, rc);
             }
-            cnt += __popc(m);
           }
         }
       }
+    } else {
+      for (int x = 0; x < nc.x; x++)
+        for (int y = 0; y < nc.y; y++) {
+          int colbase = (x * nc.y + y) * nc.z;
+          int j0 = cstart[colbase], j1 = cstart[colbase + nc.z];
+          for (int base = j0; base < j1; base += 32) {
+            int j = base + lane;
+            bool ok = false, lj = false;
+            if (j < j1 && j != s)
+              list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ok, lj);
+            row_push(ok, lj, j, lane, cap, row, rc);
+          }
+        }
     }
-    if (lane == 0) {
-      count[s] = cnt < cap ? cnt : cap;
-      if (cnt > cap) atomicOr(status, ST_LIST_OVERFLOW);
+    row_close(rc, cap, s, lane, cnt_lj, cnt_nl, status);
+  }
+}
+
+// Inner list: the outer row filtered to r < rc + skin, same segment layout.
+__device__ __forceinline__ void prune_segment(int4 pi, const int4 *__restrict__ posfx,
+                                              const int *__restrict__ src, int b0, int b1,
+                                              bool lj, float3 sc, float rp2, int lane, int cap,
+                                              int *__restrict__ dst, RowCursor &rc) {
+  for (int base = b0; base < b1; base += 32) {
+    int k = base + lane;
+    bool ok = false;
+    int j = 0;
+    if (k < b1) {
+      j = src[k];
+      int4 pj = posfx[j];
+      float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, sc.x);
+      float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, sc.y);
+      float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, sc.z);
+      ok = dx * dx + dy * dy + dz * dz < rp2;
     }
+    row_push(ok, lj, j, lane, cap, dst, rc);
+  }
+}
+
+__global__ void __launch_bounds__(kMxWarps * 32)
+k_mx_prune(int n, const int4 *__restrict__ posfx, float3 sc, float rp2, int cap,
+           const int *__restrict__ cnt_lj, const int *__restrict__ cnt_nl,
+           const int *__restrict__ ent, int *__restrict__ icnt_lj, int *__restrict__ icnt_nl,
+           int *__restrict__ ient, int *__restrict__ status) {
+  int lane = threadIdx.x & 31;
+  for (int s = blockIdx.x * kMxWarps + (threadIdx.x >> 5); s < n; s += gridDim.x * kMxWarps) {
+    int4 pi = posfx[s];
+    const int *src = ent + (size_t)s * cap;
+    int *dst = ient + (size_t)s * cap;
+    RowCursor rc = {0, 0};
+    prune_segment(pi, posfx, src, 0, cnt_lj[s], true, sc, rp2, lane, cap, dst, rc);
+    prune_segment(pi, posfx, src, cap - cnt_nl[s], cap, false, sc, rp2, lane, cap, dst, rc);
+    row_close(rc, cap, s, lane, icnt_lj, icnt_nl, status);
   }
 }
 
@@ -202,12 +349,13 @@ struct MxPair {
   int n, nt, cap;
   float rc2, kappa, c2k, qfe;  // c2k = 2 kappa / sqrt(pi); qfe = QFACTOR / epsRF
   float ron2, sw_den;
+  float3 sc;                   // L / 2^32 per axis
 };
 
 // the reference's erfc (ewald.c:817-836, Numerical Recipes "erfcc") in FP32;
 // ex = exp(-z^2) is shared with the force term
 __device__ __forceinline__ float erfc_nr_f(float z, float ex) {
-  float t = __frcp_rn(1.0f + 0.5f * z);
+  float t = __fdividef(1.0f, 1.0f + 0.5f * z);
   float p = fmaf(t, 0.17087277f, -0.82215223f);
   p = fmaf(t, p, 1.48851587f);
   p = fmaf(t, p, -1.13520398f);
@@ -220,73 +368,105 @@ __device__ __forceinline__ float erfc_nr_f(float z, float ex) {
   return t * ex * __expf(p);
 }
 
-__global__ void __launch_bounds__(kMxWarps * 32)
-k_mx_pair(MxPair P, const float4 *__restrict__ pos32, const int *__restrict__ type_s,
-          const int *__restrict__ perm, const int *__restrict__ count, const int *__restrict__ ent,
-          const float *__restrict__ shift_tab, const float *__restrict__ lj_tab,
-          unsigned long long *__restrict__ fix, double *__restrict__ partials) {
-  extern __shared__ float sh[];
-  float *s_shift = sh;                 // kCodes * 6: hi xyz, lo xyz
-  float *s_lj = sh + kCodes * 6;       // nt*nt*3: eps, sig^2, shift const
-  for (int i = threadIdx.x; i < kCodes * 6; i += blockDim.x) s_shift[i] = shift_tab[i];
+struct PairAcc {
+  float fx, fy, fz, e_lj, e_ljs, e_real, qsum;
+};
+
+// one list entry j of row i: Ewald real space always, LJ when WITH_LJ
+template <bool WITH_LJ>
+__device__ __forceinline__ void mx_pair_one(const MxPair &P, int4 pi, float qi, int j, int4 pj,
+                                            const float *__restrict__ ljrow,
+                                            const int *__restrict__ type_s, PairAcc &a) {
+  float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, P.sc.x);
+  float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, P.sc.y);
+  float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, P.sc.z);
+  float r2 = dx * dx + dy * dy + dz * dz;
+  if (r2 > P.rc2) return;
+  float rinv = rsqrtf(r2);
+  float r = r2 * rinv;
+  float rinv2 = rinv * rinv;
+  float qq = qi * __int_as_float(pj.w);
+  float kr = P.kappa * r;
+  float ex = __expf(-kr * kr);
+  float erfckr = erfc_nr_f(kr, ex);
+  float F = qq * rinv * rinv2 * fmaf(P.c2k * r, ex, erfckr);
+  a.e_real = fmaf(qq * erfckr, rinv, a.e_real);
+  a.qsum += qq;
+  if (WITH_LJ) {
+    const float *lj = ljrow + type_s[j] * 3;
+    float eps = lj[0];
+    float sr2 = lj[1] * rinv2;
+    float sr6 = sr2 * sr2 * sr2;
+    float sr12 = sr6 * sr6;
+    float flj = 12.f * eps * rinv2 * (sr12 - sr6);
+    float elj = eps * (sr12 - 2.f * sr6);
+    if (P.ron2 > 0.f) {
+      if (r2 > P.ron2) {
+        float c = P.rc2 - r2;
+        float sw = c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) / P.sw_den;
+        float dsw = 12.f * c * (r2 - P.ron2) / P.sw_den;
+        flj = flj * sw + elj * dsw;
+        elj = elj * sw;
+      }
+    } else {
+      a.e_ljs = fmaf(eps, lj[2], a.e_ljs);
+    }
+    F += flj;
+    a.e_lj += elj;
+  }
+  a.fx = fmaf(F, dx, a.fx);
+  a.fy = fmaf(F, dy, a.fy);
+  a.fz = fmaf(F, dz, a.fz);
+}
+
+// Walks entries b0 + lane, b0 + lane + 32, ... of a row with a two-deep
+// software pipeline: the entry two iterations ahead and the j position one
+// iteration ahead are in flight while the current pair is computed.
+template <bool WITH_LJ>
+__device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
+                                           const int *__restrict__ row, int b0, int b1, int lane,
+                                           const int4 *__restrict__ posfx,
+                                           const float *__restrict__ ljrow,
+                                           const int *__restrict__ type_s, PairAcc &a) {
+  int i = b0 + lane;
+  if (i >= b1) return;
+  int e_cur = row[i];
+  int e_nxt = i + 32 < b1 ? row[i + 32] : -1;
+  int4 p_cur = posfx[e_cur];
+  while (true) {
+    int e_nn = (e_nxt >= 0 && i + 64 < b1) ? row[i + 64] : -1;
+    int4 p_nxt = make_int4(0, 0, 0, 0);
+    if (e_nxt >= 0) p_nxt = posfx[e_nxt];
+    mx_pair_one<WITH_LJ>(P, pi, qi, e_cur, p_cur, ljrow, type_s, a);
+    if (e_nxt < 0) break;
+    e_cur = e_nxt;
+    p_cur = p_nxt;
+    e_nxt = e_nn;
+    i += 32;
+  }
+}
+
+__global__ void __launch_bounds__(kMxWarps * 32, 6)
+k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
+          const int *__restrict__ perm, const int *__restrict__ cnt_lj,
+          const int *__restrict__ cnt_nl, const int *__restrict__ ent,
+          const float *__restrict__ lj_tab, unsigned long long *__restrict__ fix,
+          double *__restrict__ partials, unsigned *__restrict__ ticket, double *__restrict__ out) {
+  extern __shared__ float s_lj[];  // nt*nt*3: eps, sig^2, shift constant
   for (int i = threadIdx.x; i < P.nt * P.nt * 3; i += blockDim.x) s_lj[i] = lj_tab[i];
   __syncthreads();
   int lane = threadIdx.x & 31;
-  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f;
+  PairAcc a;
+  a.e_lj = a.e_ljs = a.e_real = a.qsum = 0.f;
   for (int s = blockIdx.x * kMxWarps + (threadIdx.x >> 5); s < P.n; s += gridDim.x * kMxWarps) {
-    float4 ri = pos32[s];
-    int ti = type_s[s];
-    int cnt = count[s];
+    int4 pi = posfx[s];
+    float qi = __int_as_float(pi.w) * P.qfe;
+    const float *ljrow = s_lj + type_s[s] * P.nt * 3;
     const int *row = ent + (size_t)s * P.cap;
-    float fx = 0.f, fy = 0.f, fz = 0.f;
-    for (int bb = lane; bb < cnt; bb += 32) {
-      int e = row[bb];
-      int j = e >> 9;
-      const float *o = s_shift + (e & 511) * 6;
-      float4 rj = pos32[j];
-      float dx = ((ri.x - rj.x) + o[0]) + o[3];
-      float dy = ((ri.y - rj.y) + o[1]) + o[4];
-      float dz = ((ri.z - rj.z) + o[2]) + o[5];
-      float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 > P.rc2) continue;
-      float rinv = rsqrtf(r2);
-      float r = r2 * rinv;
-      float rinv2 = rinv * rinv;
-      float qq = ri.w * rj.w * P.qfe;
-      float kr = P.kappa * r;
-      float ex = __expf(-kr * kr);
-      float erfckr = erfc_nr_f(kr, ex);
-      float F = qq * rinv * rinv2 * (erfckr + P.c2k * r * ex);
-      e_real += qq * erfckr * rinv;
-      qsum += qq;
-      int tj = type_s[j];
-      const float *lj = s_lj + (ti * P.nt + tj) * 3;
-      float eps = lj[0];
-      if (eps != 0.f) {
-        float sr2 = lj[1] * rinv2;
-        float sr6 = sr2 * sr2 * sr2;
-        float sr12 = sr6 * sr6;
-        float flj = 12.f * eps * rinv2 * (sr12 - sr6);
-        float elj = eps * (sr12 - 2.f * sr6);
-        if (P.ron2 > 0.f) {
-          if (r2 > P.ron2) {
-            float c = P.rc2 - r2;
-            float sw = c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) / P.sw_den;
-            float dsw = 12.f * c * (r2 - P.ron2) / P.sw_den;
-            flj = flj * sw + elj * dsw;
-            elj = elj * sw;
-          }
-        } else {
-          e_ljs += eps * lj[2];
-        }
-        F += flj;
-        e_lj += elj;
-      }
-      fx += F * dx;
-      fy += F * dy;
-      fz += F * dz;
-    }
-    long long ix = to_fix(fx), iy = to_fix(fy), iz = to_fix(fz);
+    a.fx = a.fy = a.fz = 0.f;
+    mx_segment<true>(P, pi, qi, row, 0, cnt_lj[s], lane, posfx, ljrow, type_s, a);
+    mx_segment<false>(P, pi, qi, row, P.cap - cnt_nl[s], P.cap, lane, posfx, ljrow, type_s, a);
+    long long ix = to_fix(a.fx), iy = to_fix(a.fy), iz = to_fix(a.fz);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       ix += __shfl_xor_sync(0xffffffffu, ix, o);
@@ -301,8 +481,9 @@ k_mx_pair(MxPair P, const float4 *__restrict__ pos32, const int *__restrict__ ty
     }
   }
   // every pair was visited from both ends
-  double v[4] = {0.5 * (double)e_lj, 0.5 * (double)e_ljs, 0.5 * (double)e_real, 0.5 * (double)qsum};
-  block_partials<4>(v, partials);
+  double v[4] = {0.5 * (double)a.e_lj, 0.5 * (double)a.e_ljs, 0.5 * (double)a.e_real,
+                 0.5 * (double)a.qsum};
+  block_partials_final<4>(v, partials, ticket, out);
 }
 
 // excluded and 1-4 pairs (xint), cnonbond_nblist.c:245-263 and 416-437:
@@ -313,7 +494,8 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
                           const double4 *__restrict__ pos, const int *__restrict__ type, double3 L,
                           int nt, const float *__restrict__ lj_tab, float rc2, float kappa,
                           float c2k, float qf, float epsRF, unsigned long long *__restrict__ fix,
-                          double *__restrict__ partials) {
+                          double *__restrict__ partials, unsigned *__restrict__ ticket,
+                          double *__restrict__ out) {
   float e_intra = 0.f, e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nexcl; t += gridDim.x * blockDim.x) {
     int a = ab[2 * t], b = ab[2 * t + 1], xf = flag[t];
@@ -359,7 +541,7 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
     atomicAdd(&fix[3 * b + 2], (unsigned long long)(-fzq));
   }
   double v[5] = {(double)e_lj, (double)e_ljs, (double)e_real, (double)qsum, (double)e_intra};
-  block_partials<5>(v, partials);
+  block_partials_final<5>(v, partials, ticket, out);
 }
 
 // bonded terms in FP32 from FP64 differences (cbond.c, cbend.c)
@@ -367,7 +549,8 @@ __global__ void k_mx_bonded(int nbond, int nbend, double3 L, const double4 *__re
                             const int *__restrict__ bond_ab, const double *__restrict__ bond_req,
                             const double *__restrict__ bond_k, const int *__restrict__ bend_abc,
                             const double *__restrict__ bend_t0, const double *__restrict__ bend_k,
-                            unsigned long long *__restrict__ fix, double *__restrict__ partials) {
+                            unsigned long long *__restrict__ fix, double *__restrict__ partials,
+                            unsigned *__restrict__ ticket, double *__restrict__ out) {
   float eb = 0.f, ea = 0.f;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nbond + nbend;
        t += gridDim.x * blockDim.x) {
@@ -435,16 +618,11 @@ __global__ void k_mx_bonded(int nbond, int nbend, double3 L, const double4 *__re
     }
   }
   double v[2] = {(double)eb, (double)ea};
-  block_partials<2>(v, partials);
+  block_partials_final<2>(v, partials, ticket, out);
 }
 
 // ---------------------------------------------------------------------------
 // SPME in FP32
-
-__device__ __forceinline__ int wrapg32(int v, int g) {
-  v %= g;
-  return v < 0 ? v + g : v;
-}
 
 // B-spline weights of order p at fraction w (same recursion as
 // pme_spline.c:10-49), FP32
@@ -519,40 +697,107 @@ __global__ void k_mx_binsort(long K, int gcap, int *__restrict__ bcount, int *__
   }
 }
 
-// atom-free gather spreading, one thread per grid point (x, y, z)
-__global__ void k_mx_spread(int order, int3 G, const float4 *__restrict__ pos32,
-                            const float *__restrict__ sm, int gcap, const int *__restrict__ bcount,
-                            const int *__restrict__ batoms, float *__restrict__ grid) {
-  long K = (long)G.x * G.y * G.z;
-  long id = (long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (id >= K) return;
-  int z = (int)(id % G.z);
-  int y = (int)((id / G.z) % G.y);
-  int x = (int)(id / ((long)G.z * G.y));
-  float sum = 0.f;
-  for (int xi = 1; xi <= order; xi++) {
-    int fx = wrapg32(x + order - xi, G.x);
-    for (int yi = 1; yi <= order; yi++) {
-      int fy = wrapg32(y + order - yi, G.y);
-      long cb = ((long)fx * G.y + fy) * G.z;
-      for (int zi = 1; zi <= order; zi++) {
-        int fz = wrapg32(z + order - zi, G.z);
-        long c = cb + fz;
-        int m = bcount[c];
-        const int *at = batoms + c * gcap;
-        for (int k = 0; k < m; k++) {
-          int j = at[k];
-          const float *w = sm + (size_t)j * order * 3;
-          sum += w[(xi - 1) * 3] * w[(yi - 1) * 3 + 1] * w[(zi - 1) * 3 + 2] * pos32[j].w;
+// Spreading by brick-owned accumulation.  A block owns an 8x8x8 brick of
+// grid points held in shared memory and 4 warps; warp w owns the z-slab
+// [2w, 2w + 2).  The block gathers the ids of every site whose spline can
+// reach the brick (bins of floor cells [X0, X0 + 8 + order - 1) per axis, in
+// a fixed cell order) into shared memory; then each warp walks that list in
+// order and, for each site touching its slab, lane (ix, iy, iz) adds
+// theta_x[ix] theta_y[iy] theta_z[.] q to one distinct point.  Every point is
+// written by one warp in site order: deterministic, no atomics.
+__global__ void __launch_bounds__(kSp4Warps * 32)
+k_mx_spread4(int order, int3 G, const int4 *__restrict__ posfx, const float *__restrict__ sm,
+             int gcap, const int *__restrict__ bcount, const int *__restrict__ batoms,
+             float *__restrict__ grid, int *__restrict__ status) {
+  __shared__ float acc[kBrick * kBrick * kBrick];
+  __shared__ int site[kSp4MaxSites];
+  __shared__ int sfloor[kSp4MaxSites];  // local floor cell, 8 bits per axis
+  __shared__ int part[kSp4Warps * 32 + 1];
+  int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  int H = kBrick + order - 1;
+  int nbx = (G.x + kBrick - 1) / kBrick, nby = (G.y + kBrick - 1) / kBrick;
+  int bz = blockIdx.x / (nbx * nby), by = (blockIdx.x / nbx) % nby, bx = blockIdx.x % nbx;
+  int X0 = bx * kBrick, Y0 = by * kBrick, Z0 = bz * kBrick;
+  for (int i = tid; i < kBrick * kBrick * kBrick; i += blockDim.x) acc[i] = 0.f;
+  // halo columns (lx, ly): thread t takes columns t, t + T, ...; each column
+  // is H bins along z.  A block scan of the per-thread counts keeps the fixed
+  // (column, z, slot) order.
+  int T = blockDim.x;
+  int ncol = H * H;
+  int mine = 0;
+  for (int col = tid; col < ncol; col += T) {
+    int lx = col / H, ly = col - lx * H;
+    long base = ((long)wrap1(X0 + lx, G.x) * G.y + wrap1(Y0 + ly, G.y)) * G.z;
+    for (int lz = 0; lz < H; lz++) mine += bcount[base + wrap1(Z0 + lz, G.z)];
+  }
+  part[tid] = mine;
+  __syncthreads();
+  if (tid == 0) {
+    int a = 0;
+    for (int k = 0; k < T; k++) {
+      int v = part[k];
+      part[k] = a;
+      a += v;
+    }
+    part[T] = a;
+  }
+  __syncthreads();
+  int ns = part[T];
+  if (ns > kSp4MaxSites) {
+    if (tid == 0) atomicOr(status, ST_GRID_OVERFLOW);
+    ns = kSp4MaxSites;
+  }
+  int w = part[tid];
+  for (int col = tid; col < ncol; col += T) {
+    int lx = col / H, ly = col - lx * H;
+    long base = ((long)wrap1(X0 + lx, G.x) * G.y + wrap1(Y0 + ly, G.y)) * G.z;
+    for (int lz = 0; lz < H; lz++) {
+      long gc = base + wrap1(Z0 + lz, G.z);
+      int m = bcount[gc];
+      for (int k = 0; k < m; k++, w++)
+        if (w < kSp4MaxSites) {
+          site[w] = batoms[gc * gcap + k];
+          sfloor[w] = (lx << 16) | (ly << 8) | lz;
         }
-      }
     }
   }
-  grid[id] = sum;
+  __syncthreads();
+  int ix = lane & 3, iy = (lane >> 2) & 3, iz = lane >> 4;  // 4 x 4 x 2 lane layout
+  int zlo = wid * 2;                                         // slab [zlo, zlo + 2)
+  for (int a = 0; a < ns; a++) {
+    int lf = sfloor[a];
+    int lfz = lf & 255;
+    // stencil z range [lfz - order + 1, lfz] vs this slab
+    if (lfz - order + 1 > zlo + 1 || lfz < zlo) continue;
+    int lfx = lf >> 16, lfy = (lf >> 8) & 255;
+    int j = site[a];
+    const float *wj = sm + (size_t)j * order * 3;
+    float q = __int_as_float(posfx[j].w);
+    int pz = zlo + iz;
+    int zi = pz - (lfz - order + 1);  // 0-based spline index along z
+    bool zin = zi >= 0 && zi < order;
+    float wz = zin ? wj[zi * 3 + 2] * q : 0.f;
+    for (int ox = 0; ox < order; ox += 4) {
+      for (int oy = 0; oy < order; oy += 4) {
+        int px = lfx - order + 1 + ox + ix, py = lfy - order + 1 + oy + iy;
+        bool in = zin && (ox + ix < order) && (oy + iy < order) && px >= 0 && px < kBrick &&
+                  py >= 0 && py < kBrick;
+        if (in) acc[(px * kBrick + py) * kBrick + pz] += wj[(ox + ix) * 3] * wj[(oy + iy) * 3 + 1] * wz;
+      }
+    }
+    __syncwarp();  // order this site's adds before the next site's
+  }
+  __syncthreads();
+  for (int i = tid; i < kBrick * kBrick * kBrick; i += blockDim.x) {
+    int pz = i & (kBrick - 1), py = (i >> 3) & (kBrick - 1), px = i >> 6;
+    int x = X0 + px, y = Y0 + py, z = Z0 + pz;
+    if (x < G.x && y < G.y && z < G.z) grid[((long)x * G.y + y) * G.z + z] = acc[i];
+  }
 }
 
 __global__ void k_mx_recip(long Kh, const float *__restrict__ eterm, const float *__restrict__ kw,
-                           cufftComplex *__restrict__ gk, double *__restrict__ partials) {
+                           cufftComplex *__restrict__ gk, double *__restrict__ partials,
+                           unsigned *__restrict__ ticket, double *__restrict__ out) {
   double e = 0.0;
   for (long h = (long)blockIdx.x * blockDim.x + threadIdx.x; h < Kh;
        h += (long)gridDim.x * blockDim.x) {
@@ -564,14 +809,15 @@ __global__ void k_mx_recip(long Kh, const float *__restrict__ eterm, const float
     gk[h] = v;
   }
   double vv[1] = {e};
-  block_partials<1>(vv, partials);
+  block_partials_final<1>(vv, partials, ticket, out);
 }
 
 __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
-                            const float4 *__restrict__ pos32, const int *__restrict__ perm,
+                            const int4 *__restrict__ posfx, const int *__restrict__ perm,
                             const int *__restrict__ floor3, const float *__restrict__ sm,
                             const float *__restrict__ sd, const float *__restrict__ grid,
-                            unsigned long long *__restrict__ fix, double *__restrict__ partials) {
+                            unsigned long long *__restrict__ fix, double *__restrict__ partials,
+                            unsigned *__restrict__ ticket, double *__restrict__ out) {
   double sx = 0.0, sy = 0.0, sz = 0.0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     float fxi = 0.f, fyi = 0.f, fzi = 0.f;
@@ -579,14 +825,14 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
     const float *dm = sd + (size_t)s * order * 3;
     int xo = floor3[3 * s] - order, yo0 = floor3[3 * s + 1] - order, zo0 = floor3[3 * s + 2] - order;
     for (int xi = 1; xi <= order; xi++) {
-      int x = wrapg32(xo + xi, G.x);
+      int x = wrap1(xo + xi, G.x);
       float mx = m[(xi - 1) * 3], dmx = dm[(xi - 1) * 3];
       for (int yi = 1; yi <= order; yi++) {
-        int y = wrapg32(yo0 + yi, G.y);
+        int y = wrap1(yo0 + yi, G.y);
         float my = m[(yi - 1) * 3 + 1], dmy = dm[(yi - 1) * 3 + 1];
         const float *row = grid + ((long)x * G.y + y) * G.z;
         for (int zi = 1; zi <= order; zi++) {
-          int z = wrapg32(zo0 + zi, G.z);
+          int z = wrap1(zo0 + zi, G.z);
           float mz = m[(zi - 1) * 3 + 2], dmz = dm[(zi - 1) * 3 + 2];
           float term = row[z];
           fxi -= dmx * my * mz * term;
@@ -595,20 +841,21 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
         }
       }
     }
-    float fac = pos32[s].w * qfe;
+    float fac = __int_as_float(posfx[s].w) * qfe;
     fxi *= fac * gl.x;
     fyi *= fac * gl.y;
     fzi *= fac * gl.z;
     int oi = perm[s];
-    atomicAdd(&fix[3 * oi], (unsigned long long)to_fix(fxi));
-    atomicAdd(&fix[3 * oi + 1], (unsigned long long)to_fix(fyi));
-    atomicAdd(&fix[3 * oi + 2], (unsigned long long)to_fix(fzi));
-    sx += (double)to_fix(fxi);
-    sy += (double)to_fix(fyi);
-    sz += (double)to_fix(fzi);
+    long long qx = to_fix(fxi), qy = to_fix(fyi), qz = to_fix(fzi);
+    atomicAdd(&fix[3 * oi], (unsigned long long)qx);
+    atomicAdd(&fix[3 * oi + 1], (unsigned long long)qy);
+    atomicAdd(&fix[3 * oi + 2], (unsigned long long)qz);
+    sx += (double)qx;
+    sy += (double)qy;
+    sz += (double)qz;
   }
   double v[3] = {sx, sy, sz};
-  block_partials<3>(v, partials);
+  block_partials_final<3>(v, partials, ticket, out);
 }
 
 // FP64 forces from the fixed-point sums, minus the mean reciprocal force
@@ -620,7 +867,18 @@ __global__ void k_mx_finalize(int n, const unsigned long long *__restrict__ fix,
   ff[i] = (double)(long long)fix[i] / kFixScale - mean;
 }
 
+// combine the mixed kernels' sums into the reference's slots
+__global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc) {
+  if (threadIdx.x != 0) return;
+  s[SC_LJ] = s[SC_MX_PAIR + 0] + s[SC_MX_EXCL + 0];
+  s[SC_LJS] = s[SC_MX_PAIR + 1] + s[SC_MX_EXCL + 1];
+  s[SC_REAL] = s[SC_MX_PAIR + 2] + s[SC_MX_EXCL + 2];
+  s[SC_REALS] = (s[SC_MX_PAIR + 3] + s[SC_MX_EXCL + 3]) * erfc_rc_over_rc;
+  s[SC_INTRA] = s[SC_MX_EXCL + 4];
+}
+
 // ---------------------------------------------------------------------------
+// host side
 
 int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
@@ -634,10 +892,17 @@ int mixed_setup(Box *b) {
     M.h[d] = b->p.L[d] / M.nc[d];
     M.ncells *= M.nc[d];
   }
-  if (n >= (1 << 22)) {
-    set_error("mixed precision supports at most 4,194,303 sites per box");
+  if (M.nc[2] > 255) {
+    set_error("mixed precision supports at most 255 list cells per axis");
     return FE_ERR_SIZE;
   }
+  // the minimum image from wrapped 32-bit fractions needs |d| < L/2
+  double rl = b->p.rclist;
+  for (int d = 0; d < 3; d++)
+    if (rl >= 0.5 * b->p.L[d]) {
+      set_error("mixed precision needs rclist < L/2 in every direction");
+      return FE_ERR_ARG;
+    }
   FE_CUDA(cudaMalloc(&M.cell_count, sizeof(int) * M.ncells));
   FE_CUDA(cudaMalloc(&M.cell_start, sizeof(int) * (M.ncells + 1)));
   FE_CUDA(cudaMalloc(&M.cell_fill, sizeof(int) * M.ncells));
@@ -645,35 +910,24 @@ int mixed_setup(Box *b) {
   FE_CUDA(cudaMalloc(&M.perm, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.iperm, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.cell_s, sizeof(int) * n));
+  FE_CUDA(cudaMalloc(&M.cz_s, n));
   FE_CUDA(cudaMalloc(&M.type_s, sizeof(int) * n));
-  FE_CUDA(cudaMalloc(&M.pos32, sizeof(float4) * n));
+  FE_CUDA(cudaMalloc(&M.posfx, sizeof(int4) * n));
   // full-list row capacity: a sphere of rlist at the box's density, with margin
   double vol = b->p.L[0] * b->p.L[1] * b->p.L[2];
-  double rl = b->p.rclist;
   double expect = 4.0 / 3.0 * kPI * rl * rl * rl * (double)n / vol;
   int cap = (int)(1.6 * expect + 64.0);
   if (b->p.max_neighbors > 0) cap = b->p.max_neighbors;
   cap = (cap + 31) / 32 * 32;
   if (cap > n) cap = (n + 31) / 32 * 32;
   M.cap = cap;
-  FE_CUDA(cudaMalloc(&M.count, sizeof(int) * n));
+  FE_CUDA(cudaMalloc(&M.cnt_lj, sizeof(int) * n));
+  FE_CUDA(cudaMalloc(&M.cnt_nl, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.ent, sizeof(int) * (size_t)n * cap));
+  FE_CUDA(cudaMalloc(&M.icnt_lj, sizeof(int) * n));
+  FE_CUDA(cudaMalloc(&M.icnt_nl, sizeof(int) * n));
+  FE_CUDA(cudaMalloc(&M.ient, sizeof(int) * (size_t)n * cap));
   FE_CUDA(cudaMalloc(&M.fix, sizeof(unsigned long long) * 3 * n));
-  // image-shift table: o * h as a hi + lo float pair per component
-  std::vector<float> tab(kCodes * 6);
-  for (int ox = -3; ox <= 3; ox++)
-    for (int oy = -3; oy <= 3; oy++)
-      for (int oz = -3; oz <= 3; oz++) {
-        int c = ((ox + 3) * 7 + (oy + 3)) * 7 + (oz + 3);
-        double v[3] = {ox * M.h[0], oy * M.h[1], oz * M.h[2]};
-        for (int d = 0; d < 3; d++) {
-          float hi = (float)v[d];
-          tab[c * 6 + d] = hi;
-          tab[c * 6 + 3 + d] = (float)(v[d] - (double)hi);
-        }
-      }
-  FE_CUDA(cudaMalloc(&M.shift_tab, sizeof(float) * tab.size()));
-  FE_CUDA(cudaMemcpy(M.shift_tab, tab.data(), sizeof(float) * tab.size(), cudaMemcpyHostToDevice));
   // LJ table: eps, sig^2, and the energy shift constant (sr12s - 2 sr6s)
   int nt = b->nt;
   std::vector<double> eps(nt * nt), sig(nt * nt);
@@ -691,6 +945,10 @@ int mixed_setup(Box *b) {
   }
   FE_CUDA(cudaMalloc(&M.lj_tab, sizeof(float) * lj.size()));
   FE_CUDA(cudaMemcpy(M.lj_tab, lj.data(), sizeof(float) * lj.size(), cudaMemcpyHostToDevice));
+  std::vector<unsigned char> on(nt * nt);
+  for (int k = 0; k < nt * nt; k++) on[k] = lj[3 * k] != 0.f ? 1 : 0;
+  FE_CUDA(cudaMalloc(&M.lj_on, on.size()));
+  FE_CUDA(cudaMemcpy(M.lj_on, on.data(), on.size(), cudaMemcpyHostToDevice));
   // exclusion pair list (xint), for the correction kernel
   M.nexcl = b->p.nexcl;
   FE_CUDA(cudaMalloc(&M.excl_ab, sizeof(int) * 2 * (M.nexcl ? M.nexcl : 1)));
@@ -730,8 +988,9 @@ void mixed_free(Box *b) {
   if (!b->mx) return;
   Mixed &M = *b->mx;
   void *ptrs[] = {M.cell_count, M.cell_start, M.cell_fill, M.cell_of, M.perm, M.iperm, M.cell_s,
-                  M.type_s, M.pos32, M.count, M.ent, M.fix, M.shift_tab, M.lj_tab, M.excl_ab,
-                  M.excl_flag, M.eterm32, M.kw32, M.grid32, M.grid32k, M.floor3, M.sm, M.sd};
+                  M.cz_s, M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
+                  M.ient, M.fix, M.lj_tab, M.lj_on, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
+                  M.grid32, M.grid32k, M.floor3, M.sm, M.sd};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (M.plans) {
@@ -742,20 +1001,36 @@ void mixed_free(Box *b) {
   b->mx = nullptr;
 }
 
-__global__ void k_mx_types(int n, const int *__restrict__ perm, const int *__restrict__ type,
-                           int *__restrict__ type_s) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s < n) type_s[s] = type[perm[s]];
+void mixed_counts(Box *b, const int **lj, const int **rest) {
+  *lj = b->mx->cnt_lj;
+  *rest = b->mx->cnt_nl;
+}
+
+static float3 fix_scale(Box *b) {
+  return make_float3((float)(b->p.L[0] / kFixScale), (float)(b->p.L[1] / kFixScale),
+                     (float)(b->p.L[2] / kFixScale));
 }
 
 static int launch_convert(Box *b) {
   Mixed &M = *b->mx;
-  double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
-  double3 h = make_double3(M.h[0], M.h[1], M.h[2]);
-  int3 nc = make_int3(M.nc[0], M.nc[1], M.nc[2]);
-  k_mx_convert<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->pos_q, M.perm, M.cell_s, L, h, nc,
-                                                          M.pos32);
+  double3 invL = make_double3(1.0 / b->p.L[0], 1.0 / b->p.L[1], 1.0 / b->p.L[2]);
+  k_mx_convert<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->pos_q, M.perm, invL, M.posfx);
   FE_LAUNCH_CHECK("k_mx_convert");
+  return FE_OK;
+}
+
+static int list_blocks(Box *b) {
+  int blocks = (b->n + kMxWarps - 1) / kMxWarps;
+  return blocks > 152 * 8 ? 152 * 8 : blocks;
+}
+
+int launch_mx_prune(Box *b) {
+  Mixed &M = *b->mx;
+  float rp = (float)(b->p.rc + M.skin);
+  k_mx_prune<<<list_blocks(b), kMxWarps * 32, 0, b->stream>>>(
+      b->n, M.posfx, fix_scale(b), rp * rp, M.cap, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj,
+      M.icnt_nl, M.ient, b->status);
+  FE_LAUNCH_CHECK("k_mx_prune");
   return FE_OK;
 }
 
@@ -771,26 +1046,21 @@ int launch_mixed_list(Box *b) {
   k_cell_scan_ext(M.cell_count, M.ncells, M.cell_start, M.cell_fill, b->stream);
   k_mx_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.cell_of, M.cell_start, M.cell_fill, M.perm);
   FE_LAUNCH_CHECK("k_mx_fill");
-  k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s, b->status);
+  k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s, M.cz_s,
+                                                 M.nc[2], b->type, M.type_s, b->status);
   FE_LAUNCH_CHECK("k_mx_cellsort");
-  k_mx_types<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.perm, b->type, M.type_s);
-  FE_LAUNCH_CHECK("k_mx_types");
   int rc = launch_convert(b);
   if (rc) return rc;
-  float3 hf = make_float3((float)M.h[0], (float)M.h[1], (float)M.h[2]);
   float3 Lf = make_float3((float)b->p.L[0], (float)b->p.L[1], (float)b->p.L[2]);
   float rl = (float)(b->p.rclist < b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
-  int blocks = (n + kMxWarps - 1) / kMxWarps;
-  if (blocks > 152 * 8) blocks = 152 * 8;
-  k_mx_list<<<blocks, kMxWarps * 32, 0, b->stream>>>(n, M.pos32, M.perm, M.cell_s, M.cell_start, nc,
-                                                     hf, Lf, rl * rl, b->x_start, b->x_partner,
-                                                     M.cap, M.count, M.ent, b->status);
+  k_mx_list<<<list_blocks(b), kMxWarps * 32, 0, b->stream>>>(
+      n, M.posfx, M.perm, M.cell_s, M.type_s, M.cell_start, nc, fix_scale(b), Lf, rl * rl, b->nt,
+      M.lj_on, b->x_start, b->x_partner, M.cap, M.cnt_lj, M.cnt_nl, M.ent, b->status);
   FE_LAUNCH_CHECK("k_mx_list");
   b->have_list = true;
+  M.do_prune = true;
   return FE_OK;
 }
-
-const int *mixed_counts(Box *b) { return b->mx->count; }
 
 static int pair_blocks(Box *b) {
   int blocks = (b->n + kMxWarps - 1) / kMxWarps;
@@ -799,9 +1069,8 @@ static int pair_blocks(Box *b) {
 
 int launch_mx_pair_only(Box *b) {
   Mixed &M = *b->mx;
-  int n = b->n;
   MxPair P;
-  P.n = n;
+  P.n = b->n;
   P.nt = b->nt;
   P.cap = M.cap;
   P.rc2 = (float)(b->p.rc * b->p.rc);
@@ -813,10 +1082,14 @@ int launch_mx_pair_only(Box *b) {
   double rc2 = b->p.rc * b->p.rc;
   P.ron2 = (float)ron2;
   P.sw_den = ron2 > 0.0 ? (float)((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2)) : 0.f;
-  int blocks = pair_blocks(b);
-  size_t shm = sizeof(float) * (kCodes * 6 + b->nt * b->nt * 3);
-  k_mx_pair<<<blocks, kMxWarps * 32, shm, b->stream>>>(P, M.pos32, M.type_s, M.perm, M.count, M.ent,
-                                                      M.shift_tab, M.lj_tab, M.fix, b->partials);
+  P.sc = fix_scale(b);
+  size_t shm = sizeof(float) * (b->nt * b->nt * 3);
+  const int *clj = M.use_inner ? M.icnt_lj : M.cnt_lj;
+  const int *cnl = M.use_inner ? M.icnt_nl : M.cnt_nl;
+  const int *ent = M.use_inner ? M.ient : M.ent;
+  k_mx_pair<<<pair_blocks(b), kMxWarps * 32, shm, b->stream>>>(
+      P, M.posfx, M.type_s, M.perm, clj, cnl, ent, M.lj_tab, M.fix, b->partials, b->ticket,
+      b->scal + SC_MX_PAIR);
   FE_LAUNCH_CHECK("k_mx_pair");
   return FE_OK;
 }
@@ -824,9 +1097,12 @@ int launch_mx_pair_only(Box *b) {
 int launch_mx_spread_only(Box *b) {
   Mixed &M = *b->mx;
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
-  k_mx_spread<<<(unsigned)((b->K + 127) / 128), 128, 0, b->stream>>>(
-      b->order, G, M.pos32, M.sm, b->gcap, b->gbin_count, b->gbin_atoms, M.grid32);
-  FE_LAUNCH_CHECK("k_mx_spread");
+  int nbk = ((b->G[0] + kBrick - 1) / kBrick) * ((b->G[1] + kBrick - 1) / kBrick) *
+            ((b->G[2] + kBrick - 1) / kBrick);
+  k_mx_spread4<<<nbk, kSp4Warps * 32, 0, b->stream>>>(b->order, G, M.posfx, M.sm, b->gcap,
+                                                     b->gbin_count, b->gbin_atoms, M.grid32,
+                                                     b->status);
+  FE_LAUNCH_CHECK("k_mx_spread4");
   return FE_OK;
 }
 
@@ -835,9 +1111,9 @@ int forces_mixed(Box *b) {
   int n = b->n;
   int rc;
   if ((rc = launch_convert(b))) return rc;
+  if (M.use_inner && M.do_prune && (rc = launch_mx_prune(b))) return rc;
   FE_CUDA(cudaMemsetAsync(M.fix, 0, sizeof(unsigned long long) * 3 * n, b->stream));
   if ((rc = launch_mx_pair_only(b))) return rc;
-  if ((rc = launch_reduce(b, b->partials, pair_blocks(b), 4, SC_MX_PAIR, 1.0))) return rc;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
   // exclusions
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
@@ -847,9 +1123,9 @@ int forces_mixed(Box *b) {
   k_mx_excl<<<xb, 256, 0, b->stream>>>(M.nexcl, M.excl_ab, M.excl_flag, b->pos_q, b->type, L, b->nt,
                                        M.lj_tab, (float)(b->p.rc * b->p.rc), (float)b->p.kappa,
                                        (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
-                                       (float)b->p.epsRF, M.fix, b->partials);
+                                       (float)b->p.epsRF, M.fix, b->partials, b->ticket,
+                                       b->scal + SC_MX_EXCL);
   FE_LAUNCH_CHECK("k_mx_excl");
-  if ((rc = launch_reduce(b, b->partials, xb, 5, SC_MX_EXCL, 1.0))) return rc;
   // bonded
   int tot = b->nbond + b->nbend;
   int bb = (tot + 255) / 256;
@@ -857,9 +1133,8 @@ int forces_mixed(Box *b) {
   if (bb < 1) bb = 1;
   k_mx_bonded<<<bb, 256, 0, b->stream>>>(b->nbond, b->nbend, L, b->pos_q, b->bond_ab, b->bond_req,
                                          b->bond_k, b->bend_abc, b->bend_t0, b->bend_k, M.fix,
-                                         b->partials);
+                                         b->partials, b->ticket, b->scal + SC_BOND);
   FE_LAUNCH_CHECK("k_mx_bonded");
-  if ((rc = launch_reduce(b, b->partials, bb, 2, SC_BOND, 1.0))) return rc;
   // SPME
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   FE_CUDA(cudaMemsetAsync(b->gbin_count, 0, sizeof(int) * b->K, b->stream));
@@ -870,18 +1145,16 @@ int forces_mixed(Box *b) {
   k_mx_binsort<<<(unsigned)((b->K + 255) / 256), 256, 0, b->stream>>>(b->K, b->gcap, b->gbin_count,
                                                                      b->gbin_atoms);
   FE_LAUNCH_CHECK("k_mx_binsort");
-  k_mx_spread<<<(unsigned)((b->K + 127) / 128), 128, 0, b->stream>>>(
-      b->order, G, M.pos32, M.sm, b->gcap, b->gbin_count, b->gbin_atoms, M.grid32);
-  FE_LAUNCH_CHECK("k_mx_spread");
+  if ((rc = launch_mx_spread_only(b))) return rc;
   cufftResult r = cufftSetStream(M.plan_r2c, b->stream);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   r = cufftExecR2C(M.plan_r2c, M.grid32, M.grid32k);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
   int kb = (int)((b->Kh + 255) / 256);
   if (kb > 1024) kb = 1024;
-  k_mx_recip<<<kb, 256, 0, b->stream>>>(b->Kh, M.eterm32, M.kw32, M.grid32k, b->partials);
+  k_mx_recip<<<kb, 256, 0, b->stream>>>(b->Kh, M.eterm32, M.kw32, M.grid32k, b->partials,
+                                        b->ticket, b->scal + SC_ENREC);
   FE_LAUNCH_CHECK("k_mx_recip");
-  if ((rc = launch_reduce(b, b->partials, kb, 1, SC_ENREC, 1.0))) return rc;
   r = cufftSetStream(M.plan_c2r, b->stream);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   r = cufftExecC2R(M.plan_c2r, M.grid32k, M.grid32);
@@ -891,23 +1164,13 @@ int forces_mixed(Box *b) {
   int gb = (n + 127) / 128;
   if (gb > 1024) gb = 1024;
   float qfe = (float)(qf / b->p.epsRF);
-  k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.pos32, M.perm, M.floor3, M.sm,
-                                         M.sd, M.grid32, M.fix, b->partials);
+  k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3, M.sm,
+                                         M.sd, M.grid32, M.fix, b->partials, b->ticket,
+                                         b->scal + SC_FMEAN);
   FE_LAUNCH_CHECK("k_mx_gather");
-  if ((rc = launch_reduce(b, b->partials, gb, 3, SC_FMEAN, 1.0))) return rc;
   k_mx_finalize<<<(3 * n + 255) / 256, 256, 0, b->stream>>>(n, M.fix, b->scal, b->ff);
   FE_LAUNCH_CHECK("k_mx_finalize");
   return launch_mixed_assemble(b);
-}
-
-// combine the mixed kernels' sums into the reference's slots, then assemble
-__global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc) {
-  if (threadIdx.x != 0) return;
-  s[SC_LJ] = s[SC_MX_PAIR + 0] + s[SC_MX_EXCL + 0];
-  s[SC_LJS] = s[SC_MX_PAIR + 1] + s[SC_MX_EXCL + 1];
-  s[SC_REAL] = s[SC_MX_PAIR + 2] + s[SC_MX_EXCL + 2];
-  s[SC_REALS] = (s[SC_MX_PAIR + 3] + s[SC_MX_EXCL + 3]) * erfc_rc_over_rc;
-  s[SC_INTRA] = s[SC_MX_EXCL + 4];
 }
 
 int launch_mixed_assemble(Box *b) {
