@@ -222,6 +222,34 @@ int fe_mc_kspace_energy(fe_box *box, double *e);
 int fe_ewald_kspace_energy_noalloc(const double *xyzq, int n, const double *L, double kappa,
                                    int kmax, int max_k_square, double *energy, void *stream);
 
+/* ---- replicas stepped together, exchange on the device ----------------- */
+
+/* A batch steps several boxes (any sizes, same device, same Nose-Hoover
+ * chain length) in one CUDA graph per step, each box on its own stream, and
+ * attempts replica exchanges on the device.  Replaces the box loop and the
+ * swap schedule of repexch.c:139-214,268-305 and swap_box (swap_box.c:5-86).
+ * Temperature slot s initially belongs to box s at that box's params.T.  An
+ * accepted swap exchanges the slots (temperature and chain state) of two
+ * boxes instead of their coordinates and rescales their velocities as
+ * swap_box does.  The batch does not own the boxes. */
+typedef struct fe_batch fe_batch;
+int fe_batch_create(fe_batch **out, fe_box *const *boxes, int nbox, uint64_t seed);
+void fe_batch_destroy(fe_batch *batch);
+/* Steps first_step .. first_step+nsteps-1 of every box: a list rebuild before
+ * step i when i % nlist_freq == 0, an exchange attempt after step i when
+ * swap_freq > 0 and i % swap_freq == 0 (repexch.c counts steps from 1).
+ * use_nhc: integrate_nhc around integrate_vverlet (nvt_md.c:529-531). */
+int fe_batch_run(fe_batch *batch, int nsteps, int nlist_freq, int swap_freq, long first_step,
+                 int use_nhc);
+/* Any pointer may be NULL.  slot_box[s]: box holding slot s; T_box[b]:
+ * current temperature of box b; accepted/attempted[s]: swaps of the slot
+ * pair (s, s+1); attempts: exchange attempts made. */
+int fe_batch_state(fe_batch *batch, int *slot_box, double *T_box, int64_t *accepted,
+                   int64_t *attempted, uint64_t *attempts);
+/* Own kernel launches in one step graph: [plain, list, exchange, list+exchange];
+ * -1 for a variant not captured yet. */
+int fe_batch_step_launches(fe_batch *batch, int *launches4);
+
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 
 enum { FE_KERNEL_PAIR = 0, FE_KERNEL_SPREAD = 1, FE_KERNEL_LIST = 2 };

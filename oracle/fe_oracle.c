@@ -1074,3 +1074,61 @@ double or_mc_delta_energy(const or_system *s, const double *pos,
   }
   return dk + dreal + dlj;
 }
+
+/* ---- counter-based random numbers and replica exchange ---- */
+
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  /* Salmon et al., SC'11: ten rounds; multipliers 0xD2511F53 / 0xCD9E8D57,
+   * key increments 0x9E3779B9 / 0xBB67AE85 between rounds */
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; r++) {
+    if (r) {
+      k0 += 0x9E3779B9u;
+      k1 += 0xBB67AE85u;
+    }
+    uint64_t p0 = (uint64_t)0xD2511F53u * c0;
+    uint64_t p1 = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0;
+    uint32_t n1 = (uint32_t)p1;
+    uint32_t n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+    uint32_t n3 = (uint32_t)p0;
+    c0 = n0; c1 = n1; c2 = n2; c3 = n3;
+  }
+  out[0] = c0; out[1] = c1; out[2] = c2; out[3] = c3;
+}
+
+double or_uniform(uint64_t seed, uint32_t tag, uint64_t event, uint32_t lane) {
+  uint32_t c[4] = {lane, (uint32_t)event, (uint32_t)(event >> 32), tag};
+  uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  or_philox4x32_10(c, k, o);
+  uint64_t w = ((uint64_t)o[0] << 32) | o[1];
+  return (double)(w >> 11) * (1.0 / 9007199254740992.0);
+}
+
+#define OR_TAG_EXCHANGE 0x52455831u
+
+int or_rex_attempt(int R, const double *T_slot, const double *potens_box, int *slot_box,
+                   uint64_t attempt, uint64_t seed, int *vmode, double *vfac) {
+  /* swap_box.c:5-86 on temperature slots; pairs alternate as repexch.c:273-301 */
+  int nacc = 0;
+  for (int r = 0; r < R; r++) vmode[r] = 0;
+  for (int s = (int)(attempt & 1u); s + 1 < R; s += 2) {
+    int r1 = slot_box[s], r2 = slot_box[s + 1];
+    double kT1 = ((KB_ * NA_) * T_slot[s]) * .001;      /* read_sim.c:351 */
+    double kT2 = ((KB_ * NA_) * T_slot[s + 1]) * .001;
+    double delta_beta = 1.0 / kT1 - 1.0 / kT2;
+    double delta_energy = potens_box[r1] - potens_box[r2];
+    double accep_crit = exp(delta_beta * delta_energy);
+    if (accep_crit > or_uniform(seed, OR_TAG_EXCHANGE, attempt, (uint32_t)s)) {
+      slot_box[s] = r2;
+      slot_box[s + 1] = r1;
+      double v_scale_1 = sqrt(T_slot[s] / T_slot[s + 1]);
+      vmode[r2] = 1; vfac[r2] = v_scale_1;
+      vmode[r1] = 2; vfac[r1] = v_scale_1;
+      nacc++;
+    }
+  }
+  return nacc;
+}

@@ -161,6 +161,21 @@ double or_mc_delta_energy(const or_system *s, const double *pos,
                           const double *pos_new, int lb, int ub, int kmax,
                           int max_k_square, double rc_ew, double parts[3]);
 
+/* ---- counter-based random numbers and replica exchange ---- */
+
+/* Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11). */
+void or_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
+/* Uniform [0,1) from words 0,1 of the draw at counter (lane, event lo, event
+ * hi, tag) under key (seed lo, seed hi): 53 bits. */
+double or_uniform(uint64_t seed, uint32_t tag, uint64_t event, uint32_t lane);
+/* One exchange attempt (swap_box.c:5-86) on temperature slots: pairs
+ * (s, s+1) with s = attempt & 1, 2 + (attempt & 1), ... (repexch.c:273-301);
+ * accept when exp((1/kT_s - 1/kT_s+1)(U_box(s) - U_box(s+1))) > u.  Updates
+ * slot_box; vmode[b] = 1 (multiply by vfac) / 2 (divide) / 0 for each box.
+ * Returns the number of accepted swaps. */
+int or_rex_attempt(int R, const double *T_slot, const double *potens_box, int *slot_box,
+                   uint64_t attempt, uint64_t seed, int *vmode, double *vfac);
+
 #ifdef __cplusplus
 }
 #endif

@@ -232,21 +232,30 @@ class Oracle:
                                   C.c_double(Q), C.c_double(nfree), _p(zeta), _p(vv), _p(uu))
         return vv, uu, zeta
 
-    def run_md(self, nsteps, use_nhc=False, pos=None, vel=None):
+    def run_md(self, nsteps, use_nhc=False, pos=None, vel=None, zeta=None, pos_nopbc=None,
+               T=None):
+        """or_run_md from the given state; zeta / pos_nopbc / T (the
+        thermostat temperature, sim.T[k]) default to a fresh start."""
         s = self.sysm
         pos = np.ascontiguousarray(s.pos if pos is None else pos, np.float64).copy()
-        nop = pos.copy()
+        nop = pos.copy() if pos_nopbc is None else np.ascontiguousarray(pos_nopbc,
+                                                                        np.float64).copy()
         vv = np.ascontiguousarray(s.vel if vel is None else vel, np.float64).copy()
         ff = np.zeros_like(pos)
         M = s.nhc_M
-        zeta = np.zeros(3 * max(M, 1))
-        kT = 1.380662e-23 * s.T * 1e-4
-        for i in range(M - 1):  # read_config.c:369-370
-            zeta[3 * (i + 1) + 2] = (s.nhc_Q * zeta[3 * i + 1] ** 2 - kT) / s.nhc_Q
+        self.s.T = s.T if T is None else float(T)
+        if zeta is None:
+            zeta = np.zeros(3 * max(M, 1))
+            kT = 1.380662e-23 * s.T * 1e-4
+            for i in range(M - 1):  # read_config.c:369-370
+                zeta[3 * (i + 1) + 2] = (s.nhc_Q * zeta[3 * i + 1] ** 2 - kT) / s.nhc_Q
+        else:
+            zeta = np.ascontiguousarray(zeta, np.float64).reshape(-1).copy()
         rec = np.zeros((nsteps + 1, 12))
         rc = self.lib.or_run_md(self.sp, nsteps, s.nlist_freq, int(use_nhc), M,
                                 C.c_double(s.nhc_Q), _p(pos), _p(nop), _p(vv), _p(ff),
                                 _p(zeta), _p(rec))
+        self.s.T = s.T
         if rc != 0:
             raise RuntimeError("oracle md failed (list overflow)")
         return dict(en=rec, pos=pos, pos_nopbc=nop, vel=vv, force=ff, zeta=zeta.reshape(-1, 3))
@@ -332,3 +341,44 @@ def run_reference(mode, sysm, workdir, nsteps=None, fast=False):
     cmd = [binp, mode, sp, op] + ([str(nsteps)] if nsteps is not None else [])
     subprocess.check_call(cmd)
     return read_tagged(op)
+
+
+# ---- counter-based random numbers and replica exchange (no system needed) ----
+
+def _lib():
+    L = C.CDLL(build())
+    L.or_uniform.restype = C.c_double
+    L.or_uniform.argtypes = [C.c_uint64, C.c_uint32, C.c_uint64, C.c_uint32]
+    L.or_rex_attempt.restype = C.c_int
+    L.or_rex_attempt.argtypes = [C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint64,
+                                 C.c_uint64, C.c_void_p, C.c_void_p]
+    return L
+
+
+TAG_EXCHANGE = 0x52455831
+
+
+def philox4x32_10(ctr, key):
+    L = _lib()
+    c = np.ascontiguousarray(ctr, np.uint32)
+    k = np.ascontiguousarray(key, np.uint32)
+    o = np.zeros(4, np.uint32)
+    L.or_philox4x32_10(_p(c), _p(k), _p(o))
+    return o
+
+
+def uniform(seed, tag, event, lane):
+    return _lib().or_uniform(seed, tag, event, lane)
+
+
+def rex_attempt(T_slot, potens_box, slot_box, attempt, seed):
+    """One exchange attempt; returns (slot_box, vmode, vfac, n_accepted)."""
+    L = _lib()
+    T = np.ascontiguousarray(T_slot, np.float64)
+    U = np.ascontiguousarray(potens_box, np.float64)
+    slot = np.ascontiguousarray(slot_box, np.int32).copy()
+    R = len(T)
+    vmode = np.zeros(R, np.int32)
+    vfac = np.zeros(R)
+    n = L.or_rex_attempt(R, _p(T), _p(U), _p(slot), attempt, seed, _p(vmode), _p(vfac))
+    return slot, vmode, vfac, n

@@ -37,6 +37,7 @@ UNITS = {
     "k_mc.cu": ["-fmad=false"],
     "k_mixed.cu": [],
     "k_noalloc.cu": [],
+    "k_replica.cu": ["-fmad=false"],
 }
 
 

@@ -223,6 +223,7 @@ static int create(Box *b, const fe_box_params *p) {
   FE_CUDA(cudaMalloc(&b->partials, sizeof(double) * kMaxPartialBlocks * kPartialTerms));
   FE_CUDA(cudaMalloc(&b->scal, sizeof(double) * SC_COUNT));
   FE_CUDA(cudaMemset(b->scal, 0, sizeof(double) * SC_COUNT));
+  FE_CUDA(cudaMemcpy(b->scal + SC_TEMP, &p->T, sizeof(double), cudaMemcpyHostToDevice));
   FE_CUDA(cudaMalloc(&b->status, sizeof(int)));
   FE_CUDA(cudaMemset(b->status, 0, sizeof(int)));
   FE_CUDA(cudaMalloc(&b->ticket, sizeof(unsigned)));
@@ -279,7 +280,7 @@ static void stage_xyz_out(Box *b, void *atoms, size_t stride, size_t off, const 
 
 // one step of the production loop (graph body); `prune` refreshes the mixed
 // path's inner list inside the force evaluation
-static int step_body(Box *b, bool with_list, bool use_nhc, bool prune) {
+int step_body(Box *b, bool with_list, bool use_nhc, bool prune) {
   int rc;
   if (with_list && (rc = launch_list(b))) return rc;
   if (b->mx) b->mx->do_prune = with_list || prune;

@@ -50,7 +50,8 @@ enum : int {
   SC_ENERGY3 = SC_ENERGY8 + 8,     // 3 slots: pme_calc energy[]
   SC_MX_PAIR = SC_ENERGY3 + 3,     // 4 slots: mixed pair sums (lj, ljs, real, sum qq)
   SC_MX_EXCL = SC_MX_PAIR + 4,     // 5 slots: mixed exclusion sums (.., intra)
-  SC_COUNT = SC_MX_EXCL + 5
+  SC_TEMP = SC_MX_EXCL + 5,        // thermostat temperature [K] (sim.T[k]); exchanges rewrite it
+  SC_COUNT
 };
 
 // Largest number of blocks a partial-sum kernel may use.
@@ -195,6 +196,8 @@ int launch_kinet(Box *b);
 int launch_vv2_kinet(Box *b, double vscal);  // vv2 with the kinetic tensor folded in
 int launch_nhc(Box *b, double time_step);
 int launch_record(Box *b);
+// one MD step of the box on its stream (nve_md.c:359-418 / nvt_md.c:529-531)
+int step_body(Box *b, bool with_list, bool use_nhc, bool prune);
 // instrumentation: relaunch one kernel (FE_KERNEL_*) on the current state
 int relaunch_kernel(Box *b, int which);
 // k_mc.cu

@@ -272,10 +272,13 @@ int launch_kinet(Box *b) {
   return FE_OK;
 }
 
-// integrate_nhc.c:57-147 (Nc = Nys = 1, w[0] = 1): the chain, one thread
-__global__ void k_nhc_chain(int M, double Q, double nfree, double T, double time_step,
+// integrate_nhc.c:57-147 (Nc = Nys = 1, w[0] = 1): the chain, one thread.
+// The temperature is read from s[SC_TEMP] so that replica exchanges can
+// change it on the device between graph replays.
+__global__ void k_nhc_chain(int M, double Q, double nfree, double time_step,
                             double *__restrict__ zeta, double *__restrict__ s) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  double T = s[SC_TEMP];
 #define ZR(j) zeta[3 * (j)]
 #define ZV(j) zeta[3 * (j) + 1]
 #define ZG(j) zeta[3 * (j) + 2]
@@ -322,7 +325,7 @@ __global__ void k_nhc_scale(int n3, const double *__restrict__ s, double *__rest
 int launch_nhc(Box *b, double time_step) {
   int rc = launch_kinet(b);  // integrate_nhc.c:68
   if (rc) return rc;
-  k_nhc_chain<<<1, 32, 0, b->stream>>>(b->nhc_M, b->nhc_Q, b->nfree, b->p.T, time_step, b->zeta,
+  k_nhc_chain<<<1, 32, 0, b->stream>>>(b->nhc_M, b->nhc_Q, b->nfree, time_step, b->zeta,
                                        b->scal);
   FE_LAUNCH_CHECK("k_nhc_chain");
   k_nhc_scale<<<(3 * b->n + 255) / 256, 256, 0, b->stream>>>(3 * b->n, b->scal, b->vv, b->uu);

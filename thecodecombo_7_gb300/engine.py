@@ -46,6 +46,8 @@ EXPORTS = [
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats",
     "fe_ewald_kspace_energy_noalloc",
+    "fe_batch_create", "fe_batch_destroy", "fe_batch_run", "fe_batch_state",
+    "fe_batch_step_launches",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -94,8 +96,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     lib.fe_box_destroy.restype = None
     for name in EXPORTS:
         fn = getattr(lib, name)
-        if name not in ("fe_last_error", "fe_box_destroy", "fe_box_create"):
+        if name not in ("fe_last_error", "fe_box_destroy", "fe_box_create",
+                        "fe_batch_destroy"):
             fn.restype = C.c_int
+    lib.fe_batch_destroy.argtypes = [C.c_void_p]
+    lib.fe_batch_destroy.restype = None
+    lib.fe_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_void_p, C.c_int, C.c_uint64]
+    lib.fe_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_int]
     _lib = lib
     return lib
 
@@ -340,3 +347,59 @@ class Box:
         e = C.c_double()
         self._check(self.lib.fe_mc_kspace_energy(self.h, C.byref(e)))
         return e.value
+
+
+class Batch:
+    """Several boxes stepped together in one CUDA graph per step, with replica
+    exchange on the device (repexch.c:139-305, swap_box.c:5-86).
+
+    Slot s starts at box s and its temperature ``boxes[s].sysm.T``; an
+    accepted exchange swaps the slots (temperature and Nose-Hoover chain
+    state) of two boxes and rescales their velocities as swap_box does.
+    """
+
+    def __init__(self, boxes, seed: int = 1):
+        self.lib = load_library()
+        self.boxes = list(boxes)
+        arr = (C.c_void_p * len(self.boxes))(*[b.h for b in self.boxes])
+        h = C.c_void_p()
+        rc = self.lib.fe_batch_create(C.byref(h), arr, len(self.boxes), C.c_uint64(seed))
+        if rc != FE_OK:
+            raise FeError(rc, self.lib.fe_last_error().decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc != FE_OK:
+            raise FeError(rc, self.lib.fe_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fe_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsteps, nlist_freq=10, swap_freq=0, first_step=1, use_nhc=True):
+        self._check(self.lib.fe_batch_run(self.h, int(nsteps), int(nlist_freq), int(swap_freq),
+                                          int(first_step), int(use_nhc)))
+
+    def state(self):
+        R = len(self.boxes)
+        slot = np.empty(R, np.int32)
+        T = np.empty(R)
+        acc = np.empty(R, np.int64)
+        att = np.empty(R, np.int64)
+        n = C.c_uint64()
+        self._check(self.lib.fe_batch_state(self.h, _p(slot), _p(T), _p(acc), _p(att),
+                                            C.byref(n)))
+        return dict(slot_box=slot, T_box=T, accepted=acc[:R - 1], attempted=att[:R - 1],
+                    attempts=n.value)
+
+    def step_launches(self):
+        v = np.empty(4, np.int32)
+        self._check(self.lib.fe_batch_step_launches(self.h, _p(v)))
+        return v.tolist()
