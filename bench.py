@@ -190,6 +190,66 @@ def run_reference(args, world, rank):
     print(json.dumps(line))
 
 
+def nve_drift(rec, sysm):
+    """Linear drift of the total energy over the timed steps, in kT per ns
+    per degree of freedom (energies in kJ/mol, kT = RG T / 1000)."""
+    tot = rec[:, 0] + rec[:, 1] + rec[:, 2] + rec[:, 4]  # kinet + bond + bend + nbonds
+    t_ps = np.arange(len(tot)) * sysm.dt
+    slope = float(np.polyfit(t_ps, tot, 1)[0]) if len(tot) > 2 else 0.0  # kJ/mol/ps
+    kT = 1.380662e-23 * 6.022045e23 * sysm.T * 1e-3
+    nfree = 3 * sysm.n - 3
+    return {"kT_per_ns_per_dof": slope * 1000.0 / (kT * nfree), "steps": int(len(tot)),
+            "span_ps": float(t_ps[-1]) if len(tot) else 0.0}
+
+
+def batched_sample(local, steps):
+    """32 NHC replicas of the 3-site recipe, 2,000-12,000 molecules each
+    (seeded), own L at 0.1 sites/A^3 and grid ~1 point/A, T linear 300-400 K,
+    exchange every 500 steps, all boxes in one graph per step; timed with
+    CUDA events on the batch stream."""
+    import torch
+
+    from thecodecombo_7_gb300 import engine, systems
+    R = 32
+    rng = np.random.default_rng(SEED + 4)
+    nmol = rng.integers(2000, 12001, R)
+    temps = np.linspace(300.0, 400.0, R)
+    ss = [systems.water_box(int(m), density=0.1, seed=SEED + 100 + k, T=float(temps[k]))
+          for k, m in enumerate(nmol)]
+    boxes = [engine.Box(s, precision=engine.FE_PREC_MIXED, device=local) for s in ss]
+    try:
+        for b in boxes:
+            b.nblist()
+            b.forces()
+        batch = engine.Batch(boxes, seed=SEED)
+        batch.run(20, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
+        st = torch.cuda.ExternalStream(batch.stream(), device=local)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        first = 21
+        e0.record(st)
+        batch.run(steps, nlist_freq=10, swap_freq=500, first_step=first, use_nhc=True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        n_atoms = int(sum(s.n for s in ss))
+        state = batch.state()
+        lv = batch.step_launches()
+        n_list = sum(1 for i in range(first, first + steps) if i % 10 == 0)
+        n_ex = sum(1 for i in range(first, first + steps) if i % 500 == 0)
+        batch.close()
+    finally:
+        for b in boxes:
+            b.close()
+    return {"value": n_atoms * steps / (ms / 1000.0), "unit": METRIC, "replicas": R,
+            "sites": n_atoms, "steps": steps, "ms_per_step": ms / steps,
+            "workload": "32 NHC (M=3) replicas, 2,000-12,000 molecules each, own L at 0.1 "
+                        "sites/A^3, grid ~1 point/A, T 300-400 K, exchange every 500 steps",
+            "exchange_attempts": int(state["attempts"]),
+            "exchanges_in_timed_steps": n_ex, "list_steps": n_list,
+            "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]}}
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -207,6 +267,7 @@ def run_ours(args, world, rank, local):
     box.nblist()
     box.forces()
     box.kinet()
+    f_mixed0 = box.get_forces()
     W = max(args.warmup, 3)
     K = args.steps
     box.run_md(W, first_step=1)
@@ -219,7 +280,7 @@ def run_ours(args, world, rank, local):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    box.run_md(K, nlist_freq=nl, first_step=first)
+    rec = box.run_md(K, nlist_freq=nl, first_step=first)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier(world)
@@ -240,11 +301,18 @@ def run_ours(args, world, rank, local):
     traffic = profile_traffic()
     # plain FP64 drop-in on the same workload (the 10x denominator), a few steps
     fp64 = None
+    force_err = None
     if rank == 0:
         b64 = engine.Box(sysm, precision=engine.FE_PREC_FP64, device=local)
         b64.set_stream(stream.cuda_stream)
         b64.nblist()
         b64.forces()
+        f64 = b64.get_forces()
+        d = f_mixed0 - f64
+        force_err = {"rms_rel": float(np.sqrt((d ** 2).sum() / (f64 ** 2).sum())),
+                     "max_abs": float(np.abs(d).max()), "unit_max": "kJ/mol/A",
+                     "against": "FP64 drop-in on the same state (equal to the FP64 oracle "
+                                "to 1e-12 in the parity tests)", "step": 0}
         b64.kinet()
         b64.run_md(3, first_step=1)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -307,6 +375,11 @@ def run_ours(args, world, rank, local):
             cpu = {"value": None, "unit": METRIC, "cores": 1, "kind": "port",
                    "sample": f"failed: {exc}"}
     steps_per_s = K / (ms_max / 1000.0)
+    drift = nve_drift(rec, sysm)
+    try:
+        batched = batched_sample(local, steps=min(max(K, 100), 500))
+    except Exception as exc:  # the headline line must still print
+        batched = {"failed": str(exc)}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
@@ -327,6 +400,9 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "fp64_drop_in": {"value": fp64, "unit": METRIC,
                          "ratio": (value / world) / fp64 if fp64 else None},
+        "force_error": force_err,
+        "nve_drift": drift,
+        "batched_replicas": batched,
     }
     print(json.dumps(line))
 

@@ -222,6 +222,70 @@ int fe_mc_kspace_energy(fe_box *box, double *e);
 int fe_ewald_kspace_energy_noalloc(const double *xyzq, int n, const double *L, double kappa,
                                    int kmax, int max_k_square, double *energy, void *stream);
 
+/* ---- Monte Carlo chains resident on the device ------------------------- */
+
+/* nchains independent Metropolis chains of rigid-molecule moves on copies of
+ * the box's current configuration, one CTA per chain, thousands of moves per
+ * launch.  Replaces the move loop of nvt_mc.c:70-422 with its energy calls
+ * (forces_mc.c:90-573, ewald_kspace_mc ewald_mc.c:42-324, ewald_rspace_mc
+ * ewald_mc.c:328-641 with the correct minimum image) and its acceptance rule
+ * (mcmove_displ.c:130-137).  A move picks a molecule (mol_first[m] ..
+ * mol_first[m+1]-1, at most 8 sites) uniformly; with probability p_rot it
+ * rotates it about its centre of mass by an angle uniform in
+ * [-rot_max, rot_max] [rad] around a uniform random axis, otherwise it
+ * translates it by (u - 0.5) * delta per axis (mcmove_displ.c:92-94).  dE is
+ * the shifted LJ within rc, real-space Ewald within rc_ew and the
+ * classic-Ewald reciprocal sum over the k-vectors of ewald_setup with
+ * |n|^2 <= max_k_square (ewald.c:104-118, kappa of the box), in kJ/mol; T
+ * sets beta = 1/(RG T / 1000).  Coordinates are kept as 32-bit fixed-point
+ * fractions of the box and pair/phase arithmetic is FP32 with FP64 sums
+ * (|dE error| ~1e-3 kJ/mol).  Limits: n <= 10240 sites, <= 8 site types,
+ * <= 1024 k-vectors; excluded pairs must lie inside molecules.  Draws are
+ * Philox4x32-10 keyed by seed with counter (chain, move).  The first log_cap
+ * moves of chain 0 are logged. */
+int fe_mc_chains_setup(fe_box *box, int nchains, const int *mol_first, int nmol, int kmax,
+                       int max_k_square, double rc_ew, double T, double delta, double rot_max,
+                       double p_rot, uint64_t seed, int log_cap);
+/* nmoves further moves of every chain. */
+int fe_mc_chains_run(fe_box *box, int64_t nmoves);
+/* Chain state: xyz (n x 3, wrapped to [-L/2, L/2)), moves made, moves accepted. */
+int fe_mc_chains_state(fe_box *box, int chain, double *xyz, int64_t *moves, int64_t *accepted);
+/* Reciprocal energy sum_k c_k |S_k|^2 of a chain from its running S(k) [kJ/mol]. */
+int fe_mc_chains_kspace_energy(fe_box *box, int chain, double *e);
+/* Logged moves of chain 0: rec[8] per move = {2 lb + is_rotation, sites, accepted, dE,
+ * dE_k, dE_real, u, move number}; fx[24] per move = trial fixed-point coordinates
+ * (x, y, z per site; position = (u / 2^32 - 0.5) L). */
+int fe_mc_chains_log(fe_box *box, double *rec, uint32_t *fx, int64_t cap, int64_t *count);
+
+/* ---- Monte Carlo surrogate network (no counterpart in the reference) ---- */
+
+/* g(x) = w3 . silu(W2 silu(W1 (x - mean) * istd + b1) + b2) + b3, 64 inputs,
+ * hidden 128 + 128, trained and evaluated with BF16-in / FP32-accumulate
+ * tensor-core kernels (tcgen05).  A sample is 128 floats (descriptors of a
+ * trial move before | after) and a target y; the model's prediction is
+ * g(after) - g(before).  Parameters are packed W1[128][64], b1[128],
+ * W2[128][128], b2[128], w3[128], b3 (fe_mlp_param_count() floats). */
+typedef struct fe_mlp fe_mlp;
+int fe_mlp_create(fe_mlp **out, int device, uint64_t seed);
+void fe_mlp_destroy(fe_mlp *mlp);
+int fe_mlp_param_count(void);
+int fe_mlp_set_params(fe_mlp *mlp, const float *params, const float *mean, const float *istd);
+int fe_mlp_get_params(fe_mlp *mlp, float *params, float *mean, float *istd);
+/* Loss (mean squared error) and gradient at the current parameters for B
+ * samples (B % 64 == 0); out2B (may be NULL) gets g of the 2B rows
+ * (before rows first). */
+int fe_mlp_grad(fe_mlp *mlp, const float *data, const float *y, int B, float *grad, float *loss,
+                float *out2B);
+/* Adam on shuffled batches; normalisation set from the samples first;
+ * loss_hist[e] = mean batch loss of epoch e. */
+int fe_mlp_train(fe_mlp *mlp, const float *data, const float *y, int64_t n, int epochs, int batch,
+                 float lr, uint64_t seed, float *loss_hist);
+/* The tensor-core GEMM alone: D (M x N fp32) = A (M x K) B (N x K)^T + bias,
+ * A and B as bf16 bit patterns; M % 128 == 0, N in 32..256 step 32,
+ * K % 64 == 0. */
+int fe_tc_gemm_bf16(const uint16_t *A, const uint16_t *B, const float *bias, float *D, int M,
+                    int N, int K);
+
 /* ---- replicas stepped together, exchange on the device ----------------- */
 
 /* A batch steps several boxes (any sizes, same device, same Nose-Hoover
@@ -246,6 +310,8 @@ int fe_batch_run(fe_batch *batch, int nsteps, int nlist_freq, int swap_freq, lon
  * pair (s, s+1); attempts: exchange attempts made. */
 int fe_batch_state(fe_batch *batch, int *slot_box, double *T_box, int64_t *accepted,
                    int64_t *attempted, uint64_t *attempts);
+/* The stream the step graphs are launched on (for events around fe_batch_run). */
+int fe_batch_get_stream(fe_batch *batch, void **stream);
 /* Own kernel launches in one step graph: [plain, list, exchange, list+exchange];
  * -1 for a variant not captured yet. */
 int fe_batch_step_launches(fe_batch *batch, int *launches4);

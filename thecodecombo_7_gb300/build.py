@@ -38,6 +38,8 @@ UNITS = {
     "k_mixed.cu": [],
     "k_noalloc.cu": [],
     "k_replica.cu": ["-fmad=false"],
+    "k_mcrun.cu": [],
+    "k_mlp.cu": [],
 }
 
 

@@ -91,6 +91,7 @@ static void free_box(Box *b) {
   for (void *p : ptrs)
     if (p) cudaFree(p);
   mc_free(b);
+  mcc_free(b);
   mixed_free(b);
   if (b->host_scal) cudaFreeHost(b->host_scal);
   if (b->stage) cudaFreeHost(b->stage);

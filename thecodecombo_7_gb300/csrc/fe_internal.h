@@ -14,6 +14,7 @@
 namespace fe {
 
 struct Mixed;
+struct McChains;
 
 // Physical constants of the reference (defines.h:62-75).
 constexpr double kPI = 3.141592653589793238462643383;
@@ -149,6 +150,7 @@ struct Box {
 
   // mixed-precision path (k_mixed.cu); null in FP64 mode
   Mixed *mx = nullptr;
+  McChains *mcc = nullptr;     // device-resident Monte Carlo chains (k_mcrun.cu)
 };
 
 // ---- error plumbing ----
@@ -206,6 +208,8 @@ int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, dou
 int mc_accept(Box *b);
 int mc_kspace_energy(Box *b, double *e);
 void mc_free(Box *b);
+// k_mcrun.cu
+void mcc_free(Box *b);
 
 }  // namespace fe
 

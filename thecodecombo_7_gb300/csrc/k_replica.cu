@@ -354,6 +354,12 @@ int fe_batch_state(fe_batch *batch, int *slot_box, double *T_box, int64_t *accep
   return FE_OK;
 }
 
+int fe_batch_get_stream(fe_batch *batch, void **stream) {
+  if (!batch || !stream) return FE_ERR_ARG;
+  *stream = (void *)batch->B.main;
+  return FE_OK;
+}
+
 int fe_batch_step_launches(fe_batch *batch, int *launches4) {
   if (!batch || !launches4) return FE_ERR_ARG;
   for (int v = 0; v < 4; v++) launches4[v] = batch->B.g[v] ? batch->B.launches[v] : -1;

@@ -47,7 +47,11 @@ EXPORTS = [
     "fe_time_kernel", "fe_step_launches", "fe_list_stats",
     "fe_ewald_kspace_energy_noalloc",
     "fe_batch_create", "fe_batch_destroy", "fe_batch_run", "fe_batch_state",
-    "fe_batch_step_launches",
+    "fe_batch_step_launches", "fe_batch_get_stream",
+    "fe_mc_chains_setup", "fe_mc_chains_run", "fe_mc_chains_state",
+    "fe_mc_chains_kspace_energy", "fe_mc_chains_log",
+    "fe_mlp_create", "fe_mlp_destroy", "fe_mlp_param_count", "fe_mlp_set_params",
+    "fe_mlp_get_params", "fe_mlp_grad", "fe_mlp_train", "fe_tc_gemm_bf16",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -97,12 +101,26 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     for name in EXPORTS:
         fn = getattr(lib, name)
         if name not in ("fe_last_error", "fe_box_destroy", "fe_box_create",
-                        "fe_batch_destroy"):
+                        "fe_batch_destroy", "fe_mlp_destroy"):
             fn.restype = C.c_int
+    lib.fe_mlp_destroy.argtypes = [C.c_void_p]
+    lib.fe_mlp_destroy.restype = None
+    lib.fe_mlp_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_uint64]
+    lib.fe_mlp_grad.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
+                                C.c_void_p, C.c_void_p]
+    lib.fe_mlp_train.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_int,
+                                 C.c_float, C.c_uint64, C.c_void_p]
+    lib.fe_tc_gemm_bf16.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int,
+                                    C.c_int, C.c_int]
     lib.fe_batch_destroy.argtypes = [C.c_void_p]
     lib.fe_batch_destroy.restype = None
     lib.fe_batch_create.argtypes = [C.POINTER(C.c_void_p), C.c_void_p, C.c_int, C.c_uint64]
     lib.fe_batch_run.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_long, C.c_int]
+    lib.fe_mc_chains_setup.argtypes = [C.c_void_p, C.c_int, C.c_void_p, C.c_int, C.c_int, C.c_int,
+                                       C.c_double, C.c_double, C.c_double, C.c_double,
+                                       C.c_double, C.c_uint64, C.c_int]
+    lib.fe_mc_chains_run.argtypes = [C.c_void_p, C.c_int64]
+    lib.fe_mc_chains_log.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
     _lib = lib
     return lib
 
@@ -348,6 +366,43 @@ class Box:
         self._check(self.lib.fe_mc_kspace_energy(self.h, C.byref(e)))
         return e.value
 
+    # ---- Monte Carlo chains resident on the device ----
+    def mc_chains_setup(self, nchains=1, mol_first=None, kmax=7, max_k_square=None, rc_ew=None,
+                        T=None, delta=0.6, rot_max=0.2617993877991494, p_rot=0.5, seed=1,
+                        log_cap=0):
+        s = self.sysm
+        if mol_first is None:  # 3-site molecules in order
+            mol_first = np.arange(0, s.n + 1, 3, dtype=np.int32)
+        mf = _c(mol_first, np.int32)
+        mks = kmax * kmax if max_k_square is None else max_k_square
+        self._mc_nmol = len(mf) - 1
+        self._check(self.lib.fe_mc_chains_setup(
+            self.h, int(nchains), _p(mf), self._mc_nmol, int(kmax), int(mks),
+            float(s.rc_ew if rc_ew is None else rc_ew), float(s.T if T is None else T),
+            float(delta), float(rot_max), float(p_rot), C.c_uint64(seed), int(log_cap)))
+
+    def mc_chains_run(self, nmoves):
+        self._check(self.lib.fe_mc_chains_run(self.h, int(nmoves)))
+
+    def mc_chains_state(self, chain=0):
+        xyz = np.empty((self.sysm.n, 3))
+        mv, acc = C.c_int64(), C.c_int64()
+        self._check(self.lib.fe_mc_chains_state(self.h, int(chain), _p(xyz), C.byref(mv),
+                                                C.byref(acc)))
+        return xyz, mv.value, acc.value
+
+    def mc_chains_kspace_energy(self, chain=0):
+        e = C.c_double()
+        self._check(self.lib.fe_mc_chains_kspace_energy(self.h, int(chain), C.byref(e)))
+        return e.value
+
+    def mc_chains_log(self, cap):
+        rec = np.zeros((cap, 8))
+        fx = np.zeros((cap, 8, 3), np.uint32)
+        cnt = C.c_int64()
+        self._check(self.lib.fe_mc_chains_log(self.h, _p(rec), _p(fx), int(cap), C.byref(cnt)))
+        return rec[:cnt.value], fx[:cnt.value]
+
 
 class Batch:
     """Several boxes stepped together in one CUDA graph per step, with replica
@@ -403,3 +458,86 @@ class Batch:
         v = np.empty(4, np.int32)
         self._check(self.lib.fe_batch_step_launches(self.h, _p(v)))
         return v.tolist()
+
+    def stream(self) -> int:
+        """cudaStream_t (as an integer) the step graphs run on."""
+        s = C.c_void_p()
+        self._check(self.lib.fe_batch_get_stream(self.h, C.byref(s)))
+        return s.value or 0
+
+
+def tc_gemm_bf16(A_bits, B_bits, bias=None):
+    """D = A B^T (+ bias) on the tensor cores; A (M x K), B (N x K) uint16 bf16 bits."""
+    lib = load_library()
+    A = _c(A_bits, np.uint16)
+    B = _c(B_bits, np.uint16)
+    M, K = A.shape
+    N = B.shape[0]
+    D = np.empty((M, N), np.float32)
+    bb = _c(bias, np.float32) if bias is not None else None
+    rc = lib.fe_tc_gemm_bf16(_p(A), _p(B), _p(bb) if bb is not None else None, _p(D), M, N, K)
+    if rc != FE_OK:
+        raise FeError(rc, lib.fe_last_error().decode())
+    return D
+
+
+class Mlp:
+    """The Monte Carlo surrogate network (tensor-core training kernels)."""
+
+    N_IN = 64
+
+    def __init__(self, device: int = 0, seed: int = 1):
+        self.lib = load_library()
+        h = C.c_void_p()
+        self._check(self.lib.fe_mlp_create(C.byref(h), int(device), C.c_uint64(seed)))
+        self.h = h
+        self.n_params = self.lib.fe_mlp_param_count()
+
+    def _check(self, rc):
+        if rc != FE_OK:
+            raise FeError(rc, self.lib.fe_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fe_mlp_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def get_params(self):
+        P = np.empty(self.n_params, np.float32)
+        mean = np.empty(self.N_IN, np.float32)
+        istd = np.empty(self.N_IN, np.float32)
+        self._check(self.lib.fe_mlp_get_params(self.h, _p(P), _p(mean), _p(istd)))
+        return P, mean, istd
+
+    def set_params(self, P, mean=None, istd=None):
+        P = _c(P, np.float32)
+        m = _c(mean, np.float32) if mean is not None else None
+        s = _c(istd, np.float32) if istd is not None else None
+        self._check(self.lib.fe_mlp_set_params(self.h, _p(P), _p(m) if m is not None else None,
+                                               _p(s) if s is not None else None))
+
+    def grad(self, data, y):
+        data = _c(data, np.float32)
+        y = _c(y, np.float32)
+        B = data.shape[0]
+        G = np.empty(self.n_params, np.float32)
+        out = np.empty(2 * B, np.float32)
+        loss = C.c_float()
+        self._check(self.lib.fe_mlp_grad(self.h, _p(data), _p(y), B, _p(G), C.byref(loss),
+                                         _p(out)))
+        return loss.value, G, out
+
+    def train(self, data, y, epochs=10, batch=256, lr=1e-3, seed=1):
+        data = _c(data, np.float32)
+        y = _c(y, np.float32)
+        hist = np.empty(epochs, np.float32)
+        self._check(self.lib.fe_mlp_train(self.h, _p(data), _p(y), data.shape[0], int(epochs),
+                                          int(batch), C.c_float(lr), C.c_uint64(seed),
+                                          _p(hist)))
+        return hist
