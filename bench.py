@@ -191,8 +191,8 @@ def run_reference(args, world, rank):
 
 
 def nve_drift(rec, sysm):
-    """Linear drift of the total energy over the timed steps, in kT per ns
-    per degree of freedom (energies in kJ/mol, kT = RG T / 1000)."""
+    """Linear drift of the total energy (kinetic + shifted potential) over a
+    run, in kT per ns per degree of freedom (kJ/mol, kT = RG T / 1000)."""
     tot = rec[:, 0] + rec[:, 1] + rec[:, 2] + rec[:, 4]  # kinet + bond + bend + nbonds
     t_ps = np.arange(len(tot)) * sysm.dt
     slope = float(np.polyfit(t_ps, tot, 1)[0]) if len(tot) > 2 else 0.0  # kJ/mol/ps
@@ -222,11 +222,12 @@ def batched_sample(local, steps):
             b.nblist()
             b.forces()
         batch = engine.Batch(boxes, seed=SEED)
-        batch.run(20, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
+        # warm up to step 480 so that the timed steps include the exchange at step 500
+        batch.run(480, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
         st = torch.cuda.ExternalStream(batch.stream(), device=local)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
-        first = 21
+        first = 481
         e0.record(st)
         batch.run(steps, nlist_freq=10, swap_freq=500, first_step=first, use_nhc=True)
         e1.record(st)
@@ -248,6 +249,74 @@ def batched_sample(local, steps):
             "exchange_attempts": int(state["attempts"]),
             "exchanges_in_timed_steps": n_ex, "list_steps": n_list,
             "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]}}
+
+
+def mc_sample(local):
+    """Monte Carlo on the 4,095-site box: exact-dE chains against delayed
+    acceptance with the surrogate trained on 2x10^5 exact moves of the same
+    method; accepted moves/s for one chain (2x10^5 timed moves per mode) and
+    for 152 chains (one per SM, 10^6 timed moves in total)."""
+    import torch
+
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(1365, density=0.1, seed=SEED + 3)
+    box = engine.Box(s, precision=engine.FE_PREC_FP64, device=local)
+    stream = torch.cuda.Stream(device=local)
+    box.set_stream(stream.cuda_stream)
+    net = engine.Mlp(device=local, seed=SEED)
+    out = {"workload": "4,095 sites (1,365 rigid 3-site molecules, L 34.47 A), translation "
+                       "<= 0.3 A / rotation <= 15 deg, Ewald kappa 0.32, |n|^2 <= 49 "
+                       "(783 k-vectors), rc 10 A, 300 K"}
+    try:
+        # training set: 2x10^5 exact moves (152 chains x 1,316)
+        box.mc_chains_setup(nchains=152, kmax=7, T=300.0, seed=SEED)
+        box.mc_chains_collect(1316)
+        box.mc_chains_run(1316)
+        t0 = time.perf_counter()
+        hist = box.mc_chains_train_surrogate(net, epochs=20, batch=512, lr=2e-3, seed=SEED)
+        t_train = time.perf_counter() - t0
+        box.mc_chains_setup(nchains=16, kmax=7, T=300.0, seed=SEED + 1)
+        box.mc_chains_collect(512)
+        box.mc_chains_run(512)
+        held = box.mc_chains_samples()
+        B = (len(held) // 64) * 64
+        _, _, g = net.grad(held[:B, :128], held[:B, 128])
+        y = held[:B, 128].astype(np.float64)
+        res = (g[B:] - g[:B]).astype(np.float64) - y
+        out["surrogate"] = {"train_samples": 152 * 1316, "epochs": 20, "train_s": t_train,
+                            "loss_first_last": [float(hist[0]), float(hist[-1])],
+                            "heldout_dEk_rms": float(np.sqrt(np.mean(y * y))),
+                            "heldout_residual_rms": float(np.sqrt(np.mean(res * res)))}
+        for mode, name in ((0, "exact"), (1, "delayed_acceptance")):
+            for nch, moves in ((1, 200000), (152, 6600)):
+                box.mc_chains_setup(nchains=nch, kmax=7, T=300.0, seed=SEED + 7)
+                if mode:
+                    box.mc_chains_set_surrogate(net)
+                    box.mc_chains_set_mode(1)
+                box.mc_chains_run(2000)
+                st0 = [box.mc_chains_stats(c) for c in range(nch)]
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                box.mc_chains_run(moves)
+                e1.record(stream)
+                torch.cuda.synchronize()
+                sec = e0.elapsed_time(e1) / 1000.0
+                st1 = [box.mc_chains_stats(c) for c in range(nch)]
+                acc = sum(b["accepted"] - a["accepted"] for a, b in zip(st0, st1))
+                s1 = sum(b["stage1"] - a["stage1"] for a, b in zip(st0, st1))
+                tot = nch * moves
+                out[f"{name}_{nch}_chain{'s' if nch > 1 else ''}"] = {
+                    "accepted_moves_per_s": acc / sec, "moves_per_s": tot / sec,
+                    "acceptance": acc / tot, "stage1_acceptance": s1 / tot,
+                    "moves_per_chain": moves, "chains": nch, "us_per_move": 1e6 * sec / moves}
+        out["da_over_exact_accepted_per_s"] = (
+            out["delayed_acceptance_1_chain"]["accepted_moves_per_s"] /
+            out["exact_1_chain"]["accepted_moves_per_s"])
+    finally:
+        net.close()
+        box.close()
+    return out
 
 
 def run_ours(args, world, rank, local):
@@ -280,7 +349,7 @@ def run_ours(args, world, rank, local):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
-    rec = box.run_md(K, nlist_freq=nl, first_step=first)
+    box.run_md(K, nlist_freq=nl, first_step=first, record=False)
     ev1.record(stream)
     torch.cuda.synchronize()
     barrier(world)
@@ -302,6 +371,7 @@ def run_ours(args, world, rank, local):
     # plain FP64 drop-in on the same workload (the 10x denominator), a few steps
     fp64 = None
     force_err = None
+    b64 = None
     if rank == 0:
         b64 = engine.Box(sysm, precision=engine.FE_PREC_FP64, device=local)
         b64.set_stream(stream.cuda_stream)
@@ -323,7 +393,6 @@ def run_ours(args, world, rank, local):
         e1.record(stream)
         torch.cuda.synchronize()
         fp64 = n * k64 / (e0.elapsed_time(e1) / 1000.0)
-        b64.close()
     # end to end through the C ABI with host buffers (pinned)
     ke = min(K, 30)
     pos_h = torch.empty((n, 3), dtype=torch.float64, pin_memory=True).numpy()
@@ -363,6 +432,31 @@ def run_ours(args, world, rank, local):
     e2e = world * n * ke / t_e2e
     h2d = 4 * 24 * n
     d2h = 5 * 24 * n + 8 * engine.FE_EN_COUNT
+    # accuracy along one continuous trajectory: mixed-precision forces against
+    # the FP64 engine on the same coordinates at steps 0, 1,000 and 10,000;
+    # energy drift over steps 1,000..10,000
+    accuracy = None
+    if b64 is not None:
+        def fp64_error():
+            b64.set_positions(box.get_positions())
+            b64.nblist()
+            b64.forces()
+            f64 = b64.get_forces()
+            d = box.get_forces() - f64
+            return {"rms_rel": float(np.sqrt((d ** 2).sum() / (f64 ** 2).sum())),
+                    "max_abs": float(np.abs(d).max())}
+        done = W + K + ke
+        if done < 1000:
+            box.run_md(1000 - done, nlist_freq=nl, first_step=done + 1, record=False)
+        err1k = fp64_error()
+        rec_long = box.run_md(9000, nlist_freq=nl, first_step=1001, record=True)
+        err10k = fp64_error()
+        accuracy = {"force_error_vs_fp64": {"step_0": {k: force_err[k] for k in
+                                                        ("rms_rel", "max_abs")},
+                                            "step_1000": err1k, "step_10000": err10k,
+                                            "unit_max_abs": "kJ/mol/A"},
+                    "nve_drift": nve_drift(rec_long, sysm)}
+        b64.close()
     box.close()
     if rank != 0:
         return
@@ -375,11 +469,14 @@ def run_ours(args, world, rank, local):
             cpu = {"value": None, "unit": METRIC, "cores": 1, "kind": "port",
                    "sample": f"failed: {exc}"}
     steps_per_s = K / (ms_max / 1000.0)
-    drift = nve_drift(rec, sysm)
     try:
         batched = batched_sample(local, steps=min(max(K, 100), 500))
     except Exception as exc:  # the headline line must still print
         batched = {"failed": str(exc)}
+    try:
+        mc = mc_sample(local)
+    except Exception as exc:
+        mc = {"failed": str(exc)}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
@@ -400,9 +497,9 @@ def run_ours(args, world, rank, local):
         "clocks": clk,
         "fp64_drop_in": {"value": fp64, "unit": METRIC,
                          "ratio": (value / world) / fp64 if fp64 else None},
-        "force_error": force_err,
-        "nve_drift": drift,
+        "accuracy": accuracy,
         "batched_replicas": batched,
+        "mc": mc,
     }
     print(json.dumps(line))
 

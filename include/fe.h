@@ -252,8 +252,10 @@ int fe_mc_chains_run(fe_box *box, int64_t nmoves);
 int fe_mc_chains_state(fe_box *box, int chain, double *xyz, int64_t *moves, int64_t *accepted);
 /* Reciprocal energy sum_k c_k |S_k|^2 of a chain from its running S(k) [kJ/mol]. */
 int fe_mc_chains_kspace_energy(fe_box *box, int chain, double *e);
-/* Logged moves of chain 0: rec[8] per move = {2 lb + is_rotation, sites, accepted, dE,
- * dE_k, dE_real, u, move number}; fx[24] per move = trial fixed-point coordinates
+/* Logged moves of chain 0: rec[12] per move = {2 lb + is_rotation, sites,
+ * accepted, dE, dE_k (both NaN when not evaluated), dE_real, u1, dE1 (stage-1
+ * energy; dE in exact mode), u2, stage-1 accepted, dE_k evaluated, surrogate
+ * g(after) - g(before)}; fx[24] per move = trial fixed-point coordinates
  * (x, y, z per site; position = (u / 2^32 - 0.5) L). */
 int fe_mc_chains_log(fe_box *box, double *rec, uint32_t *fx, int64_t cap, int64_t *count);
 
@@ -280,6 +282,32 @@ int fe_mlp_grad(fe_mlp *mlp, const float *data, const float *y, int B, float *gr
  * loss_hist[e] = mean batch loss of epoch e. */
 int fe_mlp_train(fe_mlp *mlp, const float *data, const float *y, int64_t n, int epochs, int batch,
                  float lr, uint64_t seed, float *loss_hist);
+/* Delayed acceptance for the MC chains (Christen & Fox 2005).  Stage 1
+ * accepts with min(1, exp(-beta dE1)), dE1 = exact real-space + LJ dE plus
+ * the surrogate's g(after) - g(before) for the reciprocal part; only then is
+ * the exact reciprocal dE_k computed and stage 2 accepts with
+ * min(1, exp(-beta (dE - dE1))).  The surrogate's difference form is
+ * antisymmetric under reversing a move, so the chain keeps exact detailed
+ * balance for the full Ewald energy.  Descriptors (64 per configuration):
+ * for each moved site and partner within 9 A, the partner charge spread
+ * over 16 tent functions of r centred at 1.0, 1.5, .., 8.5 A, in 4 channels
+ * (site charge sign x partner charge sign). */
+/* Store (descriptors before, after, exact dE_k) of up to per_chain moves of
+ * every chain (0 = stop collecting); under delayed acceptance the last value
+ * is the surrogate's estimate instead of dE_k. */
+int fe_mc_chains_collect(fe_box *box, int64_t per_chain);
+/* Collected samples, 129 floats each, chain after chain (out may be NULL). */
+int fe_mc_chains_samples(fe_box *box, float *out, int64_t cap, int64_t *count);
+/* Trains the network on the collected samples without leaving the device. */
+int fe_mc_chains_train_surrogate(fe_box *box, fe_mlp *mlp, int epochs, int batch, float lr,
+                                 uint64_t seed, float *loss_hist);
+/* Copies the network into the chains (bf16 weights, FP32 arithmetic in the kernel). */
+int fe_mc_chains_set_surrogate(fe_box *box, fe_mlp *mlp);
+/* 0: exact dE in one stage; 1: delayed acceptance (after set_surrogate). */
+int fe_mc_chains_set_mode(fe_box *box, int mode);
+/* {moves, accepted, stage-1 accepted, exact reciprocal evaluations} of a chain. */
+int fe_mc_chains_stats(fe_box *box, int chain, int64_t *out4);
+
 /* The tensor-core GEMM alone: D (M x N fp32) = A (M x K) B (N x K)^T + bias,
  * A and B as bf16 bit patterns; M % 128 == 0, N in 32..256 step 32,
  * K % 64 == 0. */

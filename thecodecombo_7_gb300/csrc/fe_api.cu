@@ -668,7 +668,9 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
     return FE_ERR_STATE;
   }
   if (nsteps == 0) return FE_OK;
-  if (b->rec_cap < nsteps) {
+  // records go to the host only when asked; without `rec` the graphs keep
+  // whatever record buffer they were captured with (the kernel stops at its end)
+  if (rec && b->rec_cap < nsteps) {
     if (b->rec) cudaFree(b->rec);
     b->rec = nullptr;
     FE_CUDA(cudaMalloc(&b->rec, sizeof(double) * FE_EN_COUNT * (size_t)nsteps));

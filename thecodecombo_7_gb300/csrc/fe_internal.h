@@ -15,6 +15,7 @@ namespace fe {
 
 struct Mixed;
 struct McChains;
+struct Mlp;
 
 // Physical constants of the reference (defines.h:62-75).
 constexpr double kPI = 3.141592653589793238462643383;
@@ -210,6 +211,10 @@ int mc_kspace_energy(Box *b, double *e);
 void mc_free(Box *b);
 // k_mcrun.cu
 void mcc_free(Box *b);
+// k_mlp.cu: train the surrogate on device-resident samples
+int mlp_train_device(Mlp *m, const float *data, const float *y, long long n, int epochs, int B,
+                     float lr, uint64_t seed, float *loss_hist);
+Mlp *mlp_from_handle(fe_mlp *h);
 
 }  // namespace fe
 

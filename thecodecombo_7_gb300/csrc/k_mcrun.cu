@@ -40,7 +40,10 @@ constexpr int kMccMaxSites = 8;   // sites per molecule
 constexpr int kMccMaxTypes = 8;
 constexpr int kMccMaxK = kMccThreads;  // one k-vector per thread
 constexpr int kMccMaxN = 10240;   // sites per chain (shared-memory state)
-constexpr int kMccLogD = 8;       // doubles per logged move
+constexpr int kMccLogD = 12;      // doubles per logged move
+constexpr int kMlpInputs = 64, kMlpHidden = 128;  // surrogate network (k_mlp.cu)
+// b1, b2, w3, b3, input mean, input 1/std
+constexpr int kMlpFb = 3 * kMlpHidden + 1 + 2 * kMlpInputs;
 constexpr long long kMccChunk = 16384;  // moves per launch
 
 struct MccParams {
@@ -54,6 +57,10 @@ struct MccParams {
   double p_rot;      // probability that a move is a rotation
   uint64_t seed;
   int log_cap;
+  int mode;          // 0: exact dE; 1: delayed acceptance with the surrogate
+  int desc;          // descriptors computed (mode 1 or sample collection)
+  int collect;       // store (descriptors, exact dE_k) samples in mode 0
+  long long sample_cap;  // samples per chain
 };
 
 struct MccDev {
@@ -68,13 +75,18 @@ struct MccDev {
   long long *moves, *accepted;  // nchains
   double *log;              // log_cap * kMccLogD (chain 0)
   unsigned *log_fx;         // log_cap * kMccMaxSites * 3
+  long long *stats;         // nchains * 2: stage-1 accepts, exact k-space evaluations
+  float *samples;           // nchains * sample_cap * 129
+  long long *nsamples;      // nchains
+  const unsigned short *w1t;  // surrogate, bf16: W1 (input-normalised) transposed [64][128]
+  const unsigned short *w2t;  // W2 transposed [128][128]
+  const float *fb;          // b1, b2, w3, b3, input mean, input 1/std
 };
 
 struct McChains {
   int nchains = 0;
   MccParams P{};
   MccDev D{};
-  size_t smem = 0;
   int kmax = 0, mks = 0;
   double rc_ew = 0.0;
   std::vector<int> mol_first;
@@ -144,9 +156,50 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float x) {
   lo = e - (hi - s);
 }
 
+__device__ __forceinline__ float bf16_to_f(unsigned short h) {
+  return __uint_as_float((uint32_t)h << 16);
+}
+
+__device__ __forceinline__ float silu_f(float z) { return z / (1.f + __expf(-z)); }
+
+// Block-wide sums of two floats in a fixed order; every thread gets both.
+__device__ __forceinline__ void block_sum2(float &a, float &b, float *ra, float *rb) {
+  const int tid = threadIdx.x;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_xor_sync(0xffffffffu, a, o);
+    b += __shfl_xor_sync(0xffffffffu, b, o);
+  }
+  if ((tid & 31) == 0) {
+    ra[tid >> 5] = a;
+    rb[tid >> 5] = b;
+  }
+  __syncthreads();
+  if (tid < 32) {
+    a = tid < (int)(blockDim.x >> 5) ? ra[tid] : 0.f;
+    b = tid < (int)(blockDim.x >> 5) ? rb[tid] : 0.f;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_xor_sync(0xffffffffu, a, o);
+      b += __shfl_xor_sync(0xffffffffu, b, o);
+    }
+    if (tid == 0) {
+      ra[32] = a;
+      rb[32] = b;
+    }
+  }
+  __syncthreads();
+  a = ra[32];
+  b = rb[32];
+}
+
+// Descriptor bin of a pair at distance r: tent functions centred at
+// kDescR0 + k * kDescDr (k = 0..15), weighted by the partner's charge.
+constexpr float kDescR0 = 1.0f, kDescDr = 0.5f, kDescRmax = 9.0f, kDescScale = 65536.f;
+
 // All per-move arithmetic is FP32 (GB300's FP64 rate is a small fraction of
-// its FP32 rate): pair energies, phases, the block reduction, the proposal
-// and the Metropolis test.  S(k) is carried as a float pair so that
+// its FP32 rate): pair energies, phases, the block reductions, the proposal
+// and the Metropolis tests.  S(k) is carried as a float pair so that
 // thousands of accepted increments do not drift.
 __global__ void __launch_bounds__(kMccThreads, 1)
 k_mcc_run(MccParams P, MccDev D, long long nmoves) {
@@ -155,13 +208,19 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
   float *sm_lj = (float *)(sm_typ + ((P.n + 15) & ~15));
   int *sm_cand = (int *)(sm_lj + ((P.nt * P.nt * 3 + 3) & ~3));  // 32 * chunk
   const int chunk = ((P.n + 31) / 32 + 31) & ~31;                   // sites per warp
+  int *sm_hist = sm_cand + 32 * chunk;                               // 32 x 128 (descriptors)
+  unsigned short *sm_w1t = (unsigned short *)(sm_hist + (P.desc ? 32 * 2 * kMlpInputs : 0));
+  unsigned short *sm_w2t = sm_w1t + kMlpInputs * kMlpHidden;
+  float *sm_fb = (float *)(sm_w2t + kMlpHidden * kMlpHidden);       // kMlpFb floats
   __shared__ unsigned mv_old[kMccMaxSites][3], mv_new[kMccMaxSites][3];
   __shared__ float mv_q[kMccMaxSites];
   __shared__ int mv_t[kMccMaxSites];
-  __shared__ int mv_lb, mv_m, mv_rot, decision;
-  __shared__ float mv_u, mv_scr2;
-  __shared__ float red_a[32], red_b[32];
+  __shared__ int mv_lb, mv_m, mv_rot, decision, stage1;
+  __shared__ float mv_u, mv_u2, mv_scr2;
+  __shared__ float red_a[33], red_b[33];
   __shared__ int cand_cnt[32], cand_off[33];
+  __shared__ float sm_desc[2][kMlpInputs];
+  __shared__ float sm_h1[2][kMlpHidden];
 
   const int chain = blockIdx.x;
   const int tid = threadIdx.x;
@@ -171,6 +230,13 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
     sm_typ[i] = D.type[i];
   }
   for (int i = tid; i < P.nt * P.nt * 3; i += blockDim.x) sm_lj[i] = D.lj[i];
+  if (P.desc)
+    for (int i = tid; i < 32 * 2 * kMlpInputs; i += blockDim.x) sm_hist[i] = 0;
+  if (P.mode == 1) {
+    for (int i = tid; i < kMlpInputs * kMlpHidden; i += blockDim.x) sm_w1t[i] = D.w1t[i];
+    for (int i = tid; i < kMlpHidden * kMlpHidden; i += blockDim.x) sm_w2t[i] = D.w2t[i];
+    for (int i = tid; i < kMlpFb; i += blockDim.x) sm_fb[i] = D.fb[i];
+  }
   int kx = 0, ky = 0, kz = 0;
   float ck = 0.f, Sxh = 0.f, Sxl = 0.f, Syh = 0.f, Syl = 0.f;
   if (tid < P.nk) {
@@ -186,8 +252,10 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
     Syl = (float)(S.y - (double)Syh);
   }
   const float invx = 1.0f / P.sLf[0], invy = 1.0f / P.sLf[1], invz = 1.0f / P.sLf[2];
+  const float beta = (float)P.beta;
   long long move0 = D.moves[chain];
-  long long nacc = 0;
+  long long nacc = 0, n_s1 = 0, n_k = 0;
+  long long nsamp = P.collect ? D.nsamples[chain] : 0;
   __syncthreads();
 
   for (long long it = 0; it < nmoves; ++it) {
@@ -280,6 +348,7 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
       mv_m = m;
       mv_rot = rot;
       mv_u = u32_uniform_f(r1.v[0]);
+      mv_u2 = u32_uniform_f(r1.v[1]);
     }
     __syncthreads();
     const int lb = mv_lb, m = mv_m;
@@ -327,6 +396,7 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
     // ---- real space, pass 2: (candidate, site, old/new) items over all threads ----
     float de = 0.f;
     {
+      int *hist = sm_hist + (tid >> 5) * 2 * kMlpInputs;
       const int per = 2 * m, items = cand_off[32] * per;
       for (int t = tid; t < items; t += blockDim.x) {
         int ci = t / per, rest = t - ci * per;
@@ -337,8 +407,9 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
           if (w + step < 32 && cand_off[w + step] <= ci) w += step;
         int j = sm_cand[w * chunk + (ci - cand_off[w])];
         int4 pj = sm_pos[j];
+        float qj = __int_as_float(pj.w);
         const float *lj = sm_lj + (mv_t[i] * P.nt + sm_typ[j]) * 3;
-        float qq = mv_q[i] * __int_as_float(pj.w) * P.fconv;
+        float qq = mv_q[i] * qj * P.fconv;
         const unsigned *u = isnew ? mv_new[i] : mv_old[i];
         float dx = (float)(int)(u[0] - (unsigned)pj.x) * P.sLf[0];
         float dy = (float)(int)(u[1] - (unsigned)pj.y) * P.sLf[1];
@@ -348,67 +419,136 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
           float e = mcc_pair(P, r2, qq, lj);
           de += isnew ? e : -e;
         }
-      }
-    }
-    // ---- reciprocal space: this thread's k-vector ----
-    float dk = 0.f, dSx = 0.f, dSy = 0.f;
-    if (tid < P.nk) {
-      for (int i = 0; i < m; i++) {
-        uint32_t po = (uint32_t)kx * mv_old[i][0] + (uint32_t)ky * mv_old[i][1] +
-                      (uint32_t)kz * mv_old[i][2];
-        uint32_t pn = (uint32_t)kx * mv_new[i][0] + (uint32_t)ky * mv_new[i][1] +
-                      (uint32_t)kz * mv_new[i][2];
-        float so, co, sn, cn;
-        phase_sincos(po, so, co);
-        phase_sincos(pn, sn, cn);
-        dSx = fmaf(mv_q[i], cn - co, dSx);
-        dSy = fmaf(mv_q[i], sn - so, dSy);
-      }
-      // |S + dS|^2 - |S|^2 = 2 Re(conj(S) dS) + |dS|^2
-      dk = ck * (2.f * (Sxh * dSx + Syh * dSy) + dSx * dSx + dSy * dSy);
-    }
-    // ---- fixed-order block reduction of (dE_real, dE_k) ----
-    float a = de, b = dk;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      a += __shfl_xor_sync(0xffffffffu, a, o);
-      b += __shfl_xor_sync(0xffffffffu, b, o);
-    }
-    if ((tid & 31) == 0) {
-      red_a[tid >> 5] = a;
-      red_b[tid >> 5] = b;
-    }
-    __syncthreads();
-    if (tid < 32) {
-      a = tid < (int)(blockDim.x >> 5) ? red_a[tid] : 0.f;
-      b = tid < (int)(blockDim.x >> 5) ? red_b[tid] : 0.f;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        a += __shfl_xor_sync(0xffffffffu, a, o);
-        b += __shfl_xor_sync(0xffffffffu, b, o);
-      }
-      if (tid == 0) {
-        float dE = a + b;
-        float arg = -dE * (float)P.beta;  // (U_initial - U_final) * beta
-        int acc = (arg > 0.f) ? 1 : (__expf(arg) > mv_u ? 1 : 0);
-        decision = acc;
-        if (chain == 0 && it < (long long)P.log_cap && D.log) {
-          double *L = D.log + (size_t)it * kMccLogD;
-          L[0] = (double)((mv_lb << 1) | mv_rot);
-          L[1] = (double)m;
-          L[2] = (double)acc;
-          L[3] = (double)dE;
-          L[4] = (double)b;
-          L[5] = (double)a;
-          L[6] = (double)mv_u;
-          L[7] = (double)mv;
-          unsigned *F = D.log_fx + (size_t)it * kMccMaxSites * 3;
-          for (int i = 0; i < m; i++)
-            for (int c = 0; c < 3; c++) F[i * 3 + c] = mv_new[i][c];
+        if (P.desc && r2 < kDescRmax * kDescRmax) {
+          // 4 channels (site charge sign x partner charge sign) x 16 tents
+          float x = (sqrtf(r2) - kDescR0) * (1.f / kDescDr);
+          int k0 = x < 0.f ? 0 : (int)x;
+          float f = x < 0.f ? 0.f : x - (float)k0;
+          int base = isnew * kMlpInputs + ((mv_q[i] < 0.f ? 0 : 2) + (qj < 0.f ? 0 : 1)) * 16;
+          if (k0 < 16) atomicAdd(&hist[base + k0], __float2int_rn((1.f - f) * qj * kDescScale));
+          if (k0 + 1 < 16) atomicAdd(&hist[base + k0 + 1], __float2int_rn(f * qj * kDescScale));
         }
       }
     }
+    float g_part = 0.f;
+    if (P.desc) {
+      __syncthreads();
+      if (tid < 2 * kMlpInputs) {
+        int s = 0;
+        for (int w = 0; w < 32; w++) {
+          s += sm_hist[w * 2 * kMlpInputs + tid];
+          sm_hist[w * 2 * kMlpInputs + tid] = 0;
+        }
+        sm_desc[tid / kMlpInputs][tid % kMlpInputs] = (float)s * (1.f / kDescScale);
+      }
+      __syncthreads();
+      if (P.mode == 1) {
+        // surrogate: rows 0 (before) and 1 (after), one hidden unit per thread
+        if (tid < 2 * kMlpHidden) {
+          int r = tid / kMlpHidden, u = tid % kMlpHidden;
+          const float *mean = sm_fb + 3 * kMlpHidden + 1, *istd = mean + kMlpInputs;
+          float h = sm_fb[u];
+#pragma unroll 8
+          for (int i = 0; i < kMlpInputs; i++)
+            h = fmaf(bf16_to_f(sm_w1t[i * kMlpHidden + u]), (sm_desc[r][i] - mean[i]) * istd[i], h);
+          sm_h1[r][u] = silu_f(h);
+        }
+        __syncthreads();
+        if (tid < 2 * kMlpHidden) {
+          int r = tid / kMlpHidden, u = tid % kMlpHidden;
+          float h = sm_fb[kMlpHidden + u];
+#pragma unroll 8
+          for (int v = 0; v < kMlpHidden; v++)
+            h = fmaf(bf16_to_f(sm_w2t[v * kMlpHidden + u]), sm_h1[r][v], h);
+          float o = sm_fb[2 * kMlpHidden + u] * silu_f(h);
+          g_part = r ? o : -o;  // g(after) - g(before); b3 cancels
+        }
+      }
+    }
+    // ---- stage 1 (delayed acceptance) or the single exact stage ----
+    float dk = 0.f, dSx = 0.f, dSy = 0.f, ghat = 0.f, dE1 = 0.f;
+    if (P.mode == 1) {
+      float a = de, b = g_part;
+      block_sum2(a, b, red_a, red_b);
+      de = a;
+      ghat = b;
+      dE1 = de + ghat;
+      if (tid == 0) {
+        float arg = -dE1 * beta;
+        stage1 = (arg > 0.f) ? 1 : (__expf(arg) > mv_u ? 1 : 0);
+      }
+      __syncthreads();
+    } else {
+      if (tid == 0) stage1 = 1;
+    }
+    const bool need_k = (P.mode == 0) || stage1;
+    if (need_k) {
+      if (tid < P.nk) {
+        for (int i = 0; i < m; i++) {
+          uint32_t po = (uint32_t)kx * mv_old[i][0] + (uint32_t)ky * mv_old[i][1] +
+                        (uint32_t)kz * mv_old[i][2];
+          uint32_t pn = (uint32_t)kx * mv_new[i][0] + (uint32_t)ky * mv_new[i][1] +
+                        (uint32_t)kz * mv_new[i][2];
+          float so, co, sn, cn;
+          phase_sincos(po, so, co);
+          phase_sincos(pn, sn, cn);
+          dSx = fmaf(mv_q[i], cn - co, dSx);
+          dSy = fmaf(mv_q[i], sn - so, dSy);
+        }
+        // |S + dS|^2 - |S|^2 = 2 Re(conj(S) dS) + |dS|^2
+        dk = ck * (2.f * (Sxh * dSx + Syh * dSy) + dSx * dSx + dSy * dSy);
+      }
+      float a = (P.mode == 0) ? de : 0.f, b = dk;
+      block_sum2(a, b, red_a, red_b);
+      if (P.mode == 0) de = a;
+      dk = b;
+    }
+    if (tid == 0) {
+      int acc;
+      float dE = de + dk;
+      if (P.mode == 0) {
+        float arg = -dE * beta;  // (U_initial - U_final) * beta, mcmove_displ.c:130-137
+        acc = (arg > 0.f) ? 1 : (__expf(arg) > mv_u ? 1 : 0);
+        dE1 = dE;
+      } else if (stage1) {
+        // second stage: min(1, exp(-beta (dE - dE1))) with the exact dE
+        float arg = -(dk - ghat) * beta;
+        acc = (arg > 0.f) ? 1 : (__expf(arg) > mv_u2 ? 1 : 0);
+      } else {
+        acc = 0;
+      }
+      decision = acc;
+      if (chain == 0 && it < (long long)P.log_cap && D.log) {
+        double *L = D.log + (size_t)it * kMccLogD;
+        double nan = __longlong_as_double(0x7ff8000000000000ll);
+        L[0] = (double)((mv_lb << 1) | mv_rot);
+        L[1] = (double)m;
+        L[2] = (double)acc;
+        L[3] = need_k ? (double)dE : nan;
+        L[4] = need_k ? (double)dk : nan;
+        L[5] = (double)de;
+        L[6] = (double)mv_u;
+        L[7] = (double)dE1;
+        L[8] = (double)mv_u2;
+        L[9] = (double)stage1;
+        L[10] = (double)(need_k ? 1 : 0);
+        L[11] = (double)ghat;
+        unsigned *F = D.log_fx + (size_t)it * kMccMaxSites * 3;
+        for (int i = 0; i < m; i++)
+          for (int c = 0; c < 3; c++) F[i * 3 + c] = mv_new[i][c];
+      }
+    }
+    // samples: descriptors before / after and the exact dE_k (exact mode) or
+    // the surrogate's estimate (delayed acceptance)
+    if (P.collect && nsamp < P.sample_cap) {
+      float *smp = D.samples + ((size_t)chain * P.sample_cap + nsamp) * (2 * kMlpInputs + 1);
+      if (tid < 2 * kMlpInputs) smp[tid] = sm_desc[tid / kMlpInputs][tid % kMlpInputs];
+      if (tid == 2 * kMlpInputs) smp[tid] = P.mode == 0 ? dk : ghat;
+      nsamp++;
+    }
     __syncthreads();
+    if (stage1) n_s1++;
+    if (need_k) n_k++;
     if (decision) {
       if (tid < P.nk) {
         ff_add(Sxh, Sxl, dSx);
@@ -432,6 +572,9 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
   if (tid == 0) {
     D.moves[chain] = move0 + nmoves;
     D.accepted[chain] += nacc;
+    D.stats[2 * chain] += n_s1;
+    D.stats[2 * chain + 1] += n_k;
+    if (P.collect) D.nsamples[chain] = nsamp;
   }
 }
 
@@ -447,7 +590,8 @@ void mcc_free(Box *b) {
   if (!M) return;
   void *ptrs[] = {M->D.posfx, M->D.S, (void *)M->D.kv, (void *)M->D.ck, (void *)M->D.mol_first,
                   (void *)M->D.type, (void *)M->D.mass, (void *)M->D.lj, M->D.moves,
-                  M->D.accepted, M->D.log, M->D.log_fx};
+                  M->D.accepted, M->D.log, M->D.log_fx, M->D.stats, M->D.samples,
+                  M->D.nsamples, (void *)M->D.w1t, (void *)M->D.w2t, (void *)M->D.fb};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   delete M;
@@ -622,11 +766,34 @@ static int mcc_setup(Box *b, int nchains, const int *mol_first, int nmol, int km
   FE_CUDA(cudaMemcpy((void *)D.lj, lj.data(), sizeof(float) * nt * nt * 3, cudaMemcpyHostToDevice));
   FE_CUDA(cudaMemset(D.moves, 0, sizeof(long long) * nchains));
   FE_CUDA(cudaMemset(D.accepted, 0, sizeof(long long) * nchains));
+  FE_CUDA(cudaMalloc(&D.stats, sizeof(long long) * 2 * nchains));
+  FE_CUDA(cudaMemset(D.stats, 0, sizeof(long long) * 2 * nchains));
+  P.mode = 0;
+  P.desc = 0;
+  P.collect = 0;
+  P.sample_cap = 0;
+  return FE_OK;
+}
+
+// dynamic shared memory of k_mcc_run for the current flags
+static size_t mcc_smem(const MccParams &P) {
+  int n = P.n, nt = P.nt;
   int chunk = ((n + 31) / 32 + 31) & ~31;
-  M->smem = sizeof(int4) * (size_t)n + (size_t)((n + 15) & ~15) +
-            sizeof(float) * (size_t)((nt * nt * 3 + 3) & ~3) + sizeof(int) * 32 * (size_t)chunk;
-  FE_CUDA(cudaFuncSetAttribute(k_mcc_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)M->smem));
+  size_t s = sizeof(int4) * (size_t)n + (size_t)((n + 15) & ~15) +
+             sizeof(float) * (size_t)((nt * nt * 3 + 3) & ~3) + sizeof(int) * 32 * (size_t)chunk;
+  if (P.desc) s += sizeof(int) * 32 * 2 * kMlpInputs;
+  if (P.mode == 1)
+    s += 2 * (size_t)(kMlpInputs * kMlpHidden + kMlpHidden * kMlpHidden) + sizeof(float) * kMlpFb;
+  return s;
+}
+
+constexpr size_t kMccSmemMax = 227 * 1024 - 4096;  // dynamic part; static shared ~3 KB
+
+static int mcc_check_smem(const MccParams &P) {
+  if (mcc_smem(P) > kMccSmemMax) {
+    set_error("fe_mc_chains: too many sites for this mode's shared-memory state");
+    return FE_ERR_SIZE;
+  }
   return FE_OK;
 }
 
@@ -654,7 +821,10 @@ static int mcc_run(Box *b, long long nmoves) {
     } else {
       P.log_cap = 0;
     }
-    k_mcc_run<<<M->nchains, kMccThreads, M->smem, b->stream>>>(P, D, c);
+    size_t smem = mcc_smem(P);
+    FE_CUDA(cudaFuncSetAttribute(k_mcc_run, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)smem));
+    k_mcc_run<<<M->nchains, kMccThreads, smem, b->stream>>>(P, D, c);
     FE_LAUNCH_CHECK("k_mcc_run");
     done += c;
   }
@@ -719,6 +889,192 @@ int fe_mc_chains_kspace_energy(fe_box *box, int chain, double *e) {
   double s = 0.0;
   for (int k = 0; k < nk; k++) s += ck[k] * (S[k].x * S[k].x + S[k].y * S[k].y);
   *e = s;
+  return FE_OK;
+}
+
+int fe_mc_chains_collect(fe_box *box, int64_t per_chain) {
+  if (!box || !box->b.mcc || per_chain < 0) return FE_ERR_ARG;
+  McChains *M = box->b.mcc;
+  if (M->D.samples) cudaFree(M->D.samples);
+  if (M->D.nsamples) cudaFree(M->D.nsamples);
+  M->D.samples = nullptr;
+  M->D.nsamples = nullptr;
+  M->P.collect = 0;
+  M->P.sample_cap = 0;
+  M->P.desc = M->P.mode == 1 ? 1 : 0;
+  if (per_chain == 0) return FE_OK;
+  MccParams P = M->P;
+  P.desc = 1;
+  int rc = mcc_check_smem(P);
+  if (rc) return rc;
+  FE_CUDA(cudaMalloc(&M->D.samples, sizeof(float) * (2 * kMlpInputs + 1) * (size_t)per_chain *
+                                        M->nchains));
+  FE_CUDA(cudaMalloc(&M->D.nsamples, sizeof(long long) * M->nchains));
+  FE_CUDA(cudaMemset(M->D.nsamples, 0, sizeof(long long) * M->nchains));
+  M->P.collect = 1;
+  M->P.desc = 1;
+  M->P.sample_cap = per_chain;
+  return FE_OK;
+}
+
+// samples of every chain, chain after chain: out rows of 129 floats
+// (64 descriptors before, 64 after, exact dE_k)
+int fe_mc_chains_samples(fe_box *box, float *out, int64_t cap, int64_t *count) {
+  if (!box || !box->b.mcc) return FE_ERR_STATE;
+  McChains *M = box->b.mcc;
+  FE_CUDA(cudaStreamSynchronize(box->b.stream));
+  int64_t total = 0;
+  if (M->D.nsamples) {
+    std::vector<long long> ns(M->nchains);
+    FE_CUDA(cudaMemcpy(ns.data(), M->D.nsamples, sizeof(long long) * M->nchains,
+                       cudaMemcpyDeviceToHost));
+    const size_t row = 2 * kMlpInputs + 1;
+    for (int c = 0; c < M->nchains; c++) {
+      long long k = ns[c];
+      if (out && total + k > cap) k = cap - total;
+      if (out && k > 0)
+        FE_CUDA(cudaMemcpy(out + (size_t)total * row,
+                           M->D.samples + (size_t)c * M->P.sample_cap * row,
+                           sizeof(float) * row * (size_t)k, cudaMemcpyDeviceToHost));
+      total += k > 0 ? k : 0;
+    }
+  }
+  if (count) *count = total;
+  return FE_OK;
+}
+
+__global__ void k_mcc_split(long long n, const float *__restrict__ rows, float *__restrict__ data,
+                            float *__restrict__ y) {
+  long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n * 129) return;
+  long long r = t / 129;
+  int f = (int)(t % 129);
+  if (f < 128) data[r * 128 + f] = rows[t];
+  else y[r] = rows[t];
+}
+
+// Trains `mlp` on the collected samples of every chain (on the device).
+int fe_mc_chains_train_surrogate(fe_box *box, fe_mlp *mlp, int epochs, int batch, float lr,
+                                 uint64_t seed, float *loss_hist) {
+  if (!box || !box->b.mcc || !mlp) return FE_ERR_ARG;
+  McChains *M = box->b.mcc;
+  if (!M->D.nsamples) {
+    set_error("fe_mc_chains_train_surrogate: no samples collected");
+    return FE_ERR_STATE;
+  }
+  FE_CUDA(cudaStreamSynchronize(box->b.stream));
+  std::vector<long long> ns(M->nchains);
+  FE_CUDA(cudaMemcpy(ns.data(), M->D.nsamples, sizeof(long long) * M->nchains,
+                     cudaMemcpyDeviceToHost));
+  long long total = 0;
+  for (long long k : ns) total += k;
+  if (total < batch) {
+    set_error("fe_mc_chains_train_surrogate: fewer samples than one batch");
+    return FE_ERR_STATE;
+  }
+  const size_t row = 2 * kMlpInputs + 1;
+  float *rows = nullptr, *data = nullptr, *y = nullptr;
+  int rc = FE_OK;
+  cudaError_t e = cudaMalloc(&rows, sizeof(float) * row * (size_t)total);
+  if (e == cudaSuccess) e = cudaMalloc(&data, sizeof(float) * 128 * (size_t)total);
+  if (e == cudaSuccess) e = cudaMalloc(&y, sizeof(float) * (size_t)total);
+  long long off = 0;
+  for (int c = 0; c < M->nchains && e == cudaSuccess; c++) {
+    if (ns[c] > 0)
+      e = cudaMemcpy(rows + (size_t)off * row, M->D.samples + (size_t)c * M->P.sample_cap * row,
+                     sizeof(float) * row * (size_t)ns[c], cudaMemcpyDeviceToDevice);
+    off += ns[c];
+  }
+  if (e == cudaSuccess) {
+    long long th = total * 129;
+    k_mcc_split<<<(unsigned)((th + 255) / 256), 256>>>(total, rows, data, y);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaDeviceSynchronize();
+  if (e == cudaSuccess)
+    rc = mlp_train_device(mlp_from_handle(mlp), data, y, total, epochs, batch, lr, seed,
+                          loss_hist);
+  cudaFree(rows);
+  cudaFree(data);
+  cudaFree(y);
+  if (e != cudaSuccess) return cuda_fail(e, "fe_mc_chains_train_surrogate");
+  return rc;
+}
+
+// Loads the surrogate for delayed acceptance: bf16 W1 and W2 transposed,
+// fp32 biases, output weights and input normalisation.
+int fe_mc_chains_set_surrogate(fe_box *box, fe_mlp *mlp) {
+  if (!box || !box->b.mcc || !mlp) return FE_ERR_ARG;
+  McChains *M = box->b.mcc;
+  int np = fe_mlp_param_count();
+  std::vector<float> Pm(np), mean(kMlpInputs), istd(kMlpInputs);
+  int rc = fe_mlp_get_params(mlp, Pm.data(), mean.data(), istd.data());
+  if (rc) return rc;
+  const int H = kMlpHidden, I = kMlpInputs;
+  const float *W1 = Pm.data(), *b1 = W1 + H * I, *W2 = b1 + H, *b2 = W2 + H * H, *w3 = b2 + H,
+              *b3 = w3 + H;
+  std::vector<unsigned short> w1t(I * H), w2t(H * H);
+  std::vector<float> fb(kMlpFb);
+  auto to_bf16 = [](float f) -> unsigned short {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    u += 0x7FFFu + ((u >> 16) & 1u);
+    return (unsigned short)(u >> 16);
+  };
+  for (int u = 0; u < H; u++) {
+    for (int i = 0; i < I; i++) w1t[i * H + u] = to_bf16(W1[u * I + i]);
+    fb[u] = b1[u];
+    fb[H + u] = b2[u];
+    fb[2 * H + u] = w3[u];
+    for (int v = 0; v < H; v++) w2t[v * H + u] = to_bf16(W2[u * H + v]);
+  }
+  fb[3 * H] = b3[0];
+  for (int i = 0; i < I; i++) {
+    fb[3 * H + 1 + i] = mean[i];
+    fb[3 * H + 1 + I + i] = istd[i];
+  }
+  MccParams P = M->P;
+  P.mode = 1;
+  P.desc = 1;
+  if ((rc = mcc_check_smem(P))) return rc;
+  if (!M->D.w1t) {
+    FE_CUDA(cudaMalloc((void **)&M->D.w1t, 2 * (size_t)I * H));
+    FE_CUDA(cudaMalloc((void **)&M->D.w2t, 2 * (size_t)H * H));
+    FE_CUDA(cudaMalloc((void **)&M->D.fb, sizeof(float) * kMlpFb));
+  }
+  FE_CUDA(cudaMemcpy((void *)M->D.w1t, w1t.data(), 2 * (size_t)I * H, cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemcpy((void *)M->D.w2t, w2t.data(), 2 * (size_t)H * H, cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemcpy((void *)M->D.fb, fb.data(), sizeof(float) * kMlpFb, cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+// 0: exact dE (one stage); 1: delayed acceptance (needs a surrogate)
+int fe_mc_chains_set_mode(fe_box *box, int mode) {
+  if (!box || !box->b.mcc || (mode != 0 && mode != 1)) return FE_ERR_ARG;
+  McChains *M = box->b.mcc;
+  if (mode == 1 && !M->D.w1t) {
+    set_error("fe_mc_chains_set_mode: delayed acceptance needs fe_mc_chains_set_surrogate first");
+    return FE_ERR_STATE;
+  }
+  MccParams P = M->P;
+  P.mode = mode;
+  P.desc = (mode == 1 || P.collect) ? 1 : 0;
+  int rc = mcc_check_smem(P);
+  if (rc) return rc;
+  M->P = P;
+  return FE_OK;
+}
+
+int fe_mc_chains_stats(fe_box *box, int chain, int64_t *out4) {
+  if (!box || !box->b.mcc || !out4) return FE_ERR_ARG;
+  McChains *M = box->b.mcc;
+  if (chain < 0 || chain >= M->nchains) return FE_ERR_ARG;
+  FE_CUDA(cudaStreamSynchronize(box->b.stream));
+  long long v[4];
+  FE_CUDA(cudaMemcpy(&v[0], M->D.moves + chain, sizeof(long long), cudaMemcpyDeviceToHost));
+  FE_CUDA(cudaMemcpy(&v[1], M->D.accepted + chain, sizeof(long long), cudaMemcpyDeviceToHost));
+  FE_CUDA(cudaMemcpy(&v[2], M->D.stats + 2 * chain, 2 * sizeof(long long), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < 4; i++) out4[i] = v[i];
   return FE_OK;
 }
 

@@ -519,6 +519,10 @@ struct fe_mlp {
   Mlp m;
 };
 
+namespace fe {
+Mlp *mlp_from_handle(fe_mlp *h) { return &h->m; }
+}  // namespace fe
+
 extern "C" {
 
 int fe_mlp_create(fe_mlp **out, int device, uint64_t seed) {

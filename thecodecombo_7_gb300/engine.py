@@ -52,6 +52,8 @@ EXPORTS = [
     "fe_mc_chains_kspace_energy", "fe_mc_chains_log",
     "fe_mlp_create", "fe_mlp_destroy", "fe_mlp_param_count", "fe_mlp_set_params",
     "fe_mlp_get_params", "fe_mlp_grad", "fe_mlp_train", "fe_tc_gemm_bf16",
+    "fe_mc_chains_collect", "fe_mc_chains_samples", "fe_mc_chains_train_surrogate",
+    "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -121,6 +123,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
                                        C.c_double, C.c_uint64, C.c_int]
     lib.fe_mc_chains_run.argtypes = [C.c_void_p, C.c_int64]
     lib.fe_mc_chains_log.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.fe_mc_chains_collect.argtypes = [C.c_void_p, C.c_int64]
+    lib.fe_mc_chains_samples.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p]
+    lib.fe_mc_chains_train_surrogate.argtypes = [C.c_void_p, C.c_void_p, C.c_int, C.c_int,
+                                                 C.c_float, C.c_uint64, C.c_void_p]
+    lib.fe_mc_chains_set_surrogate.argtypes = [C.c_void_p, C.c_void_p]
+    lib.fe_mc_chains_set_mode.argtypes = [C.c_void_p, C.c_int]
+    lib.fe_mc_chains_stats.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
     _lib = lib
     return lib
 
@@ -396,8 +405,36 @@ class Box:
         self._check(self.lib.fe_mc_chains_kspace_energy(self.h, int(chain), C.byref(e)))
         return e.value
 
+    def mc_chains_collect(self, per_chain):
+        self._check(self.lib.fe_mc_chains_collect(self.h, int(per_chain)))
+
+    def mc_chains_samples(self):
+        cnt = C.c_int64()
+        self._check(self.lib.fe_mc_chains_samples(self.h, None, 0, C.byref(cnt)))
+        out = np.zeros((cnt.value, 129), np.float32)
+        self._check(self.lib.fe_mc_chains_samples(self.h, _p(out), cnt.value, C.byref(cnt)))
+        return out[:cnt.value]
+
+    def mc_chains_train_surrogate(self, mlp, epochs=20, batch=512, lr=1e-3, seed=1):
+        hist = np.empty(epochs, np.float32)
+        self._check(self.lib.fe_mc_chains_train_surrogate(self.h, mlp.h, int(epochs), int(batch),
+                                                          C.c_float(lr), C.c_uint64(seed),
+                                                          _p(hist)))
+        return hist
+
+    def mc_chains_set_surrogate(self, mlp):
+        self._check(self.lib.fe_mc_chains_set_surrogate(self.h, mlp.h))
+
+    def mc_chains_set_mode(self, mode):
+        self._check(self.lib.fe_mc_chains_set_mode(self.h, int(mode)))
+
+    def mc_chains_stats(self, chain=0):
+        v = np.zeros(4, np.int64)
+        self._check(self.lib.fe_mc_chains_stats(self.h, int(chain), _p(v)))
+        return dict(moves=int(v[0]), accepted=int(v[1]), stage1=int(v[2]), kspace=int(v[3]))
+
     def mc_chains_log(self, cap):
-        rec = np.zeros((cap, 8))
+        rec = np.zeros((cap, 12))
         fx = np.zeros((cap, 8, 3), np.uint32)
         cnt = C.c_int64()
         self._check(self.lib.fe_mc_chains_log(self.h, _p(rec), _p(fx), int(cap), C.byref(cnt)))
