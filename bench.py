@@ -251,6 +251,47 @@ def batched_sample(local, steps):
             "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]}}
 
 
+def go_sample(local):
+    """64 Go-model replicas (60-400 beads, seeded compact native structures),
+    Langevin NVT at temperatures geometric 280-450 K, exchange every 1,000
+    steps: one persistent launch per segment.  Timed: 5 segments (5,000
+    steps) with CUDA events on the batch stream; CPU port: one replica of
+    the same kind for a few steps on one thread."""
+    import torch
+
+    from oracle import oracle as orc
+    from thecodecombo_7_gb300 import engine, systems
+    g = systems.go_chains(64, seed=SEED)
+    b = engine.GoBatch(g, device=local, seed=SEED)
+    try:
+        b.run(1000, swap_freq=1000)
+        st = torch.cuda.ExternalStream(b.stream(), device=local)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        b.run(5000, swap_freq=1000)
+        e1.record(st)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1000.0
+        s = b.state()
+    finally:
+        b.close()
+    nb = int(g.nbeads.sum())
+    r = int(np.argmax(g.nbeads))
+    t0 = time.perf_counter()
+    orc.go_baoab(g, r, 20, seed=SEED)
+    cpu = int(g.nbeads[r]) * 20 / (time.perf_counter() - t0)
+    return {"value": nb * 5000 / sec, "unit": "bead-steps/s", "replicas": 64, "beads": nb,
+            "steps": 5000, "us_per_step": 1e6 * sec / 5000,
+            "exchange_attempts": int(s["attempted"].sum()),
+            "exchanges_accepted": int(s["accepted"].sum()),
+            "workload": "64 Go-model C-alpha chains (60-400 beads), bonds 3.8 A k=100 "
+                        "kcal/mol/A^2, natives 12-10 eps=1 kcal/mol, non-native (4 A/r)^12, "
+                        "BAOAB Langevin dt 10 fs gamma 1/ps, T 280-450 K geometric, exchange "
+                        "every 1,000 steps",
+            "cpu_port_bead_steps_per_s_1_thread": cpu}
+
+
 def mc_sample(local):
     """Monte Carlo on the 4,095-site box: exact-dE chains against delayed
     acceptance with the surrogate trained on 2x10^5 exact moves of the same
@@ -477,6 +518,10 @@ def run_ours(args, world, rank, local):
         mc = mc_sample(local)
     except Exception as exc:
         mc = {"failed": str(exc)}
+    try:
+        go = go_sample(local)
+    except Exception as exc:
+        go = {"failed": str(exc)}
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
@@ -500,6 +545,7 @@ def run_ours(args, world, rank, local):
         "accuracy": accuracy,
         "batched_replicas": batched,
         "mc": mc,
+        "go_replicas": go,
     }
     print(json.dumps(line))
 

@@ -344,6 +344,49 @@ int fe_batch_get_stream(fe_batch *batch, void **stream);
  * -1 for a variant not captured yet. */
 int fe_batch_step_launches(fe_batch *batch, int *launches4);
 
+/* ---- batched replica exchange of Go-model chains ------------------------ */
+
+/* nrep C-alpha chains (one per replica, 2..1024 beads each) stepped with
+ * BAOAB Langevin dynamics (Leimkuhler & Matthews 2013) in one persistent
+ * launch per exchange segment, one CTA per replica; replaces the replica loop
+ * of repexch.c:139-305 with cnbnd_golik (cgolik.c:644-948) as its pair loop
+ * and swap_box (swap_box.c:5-86) as its exchange.  Energy function: bonds
+ * k_bond (r - r_bond)^2; native pairs eps [5 (r0/r)^12 - 6 (r0/r)^10] (r0 =
+ * native distance, no cutoff); other pairs with |i - j| >= min_sep
+ * eps (sigma_rep/r)^12 shifted to zero at rc_rep.  Forces FP32, positions,
+ * velocities and the thermostat FP64.  Exchanges swap temperatures between
+ * replicas (slots as in swap_box) and rescale velocities by sqrt(T_s/T_s+1). */
+typedef struct {
+  double eps;        /* native / repulsive energy scale [kJ/mol] */
+  double sigma_rep;  /* non-native repulsion sigma [A] */
+  double rc_rep;     /* non-native repulsion cutoff [A] */
+  double k_bond;     /* [kJ/mol/A^2], E = k (r - r_bond)^2 */
+  double r_bond;     /* [A] */
+  double mass;       /* bead mass [amu] */
+  double gamma;      /* Langevin friction [1/ps] */
+  double dt;         /* [ps] */
+  int min_sep;       /* non-bonded pairs need |i - j| >= min_sep */
+  int device;
+} fe_go_params;
+typedef struct fe_go fe_go;
+/* nbeads[r] beads per replica, concatenated pos/vel (3 doubles per bead),
+ * natives as CSR over the global bead index (both directions, partners in
+ * the same chain) with native distances nat_r0; T[r] the starting
+ * temperature (slot r). */
+int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, const double *vel,
+                 const int *nat_start, const int *nat_j, const double *nat_r0, const double *T,
+                 const fe_go_params *p, uint64_t seed);
+void fe_go_destroy(fe_go *go);
+/* nsteps steps; an exchange attempt after every swap_freq steps (0 = none). */
+int fe_go_run(fe_go *go, int64_t nsteps, int swap_freq);
+/* Forces (FP32, returned as doubles) and potential energy per replica at the
+ * current positions. */
+int fe_go_forces(fe_go *go, double *f, double *epot);
+/* Any pointer may be NULL; accepted/attempted per slot pair (s, s+1). */
+int fe_go_state(fe_go *go, double *pos, double *vel, double *T, double *epot, int *slot_rep,
+                int64_t *accepted, int64_t *attempted, uint64_t *steps);
+int fe_go_get_stream(fe_go *go, void **stream);
+
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 
 enum { FE_KERNEL_PAIR = 0, FE_KERNEL_SPREAD = 1, FE_KERNEL_LIST = 2 };

@@ -1132,3 +1132,98 @@ int or_rex_attempt(int R, const double *T_slot, const double *potens_box, int *s
   }
   return nacc;
 }
+
+/* ---- Go-model chains (BAOAB Langevin) ---- */
+
+double or_go_forces(int N, const double *pos, int gbase, const int *nat_start, const int *nat_j,
+                    const double *nat_r0, const or_go_params *p, double *f) {
+  /* pair loop of cnbnd_golik (cgolik.c:644-948) with the chain workload's
+   * energy function: natives eps[5(r0/r)^12 - 6(r0/r)^10], others
+   * eps (sigma/r)^12 shifted at rc, bonds k (r - r0)^2 */
+  double e = 0.0;
+  double sr = p->sigma_rep / p->rc_rep, sr6 = sr * sr * sr * sr * sr * sr;
+  double shift = p->eps * sr6 * sr6, rc2 = p->rc_rep * p->rc_rep, s2r = p->sigma_rep * p->sigma_rep;
+  for (int i = 0; i < 3 * N; i++) f[i] = 0.0;
+  for (int i = 0; i < N; i++) {
+    const int gi = gbase + i;
+    for (int j = i + 1; j < N; j++) {
+      if (j - i < p->min_sep) continue;
+      int native = 0;
+      double r02 = 0.0;
+      for (int q = nat_start[gi]; q < nat_start[gi + 1]; q++)
+        if (nat_j[q] == gbase + j) { native = 1; r02 = nat_r0[q] * nat_r0[q]; }
+      double dx = pos[3 * i] - pos[3 * j], dy = pos[3 * i + 1] - pos[3 * j + 1],
+             dz = pos[3 * i + 2] - pos[3 * j + 2];
+      double r2 = dx * dx + dy * dy + dz * dz, fs;
+      if (native) {
+        double s2 = r02 / r2, s10 = s2 * s2 * s2 * s2 * s2, s12 = s10 * s2;
+        e += p->eps * (5.0 * s12 - 6.0 * s10);
+        fs = 60.0 * p->eps * (s12 - s10) / r2;
+      } else {
+        if (r2 >= rc2) continue;
+        double s2 = s2r / r2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+        e += p->eps * s12 - shift;
+        fs = 12.0 * p->eps * s12 / r2;
+      }
+      f[3 * i] += fs * dx; f[3 * i + 1] += fs * dy; f[3 * i + 2] += fs * dz;
+      f[3 * j] -= fs * dx; f[3 * j + 1] -= fs * dy; f[3 * j + 2] -= fs * dz;
+    }
+  }
+  for (int i = 0; i + 1 < N; i++) {  /* cbond.c:104-105 convention */
+    double dx = pos[3 * i] - pos[3 * i + 3], dy = pos[3 * i + 1] - pos[3 * i + 4],
+           dz = pos[3 * i + 2] - pos[3 * i + 5];
+    double r = sqrt(dx * dx + dy * dy + dz * dz), dr = r - p->r_bond;
+    e += p->k_bond * dr * dr;
+    double fs = -2.0 * p->k_bond * dr / r;
+    f[3 * i] += fs * dx; f[3 * i + 1] += fs * dy; f[3 * i + 2] += fs * dz;
+    f[3 * i + 3] -= fs * dx; f[3 * i + 4] -= fs * dy; f[3 * i + 5] -= fs * dz;
+  }
+  return e;
+}
+
+#define OR_TAG_GO 0x474F4C31u
+
+static void go_normals(uint64_t seed, uint32_t bead, uint64_t step, double z[3]) {
+  uint32_t c[4] = {bead, (uint32_t)step, (uint32_t)(step >> 32), OR_TAG_GO};
+  uint32_t k[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t o[4];
+  or_philox4x32_10(c, k, o);
+  double u1 = (double)((o[0] >> 8) + 1u) * (1.0 / 16777216.0);
+  double u2 = (double)(o[1] >> 8) * (1.0 / 16777216.0);
+  double u3 = (double)((o[2] >> 8) + 1u) * (1.0 / 16777216.0);
+  double u4 = (double)(o[3] >> 8) * (1.0 / 16777216.0);
+  double ra = sqrt(-2.0 * log(u1)), rb = sqrt(-2.0 * log(u3));
+  z[0] = ra * cos(2.0 * PI_ * u2);
+  z[1] = ra * sin(2.0 * PI_ * u2);
+  z[2] = rb * cos(2.0 * PI_ * u4);
+}
+
+double or_go_baoab(int N, double *pos, double *vel, int gbase, const int *nat_start,
+                   const int *nat_j, const double *nat_r0, const or_go_params *p, double T,
+                   uint64_t seed, uint64_t step0, int nsteps) {
+  /* B A O A B (Leimkuhler & Matthews 2013); a = 100 F / m (A/ps^2), kT as
+   * read_sim.c:351, the O step's normals by Box-Muller on Philox draws */
+  double *f = (double *)malloc(sizeof(double) * 3 * (size_t)N);
+  double e = or_go_forces(N, pos, gbase, nat_start, nat_j, nat_r0, p, f);
+  double c1 = exp(-p->gamma * p->dt), c2 = sqrt(1.0 - c1 * c1);
+  double kT = ((KB_ * NA_) * T) * .001;
+  double sv = sqrt(100.0 / p->mass) * sqrt(kT) * c2;
+  double hdt = 0.5 * p->dt, ha = 0.5 * p->dt * (100.0 / p->mass);
+  for (int s = 0; s < nsteps; s++) {
+    for (int i = 0; i < N; i++) {
+      double z[3];
+      go_normals(seed, (uint32_t)(gbase + i), step0 + (uint64_t)s, z);
+      for (int a = 0; a < 3; a++) {
+        double v = vel[3 * i + a] + ha * f[3 * i + a];
+        double x = pos[3 * i + a] + hdt * v;
+        v = c1 * v + sv * z[a];
+        pos[3 * i + a] = x + hdt * v;
+        vel[3 * i + a] = v;
+      }
+    }
+    e = or_go_forces(N, pos, gbase, nat_start, nat_j, nat_r0, p, f);
+    for (int i = 0; i < 3 * N; i++) vel[i] += ha * f[i];
+  }
+  free(f);
+  return e;
+}

@@ -176,6 +176,31 @@ double or_uniform(uint64_t seed, uint32_t tag, uint64_t event, uint32_t lane);
 int or_rex_attempt(int R, const double *T_slot, const double *potens_box, int *slot_box,
                    uint64_t attempt, uint64_t seed, int *vmode, double *vfac);
 
+/* ---- Go-model chains (the batched replica-exchange workload) ---- */
+
+typedef struct {
+  double eps;        /* kJ/mol */
+  double sigma_rep;  /* non-native repulsion sigma [A] */
+  double rc_rep;     /* its cutoff [A] (energy shifted to zero there) */
+  double k_bond;     /* E = k (r - r_bond)^2 [kJ/mol/A^2] */
+  double r_bond;
+  double mass;       /* amu */
+  double gamma;      /* 1/ps */
+  double dt;         /* ps */
+  int min_sep;       /* non-bonded pairs need |i - j| >= min_sep */
+} or_go_params;
+
+/* Forces (f, 3N, overwritten) and potential energy of one chain whose beads
+ * have global indices gbase..gbase+N-1; natives as CSR over global indices. */
+double or_go_forces(int N, const double *pos, int gbase, const int *nat_start, const int *nat_j,
+                    const double *nat_r0, const or_go_params *p, double *f);
+/* nsteps BAOAB Langevin steps at temperature T with the draws of step
+ * step0.. (Philox4x32-10, tag "GOL1", Box-Muller); returns the final
+ * potential energy. */
+double or_go_baoab(int N, double *pos, double *vel, int gbase, const int *nat_start,
+                   const int *nat_j, const double *nat_r0, const or_go_params *p, double T,
+                   uint64_t seed, uint64_t step0, int nsteps);
+
 #ifdef __cplusplus
 }
 #endif

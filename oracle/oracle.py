@@ -382,3 +382,55 @@ def rex_attempt(T_slot, potens_box, slot_box, attempt, seed):
     vfac = np.zeros(R)
     n = L.or_rex_attempt(R, _p(T), _p(U), _p(slot), attempt, seed, _p(vmode), _p(vfac))
     return slot, vmode, vfac, n
+
+
+# ---- Go-model chains ----
+
+class OrGoParams(C.Structure):
+    _fields_ = [("eps", C.c_double), ("sigma_rep", C.c_double), ("rc_rep", C.c_double),
+                ("k_bond", C.c_double), ("r_bond", C.c_double), ("mass", C.c_double),
+                ("gamma", C.c_double), ("dt", C.c_double), ("min_sep", C.c_int)]
+
+
+def _go_params(g):
+    return OrGoParams(g.eps, g.sigma_rep, g.rc_rep, g.k_bond, g.r_bond, g.mass, g.gamma, g.dt,
+                      g.min_sep)
+
+
+def _go_lib():
+    L = C.CDLL(build())
+    L.or_go_forces.restype = C.c_double
+    L.or_go_baoab.restype = C.c_double
+    return L
+
+
+def go_forces(g, r, pos=None):
+    """(forces (N x 3), potential energy) of replica r of a GoChains."""
+    L = _go_lib()
+    st = g.start
+    a, b = int(st[r]), int(st[r + 1])
+    x = np.ascontiguousarray(g.pos[a:b] if pos is None else pos, np.float64)
+    f = np.zeros_like(x)
+    ns = np.ascontiguousarray(g.nat_start, np.int32)
+    nj = np.ascontiguousarray(g.nat_j, np.int32)
+    r0 = np.ascontiguousarray(g.nat_r0, np.float64)
+    p = _go_params(g)
+    e = L.or_go_forces(b - a, _p(x), a, _p(ns), _p(nj), _p(r0), C.byref(p), _p(f))
+    return f, e
+
+
+def go_baoab(g, r, nsteps, seed, step0=0, T=None, pos=None, vel=None):
+    """nsteps Langevin steps of replica r; returns (pos, vel, final potential)."""
+    L = _go_lib()
+    st = g.start
+    a, b = int(st[r]), int(st[r + 1])
+    x = np.ascontiguousarray(g.pos[a:b] if pos is None else pos, np.float64).copy()
+    v = np.ascontiguousarray(g.vel[a:b] if vel is None else vel, np.float64).copy()
+    ns = np.ascontiguousarray(g.nat_start, np.int32)
+    nj = np.ascontiguousarray(g.nat_j, np.int32)
+    r0 = np.ascontiguousarray(g.nat_r0, np.float64)
+    p = _go_params(g)
+    e = L.or_go_baoab(b - a, _p(x), _p(v), a, _p(ns), _p(nj), _p(r0), C.byref(p),
+                      C.c_double(g.T[r] if T is None else T), C.c_uint64(seed),
+                      C.c_uint64(step0), int(nsteps))
+    return x, v, e

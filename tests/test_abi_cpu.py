@@ -35,6 +35,29 @@ def test_library_exports_every_declared_symbol(lib):
         assert re.search(rf"\bT {name}\b", out), name
 
 
+def _param_counts(header):
+    """Number of parameters of every fe_* prototype in the header."""
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    out = {}
+    for m in re.finditer(r"\b(fe_\w+)\s*\(([^;{]*?)\)\s*;", txt, re.S):
+        args = m.group(2).strip()
+        out[m.group(1)] = 0 if args in ("", "void") else args.count(",") + 1
+    return out
+
+
+def test_ctypes_signatures_match_header(lib):
+    """Every argtypes list the host mirror sets has the header's arity."""
+    counts = _param_counts("fe.h")
+    checked = 0
+    for name, n in counts.items():
+        at = getattr(lib, name).argtypes
+        if at is not None:
+            assert len(at) == n, (name, len(at), n)
+            checked += 1
+    assert checked >= 10
+
+
 def test_abi_version(lib):
     assert lib.fe_abi_version() == 1
 

@@ -1,0 +1,84 @@
+"""Batched Go-model replicas on the device against the oracle: FP32 forces
+and energies, BAOAB trajectories with the same Philox draws, the exchange
+decisions, and reproducibility."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from thecodecombo_7_gb300 import replicas
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def chains():
+    from thecodecombo_7_gb300 import systems
+    return systems.go_chains(6, nmin=60, nmax=300, seed=77)
+
+
+def test_go_forces_match_oracle(chains):
+    from thecodecombo_7_gb300 import engine
+    g = chains
+    b = engine.GoBatch(g, seed=1)
+    try:
+        f, e = b.forces()
+    finally:
+        b.close()
+    st = g.start
+    for r in range(len(g.nbeads)):
+        fr, er = O.go_forces(g, r)
+        fg = f[st[r]:st[r + 1]]
+        rms = np.sqrt(((fg - fr) ** 2).sum() / (fr ** 2).sum())
+        assert rms <= 1e-5, (r, rms)
+        assert abs(e[r] - er) <= 1e-5 * g.eps * g.nbeads[r], (r, e[r], er)
+
+
+def test_go_trajectory_matches_oracle(chains):
+    from thecodecombo_7_gb300 import engine
+    g = chains
+    b = engine.GoBatch(g, seed=11)
+    try:
+        b.run(25)
+        s = b.state()
+    finally:
+        b.close()
+    assert s["steps"] == 25
+    st = g.start
+    for r in range(len(g.nbeads)):
+        x, v, e = O.go_baoab(g, r, 25, seed=11)
+        assert np.abs(s["pos"][st[r]:st[r + 1]] - x).max() < 1e-4, r
+        assert np.abs(s["vel"][st[r]:st[r + 1]] - v).max() < 1e-2, r
+        assert abs(s["epot"][r] - e) <= 1e-4 * g.eps * g.nbeads[r]
+
+
+def test_go_exchange_decisions(chains):
+    from thecodecombo_7_gb300 import engine
+    g = chains
+    seed = 5
+    b = engine.GoBatch(g, seed=seed)
+    try:
+        slot = np.arange(len(g.nbeads), dtype=np.int32)
+        for a in range(4):
+            b.run(10, swap_freq=10)
+            s = b.state()
+            slot, vmode, vfac = replicas.exchange_decision(g.T, s["epot"], slot, a, seed)
+            assert np.array_equal(s["slot_rep"], slot), (a, s["slot_rep"], slot)
+            for q in range(len(slot)):
+                assert s["T"][slot[q]] == g.T[q]
+        assert s["steps"] == 40 and int(s["attempted"].sum()) > 0
+    finally:
+        b.close()
+
+
+def test_go_reproducible(chains):
+    from thecodecombo_7_gb300 import engine
+    out = []
+    for _ in range(2):
+        b = engine.GoBatch(chains, seed=3)
+        try:
+            b.run(30, swap_freq=10)
+            out.append(b.state())
+        finally:
+            b.close()
+    assert np.array_equal(out[0]["pos"], out[1]["pos"])
+    assert np.array_equal(out[0]["slot_rep"], out[1]["slot_rep"])

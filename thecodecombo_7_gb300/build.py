@@ -40,6 +40,7 @@ UNITS = {
     "k_replica.cu": ["-fmad=false"],
     "k_mcrun.cu": [],
     "k_mlp.cu": [],
+    "k_go.cu": [],
 }
 
 

@@ -54,6 +54,8 @@ EXPORTS = [
     "fe_mlp_get_params", "fe_mlp_grad", "fe_mlp_train", "fe_tc_gemm_bf16",
     "fe_mc_chains_collect", "fe_mc_chains_samples", "fe_mc_chains_train_surrogate",
     "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
+    "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
+    "fe_go_get_stream",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -84,6 +86,13 @@ class FeBoxParams(C.Structure):
     ]
 
 
+class FeGoParams(C.Structure):
+    _fields_ = [("eps", C.c_double), ("sigma_rep", C.c_double), ("rc_rep", C.c_double),
+                ("k_bond", C.c_double), ("r_bond", C.c_double), ("mass", C.c_double),
+                ("gamma", C.c_double), ("dt", C.c_double), ("min_sep", C.c_int),
+                ("device", C.c_int)]
+
+
 _lib = None
 
 
@@ -103,8 +112,13 @@ def load_library(path: str = LIB_PATH) -> C.CDLL:
     for name in EXPORTS:
         fn = getattr(lib, name)
         if name not in ("fe_last_error", "fe_box_destroy", "fe_box_create",
-                        "fe_batch_destroy", "fe_mlp_destroy"):
+                        "fe_batch_destroy", "fe_mlp_destroy", "fe_go_destroy"):
             fn.restype = C.c_int
+    lib.fe_go_destroy.argtypes = [C.c_void_p]
+    lib.fe_go_destroy.restype = None
+    lib.fe_go_create.argtypes = [C.POINTER(C.c_void_p), C.c_int] + [C.c_void_p] * 7 + [
+        C.POINTER(FeGoParams), C.c_uint64]
+    lib.fe_go_run.argtypes = [C.c_void_p, C.c_int64, C.c_int]
     lib.fe_mlp_destroy.argtypes = [C.c_void_p]
     lib.fe_mlp_destroy.restype = None
     lib.fe_mlp_create.argtypes = [C.POINTER(C.c_void_p), C.c_int, C.c_uint64]
@@ -578,3 +592,68 @@ class Mlp:
                                           int(batch), C.c_float(lr), C.c_uint64(seed),
                                           _p(hist)))
         return hist
+
+
+class GoBatch:
+    """Replicas of Go-model chains with Langevin dynamics and replica exchange
+    on the device (one persistent launch per exchange segment)."""
+
+    def __init__(self, g, device: int = 0, seed: int = 1):
+        self.lib = load_library()
+        self.g = g
+        self._keep = dict(nb=_c(g.nbeads, np.int32), pos=_c(g.pos, np.float64),
+                          vel=_c(g.vel, np.float64), ns=_c(g.nat_start, np.int32),
+                          nj=_c(g.nat_j, np.int32), r0=_c(g.nat_r0, np.float64),
+                          T=_c(g.T, np.float64))
+        k = self._keep
+        p = FeGoParams(g.eps, g.sigma_rep, g.rc_rep, g.k_bond, g.r_bond, g.mass, g.gamma, g.dt,
+                       g.min_sep, device)
+        h = C.c_void_p()
+        rc = self.lib.fe_go_create(C.byref(h), len(g.nbeads), _p(k["nb"]), _p(k["pos"]),
+                                   _p(k["vel"]), _p(k["ns"]), _p(k["nj"]), _p(k["r0"]),
+                                   _p(k["T"]), C.byref(p), C.c_uint64(seed))
+        if rc != FE_OK:
+            raise FeError(rc, self.lib.fe_last_error().decode())
+        self.h = h
+
+    def _check(self, rc):
+        if rc != FE_OK:
+            raise FeError(rc, self.lib.fe_last_error().decode())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.fe_go_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def run(self, nsteps, swap_freq=0):
+        self._check(self.lib.fe_go_run(self.h, int(nsteps), int(swap_freq)))
+
+    def forces(self):
+        n = int(self.g.nbeads.sum())
+        f = np.empty((n, 3))
+        e = np.empty(len(self.g.nbeads))
+        self._check(self.lib.fe_go_forces(self.h, _p(f), _p(e)))
+        return f, e
+
+    def state(self):
+        n, R = int(self.g.nbeads.sum()), len(self.g.nbeads)
+        pos, vel = np.empty((n, 3)), np.empty((n, 3))
+        T, e = np.empty(R), np.empty(R)
+        slot = np.empty(R, np.int32)
+        acc, att = np.empty(R, np.int64), np.empty(R, np.int64)
+        steps = C.c_uint64()
+        self._check(self.lib.fe_go_state(self.h, _p(pos), _p(vel), _p(T), _p(e), _p(slot),
+                                         _p(acc), _p(att), C.byref(steps)))
+        return dict(pos=pos, vel=vel, T=T, epot=e, slot_rep=slot, accepted=acc[:R - 1],
+                    attempted=att[:R - 1], steps=steps.value)
+
+    def stream(self) -> int:
+        s = C.c_void_p()
+        self._check(self.lib.fe_go_get_stream(self.h, C.byref(s)))
+        return s.value or 0

@@ -13,6 +13,10 @@ shapes the engine is measured on:
   site density, rejecting any O-O distance below 2.6 A, with uniformly random
   orientations, and Maxwell-Boltzmann velocities (net momentum removed).
 
+* ``go_chains`` -- replicas of C-alpha Go-model chains for batched replica
+  exchange: compact self-avoiding-walk native structures, native contacts,
+  geometric temperatures.
+
 Units are the reference's internal ones (A, ps, amu, e, kJ/mol;
 defines.h:62-75, integrate_vverlet.c:56).
 """
@@ -290,3 +294,103 @@ def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
     for k, v in params.items():
         setattr(sysm, k, v)
     return sysm
+
+
+# ---------------------------------------------------------------------------
+# Go-model chains (the batched replica-exchange workload)
+
+@dataclasses.dataclass
+class GoChains:
+    """Replicas of C-alpha chains: concatenated beads, natives as CSR over
+    the global bead index (both directions), per-replica temperatures."""
+
+    nbeads: np.ndarray      # (R,)
+    pos: np.ndarray         # (total, 3) native (starting) coordinates [A]
+    vel: np.ndarray         # (total, 3) [A/ps]
+    nat_start: np.ndarray   # (total + 1,)
+    nat_j: np.ndarray       # global partner index
+    nat_r0: np.ndarray      # native distance [A]
+    T: np.ndarray           # (R,) [K]
+    eps: float = 1.0 * KCAL        # 1 kcal/mol
+    sigma_rep: float = 4.0
+    rc_rep: float = 10.0
+    k_bond: float = 100.0 * KCAL   # E = k (r - r0)^2
+    r_bond: float = 3.8
+    mass: float = 110.0
+    gamma: float = 1.0
+    dt: float = 0.01
+    min_sep: int = 3
+    seed: int = 0
+
+    @property
+    def start(self):
+        return np.concatenate([[0], np.cumsum(self.nbeads)]).astype(np.int64)
+
+
+def _compact_saw(rng: np.random.Generator, n: int, bias: float = 1.5) -> np.ndarray:
+    """A compact self-avoiding walk of n sites on the unit cubic lattice:
+    grown site by site, each step choosing among the free neighbours with
+    weight exp(bias x occupied neighbours of the candidate); restarts on a
+    dead end."""
+    steps = np.array([[1, 0, 0], [-1, 0, 0], [0, 1, 0], [0, -1, 0], [0, 0, 1], [0, 0, -1]])
+    while True:
+        path = [(0, 0, 0)]
+        occ = {(0, 0, 0)}
+        ok = True
+        for _ in range(n - 1):
+            x = np.array(path[-1])
+            cands, w = [], []
+            for s in steps:
+                c = tuple(x + s)
+                if c in occ:
+                    continue
+                k = sum(tuple(np.array(c) + t) in occ for t in steps)
+                cands.append(c)
+                w.append(math.exp(bias * k))
+            if not cands:
+                ok = False
+                break
+            w = np.array(w) / sum(w)
+            c = cands[rng.choice(len(cands), p=w)]
+            path.append(c)
+            occ.add(c)
+        if ok:
+            return np.array(path, dtype=np.float64)
+
+
+def go_chains(n_rep: int = 64, nmin: int = 60, nmax: int = 400, seed: int = 2025,
+              T_min: float = 280.0, T_max: float = 450.0, lattice: float = 3.8,
+              jitter: float = 0.25, native_cut: float = 6.5, native_min_sep: int = 4,
+              **params) -> GoChains:
+    """Chain lengths uniform in [nmin, nmax]; native structures are compact
+    self-avoiding walks on a cubic lattice of spacing `lattice` with each bead
+    jittered uniformly by +-`jitter` per axis; natives are pairs closer than
+    `native_cut` with |i - j| >= native_min_sep; temperatures geometric from
+    T_min to T_max; Maxwell-Boltzmann velocities at each replica's T."""
+    rng = np.random.default_rng(seed)
+    nb = rng.integers(nmin, nmax + 1, n_rep)
+    T = np.geomspace(T_min, T_max, n_rep) if n_rep > 1 else np.array([T_min])
+    mass = params.get("mass", 110.0)
+    pos, vel, starts, js, r0s = [], [], [0], [], []
+    base = 0
+    for r in range(n_rep):
+        n = int(nb[r])
+        x = _compact_saw(rng, n) * lattice
+        x += rng.uniform(-jitter, jitter, x.shape)
+        x -= x.mean(axis=0)
+        d = np.sqrt(((x[:, None, :] - x[None, :, :]) ** 2).sum(-1))
+        for i in range(n):
+            nat = [j for j in range(n) if abs(i - j) >= native_min_sep and d[i, j] < native_cut]
+            js.extend(base + j for j in nat)
+            r0s.extend(d[i, j] for j in nat)
+            starts.append(starts[-1] + len(nat))
+        sv = math.sqrt(KB * T[r] / (mass * AU)) * 0.01
+        v = rng.normal(0.0, sv, (n, 3))
+        v -= v.mean(axis=0)
+        pos.append(x)
+        vel.append(v)
+        base += n
+    return GoChains(nbeads=nb.astype(np.int32), pos=np.concatenate(pos), vel=np.concatenate(vel),
+                    nat_start=np.array(starts, dtype=np.int32),
+                    nat_j=np.array(js, dtype=np.int32), nat_r0=np.array(r0s, dtype=np.float64),
+                    T=T.astype(np.float64), seed=seed, **params)
