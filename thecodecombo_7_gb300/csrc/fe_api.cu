@@ -81,12 +81,12 @@ static int forces_device(Box *b) {
 }
 
 static void free_box(Box *b) {
-  void *ptrs[] = {b->pos_q, b->pos_nopbc, b->vv, b->uu, b->ff, b->mass, b->type, b->lj_eps,
+  void *ptrs[] = {b->pos_q, b->pos_nopbc, b->vv, b->uu, b->ff, b->mass, b->imass100, b->type, b->lj_eps,
                   b->lj_sig, b->x_start, b->x_partner, b->x_flag, b->bond_ab, b->bend_abc,
                   b->bond_req, b->bond_k, b->bend_t0, b->bend_k, b->cell_count, b->cell_start,
                   b->cell_fill, b->cell_atoms, b->cell_of, b->nl_count, b->nl_ent, b->eterm,
                   b->kweight, b->grid, b->grid_k, b->spl_floor, b->spl_m, b->spl_d, b->fp,
-                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->zeta, b->rec,
+                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->facc, b->zeta, b->rec,
                   b->rec_counter};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -171,6 +171,11 @@ static int create(Box *b, const fe_box_params *p) {
   FE_CUDA(cudaMemset(b->uu, 0, sizeof(double) * 3 * n));
   FE_CUDA(cudaMemset(b->ff, 0, sizeof(double) * 3 * n));
   if ((rc = upload(&b->mass, p->mass, n))) return rc;
+  {
+    std::vector<double> im(n);
+    for (int i = 0; i < n; i++) im[i] = 100.0 / p->mass[i];
+    if ((rc = upload(&b->imass100, im.data(), n))) return rc;
+  }
   if ((rc = upload(&b->type, p->type, n))) return rc;
   size_t nt2 = (size_t)p->ntypes * p->ntypes;
   if ((rc = upload(&b->lj_eps, p->lj_eps, nt2))) return rc;
@@ -227,6 +232,8 @@ static int create(Box *b, const fe_box_params *p) {
   FE_CUDA(cudaMemcpy(b->scal + SC_TEMP, &p->T, sizeof(double), cudaMemcpyHostToDevice));
   FE_CUDA(cudaMalloc(&b->status, sizeof(int)));
   FE_CUDA(cudaMemset(b->status, 0, sizeof(int)));
+  FE_CUDA(cudaMalloc(&b->facc, sizeof(unsigned long long) * kFaccSlots));
+  FE_CUDA(cudaMemset(b->facc, 0, sizeof(unsigned long long) * kFaccSlots));
   FE_CUDA(cudaMalloc(&b->ticket, sizeof(unsigned)));
   FE_CUDA(cudaMemset(b->ticket, 0, sizeof(unsigned)));
   FE_CUDA(cudaMallocHost(&b->host_scal, sizeof(double) * SC_COUNT));

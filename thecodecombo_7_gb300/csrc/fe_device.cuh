@@ -76,6 +76,63 @@ __device__ __forceinline__ bool block_partials_final(double (&v)[NT], double *pa
   return true;
 }
 
+// Deterministic grid-wide sum of NT values per thread through 64-bit fixed
+// point: each thread's value is rounded to an integer multiple of 2^-shift,
+// integer sums are exact and independent of order, so the hot kernels need
+// no FP64 arithmetic for their reductions.  Each block adds its sums to
+// acc[0..NT) (one atomic per value); the last block to finish writes
+// out[t] = acc[t] * 2^-shift as doubles and leaves acc and ticket at zero.
+// blockDim.x a multiple of 32, at most 1024; NT <= blockDim.x.  Per-thread
+// values must stay below 2^(63 - shift) in magnitude, and so must the total.
+__device__ __forceinline__ long long to_fixed(float x, int shift) {
+  return __float2ll_rn(x * __int_as_float((127 + shift) << 23));
+}
+__device__ __forceinline__ long long to_fixed(double x, int shift) {
+  return __double2ll_rn(x * ldexp(1.0, shift));
+}
+__device__ __forceinline__ long long to_fixed(long long x, int) { return x; }
+
+template <int NT, typename T>
+__device__ __forceinline__ bool block_fix_final(const T (&v)[NT], int shift,
+                                                unsigned long long *acc, unsigned *ticket,
+                                                double *out) {
+  __shared__ long long shq[32][NT];
+  __shared__ bool last_blk;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  long long q[NT];
+#pragma unroll
+  for (int t = 0; t < NT; t++) {
+    q[t] = to_fixed(v[t], shift);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) q[t] += __shfl_xor_sync(0xffffffffu, q[t], o);
+    if (lane == 0) shq[wid][t] = q[t];
+  }
+  __syncthreads();
+  if (wid == 0) {
+    const int nw = blockDim.x >> 5;
+#pragma unroll
+    for (int t = 0; t < NT; t++) {
+      long long x = lane < nw ? shq[lane][t] : 0ll;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+      if (lane == 0) atomicAdd(&acc[t], (unsigned long long)x);
+    }
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last_blk = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last_blk) return false;
+  __threadfence();
+  if (threadIdx.x < NT) {
+    unsigned long long a = atomicExch(&acc[threadIdx.x], 0ull);
+    out[threadIdx.x] = (double)(long long)a * ldexp(1.0, -shift);
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+  __syncthreads();  // out[] complete for the caller's last-block epilogue
+  return true;
+}
+
 // The reference's erfc (ewald.c:817-836): the Chebyshev fit "erfcc" of
 // Numerical Recipes (Press et al., 2nd ed., sec. 6.2), fractional error
 // below 1.2e-7, same evaluation order.  The exponential is CUDA's exp.

@@ -53,12 +53,14 @@ enum : int {
   SC_MX_PAIR = SC_ENERGY3 + 3,     // 4 slots: mixed pair sums (lj, ljs, real, sum qq)
   SC_MX_EXCL = SC_MX_PAIR + 4,     // 5 slots: mixed exclusion sums (.., intra)
   SC_TEMP = SC_MX_EXCL + 5,        // thermostat temperature [K] (sim.T[k]); exchanges rewrite it
-  SC_COUNT
+  SC_MX_INTRA,                     // 7 slots: fused intramolecular sums (5 exclusion, bond, bend)
+  SC_COUNT = SC_MX_INTRA + 7
 };
 
 // Largest number of blocks a partial-sum kernel may use.
 constexpr int kMaxPartialBlocks = 4096;
 constexpr int kPartialTerms = 8;
+constexpr int kFaccSlots = 16;
 
 struct Box {
   fe_box_params p;  // scalars (pointers inside are not kept)
@@ -73,6 +75,7 @@ struct Box {
   double *pos_nopbc = nullptr;  // 3n
   double *vv = nullptr, *uu = nullptr, *ff = nullptr;  // 3n, struct veloc layout
   double *mass = nullptr;
+  double *imass100 = nullptr;  // 100 / mass (integrate_vverlet.c:56), one division at setup
   int *type = nullptr;
   double *lj_eps = nullptr, *lj_sig = nullptr;  // nt*nt
   // exclusions, per atom, both directions, in xint order
@@ -119,6 +122,7 @@ struct Box {
   double *scal = nullptr;      // SC_COUNT
   int *status = nullptr;       // device status word
   unsigned *ticket = nullptr;  // last-block counter of the fused reductions (0 between kernels)
+  unsigned long long *facc = nullptr;  // kFaccSlots fixed-point sums of block_fix_final (0 between kernels)
   double *host_scal = nullptr; // pinned SC_COUNT
 
   // NHC

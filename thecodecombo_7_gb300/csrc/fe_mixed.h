@@ -42,7 +42,16 @@ struct Mixed {
   int *floor3 = nullptr;
   float *sm = nullptr, *sd = nullptr;
   double erfc_rc_over_rc = 0.0;
+  // Molecules for the fused intramolecular kernel: every bonded and excluded
+  // pair lies inside a contiguous run of at most kIntraMaxSites sites.
+  // nmol == 0: the topology does not allow it (separate kernels are used).
+  int nmol = 0;
+  int *mol_first = nullptr;                    // nmol + 1
+  int *mol_x = nullptr, *mol_xi = nullptr;     // CSR: exclusion indices per molecule
+  int *mol_b = nullptr, *mol_bi = nullptr;     // bond indices
+  int *mol_a = nullptr, *mol_ai = nullptr;     // bend indices
 };
+constexpr int kIntraMaxSites = 8;
 
 int mixed_setup(Box *b);
 void mixed_free(Box *b);

@@ -114,13 +114,13 @@ __device__ __forceinline__ double pbc_wrap(double d, double h, double l, int *ba
 }
 
 // integrate_vverlet.c:54-83: half kick, drift (atom and atnopbc), pbc_all
-__global__ void k_vv1(int n, double vscal, double dt, double dt_h, double3 L,
-                      const double *__restrict__ mass, const double *__restrict__ ff,
+__global__ void k_vv1(int n, double vscal, double dt, double dt_h, double3 L, double3 H,
+                      const double *__restrict__ imass100, const double *__restrict__ ff,
                       double *__restrict__ vv, double4 *__restrict__ pos,
                       double *__restrict__ nopbc, int *__restrict__ status) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double imass = 100.0 / mass[i];
+  double imass = imass100[i];
   double v0 = vscal * (vv[3 * i] + dt_h * imass * ff[3 * i]);
   double v1 = vscal * (vv[3 * i + 1] + dt_h * imass * ff[3 * i + 1]);
   double v2 = vscal * (vv[3 * i + 2] + dt_h * imass * ff[3 * i + 2]);
@@ -136,18 +136,19 @@ __global__ void k_vv1(int n, double vscal, double dt, double dt_h, double3 L,
   p.y += ddy;
   p.z += ddz;
   int bad = 0;
-  p.x = pbc_wrap(p.x, L.x / 2.0, L.x, &bad);
-  p.y = pbc_wrap(p.y, L.y / 2.0, L.y, &bad);
-  p.z = pbc_wrap(p.z, L.z / 2.0, L.z, &bad);
+  p.x = pbc_wrap(p.x, H.x, L.x, &bad);
+  p.y = pbc_wrap(p.y, H.y, L.y, &bad);
+  p.z = pbc_wrap(p.z, H.z, L.z, &bad);
   if (bad) atomicOr(status, ST_PBC_LOOP);
   pos[i] = p;
 }
 
 int launch_vv1(Box *b, double vscal) {
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
+  double3 H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);  // pbc_all.c hx
   double dt = b->p.dt, dt_h = 0.5 * b->p.dt;
-  k_vv1<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal, dt, dt_h, L, b->mass, b->ff, b->vv,
-                                                   b->pos_q, b->pos_nopbc, b->status);
+  k_vv1<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal, dt, dt_h, L, H, b->imass100, b->ff,
+                                                   b->vv, b->pos_q, b->pos_nopbc, b->status);
   FE_LAUNCH_CHECK("k_vv1");
   return FE_OK;
 }
@@ -172,12 +173,12 @@ int launch_pbc(Box *b) {
 }
 
 // integrate_vverlet.c:93-102: second half kick and uu = vv
-__global__ void k_vv2(int n, double vscal, double dt_h, const double *__restrict__ mass,
+__global__ void k_vv2(int n, double vscal, double dt_h, const double *__restrict__ imass100,
                       const double *__restrict__ ff, double *__restrict__ vv,
                       double *__restrict__ uu) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  double imass = 100.0 / mass[i];
+  double imass = imass100[i];
   for (int c = 0; c < 3; c++) {
     double v = (vv[3 * i + c] + vscal * dt_h * imass * ff[3 * i + c]);
     vv[3 * i + c] = v;
@@ -187,7 +188,8 @@ __global__ void k_vv2(int n, double vscal, double dt_h, const double *__restrict
 
 int launch_vv2(Box *b, double vscal) {
   double dt_h = 0.5 * b->p.dt;
-  k_vv2<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal, dt_h, b->mass, b->ff, b->vv, b->uu);
+  k_vv2<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal, dt_h, b->imass100, b->ff, b->vv,
+                                                   b->uu);
   FE_LAUNCH_CHECK("k_vv2");
   return FE_OK;
 }
@@ -195,12 +197,13 @@ int launch_vv2(Box *b, double vscal) {
 // integrate_vverlet.c:93-102 and kinet.c:31-65 in one pass: second half
 // kick, uu = vv, and the kinetic tensor of the new velocities
 __global__ void k_vv2_kinet(int n, double vscal, double dt_h, const double *__restrict__ mass,
+                            const double *__restrict__ imass100,
                             const double *__restrict__ ff, double *__restrict__ vv,
-                            double *__restrict__ uu, double *__restrict__ partials,
+                            double *__restrict__ uu, unsigned long long *__restrict__ facc,
                             unsigned *__restrict__ ticket, double *__restrict__ s) {
   double k[6] = {0, 0, 0, 0, 0, 0};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    double imass = 100.0 / mass[i];
+    double imass = imass100[i];
     double v[3];
     for (int c = 0; c < 3; c++) {
       v[c] = (vv[3 * i + c] + vscal * dt_h * imass * ff[3 * i + c]);
@@ -216,7 +219,8 @@ __global__ void k_vv2_kinet(int n, double vscal, double dt_h, const double *__re
     k[4] += fac * sz * sy;
     k[5] += fac * sz * sz;
   }
-  if (block_partials_final<6>(k, partials, ticket, s + SC_KEN) && threadIdx.x == 0) {
+  // exact fixed-point sums (2^-20 amu A^2/ps^2 resolution): no FP64 tree
+  if (block_fix_final<6>(k, 20, facc, ticket, s + SC_KEN) && threadIdx.x == 0) {
     double f = (0.125) * (kNA * kAU * 10.0);  // kinet.c:50-65
     for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
     s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
@@ -227,8 +231,8 @@ int launch_vv2_kinet(Box *b, double vscal) {
   double dt_h = 0.5 * b->p.dt;
   int blocks = (b->n + 255) / 256;
   if (blocks > 512) blocks = 512;
-  k_vv2_kinet<<<blocks, 256, 0, b->stream>>>(b->n, vscal, dt_h, b->mass, b->ff, b->vv, b->uu,
-                                             b->partials, b->ticket, b->scal);
+  k_vv2_kinet<<<blocks, 256, 0, b->stream>>>(b->n, vscal, dt_h, b->mass, b->imass100, b->ff, b->vv, b->uu,
+                                             b->facc, b->ticket, b->scal);
   FE_LAUNCH_CHECK("k_vv2_kinet");
   return FE_OK;
 }

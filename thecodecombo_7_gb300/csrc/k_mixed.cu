@@ -451,7 +451,8 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
           const int *__restrict__ perm, const int *__restrict__ cnt_lj,
           const int *__restrict__ cnt_nl, const int *__restrict__ ent,
           const float *__restrict__ lj_tab, unsigned long long *__restrict__ fix,
-          double *__restrict__ partials, unsigned *__restrict__ ticket, double *__restrict__ out) {
+          unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+          double *__restrict__ out) {
   extern __shared__ float s_lj[];  // nt*nt*3: eps, sig^2, shift constant
   for (int i = threadIdx.x; i < P.nt * P.nt * 3; i += blockDim.x) s_lj[i] = lj_tab[i];
   __syncthreads();
@@ -481,9 +482,8 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
     }
   }
   // every pair was visited from both ends
-  double v[4] = {0.5 * (double)a.e_lj, 0.5 * (double)a.e_ljs, 0.5 * (double)a.e_real,
-                 0.5 * (double)a.qsum};
-  block_partials_final<4>(v, partials, ticket, out);
+  float v[4] = {0.5f * a.e_lj, 0.5f * a.e_ljs, 0.5f * a.e_real, 0.5f * a.qsum};
+  block_fix_final<4>(v, 32, facc, ticket, out);
 }
 
 // excluded and 1-4 pairs (xint), cnonbond_nblist.c:245-263 and 416-437:
@@ -491,28 +491,26 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
 // intra correction -qq (1 - erfc(kr)) / r; a 1-4 pair gets LJ, real space
 // scaled by E14FAC and the correction with (1 - E14FAC)
 __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__restrict__ flag,
-                          const double4 *__restrict__ pos, const int *__restrict__ type, double3 L,
-                          int nt, const float *__restrict__ lj_tab, float rc2, float kappa,
+                          const int4 *__restrict__ posfx, const int *__restrict__ iperm,
+                          const int *__restrict__ type, float3 sL, int nt, const float *__restrict__ lj_tab, float rc2, float kappa,
                           float c2k, float qf, float epsRF, unsigned long long *__restrict__ fix,
-                          double *__restrict__ partials, unsigned *__restrict__ ticket,
+                          unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                           double *__restrict__ out) {
   float e_intra = 0.f, e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nexcl; t += gridDim.x * blockDim.x) {
     int a = ab[2 * t], b = ab[2 * t + 1], xf = flag[t];
     if (xf == 0) continue;
-    double4 A = pos[a], B = pos[b];
-    double ddx = A.x - B.x, ddy = A.y - B.y, ddz = A.z - B.z;
-    ddx -= L.x * rint(ddx / L.x);
-    ddy -= L.y * rint(ddy / L.y);
-    ddz -= L.z * rint(ddz / L.z);
-    float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+    int4 A = posfx[iperm[a]], B = posfx[iperm[b]];
+    float dx = fx_delta((unsigned)A.x, (unsigned)B.x, sL.x);
+    float dy = fx_delta((unsigned)A.y, (unsigned)B.y, sL.y);
+    float dz = fx_delta((unsigned)A.z, (unsigned)B.z, sL.z);
     float r2 = dx * dx + dy * dy + dz * dz;
     if (r2 > rc2) continue;
     float rinv = rsqrtf(r2), r = r2 * rinv, rinv2 = rinv * rinv;
     float kr = kappa * r;
     float ex = __expf(-kr * kr);
     float erfckr = erfc_nr_f(kr, ex);
-    float qqab = (float)A.w * (float)B.w * qf;
+    float qqab = __int_as_float(A.w) * __int_as_float(B.w) * qf;
     float F = 0.f;
     float qcorr = qqab;
     if (xf == 4) {
@@ -540,28 +538,28 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
     atomicAdd(&fix[3 * b + 1], (unsigned long long)(-fyq));
     atomicAdd(&fix[3 * b + 2], (unsigned long long)(-fzq));
   }
-  double v[5] = {(double)e_lj, (double)e_ljs, (double)e_real, (double)qsum, (double)e_intra};
-  block_partials_final<5>(v, partials, ticket, out);
+  float v[5] = {e_lj, e_ljs, e_real, qsum, e_intra};
+  block_fix_final<5>(v, 32, facc, ticket, out);
 }
 
-// bonded terms in FP32 from FP64 differences (cbond.c, cbend.c)
-__global__ void k_mx_bonded(int nbond, int nbend, double3 L, const double4 *__restrict__ pos,
+// bonded terms in FP32 from the fixed-point coordinates (cbond.c, cbend.c)
+__global__ void k_mx_bonded(int nbond, int nbend, float3 sL, const int4 *__restrict__ posfx,
+                            const int *__restrict__ iperm,
                             const int *__restrict__ bond_ab, const double *__restrict__ bond_req,
                             const double *__restrict__ bond_k, const int *__restrict__ bend_abc,
                             const double *__restrict__ bend_t0, const double *__restrict__ bend_k,
-                            unsigned long long *__restrict__ fix, double *__restrict__ partials,
-                            unsigned *__restrict__ ticket, double *__restrict__ out) {
+                            unsigned long long *__restrict__ fix,
+                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+                            double *__restrict__ out) {
   float eb = 0.f, ea = 0.f;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nbond + nbend;
        t += gridDim.x * blockDim.x) {
     if (t < nbond) {
       int ia = bond_ab[2 * t], ib = bond_ab[2 * t + 1];
-      double4 A = pos[ia], B = pos[ib];
-      double ddx = B.x - A.x, ddy = B.y - A.y, ddz = B.z - A.z;
-      ddx -= L.x * rint(ddx / L.x);
-      ddy -= L.y * rint(ddy / L.y);
-      ddz -= L.z * rint(ddz / L.z);
-      float dx = (float)ddx, dy = (float)ddy, dz = (float)ddz;
+      int4 A = posfx[iperm[ia]], B = posfx[iperm[ib]];
+      float dx = fx_delta((unsigned)B.x, (unsigned)A.x, sL.x);
+      float dy = fx_delta((unsigned)B.y, (unsigned)A.y, sL.y);
+      float dz = fx_delta((unsigned)B.z, (unsigned)A.z, sL.z);
       float dr = sqrtf(dx * dx + dy * dy + dz * dz);
       float rr = dr - (float)bond_req[t];
       float fr = -(float)bond_k[t] * rr * 2.f;
@@ -577,17 +575,13 @@ __global__ void k_mx_bonded(int nbond, int nbend, double3 L, const double4 *__re
     } else {
       int u = t - nbond;
       int ia = bend_abc[3 * u], ib = bend_abc[3 * u + 1], ic = bend_abc[3 * u + 2];
-      double4 A = pos[ia], B = pos[ib], Cc = pos[ic];
-      double d0 = A.x - B.x, d1 = A.y - B.y, d2 = A.z - B.z;
-      double e0 = Cc.x - B.x, e1 = Cc.y - B.y, e2 = Cc.z - B.z;
-      d0 -= L.x * rint(d0 / L.x);
-      d1 -= L.y * rint(d1 / L.y);
-      d2 -= L.z * rint(d2 / L.z);
-      e0 -= L.x * rint(e0 / L.x);
-      e1 -= L.y * rint(e1 / L.y);
-      e2 -= L.z * rint(e2 / L.z);
-      float dax = (float)d0, day = (float)d1, daz = (float)d2;
-      float dcx = (float)e0, dcy = (float)e1, dcz = (float)e2;
+      int4 A = posfx[iperm[ia]], B = posfx[iperm[ib]], Cc = posfx[iperm[ic]];
+      float dax = fx_delta((unsigned)A.x, (unsigned)B.x, sL.x);
+      float day = fx_delta((unsigned)A.y, (unsigned)B.y, sL.y);
+      float daz = fx_delta((unsigned)A.z, (unsigned)B.z, sL.z);
+      float dcx = fx_delta((unsigned)Cc.x, (unsigned)B.x, sL.x);
+      float dcy = fx_delta((unsigned)Cc.y, (unsigned)B.y, sL.y);
+      float dcz = fx_delta((unsigned)Cc.z, (unsigned)B.z, sL.z);
       float drai = rsqrtf(dax * dax + day * day + daz * daz);
       float erax = dax * drai, eray = day * drai, eraz = daz * drai;
       float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
@@ -617,8 +611,8 @@ __global__ void k_mx_bonded(int nbond, int nbend, double3 L, const double4 *__re
       atomicAdd(&fix[3 * ic + 2], (unsigned long long)cz);
     }
   }
-  double v[2] = {(double)eb, (double)ea};
-  block_partials_final<2>(v, partials, ticket, out);
+  float v[2] = {eb, ea};
+  block_fix_final<2>(v, 32, facc, ticket, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -649,22 +643,25 @@ __device__ __forceinline__ void fillspline_f(int order, float w, float *array, f
   array[1] *= div * (1.f - w);
 }
 
-// per sorted slot: origin cell (FP64 fraction), FP32 weights, binning
-__global__ void k_mx_splines(int n, int order, int3 G, double3 L, const double4 *__restrict__ pos,
-                             const int *__restrict__ perm, int *__restrict__ floor3,
+// per sorted slot: origin cell and fraction exactly from the 32-bit
+// fixed-point coordinate (u G / 2^32: integer part and remainder), FP32
+// weights, binning
+__global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ posfx,
+                             int *__restrict__ floor3,
                              float *__restrict__ sm, float *__restrict__ sd, int gcap,
                              int *__restrict__ bcount, int *__restrict__ batoms,
                              int *__restrict__ status) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
-  double4 p = pos[perm[s]];
-  double ss[3] = {G.x * (p.x / L.x + 0.5), G.y * (p.y / L.y + 0.5), G.z * (p.z / L.z + 0.5)};
+  int4 p = posfx[s];
+  unsigned u[3] = {(unsigned)p.x, (unsigned)p.y, (unsigned)p.z};
   int g[3] = {G.x, G.y, G.z};
   int f[3];
   float mn[9], dmn[9];
   for (int d = 0; d < 3; d++) {
-    f[d] = (int)ss[d];
-    float w = (float)(ss[d] - (double)f[d]);
+    unsigned long long t = (unsigned long long)u[d] * (unsigned)g[d];
+    f[d] = (int)(t >> 32);
+    float w = (float)(unsigned)(t & 0xffffffffull) * 0x1p-32f;
     fillspline_f(order, w, mn, dmn);
     for (int m = 1; m <= order; m++) {
       sm[((size_t)s * order + (m - 1)) * 3 + d] = mn[m];
@@ -796,29 +793,30 @@ k_mx_spread4(int order, int3 G, const int4 *__restrict__ posfx, const float *__r
 }
 
 __global__ void k_mx_recip(long Kh, const float *__restrict__ eterm, const float *__restrict__ kw,
-                           cufftComplex *__restrict__ gk, double *__restrict__ partials,
+                           cufftComplex *__restrict__ gk, unsigned long long *__restrict__ facc,
                            unsigned *__restrict__ ticket, double *__restrict__ out) {
-  double e = 0.0;
+  float e = 0.f;
   for (long h = (long)blockIdx.x * blockDim.x + threadIdx.x; h < Kh;
        h += (long)gridDim.x * blockDim.x) {
     cufftComplex v = gk[h];
     float et = eterm[h];
-    e += (double)(kw[h] * et * (v.x * v.x + v.y * v.y));
+    e = fmaf(kw[h] * et, v.x * v.x + v.y * v.y, e);
     v.x *= et;
     v.y *= et;
     gk[h] = v;
   }
-  double vv[1] = {e};
-  block_partials_final<1>(vv, partials, ticket, out);
+  float vv[1] = {e};
+  block_fix_final<1>(vv, 24, facc, ticket, out);
 }
 
 __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
                             const int4 *__restrict__ posfx, const int *__restrict__ perm,
                             const int *__restrict__ floor3, const float *__restrict__ sm,
                             const float *__restrict__ sd, const float *__restrict__ grid,
-                            unsigned long long *__restrict__ fix, double *__restrict__ partials,
-                            unsigned *__restrict__ ticket, double *__restrict__ out) {
-  double sx = 0.0, sy = 0.0, sz = 0.0;
+                            unsigned long long *__restrict__ fix,
+                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+                            double *__restrict__ out) {
+  long long sx = 0, sy = 0, sz = 0;
   for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
     float fxi = 0.f, fyi = 0.f, fzi = 0.f;
     const float *m = sm + (size_t)s * order * 3;
@@ -850,26 +848,164 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
     atomicAdd(&fix[3 * oi], (unsigned long long)qx);
     atomicAdd(&fix[3 * oi + 1], (unsigned long long)qy);
     atomicAdd(&fix[3 * oi + 2], (unsigned long long)qz);
-    sx += (double)qx;
-    sy += (double)qy;
-    sz += (double)qz;
+    sx += qx;
+    sy += qy;
+    sz += qz;
   }
-  double v[3] = {sx, sy, sz};
-  block_partials_final<3>(v, partials, ticket, out);
+  long long v[3] = {sx, sy, sz};
+  block_fix_final<3>(v, 0, facc, ticket, out);
 }
 
 // FP64 forces from the fixed-point sums, minus the mean reciprocal force
 __global__ void k_mx_finalize(int n, const unsigned long long *__restrict__ fix,
                               const double *__restrict__ scal, double *__restrict__ ff) {
+  __shared__ double mean[3];
+  if (threadIdx.x < 3) mean[threadIdx.x] = scal[SC_FMEAN + threadIdx.x] / kFixScale / (double)n;
+  __syncthreads();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * n) return;
-  double mean = scal[SC_FMEAN + i % 3] / kFixScale / (double)n;
-  ff[i] = (double)(long long)fix[i] / kFixScale - mean;
+  ff[i] = (double)(long long)fix[i] * (1.0 / kFixScale) - mean[i % 3];
+}
+
+// All intramolecular terms of one molecule per thread: the exclusion
+// corrections of k_mx_excl and the bonds and bends of k_mx_bonded, same
+// arithmetic, with the molecule's forces summed in registers and added to
+// the fixed-point accumulators without atomics (each site belongs to one
+// molecule and no other kernel runs concurrently on the accumulators).
+__global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
+                           const int *__restrict__ mol_x, const int *__restrict__ mol_xi,
+                           const int *__restrict__ mol_b, const int *__restrict__ mol_bi,
+                           const int *__restrict__ mol_a, const int *__restrict__ mol_ai,
+                           const int *__restrict__ ab, const int *__restrict__ flag,
+                           const int *__restrict__ bond_ab, const double *__restrict__ bond_req,
+                           const double *__restrict__ bond_k, const int *__restrict__ bend_abc,
+                           const double *__restrict__ bend_t0, const double *__restrict__ bend_k,
+                           const int4 *__restrict__ posfx, const int *__restrict__ iperm,
+                           const int *__restrict__ type, float3 sL, int nt,
+                           const float *__restrict__ lj_tab, float rc2, float kappa, float c2k,
+                           float qf, float epsRF, unsigned long long *__restrict__ fix,
+                           unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+                           double *__restrict__ out) {
+  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, e_intra = 0.f, eb = 0.f, ea = 0.f;
+  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmol; m += gridDim.x * blockDim.x) {
+    const int lb = mol_first[m], ns = mol_first[m + 1] - lb;
+    int4 P[kIntraMaxSites];
+    float F[kIntraMaxSites][3];
+    for (int i = 0; i < ns; i++) {
+      P[i] = posfx[iperm[lb + i]];
+      F[i][0] = F[i][1] = F[i][2] = 0.f;
+    }
+    for (int t = mol_x[m]; t < mol_x[m + 1]; t++) {
+      int x = mol_xi[t];
+      int a = ab[2 * x] - lb, bq = ab[2 * x + 1] - lb, xf = flag[x];
+      if (xf == 0) continue;
+      float dx = fx_delta((unsigned)P[a].x, (unsigned)P[bq].x, sL.x);
+      float dy = fx_delta((unsigned)P[a].y, (unsigned)P[bq].y, sL.y);
+      float dz = fx_delta((unsigned)P[a].z, (unsigned)P[bq].z, sL.z);
+      float r2 = dx * dx + dy * dy + dz * dz;
+      if (r2 > rc2) continue;
+      float rinv = rsqrtf(r2), r = r2 * rinv, rinv2 = rinv * rinv;
+      float kr = kappa * r;
+      float ex = __expf(-kr * kr);
+      float erfckr = erfc_nr_f(kr, ex);
+      float qqab = __int_as_float(P[a].w) * __int_as_float(P[bq].w) * qf;
+      float Fs = 0.f;
+      float qcorr = qqab;
+      if (xf == 4) {
+        float qq = qqab * (float)kE14FAC / epsRF;
+        Fs += qq * rinv * rinv2 * (erfckr + c2k * r * ex);
+        e_real += qq * erfckr * rinv;
+        qsum += qq;
+        const float *lj = lj_tab + (type[lb + a] * nt + type[lb + bq]) * 3;
+        if (lj[0] != 0.f) {
+          float sr2 = lj[1] * rinv2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+          Fs += 12.f * lj[0] * rinv2 * (sr12 - sr6);
+          e_lj += lj[0] * (sr12 - 2.f * sr6);
+          e_ljs += lj[0] * lj[2];
+        }
+        qcorr *= (1.f - (float)kE14FAC);
+      }
+      float erfkr = 1.f - erfckr;
+      e_intra += qcorr * erfkr * rinv;
+      Fs -= qcorr * rinv * rinv2 * (erfkr - c2k * r * ex);
+      F[a][0] += Fs * dx;
+      F[a][1] += Fs * dy;
+      F[a][2] += Fs * dz;
+      F[bq][0] -= Fs * dx;
+      F[bq][1] -= Fs * dy;
+      F[bq][2] -= Fs * dz;
+    }
+    for (int t = mol_b[m]; t < mol_b[m + 1]; t++) {
+      int u = mol_bi[t];
+      int ia = bond_ab[2 * u] - lb, ib = bond_ab[2 * u + 1] - lb;
+      float dx = fx_delta((unsigned)P[ib].x, (unsigned)P[ia].x, sL.x);
+      float dy = fx_delta((unsigned)P[ib].y, (unsigned)P[ia].y, sL.y);
+      float dz = fx_delta((unsigned)P[ib].z, (unsigned)P[ia].z, sL.z);
+      float dr = sqrtf(dx * dx + dy * dy + dz * dz);
+      float rr = dr - (float)bond_req[u];
+      float fr = -(float)bond_k[u] * rr * 2.f;
+      eb += -(fr * rr * 0.5f);
+      float sc = fr / dr;
+      F[ia][0] -= sc * dx;
+      F[ia][1] -= sc * dy;
+      F[ia][2] -= sc * dz;
+      F[ib][0] += sc * dx;
+      F[ib][1] += sc * dy;
+      F[ib][2] += sc * dz;
+    }
+    for (int t = mol_a[m]; t < mol_a[m + 1]; t++) {
+      int u = mol_ai[t];
+      int ia = bend_abc[3 * u] - lb, ib = bend_abc[3 * u + 1] - lb, ic = bend_abc[3 * u + 2] - lb;
+      float dax = fx_delta((unsigned)P[ia].x, (unsigned)P[ib].x, sL.x);
+      float day = fx_delta((unsigned)P[ia].y, (unsigned)P[ib].y, sL.y);
+      float daz = fx_delta((unsigned)P[ia].z, (unsigned)P[ib].z, sL.z);
+      float dcx = fx_delta((unsigned)P[ic].x, (unsigned)P[ib].x, sL.x);
+      float dcy = fx_delta((unsigned)P[ic].y, (unsigned)P[ib].y, sL.y);
+      float dcz = fx_delta((unsigned)P[ic].z, (unsigned)P[ib].z, sL.z);
+      float drai = rsqrtf(dax * dax + day * day + daz * daz);
+      float erax = dax * drai, eray = day * drai, eraz = daz * drai;
+      float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+      float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
+      float cosphi = erax * ercx + eray * ercy + eraz * ercz;
+      cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
+      float phi = acosf(cosphi);
+      float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
+      float rr = phi - (float)bend_t0[u];
+      float fr = -(float)bend_k[u] * rr * 2.f;
+      ea += -fr * rr * 0.5f;
+      float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
+      float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
+            fza = (eraz * cosphi - ercz) * irasin;
+      float fxc = (ercx * cosphi - erax) * ircsin, fyc = (ercy * cosphi - eray) * ircsin,
+            fzc = (ercz * cosphi - eraz) * ircsin;
+      F[ia][0] += fxa;
+      F[ia][1] += fya;
+      F[ia][2] += fza;
+      F[ic][0] += fxc;
+      F[ic][1] += fyc;
+      F[ic][2] += fzc;
+      F[ib][0] -= fxa + fxc;
+      F[ib][1] -= fya + fyc;
+      F[ib][2] -= fza + fzc;
+    }
+    for (int i = 0; i < ns; i++)
+      for (int c = 0; c < 3; c++) {
+        unsigned long long *q = fix + 3 * (size_t)(lb + i) + c;
+        *q = *q + (unsigned long long)to_fix(F[i][c]);
+      }
+  }
+  float v[7] = {e_lj, e_ljs, e_real, qsum, e_intra, eb, ea};
+  block_fix_final<7>(v, 32, facc, ticket, out);
 }
 
 // combine the mixed kernels' sums into the reference's slots
-__global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc) {
+__global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc, int fused) {
   if (threadIdx.x != 0) return;
+  if (fused) {
+    for (int t = 0; t < 5; t++) s[SC_MX_EXCL + t] = s[SC_MX_INTRA + t];
+    s[SC_BOND] = s[SC_MX_INTRA + 5];
+    s[SC_BEND] = s[SC_MX_INTRA + 6];
+  }
   s[SC_LJ] = s[SC_MX_PAIR + 0] + s[SC_MX_EXCL + 0];
   s[SC_LJS] = s[SC_MX_PAIR + 1] + s[SC_MX_EXCL + 1];
   s[SC_REAL] = s[SC_MX_PAIR + 2] + s[SC_MX_EXCL + 2];
@@ -879,6 +1015,13 @@ __global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc) {
 
 // ---------------------------------------------------------------------------
 // host side
+
+static int up(int **dst, const std::vector<int> &v) {
+  FE_CUDA(cudaMalloc(dst, sizeof(int) * (v.empty() ? 1 : v.size())));
+  if (!v.empty())
+    FE_CUDA(cudaMemcpy(*dst, v.data(), sizeof(int) * v.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
 
 int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
@@ -956,7 +1099,64 @@ int mixed_setup(Box *b) {
   if (M.nexcl) {
     FE_CUDA(cudaMemcpy(M.excl_ab, b->p.excl_ab, sizeof(int) * 2 * M.nexcl, cudaMemcpyHostToDevice));
     FE_CUDA(cudaMemcpy(M.excl_flag, b->p.excl_flag, sizeof(int) * M.nexcl, cudaMemcpyHostToDevice));
+  }  {
+    // molecules for the fused intramolecular kernel: connected components of
+    // bonds, bends and exclusions; usable when each is a contiguous run of
+    // at most kIntraMaxSites sites
+    std::vector<int> par(n);
+    for (int i = 0; i < n; i++) par[i] = i;
+    auto find = [&](int x) {
+      while (par[x] != x) x = par[x] = par[par[x]];
+      return x;
+    };
+    auto unite = [&](int x, int y) {
+      x = find(x);
+      y = find(y);
+      if (x != y) par[x > y ? x : y] = x < y ? x : y;
+    };
+    const fe_box_params &pp = b->p;
+    for (int t = 0; t < pp.nbond; t++) unite(pp.bond_ab[2 * t], pp.bond_ab[2 * t + 1]);
+    for (int t = 0; t < pp.nbend; t++) {
+      unite(pp.bend_abc[3 * t], pp.bend_abc[3 * t + 1]);
+      unite(pp.bend_abc[3 * t + 1], pp.bend_abc[3 * t + 2]);
+    }
+    for (int t = 0; t < pp.nexcl; t++) unite(pp.excl_ab[2 * t], pp.excl_ab[2 * t + 1]);
+    std::vector<int> first, mol_of(n);
+    bool ok = true;
+    for (int i = 0; i < n && ok; i++) {
+      int r = find(i);
+      if (i == 0 || r != find(i - 1)) {
+        if (r != i) ok = false;  // a component that does not start here: not contiguous
+        first.push_back(i);
+      }
+      mol_of[i] = (int)first.size() - 1;
+    }
+    first.push_back(n);
+    int nm = (int)first.size() - 1;
+    for (int m = 0; m < nm && ok; m++)
+      if (first[m + 1] - first[m] > kIntraMaxSites) ok = false;
+    if (ok && nm > 0) {
+      auto csr = [&](int count, auto mol_fn, std::vector<int> &off, std::vector<int> &idx) {
+        off.assign(nm + 1, 0);
+        for (int t = 0; t < count; t++) off[mol_fn(t) + 1]++;
+        for (int m = 0; m < nm; m++) off[m + 1] += off[m];
+        std::vector<int> fill(off.begin(), off.end() - 1);
+        idx.assign(count > 0 ? count : 1, 0);
+        for (int t = 0; t < count; t++) idx[fill[mol_fn(t)]++] = t;
+      };
+      std::vector<int> xo, xi, bo, bi, ao, ai;
+      csr(pp.nexcl, [&](int t) { return mol_of[pp.excl_ab[2 * t]]; }, xo, xi);
+      csr(pp.nbond, [&](int t) { return mol_of[pp.bond_ab[2 * t]]; }, bo, bi);
+      csr(pp.nbend, [&](int t) { return mol_of[pp.bend_abc[3 * t]]; }, ao, ai);
+      int rc;
+      if ((rc = up(&M.mol_first, first))) return rc;
+      if ((rc = up(&M.mol_x, xo)) || (rc = up(&M.mol_xi, xi))) return rc;
+      if ((rc = up(&M.mol_b, bo)) || (rc = up(&M.mol_bi, bi))) return rc;
+      if ((rc = up(&M.mol_a, ao)) || (rc = up(&M.mol_ai, ai))) return rc;
+      M.nmol = nm;
+    }
   }
+
   // SPME, FP32
   long K = b->K, Kh = b->Kh;
   std::vector<double> et(Kh), kw(Kh);
@@ -990,7 +1190,8 @@ void mixed_free(Box *b) {
   void *ptrs[] = {M.cell_count, M.cell_start, M.cell_fill, M.cell_of, M.perm, M.iperm, M.cell_s,
                   M.cz_s, M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
                   M.ient, M.fix, M.lj_tab, M.lj_on, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
-                  M.grid32, M.grid32k, M.floor3, M.sm, M.sd};
+                  M.grid32, M.grid32k, M.floor3, M.sm, M.sd, M.mol_first, M.mol_x,
+                  M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (M.plans) {
@@ -1088,7 +1289,7 @@ int launch_mx_pair_only(Box *b) {
   const int *cnl = M.use_inner ? M.icnt_nl : M.cnt_nl;
   const int *ent = M.use_inner ? M.ient : M.ent;
   k_mx_pair<<<pair_blocks(b), kMxWarps * 32, shm, b->stream>>>(
-      P, M.posfx, M.type_s, M.perm, clj, cnl, ent, M.lj_tab, M.fix, b->partials, b->ticket,
+      P, M.posfx, M.type_s, M.perm, clj, cnl, ent, M.lj_tab, M.fix, b->facc, b->ticket,
       b->scal + SC_MX_PAIR);
   FE_LAUNCH_CHECK("k_mx_pair");
   return FE_OK;
@@ -1115,30 +1316,44 @@ int forces_mixed(Box *b) {
   FE_CUDA(cudaMemsetAsync(M.fix, 0, sizeof(unsigned long long) * 3 * n, b->stream));
   if ((rc = launch_mx_pair_only(b))) return rc;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
-  // exclusions
-  double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
-  int xb = (M.nexcl + 255) / 256;
-  if (xb > 1024) xb = 1024;
-  if (xb < 1) xb = 1;
-  k_mx_excl<<<xb, 256, 0, b->stream>>>(M.nexcl, M.excl_ab, M.excl_flag, b->pos_q, b->type, L, b->nt,
-                                       M.lj_tab, (float)(b->p.rc * b->p.rc), (float)b->p.kappa,
-                                       (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
-                                       (float)b->p.epsRF, M.fix, b->partials, b->ticket,
-                                       b->scal + SC_MX_EXCL);
-  FE_LAUNCH_CHECK("k_mx_excl");
-  // bonded
-  int tot = b->nbond + b->nbend;
-  int bb = (tot + 255) / 256;
-  if (bb > 1024) bb = 1024;
-  if (bb < 1) bb = 1;
-  k_mx_bonded<<<bb, 256, 0, b->stream>>>(b->nbond, b->nbend, L, b->pos_q, b->bond_ab, b->bond_req,
-                                         b->bond_k, b->bend_abc, b->bend_t0, b->bend_k, M.fix,
-                                         b->partials, b->ticket, b->scal + SC_BOND);
-  FE_LAUNCH_CHECK("k_mx_bonded");
+  // intramolecular terms: one thread per molecule when the topology allows,
+  // else the exclusion and bonded kernels
+  float3 sL = fix_scale(b);
+  if (M.nmol > 0) {
+    int mb = (M.nmol + 127) / 128;
+    if (mb > 2048) mb = 2048;
+    k_mx_intra<<<mb, 128, 0, b->stream>>>(
+        M.nmol, M.mol_first, M.mol_x, M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai, M.excl_ab,
+        M.excl_flag, b->bond_ab, b->bond_req, b->bond_k, b->bend_abc, b->bend_t0, b->bend_k,
+        M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),
+        (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,
+        M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA);
+    FE_LAUNCH_CHECK("k_mx_intra");
+  } else {
+    int xb = (M.nexcl + 255) / 256;
+    if (xb > 1024) xb = 1024;
+    if (xb < 1) xb = 1;
+    k_mx_excl<<<xb, 256, 0, b->stream>>>(M.nexcl, M.excl_ab, M.excl_flag, M.posfx, M.iperm,
+                                         b->type, sL, b->nt, M.lj_tab,
+                                         (float)(b->p.rc * b->p.rc), (float)b->p.kappa,
+                                         (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
+                                         (float)b->p.epsRF, M.fix, b->facc, b->ticket,
+                                         b->scal + SC_MX_EXCL);
+    FE_LAUNCH_CHECK("k_mx_excl");
+    int tot = b->nbond + b->nbend;
+    int bb = (tot + 255) / 256;
+    if (bb > 1024) bb = 1024;
+    if (bb < 1) bb = 1;
+    k_mx_bonded<<<bb, 256, 0, b->stream>>>(b->nbond, b->nbend, sL, M.posfx, M.iperm, b->bond_ab,
+                                           b->bond_req, b->bond_k, b->bend_abc, b->bend_t0,
+                                           b->bend_k, M.fix, b->facc, b->ticket,
+                                           b->scal + SC_BOND);
+    FE_LAUNCH_CHECK("k_mx_bonded");
+  }
   // SPME
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   FE_CUDA(cudaMemsetAsync(b->gbin_count, 0, sizeof(int) * b->K, b->stream));
-  k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, L, b->pos_q, M.perm, M.floor3,
+  k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, M.posfx, M.floor3,
                                                        M.sm, M.sd, b->gcap, b->gbin_count,
                                                        b->gbin_atoms, b->status);
   FE_LAUNCH_CHECK("k_mx_splines");
@@ -1152,7 +1367,7 @@ int forces_mixed(Box *b) {
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
   int kb = (int)((b->Kh + 255) / 256);
   if (kb > 1024) kb = 1024;
-  k_mx_recip<<<kb, 256, 0, b->stream>>>(b->Kh, M.eterm32, M.kw32, M.grid32k, b->partials,
+  k_mx_recip<<<kb, 256, 0, b->stream>>>(b->Kh, M.eterm32, M.kw32, M.grid32k, b->facc,
                                         b->ticket, b->scal + SC_ENREC);
   FE_LAUNCH_CHECK("k_mx_recip");
   r = cufftSetStream(M.plan_c2r, b->stream);
@@ -1165,7 +1380,7 @@ int forces_mixed(Box *b) {
   if (gb > 1024) gb = 1024;
   float qfe = (float)(qf / b->p.epsRF);
   k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3, M.sm,
-                                         M.sd, M.grid32, M.fix, b->partials, b->ticket,
+                                         M.sd, M.grid32, M.fix, b->facc, b->ticket,
                                          b->scal + SC_FMEAN);
   FE_LAUNCH_CHECK("k_mx_gather");
   k_mx_finalize<<<(3 * n + 255) / 256, 256, 0, b->stream>>>(n, M.fix, b->scal, b->ff);
@@ -1174,7 +1389,7 @@ int forces_mixed(Box *b) {
 }
 
 int launch_mixed_assemble(Box *b) {
-  k_mx_slots<<<1, 32, 0, b->stream>>>(b->scal, b->mx->erfc_rc_over_rc);
+  k_mx_slots<<<1, 32, 0, b->stream>>>(b->scal, b->mx->erfc_rc_over_rc, b->mx->nmol > 0 ? 1 : 0);
   FE_LAUNCH_CHECK("k_mx_slots");
   return launch_assemble_energies(b, 1);
 }
