@@ -218,9 +218,11 @@ def batched_sample(local, steps):
           for k, m in enumerate(nmol)]
     boxes = [engine.Box(s, precision=engine.FE_PREC_MIXED, device=local) for s in ss]
     try:
+        shapes = []
         for b in boxes:
             b.nblist()
             b.forces()
+            shapes.append(b.autotune()[:2])  # per-box launch shape (uneven sizes)
         batch = engine.Batch(boxes, seed=SEED)
         # warm up to step 480 so that the timed steps include the exchange at step 500
         batch.run(480, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
@@ -248,7 +250,8 @@ def batched_sample(local, steps):
                         "sites/A^3, grid ~1 point/A, T 300-400 K, exchange every 500 steps",
             "exchange_attempts": int(state["attempts"]),
             "exchanges_in_timed_steps": n_ex, "list_steps": n_list,
-            "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]}}
+            "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]},
+            "pair_launch_shapes": sorted(set(tuple(x) for x in shapes))}
 
 
 def go_sample(local):
@@ -378,6 +381,7 @@ def run_ours(args, world, rank, local):
     box.forces()
     box.kinet()
     f_mixed0 = box.get_forces()
+    tune = box.autotune()  # launch shape of the pair kernel for this box (untimed)
     W = max(args.warmup, 3)
     K = args.steps
     box.run_md(W, first_step=1)
@@ -534,7 +538,9 @@ def run_ours(args, world, rank, local):
         "roofline": {"kernel": "k_mx_pair", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
-                     "us_per_launch": pair_us, "list_entries": entries, "max_row": max_row},
+                     "us_per_launch": pair_us, "list_entries": entries, "max_row": max_row,
+                     "launch_shape": {"warps_per_block": tune[0], "blocks": tune[1],
+                                      "chosen_by": "autotune (events, this box)"}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "steps": ke},

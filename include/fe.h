@@ -387,6 +387,15 @@ int fe_go_state(fe_go *go, double *pos, double *vel, double *T, double *epot, in
                 int64_t *accepted, int64_t *attempted, uint64_t *steps);
 int fe_go_get_stream(fe_go *go, void **stream);
 
+/* ---- launch-shape autotuning (no counterpart in the reference) --------- */
+
+/* Times the mixed-precision pair kernel over the box's current list for
+ * warps per block in {4, 8, 16} and several grid sizes and keeps the fastest
+ * for this box (results do not depend on the shape: forces are fixed-point
+ * sums).  choice2 = {warps per block, blocks}, *us = its time per launch.
+ * Recomputes the forces afterwards; a no-op for FP64 boxes. */
+int fe_autotune(fe_box *box, int *choice2, double *us);
+
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 
 enum { FE_KERNEL_PAIR = 0, FE_KERNEL_SPREAD = 1, FE_KERNEL_LIST = 2 };

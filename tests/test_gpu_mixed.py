@@ -114,3 +114,18 @@ def test_mixed_drift_matches_fp64():
     kT = 1.380662e-23 * 6.022045e23 * s.T * 1e-3
     per_dof = [x * 1000.0 / (kT * (3 * s.n - 3)) for x in slopes]  # kT / ns / dof
     assert abs(per_dof[1] - per_dof[0]) <= 0.1 * max(abs(per_dof[0]), 0.05), per_dof
+
+
+def test_autotune_keeps_results_bitwise(case):
+    """Every launch shape gives the same fixed-point forces and energies."""
+    s, _, _ = case
+    with _mixed(s) as b:
+        b.nblist()
+        e1 = b.forces()
+        f1 = b.get_forces()
+        nw, blocks, us = b.autotune()
+        e2 = b.forces()
+        f2 = b.get_forces()
+    assert nw in (4, 8, 16) and blocks > 0 and us > 0
+    assert np.array_equal(f1, f2)
+    assert e1 == e2

@@ -187,6 +187,20 @@ __device__ __forceinline__ void row_close(const RowCursor &rc, int cap, int s, i
   }
 }
 
+constexpr int kListExcl = 4;  // excluded partners per site compared in registers
+
+// The excluded partners of a site as sorted slots (up to kListExcl; -1
+// pads); *many is set when the site has more (then the lists are searched).
+__device__ __forceinline__ void site_exclusions(int oi, const int *__restrict__ xs,
+                                                const int *__restrict__ xp,
+                                                const int *__restrict__ iperm,
+                                                int (&ex)[kListExcl], bool *many) {
+  int a = xs[oi], nx = xs[oi + 1] - a;
+#pragma unroll
+  for (int q = 0; q < kListExcl; q++) ex[q] = q < nx ? iperm[xp[a + q]] : -1;
+  *many = nx > kListExcl;
+}
+
 // one candidate j of row s: fixed-point distance, exclusion, LJ class
 __device__ __forceinline__ void list_test(int j, int4 pi, int oi, int ti,
                                           const int4 *__restrict__ posfx,
@@ -194,15 +208,22 @@ __device__ __forceinline__ void list_test(int j, int4 pi, int oi, int ti,
                                           const int *__restrict__ type_s, float3 sc, float rl2,
                                           int nt, const unsigned char *__restrict__ lj_on,
                                           const int *__restrict__ xs, const int *__restrict__ xp,
-                                          bool &ok, bool &lj) {
+                                          const int (&ex)[kListExcl], bool many, bool &ok,
+                                          bool &lj) {
   int4 pj = posfx[j];
   float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, sc.x);
   float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, sc.y);
   float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, sc.z);
   float r2 = dx * dx + dy * dy + dz * dz;
-  if (r2 < rl2 && !mx_is_excluded(xs, xp, oi, perm[j])) {
-    ok = true;
-    lj = lj_on[ti * nt + type_s[j]] != 0;
+  if (r2 < rl2) {
+    bool excl = false;
+#pragma unroll
+    for (int q = 0; q < kListExcl; q++) excl |= (ex[q] == j);
+    if (many && !excl) excl = mx_is_excluded(xs, xp, oi, perm[j]);
+    if (!excl) {
+      ok = true;
+      lj = lj_on[ti * nt + type_s[j]] != 0;
+    }
   }
 }
 
@@ -220,7 +241,8 @@ __device__ __forceinline__ float cell_gap(int c, int nc, float u, float L) {
 // come out in a fixed (column, slot) order: deterministic.
 __global__ void __launch_bounds__(kMxWarps * 32)
 k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
-          const int *__restrict__ cell_s, const int *__restrict__ type_s,
+          const int *__restrict__ iperm, const int *__restrict__ cell_s,
+          const int *__restrict__ type_s,
           const int *__restrict__ cstart, int3 nc, float3 sc, float3 Lf, float rlist2, int nt,
           const unsigned char *__restrict__ lj_on, const int *__restrict__ xs,
           const int *__restrict__ xp, int cap, int *__restrict__ cnt_lj,
@@ -233,6 +255,9 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
     int cz = c % nc.z, cy = (c / nc.z) % nc.y, cx = c / (nc.z * nc.y);
     int oi = perm[s];
     int ti = type_s[s];
+    int ex[kListExcl];
+    bool many;
+    site_exclusions(oi, xs, xp, iperm, ex, &many);
     RowCursor rc = {0, 0};
     int *row = ent + (size_t)s * cap;
     if (fast) {
@@ -279,8 +304,8 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
               int j = base + lane;
               bool ok = false, lj = false;
               if (j < j1 && j != s)
-                list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ok,
-                          lj);
+                list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ex,
+                          many, ok, lj);
               row_push(ok, lj, j, lane, cap, row, rc);
             }
           }
@@ -295,7 +320,8 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
             int j = base + lane;
             bool ok = false, lj = false;
             if (j < j1 && j != s)
-              list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ok, lj);
+              list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ex, many,
+                        ok, lj);
             row_push(ok, lj, j, lane, cap, row, rc);
           }
         }
@@ -446,7 +472,10 @@ __device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
   }
 }
 
-__global__ void __launch_bounds__(kMxWarps * 32, 6)
+// NW warps per block (a launch shape chosen by mixed_autotune); the register
+// budget is the same for every shape: 48 resident warps per SM.
+template <int NW>
+__global__ void __launch_bounds__(NW * 32, 48 / NW)
 k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
           const int *__restrict__ perm, const int *__restrict__ cnt_lj,
           const int *__restrict__ cnt_nl, const int *__restrict__ ent,
@@ -459,7 +488,7 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   int lane = threadIdx.x & 31;
   PairAcc a;
   a.e_lj = a.e_ljs = a.e_real = a.qsum = 0.f;
-  for (int s = blockIdx.x * kMxWarps + (threadIdx.x >> 5); s < P.n; s += gridDim.x * kMxWarps) {
+  for (int s = blockIdx.x * NW + (threadIdx.x >> 5); s < P.n; s += gridDim.x * NW) {
     int4 pi = posfx[s];
     float qi = __int_as_float(pi.w) * P.qfe;
     const float *ljrow = s_lj + type_s[s] * P.nt * 3;
@@ -1255,7 +1284,8 @@ int launch_mixed_list(Box *b) {
   float3 Lf = make_float3((float)b->p.L[0], (float)b->p.L[1], (float)b->p.L[2]);
   float rl = (float)(b->p.rclist < b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
   k_mx_list<<<list_blocks(b), kMxWarps * 32, 0, b->stream>>>(
-      n, M.posfx, M.perm, M.cell_s, M.type_s, M.cell_start, nc, fix_scale(b), Lf, rl * rl, b->nt,
+      n, M.posfx, M.perm, M.iperm, M.cell_s, M.type_s, M.cell_start, nc, fix_scale(b), Lf, rl * rl,
+      b->nt,
       M.lj_on, b->x_start, b->x_partner, M.cap, M.cnt_lj, M.cnt_nl, M.ent, b->status);
   FE_LAUNCH_CHECK("k_mx_list");
   b->have_list = true;
@@ -1263,8 +1293,8 @@ int launch_mixed_list(Box *b) {
   return FE_OK;
 }
 
-static int pair_blocks(Box *b) {
-  int blocks = (b->n + kMxWarps - 1) / kMxWarps;
+static int pair_blocks(Box *b, int nw) {
+  int blocks = (b->n + nw - 1) / nw;
   return blocks > 2048 ? 2048 : blocks;
 }
 
@@ -1288,10 +1318,68 @@ int launch_mx_pair_only(Box *b) {
   const int *clj = M.use_inner ? M.icnt_lj : M.cnt_lj;
   const int *cnl = M.use_inner ? M.icnt_nl : M.cnt_nl;
   const int *ent = M.use_inner ? M.ient : M.ent;
-  k_mx_pair<<<pair_blocks(b), kMxWarps * 32, shm, b->stream>>>(
-      P, M.posfx, M.type_s, M.perm, clj, cnl, ent, M.lj_tab, M.fix, b->facc, b->ticket,
-      b->scal + SC_MX_PAIR);
+  int nw = M.tune_nw, blocks = M.tune_blocks > 0 ? M.tune_blocks : pair_blocks(b, nw);
+#define FE_PAIR_LAUNCH(NWV)                                                                   \
+  k_mx_pair<NWV><<<blocks, NWV * 32, shm, b->stream>>>(P, M.posfx, M.type_s, M.perm, clj, cnl, \
+                                                       ent, M.lj_tab, M.fix, b->facc,         \
+                                                       b->ticket, b->scal + SC_MX_PAIR)
+  if (nw == 4) FE_PAIR_LAUNCH(4);
+  else if (nw == 16) FE_PAIR_LAUNCH(16);
+  else FE_PAIR_LAUNCH(8);
+#undef FE_PAIR_LAUNCH
   FE_LAUNCH_CHECK("k_mx_pair");
+  return FE_OK;
+}
+
+// Chooses the pair kernel's launch shape for this box: warps per block in
+// {4, 8, 16} and the grid size (multiples of the SM count, or one warp per
+// row), each timed with CUDA events on the box's stream over the current
+// list; the fastest is kept.  Forces and energies must be recomputed after.
+int mixed_autotune(Box *b, int *nw_out, int *blocks_out, double *us_out) {
+  Mixed &M = *b->mx;
+  int nsm = 0;
+  FE_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev));
+  const int nws[3] = {4, 8, 16};
+  cudaEvent_t e0, e1;
+  FE_CUDA(cudaEventCreate(&e0));
+  FE_CUDA(cudaEventCreate(&e1));
+  int best_nw = M.tune_nw, best_blocks = M.tune_blocks;
+  float best = 1e30f;
+  int rc = FE_OK;
+  for (int a = 0; a < 3 && rc == FE_OK; a++) {
+    int nw = nws[a];
+    int full = (b->n + nw - 1) / nw;
+    int grids[6] = {nsm * 4, nsm * 8, nsm * 12, nsm * 16, nsm * 24, full};
+    for (int g = 0; g < 6 && rc == FE_OK; g++) {
+      int blocks = grids[g] < full ? grids[g] : full;
+      M.tune_nw = nw;
+      M.tune_blocks = blocks;
+      if ((rc = launch_mx_pair_only(b))) break;  // warm-up
+      cudaEventRecord(e0, b->stream);
+      for (int r = 0; r < 3 && rc == FE_OK; r++) rc = launch_mx_pair_only(b);
+      cudaEventRecord(e1, b->stream);
+      cudaError_t e = cudaEventSynchronize(e1);
+      if (e != cudaSuccess) {
+        rc = cuda_fail(e, "mixed_autotune");
+        break;
+      }
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      if (ms < best) {
+        best = ms;
+        best_nw = nw;
+        best_blocks = blocks;
+      }
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  M.tune_nw = best_nw;
+  M.tune_blocks = best_blocks;
+  if (rc) return rc;
+  if (nw_out) *nw_out = best_nw;
+  if (blocks_out) *blocks_out = best_blocks;
+  if (us_out) *us_out = 1000.0 * best / 3.0;
   return FE_OK;
 }
 

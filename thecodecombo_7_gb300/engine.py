@@ -55,7 +55,7 @@ EXPORTS = [
     "fe_mc_chains_collect", "fe_mc_chains_samples", "fe_mc_chains_train_surrogate",
     "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
-    "fe_go_get_stream",
+    "fe_go_get_stream", "fe_autotune",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -350,6 +350,14 @@ class Box:
         self._check(self.lib.fe_run_md(self.h, int(nsteps), int(nl), int(use_nhc),
                                        C.c_long(first_step), _p(rec) if record else None))
         return rec[:nsteps] if record else None
+
+    def autotune(self):
+        """Picks the pair kernel's launch shape for this box (mixed precision);
+        returns (warps per block, blocks, us per launch)."""
+        ch = np.zeros(2, np.int32)
+        us = C.c_double()
+        self._check(self.lib.fe_autotune(self.h, _p(ch), C.byref(us)))
+        return int(ch[0]), int(ch[1]), us.value
 
     # ---- instrumentation ----
     def time_kernel(self, which=FE_KERNEL_PAIR, reps=20):
