@@ -222,7 +222,7 @@ def batched_sample(local, steps):
         for b in boxes:
             b.nblist()
             b.forces()
-            shapes.append(b.autotune()[:2])  # per-box launch shape (uneven sizes)
+            shapes.append(b.autotune()[:3])  # per-box launch shape (uneven sizes)
         batch = engine.Batch(boxes, seed=SEED)
         # warm up to step 480 so that the timed steps include the exchange at step 500
         batch.run(480, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
@@ -539,7 +539,8 @@ def run_ours(args, world, rank, local):
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
                      "us_per_launch": pair_us, "list_entries": entries, "max_row": max_row,
-                     "launch_shape": {"warps_per_block": tune[0], "blocks": tune[1],
+                     "launch_shape": {"warps_per_block": tune[0], "registers": tune[1],
+                                      "blocks": tune[2],
                                       "chosen_by": "autotune (events, this box)"}},
         "cpu_baseline": cpu,
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": h2d,

@@ -390,11 +390,12 @@ int fe_go_get_stream(fe_go *go, void **stream);
 /* ---- launch-shape autotuning (no counterpart in the reference) --------- */
 
 /* Times the mixed-precision pair kernel over the box's current list for
- * warps per block in {4, 8, 16} and several grid sizes and keeps the fastest
- * for this box (results do not depend on the shape: forces are fixed-point
- * sums).  choice2 = {warps per block, blocks}, *us = its time per launch.
+ * warps per block in {4, 8, 16}, register budgets of 40 and 64 per thread
+ * and several grid sizes, and keeps the fastest for this box (results do not
+ * depend on the shape: forces are fixed-point sums).  choice3 = {warps per
+ * block, registers per thread, blocks}, *us = its time per launch.
  * Recomputes the forces afterwards; a no-op for FP64 boxes. */
-int fe_autotune(fe_box *box, int *choice2, double *us);
+int fe_autotune(fe_box *box, int *choice3, double *us);
 
 /* ---- instrumentation (no counterpart in the reference) ----------------- */
 

@@ -123,9 +123,9 @@ def test_autotune_keeps_results_bitwise(case):
         b.nblist()
         e1 = b.forces()
         f1 = b.get_forces()
-        nw, blocks, us = b.autotune()
+        nw, regs, blocks, us = b.autotune()
         e2 = b.forces()
         f2 = b.get_forces()
-    assert nw in (4, 8, 16) and blocks > 0 and us > 0
+    assert nw in (4, 8, 16) and regs in (40, 64) and blocks > 0 and us > 0
     assert np.array_equal(f1, f2)
     assert e1 == e2

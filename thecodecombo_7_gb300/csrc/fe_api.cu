@@ -717,7 +717,7 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
   return FE_OK;
 }
 
-int fe_autotune(fe_box *box, int *choice2, double *us) {
+int fe_autotune(fe_box *box, int *choice3, double *us) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;
   if (!b->mx) return FE_OK;  // the FP64 drop-in keeps the reference's one-row-per-warp shape
@@ -725,12 +725,13 @@ int fe_autotune(fe_box *box, int *choice2, double *us) {
     set_error("fe_autotune needs a neighbour list");
     return FE_ERR_STATE;
   }
-  int nw = 0, blocks = 0;
-  int rc = mixed_autotune(b, &nw, &blocks, us);
+  int nw = 0, rw = 0, blocks = 0;
+  int rc = mixed_autotune(b, &nw, &rw, &blocks, us);
   if (rc) return rc;
-  if (choice2) {
-    choice2[0] = nw;
-    choice2[1] = blocks;
+  if (choice3) {
+    choice3[0] = nw;
+    choice3[1] = (65536 / (rw * 32)) & ~7;  // the per-thread register cap it compiles to
+    choice3[2] = blocks;
   }
   b->g_key = -1;  // step graphs are recaptured with the new shape
   return forces_device(b);

@@ -44,6 +44,7 @@ struct Mixed {
   double erfc_rc_over_rc = 0.0;
   // pair kernel launch shape (mixed_autotune): warps per block, grid (0: one warp per row)
   int tune_nw = 8;
+  int tune_rw = 48;     // resident warps per SM the register budget is sized for
   int tune_blocks = 0;
   // Molecules for the fused intramolecular kernel: every bonded and excluded
   // pair lies inside a contiguous run of at most kIntraMaxSites sites.
@@ -64,7 +65,7 @@ int forces_mixed(Box *b);
 int launch_mixed_assemble(Box *b);
 int launch_mx_pair_only(Box *b);    // the pair kernel alone (timing)
 int launch_mx_spread_only(Box *b);  // the spreading kernel alone (timing)
-int mixed_autotune(Box *b, int *nw, int *blocks, double *us);
+int mixed_autotune(Box *b, int *nw, int *rw, int *blocks, double *us);
 void mixed_counts(Box *b, const int **lj, const int **rest);  // device row counts (outer)
 void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s);
 

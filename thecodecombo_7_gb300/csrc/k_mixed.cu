@@ -472,10 +472,11 @@ __device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
   }
 }
 
-// NW warps per block (a launch shape chosen by mixed_autotune); the register
-// budget is the same for every shape: 48 resident warps per SM.
-template <int NW>
-__global__ void __launch_bounds__(NW * 32, 48 / NW)
+// NW warps per block and a register budget of 65536 / (RW * 32) per thread
+// for RW resident warps per SM (48: 40 registers, 32: 64 registers): a
+// launch shape chosen by mixed_autotune.
+template <int NW, int RW>
+__global__ void __launch_bounds__(NW * 32, RW / NW)
 k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
           const int *__restrict__ perm, const int *__restrict__ cnt_lj,
           const int *__restrict__ cnt_nl, const int *__restrict__ ent,
@@ -496,18 +497,20 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
     a.fx = a.fy = a.fz = 0.f;
     mx_segment<true>(P, pi, qi, row, 0, cnt_lj[s], lane, posfx, ljrow, type_s, a);
     mx_segment<false>(P, pi, qi, row, P.cap - cnt_nl[s], P.cap, lane, posfx, ljrow, type_s, a);
-    long long ix = to_fix(a.fx), iy = to_fix(a.fy), iz = to_fix(a.fz);
+    // the row's force: a fixed butterfly of FP32 partial sums (deterministic),
+    // converted once to the fixed-point accumulators
+    float fx = a.fx, fy = a.fy, fz = a.fz;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-      ix += __shfl_xor_sync(0xffffffffu, ix, o);
-      iy += __shfl_xor_sync(0xffffffffu, iy, o);
-      iz += __shfl_xor_sync(0xffffffffu, iz, o);
+      fx += __shfl_xor_sync(0xffffffffu, fx, o);
+      fy += __shfl_xor_sync(0xffffffffu, fy, o);
+      fz += __shfl_xor_sync(0xffffffffu, fz, o);
     }
     if (lane == 0) {
       int oi = perm[s];
-      atomicAdd(&fix[3 * oi], (unsigned long long)ix);
-      atomicAdd(&fix[3 * oi + 1], (unsigned long long)iy);
-      atomicAdd(&fix[3 * oi + 2], (unsigned long long)iz);
+      atomicAdd(&fix[3 * oi], (unsigned long long)to_fix(fx));
+      atomicAdd(&fix[3 * oi + 1], (unsigned long long)to_fix(fy));
+      atomicAdd(&fix[3 * oi + 2], (unsigned long long)to_fix(fz));
     }
   }
   // every pair was visited from both ends
@@ -1319,40 +1322,48 @@ int launch_mx_pair_only(Box *b) {
   const int *cnl = M.use_inner ? M.icnt_nl : M.cnt_nl;
   const int *ent = M.use_inner ? M.ient : M.ent;
   int nw = M.tune_nw, blocks = M.tune_blocks > 0 ? M.tune_blocks : pair_blocks(b, nw);
-#define FE_PAIR_LAUNCH(NWV)                                                                   \
-  k_mx_pair<NWV><<<blocks, NWV * 32, shm, b->stream>>>(P, M.posfx, M.type_s, M.perm, clj, cnl, \
-                                                       ent, M.lj_tab, M.fix, b->facc,         \
-                                                       b->ticket, b->scal + SC_MX_PAIR)
-  if (nw == 4) FE_PAIR_LAUNCH(4);
-  else if (nw == 16) FE_PAIR_LAUNCH(16);
-  else FE_PAIR_LAUNCH(8);
+#define FE_PAIR_LAUNCH(NWV, RWV)                                                             \
+  k_mx_pair<NWV, RWV><<<blocks, NWV * 32, shm, b->stream>>>(P, M.posfx, M.type_s, M.perm, clj, \
+                                                            cnl, ent, M.lj_tab, M.fix, b->facc, \
+                                                            b->ticket, b->scal + SC_MX_PAIR)
+  if (M.tune_rw == 32) {
+    if (nw == 4) FE_PAIR_LAUNCH(4, 32);
+    else if (nw == 16) FE_PAIR_LAUNCH(16, 32);
+    else FE_PAIR_LAUNCH(8, 32);
+  } else {
+    if (nw == 4) FE_PAIR_LAUNCH(4, 48);
+    else if (nw == 16) FE_PAIR_LAUNCH(16, 48);
+    else FE_PAIR_LAUNCH(8, 48);
+  }
 #undef FE_PAIR_LAUNCH
   FE_LAUNCH_CHECK("k_mx_pair");
   return FE_OK;
 }
 
 // Chooses the pair kernel's launch shape for this box: warps per block in
-// {4, 8, 16} and the grid size (multiples of the SM count, or one warp per
-// row), each timed with CUDA events on the box's stream over the current
-// list; the fastest is kept.  Forces and energies must be recomputed after.
-int mixed_autotune(Box *b, int *nw_out, int *blocks_out, double *us_out) {
+// {4, 8, 16}, register budget (40 or 64 per thread) and the grid size
+// (multiples of the SM count, or one warp per row), each timed with CUDA
+// events on the box's stream over the current list; the fastest is kept.
+// Forces and energies must be recomputed after.
+int mixed_autotune(Box *b, int *nw_out, int *rw_out, int *blocks_out, double *us_out) {
   Mixed &M = *b->mx;
   int nsm = 0;
   FE_CUDA(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, b->dev));
-  const int nws[3] = {4, 8, 16};
+  const int nws[3] = {4, 8, 16}, rws[2] = {48, 32};
   cudaEvent_t e0, e1;
   FE_CUDA(cudaEventCreate(&e0));
   FE_CUDA(cudaEventCreate(&e1));
-  int best_nw = M.tune_nw, best_blocks = M.tune_blocks;
+  int best_nw = M.tune_nw, best_blocks = M.tune_blocks, best_rw = M.tune_rw;
   float best = 1e30f;
   int rc = FE_OK;
-  for (int a = 0; a < 3 && rc == FE_OK; a++) {
-    int nw = nws[a];
+  for (int c = 0; c < 6 && rc == FE_OK; c++) {
+    int nw = nws[c % 3], rw = rws[c / 3];
     int full = (b->n + nw - 1) / nw;
     int grids[6] = {nsm * 4, nsm * 8, nsm * 12, nsm * 16, nsm * 24, full};
     for (int g = 0; g < 6 && rc == FE_OK; g++) {
       int blocks = grids[g] < full ? grids[g] : full;
       M.tune_nw = nw;
+      M.tune_rw = rw;
       M.tune_blocks = blocks;
       if ((rc = launch_mx_pair_only(b))) break;  // warm-up
       cudaEventRecord(e0, b->stream);
@@ -1368,6 +1379,7 @@ int mixed_autotune(Box *b, int *nw_out, int *blocks_out, double *us_out) {
       if (ms < best) {
         best = ms;
         best_nw = nw;
+        best_rw = rw;
         best_blocks = blocks;
       }
     }
@@ -1375,9 +1387,11 @@ int mixed_autotune(Box *b, int *nw_out, int *blocks_out, double *us_out) {
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
   M.tune_nw = best_nw;
+  M.tune_rw = best_rw;
   M.tune_blocks = best_blocks;
   if (rc) return rc;
   if (nw_out) *nw_out = best_nw;
+  if (rw_out) *rw_out = best_rw;
   if (blocks_out) *blocks_out = best_blocks;
   if (us_out) *us_out = 1000.0 * best / 3.0;
   return FE_OK;

@@ -353,11 +353,11 @@ class Box:
 
     def autotune(self):
         """Picks the pair kernel's launch shape for this box (mixed precision);
-        returns (warps per block, blocks, us per launch)."""
-        ch = np.zeros(2, np.int32)
+        returns (warps per block, registers per thread, blocks, us per launch)."""
+        ch = np.zeros(3, np.int32)
         us = C.c_double()
         self._check(self.lib.fe_autotune(self.h, _p(ch), C.byref(us)))
-        return int(ch[0]), int(ch[1]), us.value
+        return int(ch[0]), int(ch[1]), int(ch[2]), us.value
 
     # ---- instrumentation ----
     def time_kernel(self, which=FE_KERNEL_PAIR, reps=20):
