@@ -86,7 +86,7 @@ static void free_box(Box *b) {
                   b->bond_req, b->bond_k, b->bend_t0, b->bend_k, b->cell_count, b->cell_start,
                   b->cell_fill, b->cell_atoms, b->cell_of, b->nl_count, b->nl_ent, b->eterm,
                   b->kweight, b->grid, b->grid_k, b->spl_floor, b->spl_m, b->spl_d, b->fp,
-                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->facc, b->zeta, b->rec,
+                  b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->facc, b->xyz_dev, b->zeta, b->rec,
                   b->rec_counter};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -238,6 +238,7 @@ static int create(Box *b, const fe_box_params *p) {
   FE_CUDA(cudaMemset(b->ticket, 0, sizeof(unsigned)));
   FE_CUDA(cudaMallocHost(&b->host_scal, sizeof(double) * SC_COUNT));
   FE_CUDA(cudaMallocHost(&b->stage, sizeof(double) * 4 * (size_t)n));
+  FE_CUDA(cudaMalloc(&b->xyz_dev, sizeof(double) * 3 * (size_t)n));
   FE_CUDA(cudaMalloc(&b->rec_counter, sizeof(int)));
   // self energy, ewald.c:61,172-178
   double fconv = (kELEC * kELEQ * kELEQ * kNA * 0.001) / p->epsRF;
@@ -270,20 +271,57 @@ static int create(Box *b, const fe_box_params *p) {
   return FE_OK;
 }
 
-static int stage_xyz_in(Box *b, const void *atoms, size_t stride, size_t off, std::vector<double> &v) {
+// Host <-> device transfer of x, y, z from `struct atoms`-like records.  A
+// contiguous xyz array (stride 24, offset 0) in page-locked memory is copied
+// by DMA as it is; anything else is packed through the box's pinned staging
+// buffer.  One linear copy either way; the double4 layout is handled by a
+// kernel on the device.
+static bool pinned_host(const void *p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+static int xyz_to_device(Box *b, const void *atoms, size_t stride, size_t off, double *dst) {
   if (!atoms || stride < 24) {
     set_error("positions: null pointer or stride < 24");
     return FE_ERR_ARG;
   }
-  v.resize(3 * (size_t)b->n);
+  size_t bytes = sizeof(double) * 3 * (size_t)b->n;
   const char *base = (const char *)atoms + off;
-  for (int i = 0; i < b->n; i++) memcpy(&v[3 * (size_t)i], base + (size_t)i * stride, 24);
+  const void *src = base;
+  if (!(stride == 24 && pinned_host(base))) {
+    double *st = b->stage;
+    if (stride == 24) memcpy(st, base, bytes);
+    else
+      for (int i = 0; i < b->n; i++) memcpy(st + 3 * (size_t)i, base + (size_t)i * stride, 24);
+    src = st;
+  }
+  FE_CUDA(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, b->stream));
   return FE_OK;
 }
 
-static void stage_xyz_out(Box *b, void *atoms, size_t stride, size_t off, const std::vector<double> &v) {
+static int xyz_to_host(Box *b, const double *src, void *atoms, size_t stride, size_t off) {
+  if (!atoms || stride < 24) {
+    set_error("positions: null pointer or stride < 24");
+    return FE_ERR_ARG;
+  }
+  size_t bytes = sizeof(double) * 3 * (size_t)b->n;
   char *base = (char *)atoms + off;
-  for (int i = 0; i < b->n; i++) memcpy(base + (size_t)i * stride, &v[3 * (size_t)i], 24);
+  bool direct = stride == 24 && pinned_host(base);
+  FE_CUDA(cudaMemcpyAsync(direct ? (void *)base : (void *)b->stage, src, bytes,
+                          cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  if (!direct) {
+    const double *st = b->stage;
+    if (stride == 24) memcpy(base, st, bytes);
+    else
+      for (int i = 0; i < b->n; i++) memcpy(base + (size_t)i * stride, st + 3 * (size_t)i, 24);
+  }
+  return FE_OK;
 }
 
 // one step of the production loop (graph body); `prune` refreshes the mixed
@@ -397,56 +435,33 @@ int fe_box_set_stream(fe_box *box, void *stream) {
 int fe_set_positions(fe_box *box, const void *atoms, size_t stride, size_t off_x, int nopbc) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;
-  if (!atoms || stride < 24) {
-    set_error("positions: null pointer or stride < 24");
-    return FE_ERR_ARG;
-  }
-  // gather x, y, z into pinned staging laid out as double4 (q untouched on the device)
-  double *st = b->stage;
-  const char *base = (const char *)atoms + off_x;
-  for (int i = 0; i < b->n; i++) memcpy(st + 4 * (size_t)i, base + (size_t)i * stride, 24);
-  FE_CUDA(cudaMemcpy2DAsync(b->pos_q, sizeof(double4), st, sizeof(double4), 3 * sizeof(double),
-                            b->n, cudaMemcpyHostToDevice, b->stream));
-  if (nopbc)
-    FE_CUDA(cudaMemcpy2DAsync(b->pos_nopbc, 3 * sizeof(double), st, sizeof(double4),
-                              3 * sizeof(double), b->n, cudaMemcpyHostToDevice, b->stream));
+  int rc = xyz_to_device(b, atoms, stride, off_x, b->xyz_dev);
+  if (rc) return rc;
+  if ((rc = launch_xyz_scatter(b, b->xyz_dev, true, nopbc != 0))) return rc;
   FE_CUDA(cudaStreamSynchronize(b->stream));
   return FE_OK;
 }
 
 int fe_get_positions(fe_box *box, void *atoms, size_t stride, size_t off_x) {
-  if (!box || !atoms || stride < 24) return FE_ERR_ARG;
+  if (!box) return FE_ERR_ARG;
   Box *b = &box->b;
-  double *st = b->stage;
-  FE_CUDA(cudaMemcpy2DAsync(st, 3 * sizeof(double), b->pos_q, sizeof(double4), 3 * sizeof(double),
-                            b->n, cudaMemcpyDeviceToHost, b->stream));
-  FE_CUDA(cudaStreamSynchronize(b->stream));
-  char *base = (char *)atoms + off_x;
-  for (int i = 0; i < b->n; i++) memcpy(base + (size_t)i * stride, st + 3 * (size_t)i, 24);
-  return FE_OK;
+  int rc = launch_xyz_gather(b, b->xyz_dev);
+  if (rc) return rc;
+  return xyz_to_host(b, b->xyz_dev, atoms, stride, off_x);
 }
 
 int fe_set_positions_nopbc(fe_box *box, const void *atoms, size_t stride, size_t off_x) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;
-  std::vector<double> v;
-  int rc = stage_xyz_in(b, atoms, stride, off_x, v);
+  int rc = xyz_to_device(b, atoms, stride, off_x, b->pos_nopbc);
   if (rc) return rc;
-  FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, v.data(), sizeof(double) * 3 * b->n, cudaMemcpyHostToDevice,
-                          b->stream));
   FE_CUDA(cudaStreamSynchronize(b->stream));
   return FE_OK;
 }
 
 int fe_get_positions_nopbc(fe_box *box, void *atoms, size_t stride, size_t off_x) {
-  if (!box || !atoms || stride < 24) return FE_ERR_ARG;
-  Box *b = &box->b;
-  std::vector<double> v(3 * (size_t)b->n);
-  FE_CUDA(cudaMemcpyAsync(v.data(), b->pos_nopbc, sizeof(double) * 3 * b->n, cudaMemcpyDeviceToHost,
-                          b->stream));
-  FE_CUDA(cudaStreamSynchronize(b->stream));
-  stage_xyz_out(b, atoms, stride, off_x, v);
-  return FE_OK;
+  if (!box) return FE_ERR_ARG;
+  return xyz_to_host(&box->b, box->b.pos_nopbc, atoms, stride, off_x);
 }
 
 int fe_set_velocities(fe_box *box, const double *vv, const double *uu) {

@@ -139,7 +139,8 @@ struct Box {
   int g_key = -1;              // graph capture key (use_nhc)
   int launches_plain = 0, launches_list = 0, launches_prune = 0;  // own kernels per step
   int prune_every = 2;         // mixed path: inner-list prune period in fe_run_md
-  double *stage = nullptr;     // pinned host staging, 3n doubles
+  double *stage = nullptr;     // pinned host staging, 4n doubles
+  double *xyz_dev = nullptr;   // device staging, 3n doubles (packed x, y, z)
 
   // MC (classic Ewald)
   int mc_nk = 0, mc_kmax = 0, mc_mks = 0;
@@ -205,6 +206,9 @@ int launch_nhc(Box *b, double time_step);
 int launch_record(Box *b);
 // one MD step of the box on its stream (nve_md.c:359-418 / nvt_md.c:529-531)
 int step_body(Box *b, bool with_list, bool use_nhc, bool prune);
+// packed xyz (3n doubles) <-> the double4 positions, on the box's stream
+int launch_xyz_scatter(Box *b, const double *xyz, bool to_pos, bool to_nopbc);
+int launch_xyz_gather(Box *b, double *xyz);
 // instrumentation: relaunch one kernel (FE_KERNEL_*) on the current state
 int relaunch_kernel(Box *b, int which);
 // k_mc.cu

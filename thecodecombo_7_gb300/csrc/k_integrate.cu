@@ -345,6 +345,47 @@ __global__ void k_record(const double *__restrict__ s, double *__restrict__ rec,
   if (threadIdx.x == 0) *counter = c + 1;
 }
 
+__global__ void k_xyz_scatter(int n, const double *__restrict__ xyz, double4 *__restrict__ pos,
+                              double *__restrict__ nopbc) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+  if (pos) {
+    double4 p = pos[i];
+    p.x = x;
+    p.y = y;
+    p.z = z;
+    pos[i] = p;
+  }
+  if (nopbc) {
+    nopbc[3 * i] = x;
+    nopbc[3 * i + 1] = y;
+    nopbc[3 * i + 2] = z;
+  }
+}
+
+__global__ void k_xyz_gather(int n, const double4 *__restrict__ pos, double *__restrict__ xyz) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double4 p = pos[i];
+  xyz[3 * i] = p.x;
+  xyz[3 * i + 1] = p.y;
+  xyz[3 * i + 2] = p.z;
+}
+
+int launch_xyz_scatter(Box *b, const double *xyz, bool to_pos, bool to_nopbc) {
+  k_xyz_scatter<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, xyz, to_pos ? b->pos_q : nullptr,
+                                                           to_nopbc ? b->pos_nopbc : nullptr);
+  FE_LAUNCH_CHECK("k_xyz_scatter");
+  return FE_OK;
+}
+
+int launch_xyz_gather(Box *b, double *xyz) {
+  k_xyz_gather<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->pos_q, xyz);
+  FE_LAUNCH_CHECK("k_xyz_gather");
+  return FE_OK;
+}
+
 int launch_record(Box *b) {
   k_record<<<1, 32, 0, b->stream>>>(b->scal, b->rec, b->rec_cap, b->rec_counter);
   FE_LAUNCH_CHECK("k_record");
