@@ -77,15 +77,16 @@ __device__ __forceinline__ bool block_partials_final(double (&v)[NT], double *pa
 }
 
 // Deterministic grid-wide sum of NT values per thread through 64-bit fixed
-// point: each warp first sums its lanes in a fixed butterfly order in the
-// values' own type, the warp sum is rounded to an integer multiple of
-// 2^-shift, and the integer sums across warps and blocks are exact and
-// independent of order, so the hot kernels need no FP64 arithmetic for
-// their reductions.  Each block adds its sums to
+// point: FP32 values are first summed over the warp in a fixed butterfly
+// order, FP64 and integer values are converted per lane; the (warp or lane)
+// values are rounded to integer multiples of 2^-shift, and the integer sums
+// across lanes, warps and blocks are exact and independent of order, so the
+// hot kernels need no FP64 arithmetic for their reductions.  Each block adds its sums to
 // acc[0..NT) (one atomic per value); the last block to finish writes
 // out[t] = acc[t] * 2^-shift as doubles and leaves acc and ticket at zero.
 // blockDim.x a multiple of 32, at most 1024; NT <= blockDim.x.  Per-thread
-// warp sums must stay below 2^(63 - shift) in magnitude, and so must the total.
+// (warp or lane) values must stay below 2^(63 - shift) in magnitude, and so
+// must the total.
 __device__ __forceinline__ long long to_fixed(float x, int shift) {
   return __float2ll_rn(x * __int_as_float((127 + shift) << 23));
 }
@@ -104,10 +105,19 @@ __device__ __forceinline__ bool block_fix_final(const T (&v)[NT], int shift,
   long long q[NT];
 #pragma unroll
   for (int t = 0; t < NT; t++) {
-    T w = v[t];
+    if (sizeof(T) == sizeof(float)) {
+      // FP32 lanes: a fixed butterfly in FP32, one conversion per warp
+      T w = v[t];
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
-    q[t] = to_fixed(w, shift);
+      for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+      q[t] = to_fixed(w, shift);
+    } else {
+      // FP64 or integer lanes: convert per lane, integer butterfly (FP64 adds
+      // cost more than conversions on this GPU)
+      q[t] = to_fixed(v[t], shift);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) q[t] += __shfl_xor_sync(0xffffffffu, q[t], o);
+    }
     if (lane == 0) shq[wid][t] = q[t];
   }
   __syncthreads();

@@ -36,8 +36,6 @@ constexpr float kInvTwo32 = 2.3283064365386963e-10f;  // 2^-32
 constexpr int kMxWarps = 8;                 // warps per block (list, prune, pair)
 constexpr int kMxMaxCellAtoms = 2048;       // sites per cell a sort block handles
 constexpr int kBrick = 8;                   // spreading brick edge (grid points)
-constexpr int kSp4Warps = 4;
-constexpr int kSp4MaxSites = 1024;
 
 __device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScaleF); }
 
@@ -488,13 +486,19 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   __syncthreads();
   int lane = threadIdx.x & 31;
   PairAcc a;
-  a.e_lj = a.e_ljs = a.e_real = a.qsum = 0.f;
+  // energies per row in FP32, then exact fixed-point sums across rows (kept
+  // in shared memory by each warp's lane 0): the totals do not depend on how
+  // rows are spread over warps (the launch shape)
+  __shared__ long long weq[NW][4];
+  if (lane < 4) weq[threadIdx.x >> 5][lane] = 0;
+  __syncwarp();
   for (int s = blockIdx.x * NW + (threadIdx.x >> 5); s < P.n; s += gridDim.x * NW) {
     int4 pi = posfx[s];
     float qi = __int_as_float(pi.w) * P.qfe;
     const float *ljrow = s_lj + type_s[s] * P.nt * 3;
     const int *row = ent + (size_t)s * P.cap;
     a.fx = a.fy = a.fz = 0.f;
+    a.e_lj = a.e_ljs = a.e_real = a.qsum = 0.f;
     mx_segment<true>(P, pi, qi, row, 0, cnt_lj[s], lane, posfx, ljrow, type_s, a);
     mx_segment<false>(P, pi, qi, row, P.cap - cnt_nl[s], P.cap, lane, posfx, ljrow, type_s, a);
     // the row's force: a fixed butterfly of FP32 partial sums (deterministic),
@@ -506,16 +510,28 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
       fy += __shfl_xor_sync(0xffffffffu, fy, o);
       fz += __shfl_xor_sync(0xffffffffu, fz, o);
     }
+    // every pair is visited from both ends: half of each row's energy
+    float e[4] = {0.5f * a.e_lj, 0.5f * a.e_ljs, 0.5f * a.e_real, 0.5f * a.qsum};
+#pragma unroll
+    for (int t = 0; t < 4; t++) {
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) e[t] += __shfl_xor_sync(0xffffffffu, e[t], o);
+    }
     if (lane == 0) {
       int oi = perm[s];
       atomicAdd(&fix[3 * oi], (unsigned long long)to_fix(fx));
       atomicAdd(&fix[3 * oi + 1], (unsigned long long)to_fix(fy));
       atomicAdd(&fix[3 * oi + 2], (unsigned long long)to_fix(fz));
+#pragma unroll
+      for (int t = 0; t < 4; t++) weq[threadIdx.x >> 5][t] += to_fix(e[t]);
     }
   }
-  // every pair was visited from both ends
-  float v[4] = {0.5f * a.e_lj, 0.5f * a.e_ljs, 0.5f * a.e_real, 0.5f * a.qsum};
-  block_fix_final<4>(v, 32, facc, ticket, out);
+  __syncwarp();
+  long long eq[4] = {0, 0, 0, 0};
+  if (lane == 0)
+#pragma unroll
+    for (int t = 0; t < 4; t++) eq[t] = weq[threadIdx.x >> 5][t];
+  block_fix_final<4>(eq, 32, facc, ticket, out);
 }
 
 // excluded and 1-4 pairs (xint), cnonbond_nblist.c:245-263 and 416-437:
@@ -726,33 +742,36 @@ __global__ void k_mx_binsort(long K, int gcap, int *__restrict__ bcount, int *__
   }
 }
 
-// Spreading by brick-owned accumulation.  A block owns an 8x8x8 brick of
-// grid points held in shared memory and 4 warps; warp w owns the z-slab
-// [2w, 2w + 2).  The block gathers the ids of every site whose spline can
-// reach the brick (bins of floor cells [X0, X0 + 8 + order - 1) per axis, in
-// a fixed cell order) into shared memory; then each warp walks that list in
-// order and, for each site touching its slab, lane (ix, iy, iz) adds
-// theta_x[ix] theta_y[iy] theta_z[.] q to one distinct point.  Every point is
-// written by one warp in site order: deterministic, no atomics.
-__global__ void __launch_bounds__(kSp4Warps * 32)
-k_mx_spread4(int order, int3 G, const int4 *__restrict__ posfx, const float *__restrict__ sm,
+// Spreading by point ownership.  A CTA of 128 threads owns an 8x8x8 brick;
+// thread t owns the column (px, py) = ((t >> 1) >> 3, (t >> 1) & 7) and the
+// four points z in [4 (t & 1), 4 (t & 1) + 4).  The CTA stages the ids of
+// every site whose spline reaches the brick, grouped by halo column (bins of
+// the column, fixed order), then their charge-scaled B-spline weights; each
+// thread then visits only the order x order halo columns that reach its
+// column and adds the weights of its own points.  Every point is summed by
+// one thread in a fixed order: deterministic, with no atomics, no shared
+// accumulator and no per-site synchronisation.
+constexpr int kSp5Threads = 128;
+constexpr int kSp5MaxSites = 512;
+constexpr int kSp5MaxCols = (8 + 8 - 1) * (8 + 8 - 1);  // halo columns at order 8
+
+__global__ void __launch_bounds__(kSp5Threads)
+k_mx_spread5(int order, int3 G, const int4 *__restrict__ posfx, const float *__restrict__ sm,
              int gcap, const int *__restrict__ bcount, const int *__restrict__ batoms,
              float *__restrict__ grid, int *__restrict__ status) {
-  __shared__ float acc[kBrick * kBrick * kBrick];
-  __shared__ int site[kSp4MaxSites];
-  __shared__ int sfloor[kSp4MaxSites];  // local floor cell, 8 bits per axis
-  __shared__ int part[kSp4Warps * 32 + 1];
-  int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  int H = kBrick + order - 1;
-  int nbx = (G.x + kBrick - 1) / kBrick, nby = (G.y + kBrick - 1) / kBrick;
-  int bz = blockIdx.x / (nbx * nby), by = (blockIdx.x / nbx) % nby, bx = blockIdx.x % nbx;
-  int X0 = bx * kBrick, Y0 = by * kBrick, Z0 = bz * kBrick;
-  for (int i = tid; i < kBrick * kBrick * kBrick; i += blockDim.x) acc[i] = 0.f;
-  // halo columns (lx, ly): thread t takes columns t, t + T, ...; each column
-  // is H bins along z.  A block scan of the per-thread counts keeps the fixed
-  // (column, z, slot) order.
-  int T = blockDim.x;
-  int ncol = H * H;
+  __shared__ int site[kSp5MaxSites];
+  __shared__ int sfloor[kSp5MaxSites];  // brick-local floor cell along z
+  __shared__ int part[kSp5Threads + 1];
+  __shared__ int colstart[kSp5MaxCols], colend[kSp5MaxCols];  // staged range of each halo column
+  extern __shared__ float sw[];  // [axis][order][kSp5MaxSites] weights, q folded into x
+  const int tid = threadIdx.x;
+  const int H = kBrick + order - 1;
+  const int nbx = (G.x + kBrick - 1) / kBrick, nby = (G.y + kBrick - 1) / kBrick;
+  const int bz = blockIdx.x / (nbx * nby), by = (blockIdx.x / nbx) % nby, bx = blockIdx.x % nbx;
+  const int X0 = bx * kBrick, Y0 = by * kBrick, Z0 = bz * kBrick;
+  // halo columns: thread t takes columns t, t + T, ...; a block scan of the
+  // per-thread counts keeps the fixed (column, z, slot) order
+  const int T = blockDim.x, ncol = H * H;
   int mine = 0;
   for (int col = tid; col < ncol; col += T) {
     int lx = col / H, ly = col - lx * H;
@@ -772,55 +791,66 @@ k_mx_spread4(int order, int3 G, const int4 *__restrict__ posfx, const float *__r
   }
   __syncthreads();
   int ns = part[T];
-  if (ns > kSp4MaxSites) {
+  if (ns > kSp5MaxSites) {
     if (tid == 0) atomicOr(status, ST_GRID_OVERFLOW);
-    ns = kSp4MaxSites;
+    ns = kSp5MaxSites;
   }
   int w = part[tid];
   for (int col = tid; col < ncol; col += T) {
     int lx = col / H, ly = col - lx * H;
     long base = ((long)wrap1(X0 + lx, G.x) * G.y + wrap1(Y0 + ly, G.y)) * G.z;
+    colstart[col] = min(w, kSp5MaxSites);
     for (int lz = 0; lz < H; lz++) {
       long gc = base + wrap1(Z0 + lz, G.z);
       int m = bcount[gc];
       for (int k = 0; k < m; k++, w++)
-        if (w < kSp4MaxSites) {
+        if (w < kSp5MaxSites) {
           site[w] = batoms[gc * gcap + k];
-          sfloor[w] = (lx << 16) | (ly << 8) | lz;
+          sfloor[w] = lz;
         }
     }
+    colend[col] = min(w, kSp5MaxSites);
   }
   __syncthreads();
-  int ix = lane & 3, iy = (lane >> 2) & 3, iz = lane >> 4;  // 4 x 4 x 2 lane layout
-  int zlo = wid * 2;                                         // slab [zlo, zlo + 2)
-  for (int a = 0; a < ns; a++) {
-    int lf = sfloor[a];
-    int lfz = lf & 255;
-    // stencil z range [lfz - order + 1, lfz] vs this slab
-    if (lfz - order + 1 > zlo + 1 || lfz < zlo) continue;
-    int lfx = lf >> 16, lfy = (lf >> 8) & 255;
+  for (int a = tid; a < ns; a += T) {
     int j = site[a];
-    const float *wj = sm + (size_t)j * order * 3;
     float q = __int_as_float(posfx[j].w);
-    int pz = zlo + iz;
-    int zi = pz - (lfz - order + 1);  // 0-based spline index along z
-    bool zin = zi >= 0 && zi < order;
-    float wz = zin ? wj[zi * 3 + 2] * q : 0.f;
-    for (int ox = 0; ox < order; ox += 4) {
-      for (int oy = 0; oy < order; oy += 4) {
-        int px = lfx - order + 1 + ox + ix, py = lfy - order + 1 + oy + iy;
-        bool in = zin && (ox + ix < order) && (oy + iy < order) && px >= 0 && px < kBrick &&
-                  py >= 0 && py < kBrick;
-        if (in) acc[(px * kBrick + py) * kBrick + pz] += wj[(ox + ix) * 3] * wj[(oy + iy) * 3 + 1] * wz;
+    const float *wj = sm + (size_t)j * order * 3;
+    for (int m = 0; m < order; m++) {
+      sw[(0 * order + m) * kSp5MaxSites + a] = wj[m * 3] * q;
+      sw[(1 * order + m) * kSp5MaxSites + a] = wj[m * 3 + 1];
+      sw[(2 * order + m) * kSp5MaxSites + a] = wj[m * 3 + 2];
+    }
+  }
+  __syncthreads();
+  const int pcol = tid >> 1, px = pcol >> 3, py = pcol & 7, pz0 = (tid & 1) * 4;
+  float acc0 = 0.f, acc1 = 0.f, acc2 = 0.f, acc3 = 0.f;
+  // only the halo columns (lx, ly) in [px, px + order) x [py, py + order) reach
+  // this thread's points; their sites are contiguous in the staging
+  for (int ox = 0; ox < order; ox++) {
+    const int dx = order - 1 - ox;  // spline index along x of column lx = px + ox
+    for (int oy = 0; oy < order; oy++) {
+      const int dy = order - 1 - oy;
+      const int c = (px + ox) * H + (py + oy);
+      for (int a = colstart[c]; a < colend[c]; a++) {
+        const float *wz = sw + (2 * order) * kSp5MaxSites + a;
+        float wxy = sw[dx * kSp5MaxSites + a] * sw[(order + dy) * kSp5MaxSites + a];
+        int dz = pz0 - (sfloor[a] - order + 1);
+        if ((unsigned)dz < (unsigned)order) acc0 = fmaf(wxy, wz[dz * kSp5MaxSites], acc0);
+        if ((unsigned)(dz + 1) < (unsigned)order) acc1 = fmaf(wxy, wz[(dz + 1) * kSp5MaxSites], acc1);
+        if ((unsigned)(dz + 2) < (unsigned)order) acc2 = fmaf(wxy, wz[(dz + 2) * kSp5MaxSites], acc2);
+        if ((unsigned)(dz + 3) < (unsigned)order) acc3 = fmaf(wxy, wz[(dz + 3) * kSp5MaxSites], acc3);
       }
     }
-    __syncwarp();  // order this site's adds before the next site's
   }
-  __syncthreads();
-  for (int i = tid; i < kBrick * kBrick * kBrick; i += blockDim.x) {
-    int pz = i & (kBrick - 1), py = (i >> 3) & (kBrick - 1), px = i >> 6;
-    int x = X0 + px, y = Y0 + py, z = Z0 + pz;
-    if (x < G.x && y < G.y && z < G.z) grid[((long)x * G.y + y) * G.z + z] = acc[i];
+  int x = X0 + px, y = Y0 + py;
+  if (x < G.x && y < G.y) {
+    float *g = grid + ((long)x * G.y + y) * G.z;
+    int z = Z0 + pz0;
+    if (z < G.z) g[z] = acc0;
+    if (z + 1 < G.z) g[z + 1] = acc1;
+    if (z + 2 < G.z) g[z + 2] = acc2;
+    if (z + 3 < G.z) g[z + 3] = acc3;
   }
 }
 
@@ -1048,6 +1078,13 @@ __global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc, int f
 // ---------------------------------------------------------------------------
 // host side
 
+static int spread_attr() {
+  // weights of up to order 8 (the largest order a box accepts): 48 KB
+  FE_CUDA(cudaFuncSetAttribute(k_mx_spread5, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)(sizeof(float) * 3 * 8 * kSp5MaxSites)));
+  return FE_OK;
+}
+
 static int up(int **dst, const std::vector<int> &v) {
   FE_CUDA(cudaMalloc(dst, sizeof(int) * (v.empty() ? 1 : v.size())));
   if (!v.empty())
@@ -1058,6 +1095,7 @@ static int up(int **dst, const std::vector<int> &v) {
 int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
+  if (int rc = spread_attr()) return rc;
   // cell grid of edge >= rlist / 2
   double half = 0.5 * (b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
   M.ncells = 1;
@@ -1402,10 +1440,11 @@ int launch_mx_spread_only(Box *b) {
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   int nbk = ((b->G[0] + kBrick - 1) / kBrick) * ((b->G[1] + kBrick - 1) / kBrick) *
             ((b->G[2] + kBrick - 1) / kBrick);
-  k_mx_spread4<<<nbk, kSp4Warps * 32, 0, b->stream>>>(b->order, G, M.posfx, M.sm, b->gcap,
-                                                     b->gbin_count, b->gbin_atoms, M.grid32,
-                                                     b->status);
-  FE_LAUNCH_CHECK("k_mx_spread4");
+  size_t swb = sizeof(float) * 3 * (size_t)b->order * kSp5MaxSites;
+  k_mx_spread5<<<nbk, kSp5Threads, swb, b->stream>>>(b->order, G, M.posfx, M.sm, b->gcap,
+                                                  b->gbin_count, b->gbin_atoms, M.grid32,
+                                                  b->status);
+  FE_LAUNCH_CHECK("k_mx_spread5");
   return FE_OK;
 }
 
