@@ -132,3 +132,58 @@ def test_autotune_keeps_results_bitwise(case):
     assert nw in (4, 8, 16) and regs in (40, 64) and blocks > 0 and us > 0
     assert np.array_equal(f1, f2)
     assert e1 == e2
+
+
+def _exact_row_counts(s, rl):
+    """Per-site count of non-excluded partners within rl, from the same
+    32-bit fractional coordinates the engine lists from (minimum image)."""
+    L = np.asarray(s.L, float)
+    u = np.rint((s.pos / L + 0.5) * 2.0 ** 32).astype(np.int64) & 0xFFFFFFFF
+    n = s.n
+    cnt = np.zeros(n, np.int64)
+    near = 0
+    for a in range(0, n, 512):
+        d = u[a:a + 512, None, :] - u[None, :, :]
+        d = ((d + 2 ** 31) & 0xFFFFFFFF) - 2 ** 31
+        r2 = ((d * (L / 2.0 ** 32)) ** 2).sum(-1)
+        inside = r2 < rl * rl
+        inside[np.arange(inside.shape[0]), np.arange(a, a + inside.shape[0])] = False
+        cnt[a:a + 512] = inside.sum(1)
+        near += int((np.abs(np.sqrt(r2) - rl) < 1e-4).sum())
+    for i, j in np.asarray(s.excl).reshape(-1, 2):
+        d = ((u[i] - u[j] + 2 ** 31) & 0xFFFFFFFF) - 2 ** 31
+        if ((d * (L / 2.0 ** 32)) ** 2).sum() < rl * rl:
+            cnt[i] -= 1
+            cnt[j] -= 1
+    return cnt, near
+
+
+@pytest.mark.parametrize("kind", ["water12000", "water900_small_box", "ortho_3000"])
+def test_mixed_list_is_complete(kind):
+    """The outer list holds exactly the non-excluded pairs within rlist
+    (both directions): total entries and the longest row against an exact
+    count, up to pairs within 1e-4 A of rlist."""
+    from thecodecombo_7_gb300 import systems
+    if kind == "water12000":
+        s = systems.water_box(4000, density=0.1, seed=11)
+    elif kind == "water900_small_box":
+        s = systems.water_box(300, density=0.1, seed=5, grid=(16, 16, 16))
+        s.rc = s.rc_ew = 8.0
+        s.rclist = s.rclist_ew = 9.0
+    else:
+        s = systems.water_box(1000, density=0.1, seed=9)
+        rng = np.random.default_rng(2)
+        s.L = np.array([30.0, 42.0, 26.0])
+        s.pos = (rng.random((s.n, 3)) - 0.5) * s.L
+        s.pos[:5, 0] = s.L[0] / 2
+        s.pos[5:10, 1] = -s.L[1] / 2
+        s.grid = (32, 40, 24)
+        s.rc = s.rc_ew = 11.0
+        s.rclist = s.rclist_ew = 12.5
+    rl = min(s.rclist, s.rclist_ew)
+    want, near = _exact_row_counts(s, rl)
+    with _mixed(s) as b:
+        b.nblist()
+        entries, max_row = b.list_stats()
+    assert abs(entries - int(want.sum())) <= 2 * near, (entries, int(want.sum()), near)
+    assert abs(max_row - int(want.max())) <= (1 if near else 0), (max_row, int(want.max()))

@@ -9,7 +9,7 @@ namespace fe {
 struct Box;
 
 struct Mixed {
-  // cell grid (edge >= rlist / 2) used to sort sites and enumerate candidates
+  // cell grid (edge >= rlist / 3) used to sort sites and enumerate candidates
   int nc[3] = {1, 1, 1};
   double h[3] = {0, 0, 0};
   int ncells = 1;
@@ -32,6 +32,7 @@ struct Mixed {
   unsigned long long *fix = nullptr;  // 3n fixed-point forces (2^32 per kJ/mol/A)
   float *lj_tab = nullptr;        // nt*nt x (eps, sig^2, shift constant)
   unsigned char *lj_on = nullptr; // nt*nt: pair type has an LJ term
+  unsigned *lj_row = nullptr;     // nt <= 32: bit t of lj_row[t'] = lj_on[t][t']
   int nexcl = 0;
   int *excl_ab = nullptr, *excl_flag = nullptr;
   float *eterm32 = nullptr, *kw32 = nullptr;

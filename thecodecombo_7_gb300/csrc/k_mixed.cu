@@ -3,8 +3,9 @@
 // order of summation), FP64 integration and energy reductions.
 //
 // Layout (rebuilt with the list, every nlist steps):
-//   * sites are sorted by a cell grid of edge h >= rlist/2; perm[s] is the
-//     original index of sorted slot s;
+//   * sites are sorted by a cell grid of edge h >= rlist/3 (cells assigned
+//     from the same 32-bit fractions as below); perm[s] is the original
+//     index of sorted slot s;
 //   * every step, posfx[s] = (x, y, z) as unsigned 32-bit fractions of the box
 //     length (x/L + 1/2 scaled by 2^32) and the charge: the difference of two
 //     coordinates taken in 32-bit integer arithmetic wraps around, which IS the
@@ -12,7 +13,9 @@
 //     of 2^-24 (~2e-7 A at 3 A) -- no image shifts, no cell-relative frames;
 //   * the OUTER list is full (both directions, no Newton-3 scatter): row s
 //     holds every non-excluded j within rlist, pairs with an LJ term at the
-//     front and the rest at the back.  Optionally (use_inner) it is pruned
+//     front and the rest at the back.  It is built per unit of 8 sorted
+//     sites: the candidates near the unit's bounding box are loaded once and
+//     tested against all 8 sites.  Optionally (use_inner) it is pruned
 //     every few steps into an INNER list (rc + skin) for the pair kernel; on
 //     this hardware the prune pass costs about what it saves, because both
 //     are bound by the same j-position gathers, so it is off by default;
@@ -32,7 +35,6 @@ namespace fe {
 
 constexpr double kFixScale = 4294967296.0;  // 2^32
 constexpr float kFixScaleF = 4294967296.0f;
-constexpr float kInvTwo32 = 2.3283064365386963e-10f;  // 2^-32
 constexpr int kMxWarps = 8;                 // warps per block (list, prune, pair)
 constexpr int kMxMaxCellAtoms = 2048;       // sites per cell a sort block handles
 constexpr int kBrick = 8;                   // spreading brick edge (grid points)
@@ -55,17 +57,21 @@ __device__ __forceinline__ float fx_delta(unsigned a, unsigned b, float scale) {
 // ---------------------------------------------------------------------------
 // sorting by cells
 
-__global__ void k_mx_cell(int n, const double4 *__restrict__ pos, double3 L, double3 h, int3 nc,
+// x / L + 1/2 as an unsigned 32-bit fraction (wraps: -L/2 and +L/2 coincide)
+__device__ __forceinline__ unsigned frac32(double x, double invL) {
+  return (unsigned)(unsigned long long)llrint((x * invL + 0.5) * kFixScale);
+}
+
+// cell of each site from the same 32-bit fractions the kernels see, so that
+// cell membership and fixed-point coordinates always agree
+__global__ void k_mx_cell(int n, const double4 *__restrict__ pos, double3 invL, int3 nc,
                           int *__restrict__ cell_of, int *__restrict__ count) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double4 p = pos[i];
-  int cx = (int)floor((p.x + 0.5 * L.x) / h.x);
-  int cy = (int)floor((p.y + 0.5 * L.y) / h.y);
-  int cz = (int)floor((p.z + 0.5 * L.z) / h.z);
-  cx = min(max(cx, 0), nc.x - 1);
-  cy = min(max(cy, 0), nc.y - 1);
-  cz = min(max(cz, 0), nc.z - 1);
+  int cx = (int)(((unsigned long long)frac32(p.x, invL.x) * (unsigned)nc.x) >> 32);
+  int cy = (int)(((unsigned long long)frac32(p.y, invL.y) * (unsigned)nc.y) >> 32);
+  int cz = (int)(((unsigned long long)frac32(p.z, invL.z) * (unsigned)nc.z) >> 32);
   int c = (cx * nc.y + cy) * nc.z + cz;
   cell_of[i] = c;
   atomicAdd(&count[c], 1);
@@ -130,10 +136,8 @@ __global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   double4 p = pos[perm[s]];
-  unsigned ux = (unsigned)(unsigned long long)llrint((p.x * invL.x + 0.5) * kFixScale);
-  unsigned uy = (unsigned)(unsigned long long)llrint((p.y * invL.y + 0.5) * kFixScale);
-  unsigned uz = (unsigned)(unsigned long long)llrint((p.z * invL.z + 0.5) * kFixScale);
-  posfx[s] = make_int4((int)ux, (int)uy, (int)uz, __float_as_int((float)p.w));
+  posfx[s] = make_int4((int)frac32(p.x, invL.x), (int)frac32(p.y, invL.y), (int)frac32(p.z, invL.z),
+                       __float_as_int((float)p.w));
 }
 
 __device__ __forceinline__ int mx_is_excluded(const int *__restrict__ xs, const int *__restrict__ xp,
@@ -185,146 +189,274 @@ __device__ __forceinline__ void row_close(const RowCursor &rc, int cap, int s, i
   }
 }
 
-constexpr int kListExcl = 4;  // excluded partners per site compared in registers
+constexpr int kListUnit = 8;  // consecutive sorted sites one warp lists together
+// cells per rlist along each axis: finer cells trim the candidates of a unit
+// (rlist/2: ~3000 per unit of 8 water sites, rlist/3: ~2250), coarser ones
+// make fewer, longer contiguous ranges; 3 measured fastest of 2, 3, 4
+constexpr double kListCellsPerReach = 3.0;
+constexpr int kListExcl = 4;  // excluded partners per site handled by lane masks
+constexpr int kListBlocksPerSM = 2;  // register budget of the list build (no spills)
+static_assert(kListUnit * kListExcl == 32, "one lane per (site, excluded partner)");
 
-// The excluded partners of a site as sorted slots (up to kListExcl; -1
-// pads); *many is set when the site has more (then the lists are searched).
-__device__ __forceinline__ void site_exclusions(int oi, const int *__restrict__ xs,
-                                                const int *__restrict__ xp,
-                                                const int *__restrict__ iperm,
-                                                int (&ex)[kListExcl], bool *many) {
-  int a = xs[oi], nx = xs[oi + 1] - a;
+__device__ __forceinline__ float warp_fmin(float v) {
 #pragma unroll
-  for (int q = 0; q < kListExcl; q++) ex[q] = q < nx ? iperm[xp[a + q]] : -1;
-  *many = nx > kListExcl;
+  for (int o = 16; o; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_fmax(float v) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ int wrap_mod(int v, int g) {
+  v %= g;
+  return v < 0 ? v + g : v;
 }
 
-// one candidate j of row s: fixed-point distance, exclusion, LJ class
-__device__ __forceinline__ void list_test(int j, int4 pi, int oi, int ti,
-                                          const int4 *__restrict__ posfx,
-                                          const int *__restrict__ perm,
-                                          const int *__restrict__ type_s, float3 sc, float rl2,
-                                          int nt, const unsigned char *__restrict__ lj_on,
-                                          const int *__restrict__ xs, const int *__restrict__ xp,
-                                          const int (&ex)[kListExcl], bool many, bool &ok,
-                                          bool &lj) {
-  int4 pj = posfx[j];
-  float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, sc.x);
-  float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, sc.y);
-  float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, sc.z);
-  float r2 = dx * dx + dy * dy + dz * dz;
-  if (r2 < rl2) {
-    bool excl = false;
+// gap between the interval [lo, hi] and cell c of edge h along one axis
+__device__ __forceinline__ float cell_gap(int c, float h, float lo, float hi) {
+  return fmaxf(fmaxf(c * h - hi, lo - (c + 1) * h), 0.f);
+}
+
+// Appends one chunk's passing candidates to a row without divergent branches.
+__device__ __forceinline__ void row_push_bf(bool ok, bool lj, int entry, unsigned lt, int cap,
+                                            int *__restrict__ row, RowCursor &rc) {
+  unsigned mlj = __ballot_sync(0xffffffffu, ok && lj);
+  unsigned mnl = __ballot_sync(0xffffffffu, ok && !lj);
+  int p = lj ? rc.nlj + __popc(mlj & lt) : rc.nnl + __popc(mnl & lt);
+  int other = lj ? rc.nnl : rc.nlj;
+  int idx = lj ? p : cap - 1 - p;
+  if (ok && p + other < cap) row[idx] = entry;
+  rc.nlj += __popc(mlj);
+  rc.nnl += __popc(mnl);
+}
+
+// One chunk of candidates (one per lane) against every site of the unit.
+// FAST: the FP32 frame of the unit's first site covers every pair, the
+// sites have at most kListExcl excluded partners and nt <= 32; otherwise
+// the exact fixed-point differences, the exclusion lists and the type table
+// are used.  Sites past the end of the unit carry NaN offsets: no pair passes.
+template <bool FAST>
+__device__ __forceinline__ void list_chunk(
+    int j, int js, int4 pj, float fjx, float fjy, float fjz, int tj, unsigned mj, unsigned ebit,
+    unsigned lanebit, unsigned lt, const float4 (&site)[kListUnit], const int4 (&spk)[kListUnit],
+    float3 sc, float rl2, int nt, const unsigned char *__restrict__ lj_on,
+    const int *__restrict__ xs, const int *__restrict__ xp, int ok_orig, int oj, int cap,
+    int *__restrict__ row0, RowCursor (&rc)[kListUnit]) {
 #pragma unroll
-    for (int q = 0; q < kListExcl; q++) excl |= (ex[q] == j);
-    if (many && !excl) excl = mx_is_excluded(xs, xp, oi, perm[j]);
-    if (!excl) {
-      ok = true;
-      lj = lj_on[ti * nt + type_s[j]] != 0;
+  for (int k = 0; k < kListUnit; k++) {
+    unsigned exm = __shfl_sync(0xffffffffu, ebit, 4 * k);
+    float4 si = site[k];
+    int tik = __float_as_int(si.w);
+    float dx, dy, dz;
+    if (FAST) {
+      dx = fjx - si.x;
+      dy = fjy - si.y;
+      dz = fjz - si.z;
+    } else {
+      int4 pik = spk[k];
+      dx = fx_delta((unsigned)pj.x, (unsigned)pik.x, sc.x);
+      dy = fx_delta((unsigned)pj.y, (unsigned)pik.y, sc.y);
+      dz = fx_delta((unsigned)pj.z, (unsigned)pik.z, sc.z);
+      if (si.x != si.x) dx = si.x;  // padding site
     }
+    float r2 = dx * dx + dy * dy + dz * dz;
+    bool ok = r2 < rl2 && js != k && (exm & lanebit) == 0u;
+    bool lj;
+    if (FAST) {
+      lj = ((mj >> tik) & 1u) != 0u;
+    } else {
+      int oi = __shfl_sync(0xffffffffu, ok_orig, k);
+      if (ok) ok = !mx_is_excluded(xs, xp, oi, oj);
+      lj = lj_on[tik * nt + tj] != 0;
+    }
+    row_push_bf(ok, lj, j, lt, cap, row0 + (size_t)k * cap, rc[k]);
   }
 }
 
-// gap along one axis between a site at fraction u and cell c (of nc), in A
-__device__ __forceinline__ float cell_gap(int c, int nc, float u, float L) {
-  float lo = (float)c / nc - u;
-  float g = fmaxf(fmaxf(lo, -(lo + 1.0f / nc)), 0.f) * L - 1e-3f;
-  return fmaxf(g, 0.f);
-}
-
-// Outer list: one warp per sorted site, every non-excluded j != i within
-// rlist.  With at least 5 cells per axis the 5x5x5 neighbourhood is walked as
-// (x, y) columns whose z cells within rlist of the site (box distance) form
-// one or two contiguous sorted ranges; smaller grids visit every cell.  Rows
-// come out in a fixed (column, slot) order: deterministic.
-__global__ void __launch_bounds__(kMxWarps * 32)
+// Outer list: one warp per UNIT of kListUnit consecutive sorted sites (mostly
+// one or two neighbouring cells).  The warp takes the bounding box of the
+// unit's sites (minimum-image offsets from its first site, in A), walks the
+// cell columns within reach of it -- 32 columns at a time, one per lane, each
+// with the z cells within rlist of the box as one or two contiguous sorted
+// ranges -- and packs those ranges into full 32-lane chunks of candidates.
+// Every candidate is loaded once and tested against all sites of the unit.
+// Excluded partners are turned into per-chunk lane masks (lane 4k+q owns the
+// q-th partner of site k and locates it among the candidates once per column
+// batch), so the per-pair test is a distance, a mask bit and a ballot.
+// Rows come out in a fixed (column, slot) order: deterministic.
+__global__ void __launch_bounds__(kMxWarps * 32, kListBlocksPerSM)
 k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
           const int *__restrict__ iperm, const int *__restrict__ cell_s,
-          const int *__restrict__ type_s,
-          const int *__restrict__ cstart, int3 nc, float3 sc, float3 Lf, float rlist2, int nt,
+          const int *__restrict__ type_s, const int *__restrict__ cstart, int3 nc, float3 sc,
+          float3 Lf, float rlist, int nt, const unsigned *__restrict__ lj_row,
           const unsigned char *__restrict__ lj_on, const int *__restrict__ xs,
           const int *__restrict__ xp, int cap, int *__restrict__ cnt_lj,
           int *__restrict__ cnt_nl, int *__restrict__ ent, int *__restrict__ status) {
-  int lane = threadIdx.x & 31;
-  bool fast = nc.x >= 5 && nc.y >= 5 && nc.z >= 5;
-  for (int s = blockIdx.x * kMxWarps + (threadIdx.x >> 5); s < n; s += gridDim.x * kMxWarps) {
-    int4 pi = posfx[s];
-    int c = cell_s[s];
-    int cz = c % nc.z, cy = (c / nc.z) % nc.y, cx = c / (nc.z * nc.y);
-    int oi = perm[s];
-    int ti = type_s[s];
-    int ex[kListExcl];
-    bool many;
-    site_exclusions(oi, xs, xp, iperm, ex, &many);
-    RowCursor rc = {0, 0};
-    int *row = ent + (size_t)s * cap;
-    if (fast) {
-      float ux = (float)(unsigned)pi.x * kInvTwo32, uy = (float)(unsigned)pi.y * kInvTwo32,
-            uz = (float)(unsigned)pi.z * kInvTwo32;
-      for (int dcx = -2; dcx <= 2; dcx++) {
-        float gx = cell_gap(cx + dcx, nc.x, ux, Lf.x);
-        if (gx * gx >= rlist2) continue;
-        int x = wrap1(cx + dcx, nc.x);
-        for (int dcy = -2; dcy <= 2; dcy++) {
-          float gy = cell_gap(cy + dcy, nc.y, uy, Lf.y);
-          float gxy = gx * gx + gy * gy;
-          if (gxy >= rlist2) continue;
-          int y = wrap1(cy + dcy, nc.y);
-          int zlo = 3, zhi = -3;
-          for (int dcz = -2; dcz <= 2; dcz++) {
-            float gz = cell_gap(cz + dcz, nc.z, uz, Lf.z);
-            if (gxy + gz * gz < rlist2) {
-              zlo = min(zlo, dcz);
-              zhi = max(zhi, dcz);
-            }
-          }
-          if (zhi < zlo) continue;
-          int colbase = (x * nc.y + y) * nc.z;
-          int zs = cz + zlo, ze = cz + zhi;  // inclusive, may leave [0, nc.z)
-          for (int part = 0; part < 2; part++) {
-            int za, zb;
-            if (part == 0) {
-              za = max(zs, 0);
-              zb = min(ze, nc.z - 1);
+  const unsigned full = 0xffffffffu;
+  __shared__ float4 s_site[kMxWarps][kListUnit];
+  __shared__ int4 s_pk[kMxWarps][kListUnit];
+  int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  unsigned lanebit = 1u << lane, lt = lanebit - 1u;
+  float rl2 = rlist * rlist;
+  // reach of the cell walk: rlist plus a margin for the FP32 frame's rounding
+  float ra = rlist + 1e-3f + 4e-6f * fmaxf(Lf.x, fmaxf(Lf.y, Lf.z));
+  float ra2 = ra * ra;
+  float3 hc = make_float3(Lf.x / nc.x, Lf.y / nc.y, Lf.z / nc.z);
+  float3 ihc = make_float3(nc.x / Lf.x, nc.y / Lf.y, nc.z / Lf.z);
+  int nunits = (n + kListUnit - 1) / kListUnit;
+  for (int u = blockIdx.x * kMxWarps + wib; u < nunits; u += gridDim.x * kMxWarps) {
+    int s0 = u * kListUnit, nk = min(kListUnit, n - s0);
+    int sl = s0 + min(lane, nk - 1);  // lanes past the unit repeat its last site
+    int4 pk = posfx[sl];
+    int tk = type_s[sl];
+    int ok_orig = perm[sl];
+    unsigned r0x = __shfl_sync(full, (unsigned)pk.x, 0), r0y = __shfl_sync(full, (unsigned)pk.y, 0),
+             r0z = __shfl_sync(full, (unsigned)pk.z, 0);
+    float ox = fx_delta((unsigned)pk.x, r0x, sc.x), oy = fx_delta((unsigned)pk.y, r0y, sc.y),
+          oz = fx_delta((unsigned)pk.z, r0z, sc.z);
+    float lox = warp_fmin(ox), hix = warp_fmax(ox), loy = warp_fmin(oy), hiy = warp_fmax(oy),
+          loz = warp_fmin(oz), hiz = warp_fmax(oz);
+    // the FP32 frame of the first site gives the minimum image of every pair
+    // within reach when offsets + reach stay under half the box
+    bool frame = fmaxf(-lox, hix) + ra < 0.5f * Lf.x && fmaxf(-loy, hiy) + ra < 0.5f * Lf.y &&
+                 fmaxf(-loz, hiz) + ra < 0.5f * Lf.z;
+    // the unit's sites for the per-pair tests: offsets and type, and the
+    // fixed-point coordinates for units the FP32 frame does not cover
+    __syncwarp();
+    if (lane < kListUnit) {
+      float pad = lane < nk ? 0.f : __int_as_float(0x7fc00000);  // NaN: no pair passes
+      s_site[wib][lane] = make_float4(ox + pad, oy + pad, oz + pad, __int_as_float(tk));
+      s_pk[wib][lane] = pk;
+    }
+    __syncwarp();
+    // lane 4k+q: q-th excluded partner of site k (sorted slot, -1 if none)
+    int ek = lane >> 2, eq = lane & 3, exs = -1;
+    bool many_l = false;
+    if (ek < nk) {
+      int o = perm[s0 + ek];
+      int a = xs[o], m = xs[o + 1] - a;
+      if (eq < m) exs = iperm[xp[a + eq]];
+      many_l = eq == 0 && m > kListExcl;
+    }
+    bool fast = frame && lj_row != nullptr && !__any_sync(full, many_l);
+    int *row0 = ent + (size_t)s0 * cap;
+    int ecx = 0, ecy = 0;
+    if (exs >= 0) {
+      int c = cell_s[exs];
+      ecy = (c / nc.z) % nc.y;
+      ecx = c / (nc.z * nc.y);
+    }
+    // cell window of the unit, unwrapped (the whole axis when it wraps onto itself)
+    float X0 = __uint2float_rn(r0x) * sc.x, Y0 = __uint2float_rn(r0y) * sc.y,
+          Z0 = __uint2float_rn(r0z) * sc.z;
+    float Xlo = X0 + lox, Xhi = X0 + hix, Ylo = Y0 + loy, Yhi = Y0 + hiy, Zlo = Z0 + loz,
+          Zhi = Z0 + hiz;
+    int xa = __float2int_rd((Xlo - ra) * ihc.x), xb = __float2int_rd((Xhi + ra) * ihc.x);
+    int ya = __float2int_rd((Ylo - ra) * ihc.y), yb = __float2int_rd((Yhi + ra) * ihc.y);
+    bool allx = xb - xa + 1 >= nc.x, ally = yb - ya + 1 >= nc.y;
+    if (allx) {
+      xa = 0;
+      xb = nc.x - 1;
+    }
+    if (ally) {
+      ya = 0;
+      yb = nc.y - 1;
+    }
+    int nx = xb - xa + 1, ny = yb - ya + 1, ncol = nx * ny;
+    // column of the excluded partner within the window (-1: outside)
+    int eqcol = -1;
+    if (exs >= 0) {
+      int dx = wrap_mod(ecx - xa, nc.x), dy = wrap_mod(ecy - ya, nc.y);
+      if (dx < nx && dy < ny) eqcol = dx * ny + dy;
+    }
+    RowCursor rc[kListUnit];
+#pragma unroll
+    for (int k = 0; k < kListUnit; k++) rc[k] = {0, 0};
+    for (int q0 = 0; q0 < ncol; q0 += 32) {
+      int q = q0 + lane;
+      int a0 = 0, la = 0, b0 = 0, lb = 0;
+      if (q < ncol) {
+        int x = xa + q / ny, y = ya + q % ny;
+        float gx = allx ? 0.f : cell_gap(x, hc.x, Xlo, Xhi);
+        float gy = ally ? 0.f : cell_gap(y, hc.y, Ylo, Yhi);
+        float g2 = gx * gx + gy * gy;
+        if (g2 < ra2) {
+          float rho = sqrtf(ra2 - g2);
+          int za = __float2int_rd((Zlo - rho) * ihc.z), zb = __float2int_rd((Zhi + rho) * ihc.z);
+          const int *cs = cstart + (wrap_mod(x, nc.x) * nc.y + wrap_mod(y, nc.y)) * nc.z;
+          if (zb - za + 1 >= nc.z) {
+            a0 = cs[0];
+            la = cs[nc.z] - a0;
+          } else {
+            int zaw = wrap_mod(za, nc.z), zbw = wrap_mod(zb, nc.z);
+            a0 = cs[zaw];
+            if (zaw <= zbw) {
+              la = cs[zbw + 1] - a0;
             } else {
-              if (zs >= 0 && ze < nc.z) break;
-              if (zs < 0) {
-                za = zs + nc.z;
-                zb = nc.z - 1;
-              } else {
-                za = 0;
-                zb = ze - nc.z;
-              }
-            }
-            if (za > zb) continue;
-            int j0 = cstart[colbase + za], j1 = cstart[colbase + zb + 1];
-            for (int base = j0; base < j1; base += 32) {
-              int j = base + lane;
-              bool ok = false, lj = false;
-              if (j < j1 && j != s)
-                list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ex,
-                          many, ok, lj);
-              row_push(ok, lj, j, lane, cap, row, rc);
+              la = cs[nc.z] - a0;
+              b0 = cs[0];
+              lb = cs[zbw + 1] - b0;
             }
           }
         }
       }
-    } else {
-      for (int x = 0; x < nc.x; x++)
-        for (int y = 0; y < nc.y; y++) {
-          int colbase = (x * nc.y + y) * nc.z;
-          int j0 = cstart[colbase], j1 = cstart[colbase + nc.z];
-          for (int base = j0; base < j1; base += 32) {
-            int j = base + lane;
-            bool ok = false, lj = false;
-            if (j < j1 && j != s)
-              list_test(j, pi, oi, ti, posfx, perm, type_s, sc, rlist2, nt, lj_on, xs, xp, ex, many,
-                        ok, lj);
-            row_push(ok, lj, j, lane, cap, row, rc);
-          }
+      // exclusive prefix of the columns' candidate counts
+      int len = la + lb, incl = len;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        int t = __shfl_up_sync(full, incl, o);
+        if (lane >= o) incl += t;
+      }
+      int P = incl - len, T = __shfl_sync(full, incl, 31);
+      // virtual index of this lane's excluded partner among the batch's candidates
+      bool here = eqcol >= q0 && eqcol < q0 + 32;
+      int src = here ? eqcol - q0 : 0;
+      int eP = __shfl_sync(full, P, src), ea0 = __shfl_sync(full, a0, src),
+          ela = __shfl_sync(full, la, src), eb0 = __shfl_sync(full, b0, src),
+          elb = __shfl_sync(full, lb, src);
+      int ve = -1;
+      if (here) {
+        if (exs >= ea0 && exs < ea0 + ela) ve = eP + exs - ea0;
+        else if (exs >= eb0 && exs < eb0 + elb) ve = eP + ela + exs - eb0;
+      }
+      for (int vb = 0; vb < T; vb += 32) {
+        int v = vb + lane;
+        bool valid = v < T;
+        int c = 0;
+#pragma unroll
+        for (int st = 16; st; st >>= 1) {
+          int Pt = __shfl_sync(full, P, c + st);
+          if (Pt <= v) c += st;
         }
+        int Pc = __shfl_sync(full, P, c), a0c = __shfl_sync(full, a0, c),
+            lac = __shfl_sync(full, la, c), b0c = __shfl_sync(full, b0, c);
+        int off = v - Pc;
+        int j = off < lac ? a0c + off : b0c + (off - lac);
+        if (!valid) j = s0;
+        int4 pj = posfx[j];
+        int tj = type_s[j];
+        float fjx = fx_delta((unsigned)pj.x, r0x, sc.x), fjy = fx_delta((unsigned)pj.y, r0y, sc.y),
+              fjz = fx_delta((unsigned)pj.z, r0z, sc.z);
+        unsigned te = (unsigned)(ve - vb);
+        unsigned ebit = (ve >= 0 && te < 32u) ? 1u << te : 0u;
+        ebit |= __shfl_xor_sync(full, ebit, 1);
+        ebit |= __shfl_xor_sync(full, ebit, 2);
+        int js = valid ? j - s0 : -1;  // this lane's candidate is site js of the unit
+        if (fast) {
+          list_chunk<true>(j, js, pj, fjx, fjy, fjz, tj, lj_row[tj], ebit, lanebit, lt,
+                           s_site[wib], s_pk[wib], sc, valid ? rl2 : -1.f, nt, lj_on, xs, xp,
+                           ok_orig, 0, cap, row0, rc);
+        } else {
+          list_chunk<false>(j, js, pj, fjx, fjy, fjz, tj, 0u, ebit, lanebit, lt, s_site[wib],
+                            s_pk[wib], sc, valid ? rl2 : -1.f, nt, lj_on, xs, xp, ok_orig,
+                            perm[j], cap, row0, rc);
+        }
+      }
     }
-    row_close(rc, cap, s, lane, cnt_lj, cnt_nl, status);
+#pragma unroll
+    for (int k = 0; k < kListUnit; k++)
+      if (k < nk) row_close(rc[k], cap, s0 + k, lane - k, cnt_lj, cnt_nl, status);
   }
 }
 
@@ -1096,11 +1228,11 @@ int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
   if (int rc = spread_attr()) return rc;
-  // cell grid of edge >= rlist / 2
-  double half = 0.5 * (b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
+  // cell grid of edge >= rlist / kListCellsPerReach
+  double edge = (b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew) / kListCellsPerReach;
   M.ncells = 1;
   for (int d = 0; d < 3; d++) {
-    int m = (int)(b->p.L[d] / half);
+    int m = (int)(b->p.L[d] / edge);
     M.nc[d] = m < 1 ? 1 : m;
     M.h[d] = b->p.L[d] / M.nc[d];
     M.ncells *= M.nc[d];
@@ -1162,6 +1294,14 @@ int mixed_setup(Box *b) {
   for (int k = 0; k < nt * nt; k++) on[k] = lj[3 * k] != 0.f ? 1 : 0;
   FE_CUDA(cudaMalloc(&M.lj_on, on.size()));
   FE_CUDA(cudaMemcpy(M.lj_on, on.data(), on.size(), cudaMemcpyHostToDevice));
+  if (nt <= 32) {  // lj_row[t'] bit t: pair (t, t') has an LJ term
+    std::vector<unsigned> row(nt, 0u);
+    for (int t = 0; t < nt; t++)
+      for (int t2 = 0; t2 < nt; t2++)
+        if (on[t * nt + t2]) row[t2] |= 1u << t;
+    FE_CUDA(cudaMalloc(&M.lj_row, sizeof(unsigned) * nt));
+    FE_CUDA(cudaMemcpy(M.lj_row, row.data(), sizeof(unsigned) * nt, cudaMemcpyHostToDevice));
+  }
   // exclusion pair list (xint), for the correction kernel
   M.nexcl = b->p.nexcl;
   FE_CUDA(cudaMalloc(&M.excl_ab, sizeof(int) * 2 * (M.nexcl ? M.nexcl : 1)));
@@ -1259,7 +1399,7 @@ void mixed_free(Box *b) {
   Mixed &M = *b->mx;
   void *ptrs[] = {M.cell_count, M.cell_start, M.cell_fill, M.cell_of, M.perm, M.iperm, M.cell_s,
                   M.cz_s, M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
-                  M.ient, M.fix, M.lj_tab, M.lj_on, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
+                  M.ient, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
                   M.grid32, M.grid32k, M.floor3, M.sm, M.sd, M.mol_first, M.mol_x,
                   M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai};
   for (void *p : ptrs)
@@ -1309,10 +1449,11 @@ int launch_mixed_list(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
-  double3 h = make_double3(M.h[0], M.h[1], M.h[2]);
+  double3 invL = make_double3(1.0 / b->p.L[0], 1.0 / b->p.L[1], 1.0 / b->p.L[2]);
   int3 nc = make_int3(M.nc[0], M.nc[1], M.nc[2]);
   FE_CUDA(cudaMemsetAsync(M.cell_count, 0, sizeof(int) * M.ncells, b->stream));
-  k_mx_cell<<<(n + 255) / 256, 256, 0, b->stream>>>(n, b->pos_q, L, h, nc, M.cell_of, M.cell_count);
+  k_mx_cell<<<(n + 255) / 256, 256, 0, b->stream>>>(n, b->pos_q, invL, nc, M.cell_of,
+                                                    M.cell_count);
   FE_LAUNCH_CHECK("k_mx_cell");
   k_cell_scan_ext(M.cell_count, M.ncells, M.cell_start, M.cell_fill, b->stream);
   k_mx_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.cell_of, M.cell_start, M.cell_fill, M.perm);
@@ -1324,10 +1465,12 @@ int launch_mixed_list(Box *b) {
   if (rc) return rc;
   float3 Lf = make_float3((float)b->p.L[0], (float)b->p.L[1], (float)b->p.L[2]);
   float rl = (float)(b->p.rclist < b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
-  k_mx_list<<<list_blocks(b), kMxWarps * 32, 0, b->stream>>>(
-      n, M.posfx, M.perm, M.iperm, M.cell_s, M.type_s, M.cell_start, nc, fix_scale(b), Lf, rl * rl,
-      b->nt,
-      M.lj_on, b->x_start, b->x_partner, M.cap, M.cnt_lj, M.cnt_nl, M.ent, b->status);
+  int units = (n + kListUnit - 1) / kListUnit;
+  int blocks = (units + kMxWarps - 1) / kMxWarps;
+  k_mx_list<<<blocks < 152 * 8 ? blocks : 152 * 8, kMxWarps * 32, 0, b->stream>>>(
+      n, M.posfx, M.perm, M.iperm, M.cell_s, M.type_s, M.cell_start, nc, fix_scale(b), Lf, rl,
+      b->nt, M.lj_row, M.lj_on, b->x_start, b->x_partner, M.cap, M.cnt_lj, M.cnt_nl, M.ent,
+      b->status);
   FE_LAUNCH_CHECK("k_mx_list");
   b->have_list = true;
   M.do_prune = true;
