@@ -393,6 +393,7 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
+    _, _, prunes0 = box.inner_list_stats()
     ev0.record(stream)
     box.run_md(K, nlist_freq=nl, first_step=first, record=False)
     ev1.record(stream)
@@ -405,9 +406,12 @@ def run_ours(args, world, rank, local):
     n_list_steps = sum(1 for i in range(first, first + K) if i % nl == 0)
     lp, ll = box.step_launches(False)
     launches = lp * (K - n_list_steps) + ll * n_list_steps
-    # dominant kernel: the pair loop, timed live on the same stream
+    # dominant kernel: the pair loop over the inner list (its steady state
+    # between prunes), timed live on the same stream
+    _, _, prunes1 = box.inner_list_stats()
     pair_us = box.time_kernel(engine.FE_KERNEL_PAIR, reps=20)
-    entries, max_row = box.list_stats()
+    outer_entries, _ = box.list_stats()
+    entries, max_row, _ = box.inner_list_stats()
     alg_bytes = 4.0 * entries + n * (16.0 + 4.0 + 4.0 + 24.0)
     peaks, peak_kind = load_peaks()
     achieved = alg_bytes / (pair_us * 1e-6) / 1e9
@@ -533,12 +537,16 @@ def run_ours(args, world, rank, local):
         "config": {"workload": WORKLOAD, "precision": "mixed (FP32 pair/PME math, int64 "
                    "fixed-point force sums, FP64 integration and energy sums)",
                    "parallelism": f"replicas x{world}",
-                   "cache": "inputs larger than L2 (pair list ~280 MB read per step)",
+                   "cache": f"inputs larger than L2 (pair list ~{4e-6 * entries:.0f} MB read "
+                            "per step)",
                    "ns_per_day": steps_per_s * 0.0005e-3 * 86400.0},
         "roofline": {"kernel": "k_mx_pair", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
                      "us_per_launch": pair_us, "list_entries": entries, "max_row": max_row,
+                     "list": f"inner list (rc + 0.8 A, {entries} entries) between prunes; "
+                             f"outer list (rlist, {outer_entries} entries) read by the "
+                             f"{prunes1 - prunes0} pruning launches of the {K} timed steps",
                      "launch_shape": {"warps_per_block": tune[0], "registers": tune[1],
                                       "blocks": tune[2],
                                       "chosen_by": "autotune (events, this box)"}},

@@ -410,6 +410,12 @@ int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list);
 /* Entries of the current pair list (half list in FP64 mode, full list in
  * mixed mode) and the longest row. */
 int fe_list_stats(fe_box *box, int64_t *entries, int *max_row);
+/* Mixed mode: entries and longest row of the inner list (rc + 0.8 A) the
+ * pair kernel walks between prunes, and how many pair-kernel launches have
+ * pruned it from the outer list so far (after every list rebuild, and when a
+ * site has moved 0.4 A since the last prune).  FE_ERR_STATE in FP64 mode or
+ * when the inner list is off (rc + 0.8 A >= rclist). */
+int fe_inner_list_stats(fe_box *box, int64_t *entries, int *max_row, int64_t *prunes);
 
 #ifdef __cplusplus
 }

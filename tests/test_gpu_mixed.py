@@ -124,6 +124,7 @@ def test_autotune_keeps_results_bitwise(case):
     s, _, _ = case
     with _mixed(s) as b:
         b.nblist()
+        b.forces()  # prunes the inner list: the calls below walk it
         e1 = b.forces()
         f1 = b.get_forces()
         nw, regs, blocks, us = b.autotune()
@@ -187,3 +188,37 @@ def test_mixed_list_is_complete(kind):
         entries, max_row = b.list_stats()
     assert abs(entries - int(want.sum())) <= 2 * near, (entries, int(want.sum()), near)
     assert abs(max_row - int(want.max())) <= (1 if near else 0), (max_row, int(want.max()))
+
+
+def test_inner_list_pruning():
+    """The pair kernel walks an inner list (rc + 0.8 A) between prunes: it is
+    pruned after a list rebuild, kept while displacements stay under 0.4 A,
+    re-pruned on the device when a site moves further, and forces from the
+    inner list agree with a walk of the outer list at the same positions to
+    FP32 summation order."""
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(4000, density=0.1, seed=21)
+    with _mixed(s) as b:
+        b.nblist()
+        b.forces()
+        e0, m0, p0 = b.inner_list_stats()
+        want, near = _exact_row_counts(s, s.rc + 0.8)
+        assert abs(e0 - int(want.sum())) <= 2 * near, (e0, int(want.sum()))
+        assert abs(m0 - int(want.max())) <= (1 if near else 0)
+        b.run_md(5, nlist_freq=1000, first_step=1, record=False)
+        _, _, p1 = b.inner_list_stats()
+        assert p1 == p0, "no prune expected for small displacements"
+        f_step = b.get_forces()
+        b.forces()
+        assert np.array_equal(b.get_forces(), f_step)
+        b.nblist()
+        b.forces()  # after a rebuild: walks the outer list
+        _, _, p2 = b.inner_list_stats()
+        assert p2 == p1 + 1
+        assert _rms_rel(f_step, b.get_forces()) < 1e-6
+        pos = b.get_positions()
+        pos[0, 0] += 0.45
+        b.set_positions(pos)
+        b.run_md(1, nlist_freq=1000, first_step=100, record=False)
+        _, _, p3 = b.inner_list_stats()
+        assert p3 == p2 + 1, "a 0.45 A displacement must trigger a prune"

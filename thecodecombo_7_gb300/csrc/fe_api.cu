@@ -101,7 +101,6 @@ static void free_box(Box *b) {
   }
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-  if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
 }
 
@@ -324,12 +323,10 @@ static int xyz_to_host(Box *b, const double *src, void *atoms, size_t stride, si
   return FE_OK;
 }
 
-// one step of the production loop (graph body); `prune` refreshes the mixed
-// path's inner list inside the force evaluation
-int step_body(Box *b, bool with_list, bool use_nhc, bool prune) {
+// one step of the production loop (graph body)
+int step_body(Box *b, bool with_list, bool use_nhc) {
   int rc;
   if (with_list && (rc = launch_list(b))) return rc;
-  if (b->mx) b->mx->do_prune = with_list || prune;
   if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
   if ((rc = launch_vv1(b, 1.0))) return rc;
   if ((rc = forces_device(b))) return rc;
@@ -341,7 +338,6 @@ int step_body(Box *b, bool with_list, bool use_nhc, bool prune) {
     // kinet of the fresh velocities folded into the second half kick
     if ((rc = launch_vv2_kinet(b, 1.0))) return rc;
   }
-  if (b->mx) b->mx->do_prune = true;  // direct API calls always prune
   return launch_record(b);
 }
 
@@ -359,14 +355,13 @@ int relaunch_kernel(Box *b, int which) {
   return FE_ERR_ARG;
 }
 
-static int capture(Box *b, bool with_list, bool use_nhc, bool prune, cudaGraphExec_t *out) {
+static int capture(Box *b, bool with_list, bool use_nhc, cudaGraphExec_t *out) {
   cudaGraph_t g;
   FE_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
   long l0 = g_launches;
-  int rc = step_body(b, with_list, use_nhc, prune);
+  int rc = step_body(b, with_list, use_nhc);
   int nl = (int)(g_launches - l0);
   if (with_list) b->launches_list = nl;
-  else if (prune) b->launches_prune = nl;
   else b->launches_plain = nl;
   cudaError_t e = cudaStreamEndCapture(b->stream, &g);
   if (rc) return rc;
@@ -426,8 +421,7 @@ int fe_box_set_stream(fe_box *box, void *stream) {
   }
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-  if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
-  b->g_step = b->g_step_list = b->g_step_prune = nullptr;
+  b->g_step = b->g_step_list = nullptr;
   b->g_key = -1;
   return FE_OK;
 }
@@ -700,8 +694,7 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
     // the record kernel's capacity is baked into the graphs: recapture
     if (b->g_step) cudaGraphExecDestroy(b->g_step);
     if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-    if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
-    b->g_step = b->g_step_list = b->g_step_prune = nullptr;
+    b->g_step = b->g_step_list = nullptr;
     b->g_key = -1;
   }
   FE_CUDA(cudaMemsetAsync(b->rec_counter, 0, sizeof(int), b->stream));
@@ -710,19 +703,14 @@ int fe_run_md(fe_box *box, int nsteps, int nlist_freq, int use_nhc, long first_s
   if (b->g_key != key) {
     if (b->g_step) cudaGraphExecDestroy(b->g_step);
     if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
-    if (b->g_step_prune) cudaGraphExecDestroy(b->g_step_prune);
-    b->g_step = b->g_step_list = b->g_step_prune = nullptr;
-    if ((rc = capture(b, false, use_nhc != 0, false, &b->g_step))) return rc;
-    if ((rc = capture(b, true, use_nhc != 0, false, &b->g_step_list))) return rc;
-    if (b->mx && b->mx->use_inner &&
-        (rc = capture(b, false, use_nhc != 0, true, &b->g_step_prune)))
-      return rc;
+    b->g_step = b->g_step_list = nullptr;
+    if ((rc = capture(b, false, use_nhc != 0, &b->g_step))) return rc;
+    if ((rc = capture(b, true, use_nhc != 0, &b->g_step_list))) return rc;
     b->g_key = key;
   }
   for (long i = first_step; i < first_step + nsteps; i++) {
     cudaGraphExec_t g = b->g_step;
     if (i % nlist_freq == 0) g = b->g_step_list;
-    else if (b->g_step_prune && i % b->prune_every == 0) g = b->g_step_prune;
     FE_CUDA(cudaGraphLaunch(g, b->stream));
   }
   if (rec)
@@ -787,7 +775,6 @@ int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list) {
   }
   if (plain) *plain = b->launches_plain;
   if (with_list) *with_list = b->launches_list;
-  // a prune step launches exactly one kernel more than a plain step
   return FE_OK;
 }
 
@@ -818,6 +805,36 @@ int fe_list_stats(fe_box *box, int64_t *entries, int *max_row) {
   }
   if (entries) *entries = e;
   if (max_row) *max_row = m;
+  return FE_OK;
+}
+
+int fe_inner_list_stats(fe_box *box, int64_t *entries, int *max_row, int64_t *prunes) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  const int *a = nullptr, *r = nullptr;
+  bool on = false;
+  if (b->mx) mixed_inner_counts(b, &a, &r, &on);
+  if (!on) {
+    set_error("fe_inner_list_stats: no inner list (FP64 mode, or rc + skin >= rclist)");
+    return FE_ERR_STATE;
+  }
+  std::vector<int> c(b->n), c2(b->n);
+  MxPruneState st;
+  FE_CUDA(cudaMemcpyAsync(c.data(), a, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(c2.data(), r, sizeof(int) * b->n, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(&st, mixed_prune_state(b), sizeof(st), cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  int64_t e = 0;
+  int m = 0;
+  for (int i = 0; i < b->n; i++) {
+    int v = c[i] + c2[i];
+    e += v;
+    if (v > m) m = v;
+  }
+  if (entries) *entries = e;
+  if (max_row) *max_row = m;
+  if (prunes) *prunes = (int64_t)st.prunes;
   return FE_OK;
 }
 

@@ -135,10 +135,9 @@ struct Box {
   double *rec = nullptr;       // device records
   long rec_cap = 0;
   int *rec_counter = nullptr;
-  cudaGraphExec_t g_step = nullptr, g_step_list = nullptr, g_step_prune = nullptr;
+  cudaGraphExec_t g_step = nullptr, g_step_list = nullptr;
   int g_key = -1;              // graph capture key (use_nhc)
-  int launches_plain = 0, launches_list = 0, launches_prune = 0;  // own kernels per step
-  int prune_every = 2;         // mixed path: inner-list prune period in fe_run_md
+  int launches_plain = 0, launches_list = 0;  // own kernels per step
   double *stage = nullptr;     // pinned host staging, 4n doubles
   double *xyz_dev = nullptr;   // device staging, 3n doubles (packed x, y, z)
 
@@ -205,7 +204,7 @@ int launch_vv2_kinet(Box *b, double vscal);  // vv2 with the kinetic tensor fold
 int launch_nhc(Box *b, double time_step);
 int launch_record(Box *b);
 // one MD step of the box on its stream (nve_md.c:359-418 / nvt_md.c:529-531)
-int step_body(Box *b, bool with_list, bool use_nhc, bool prune);
+int step_body(Box *b, bool with_list, bool use_nhc);
 // packed xyz (3n doubles) <-> the double4 positions, on the box's stream
 int launch_xyz_scatter(Box *b, const double *xyz, bool to_pos, bool to_nopbc);
 int launch_xyz_gather(Box *b, double *xyz);

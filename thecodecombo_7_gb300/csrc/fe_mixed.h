@@ -8,6 +8,14 @@ namespace fe {
 
 struct Box;
 
+// Device state of the inner list: need (set by a list rebuild), the largest
+// squared displacement since the last prune (float bits) and a prune count.
+struct MxPruneState {
+  int need;
+  unsigned dmax2;
+  unsigned long long prunes;
+};
+
 struct Mixed {
   // cell grid (edge >= rlist / 3) used to sort sites and enumerate candidates
   int nc[3] = {1, 1, 1};
@@ -21,14 +29,15 @@ struct Mixed {
   int *type_s = nullptr;          // site type per sorted slot
   int4 *posfx = nullptr;          // sorted x, y, z as 32-bit fractions of L; w = bits of (float)q
   // outer list (rlist, rebuilt every nlist steps) and inner list (rc + skin,
-  // pruned from it every few steps); rows hold LJ pairs at the front and the
-  // rest at the back, entries are sorted-slot indices
+  // rewritten by the pair kernel when it prunes); rows hold LJ pairs at the
+  // front and the rest at the back, entries are sorted-slot indices
   int cap = 0;
   int *cnt_lj = nullptr, *cnt_nl = nullptr, *ent = nullptr;
   int *icnt_lj = nullptr, *icnt_nl = nullptr, *ient = nullptr;
-  double skin = 0.6;              // inner list radius = rc + skin
-  bool use_inner = false;         // pair kernel reads the inner list (pruning on)
-  bool do_prune = true;           // prune inside the next forces evaluation
+  double skin = 0.8;              // inner list radius = rc + skin
+  bool inner_on = false;          // rc + skin < rlist: the inner list is used
+  int4 *snap = nullptr;           // posfx at the last prune
+  MxPruneState *ps = nullptr;
   unsigned long long *fix = nullptr;  // 3n fixed-point forces (2^32 per kJ/mol/A)
   float *lj_tab = nullptr;        // nt*nt x (eps, sig^2, shift constant)
   unsigned char *lj_on = nullptr; // nt*nt: pair type has an LJ term
@@ -60,14 +69,17 @@ constexpr int kIntraMaxSites = 8;
 
 int mixed_setup(Box *b);
 void mixed_free(Box *b);
-int launch_mixed_list(Box *b);      // sort + outer list + inner list
-int launch_mx_prune(Box *b);        // inner list from the outer list
+int launch_mixed_list(Box *b);      // sort + outer list
 int forces_mixed(Box *b);
 int launch_mixed_assemble(Box *b);
-int launch_mx_pair_only(Box *b);    // the pair kernel alone (timing)
+// the pair kernel alone (inner list unless a rebuild or a displacement asks
+// for a prune)
+int launch_mx_pair_only(Box *b);
 int launch_mx_spread_only(Box *b);  // the spreading kernel alone (timing)
 int mixed_autotune(Box *b, int *nw, int *rw, int *blocks, double *us);
 void mixed_counts(Box *b, const int **lj, const int **rest);  // device row counts (outer)
+void mixed_inner_counts(Box *b, const int **lj, const int **rest, bool *on);
+MxPruneState *mixed_prune_state(Box *b);
 void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s);
 
 }  // namespace fe

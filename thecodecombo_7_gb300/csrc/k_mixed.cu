@@ -15,10 +15,13 @@
 //     holds every non-excluded j within rlist, pairs with an LJ term at the
 //     front and the rest at the back.  It is built per unit of 8 sorted
 //     sites: the candidates near the unit's bounding box are loaded once and
-//     tested against all 8 sites.  Optionally (use_inner) it is pruned
-//     every few steps into an INNER list (rc + skin) for the pair kernel; on
-//     this hardware the prune pass costs about what it saves, because both
-//     are bound by the same j-position gathers, so it is off by default;
+//     tested against all 8 sites;
+//   * the pair kernel reads an INNER list (rc + skin, skin 0.8 A): it prunes
+//     the outer rows into it while computing forces after every list
+//     rebuild and whenever some site has moved skin/2 since the last prune
+//     (measured every step against a snapshot of the positions), so every
+//     pair within rc is always in it -- the forces are those of the outer
+//     list, with ~27 % fewer entries walked;
 //   * excluded / 1-4 pairs (xint) are handled by their own kernel over the
 //     exclusion list (cnonbond_nblist.c:245-263, 416-437 semantics).
 // One warp per i site walks its row with coalesced entry loads; each lane
@@ -130,14 +133,33 @@ __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ p
   }
 }
 
-// per step: sorted fixed-point coordinates and charge
+// per step: sorted fixed-point coordinates and charge; with `snap`, also the
+// largest squared displacement (A^2) of any site since the inner list was
+// last pruned (float bits, atomicMax: non-negative floats order as integers)
 __global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *__restrict__ perm,
-                             double3 invL, int4 *__restrict__ posfx) {
+                             double3 invL, int4 *__restrict__ posfx,
+                             const int4 *__restrict__ snap, float3 sc,
+                             unsigned *__restrict__ dmax2) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
-  if (s >= n) return;
-  double4 p = pos[perm[s]];
-  posfx[s] = make_int4((int)frac32(p.x, invL.x), (int)frac32(p.y, invL.y), (int)frac32(p.z, invL.z),
-                       __float_as_int((float)p.w));
+  float d2 = 0.f;
+  if (s < n) {
+    double4 p = pos[perm[s]];
+    int4 q = make_int4((int)frac32(p.x, invL.x), (int)frac32(p.y, invL.y),
+                       (int)frac32(p.z, invL.z), __float_as_int((float)p.w));
+    posfx[s] = q;
+    if (snap) {
+      int4 o = snap[s];
+      float dx = fx_delta((unsigned)q.x, (unsigned)o.x, sc.x);
+      float dy = fx_delta((unsigned)q.y, (unsigned)o.y, sc.y);
+      float dz = fx_delta((unsigned)q.z, (unsigned)o.z, sc.z);
+      d2 = dx * dx + dy * dy + dz * dz;
+    }
+  }
+  if (snap) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
+    if ((threadIdx.x & 31) == 0 && d2 > 0.f) atomicMax(dmax2, __float_as_uint(d2));
+  }
 }
 
 __device__ __forceinline__ int mx_is_excluded(const int *__restrict__ xs, const int *__restrict__ xp,
@@ -460,43 +482,6 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
   }
 }
 
-// Inner list: the outer row filtered to r < rc + skin, same segment layout.
-__device__ __forceinline__ void prune_segment(int4 pi, const int4 *__restrict__ posfx,
-                                              const int *__restrict__ src, int b0, int b1,
-                                              bool lj, float3 sc, float rp2, int lane, int cap,
-                                              int *__restrict__ dst, RowCursor &rc) {
-  for (int base = b0; base < b1; base += 32) {
-    int k = base + lane;
-    bool ok = false;
-    int j = 0;
-    if (k < b1) {
-      j = src[k];
-      int4 pj = posfx[j];
-      float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, sc.x);
-      float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, sc.y);
-      float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, sc.z);
-      ok = dx * dx + dy * dy + dz * dz < rp2;
-    }
-    row_push(ok, lj, j, lane, cap, dst, rc);
-  }
-}
-
-__global__ void __launch_bounds__(kMxWarps * 32)
-k_mx_prune(int n, const int4 *__restrict__ posfx, float3 sc, float rp2, int cap,
-           const int *__restrict__ cnt_lj, const int *__restrict__ cnt_nl,
-           const int *__restrict__ ent, int *__restrict__ icnt_lj, int *__restrict__ icnt_nl,
-           int *__restrict__ ient, int *__restrict__ status) {
-  int lane = threadIdx.x & 31;
-  for (int s = blockIdx.x * kMxWarps + (threadIdx.x >> 5); s < n; s += gridDim.x * kMxWarps) {
-    int4 pi = posfx[s];
-    const int *src = ent + (size_t)s * cap;
-    int *dst = ient + (size_t)s * cap;
-    RowCursor rc = {0, 0};
-    prune_segment(pi, posfx, src, 0, cnt_lj[s], true, sc, rp2, lane, cap, dst, rc);
-    prune_segment(pi, posfx, src, cap - cnt_nl[s], cap, false, sc, rp2, lane, cap, dst, rc);
-    row_close(rc, cap, s, lane, icnt_lj, icnt_nl, status);
-  }
-}
 
 // ---------------------------------------------------------------------------
 // pair kernel
@@ -506,7 +491,12 @@ struct MxPair {
   float rc2, kappa, c2k, qfe;  // c2k = 2 kappa / sqrt(pi); qfe = QFACTOR / epsRF
   float ron2, sw_den;
   float3 sc;                   // L / 2^32 per axis
+  // inner list: radius^2 (rc + skin)^2, and the squared displacement that
+  // forces a prune ((skin / 2)^2, less a rounding margin)
+  float rp2, thresh2;
+  int inner_on;                // 0: rows always come from the outer list
 };
+
 
 // the reference's erfc (ewald.c:817-836, Numerical Recipes "erfcc") in FP32;
 // ex = exp(-z^2) is shared with the force term
@@ -602,6 +592,41 @@ __device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
   }
 }
 
+// The same walk over an OUTER row while writing the inner row: entries
+// within rc + skin are appended to `irow` (same LJ-front / rest-back layout).
+// Each lane visits the same entries in the same order as mx_segment (and the
+// same two-deep pipeline), but the loop runs the warp's common trip count so
+// that the appends can use warp ballots; lanes past the row end compute
+// nothing and append nothing.
+template <bool WITH_LJ>
+__device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float qi,
+                                                 const int *__restrict__ row, int b0, int b1,
+                                                 int lane, unsigned lt,
+                                                 const int4 *__restrict__ posfx,
+                                                 const float *__restrict__ ljrow,
+                                                 const int *__restrict__ type_s,
+                                                 int *__restrict__ irow, RowCursor &rc,
+                                                 PairAcc &a) {
+  int i = b0 + lane;
+  int e_cur = i < b1 ? row[i] : 0;
+  int e_nxt = i + 32 < b1 ? row[i + 32] : 0;
+  int4 p_cur = posfx[e_cur];
+  for (int base = b0; base < b1; base += 32, i += 32) {
+    int e_nn = i + 64 < b1 ? row[i + 64] : 0;
+    int4 p_nxt = posfx[e_nxt];
+    bool v = i < b1;
+    float dx = fx_delta((unsigned)pi.x, (unsigned)p_cur.x, P.sc.x);
+    float dy = fx_delta((unsigned)pi.y, (unsigned)p_cur.y, P.sc.y);
+    float dz = fx_delta((unsigned)pi.z, (unsigned)p_cur.z, P.sc.z);
+    float r2 = dx * dx + dy * dy + dz * dz;
+    if (v) mx_pair_one<WITH_LJ>(P, pi, qi, e_cur, p_cur, ljrow, type_s, a);
+    if (P.inner_on) row_push_bf(v && r2 < P.rp2, WITH_LJ, e_cur, lt, P.cap, irow, rc);
+    e_cur = e_nxt;
+    p_cur = p_nxt;
+    e_nxt = e_nn;
+  }
+}
+
 // NW warps per block and a register budget of 65536 / (RW * 32) per thread
 // for RW resident warps per SM (48: 40 registers, 32: 64 registers): a
 // launch shape chosen by mixed_autotune.
@@ -610,13 +635,24 @@ __global__ void __launch_bounds__(NW * 32, RW / NW)
 k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
           const int *__restrict__ perm, const int *__restrict__ cnt_lj,
           const int *__restrict__ cnt_nl, const int *__restrict__ ent,
+          int *__restrict__ icnt_lj, int *__restrict__ icnt_nl, int *__restrict__ ient,
+          int4 *__restrict__ snap, MxPruneState *__restrict__ ps,
           const float *__restrict__ lj_tab, unsigned long long *__restrict__ fix,
           unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
-          double *__restrict__ out) {
+          double *__restrict__ out, int *__restrict__ status) {
   extern __shared__ float s_lj[];  // nt*nt*3: eps, sig^2, shift constant
   for (int i = threadIdx.x; i < P.nt * P.nt * 3; i += blockDim.x) s_lj[i] = lj_tab[i];
   __syncthreads();
   int lane = threadIdx.x & 31;
+  unsigned lt = (1u << lane) - 1u;
+  // prune (read the outer list, rewrite the inner one) after a list rebuild
+  // or when some site has moved half the skin since the last prune; between
+  // prunes no pair can come within rc from beyond rc + skin
+  bool prune = !P.inner_on || ps->need != 0 || __uint_as_float(ps->dmax2) >= P.thresh2;
+  if (prune && P.inner_on && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps->prunes, 1ull);
+  const int *rlj = prune ? cnt_lj : icnt_lj;
+  const int *rnl = prune ? cnt_nl : icnt_nl;
+  const int *rent = prune ? ent : ient;
   PairAcc a;
   // energies per row in FP32, then exact fixed-point sums across rows (kept
   // in shared memory by each warp's lane 0): the totals do not depend on how
@@ -628,11 +664,24 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
     int4 pi = posfx[s];
     float qi = __int_as_float(pi.w) * P.qfe;
     const float *ljrow = s_lj + type_s[s] * P.nt * 3;
-    const int *row = ent + (size_t)s * P.cap;
+    const int *row = rent + (size_t)s * P.cap;
     a.fx = a.fy = a.fz = 0.f;
     a.e_lj = a.e_ljs = a.e_real = a.qsum = 0.f;
-    mx_segment<true>(P, pi, qi, row, 0, cnt_lj[s], lane, posfx, ljrow, type_s, a);
-    mx_segment<false>(P, pi, qi, row, P.cap - cnt_nl[s], P.cap, lane, posfx, ljrow, type_s, a);
+    if (prune) {
+      int *irow = ient + (size_t)s * P.cap;
+      RowCursor rc = {0, 0};
+      mx_segment_prune<true>(P, pi, qi, row, 0, rlj[s], lane, lt, posfx, ljrow, type_s, irow, rc,
+                             a);
+      mx_segment_prune<false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, lt, posfx, ljrow,
+                              type_s, irow, rc, a);
+      if (P.inner_on) {
+        row_close(rc, P.cap, s, lane, icnt_lj, icnt_nl, status);
+        if (lane == 0) snap[s] = pi;
+      }
+    } else {
+      mx_segment<true>(P, pi, qi, row, 0, rlj[s], lane, posfx, ljrow, type_s, a);
+      mx_segment<false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, posfx, ljrow, type_s, a);
+    }
     // the row's force: a fixed butterfly of FP32 partial sums (deterministic),
     // converted once to the fixed-point accumulators
     float fx = a.fx, fy = a.fy, fz = a.fz;
@@ -663,7 +712,11 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   if (lane == 0)
 #pragma unroll
     for (int t = 0; t < 4; t++) eq[t] = weq[threadIdx.x >> 5][t];
-  block_fix_final<4>(eq, 32, facc, ticket, out);
+  // the last block: every block has read the prune state, clear it
+  if (block_fix_final<4>(eq, 32, facc, ticket, out) && threadIdx.x == 0) {
+    ps->need = 0;
+    ps->dmax2 = 0u;
+  }
 }
 
 // excluded and 1-4 pairs (xint), cnonbond_nblist.c:245-263 and 416-437:
@@ -1272,6 +1325,10 @@ int mixed_setup(Box *b) {
   FE_CUDA(cudaMalloc(&M.icnt_lj, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.icnt_nl, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.ient, sizeof(int) * (size_t)n * cap));
+  FE_CUDA(cudaMalloc(&M.snap, sizeof(int4) * n));
+  FE_CUDA(cudaMalloc(&M.ps, sizeof(MxPruneState)));
+  FE_CUDA(cudaMemset(M.ps, 0, sizeof(MxPruneState)));
+  M.inner_on = b->p.rc + M.skin < (b->p.rclist < b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
   FE_CUDA(cudaMalloc(&M.fix, sizeof(unsigned long long) * 3 * n));
   // LJ table: eps, sig^2, and the energy shift constant (sr12s - 2 sr6s)
   int nt = b->nt;
@@ -1399,7 +1456,7 @@ void mixed_free(Box *b) {
   Mixed &M = *b->mx;
   void *ptrs[] = {M.cell_count, M.cell_start, M.cell_fill, M.cell_of, M.perm, M.iperm, M.cell_s,
                   M.cz_s, M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
-                  M.ient, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
+                  M.ient, M.snap, M.ps, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
                   M.grid32, M.grid32k, M.floor3, M.sm, M.sd, M.mol_first, M.mol_x,
                   M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai};
   for (void *p : ptrs)
@@ -1417,6 +1474,14 @@ void mixed_counts(Box *b, const int **lj, const int **rest) {
   *rest = b->mx->cnt_nl;
 }
 
+void mixed_inner_counts(Box *b, const int **lj, const int **rest, bool *on) {
+  *lj = b->mx->icnt_lj;
+  *rest = b->mx->icnt_nl;
+  *on = b->mx->inner_on;
+}
+
+MxPruneState *mixed_prune_state(Box *b) { return b->mx->ps; }
+
 static float3 fix_scale(Box *b) {
   return make_float3((float)(b->p.L[0] / kFixScale), (float)(b->p.L[1] / kFixScale),
                      (float)(b->p.L[2] / kFixScale));
@@ -1425,25 +1490,14 @@ static float3 fix_scale(Box *b) {
 static int launch_convert(Box *b) {
   Mixed &M = *b->mx;
   double3 invL = make_double3(1.0 / b->p.L[0], 1.0 / b->p.L[1], 1.0 / b->p.L[2]);
-  k_mx_convert<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->pos_q, M.perm, invL, M.posfx);
+  k_mx_convert<<<(b->n + 255) / 256, 256, 0, b->stream>>>(
+      b->n, b->pos_q, M.perm, invL, M.posfx, M.inner_on ? M.snap : nullptr, fix_scale(b),
+      &M.ps->dmax2);
   FE_LAUNCH_CHECK("k_mx_convert");
   return FE_OK;
 }
 
-static int list_blocks(Box *b) {
-  int blocks = (b->n + kMxWarps - 1) / kMxWarps;
-  return blocks > 152 * 8 ? 152 * 8 : blocks;
-}
 
-int launch_mx_prune(Box *b) {
-  Mixed &M = *b->mx;
-  float rp = (float)(b->p.rc + M.skin);
-  k_mx_prune<<<list_blocks(b), kMxWarps * 32, 0, b->stream>>>(
-      b->n, M.posfx, fix_scale(b), rp * rp, M.cap, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj,
-      M.icnt_nl, M.ient, b->status);
-  FE_LAUNCH_CHECK("k_mx_prune");
-  return FE_OK;
-}
 
 int launch_mixed_list(Box *b) {
   Mixed &M = *b->mx;
@@ -1472,8 +1526,9 @@ int launch_mixed_list(Box *b) {
       b->nt, M.lj_row, M.lj_on, b->x_start, b->x_partner, M.cap, M.cnt_lj, M.cnt_nl, M.ent,
       b->status);
   FE_LAUNCH_CHECK("k_mx_list");
+  // the inner list and its snapshot belong to the old sort: prune next
+  FE_CUDA(cudaMemsetAsync(&M.ps->need, 0x01, sizeof(int), b->stream));
   b->have_list = true;
-  M.do_prune = true;
   return FE_OK;
 }
 
@@ -1499,14 +1554,15 @@ int launch_mx_pair_only(Box *b) {
   P.sw_den = ron2 > 0.0 ? (float)((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2)) : 0.f;
   P.sc = fix_scale(b);
   size_t shm = sizeof(float) * (b->nt * b->nt * 3);
-  const int *clj = M.use_inner ? M.icnt_lj : M.cnt_lj;
-  const int *cnl = M.use_inner ? M.icnt_nl : M.cnt_nl;
-  const int *ent = M.use_inner ? M.ient : M.ent;
+  double rp = b->p.rc + M.skin, hs = 0.5 * M.skin - 1e-4;
+  P.rp2 = (float)(rp * rp);
+  P.thresh2 = (float)(hs * hs);
+  P.inner_on = M.inner_on ? 1 : 0;
   int nw = M.tune_nw, blocks = M.tune_blocks > 0 ? M.tune_blocks : pair_blocks(b, nw);
-#define FE_PAIR_LAUNCH(NWV, RWV)                                                             \
-  k_mx_pair<NWV, RWV><<<blocks, NWV * 32, shm, b->stream>>>(P, M.posfx, M.type_s, M.perm, clj, \
-                                                            cnl, ent, M.lj_tab, M.fix, b->facc, \
-                                                            b->ticket, b->scal + SC_MX_PAIR)
+#define FE_PAIR_LAUNCH(NWV, RWV)                                                                \
+  k_mx_pair<NWV, RWV><<<blocks, NWV * 32, shm, b->stream>>>(                                    \
+      P, M.posfx, M.type_s, M.perm, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl, M.ient,   \
+      M.snap, M.ps, M.lj_tab, M.fix, b->facc, b->ticket, b->scal + SC_MX_PAIR, b->status)
   if (M.tune_rw == 32) {
     if (nw == 4) FE_PAIR_LAUNCH(4, 32);
     else if (nw == 16) FE_PAIR_LAUNCH(16, 32);
@@ -1524,7 +1580,8 @@ int launch_mx_pair_only(Box *b) {
 // Chooses the pair kernel's launch shape for this box: warps per block in
 // {4, 8, 16}, register budget (40 or 64 per thread) and the grid size
 // (multiples of the SM count, or one warp per row), each timed with CUDA
-// events on the box's stream over the current list; the fastest is kept.
+// events on the box's stream over the current (inner) list; the fastest is
+// kept.
 // Forces and energies must be recomputed after.
 int mixed_autotune(Box *b, int *nw_out, int *rw_out, int *blocks_out, double *us_out) {
   Mixed &M = *b->mx;
@@ -1596,7 +1653,6 @@ int forces_mixed(Box *b) {
   int n = b->n;
   int rc;
   if ((rc = launch_convert(b))) return rc;
-  if (M.use_inner && M.do_prune && (rc = launch_mx_prune(b))) return rc;
   FE_CUDA(cudaMemsetAsync(M.fix, 0, sizeof(unsigned long long) * 3 * n, b->stream));
   if ((rc = launch_mx_pair_only(b))) return rc;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;

@@ -166,7 +166,7 @@ static int capture_batch(Batch *B, bool with_list, bool exchange, bool use_nhc,
     Box *b = B->boxes[r];
     e = cudaStreamWaitEvent(b->stream, B->fork, 0);
     if (e != cudaSuccess) break;
-    rc = step_body(b, with_list, use_nhc, false);
+    rc = step_body(b, with_list, use_nhc);
     if (rc) break;
     e = cudaEventRecord(B->join[r], b->stream);
     if (e != cudaSuccess) break;
