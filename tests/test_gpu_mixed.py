@@ -222,3 +222,30 @@ def test_inner_list_pruning():
         b.run_md(1, nlist_freq=1000, first_step=100, record=False)
         _, _, p3 = b.inner_list_stats()
         assert p3 == p2 + 1, "a 0.45 A displacement must trigger a prune"
+
+
+@pytest.mark.parametrize("grid", [(8, 8, 8), (10, 12, 9), (20, 18, 12)],
+                         ids=["8^3", "10x12x9", "20x18x12"])
+def test_mixed_spme_small_and_ragged_grids(grid):
+    """Spreading by bricks of 8^3 points with grids narrower than a brick's
+    halo (a site's spline then reaches the brick through two periodic images)
+    and with short last bricks along an axis (a halo covered by three
+    bricks): forces and the reciprocal energy against the FP64 oracle."""
+    from thecodecombo_7_gb300 import systems
+    if grid == (8, 8, 8):
+        # every brick stages all sites with up to 8 images: at most 512 staged
+        s = systems.water_box(50, L=18.5, seed=5, grid=grid)
+    elif grid == (10, 12, 9):
+        s = systems.water_box(100, L=18.5, seed=5, grid=grid)
+    else:
+        s = systems.water_box(300, density=0.1, seed=5, grid=grid)
+    s.rc = s.rc_ew = 8.0
+    s.rclist = s.rclist_ew = 9.0
+    f_ref, en_ref = O.Oracle(s).forces(s.pos)
+    with _mixed(s) as b:
+        b.nblist()
+        en = b.forces()
+        f = b.get_forces()
+    err = _rms_rel(f, f_ref)
+    assert err <= RMS_TOL, f"rms force error {err:.3e}"
+    assert abs(en["kewald"] - en_ref["kewald"]) <= 2e-6 * abs(en_ref["sewald"])
