@@ -227,13 +227,11 @@ def test_inner_list_pruning():
 @pytest.mark.parametrize("grid", [(8, 8, 8), (10, 12, 9), (20, 18, 12)],
                          ids=["8^3", "10x12x9", "20x18x12"])
 def test_mixed_spme_small_and_ragged_grids(grid):
-    """Spreading by bricks of 8^3 points with grids narrower than a brick's
-    halo (a site's spline then reaches the brick through two periodic images)
-    and with short last bricks along an axis (a halo covered by three
-    bricks): forces and the reciprocal energy against the FP64 oracle."""
+    """Spreading (fixed-point reductions with periodic wrap of the spline
+    points) and gathering on a grid of a few points per axis and on odd
+    grid sizes: forces and the reciprocal energy against the FP64 oracle."""
     from thecodecombo_7_gb300 import systems
     if grid == (8, 8, 8):
-        # every brick stages all sites with up to 8 images: at most 512 staged
         s = systems.water_box(50, L=18.5, seed=5, grid=grid)
     elif grid == (10, 12, 9):
         s = systems.water_box(100, L=18.5, seed=5, grid=grid)

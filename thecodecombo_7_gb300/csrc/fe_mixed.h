@@ -50,10 +50,7 @@ struct Mixed {
   cufftHandle plan_r2c = 0, plan_c2r = 0;
   bool plans = false;
   int *floor3 = nullptr;
-  // spreading: sites binned by the 8x8x8-point brick of their spline origin
-  int nb[3] = {1, 1, 1};
-  int nbk = 1, bkcap = 0;
-  int *bk_count = nullptr, *bk_sites = nullptr;
+  unsigned long long *gfix = nullptr;  // K fixed-point grid sums (2^40 per unit), kept zeroed
   float *sm = nullptr, *sd = nullptr;
   double erfc_rc_over_rc = 0.0;
   // pair kernel launch shape (mixed_autotune): warps per block, grid (0: one warp per row)

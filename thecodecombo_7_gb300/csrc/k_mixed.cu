@@ -40,7 +40,6 @@ constexpr double kFixScale = 4294967296.0;  // 2^32
 constexpr float kFixScaleF = 4294967296.0f;
 constexpr int kMxWarps = 8;                 // warps per block (list, prune, pair)
 constexpr int kMxMaxCellAtoms = 2048;       // sites per cell a sort block handles
-constexpr int kBrick = 8;                   // spreading brick edge (grid points)
 
 __device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScaleF); }
 
@@ -879,244 +878,70 @@ __device__ __forceinline__ void fillspline_f(int order, float w, float *array, f
 // per sorted slot: origin cell and fraction exactly from the 32-bit
 // fixed-point coordinate (u G / 2^32: integer part and remainder), FP32
 // weights, binning
-// B-spline weights and derivatives of every site, its integer spline origin
-// (floor of u G, exact from the 32-bit fraction) and its brick bin: the
-// 8x8x8-point brick holding the origin gets the site's slot appended (in
-// no particular order: the spreading kernel sorts what it stages)
+// B-spline weights and derivatives of every site and its integer spline
+// origin (floor of u G, exact from the 32-bit fraction)
 __global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ posfx,
                              int *__restrict__ floor3, float *__restrict__ sm,
-                             float *__restrict__ sd, int3 nb, int bkcap,
-                             int *__restrict__ bk_count, int *__restrict__ bk_sites,
-                             int *__restrict__ status) {
+                             float *__restrict__ sd) {
   int s = blockIdx.x * blockDim.x + threadIdx.x;
   if (s >= n) return;
   int4 p = posfx[s];
   unsigned u[3] = {(unsigned)p.x, (unsigned)p.y, (unsigned)p.z};
   int g[3] = {G.x, G.y, G.z};
-  int f[3];
   float mn[9], dmn[9];
   for (int d = 0; d < 3; d++) {
     unsigned long long t = (unsigned long long)u[d] * (unsigned)g[d];
-    f[d] = (int)(t >> 32);
     float w = (float)(unsigned)(t & 0xffffffffull) * 0x1p-32f;
     fillspline_f(order, w, mn, dmn);
     for (int m = 1; m <= order; m++) {
       sm[((size_t)s * order + (m - 1)) * 3 + d] = mn[m];
       sd[((size_t)s * order + (m - 1)) * 3 + d] = dmn[m];
     }
-    floor3[3 * s + d] = f[d];
+    floor3[3 * s + d] = (int)(t >> 32);
   }
-  int bin = ((f[0] / kBrick) * nb.y + f[1] / kBrick) * nb.z + f[2] / kBrick;
-  int k = atomicAdd(&bk_count[bin], 1);
-  if (k < bkcap) bk_sites[(size_t)bin * bkcap + k] = s;
-  else atomicOr(status, ST_GRID_OVERFLOW);
 }
 
-// Spreading by point ownership.  A CTA of 256 threads owns an 8x8x8 brick;
-// thread t owns the column (px, py) = ((t >> 2) >> 3, (t >> 2) & 7) and the
-// two points z in [2 (t & 3), 2 (t & 3) + 2).  The sites whose spline
-// reaches the brick have their origin in the brick's halo, the H^3 origins
-// (H = 8 + order - 1) from the brick's corner upward.  The CTA stages them
-// from the brick bins that cover the halo, all bins at once (a site appears
-// once per periodic image of its origin inside the halo, which matters only
-// for grids narrower than H), sorts the staged entries by the key (halo
-// column, z origin, slot) -- a fixed order whatever the bins' order; a
-// bitonic sort held in registers, two keys per thread, with warp shuffles
-// for the strides below 32 -- and stages their charge-scaled B-spline
-// weights.  Each thread then visits only the order x order halo columns
-// that reach its column and adds the weights of its own points.  Every
-// point is summed by one thread in a fixed order: deterministic, with no
-// atomics on the grid and no shared accumulator.
-constexpr int kSp6Threads = 256;
-constexpr int kSp6MaxSites = 2 * kSp6Threads;
-constexpr int kSp6MaxCols = (8 + 8 - 1) * (8 + 8 - 1);  // halo columns at order 8
-constexpr int kSp6MaxBins = 27;
-constexpr int kSp6SlotBits = 20;  // key: col (8 bits) | z origin (4 bits) | slot (20 bits)
+// Spreading by fixed-point reductions: thread (site, mx) adds the
+// contributions q wx wy wz of its site's spline slab mx (order x order
+// points) to a 64-bit fixed-point grid (2^40 per unit) with fire-and-forget
+// integer reductions.  Integer sums do not depend on the order of the
+// additions, so the grid is bitwise reproducible; sites in sorted (spatial)
+// order keep neighbouring threads on neighbouring grid lines.
+constexpr float kSpRedFix = 1099511627776.0f;  // 2^40
+constexpr double kSpRedUnfix = 1.0 / 1099511627776.0;
 
-// one bitonic stage (size k, stride jj) on the keys v0 (index t) and v1
-// (index t + kSp6Threads) held by thread t
-__device__ __forceinline__ void sp6_stage(unsigned &v0, unsigned &v1, int k, int jj,
-                                          unsigned *skey) {
-  const int t = threadIdx.x;
-  if (jj == kSp6Threads) {  // partners in the same thread
-    bool up = (t & k) == 0;
-    unsigned lo = min(v0, v1), hi = max(v0, v1);
-    v0 = up ? lo : hi;
-    v1 = up ? hi : lo;
-    return;
+__global__ void k_mx_spread_red(int n, int order, int3 G, const int4 *__restrict__ posfx,
+                                const float *__restrict__ sm, const int *__restrict__ floor3,
+                                unsigned long long *__restrict__ gfix) {
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = t / order, mx = t - s * order;
+  if (s >= n) return;
+  const float *w = sm + (size_t)s * order * 3;
+  float qwx = __int_as_float(posfx[s].w) * w[mx * 3];
+  int x = floor3[3 * s] - order + 1 + mx, y0 = floor3[3 * s + 1] - order + 1,
+      z0 = floor3[3 * s + 2] - order + 1;
+  if (x < 0) x += G.x;
+  unsigned long long *gx = gfix + (size_t)x * G.y * G.z;
+  for (int my = 0; my < order; my++) {
+    int y = y0 + my;
+    if (y < 0) y += G.y;
+    float v = qwx * w[my * 3 + 1];
+    unsigned long long *gy = gx + (size_t)y * G.z;
+    for (int mz = 0; mz < order; mz++) {
+      int z = z0 + mz;
+      if (z < 0) z += G.z;
+      atomicAdd(gy + z, (unsigned long long)__float2ll_rn(v * w[mz * 3 + 2] * kSpRedFix));
+    }
   }
-  unsigned p0, p1;
-  if (jj < 32) {
-    p0 = __shfl_xor_sync(0xffffffffu, v0, jj);
-    p1 = __shfl_xor_sync(0xffffffffu, v1, jj);
-  } else {
-    skey[t] = v0;
-    skey[t + kSp6Threads] = v1;
-    __syncthreads();
-    p0 = skey[t ^ jj];
-    p1 = skey[(t + kSp6Threads) ^ jj];
-    __syncthreads();
-  }
-  const int i0 = t, i1 = t + kSp6Threads;
-  bool keep_min0 = ((i0 & k) == 0) == (i0 < (i0 ^ jj));
-  bool keep_min1 = ((i1 & k) == 0) == (i1 < (i1 ^ jj));
-  v0 = keep_min0 ? min(v0, p0) : max(v0, p0);
-  v1 = keep_min1 ? min(v1, p1) : max(v1, p1);
 }
 
-__global__ void __launch_bounds__(kSp6Threads)
-k_mx_spread6(int order, int3 G, int3 nb, const int4 *__restrict__ posfx,
-             const float *__restrict__ sm, const int *__restrict__ floor3, int bkcap,
-             const int *__restrict__ bk_count, const int *__restrict__ bk_sites,
-             float *__restrict__ grid, int *__restrict__ status) {
-  __shared__ unsigned key[kSp6MaxSites];
-  __shared__ int colstart[kSp6MaxCols + 1];
-  __shared__ int binid[kSp6MaxBins], binoff[kSp6MaxBins + 1];
-  __shared__ int s_n;
-  extern __shared__ float sw[];  // [axis][order][ns] weights, q folded into x
-  const int tid = threadIdx.x;
-  const int H = kBrick + order - 1, ncol = H * H;
-  const int bz = blockIdx.x % nb.z, by = (blockIdx.x / nb.z) % nb.y, bx = blockIdx.x / (nb.z * nb.y);
-  const int X0 = bx * kBrick, Y0 = by * kBrick, Z0 = bz * kBrick;
-  // bricks covering the halo along each axis (at most 3: the last brick of
-  // an axis may be short), without repeats when the axis wraps onto itself;
-  // the bins' counts are read by one warp in parallel
-  if (tid < 32) {
-    const int gg[3] = {G.x, G.y, G.z}, nn[3] = {nb.x, nb.y, nb.z}, b0[3] = {bx, by, bz};
-    int bl[3][3], bn[3];
-#pragma unroll
-    for (int d = 0; d < 3; d++) {
-      int cnt = 0, covered = 0;
-#pragma unroll
-      for (int k = 0; k < 3; k++)
-        if (k < nn[d] && covered < H) {
-          int b = (b0[d] + k) % nn[d];
-          bl[d][k] = b;
-          cnt++;
-          covered += min(kBrick, gg[d] - b * kBrick);
-        }
-      bn[d] = cnt;
-    }
-    int nbin = bn[0] * bn[1] * bn[2];
-    int lane = tid, bin = 0, m = 0;
-    if (lane < nbin) {
-      int iz = lane % bn[2], iy = (lane / bn[2]) % bn[1], ix = lane / (bn[2] * bn[1]);
-      int bxi = ix == 0 ? bl[0][0] : (ix == 1 ? bl[0][1] : bl[0][2]);
-      int byi = iy == 0 ? bl[1][0] : (iy == 1 ? bl[1][1] : bl[1][2]);
-      int bzi = iz == 0 ? bl[2][0] : (iz == 1 ? bl[2][1] : bl[2][2]);
-      bin = (bxi * nb.y + byi) * nb.z + bzi;
-      m = min(bk_count[bin], bkcap);
-    }
-    int x = m;  // inclusive prefix: lanes past the bins repeat the total
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      int t = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += t;
-    }
-    if (lane < kSp6MaxBins) {
-      binid[lane] = bin;
-      binoff[lane + 1] = x;
-    }
-    if (lane == 0) {
-      binoff[0] = 0;
-      s_n = 0;
-    }
-  }
-  for (int c = tid; c <= ncol; c += kSp6Threads) colstart[c] = 0;
-  __syncthreads();
-  // 1. stage every (site, image) with its origin in the halo
-  const int total = binoff[kSp6MaxBins];
-  for (int e = tid; e < total; e += kSp6Threads) {
-    int k = 0;
-    while (binoff[k + 1] <= e) k++;
-    int j = bk_sites[(size_t)binid[k] * bkcap + (e - binoff[k])];
-    int lx0 = floor3[3 * j] - X0, ly0 = floor3[3 * j + 1] - Y0, lz0 = floor3[3 * j + 2] - Z0;
-    if (lx0 < 0) lx0 += G.x;
-    if (ly0 < 0) ly0 += G.y;
-    if (lz0 < 0) lz0 += G.z;
-    // images lx0, lx0 + G, ... inside the halo
-    for (int lx = lx0; lx < H; lx += G.x)
-      for (int ly = ly0; ly < H; ly += G.y)
-        for (int lz = lz0; lz < H; lz += G.z) {
-          int col = lx * H + ly;
-          int a = atomicAdd(&s_n, 1);
-          if (a < kSp6MaxSites) {
-            key[a] = (unsigned)col << 24 | (unsigned)lz << kSp6SlotBits | (unsigned)j;
-            atomicAdd(&colstart[col + 1], 1);
-          }
-        }
-  }
-  __syncthreads();
-  int ns = s_n;
-  if (ns > kSp6MaxSites) {
-    if (tid == 0) atomicOr(status, ST_GRID_OVERFLOW);
-    ns = kSp6MaxSites;
-  }
-  // 2. sort the keys and turn the column counts into starts
-  unsigned v0 = tid < ns ? key[tid] : ~0u;
-  unsigned v1 = tid + kSp6Threads < ns ? key[tid + kSp6Threads] : ~0u;
-  if (tid < 32) {
-    int run = 0;
-    for (int c0 = 1; c0 <= ncol; c0 += 32) {
-      int c = c0 + tid;
-      int v = c <= ncol ? colstart[c] : 0, x = v;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        int t = __shfl_up_sync(0xffffffffu, x, o);
-        if (tid >= o) x += t;
-      }
-      if (c <= ncol) colstart[c] = run + x;
-      run += __shfl_sync(0xffffffffu, x, 31);
-    }
-  }
-  __syncthreads();
-  int P = 2;
-  while (P < ns) P <<= 1;
-  for (int k = 2; k <= P; k <<= 1)
-    for (int jj = k >> 1; jj > 0; jj >>= 1) sp6_stage(v0, v1, k, jj, key);
-  key[tid] = v0;
-  key[tid + kSp6Threads] = v1;
-  __syncthreads();
-  // 3. weights
-  const int na = ns;
-  for (int a = tid; a < na; a += kSp6Threads) {
-    int j = (int)(key[a] & ((1u << kSp6SlotBits) - 1u));
-    float q = __int_as_float(posfx[j].w);
-    const float *wj = sm + (size_t)j * order * 3;
-    for (int m = 0; m < order; m++) {
-      sw[(0 * order + m) * na + a] = wj[m * 3] * q;
-      sw[(1 * order + m) * na + a] = wj[m * 3 + 1];
-      sw[(2 * order + m) * na + a] = wj[m * 3 + 2];
-    }
-  }
-  __syncthreads();
-  // 4. sum: only the halo columns (lx, ly) in [px, px + order) x [py, py + order)
-  // reach this thread's points; their sites are contiguous after the sort
-  const int pcol = tid >> 2, px = pcol >> 3, py = pcol & 7, pz0 = (tid & 3) * 2;
-  float acc0 = 0.f, acc1 = 0.f;
-  for (int ox = 0; ox < order; ox++) {
-    const int dx = order - 1 - ox;  // spline index along x of column lx = px + ox
-    for (int oy = 0; oy < order; oy++) {
-      const int dy = order - 1 - oy;
-      const int c = (px + ox) * H + (py + oy);
-      const int a1 = min(colstart[c + 1], na);
-      for (int a = min(colstart[c], na); a < a1; a++) {
-        int lz = (int)((key[a] >> kSp6SlotBits) & 15u);
-        int dz = pz0 - (lz - order + 1);
-        if ((unsigned)dz >= (unsigned)order && (unsigned)(dz + 1) >= (unsigned)order) continue;
-        const float *wz = sw + (2 * order) * na + a;
-        float wxy = sw[dx * na + a] * sw[(order + dy) * na + a];
-        if ((unsigned)dz < (unsigned)order) acc0 = fmaf(wxy, wz[dz * na], acc0);
-        if ((unsigned)(dz + 1) < (unsigned)order) acc1 = fmaf(wxy, wz[(dz + 1) * na], acc1);
-      }
-    }
-  }
-  int x = X0 + px, y = Y0 + py;
-  if (x < G.x && y < G.y) {
-    float *g = grid + ((long)x * G.y + y) * G.z;
-    int z = Z0 + pz0;
-    if (z < G.z) g[z] = acc0;
-    if (z + 1 < G.z) g[z + 1] = acc1;
+// FP32 grid from the fixed-point sums; the sums are cleared for the next step
+__global__ void k_mx_fix2grid(long K, unsigned long long *__restrict__ gfix,
+                              float *__restrict__ grid) {
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
+       i += (long)gridDim.x * blockDim.x) {
+    grid[i] = (float)((double)(long long)gfix[i] * kSpRedUnfix);
+    gfix[i] = 0ull;
   }
 }
 
@@ -1344,13 +1169,6 @@ __global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc, int f
 // ---------------------------------------------------------------------------
 // host side
 
-static int spread_attr() {
-  // weights of up to order 8 (the largest order a box accepts): 48 KB
-  FE_CUDA(cudaFuncSetAttribute(k_mx_spread6, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               (int)(sizeof(float) * 3 * 8 * kSp6MaxSites)));
-  return FE_OK;
-}
-
 static int up(int **dst, const std::vector<int> &v) {
   FE_CUDA(cudaMalloc(dst, sizeof(int) * (v.empty() ? 1 : v.size())));
   if (!v.empty())
@@ -1361,11 +1179,6 @@ static int up(int **dst, const std::vector<int> &v) {
 int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
-  if (int rc = spread_attr()) return rc;
-  if (n >= (1 << kSp6SlotBits)) {  // slots share a 32-bit sort key in spreading
-    set_error("mixed precision supports fewer than 2^20 sites per box");
-    return FE_ERR_SIZE;
-  }
   // cell grid of edge >= rlist / kListCellsPerReach
   double edge = (b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew) / kListCellsPerReach;
   M.ncells = 1;
@@ -1526,17 +1339,8 @@ int mixed_setup(Box *b) {
   FE_CUDA(cudaMalloc(&M.grid32, sizeof(float) * K));
   FE_CUDA(cudaMalloc(&M.grid32k, sizeof(cufftComplex) * Kh));
   FE_CUDA(cudaMalloc(&M.floor3, sizeof(int) * 3 * n));
-  // brick bins for spreading: 8x8x8 grid points each, room for twice the
-  // mean occupancy plus 64
-  M.nbk = 1;
-  for (int d = 0; d < 3; d++) {
-    M.nb[d] = (b->G[d] + kBrick - 1) / kBrick;
-    M.nbk *= M.nb[d];
-  }
-  M.bkcap = (2 * n / M.nbk + 64 + 31) / 32 * 32;
-  if (M.bkcap > n + 31) M.bkcap = (n + 31) / 32 * 32;
-  FE_CUDA(cudaMalloc(&M.bk_count, sizeof(int) * M.nbk));
-  FE_CUDA(cudaMalloc(&M.bk_sites, sizeof(int) * (size_t)M.nbk * M.bkcap));
+  FE_CUDA(cudaMalloc(&M.gfix, sizeof(unsigned long long) * b->K));
+  FE_CUDA(cudaMemset(M.gfix, 0, sizeof(unsigned long long) * b->K));
   FE_CUDA(cudaMalloc(&M.sm, sizeof(float) * 3 * (size_t)n * b->order));
   FE_CUDA(cudaMalloc(&M.sd, sizeof(float) * 3 * (size_t)n * b->order));
   cufftResult r = cufftPlan3d(&M.plan_r2c, b->G[0], b->G[1], b->G[2], CUFFT_R2C);
@@ -1553,7 +1357,7 @@ void mixed_free(Box *b) {
   void *ptrs[] = {M.cell_count, M.cell_start, M.cell_fill, M.cell_of, M.perm, M.iperm, M.cell_s,
                   M.cz_s, M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
                   M.ient, M.snap, M.ps, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
-                  M.grid32, M.grid32k, M.floor3, M.bk_count, M.bk_sites, M.sm, M.sd, M.mol_first, M.mol_x,
+                  M.grid32, M.grid32k, M.floor3, M.gfix, M.sm, M.sd, M.mol_first, M.mol_x,
                   M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai};
   for (void *p : ptrs)
     if (p) cudaFree(p);
@@ -1734,12 +1538,12 @@ int mixed_autotune(Box *b, int *nw_out, int *rw_out, int *blocks_out, double *us
 int launch_mx_spread_only(Box *b) {
   Mixed &M = *b->mx;
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
-  int3 nb = make_int3(M.nb[0], M.nb[1], M.nb[2]);
-  size_t swb = sizeof(float) * 3 * (size_t)b->order * kSp6MaxSites;
-  k_mx_spread6<<<M.nbk, kSp6Threads, swb, b->stream>>>(b->order, G, nb, M.posfx, M.sm, M.floor3,
-                                                    M.bkcap, M.bk_count, M.bk_sites, M.grid32,
-                                                    b->status);
-  FE_LAUNCH_CHECK("k_mx_spread6");
+  long nt = (long)b->n * b->order;
+  k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, b->order, G, M.posfx,
+                                                                     M.sm, M.floor3, M.gfix);
+  FE_LAUNCH_CHECK("k_mx_spread_red");
+  k_mx_fix2grid<<<152 * 8, 256, 0, b->stream>>>(b->K, M.gfix, M.grid32);
+  FE_LAUNCH_CHECK("k_mx_fix2grid");
   return FE_OK;
 }
 
@@ -1787,11 +1591,8 @@ int forces_mixed(Box *b) {
   }
   // SPME
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
-  int3 nb = make_int3(M.nb[0], M.nb[1], M.nb[2]);
-  FE_CUDA(cudaMemsetAsync(M.bk_count, 0, sizeof(int) * M.nbk, b->stream));
   k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, M.posfx, M.floor3, M.sm,
-                                                       M.sd, nb, M.bkcap, M.bk_count, M.bk_sites,
-                                                       b->status);
+                                                       M.sd);
   FE_LAUNCH_CHECK("k_mx_splines");
   if ((rc = launch_mx_spread_only(b))) return rc;
   cufftResult r = cufftSetStream(M.plan_r2c, b->stream);
