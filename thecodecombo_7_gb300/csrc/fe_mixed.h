@@ -8,12 +8,15 @@ namespace fe {
 
 struct Box;
 
-// Device state of the inner list: need (set by a list rebuild), the largest
-// squared displacement since the last prune (float bits) and a prune count.
+// Device state of the pair kernel: need (set by a list rebuild), the largest
+// squared displacement since the last prune (float bits), a prune count and
+// the next row to hand out (zero between launches).
 struct MxPruneState {
   int need;
   unsigned dmax2;
   unsigned long long prunes;
+  int next_row;
+  int pad;
 };
 
 struct Mixed {

@@ -485,6 +485,8 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
 // ---------------------------------------------------------------------------
 // pair kernel
 
+constexpr int kPairGrab = 2;  // rows a warp takes from the row counter at a time
+
 struct MxPair {
   int n, nt, cap;
   float rc2, kappa, c2k, qfe;  // c2k = 2 kappa / sqrt(pi); qfe = QFACTOR / epsRF
@@ -518,14 +520,12 @@ struct PairAcc {
 };
 
 // one list entry j of row i: Ewald real space always, LJ when WITH_LJ
+// one pair with its separation (dx, dy, dz), r2 already formed
 template <bool WITH_LJ>
-__device__ __forceinline__ void mx_pair_one(const MxPair &P, int4 pi, float qi, int j, int4 pj,
-                                            const float *__restrict__ ljrow,
-                                            const int *__restrict__ type_s, PairAcc &a) {
-  float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, P.sc.x);
-  float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, P.sc.y);
-  float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, P.sc.z);
-  float r2 = dx * dx + dy * dy + dz * dz;
+__device__ __forceinline__ void mx_pair_core(const MxPair &P, float qi, int j, int4 pj, float dx,
+                                             float dy, float dz, float r2,
+                                             const float *__restrict__ ljrow,
+                                             const int *__restrict__ type_s, PairAcc &a) {
   if (r2 > P.rc2) return;
   float rinv = rsqrtf(r2);
   float r = r2 * rinv;
@@ -562,6 +562,16 @@ __device__ __forceinline__ void mx_pair_one(const MxPair &P, int4 pi, float qi, 
   a.fx = fmaf(F, dx, a.fx);
   a.fy = fmaf(F, dy, a.fy);
   a.fz = fmaf(F, dz, a.fz);
+}
+
+template <bool WITH_LJ>
+__device__ __forceinline__ void mx_pair_one(const MxPair &P, int4 pi, float qi, int j, int4 pj,
+                                            const float *__restrict__ ljrow,
+                                            const int *__restrict__ type_s, PairAcc &a) {
+  float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, P.sc.x);
+  float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, P.sc.y);
+  float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, P.sc.z);
+  mx_pair_core<WITH_LJ>(P, qi, j, pj, dx, dy, dz, dx * dx + dy * dy + dz * dz, ljrow, type_s, a);
 }
 
 // Walks entries b0 + lane, b0 + lane + 32, ... of a row with a two-deep
@@ -618,7 +628,7 @@ __device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float
     float dy = fx_delta((unsigned)pi.y, (unsigned)p_cur.y, P.sc.y);
     float dz = fx_delta((unsigned)pi.z, (unsigned)p_cur.z, P.sc.z);
     float r2 = dx * dx + dy * dy + dz * dz;
-    if (v) mx_pair_one<WITH_LJ>(P, pi, qi, e_cur, p_cur, ljrow, type_s, a);
+    if (v) mx_pair_core<WITH_LJ>(P, qi, e_cur, p_cur, dx, dy, dz, r2, ljrow, type_s, a);
     if (P.inner_on) row_push_bf(v && r2 < P.rp2, WITH_LJ, e_cur, lt, P.cap, irow, rc);
     e_cur = e_nxt;
     p_cur = p_nxt;
@@ -659,7 +669,16 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   __shared__ long long weq[NW][4];
   if (lane < 4) weq[threadIdx.x >> 5][lane] = 0;
   __syncwarp();
-  for (int s = blockIdx.x * NW + (threadIdx.x >> 5); s < P.n; s += gridDim.x * NW) {
+  // rows are taken kPairGrab at a time from a device counter: warps finish
+  // together whatever their rows' lengths (the per-row energies are exact
+  // fixed-point sums, so the results do not depend on which warp took a row)
+  for (;;) {
+    int s0 = 0;
+    if (lane == 0) s0 = atomicAdd(&ps->next_row, kPairGrab);
+    s0 = __shfl_sync(0xffffffffu, s0, 0);
+    if (s0 >= P.n) break;
+    const int s1 = min(s0 + kPairGrab, P.n);
+    for (int s = s0; s < s1; s++) {
     int4 pi = posfx[s];
     float qi = __int_as_float(pi.w) * P.qfe;
     const float *ljrow = s_lj + type_s[s] * P.nt * 3;
@@ -705,16 +724,19 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
 #pragma unroll
       for (int t = 0; t < 4; t++) weq[threadIdx.x >> 5][t] += to_fix(e[t]);
     }
+    }
   }
   __syncwarp();
   long long eq[4] = {0, 0, 0, 0};
   if (lane == 0)
 #pragma unroll
     for (int t = 0; t < 4; t++) eq[t] = weq[threadIdx.x >> 5][t];
-  // the last block: every block has read the prune state, clear it
+  // the last block: every block has read the prune state and taken its
+  // rows, clear both
   if (block_fix_final<4>(eq, 32, facc, ticket, out) && threadIdx.x == 0) {
     ps->need = 0;
     ps->dmax2 = 0u;
+    ps->next_row = 0;
   }
 }
 
