@@ -95,12 +95,11 @@ __device__ __forceinline__ long long to_fixed(double x, int shift) {
 }
 __device__ __forceinline__ long long to_fixed(long long x, int) { return x; }
 
+// The block's part of block_fix_final: its sums added to acc[0..NT).
 template <int NT, typename T>
-__device__ __forceinline__ bool block_fix_final(const T (&v)[NT], int shift,
-                                                unsigned long long *acc, unsigned *ticket,
-                                                double *out) {
+__device__ __forceinline__ void block_fix_add(const T (&v)[NT], int shift,
+                                              unsigned long long *acc) {
   __shared__ long long shq[32][NT];
-  __shared__ bool last_blk;
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   long long q[NT];
 #pragma unroll
@@ -131,6 +130,14 @@ __device__ __forceinline__ bool block_fix_final(const T (&v)[NT], int shift,
       if (lane == 0) atomicAdd(&acc[t], (unsigned long long)x);
     }
   }
+}
+
+template <int NT, typename T>
+__device__ __forceinline__ bool block_fix_final(const T (&v)[NT], int shift,
+                                                unsigned long long *acc, unsigned *ticket,
+                                                double *out) {
+  __shared__ bool last_blk;
+  block_fix_add<NT>(v, shift, acc);
   __threadfence();
   __syncthreads();
   if (threadIdx.x == 0) last_blk = atomicAdd(ticket, 1u) == gridDim.x - 1;

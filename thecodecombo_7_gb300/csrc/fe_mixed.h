@@ -60,6 +60,7 @@ struct Mixed {
   int tune_nw = 8;
   int tune_rw = 48;     // resident warps per SM the register budget is sized for
   int tune_blocks = 0;
+  int nsm = 152;                  // SMs of the box's device
   // Molecules for the fused intramolecular kernel: every bonded and excluded
   // pair lies inside a contiguous run of at most kIntraMaxSites sites.
   // nmol == 0: the topology does not allow it (separate kernels are used).

@@ -629,7 +629,7 @@ __device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float
     float dz = fx_delta((unsigned)pi.z, (unsigned)p_cur.z, P.sc.z);
     float r2 = dx * dx + dy * dy + dz * dz;
     if (v) mx_pair_core<WITH_LJ>(P, qi, e_cur, p_cur, dx, dy, dz, r2, ljrow, type_s, a);
-    if (P.inner_on) row_push_bf(v && r2 < P.rp2, WITH_LJ, e_cur, lt, P.cap, irow, rc);
+    row_push_bf(v && r2 < P.rp2, WITH_LJ, e_cur, lt, P.cap, irow, rc);
     e_cur = e_nxt;
     p_cur = p_nxt;
     e_nxt = e_nn;
@@ -639,7 +639,12 @@ __device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float
 // NW warps per block and a register budget of 65536 / (RW * 32) per thread
 // for RW resident warps per SM (48: 40 registers, 32: 64 registers): a
 // launch shape chosen by mixed_autotune.
-template <int NW, int RW>
+// Two variants run one after the other every evaluation and read the same
+// device state.  PRUNE walks the outer rows, rewrites the inner ones and
+// adds its block sums to the energy accumulators; it returns at once when no
+// prune is due.  The plain variant walks the inner rows (nothing when the
+// PRUNE variant ran), finishes the energies and clears the state.
+template <int NW, int RW, bool PRUNE>
 __global__ void __launch_bounds__(NW * 32, RW / NW)
 k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
           const int *__restrict__ perm, const int *__restrict__ cnt_lj,
@@ -649,19 +654,21 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
           const float *__restrict__ lj_tab, unsigned long long *__restrict__ fix,
           unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
           double *__restrict__ out, int *__restrict__ status) {
+  // prune (read the outer list, rewrite the inner one) after a list rebuild
+  // or when some site has moved half the skin since the last prune; between
+  // prunes no pair can come within rc from beyond rc + skin
+  const bool prune = !P.inner_on || ps->need != 0 || __uint_as_float(ps->dmax2) >= P.thresh2;
+  if (PRUNE && !prune) return;
+  const bool work = PRUNE || !prune;
   extern __shared__ float s_lj[];  // nt*nt*3: eps, sig^2, shift constant
   for (int i = threadIdx.x; i < P.nt * P.nt * 3; i += blockDim.x) s_lj[i] = lj_tab[i];
   __syncthreads();
   int lane = threadIdx.x & 31;
   unsigned lt = (1u << lane) - 1u;
-  // prune (read the outer list, rewrite the inner one) after a list rebuild
-  // or when some site has moved half the skin since the last prune; between
-  // prunes no pair can come within rc from beyond rc + skin
-  bool prune = !P.inner_on || ps->need != 0 || __uint_as_float(ps->dmax2) >= P.thresh2;
-  if (prune && P.inner_on && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps->prunes, 1ull);
-  const int *rlj = prune ? cnt_lj : icnt_lj;
-  const int *rnl = prune ? cnt_nl : icnt_nl;
-  const int *rent = prune ? ent : ient;
+  if (PRUNE && P.inner_on && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps->prunes, 1ull);
+  const int *rlj = PRUNE ? cnt_lj : icnt_lj;
+  const int *rnl = PRUNE ? cnt_nl : icnt_nl;
+  const int *rent = PRUNE ? ent : ient;
   PairAcc a;
   // energies per row in FP32, then exact fixed-point sums across rows (kept
   // in shared memory by each warp's lane 0): the totals do not depend on how
@@ -672,7 +679,7 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   // rows are taken kPairGrab at a time from a device counter: warps finish
   // together whatever their rows' lengths (the per-row energies are exact
   // fixed-point sums, so the results do not depend on which warp took a row)
-  for (;;) {
+  while (work) {
     int s0 = 0;
     if (lane == 0) s0 = atomicAdd(&ps->next_row, kPairGrab);
     s0 = __shfl_sync(0xffffffffu, s0, 0);
@@ -685,17 +692,15 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
     const int *row = rent + (size_t)s * P.cap;
     a.fx = a.fy = a.fz = 0.f;
     a.e_lj = a.e_ljs = a.e_real = a.qsum = 0.f;
-    if (prune) {
+    if (PRUNE && P.inner_on) {
       int *irow = ient + (size_t)s * P.cap;
       RowCursor rc = {0, 0};
       mx_segment_prune<true>(P, pi, qi, row, 0, rlj[s], lane, lt, posfx, ljrow, type_s, irow, rc,
                              a);
       mx_segment_prune<false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, lt, posfx, ljrow,
                               type_s, irow, rc, a);
-      if (P.inner_on) {
-        row_close(rc, P.cap, s, lane, icnt_lj, icnt_nl, status);
-        if (lane == 0) snap[s] = pi;
-      }
+      row_close(rc, P.cap, s, lane, icnt_lj, icnt_nl, status);
+      if (lane == 0) snap[s] = pi;
     } else {
       mx_segment<true>(P, pi, qi, row, 0, rlj[s], lane, posfx, ljrow, type_s, a);
       mx_segment<false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, posfx, ljrow, type_s, a);
@@ -731,8 +736,12 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   if (lane == 0)
 #pragma unroll
     for (int t = 0; t < 4; t++) eq[t] = weq[threadIdx.x >> 5][t];
-  // the last block: every block has read the prune state and taken its
-  // rows, clear both
+  if (PRUNE) {
+    block_fix_add<4>(eq, 32, facc);
+    return;
+  }
+  // the last block: both variants have read the prune state and every row
+  // has been taken, clear both
   if (block_fix_final<4>(eq, 32, facc, ticket, out) && threadIdx.x == 0) {
     ps->need = 0;
     ps->dmax2 = 0u;
@@ -1201,6 +1210,7 @@ static int up(int **dst, const std::vector<int> &v) {
 int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
+  FE_CUDA(cudaDeviceGetAttribute(&M.nsm, cudaDevAttrMultiProcessorCount, b->dev));
   // cell grid of edge >= rlist / kListCellsPerReach
   double edge = (b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew) / kListCellsPerReach;
   M.ncells = 1;
@@ -1481,10 +1491,14 @@ int launch_mx_pair_only(Box *b) {
   P.thresh2 = (float)(hs * hs);
   P.inner_on = M.inner_on ? 1 : 0;
   int nw = M.tune_nw, blocks = M.tune_blocks > 0 ? M.tune_blocks : pair_blocks(b, nw);
-#define FE_PAIR_LAUNCH(NWV, RWV)                                                                \
-  k_mx_pair<NWV, RWV><<<blocks, NWV * 32, shm, b->stream>>>(                                    \
-      P, M.posfx, M.type_s, M.perm, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl, M.ient,   \
-      M.snap, M.ps, M.lj_tab, M.fix, b->facc, b->ticket, b->scal + SC_MX_PAIR, b->status)
+#define FE_PAIR_ARGS                                                                          \
+  P, M.posfx, M.type_s, M.perm, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl, M.ient, M.snap, \
+      M.ps, M.lj_tab, M.fix, b->facc, b->ticket, b->scal + SC_MX_PAIR, b->status
+  // the pruning variant: 64 registers, one resident wave of 8-warp blocks
+  k_mx_pair<8, 32, true><<<M.nsm * 4, 256, shm, b->stream>>>(FE_PAIR_ARGS);
+  FE_LAUNCH_CHECK("k_mx_pair<prune>");
+#define FE_PAIR_LAUNCH(NWV, RWV) \
+  k_mx_pair<NWV, RWV, false><<<blocks, NWV * 32, shm, b->stream>>>(FE_PAIR_ARGS)
   if (M.tune_rw == 32) {
     if (nw == 4) FE_PAIR_LAUNCH(4, 32);
     else if (nw == 16) FE_PAIR_LAUNCH(16, 32);
@@ -1495,6 +1509,7 @@ int launch_mx_pair_only(Box *b) {
     else FE_PAIR_LAUNCH(8, 48);
   }
 #undef FE_PAIR_LAUNCH
+#undef FE_PAIR_ARGS
   FE_LAUNCH_CHECK("k_mx_pair");
   return FE_OK;
 }
