@@ -244,6 +244,7 @@ __device__ __forceinline__ void row_push_bf(bool ok, bool lj, int entry, unsigne
                                             int *__restrict__ row, RowCursor &rc) {
   unsigned mlj = __ballot_sync(0xffffffffu, ok && lj);
   unsigned mnl = __ballot_sync(0xffffffffu, ok && !lj);
+  if ((mlj | mnl) == 0u) return;  // warp-uniform: nothing to append
   int p = lj ? rc.nlj + __popc(mlj & lt) : rc.nnl + __popc(mnl & lt);
   int other = lj ? rc.nnl : rc.nlj;
   int idx = lj ? p : cap - 1 - p;
@@ -967,12 +968,21 @@ __global__ void k_mx_spread_red(int n, int order, int3 G, const int4 *__restrict
 }
 
 // FP32 grid from the fixed-point sums; the sums are cleared for the next step
+// (two points per thread and iteration: 16-byte loads and stores)
 __global__ void k_mx_fix2grid(long K, unsigned long long *__restrict__ gfix,
                               float *__restrict__ grid) {
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < K;
+  const long K2 = K >> 1;
+  longlong2 *g2 = reinterpret_cast<longlong2 *>(gfix);
+  float2 *o2 = reinterpret_cast<float2 *>(grid);
+  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < K2;
        i += (long)gridDim.x * blockDim.x) {
-    grid[i] = (float)((double)(long long)gfix[i] * kSpRedUnfix);
-    gfix[i] = 0ull;
+    longlong2 v = g2[i];
+    o2[i] = make_float2((float)((double)v.x * kSpRedUnfix), (float)((double)v.y * kSpRedUnfix));
+    g2[i] = make_longlong2(0, 0);
+  }
+  if ((K & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+    grid[K - 1] = (float)((double)(long long)gfix[K - 1] * kSpRedUnfix);
+    gfix[K - 1] = 0ull;
   }
 }
 
