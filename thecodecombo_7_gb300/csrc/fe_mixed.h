@@ -11,6 +11,8 @@ struct Box;
 // Device state of the pair kernel: need (set by a list rebuild), the largest
 // squared displacement since the last prune (float bits), a prune count and
 // the next row to hand out (zero between launches).
+constexpr int kIntraMaxSites = 8;
+
 struct MxPruneState {
   int need;
   unsigned dmax2;
@@ -65,12 +67,13 @@ struct Mixed {
   // pair lies inside a contiguous run of at most kIntraMaxSites sites.
   // nmol == 0: the topology does not allow it (separate kernels are used).
   int nmol = 0;
+  int intra_maxs = kIntraMaxSites;  // sites of the largest molecule
   int *mol_first = nullptr;                    // nmol + 1
   int *mol_x = nullptr, *mol_xi = nullptr;     // CSR: exclusion indices per molecule
   int *mol_b = nullptr, *mol_bi = nullptr;     // bond indices
   int *mol_a = nullptr, *mol_ai = nullptr;     // bend indices
 };
-constexpr int kIntraMaxSites = 8;
+
 
 int mixed_setup(Box *b);
 void mixed_free(Box *b);

@@ -1066,6 +1066,29 @@ __global__ void k_mx_finalize(int n, const unsigned long long *__restrict__ fix,
 // arithmetic, with the molecule's forces summed in registers and added to
 // the fixed-point accumulators without atomics (each site belongs to one
 // molecule and no other kernel runs concurrently on the accumulators).
+// site a of a molecule's register arrays, selected without dynamic indexing
+template <int NS>
+__device__ __forceinline__ int4 intra_pick(const int4 (&P)[NS], int a) {
+  int4 r = P[0];
+#pragma unroll
+  for (int i = 1; i < NS; i++)
+    if (a == i) r = P[i];
+  return r;
+}
+template <int NS>
+__device__ __forceinline__ void intra_add(float (&F)[NS][3], int a, float x, float y, float z) {
+#pragma unroll
+  for (int i = 0; i < NS; i++)
+    if (a == i) {
+      F[i][0] += x;
+      F[i][1] += y;
+      F[i][2] += z;
+    }
+}
+
+// NS: the largest molecule (sites) of the box, so that the molecule's
+// positions and forces stay in registers
+template <int NS>
 __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
                            const int *__restrict__ mol_x, const int *__restrict__ mol_xi,
                            const int *__restrict__ mol_b, const int *__restrict__ mol_bi,
@@ -1083,26 +1106,28 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
   float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, e_intra = 0.f, eb = 0.f, ea = 0.f;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmol; m += gridDim.x * blockDim.x) {
     const int lb = mol_first[m], ns = mol_first[m + 1] - lb;
-    int4 P[kIntraMaxSites];
-    float F[kIntraMaxSites][3];
-    for (int i = 0; i < ns; i++) {
-      P[i] = posfx[iperm[lb + i]];
+    int4 P[NS];
+    float F[NS][3];
+#pragma unroll
+    for (int i = 0; i < NS; i++) {
+      P[i] = i < ns ? posfx[iperm[lb + i]] : make_int4(0, 0, 0, 0);
       F[i][0] = F[i][1] = F[i][2] = 0.f;
     }
     for (int t = mol_x[m]; t < mol_x[m + 1]; t++) {
       int x = mol_xi[t];
       int a = ab[2 * x] - lb, bq = ab[2 * x + 1] - lb, xf = flag[x];
       if (xf == 0) continue;
-      float dx = fx_delta((unsigned)P[a].x, (unsigned)P[bq].x, sL.x);
-      float dy = fx_delta((unsigned)P[a].y, (unsigned)P[bq].y, sL.y);
-      float dz = fx_delta((unsigned)P[a].z, (unsigned)P[bq].z, sL.z);
+      const int4 Pa = intra_pick(P, a), Pb = intra_pick(P, bq);
+      float dx = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
+      float dy = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
+      float dz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
       float r2 = dx * dx + dy * dy + dz * dz;
       if (r2 > rc2) continue;
       float rinv = rsqrtf(r2), r = r2 * rinv, rinv2 = rinv * rinv;
       float kr = kappa * r;
       float ex = __expf(-kr * kr);
       float erfckr = erfc_nr_f(kr, ex);
-      float qqab = __int_as_float(P[a].w) * __int_as_float(P[bq].w) * qf;
+      float qqab = __int_as_float(Pa.w) * __int_as_float(Pb.w) * qf;
       float Fs = 0.f;
       float qcorr = qqab;
       if (xf == 4) {
@@ -1122,40 +1147,34 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
       float erfkr = 1.f - erfckr;
       e_intra += qcorr * erfkr * rinv;
       Fs -= qcorr * rinv * rinv2 * (erfkr - c2k * r * ex);
-      F[a][0] += Fs * dx;
-      F[a][1] += Fs * dy;
-      F[a][2] += Fs * dz;
-      F[bq][0] -= Fs * dx;
-      F[bq][1] -= Fs * dy;
-      F[bq][2] -= Fs * dz;
+      intra_add(F, a, Fs * dx, Fs * dy, Fs * dz);
+      intra_add(F, bq, -Fs * dx, -Fs * dy, -Fs * dz);
     }
     for (int t = mol_b[m]; t < mol_b[m + 1]; t++) {
       int u = mol_bi[t];
       int ia = bond_ab[2 * u] - lb, ib = bond_ab[2 * u + 1] - lb;
-      float dx = fx_delta((unsigned)P[ib].x, (unsigned)P[ia].x, sL.x);
-      float dy = fx_delta((unsigned)P[ib].y, (unsigned)P[ia].y, sL.y);
-      float dz = fx_delta((unsigned)P[ib].z, (unsigned)P[ia].z, sL.z);
+      const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib);
+      float dx = fx_delta((unsigned)Pb.x, (unsigned)Pa.x, sL.x);
+      float dy = fx_delta((unsigned)Pb.y, (unsigned)Pa.y, sL.y);
+      float dz = fx_delta((unsigned)Pb.z, (unsigned)Pa.z, sL.z);
       float dr = sqrtf(dx * dx + dy * dy + dz * dz);
       float rr = dr - (float)bond_req[u];
       float fr = -(float)bond_k[u] * rr * 2.f;
       eb += -(fr * rr * 0.5f);
       float sc = fr / dr;
-      F[ia][0] -= sc * dx;
-      F[ia][1] -= sc * dy;
-      F[ia][2] -= sc * dz;
-      F[ib][0] += sc * dx;
-      F[ib][1] += sc * dy;
-      F[ib][2] += sc * dz;
+      intra_add(F, ia, -sc * dx, -sc * dy, -sc * dz);
+      intra_add(F, ib, sc * dx, sc * dy, sc * dz);
     }
     for (int t = mol_a[m]; t < mol_a[m + 1]; t++) {
       int u = mol_ai[t];
       int ia = bend_abc[3 * u] - lb, ib = bend_abc[3 * u + 1] - lb, ic = bend_abc[3 * u + 2] - lb;
-      float dax = fx_delta((unsigned)P[ia].x, (unsigned)P[ib].x, sL.x);
-      float day = fx_delta((unsigned)P[ia].y, (unsigned)P[ib].y, sL.y);
-      float daz = fx_delta((unsigned)P[ia].z, (unsigned)P[ib].z, sL.z);
-      float dcx = fx_delta((unsigned)P[ic].x, (unsigned)P[ib].x, sL.x);
-      float dcy = fx_delta((unsigned)P[ic].y, (unsigned)P[ib].y, sL.y);
-      float dcz = fx_delta((unsigned)P[ic].z, (unsigned)P[ib].z, sL.z);
+      const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib), Pc = intra_pick(P, ic);
+      float dax = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
+      float day = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
+      float daz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
+      float dcx = fx_delta((unsigned)Pc.x, (unsigned)Pb.x, sL.x);
+      float dcy = fx_delta((unsigned)Pc.y, (unsigned)Pb.y, sL.y);
+      float dcz = fx_delta((unsigned)Pc.z, (unsigned)Pb.z, sL.z);
       float drai = rsqrtf(dax * dax + day * day + daz * daz);
       float erax = dax * drai, eray = day * drai, eraz = daz * drai;
       float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
@@ -1172,21 +1191,18 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
             fza = (eraz * cosphi - ercz) * irasin;
       float fxc = (ercx * cosphi - erax) * ircsin, fyc = (ercy * cosphi - eray) * ircsin,
             fzc = (ercz * cosphi - eraz) * ircsin;
-      F[ia][0] += fxa;
-      F[ia][1] += fya;
-      F[ia][2] += fza;
-      F[ic][0] += fxc;
-      F[ic][1] += fyc;
-      F[ic][2] += fzc;
-      F[ib][0] -= fxa + fxc;
-      F[ib][1] -= fya + fyc;
-      F[ib][2] -= fza + fzc;
+      intra_add(F, ia, fxa, fya, fza);
+      intra_add(F, ic, fxc, fyc, fzc);
+      intra_add(F, ib, -(fxa + fxc), -(fya + fyc), -(fza + fzc));
     }
-    for (int i = 0; i < ns; i++)
-      for (int c = 0; c < 3; c++) {
-        unsigned long long *q = fix + 3 * (size_t)(lb + i) + c;
-        *q = *q + (unsigned long long)to_fix(F[i][c]);
-      }
+#pragma unroll
+    for (int i = 0; i < NS; i++)
+      if (i < ns)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+          unsigned long long *q = fix + 3 * (size_t)(lb + i) + c;
+          *q = *q + (unsigned long long)to_fix(F[i][c]);
+        }
   }
   float v[7] = {e_lj, e_ljs, e_real, qsum, e_intra, eb, ea};
   block_fix_final<7>(v, 32, facc, ticket, out);
@@ -1361,6 +1377,9 @@ int mixed_setup(Box *b) {
       if ((rc = up(&M.mol_b, bo)) || (rc = up(&M.mol_bi, bi))) return rc;
       if ((rc = up(&M.mol_a, ao)) || (rc = up(&M.mol_ai, ai))) return rc;
       M.nmol = nm;
+      M.intra_maxs = 1;
+      for (int m = 0; m < nm; m++)
+        if (first[m + 1] - first[m] > M.intra_maxs) M.intra_maxs = first[m + 1] - first[m];
     }
   }
 
@@ -1608,12 +1627,16 @@ int forces_mixed(Box *b) {
   if (M.nmol > 0) {
     int mb = (M.nmol + 127) / 128;
     if (mb > 2048) mb = 2048;
-    k_mx_intra<<<mb, 128, 0, b->stream>>>(
-        M.nmol, M.mol_first, M.mol_x, M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai, M.excl_ab,
-        M.excl_flag, b->bond_ab, b->bond_req, b->bond_k, b->bend_abc, b->bend_t0, b->bend_k,
-        M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),
-        (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,
-        M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA);
+#define FE_INTRA_ARGS                                                                           \
+  M.nmol, M.mol_first, M.mol_x, M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai, M.excl_ab,        \
+      M.excl_flag, b->bond_ab, b->bond_req, b->bond_k, b->bend_abc, b->bend_t0, b->bend_k,        \
+      M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),                 \
+      (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,     \
+      M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA
+    if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
+    else if (M.intra_maxs <= 4) k_mx_intra<4><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
+    else k_mx_intra<kIntraMaxSites><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
+#undef FE_INTRA_ARGS
     FE_LAUNCH_CHECK("k_mx_intra");
   } else {
     int xb = (M.nexcl + 255) / 256;
