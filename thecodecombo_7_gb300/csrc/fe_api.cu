@@ -27,10 +27,8 @@ int cufft_fail(cufftResult r, const char *what) {
   return FE_ERR_CUDA;
 }
 
-int check_status(Box *b) {
-  int st = 0;
-  FE_CUDA(cudaMemcpyAsync(&st, b->status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
-  FE_CUDA(cudaStreamSynchronize(b->stream));
+// the error behind a device status word st (zero: none); clears the word
+static int status_error(Box *b, int st) {
   if (st == 0) return FE_OK;
   FE_CUDA(cudaMemsetAsync(b->status, 0, sizeof(int), b->stream));
   std::string m = "device status:";
@@ -45,6 +43,13 @@ int check_status(Box *b) {
   return FE_ERR_DEVICE;
 }
 
+int check_status(Box *b) {
+  int st = 0;
+  FE_CUDA(cudaMemcpyAsync(&st, b->status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return status_error(b, st);
+}
+
 template <class T>
 static int upload(T **dst, const T *src, size_t count) {
   FE_CUDA(cudaMalloc(dst, sizeof(T) * (count ? count : 1)));
@@ -52,11 +57,14 @@ static int upload(T **dst, const T *src, size_t count) {
   return FE_OK;
 }
 
+// scalars and the status word to the host with one synchronisation
 static int sync_scal(Box *b) {
+  int st = 0;
   FE_CUDA(cudaMemcpyAsync(b->host_scal, b->scal, sizeof(double) * SC_COUNT, cudaMemcpyDeviceToHost,
                           b->stream));
+  FE_CUDA(cudaMemcpyAsync(&st, b->status, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
   FE_CUDA(cudaStreamSynchronize(b->stream));
-  return check_status(b);
+  return status_error(b, st);
 }
 
 static int launch_list(Box *b) {

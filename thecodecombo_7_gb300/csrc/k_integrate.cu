@@ -264,9 +264,40 @@ __global__ void k_kinet_final(double *__restrict__ s) {
   s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
 }
 
+// kinet for the mixed-precision path: the same tensor in one launch, summed
+// in exact fixed point (2^-20 amu A^2/ps^2) like the fused second half kick
+__global__ void k_kinet_fix(int n, const double *__restrict__ mass, const double *__restrict__ vv,
+                            const double *__restrict__ uu, unsigned long long *__restrict__ facc,
+                            unsigned *__restrict__ ticket, double *__restrict__ s) {
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double fac = mass[i];
+    double sx = vv[3 * i] + uu[3 * i];
+    double sy = vv[3 * i + 1] + uu[3 * i + 1];
+    double sz = vv[3 * i + 2] + uu[3 * i + 2];
+    k[0] += fac * sx * sx;
+    k[1] += fac * sy * sx;
+    k[2] += fac * sy * sy;
+    k[3] += fac * sz * sx;
+    k[4] += fac * sz * sy;
+    k[5] += fac * sz * sz;
+  }
+  if (block_fix_final<6>(k, 20, facc, ticket, s + SC_KEN) && threadIdx.x == 0) {
+    double f = (0.125) * (kNA * kAU * 10.0);  // kinet.c:50-65
+    for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
+    s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
+  }
+}
+
 int launch_kinet(Box *b) {
   int blocks = (b->n + 255) / 256;
   if (blocks > 512) blocks = 512;
+  if (b->mx) {
+    k_kinet_fix<<<blocks, 256, 0, b->stream>>>(b->n, b->mass, b->vv, b->uu, b->facc, b->ticket,
+                                               b->scal);
+    FE_LAUNCH_CHECK("k_kinet_fix");
+    return FE_OK;
+  }
   k_kinet<<<blocks, 256, 0, b->stream>>>(b->n, b->mass, b->vv, b->uu, b->partials);
   FE_LAUNCH_CHECK("k_kinet");
   int rc = launch_reduce(b, b->partials, blocks, 6, SC_KEN, 1.0);
