@@ -410,6 +410,12 @@ int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list);
 /* Entries of the current pair list (half list in FP64 mode, full list in
  * mixed mode) and the longest row. */
 int fe_list_stats(fe_box *box, int64_t *entries, int *max_row);
+/* nl_check(lb, ub, k), nblist.c:607-647 (DLIST): *nl_flag = 1 if any site
+ * of [lb, ub) has moved more than (rclist - rc)/4 since the last fe_nblist
+ * (along one axis or in distance, with the reference's image rule), else 0.
+ * The reference keeps its nl_flag set until the next nblist; a caller that
+ * mirrors it ORs the result in. */
+int fe_nl_check(fe_box *box, int lb, int ub, int *nl_flag);
 /* Mixed mode: entries and longest row of the inner list (rc + 0.8 A) the
  * pair kernel walks between prunes, and how many pair-kernel launches have
  * pruned it from the outer list so far (after every list rebuild, and when a

@@ -434,3 +434,21 @@ def go_baoab(g, r, nsteps, seed, step0=0, T=None, pos=None, vel=None):
                       C.c_double(g.T[r] if T is None else T), C.c_uint64(seed),
                       C.c_uint64(step0), int(nsteps))
     return x, v, e
+
+
+def nl_check(pos, pos0, L, rclist, rc, lb=0, ub=None):
+    """nl_check (nblist.c:607-647, DLIST), restated: 1 if any site of
+    [lb, ub) has moved more than (rclist - rc)/4 from pos0 along one axis or
+    in distance; per axis |d| > L/2 subtracts L, as the reference does."""
+    ub = len(pos) if ub is None else ub
+    L = np.asarray(L, float)
+    h = L / 2.0
+    rcut = (rclist - rc) / 4.0
+    for i in range(lb, ub):
+        d = np.abs(np.asarray(pos[i], float) - np.asarray(pos0[i], float))
+        d = np.where(d > h, d - L, d)
+        if (d > rcut).any():
+            return 1
+        if d[0] * d[0] + d[1] * d[1] + d[2] * d[2] > rcut * rcut:
+            return 1
+    return 0

@@ -247,3 +247,39 @@ def test_mixed_spme_small_and_ragged_grids(grid):
     err = _rms_rel(f, f_ref)
     assert err <= RMS_TOL, f"rms force error {err:.3e}"
     assert abs(en["kewald"] - en_ref["kewald"]) <= 2e-6 * abs(en_ref["sewald"])
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_nl_check_matches_oracle(precision):
+    """fe_nl_check against the oracle's restatement of nl_check after moves
+    below, at and above (rclist - rc)/4, including a site moved across the
+    periodic boundary and a restricted site range."""
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(300, density=0.1, seed=4)
+    prec = engine.FE_PREC_FP64 if precision == "fp64" else engine.FE_PREC_MIXED
+    with engine.Box(s, precision=prec) as b:
+        b.nblist()
+        p0 = b.get_positions()
+        rng = np.random.default_rng(3)
+        rcut = (s.rclist - s.rc) / 4.0
+        cases = []
+        for amp in (0.2 * rcut, 0.55 * rcut, 0.95 * rcut, 1.05 * rcut):
+            d = np.zeros_like(p0)
+            d[rng.integers(0, s.n, 5)] = rng.normal(size=(5, 3)) * amp / np.sqrt(3)
+            cases.append(d)
+        far = np.zeros_like(p0)
+        far[s.n - 1, 2] = 1.2 * rcut  # a site past the threshold, outside [0, n/2)
+        cases.append(far)
+        edge = np.zeros_like(p0)
+        k = int(np.argmax(p0[:, 0]))
+        edge[k, 0] = s.L[0] / 2 - p0[k, 0] + 0.3 * rcut  # crosses +L/2, wraps
+        cases.append(edge)
+        got, want = [], []
+        for d in cases:
+            b.set_positions(p0 + d)
+            p = b.get_positions()
+            for lb, ub in ((0, s.n), (0, s.n // 2)):
+                got.append(b.nl_check(lb, ub))
+                want.append(O.nl_check(p, p0, s.L, s.rclist, s.rc, lb, ub))
+        assert got == want
+        assert 0 in want and 1 in want

@@ -67,9 +67,13 @@ static int sync_scal(Box *b) {
   return status_error(b, st);
 }
 
+// the list, then the snapshot nl_check compares against (nblist.c:583-591)
 static int launch_list(Box *b) {
-  if (b->mx) return launch_mixed_list(b);
-  return launch_nblist(b);
+  int rc = b->mx ? launch_mixed_list(b) : launch_nblist(b);
+  if (rc) return rc;
+  FE_CUDA(cudaMemcpyAsync(b->pos_list0, b->pos_q, sizeof(double4) * b->n,
+                          cudaMemcpyDeviceToDevice, b->stream));
+  return FE_OK;
 }
 
 // forces() on the device, forces.c:118-219
@@ -89,7 +93,7 @@ static int forces_device(Box *b) {
 }
 
 static void free_box(Box *b) {
-  void *ptrs[] = {b->pos_q, b->pos_nopbc, b->vv, b->uu, b->ff, b->mass, b->imass100, b->type, b->lj_eps,
+  void *ptrs[] = {b->pos_q, b->pos_nopbc, b->pos_list0, b->nl_dev, b->vv, b->uu, b->ff, b->mass, b->imass100, b->type, b->lj_eps,
                   b->lj_sig, b->x_start, b->x_partner, b->x_flag, b->bond_ab, b->bend_abc,
                   b->bond_req, b->bond_k, b->bend_t0, b->bend_k, b->cell_count, b->cell_start,
                   b->cell_fill, b->cell_atoms, b->cell_of, b->nl_count, b->nl_ent, b->eterm,
@@ -170,6 +174,8 @@ static int create(Box *b, const fe_box_params *p) {
   int rc;
   if ((rc = upload(&b->pos_q, pq.data(), n))) return rc;
   FE_CUDA(cudaMalloc(&b->pos_nopbc, sizeof(double) * 3 * n));
+  FE_CUDA(cudaMalloc(&b->pos_list0, sizeof(double4) * n));
+  FE_CUDA(cudaMalloc(&b->nl_dev, sizeof(int)));
   FE_CUDA(cudaMalloc(&b->vv, sizeof(double) * 3 * n));
   FE_CUDA(cudaMalloc(&b->uu, sizeof(double) * 3 * n));
   FE_CUDA(cudaMalloc(&b->ff, sizeof(double) * 3 * n));
@@ -813,6 +819,23 @@ int fe_list_stats(fe_box *box, int64_t *entries, int *max_row) {
   }
   if (entries) *entries = e;
   if (max_row) *max_row = m;
+  return FE_OK;
+}
+
+int fe_nl_check(fe_box *box, int lb, int ub, int *nl_flag) {
+  if (!box || !nl_flag || lb < 0 || ub < lb || ub > box->b.n) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!b->have_list) {
+    set_error("fe_nl_check needs a list built by fe_nblist");
+    return FE_ERR_STATE;
+  }
+  FE_CUDA(cudaMemsetAsync(b->nl_dev, 0, sizeof(int), b->stream));
+  int rc = launch_nl_check(b, lb, ub, b->nl_dev);
+  if (rc) return rc;
+  int f = 0;
+  FE_CUDA(cudaMemcpyAsync(&f, b->nl_dev, sizeof(int), cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  *nl_flag = f;
   return FE_OK;
 }
 

@@ -73,6 +73,8 @@ struct Box {
   // sites
   double4 *pos_q = nullptr;   // x, y, z (wrapped), q
   double *pos_nopbc = nullptr;  // 3n
+  double4 *pos_list0 = nullptr; // n: wrapped positions at the last list build (nl_check)
+  int *nl_dev = nullptr;        // 1: nl_check's flag
   double *vv = nullptr, *uu = nullptr, *ff = nullptr;  // 3n, struct veloc layout
   double *mass = nullptr;
   double *imass100 = nullptr;  // 100 / mass (integrate_vverlet.c:56), one division at setup
@@ -184,6 +186,7 @@ extern thread_local long g_launches;
 // k_nblist.cu
 int nblist_setup(Box *b);
 int launch_nblist(Box *b);
+int launch_nl_check(Box *b, int lb, int ub, int *dflag);  // nblist.c:607-647
 // k_pair64.cu
 int launch_pair64(Box *b);
 int launch_bonded64(Box *b);

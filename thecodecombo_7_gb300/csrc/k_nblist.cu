@@ -207,6 +207,36 @@ int nblist_setup(Box *b) {
   return FE_OK;
 }
 
+// nblist.c:607-647 (DLIST): whether any site of [lb, ub) has moved more than
+// (rclist - rc) / 4 from its position at the last list build, along one axis
+// or in distance, with the reference's per-axis image rule (|d| > half box:
+// subtract the box length)
+__global__ void k_nl_check(int lb, int ub, double3 L, double3 H, double rcut, double rcut2,
+                           const double4 *__restrict__ pos, const double4 *__restrict__ pos0,
+                           int *__restrict__ flag) {
+  int i = lb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ub) return;
+  double4 p = pos[i], q = pos0[i];
+  double dx = fabs(p.x - q.x);
+  if (dx > H.x) dx -= L.x;
+  double dy = fabs(p.y - q.y);
+  if (dy > H.y) dy -= L.y;
+  double dz = fabs(p.z - q.z);
+  if (dz > H.z) dz -= L.z;
+  if (dx > rcut || dy > rcut || dz > rcut || dx * dx + dy * dy + dz * dz > rcut2) atomicOr(flag, 1);
+}
+
+int launch_nl_check(Box *b, int lb, int ub, int *dflag) {
+  if (ub <= lb) return FE_OK;
+  double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
+  double3 H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);
+  double rcut = (b->p.rclist - b->p.rc) / 4.0;
+  k_nl_check<<<(ub - lb + 255) / 256, 256, 0, b->stream>>>(lb, ub, L, H, rcut, rcut * rcut,
+                                                           b->pos_q, b->pos_list0, dflag);
+  FE_LAUNCH_CHECK("k_nl_check");
+  return FE_OK;
+}
+
 int launch_nblist(Box *b) {
   int n = b->n;
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);

@@ -44,7 +44,7 @@ EXPORTS = [
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
-    "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats",
+    "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats", "fe_nl_check",
     "fe_ewald_kspace_energy_noalloc",
     "fe_batch_create", "fe_batch_destroy", "fe_batch_run", "fe_batch_state",
     "fe_batch_step_launches", "fe_batch_get_stream",
@@ -369,6 +369,14 @@ class Box:
         e, m = C.c_int64(), C.c_int()
         self._check(self.lib.fe_list_stats(self.h, C.byref(e), C.byref(m)))
         return e.value, m.value
+
+    def nl_check(self, lb=0, ub=None):
+        """nl_check (nblist.c:607-647): 1 if a site of [lb, ub) moved more than
+        (rclist - rc)/4 since the last nblist, else 0."""
+        f = C.c_int()
+        ub = self.sysm.n if ub is None else ub
+        self._check(self.lib.fe_nl_check(self.h, int(lb), int(ub), C.byref(f)))
+        return f.value
 
     def inner_list_stats(self):
         """Mixed mode: (entries, longest row, prunes so far) of the inner list."""
