@@ -173,12 +173,27 @@ static void put_energies(int k, const double *e) {
   en[k].iewald = e[FE_EN_IEWALD];
 }
 
-/* nblist.c:32 */
+/* nblist.c:32 (under DLIST it also takes the snapshot nl_check compares
+ * against and clears nl_flag, nblist.c:583-591) */
 void nblist(int ibox) {
   fe_box *b = fe_of(ibox);
   put_atoms(b, ibox, 0);
   FE_OR_DIE(fe_nblist(b), "nblist");
+#ifdef DLIST
+  nl_flag[ibox] = 0;
+#endif
 }
+
+#ifdef DLIST
+/* nblist.c:607 */
+void nl_check(int lb, int ub, int k) {
+  fe_box *b = fe_of(k);
+  int f = 0;
+  put_atoms(b, k, 0);
+  FE_OR_DIE(fe_nl_check(b, lb, ub, &f), "nl_check");
+  if (f) nl_flag[k] = 1;
+}
+#endif
 
 /* forces.c:118 */
 void forces(int ibox) {
