@@ -256,6 +256,8 @@ def test_nl_check_matches_oracle(precision):
     periodic boundary and a restricted site range."""
     from thecodecombo_7_gb300 import engine, systems
     s = systems.water_box(300, density=0.1, seed=4)
+    s.rc = s.rc_ew = 8.0  # mixed precision needs rclist < L/2 (L = 20.8 A)
+    s.rclist = s.rclist_ew = 9.0
     prec = engine.FE_PREC_FP64 if precision == "fp64" else engine.FE_PREC_MIXED
     with engine.Box(s, precision=prec) as b:
         b.nblist()
