@@ -8,6 +8,7 @@
 #                     bit-reproducible, used for golden vectors
 #   ref_harness_fast  the reference makefile's own flags (makefile:84-88:
 #                     -O3 -ffast-math -funroll-all-loops -std=c99), for timing
+#   ref_harness_dlist the strict build with -DDLIST (nl_check)
 #
 # Feature flags: -DNLIST -DEWALD -DSPME -DSTYPE.  FFTW3 is not installed, so
 # the five FFTW symbols come from oracle/fftw_shim (the oracle's own FFT).
@@ -34,4 +35,6 @@ build() {
 }
 build ref_harness -std=gnu99 -O2 -ffp-contract=off
 build ref_harness_fast -std=c99 -D_POSIX_C_SOURCE=200809L -O3 -ffast-math -funroll-all-loops
-echo "build_ref: built $OUT/ref_harness and $OUT/ref_harness_fast"
+# the DLIST build (nl_check and the list-time snapshot, nblist.c:583-647)
+build ref_harness_dlist -std=gnu99 -O2 -ffp-contract=off -DDLIST
+echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast and $OUT/ref_harness_dlist"

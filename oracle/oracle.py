@@ -22,6 +22,7 @@ LIB_FAST = os.path.join(HERE, "liboracle_fast.so")
 SRC = [os.path.join(HERE, "fe_oracle.c"), os.path.join(HERE, "fe_fft.c")]
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 REF_BIN_FAST = os.path.join(HERE, "_ref", "ref_harness_fast")
+REF_BIN_DLIST = os.path.join(HERE, "_ref", "ref_harness_dlist")
 
 # strict IEEE: no FMA contraction, no fast-math, so results are reproducible
 # on x86-64 and aarch64 alike and match a strict build of the reference
@@ -340,6 +341,25 @@ def run_reference(mode, sysm, workdir, nsteps=None, fast=False):
     write_system_file(sp, sysm)
     cmd = [binp, mode, sp, op] + ([str(nsteps)] if nsteps is not None else [])
     subprocess.check_call(cmd)
+    return read_tagged(op)
+
+
+def run_reference_nlcheck(sysm, cases, workdir):
+    """The reference's own nl_check (-DDLIST build) on sysm: cases are
+    (lb, ub, [(site, dx, dy, dz), ...]) applied to the list-time positions,
+    wrapped by the reference's pbc_all, then checked."""
+    os.makedirs(workdir, exist_ok=True)
+    sp = os.path.join(workdir, "system.bin")
+    cp = os.path.join(workdir, "cases.bin")
+    op = os.path.join(workdir, "out_nlcheck.bin")
+    write_system_file(sp, sysm)
+    with open(cp, "wb") as f:
+        f.write(struct.pack("<i", len(cases)))
+        for lb, ub, moves in cases:
+            f.write(struct.pack("<iii", lb, ub, len(moves)))
+            for i, dx, dy, dz in moves:
+                f.write(struct.pack("<iddd", i, dx, dy, dz))
+    subprocess.check_call([REF_BIN_DLIST, "nlcheck", sp, op, cp])
     return read_tagged(op)
 
 

@@ -21,6 +21,11 @@
  *   mode forces : force/energy breakdown at the input configuration
  *   mode nve    : nsteps of NVE velocity Verlet (list rebuilt every nlist)
  *   mode nhc    : nsteps of NHC-VV (integrate_nhc / integrate_vverlet / integrate_nhc)
+ *   mode nlcheck (the -DDLIST build, ref_harness_dlist): nblist, then per
+ *                 case of <cases.bin> (the 4th argument) the snapshot
+ *                 positions plus the case's displacements, pbc_all, and
+ *                 nl_check(lb, ub) (nblist.c:607-647); dumps the flags and
+ *                 the checked positions
  */
 #define MAIN
 #include "defines.h"
@@ -37,6 +42,10 @@ void cnonbondnl(int, double *);
 void integrate_vverlet(int, double);
 void integrate_nhc(double, int);
 void kinet(int);
+void pbc_all(int);
+#ifdef DLIST
+void nl_check(int, int, int);
+#endif
 double cbond(int);
 double cbend(int);
 
@@ -392,6 +401,66 @@ int main(int argc, char **argv) {
       dump_d("zeta", z, 3 * (int64_t)M);
     }
     free(rec);
+#ifdef DLIST
+  } else if (strcmp(mode, "nlcheck") == 0) {
+    /* allocate.c:51-74 */
+    rx0 = calloc(1, sizeof(double *));
+    ry0 = calloc(1, sizeof(double *));
+    rz0 = calloc(1, sizeof(double *));
+    rx0[k] = calloc(N, sizeof(double));
+    ry0[k] = calloc(N, sizeof(double));
+    rz0[k] = calloc(N, sizeof(double));
+    nl_flag = calloc(1, sizeof(int));
+    nblist(k); /* takes the snapshot, nblist.c:583-591 */
+    if (argc < 5) die("nlcheck needs a cases file");
+    FILE *cf = fopen(argv[4], "rb");
+    if (!cf) die("cannot open cases file");
+    int32_t ncase;
+    rd(&ncase, 4, 1, cf);
+    int *flags = malloc(sizeof(int) * (size_t)ncase);
+    double *pos = malloc(sizeof(double) * 3 * (size_t)N * (size_t)ncase);
+    for (int c = 0; c < ncase; c++) {
+      int32_t hdr[3];
+      rd(hdr, 4, 3, cf);
+      for (int i = 0; i < N; i++) {
+        atom[k][i].x = rx0[k][i];
+        atom[k][i].y = ry0[k][i];
+        atom[k][i].z = rz0[k][i];
+      }
+      for (int m = 0; m < hdr[2]; m++) {
+        int32_t idx;
+        double d[3];
+        rd(&idx, 4, 1, cf);
+        rd(d, 8, 3, cf);
+        if (idx < 0 || idx >= N) die("case index out of range");
+        atom[k][idx].x += d[0];
+        atom[k][idx].y += d[1];
+        atom[k][idx].z += d[2];
+      }
+      pbc_all(k);
+      nl_flag[k] = 0;
+      nl_check(hdr[0], hdr[1], k);
+      flags[c] = nl_flag[k];
+      for (int i = 0; i < N; i++) {
+        pos[3 * ((size_t)c * N + i)] = atom[k][i].x;
+        pos[3 * ((size_t)c * N + i) + 1] = atom[k][i].y;
+        pos[3 * ((size_t)c * N + i) + 2] = atom[k][i].z;
+      }
+    }
+    fclose(cf);
+    double *p0 = malloc(sizeof(double) * 3 * (size_t)N);
+    for (int i = 0; i < N; i++) {
+      p0[3 * i] = rx0[k][i];
+      p0[3 * i + 1] = ry0[k][i];
+      p0[3 * i + 2] = rz0[k][i];
+    }
+    dump_d("pos0", p0, 3 * (int64_t)N);
+    dump_d("pos_cases", pos, 3 * (int64_t)N * ncase);
+    dump_i("nl_flg", flags, ncase);
+    free(p0);
+    free(pos);
+    free(flags);
+#endif
   } else {
     die("unknown mode");
   }

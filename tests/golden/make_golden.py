@@ -16,6 +16,10 @@ Fixtures:
   water4095.npz  the 4,095-site box at 0.1 sites/A^3 (L = 34.47 A, grid 32^3):
                  per-atom list counts, a SHA-256 of the sorted pair list,
                  forces and energies
+  nlcheck600.npz the DLIST rebuild trigger (nl_check, -DDLIST build) on the
+                 600-site box: list-time positions, the positions of 10
+                 displacement cases after the reference's pbc_all, the site
+                 ranges and the reference's nl_flag for each
 """
 import hashlib
 import os
@@ -76,8 +80,47 @@ def main():
               "e_bonded", "en"):
         out["forces_" + k] = fo[k]
     np.savez_compressed(os.path.join(HERE, "water4095.npz"), **out)
+    make_nlcheck(tmp)
     print("golden fixtures written to", HERE)
 
 
+def nlcheck_cases(s):
+    """Displacement cases around the DLIST threshold (rclist - rc)/4."""
+    rcut = (s.rclist - s.rc) / 4.0
+    n = s.n
+    rng = np.random.default_rng(11)
+    edge = int(np.argmax(s.pos[:, 0]))  # the site nearest +L/2 along x
+    to_edge = s.L[0] / 2 - s.pos[edge, 0]
+    small = [(int(i), *(rng.uniform(-0.35, 0.35, 3) * rcut)) for i in rng.choice(n, 40, False)]
+    return [
+        (0, n, []),
+        (0, n, [(17, 0.98 * rcut, 0.0, 0.0)]),
+        (0, n, [(17, 1.02 * rcut, 0.0, 0.0)]),
+        (0, n, [(33, 0.6 * rcut, 0.6 * rcut, 0.6 * rcut)]),  # each axis below, distance above
+        (0, n, [(edge, to_edge + 0.4 * rcut, 0.0, 0.0)]),      # wraps, moved 0.4 rcut
+        (0, n, [(edge, to_edge + 1.2 * rcut, 0.0, 0.0)]),      # wraps, moved 1.2 rcut
+        (0, n // 2, [(n - 3, 0.0, 2.0 * rcut, 0.0)]),          # outside the range
+        (n // 2, n, [(n - 3, 0.0, 2.0 * rcut, 0.0)]),          # inside the range
+        (0, n, small),
+        (0, n, small + [(5, 0.0, 0.0, -1.1 * rcut)]),
+    ]
+
+
+def make_nlcheck(tmp):
+    s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27))
+    cases = nlcheck_cases(s)
+    r = O.run_reference_nlcheck(s, cases, tmp)
+    np.savez_compressed(os.path.join(HERE, "nlcheck600.npz"), L=s.L, rclist=s.rclist, rc=s.rc,
+                        pos0=r["pos0"].reshape(-1, 3),
+                        pos_cases=r["pos_cases"].reshape(len(cases), -1, 3),
+                        lb=np.array([c[0] for c in cases]), ub=np.array([c[1] for c in cases]),
+                        flags=r["nl_flg"])
+
+
 if __name__ == "__main__":
-    main()
+    if sys.argv[1:] == ["nlcheck"]:  # this fixture alone
+        if not O.build_reference():
+            raise SystemExit("reference sources not available")
+        make_nlcheck(tempfile.mkdtemp(prefix="fe_golden_"))
+    else:
+        main()

@@ -1,5 +1,6 @@
 """The DLIST rebuild trigger (nl_check, nblist.c:607-647) restated in the
-oracle: thresholds, the per-axis image rule and the site range."""
+oracle: thresholds, the per-axis image rule and the site range, pinned to
+the reference's own nl_check on golden cases."""
 import numpy as np
 
 from oracle import oracle as O
@@ -43,3 +44,15 @@ def test_range_limits_the_sites_checked():
     p[15, 1] += 1.0
     assert O.nl_check(p, p0, L, RCLIST, RC, 0, 10) == 0
     assert O.nl_check(p, p0, L, RCLIST, RC, 10, 20) == 1
+
+
+def test_restatement_matches_the_reference_golden_cases():
+    """oracle.nl_check against the reference's own nl_check (nblist.c built
+    with -DDLIST, tests/golden/nlcheck600.npz): below, at and above the
+    threshold, the distance test, boundary crossings, site ranges."""
+    import os
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "nlcheck600.npz"))
+    got = [O.nl_check(d["pos_cases"][c], d["pos0"], d["L"], float(d["rclist"]), float(d["rc"]),
+                      int(d["lb"][c]), int(d["ub"][c])) for c in range(len(d["flags"]))]
+    assert got == [int(f) for f in d["flags"]]
+    assert 0 in got and 1 in got

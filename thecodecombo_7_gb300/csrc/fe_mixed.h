@@ -30,7 +30,6 @@ struct Mixed {
   int *perm = nullptr;            // sorted slot -> original site
   int *iperm = nullptr;           // original site -> sorted slot
   int *cell_s = nullptr;          // cell of each sorted slot at the last rebuild
-  unsigned char *cz_s = nullptr;  // z index of that cell (nc[2] <= 255)
   int *type_s = nullptr;          // site type per sorted slot
   int4 *posfx = nullptr;          // sorted x, y, z as 32-bit fractions of L; w = bits of (float)q
   // outer list (rlist, rebuilt every nlist steps) and inner list (rc + skin,

@@ -38,18 +38,13 @@ namespace fe {
 
 constexpr double kFixScale = 4294967296.0;  // 2^32
 constexpr float kFixScaleF = 4294967296.0f;
-constexpr int kMxWarps = 8;                 // warps per block (list, prune, pair)
+constexpr int kMxWarps = 8;                 // warps per block of the list build
 constexpr int kMxMaxCellAtoms = 2048;       // sites per cell a sort block handles
 
 __device__ __forceinline__ long long to_fix(float v) { return __float2ll_rn(v * kFixScaleF); }
 
 // v in [-g, 2g) wrapped into [0, g) without a division
 __device__ __forceinline__ int wrap1(int v, int g) { return v < 0 ? v + g : (v >= g ? v - g : v); }
-
-__device__ __forceinline__ int wrapg32(int v, int g) {
-  v %= g;
-  return v < 0 ? v + g : v;
-}
 
 // minimum-image separation from 32-bit fractional coordinates
 __device__ __forceinline__ float fx_delta(unsigned a, unsigned b, float scale) {
@@ -91,7 +86,6 @@ __global__ void k_mx_fill(int n, const int *__restrict__ cell_of, const int *__r
 // order each cell's sites by original index (deterministic layout)
 __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ perm,
                               int *__restrict__ iperm, int *__restrict__ cell_s,
-                              unsigned char *__restrict__ cz_s, int ncz,
                               const int *__restrict__ type, int *__restrict__ type_s,
                               int *__restrict__ status) {
   __shared__ int buf[kMxMaxCellAtoms];
@@ -121,13 +115,11 @@ __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ p
       }
       __syncthreads();
     }
-  int cz = c % ncz;
   for (int i = threadIdx.x; i < m; i += blockDim.x) {
     int o = buf[i];
     perm[s0 + i] = o;
     iperm[o] = s0 + i;
     cell_s[s0 + i] = c;
-    cz_s[s0 + i] = (unsigned char)cz;
     type_s[s0 + i] = type[o];
   }
 }
@@ -1246,10 +1238,6 @@ int mixed_setup(Box *b) {
     M.h[d] = b->p.L[d] / M.nc[d];
     M.ncells *= M.nc[d];
   }
-  if (M.nc[2] > 255) {
-    set_error("mixed precision supports at most 255 list cells per axis");
-    return FE_ERR_SIZE;
-  }
   // the minimum image from wrapped 32-bit fractions needs |d| < L/2
   double rl = b->p.rclist;
   for (int d = 0; d < 3; d++)
@@ -1264,7 +1252,6 @@ int mixed_setup(Box *b) {
   FE_CUDA(cudaMalloc(&M.perm, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.iperm, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.cell_s, sizeof(int) * n));
-  FE_CUDA(cudaMalloc(&M.cz_s, n));
   FE_CUDA(cudaMalloc(&M.type_s, sizeof(int) * n));
   FE_CUDA(cudaMalloc(&M.posfx, sizeof(int4) * n));
   // full-list row capacity: a sphere of rlist at the box's density, with margin
@@ -1416,7 +1403,7 @@ void mixed_free(Box *b) {
   if (!b->mx) return;
   Mixed &M = *b->mx;
   void *ptrs[] = {M.cell_count, M.cell_start, M.cell_fill, M.cell_of, M.perm, M.iperm, M.cell_s,
-                  M.cz_s, M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
+                  M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
                   M.ient, M.snap, M.ps, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
                   M.grid32, M.grid32k, M.floor3, M.gfix, M.sm, M.sd, M.mol_first, M.mol_x,
                   M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai};
@@ -1473,8 +1460,8 @@ int launch_mixed_list(Box *b) {
   k_cell_scan_ext(M.cell_count, M.ncells, M.cell_start, M.cell_fill, b->stream);
   k_mx_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.cell_of, M.cell_start, M.cell_fill, M.perm);
   FE_LAUNCH_CHECK("k_mx_fill");
-  k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s, M.cz_s,
-                                                 M.nc[2], b->type, M.type_s, b->status);
+  k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s,
+                                                 b->type, M.type_s, b->status);
   FE_LAUNCH_CHECK("k_mx_cellsort");
   int rc = launch_convert(b);
   if (rc) return rc;
@@ -1482,7 +1469,7 @@ int launch_mixed_list(Box *b) {
   float rl = (float)(b->p.rclist < b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
   int units = (n + kListUnit - 1) / kListUnit;
   int blocks = (units + kMxWarps - 1) / kMxWarps;
-  k_mx_list<<<blocks < 152 * 8 ? blocks : 152 * 8, kMxWarps * 32, 0, b->stream>>>(
+  k_mx_list<<<blocks < M.nsm * 8 ? blocks : M.nsm * 8, kMxWarps * 32, 0, b->stream>>>(
       n, M.posfx, M.perm, M.iperm, M.cell_s, M.type_s, M.cell_start, nc, fix_scale(b), Lf, rl,
       b->nt, M.lj_row, M.lj_on, b->x_start, b->x_partner, M.cap, M.cnt_lj, M.cnt_nl, M.ent,
       b->status);
@@ -1608,7 +1595,7 @@ int launch_mx_spread_only(Box *b) {
   k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, b->order, G, M.posfx,
                                                                      M.sm, M.floor3, M.gfix);
   FE_LAUNCH_CHECK("k_mx_spread_red");
-  k_mx_fix2grid<<<152 * 8, 256, 0, b->stream>>>(b->K, M.gfix, M.grid32);
+  k_mx_fix2grid<<<M.nsm * 8, 256, 0, b->stream>>>(b->K, M.gfix, M.grid32);
   FE_LAUNCH_CHECK("k_mx_fix2grid");
   return FE_OK;
 }
