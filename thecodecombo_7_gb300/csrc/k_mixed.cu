@@ -22,11 +22,17 @@
 //     (measured every step against a snapshot of the positions), so every
 //     pair within rc is always in it -- the forces are those of the outer
 //     list, with ~27 % fewer entries walked;
-//   * excluded / 1-4 pairs (xint) are handled by their own kernel over the
-//     exclusion list (cnonbond_nblist.c:245-263, 416-437 semantics).
-// One warp per i site walks its row with coalesced entry loads; each lane
-// keeps an FP32 partial, converts it to fixed point (2^32 per kJ/mol/A) and
-// the warp adds the integers -- exact and order independent.
+//   * excluded / 1-4 pairs (xint) are handled with the bonded terms, one
+//     thread per molecule when molecules are contiguous runs of sites, else
+//     by kernels over the exclusion list (cnonbond_nblist.c:245-263, 416-437
+//     semantics);
+//   * SPME spreading adds every site's spline contributions to 64-bit
+//     fixed-point grid sums with integer reductions (order independent),
+//     converted once per step to the FP32 grid for cuFFT.
+// In the pair kernel one warp walks a row (rows handed out from a device
+// counter) with coalesced entry loads; the row's FP32 partial sums are added
+// over the warp in a fixed butterfly and converted once to the fixed-point
+// accumulators (2^32 per kJ/mol/A) -- deterministic.
 #include <climits>
 #include <cmath>
 #include <vector>
