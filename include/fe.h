@@ -217,8 +217,11 @@ int fe_mc_kspace_energy(fe_box *box, double *e);
  * the library keeps until the process exits.  Limit: (kmax+1)*(2*kmax+1)^2 <=
  * 8192 candidate k-vectors (kmax <= 12), else FE_ERR_SIZE.  The first call on
  * a device looks up that array's device address, so make the first call on
- * each device before any stream capture.  All calls share the array; calls
- * whose kernels overlap on the GPU race and must be serialised. */
+ * each device before any stream capture (outside a capture every call looks
+ * it up again, so a device reset between calls is fine).  All calls share the
+ * array; calls whose kernels overlap on the GPU race and must be serialised.
+ * xyzq and energy must be device or managed memory: a host pointer is refused
+ * with FE_ERR_ARG before anything is launched. */
 int fe_ewald_kspace_energy_noalloc(const double *xyzq, int n, const double *L, double kappa,
                                    int kmax, int max_k_square, double *energy, void *stream);
 

@@ -18,8 +18,11 @@
 // call writes every slot it later reads, so nothing has to start at zero.
 // Two calls whose kernels overlap on the GPU (different streams, or
 // different host threads on one device) race on the array and must be
-// serialised by the caller.
+// serialised by the caller.  The first call on each device must come before
+// any stream capture (its address lookup may load the module).  Host
+// pointers are refused on the host (FE_ERR_ARG) before anything is launched.
 #include <cmath>
+#include <cstdint>
 #include <mutex>
 
 #include "fe_device.cuh"
@@ -32,7 +35,8 @@ constexpr int kNoAllocMaxDevices = 64;
 
 static __device__ __align__(256) double g_kspace_partial[kNoAllocMaxK];
 
-// host-side addresses of g_kspace_partial, resolved once per device
+// device addresses of g_kspace_partial from the last lookup on each device
+// (used inside stream captures)
 static double *g_partial_addr[kNoAllocMaxDevices];
 static bool g_partial_ready[kNoAllocMaxDevices];
 static std::mutex g_partial_mu;
@@ -101,25 +105,53 @@ __global__ void k_na_sum(const double *__restrict__ partial, int nb, double *__r
   if (threadIdx.x == 0) *out = sh[0];
 }
 
-// Resolves the device address of the scratch array for the current device.
-// Done on the first call on each device; later calls only read the table.
-static int scratch_for_current_device(double **out) {
+// Device address of the scratch array in the current context.  Outside a
+// stream capture it is looked up on every call (a symbol lookup allocates
+// nothing), so a context that the host program reset or replaced since the
+// last call gets the address of its own copy of the array.  Inside a capture
+// the lookup is not made (the first lookup in a context may load the module,
+// which a capture forbids) and the address of the last lookup on this device
+// is used: the first call on each device must come before any capture.
+static int scratch_for_current_device(cudaStream_t s, double **out) {
   int dev = 0;
   FE_CUDA(cudaGetDevice(&dev));
   if (dev < 0 || dev >= kNoAllocMaxDevices) {
     set_error("fe_ewald_kspace_energy_noalloc: device ordinal beyond 63");
     return FE_ERR_SIZE;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  cudaError_t ce = cudaStreamIsCapturing(s, &cap);
+  if (ce != cudaSuccess) {
+    cudaGetLastError();
+    cap = cudaStreamCaptureStatusActive;  // cannot tell: do nothing a capture forbids
+  }
   std::lock_guard<std::mutex> lock(g_partial_mu);
-  if (!g_partial_ready[dev]) {
+  if (cap == cudaStreamCaptureStatusNone) {
     void *ptr = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&ptr, g_kspace_partial);
     if (e != cudaSuccess) return cuda_fail(e, "cudaGetSymbolAddress(g_kspace_partial)");
     g_partial_addr[dev] = static_cast<double *>(ptr);
     g_partial_ready[dev] = true;
+  } else if (!g_partial_ready[dev]) {
+    set_error("fe_ewald_kspace_energy_noalloc: first call on this device inside a stream "
+              "capture (make one call before capturing)");
+    return FE_ERR_STATE;
   }
   *out = g_partial_addr[dev];
   return FE_OK;
+}
+
+// The caller's buffers must be device memory: a host pointer handed to the
+// kernels would fault the GPU, so it is refused here, on the host.
+static bool is_device_buffer(const void *p, size_t align) {
+  if (reinterpret_cast<uintptr_t>(p) % align != 0) return false;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
 }
 
 }  // namespace fe
@@ -129,21 +161,29 @@ using namespace fe;
 extern "C" int fe_ewald_kspace_energy_noalloc(const double *xyzq, int n, const double *L,
                                               double kappa, int kmax, int max_k_square,
                                               double *energy, void *stream) {
-  if (!xyzq || !L || !energy || n < 1 || kmax < 1 || max_k_square < 1 || kappa <= 0.0) {
+  if (!xyzq || !L || !energy || n < 1 || kmax < 1 || max_k_square < 1 || !(kappa > 0.0) ||
+      !(L[0] > 0.0) || !(L[1] > 0.0) || !(L[2] > 0.0)) {
     set_error("fe_ewald_kspace_energy_noalloc: need device xyzq and energy, n >= 1, "
-              "kmax >= 1, max_k_square >= 1, kappa > 0");
+              "kmax >= 1, max_k_square >= 1, kappa > 0, L > 0");
     return FE_ERR_ARG;
   }
-  long nb = (long)(kmax + 1) * (2 * kmax + 1) * (2 * kmax + 1);
+  // (kmax+1)(2kmax+1)^2 <= 8192 holds exactly for kmax <= 12; test kmax first
+  // so that the product below cannot overflow
+  long nb = kmax <= 12 ? ((long)kmax + 1) * (2L * kmax + 1) * (2L * kmax + 1) : kNoAllocMaxK + 1L;
   if (nb > kNoAllocMaxK) {
     set_error("fe_ewald_kspace_energy_noalloc: (kmax+1)*(2*kmax+1)^2 exceeds 8192 "
               "candidate k-vectors (kmax <= 12)");
     return FE_ERR_SIZE;
   }
-  double *partial = nullptr;
-  int rc = scratch_for_current_device(&partial);
-  if (rc) return rc;
+  if (!is_device_buffer(xyzq, alignof(double)) || !is_device_buffer(energy, alignof(double))) {
+    set_error("fe_ewald_kspace_energy_noalloc: xyzq and energy must be 8-byte aligned device "
+              "(or managed) memory");
+    return FE_ERR_ARG;
+  }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  double *partial = nullptr;
+  int rc = scratch_for_current_device(s, &partial);
+  if (rc) return rc;
   double3 Ld = make_double3(L[0], L[1], L[2]);
   k_na_kspace<<<(unsigned)nb, 256, 0, s>>>(xyzq, n, Ld, kappa, kmax, max_k_square, partial);
   FE_LAUNCH_CHECK("k_na_kspace");
