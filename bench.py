@@ -2,10 +2,10 @@
 
 Workload (one step = one production MD step of nve_md.c:359-418): the 3-site
 water recipe scaled to 32,000 molecules (96,000 sites, L = 98.65 A, density
-0.1 sites/A^3), SPME 96^3 order 4, kappa 0.32, rc 10 A, Verlet list 12 A
-rebuilt every 10 steps, NVE velocity Verlet with dt = 0.5 fs, mixed
-precision (FP32 pair/PME math, 64-bit fixed-point force sums, FP64
-integration).  Synthetic seeded input (no dataset is involved).
+0.1 sites/A^3), SPME 96^3 order 4, kappa 0.32, rc 10 A with the LJ switched
+from 8 A, Verlet list 12 A rebuilt every 10 steps, NVE velocity Verlet with
+dt = 0.5 fs, mixed precision (FP32 pair/PME math, 64-bit fixed-point force
+sums, FP64 integration).  Synthetic seeded input (no dataset is involved).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
@@ -18,7 +18,8 @@ Under torchrun each rank runs its own replica (the single-box path does not
 shard: replicas only) and the slowest rank's time is used.
 ``--impl reference`` times the reference's CPU implementation of the path
 (the pinned CPU restatement, built with the reference makefile's flags) on a
-bounded sample of the same workload, on rank 0 only.
+bounded sample of the same workload, on rank 0 only: W + K real MD steps of
+the CPU path (at most 5 + 40), each step timed as it runs.
 """
 from __future__ import annotations
 
@@ -38,11 +39,16 @@ sys.path.insert(0, ROOT)
 
 N_MOL = 32000
 SEED = 2025
+R_SWITCH = 8.0  # LJ switched from 8 A to rc = 10 A in every leg
 METRIC = "atom-steps/s"
 PEAKS_FALLBACK = {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}
 PROFILE = os.path.join(ROOT, "profiles", "k_mx_pair_water96k.md")
 WORKLOAD = ("water 3-site, 96,000 sites (32,000 molecules), L=98.65 A, SPME 96^3 order 4, "
-            "kappa 0.32, rc 10 A, list 12 A every 10 steps, NVE velocity Verlet dt 0.5 fs")
+            "kappa 0.32, rc 10 A, LJ switch 8-10 A (CHARMM), list 12 A every 10 steps, "
+            "NVE velocity Verlet dt 0.5 fs")
+CONFIG = {"workload": WORKLOAD, "cache": "inputs larger than L2 (pair list > 129 MB per step)"}
+EN_TERMS = ("bond", "bend", "nbond", "nbonds", "coulomb", "rewald", "rewalds", "kewald",
+            "sewald", "iewald", "tewald")
 
 
 def load_peaks():
@@ -170,36 +176,141 @@ def cpu_sample(sysm, nsteps_cap: int = 3):
 
 
 def run_reference(args, world, rank):
+    """The CPU path of the reference on the same workload: W warm-up and K
+    timed MD steps (list every 10 steps, as the workload) of the CPU
+    restatement built with the reference makefile's flags, one thread (the
+    reference is single-threaded).  At most 5 + 40 steps are run; the line
+    says how many were timed.  The box is placed with numpy only: no
+    compiled code of the engine is loaded."""
     if rank != 0:
         return
+    from oracle import oracle as orc
     from thecodecombo_7_gb300 import systems
-    sysm = systems.water_box(N_MOL, density=0.1, seed=SEED)
-    base = cpu_sample(sysm)
-    # --warmup/--steps map to bounded samples of the same workload
+    sysm = systems.water_box(N_MOL, density=0.1, seed=SEED, r_switch=R_SWITCH, helper=False)
+    W = min(args.warmup, 5)
+    K = min(args.steps, 40)
+    o = orc.Oracle(sysm, fast=True)
+    md = o.run_md(W + K, timed=True)
+    ts = md["tstamp"]
+    sec = float(ts[W + K] - ts[W])
+    value = sysm.n * K / sec
+    sample = (f"{K} timed MD steps after {W} warm-up steps ({sec:.1f} s; list rebuilt "
+              f"(O(N^2)) at every 10th step as in the workload), 96,000 sites, single thread, "
+              "CPU restatement built with the reference makefile's flags")
     line = {
-        "impl": "reference", "metric": METRIC, "value": base["value"], "unit": METRIC,
-        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": 1000.0 * sysm.n / base["value"], "higher_is_better": True,
+        "impl": "reference", "metric": METRIC, "value": value, "unit": METRIC,
+        "n_gpus": args.gpus, "steps": K, "warmup": W,
+        "ms_per_step": 1000.0 * sec / K, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": "fp64 CPU (reference arithmetic)",
-                   "parallelism": "1 replica, 1 thread"},
-        "cpu_baseline": {k: base[k] for k in ("value", "unit", "cores", "kind", "sample")},
-        "e2e": {"value": base["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+        "config": dict(CONFIG, parallelism=f"replicas x{world}"),
+        "precision": "fp64 CPU (reference arithmetic)",
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
+    if K != args.steps or W != args.warmup:
+        line["steps_requested"] = args.steps
+        line["warmup_requested"] = args.warmup
     print(json.dumps(line))
 
 
-def nve_drift(rec, sysm):
-    """Linear drift of the total energy (kinetic + shifted potential) over a
-    run, in kT per ns per degree of freedom (kJ/mol, kT = RG T / 1000)."""
+def nve_drift(rec, sysm, dt=None):
+    """Linear drift of the total energy (kinetic + bond + bend + shifted
+    non-bonded) over an NVE run, in kT per ns per degree of freedom
+    (kJ/mol, kT = RG T / 1000), with the fit's standard error and the rms
+    fluctuation about the line (kJ/mol)."""
+    dt = sysm.dt if dt is None else dt
     tot = rec[:, 0] + rec[:, 1] + rec[:, 2] + rec[:, 4]  # kinet + bond + bend + nbonds
-    t_ps = np.arange(len(tot)) * sysm.dt
-    slope = float(np.polyfit(t_ps, tot, 1)[0]) if len(tot) > 2 else 0.0  # kJ/mol/ps
+    t_ps = np.arange(len(tot)) * dt
     kT = 1.380662e-23 * 6.022045e23 * sysm.T * 1e-3
     nfree = 3 * sysm.n - 3
-    return {"kT_per_ns_per_dof": slope * 1000.0 / (kT * nfree), "steps": int(len(tot)),
-            "span_ps": float(t_ps[-1]) if len(tot) else 0.0}
+    if len(tot) < 3:
+        return {"kT_per_ns_per_dof": 0.0, "steps": int(len(tot))}
+    A = np.vstack([t_ps, np.ones_like(t_ps)]).T
+    coef, res, _, _ = np.linalg.lstsq(A, tot, rcond=None)
+    resid = tot - A @ coef
+    # standard error of the slope from the means of 0.25 ps blocks (the
+    # fluctuations are correlated over many steps; block means much less)
+    nb = max(int(t_ps[-1] // 0.25), 3)
+    blk = [b for b in np.array_split(np.arange(len(tot)), nb) if len(b)]
+    tm = np.array([t_ps[b].mean() for b in blk])
+    em = np.array([tot[b].mean() for b in blk])
+    cb = np.polyfit(tm, em, 1)
+    rb = em - np.polyval(cb, tm)
+    se = float(np.sqrt((rb ** 2).sum() / max(len(tm) - 2, 1) / ((tm - tm.mean()) ** 2).sum()))
+    scale = 1000.0 / (kT * nfree)
+    return {"kT_per_ns_per_dof": float(coef[0]) * scale,
+            "stderr_kT_per_ns_per_dof": se * scale,
+            "fluct_rms_kJ_mol": float(np.sqrt(np.mean(resid ** 2))),
+            "steps": int(len(tot)), "span_ps": float(t_ps[-1]), "dt_fs": dt * 1e3}
+
+
+def drift_study(local, n_mol, equil_steps, nve_steps, fp64=True, seed=SEED + 9):
+    """NVE energy drift on an equilibrated box: Nose-Hoover (M=3) at 300 K for
+    equil_steps from the random start (mixed precision), then from that state
+    NVE for nve_steps at dt = 0.5 fs and 2 * nve_steps at dt/2, in mixed
+    precision and (fp64=True) in the FP64 drop-in.  Drift from the
+    integrator scales as dt^2; drift from the force field's cutoffs does not."""
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(n_mol, density=0.1, seed=seed, r_switch=R_SWITCH)
+    out = {"sites": s.n, "equilibration": f"{equil_steps} NHC steps at 300 K (mixed)"}
+    with engine.Box(s, precision=engine.FE_PREC_MIXED, device=local) as b:
+        b.nblist()
+        b.forces()
+        b.kinet()
+        rec = b.run_md(equil_steps, first_step=1, use_nhc=True, record=True)
+        out["T_end_K"] = float(2.0 * rec[-1, 0] / ((3 * s.n - 3) * 8.31441e-3))
+        pos, nop = b.get_positions(), b.get_positions_nopbc()
+        vel, _ = b.get_velocities()
+    precs = [("mixed", engine.FE_PREC_MIXED)] + ([("fp64", engine.FE_PREC_FP64)] if fp64 else [])
+    for name, prec in precs:
+        for div in (1, 2):
+            sd = s.copy()
+            sd.dt = s.dt / div
+            with engine.Box(sd, precision=prec, device=local) as b:
+                b.set_positions(pos)
+                b.set_positions_nopbc_array(nop)
+                b.set_velocities(vel)
+                b.nblist()
+                b.forces()
+                b.kinet()
+                rec = b.run_md(nve_steps * div, first_step=1, record=True)
+            out[f"{name}_dt{'' if div == 1 else '/2'}"] = nve_drift(rec, sd, sd.dt)
+    return out
+
+
+def config0_sample(local):
+    """The plain FP64 drop-in on the 4,095-site box (1,365 molecules, L 34.47 A,
+    SPME 32^3, LJ switch 8-10 A, list every 10 steps, dt 0.5 fs): 1,000 NVE
+    steps timed with CUDA events; CPU: 10 real steps of the CPU restatement
+    (reference makefile flags, one thread) on the same box."""
+    import torch
+
+    from oracle import oracle as orc
+    from thecodecombo_7_gb300 import engine, systems
+    s = systems.water_box(1365, density=0.1, seed=SEED + 1, r_switch=R_SWITCH)
+    stream = torch.cuda.Stream(device=local)
+    with engine.Box(s, precision=engine.FE_PREC_FP64, device=local) as b:
+        b.set_stream(stream.cuda_stream)
+        b.nblist()
+        b.forces()
+        b.kinet()
+        b.run_md(10, first_step=1, record=False)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run_md(1000, first_step=11, record=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        sec = e0.elapsed_time(e1) / 1000.0
+    md = orc.Oracle(s, fast=True).run_md(10, timed=True)
+    cpu_sec = float(md["tstamp"][10] - md["tstamp"][0])
+    return {"value": s.n * 1000 / sec, "unit": METRIC, "sites": s.n, "steps": 1000,
+            "ns_per_day": 1000 / sec * 0.0005e-3 * 86400.0, "ms_per_step": 1000.0 * sec / 1000,
+            "cpu_port_1_thread": s.n * 10 / cpu_sec,
+            "workload": "4,095 sites (1,365 molecules), L 34.47 A, SPME 32^3 order 4, rc 10 A, "
+                        "LJ switch 8-10 A, list 12 A every 10 steps, NVE dt 0.5 fs, FP64 drop-in"}
 
 
 def batched_sample(local, steps):
@@ -214,7 +325,8 @@ def batched_sample(local, steps):
     rng = np.random.default_rng(SEED + 4)
     nmol = rng.integers(2000, 12001, R)
     temps = np.linspace(300.0, 400.0, R)
-    ss = [systems.water_box(int(m), density=0.1, seed=SEED + 100 + k, T=float(temps[k]))
+    ss = [systems.water_box(int(m), density=0.1, seed=SEED + 100 + k, T=float(temps[k]),
+                            r_switch=R_SWITCH)
           for k, m in enumerate(nmol)]
     boxes = [engine.Box(s, precision=engine.FE_PREC_MIXED, device=local) for s in ss]
     try:
@@ -247,7 +359,8 @@ def batched_sample(local, steps):
     return {"value": n_atoms * steps / (ms / 1000.0), "unit": METRIC, "replicas": R,
             "sites": n_atoms, "steps": steps, "ms_per_step": ms / steps,
             "workload": "32 NHC (M=3) replicas, 2,000-12,000 molecules each, own L at 0.1 "
-                        "sites/A^3, grid ~1 point/A, T 300-400 K, exchange every 500 steps",
+                        "sites/A^3, grid ~1 point/A, LJ switch 8-10 A, T 300-400 K, exchange "
+                        "every 500 steps",
             "exchange_attempts": int(state["attempts"]),
             "exchanges_in_timed_steps": n_ex, "list_steps": n_list,
             "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]},
@@ -303,14 +416,14 @@ def mc_sample(local):
     import torch
 
     from thecodecombo_7_gb300 import engine, systems
-    s = systems.water_box(1365, density=0.1, seed=SEED + 3)
+    s = systems.water_box(1365, density=0.1, seed=SEED + 3, r_switch=R_SWITCH)
     box = engine.Box(s, precision=engine.FE_PREC_FP64, device=local)
     stream = torch.cuda.Stream(device=local)
     box.set_stream(stream.cuda_stream)
     net = engine.Mlp(device=local, seed=SEED)
     out = {"workload": "4,095 sites (1,365 rigid 3-site molecules, L 34.47 A), translation "
                        "<= 0.3 A / rotation <= 15 deg, Ewald kappa 0.32, |n|^2 <= 49 "
-                       "(783 k-vectors), rc 10 A, 300 K"}
+                       "(783 k-vectors), rc 10 A, LJ switch 8-10 A, 300 K"}
     try:
         # training set: 2x10^5 exact moves (152 chains x 1,316)
         box.mc_chains_setup(nchains=152, kmax=7, T=300.0, seed=SEED)
@@ -357,9 +470,34 @@ def mc_sample(local):
         out["da_over_exact_accepted_per_s"] = (
             out["delayed_acceptance_1_chain"]["accepted_moves_per_s"] /
             out["exact_1_chain"]["accepted_moves_per_s"])
+        # the reference's exact dE recomputes the whole structure factor twice
+        # per move (ewald_mc.c:109-156 via forces_mc); its CPU restatement,
+        # one thread, reference makefile flags, on 40 translation moves
+        from oracle import oracle as orc
+        o = orc.Oracle(s, fast=True)
+        rng = np.random.default_rng(SEED)
+        t0 = time.perf_counter()
+        for _ in range(40):
+            m = int(rng.integers(0, 1365))
+            pn = s.pos.copy()
+            pn[3 * m:3 * m + 3] += (rng.uniform(size=3) - 0.5) * 0.6
+            o.mc_delta_energy(s.pos, pn, 3 * m, 3 * m + 3, kmax=7, max_k_square=49)
+        out["cpu_port_full_recompute_moves_per_s_1_thread"] = 40 / (time.perf_counter() - t0)
     finally:
         net.close()
         box.close()
+    return out
+
+
+def energy_errors(en_mixed, en_fp64):
+    """Per-term relative error of the mixed-precision energies against the
+    FP64 drop-in on the same coordinates (equal to the FP64 oracle to 1e-12
+    in the parity tests); terms that vanish (bond, bend at a rigid start) get
+    their absolute error instead."""
+    out = {}
+    for k in EN_TERMS:
+        a, b = en_fp64[k], en_mixed[k]
+        out[k] = (b - a) / abs(a) if abs(a) > 1e-6 else {"abs": b - a}
     return out
 
 
@@ -372,13 +510,13 @@ def run_ours(args, world, rank, local):
     if not os.path.exists(engine.LIB_PATH):
         fe_build.build()
     torch.cuda.set_device(local)
-    sysm = systems.water_box(N_MOL, density=0.1, seed=SEED + rank)
+    sysm = systems.water_box(N_MOL, density=0.1, seed=SEED + rank, r_switch=R_SWITCH)
     n = sysm.n
     stream = torch.cuda.Stream(device=local)
     box = engine.Box(sysm, precision=engine.FE_PREC_MIXED, device=local)
     box.set_stream(stream.cuda_stream)
     box.nblist()
-    box.forces()
+    en_mixed0 = box.forces()
     box.kinet()
     f_mixed0 = box.get_forces()
     tune = box.autotune()  # launch shape of the pair kernel for this box (untimed)
@@ -417,21 +555,27 @@ def run_ours(args, world, rank, local):
     achieved = alg_bytes / (pair_us * 1e-6) / 1e9
     peak = float(peaks["hbm_gbs"])
     traffic = profile_traffic()
+    pipe = {"fp32_tflops": engine.pipe_peak(0, local), "fp64_tflops": engine.pipe_peak(1, local),
+            "mufu_tera_ops": engine.pipe_peak(2, local),
+            "how": "fe_pipe_peak: FMA / ex2.approx chains, 8 per thread, 8 blocks of 256 per "
+                   "SM, best of 3 (CUDA events)"}
     # plain FP64 drop-in on the same workload (the 10x denominator), a few steps
     fp64 = None
     force_err = None
+    en_err = None
+    counts = None
     b64 = None
     if rank == 0:
         b64 = engine.Box(sysm, precision=engine.FE_PREC_FP64, device=local)
         b64.set_stream(stream.cuda_stream)
         b64.nblist()
-        b64.forces()
+        en64 = b64.forces()
         f64 = b64.get_forces()
+        counts = b64.pair_counts()
         d = f_mixed0 - f64
         force_err = {"rms_rel": float(np.sqrt((d ** 2).sum() / (f64 ** 2).sum())),
-                     "max_abs": float(np.abs(d).max()), "unit_max": "kJ/mol/A",
-                     "against": "FP64 drop-in on the same state (equal to the FP64 oracle "
-                                "to 1e-12 in the parity tests)", "step": 0}
+                     "max_abs": float(np.abs(d).max())}
+        en_err = energy_errors(en_mixed0, en64)
         b64.kinet()
         b64.run_md(3, first_step=1)
         e0 = torch.cuda.Event(enable_timing=True)
@@ -482,29 +626,28 @@ def run_ours(args, world, rank, local):
     h2d = 4 * 24 * n
     d2h = 5 * 24 * n + 8 * engine.FE_EN_COUNT
     # accuracy along one continuous trajectory: mixed-precision forces against
-    # the FP64 engine on the same coordinates at steps 0, 1,000 and 10,000;
-    # energy drift over steps 1,000..10,000
+    # the FP64 engine on the same coordinates at steps 0, 1,000 and 10,000
     accuracy = None
     if b64 is not None:
         def fp64_error():
             b64.set_positions(box.get_positions())
             b64.nblist()
-            b64.forces()
+            e64 = b64.forces()
             f64 = b64.get_forces()
+            em = box.forces()
             d = box.get_forces() - f64
             return {"rms_rel": float(np.sqrt((d ** 2).sum() / (f64 ** 2).sum())),
-                    "max_abs": float(np.abs(d).max())}
+                    "max_abs": float(np.abs(d).max())}, energy_errors(em, e64)
         done = W + K + ke
         if done < 1000:
             box.run_md(1000 - done, nlist_freq=nl, first_step=done + 1, record=False)
-        err1k = fp64_error()
-        rec_long = box.run_md(9000, nlist_freq=nl, first_step=1001, record=True)
-        err10k = fp64_error()
-        accuracy = {"force_error_vs_fp64": {"step_0": {k: force_err[k] for k in
-                                                        ("rms_rel", "max_abs")},
-                                            "step_1000": err1k, "step_10000": err10k,
-                                            "unit_max_abs": "kJ/mol/A"},
-                    "nve_drift": nve_drift(rec_long, sysm)}
+        err1k, en1k = fp64_error()
+        box.run_md(9000, nlist_freq=nl, first_step=1001, record=False)
+        err10k, en10k = fp64_error()
+        accuracy = {"force_error_vs_fp64": {"step_0": force_err, "step_1000": err1k,
+                                            "step_10000": err10k, "unit_max_abs": "kJ/mol/A"},
+                    "energy_rel_error_vs_fp64": {"step_0": en_err, "step_1000": en1k,
+                                                 "step_10000": en10k}}
         b64.close()
     box.close()
     if rank != 0:
@@ -518,32 +661,44 @@ def run_ours(args, world, rank, local):
             cpu = {"value": None, "unit": METRIC, "cores": 1, "kind": "port",
                    "sample": f"failed: {exc}"}
     steps_per_s = K / (ms_max / 1000.0)
-    try:
-        batched = batched_sample(local, steps=min(max(K, 100), 500))
-    except Exception as exc:  # the headline line must still print
-        batched = {"failed": str(exc)}
-    try:
-        mc = mc_sample(local)
-    except Exception as exc:
-        mc = {"failed": str(exc)}
-    try:
-        go = go_sample(local)
-    except Exception as exc:
-        go = {"failed": str(exc)}
+    extras = {}
+    for name, fn in (("batched_replicas", lambda: batched_sample(local, min(max(K, 100), 500))),
+                     ("mc", lambda: mc_sample(local)), ("go_replicas", lambda: go_sample(local)),
+                     ("config0_fp64", lambda: config0_sample(local)),
+                     ("nve_drift_4095", lambda: drift_study(local, 1365, 20000, 10000)),
+                     ("nve_drift_96000", lambda: drift_study(local, N_MOL, 10000, 10000,
+                                                             fp64=False))):
+        try:
+            extras[name] = fn()
+        except Exception as exc:  # the headline line must still print
+            extras[name] = {"failed": str(exc)}
+    # the pair loop's algorithmic FLOPs per step (half-list units, counted
+    # from the reference loop): 11 per list entry, +30 per pair inside rc,
+    # +17 per LJ pair, +12 per excluded pair inside rc
+    L_pairs, P_rc, P_lj, P_x = counts if counts else (0, 0, 0, 0)
+    flops = 11.0 * L_pairs + 30.0 * P_rc + 17.0 * P_lj + 12.0 * P_x
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": K,
         "warmup": W, "ms_per_step": ms_max / K, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "fp32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "precision": "mixed (FP32 pair/PME math, int64 "
-                   "fixed-point force sums, FP64 integration and energy sums)",
-                   "parallelism": f"replicas x{world}",
-                   "cache": f"inputs larger than L2 (pair list ~{4e-6 * entries:.0f} MB read "
-                            "per step)",
-                   "ns_per_day": steps_per_s * 0.0005e-3 * 86400.0},
+        "vs_baseline": (value / world) / fp64 if fp64 else None,
+        "vs_baseline_basis": "mixed-precision engine / plain FP64 drop-in on the same box and "
+                             "the same GPU, this run (the metric's denominator)",
+        "dtype": "fp32", "data": "synthetic",
+        "config": dict(CONFIG, parallelism=f"replicas x{world}"),
+        "precision": "mixed (FP32 pair/PME math, int64 fixed-point force sums, FP64 "
+                     "integration and energy sums)",
+        "ns_per_day": steps_per_s * 0.0005e-3 * 86400.0,
         "roofline": {"kernel": "k_mx_pair", "bound": "hbm", "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind, "algorithmic_bytes": alg_bytes,
                      "us_per_launch": pair_us, "list_entries": entries, "max_row": max_row,
+                     "fp32_pipe": {"algorithmic_gflop_per_launch": flops * 1e-9,
+                                   "achieved_tflops": flops / (pair_us * 1e-6) * 1e-12,
+                                   "peak_tflops": pipe["fp32_tflops"],
+                                   "frac": flops / (pair_us * 1e-6) * 1e-12 / pipe["fp32_tflops"],
+                                   "half_list_counts": {"entries": L_pairs, "pairs_in_rc": P_rc,
+                                                        "lj_pairs_in_rc": P_lj,
+                                                        "excluded_in_rc": P_x}},
                      "list": f"inner list (rc + 0.8 A, {entries} entries) between prunes; "
                              f"outer list (rlist, {outer_entries} entries) read by the "
                              f"{prunes1 - prunes0} pruning launches of the {K} timed steps",
@@ -555,13 +710,13 @@ def run_ours(args, world, rank, local):
                 "d2h_bytes_per_step": d2h, "steps": ke},
         "gpu_launches": launches,
         "clocks": clk,
-        "fp64_drop_in": {"value": fp64, "unit": METRIC,
-                         "ratio": (value / world) / fp64 if fp64 else None},
-        "accuracy": accuracy,
-        "batched_replicas": batched,
-        "mc": mc,
-        "go_replicas": go,
+        "pipe_peaks": pipe,
     }
+    line.update(extras)
+    # last, so that a truncated tail of the line still carries them
+    line["accuracy"] = accuracy
+    line["fp64_drop_in"] = {"value": fp64, "unit": METRIC,
+                            "ratio": (value / world) / fp64 if fp64 else None}
     print(json.dumps(line))
 
 

@@ -407,12 +407,20 @@ enum { FE_KERNEL_PAIR = 0, FE_KERNEL_SPREAD = 1, FE_KERNEL_LIST = 2 };
  * between CUDA events on the box's stream; *us = mean device time per launch.
  * Scratch sums are overwritten; call fe_forces again before reading forces. */
 int fe_time_kernel(fe_box *box, int which, int reps, double *us);
+/* Measured arithmetic peak of a device, the denominator of pipe fractions:
+ * which = 0 FP32 FMA, 1 FP64 FMA (TFLOP/s, an FMA counted as two), 2 the
+ * special-function unit's ex2.approx (Tera-ops/s). */
+int fe_pipe_peak(int device, int which, double *tera_per_s);
 /* Number of this library's own kernel launches in one fe_run_md step without
  * and with a list rebuild (cuFFT's kernels not included). */
 int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list);
 /* Entries of the current pair list (half list in FP64 mode, full list in
  * mixed mode) and the longest row. */
 int fe_list_stats(fe_box *box, int64_t *entries, int *max_row);
+/* FP64 boxes: {half-list entries, pairs within rc that the pair loop
+ * evaluates, those with an LJ term, excluded pairs within rc} of the current
+ * list -- the units of the pair loop's algorithmic FLOP count. */
+int fe_pair_counts(fe_box *box, int64_t *counts4);
 /* nl_check(lb, ub, k), nblist.c:607-647 (DLIST): *nl_flag = 1 if any site
  * of [lb, ub) has moved more than (rclist - rc)/4 since the last fe_nblist
  * (along one axis or in distance, with the reference's image rule), else 0.

@@ -17,6 +17,7 @@
 #include <math.h>
 #include <stdlib.h>
 #include <string.h>
+#include <time.h>
 
 #include "fe_fft.h"
 
@@ -800,9 +801,24 @@ static void en_rec(const or_energy *e, double kin, double *r) {
   r[8] = e->kewald; r[9] = e->sewald; r[10] = e->iewald; r[11] = e->tewald;
 }
 
+static double now_s(void) {
+  struct timespec ts;
+  clock_gettime(CLOCK_MONOTONIC, &ts);
+  return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
 int or_run_md(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
               int nhc_M, double nhc_Q, double *pos, double *pos_nopbc,
               double *vv, double *ff, double *zeta, double *rec) {
+  return or_run_md_timed(s, nsteps, nlist_freq, use_nhc, nhc_M, nhc_Q, pos, pos_nopbc, vv, ff,
+                         zeta, rec, NULL);
+}
+
+/* or_run_md with tstamp[i] = monotonic time (s) at the end of step i
+ * (tstamp[0]: after the initial list and forces); tstamp may be NULL */
+int or_run_md_timed(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
+                    int nhc_M, double nhc_Q, double *pos, double *pos_nopbc,
+                    double *vv, double *ff, double *zeta, double *rec, double *tstamp) {
   int n = s->n;
   int64_t cap = (int64_t)n * 2000 + 16;
   if (cap > (int64_t)n * n / 2 + 16) cap = (int64_t)n * n / 2 + 16;
@@ -818,6 +834,7 @@ int or_run_md(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
   if (or_nblist(s, pos, cnt, idx, flag, cap, NULL, NULL, NULL, 0) < 0) goto fail;
   or_forces(s, pos, cnt, idx, flag, sewald, ff, &en);
   en_rec(&en, or_kinet(s, vv, uu, NULL), rec);
+  if (tstamp) tstamp[0] = now_s();
   for (int i = 1; i <= nsteps; i++) {
     if (i % nlist_freq == 0)
       if (or_nblist(s, pos, cnt, idx, flag, cap, NULL, NULL, NULL, 0) < 0) goto fail;
@@ -826,6 +843,7 @@ int or_run_md(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
                          sewald, &en);
     if (use_nhc) or_integrate_nhc(s, s->dt, nhc_M, nhc_Q, nfree, zeta, vv, uu);
     en_rec(&en, or_kinet(s, vv, uu, NULL), rec + 12 * i);
+    if (tstamp) tstamp[i] = now_s();
   }
   free(cnt); free(idx); free(flag); free(uu);
   return 0;
@@ -970,7 +988,8 @@ double or_ewald_kspace_energy(const or_system *s, const double *pos, int kmax,
 }
 
 /* one pair's MC energy terms (enbnd_mc.c / ewald_mc.c:390-606 restated with
- * the reference's minimum image of cnonbond_nblist.c:167-172) */
+ * the reference's minimum image of cnonbond_nblist.c:167-172); with
+ * r_switch > 0 the LJ term is switched as in or_cnonbond_pairs (no shift) */
 static void mc_pair(const or_system *s, const xtab *t, int a, int b,
                     const double *pa, const double *pb, double rc_ew,
                     double e4[4]) {
@@ -995,10 +1014,20 @@ static void mc_pair(const or_system *s, const xtab *t, int a, int b,
       double sr2 = (sig * sig) / dr2;
       double sr6 = sr2 * sr2 * sr2;
       double sr12 = sr6 * sr6;
-      double sr2s = (sig * sig) / rc2;
-      double sr6s = sr2s * sr2s * sr2s;
-      double sr12s = sr6s * sr6s;
-      e4[0] += eps * (sr12 - 2.0 * sr6) - eps * (sr12s - 2.0 * sr6s);
+      if (s->r_switch > 0.0) {
+        /* the CHARMM switch of or_cnonbond_pairs instead of the shift */
+        double ron2 = s->r_switch * s->r_switch, elj = eps * (sr12 - 2.0 * sr6);
+        if (dr2 > ron2) {
+          double c = rc2 - dr2, den = (rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2);
+          elj *= c * c * (rc2 + 2.0 * dr2 - 3.0 * ron2) / den;
+        }
+        e4[0] += elj;
+      } else {
+        double sr2s = (sig * sig) / rc2;
+        double sr6s = sr2s * sr2s * sr2s;
+        double sr12s = sr6s * sr6s;
+        e4[0] += eps * (sr12 - 2.0 * sr6) - eps * (sr12s - 2.0 * sr6s);
+      }
     }
   }
   double rce2 = rc_ew * rc_ew;

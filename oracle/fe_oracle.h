@@ -133,6 +133,11 @@ void or_integrate_nhc(const or_system *s, double time_step, int M, double Q,
 int or_run_md(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
               int nhc_M, double nhc_Q, double *pos, double *pos_nopbc,
               double *vv, double *ff, double *zeta, double *rec);
+/* or_run_md with tstamp[i] = CLOCK_MONOTONIC seconds at the end of step i
+ * (tstamp[0] after the initial list and forces); for timing the CPU path. */
+int or_run_md_timed(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
+                    int nhc_M, double nhc_Q, double *pos, double *pos_nopbc,
+                    double *vv, double *ff, double *zeta, double *rec, double *tstamp);
 
 /* ---- classic-Ewald MC energy path (ewald.c:46-118, ewald_mc.c) ---- */
 

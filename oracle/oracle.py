@@ -234,9 +234,11 @@ class Oracle:
         return vv, uu, zeta
 
     def run_md(self, nsteps, use_nhc=False, pos=None, vel=None, zeta=None, pos_nopbc=None,
-               T=None):
+               T=None, timed=False):
         """or_run_md from the given state; zeta / pos_nopbc / T (the
-        thermostat temperature, sim.T[k]) default to a fresh start."""
+        thermostat temperature, sim.T[k]) default to a fresh start.  With
+        timed=True the result also holds ``tstamp`` (monotonic seconds at the
+        end of each step, index 0 after the initial list and forces)."""
         s = self.sysm
         pos = np.ascontiguousarray(s.pos if pos is None else pos, np.float64).copy()
         nop = pos.copy() if pos_nopbc is None else np.ascontiguousarray(pos_nopbc,
@@ -253,13 +255,17 @@ class Oracle:
         else:
             zeta = np.ascontiguousarray(zeta, np.float64).reshape(-1).copy()
         rec = np.zeros((nsteps + 1, 12))
-        rc = self.lib.or_run_md(self.sp, nsteps, s.nlist_freq, int(use_nhc), M,
-                                C.c_double(s.nhc_Q), _p(pos), _p(nop), _p(vv), _p(ff),
-                                _p(zeta), _p(rec))
+        ts = np.zeros(nsteps + 1)
+        rc = self.lib.or_run_md_timed(self.sp, nsteps, s.nlist_freq, int(use_nhc), M,
+                                      C.c_double(s.nhc_Q), _p(pos), _p(nop), _p(vv), _p(ff),
+                                      _p(zeta), _p(rec), _p(ts) if timed else None)
         self.s.T = s.T
         if rc != 0:
             raise RuntimeError("oracle md failed (list overflow)")
-        return dict(en=rec, pos=pos, pos_nopbc=nop, vel=vv, force=ff, zeta=zeta.reshape(-1, 3))
+        out = dict(en=rec, pos=pos, pos_nopbc=nop, vel=vv, force=ff, zeta=zeta.reshape(-1, 3))
+        if timed:
+            out["tstamp"] = ts
+        return out
 
     # ---- MC ----
     def ewald_kspace_energy(self, pos, kmax=7, max_k_square=49):

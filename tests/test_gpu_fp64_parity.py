@@ -212,3 +212,41 @@ def test_mc_delta_matches_oracle():
                 pos = pn
         ek = b.mc_kspace_energy()
         assert abs(ek - orc.ewald_kspace_energy(pos, 5, 25)) <= 1e-9 * abs(ek)
+
+
+def test_fp64_switch_matches_oracle():
+    """The FP64 pair kernel with the LJ switch (8 -> 10 A) against the
+    oracle's switched pair term (itself checked by finite differences and
+    continuity in tests/test_switch_cpu.py)."""
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(1365, density=0.1, seed=9, r_switch=8.0)
+    o = O.Oracle(s)
+    f_ref, en_ref = o.forces(s.pos)
+    with _box(s) as b:
+        b.nblist()
+        en = b.forces()
+        f = b.get_forces()
+    _close_f(f, f_ref)
+    for k in ("nbond", "nbonds", "rewald", "kewald", "iewald", "tewald"):
+        _close_e(en[k], en_ref[k], k)
+    assert en["nbonds"] == en["nbond"]  # no shift term under the switch
+
+
+def test_mc_delta_with_switch_matches_oracle():
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(300, L=26.0, seed=6, grid=(24, 24, 24), r_switch=8.0)
+    orc = O.Oracle(s)
+    rng = np.random.default_rng(12)
+    with _box(s) as b:
+        b.mc_setup(kmax=5)
+        for trial in range(6):
+            m = int(rng.integers(0, 300))
+            lb, ub = 3 * m, 3 * m + 3
+            new = s.pos[lb:ub] + rng.uniform(-0.3, 0.3, size=3)
+            new -= s.L * np.floor(new / s.L + 0.5)
+            de, parts = b.mc_delta(lb, ub, new)
+            pn = s.pos.copy()
+            pn[lb:ub] = new
+            want, wparts = orc.mc_delta_energy(s.pos, pn, lb, ub, kmax=5, max_k_square=25)
+            assert abs(de - want) <= 1e-8 * max(1.0, abs(want)), (de, want)
+            np.testing.assert_allclose(parts, wparts, rtol=1e-8, atol=1e-8)

@@ -41,6 +41,7 @@ UNITS = {
     "k_mcrun.cu": [],
     "k_mlp.cu": [],
     "k_go.cu": [],
+    "k_peaks.cu": [],
 }
 
 

@@ -792,6 +792,20 @@ int fe_step_launches(fe_box *box, int use_nhc, int *plain, int *with_list) {
   return FE_OK;
 }
 
+int fe_pair_counts(fe_box *box, int64_t *counts4) {
+  if (!box || !counts4) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (b->mx || !b->have_list) {
+    set_error("fe_pair_counts needs an FP64 box with a list");
+    return FE_ERR_STATE;
+  }
+  long long c[4];
+  int rc = pair_counts64(b, c);
+  if (rc) return rc;
+  for (int t = 0; t < 4; t++) counts4[t] = c[t];
+  return FE_OK;
+}
+
 int fe_list_stats(fe_box *box, int64_t *entries, int *max_row) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;

@@ -189,6 +189,7 @@ int launch_nblist(Box *b);
 int launch_nl_check(Box *b, int lb, int ub, int *dflag);  // nblist.c:607-647
 // k_pair64.cu
 int launch_pair64(Box *b);
+int pair_counts64(Box *b, long long *out4);  // instrumentation: half-list counts
 int launch_bonded64(Box *b);
 // k_spme.cu
 int spme_setup(Box *b);

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <cufft.h>
 
+#include "fe_df.cuh"
+
 namespace fe {
 
 struct Box;
@@ -71,6 +73,9 @@ struct Mixed {
   int *mol_x = nullptr, *mol_xi = nullptr;     // CSR: exclusion indices per molecule
   int *mol_b = nullptr, *mol_bi = nullptr;     // bond indices
   int *mol_a = nullptr, *mol_ai = nullptr;     // bend indices
+  // double-float intramolecular correction energy: exp(k/64) table, constants
+  float2 *exptab = nullptr;
+  DfIntra dfi{};
 };
 
 

@@ -78,6 +78,7 @@ __global__ void k_mc_recip(int nk, int lb, int m, double3 tp, const double4 *__r
 struct McPair {
   double3 L, H;
   double rc2, rce2, kappa, fconv, lj_shift_rc2;
+  double ron2, sw_den;  // LJ switch (ron2 = 0: the reference's shift)
   int n, nt, lb, ub;
 };
 
@@ -115,10 +116,19 @@ __device__ __forceinline__ void mc_pair_energy(const McPair &P, double3 pa, doub
       double sr2 = (sig * sig) / dr2;
       double sr6 = sr2 * sr2 * sr2;
       double sr12 = sr6 * sr6;
-      double sr2s = (sig * sig) / P.rc2;
-      double sr6s = sr2s * sr2s * sr2s;
-      double sr12s = sr6s * sr6s;
-      elj += eps * (sr12 - 2.0 * sr6) - eps * (sr12s - 2.0 * sr6s);
+      if (P.ron2 > 0.0) {  // optional CHARMM switch (no shift), as the pair kernel
+        double e = eps * (sr12 - 2.0 * sr6);
+        if (dr2 > P.ron2) {
+          double c = P.rc2 - dr2;
+          e *= c * c * (P.rc2 + 2.0 * dr2 - 3.0 * P.ron2) / P.sw_den;
+        }
+        elj += e;
+      } else {
+        double sr2s = (sig * sig) / P.rc2;
+        double sr6s = sr2s * sr2s * sr2s;
+        double sr12s = sr6s * sr6s;
+        elj += eps * (sr12 - 2.0 * sr6) - eps * (sr12s - 2.0 * sr6s);
+      }
     }
   }
   if (dr2 > P.rce2) return;
@@ -275,6 +285,8 @@ int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, dou
   P.L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   P.H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);
   P.rc2 = b->p.rc * b->p.rc;
+  P.ron2 = b->p.r_switch > 0.0 ? b->p.r_switch * b->p.r_switch : 0.0;
+  P.sw_den = (P.rc2 - P.ron2) * (P.rc2 - P.ron2) * (P.rc2 - P.ron2);
   P.rce2 = b->mc_rc_ew * b->mc_rc_ew;
   P.kappa = b->p.kappa;
   P.fconv = (kELEC * kELEQ * kELEQ * kNA * 0.001);

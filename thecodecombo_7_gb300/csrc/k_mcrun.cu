@@ -51,6 +51,7 @@ struct MccParams {
   float sLf[3];      // L / 2^32 per axis
   double sLd[3];
   float rc2, rce2, kappa, fconv;
+  float ron2, sw_den;  // LJ switch (ron2 = 0: the reference's shift, lj[2])
   double beta;       // 1 / kT [mol/kJ], kT = RG T / 1000 (read_sim.c:351)
   double delta;      // translation (u - 0.5) * delta per axis (mcmove_displ.c:92-94)
   double rot_max;    // rotation angle in [-rot_max, rot_max] about the centre of mass
@@ -121,7 +122,8 @@ __device__ __forceinline__ void phase_sincos(uint32_t ph, float &s, float &c) {
   }
 }
 
-// energy of one pair at squared distance r2 (shifted LJ + real-space Ewald)
+// energy of one pair at squared distance r2 (shifted or switched LJ +
+// real-space Ewald)
 __device__ __forceinline__ float mcc_pair(const MccParams &P, float r2, float qq,
                                           const float *lj) {
   float e = 0.f;
@@ -133,7 +135,12 @@ __device__ __forceinline__ float mcc_pair(const MccParams &P, float r2, float qq
   if (r2 <= P.rc2 && lj[0] != 0.f) {
     float sr2 = lj[1] / r2;
     float sr6 = sr2 * sr2 * sr2;
-    e += lj[0] * (sr6 * sr6 - 2.f * sr6) - lj[2];
+    float elj = lj[0] * (sr6 * sr6 - 2.f * sr6) - lj[2];
+    if (r2 > P.ron2 && P.ron2 > 0.f) {
+      float c = P.rc2 - r2;
+      elj *= c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) / P.sw_den;
+    }
+    e += elj;
   }
   return e;
 }
@@ -710,7 +717,7 @@ static int mcc_setup(Box *b, int nchains, const int *mol_first, int nmol, int km
     double sr2s = s2 / rc2, sr6s = sr2s * sr2s * sr2s;
     lj[3 * t] = on ? (float)e : 0.f;
     lj[3 * t + 1] = (float)s2;
-    lj[3 * t + 2] = on ? (float)(e * (sr6s * sr6s - 2.0 * sr6s)) : 0.f;
+    lj[3 * t + 2] = on && !(b->p.r_switch > 0.0) ? (float)(e * (sr6s * sr6s - 2.0 * sr6s)) : 0.f;
   }
   mcc_free(b);
   McChains *M = new McChains();
@@ -731,6 +738,11 @@ static int mcc_setup(Box *b, int nchains, const int *mol_first, int nmol, int km
   }
   P.rc2 = (float)rc2;
   P.rce2 = (float)(rc_ew * rc_ew);
+  {
+    double ron2 = b->p.r_switch > 0.0 ? b->p.r_switch * b->p.r_switch : 0.0;
+    P.ron2 = (float)ron2;
+    P.sw_den = (float)((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2));
+  }
   P.kappa = (float)b->p.kappa;
   P.fconv = (float)fconv;
   P.beta = 1.0 / (((kKB * kNA) * T) * .001);

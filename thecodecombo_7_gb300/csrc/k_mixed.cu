@@ -38,6 +38,7 @@
 #include <vector>
 
 #include "fe_device.cuh"
+#include "fe_df.cuh"
 #include "fe_mixed.h"
 
 namespace fe {
@@ -748,6 +749,32 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   }
 }
 
+// qq (1 - erfc(kappa r)) / r of an excluded pair in double-float, from the
+// exact integer separation of the 32-bit fractional coordinates and the FP64
+// charges (the term eewald_intra of cnonbond_nblist.c:416-437)
+__device__ __forceinline__ dfl intra_energy_df(const DfIntra &D, int4 A, int4 B, double qa,
+                                               double qb, float qscale,
+                                               const float2 *__restrict__ exptab) {
+  dfl r2 = {0.f, 0.f};
+  int dd[3] = {(int)((unsigned)A.x - (unsigned)B.x), (int)((unsigned)A.y - (unsigned)B.y),
+               (int)((unsigned)A.z - (unsigned)B.z)};
+#pragma unroll
+  for (int c = 0; c < 3; c++) {
+    dfl d = df_mul(df_from_ll((long long)dd[c]), {D.sl[c].x, D.sl[c].y});
+    r2 = df_add(r2, df_mul(d, d));
+  }
+  dfl r = df_sqrt(r2);
+  dfl z = df_mul(r, {D.kappa.x, D.kappa.y});
+  dfl erf = df_add({1.0f, 0.0f}, df_neg(df_erfc_nr(z, D.C, exptab)));
+  dfl qq = df_mul(df_mul(df_from_double(qa), df_from_double(qb)), {D.qf.x, D.qf.y});
+  qq = df_mul_f(qq, qscale);
+  return df_mul(df_mul(qq, erf), df_recip(r));
+}
+
+__device__ __forceinline__ long long df_to_fixed(dfl v, int shift) {
+  return to_fixed(v.hi, shift) + to_fixed(v.lo, shift);
+}
+
 // excluded and 1-4 pairs (xint), cnonbond_nblist.c:245-263 and 416-437:
 // inside rc an excluded pair contributes no LJ and no real-space term but the
 // intra correction -qq (1 - erfc(kr)) / r; a 1-4 pair gets LJ, real space
@@ -755,10 +782,13 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
 __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__restrict__ flag,
                           const int4 *__restrict__ posfx, const int *__restrict__ iperm,
                           const int *__restrict__ type, float3 sL, int nt, const float *__restrict__ lj_tab, float rc2, float kappa,
-                          float c2k, float qf, float epsRF, unsigned long long *__restrict__ fix,
+                          float c2k, float qf, float epsRF, const double4 *__restrict__ pos_q,
+                          const float2 *__restrict__ exptab, DfIntra D,
+                          unsigned long long *__restrict__ fix,
                           unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                           double *__restrict__ out) {
-  float e_intra = 0.f, e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f;
+  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f;
+  long long q_intra = 0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nexcl; t += gridDim.x * blockDim.x) {
     int a = ab[2 * t], b = ab[2 * t + 1], xf = flag[t];
     if (xf == 0) continue;
@@ -790,7 +820,9 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
       qcorr *= (1.f - (float)kE14FAC);
     }
     float erfkr = 1.f - erfckr;
-    e_intra += qcorr * erfkr * rinv;
+    q_intra += df_to_fixed(intra_energy_df(D, A, B, pos_q[a].w, pos_q[b].w,
+                                           xf == 4 ? (float)(1.0 - kE14FAC) : 1.f, exptab),
+                           32);
     F -= qcorr * rinv * rinv2 * (erfkr - c2k * r * ex);
     long long fxq = to_fix(F * dx), fyq = to_fix(F * dy), fzq = to_fix(F * dz);
     atomicAdd(&fix[3 * a], (unsigned long long)fxq);
@@ -800,7 +832,8 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
     atomicAdd(&fix[3 * b + 1], (unsigned long long)(-fyq));
     atomicAdd(&fix[3 * b + 2], (unsigned long long)(-fzq));
   }
-  float v[5] = {e_lj, e_ljs, e_real, qsum, e_intra};
+  long long v[5] = {to_fixed(e_lj, 32), to_fixed(e_ljs, 32), to_fixed(e_real, 32),
+                    to_fixed(qsum, 32), q_intra};
   block_fix_final<5>(v, 32, facc, ticket, out);
 }
 
@@ -1098,10 +1131,13 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
                            const int4 *__restrict__ posfx, const int *__restrict__ iperm,
                            const int *__restrict__ type, float3 sL, int nt,
                            const float *__restrict__ lj_tab, float rc2, float kappa, float c2k,
-                           float qf, float epsRF, unsigned long long *__restrict__ fix,
+                           float qf, float epsRF, const double4 *__restrict__ pos_q,
+                           const float2 *__restrict__ exptab, DfIntra D,
+                           unsigned long long *__restrict__ fix,
                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                            double *__restrict__ out) {
-  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, e_intra = 0.f, eb = 0.f, ea = 0.f;
+  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, eb = 0.f, ea = 0.f;
+  long long q_intra = 0;
   for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmol; m += gridDim.x * blockDim.x) {
     const int lb = mol_first[m], ns = mol_first[m + 1] - lb;
     int4 P[NS];
@@ -1143,7 +1179,9 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
         qcorr *= (1.f - (float)kE14FAC);
       }
       float erfkr = 1.f - erfckr;
-      e_intra += qcorr * erfkr * rinv;
+      q_intra += df_to_fixed(intra_energy_df(D, Pa, Pb, pos_q[lb + a].w, pos_q[lb + bq].w,
+                                             xf == 4 ? (float)(1.0 - kE14FAC) : 1.f, exptab),
+                             32);
       Fs -= qcorr * rinv * rinv2 * (erfkr - c2k * r * ex);
       intra_add(F, a, Fs * dx, Fs * dy, Fs * dz);
       intra_add(F, bq, -Fs * dx, -Fs * dy, -Fs * dz);
@@ -1202,7 +1240,8 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
           *q = *q + (unsigned long long)to_fix(F[i][c]);
         }
   }
-  float v[7] = {e_lj, e_ljs, e_real, qsum, e_intra, eb, ea};
+  long long v[7] = {to_fixed(e_lj, 32), to_fixed(e_ljs, 32), to_fixed(e_real, 32),
+                    to_fixed(qsum, 32), q_intra, to_fixed(eb, 32), to_fixed(ea, 32)};
   block_fix_final<7>(v, 32, facc, ticket, out);
 }
 
@@ -1376,6 +1415,25 @@ int mixed_setup(Box *b) {
     }
   }
 
+  {
+    // double-float constants of the intramolecular correction energy
+    std::vector<float2> tab(kDfExpN);
+    for (int k = kDfExpLo; k <= kDfExpHi; k++) {
+      float hi, lo;
+      df_split(exp((double)k / 64.0), hi, lo);
+      tab[k - kDfExpLo] = make_float2(hi, lo);
+    }
+    FE_CUDA(cudaMalloc(&M.exptab, sizeof(float2) * kDfExpN));
+    FE_CUDA(cudaMemcpy(M.exptab, tab.data(), sizeof(float2) * kDfExpN, cudaMemcpyHostToDevice));
+    // ewald.c:817-836, constant term first
+    const double c[10] = {-1.26551223, 1.00002368, 0.37409196, 0.09678418, -0.18628806,
+                          0.27886807, -1.13520398, 1.48851587, -0.82215223, 0.17087277};
+    for (int k = 0; k < 10; k++) df_split(c[k], M.dfi.C.c[k].x, M.dfi.C.c[k].y);
+    df_split(b->p.kappa, M.dfi.kappa.x, M.dfi.kappa.y);
+    df_split(kELEC * kELEQ * kELEQ * kNA * 1.0E-3, M.dfi.qf.x, M.dfi.qf.y);
+    for (int d = 0; d < 3; d++) df_split(b->p.L[d] / kFixScale, M.dfi.sl[d].x, M.dfi.sl[d].y);
+  }
+
   // SPME, FP32
   long K = b->K, Kh = b->Kh;
   std::vector<double> et(Kh), kw(Kh);
@@ -1412,7 +1470,7 @@ void mixed_free(Box *b) {
                   M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
                   M.ient, M.snap, M.ps, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
                   M.grid32, M.grid32k, M.floor3, M.gfix, M.sm, M.sd, M.mol_first, M.mol_x,
-                  M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai};
+                  M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai, M.exptab};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (M.plans) {
@@ -1617,6 +1675,7 @@ int forces_mixed(Box *b) {
   // intramolecular terms: one thread per molecule when the topology allows,
   // else the exclusion and bonded kernels
   float3 sL = fix_scale(b);
+  const DfIntra &dfi = M.dfi;
   if (M.nmol > 0) {
     int mb = (M.nmol + 127) / 128;
     if (mb > 2048) mb = 2048;
@@ -1625,7 +1684,7 @@ int forces_mixed(Box *b) {
       M.excl_flag, b->bond_ab, b->bond_req, b->bond_k, b->bend_abc, b->bend_t0, b->bend_k,        \
       M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),                 \
       (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,     \
-      M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA
+      b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA
     if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
     else if (M.intra_maxs <= 4) k_mx_intra<4><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
     else k_mx_intra<kIntraMaxSites><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
@@ -1639,8 +1698,8 @@ int forces_mixed(Box *b) {
                                          b->type, sL, b->nt, M.lj_tab,
                                          (float)(b->p.rc * b->p.rc), (float)b->p.kappa,
                                          (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
-                                         (float)b->p.epsRF, M.fix, b->facc, b->ticket,
-                                         b->scal + SC_MX_EXCL);
+                                         (float)b->p.epsRF, b->pos_q, M.exptab, dfi, M.fix,
+                                         b->facc, b->ticket, b->scal + SC_MX_EXCL);
     FE_LAUNCH_CHECK("k_mx_excl");
     int tot = b->nbond + b->nbend;
     int bb = (tot + 255) / 256;

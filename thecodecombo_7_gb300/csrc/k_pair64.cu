@@ -210,6 +210,63 @@ k_bonded64(int nbond, int nbend, double3 L, const double4 *__restrict__ pos,
   block_partials<2>(v, partials);
 }
 
+// Counts of the half list (instrumentation): entries, pairs within rc that
+// the pair loop evaluates (not excluded), and those with an LJ term -- the
+// units of the pair loop's algorithmic FLOP count.
+__global__ void k_pair_counts(PairParams P, const double4 *__restrict__ pos,
+                              const int *__restrict__ type, const double *__restrict__ lj_eps,
+                              const double *__restrict__ lj_sig, const int *__restrict__ count,
+                              const int *__restrict__ ent, unsigned long long *__restrict__ out) {
+  unsigned long long c[4] = {0, 0, 0, 0};
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < P.n - 1; a += gridDim.x * blockDim.x) {
+    double4 pa = pos[a];
+    const int *row = ent + (size_t)a * P.max_nb;
+    int cnt = count[a];
+    c[0] += cnt;
+    for (int bb = 0; bb < cnt; bb++) {
+      int e = row[bb];
+      int b = e >> 3, xflag = e & 7;
+      double4 pb = pos[b];
+      double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+      dx -= P.L.x * rint(dx / P.L.x);
+      dy -= P.L.y * rint(dy / P.L.y);
+      dz -= P.L.z * rint(dz / P.L.z);
+      if (dx * dx + dy * dy + dz * dz > P.rc2) continue;
+      if (xflag != 0 && xflag != 4) {
+        c[3]++;
+        continue;
+      }
+      c[1]++;
+      int k = type[a] * P.nt + type[b];
+      if (lj_eps[k] * lj_sig[k] != 0.0) c[2]++;
+    }
+  }
+  for (int t = 0; t < 4; t++) atomicAdd(&out[t], c[t]);
+}
+
+int pair_counts64(Box *b, long long *out4) {
+  PairParams P;
+  P.L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
+  P.rc2 = b->p.rc * b->p.rc;
+  P.n = b->n;
+  P.nt = b->nt;
+  P.max_nb = b->max_nb;
+  unsigned long long *d = nullptr;
+  FE_CUDA(cudaMalloc(&d, 4 * sizeof(unsigned long long)));
+  cudaMemsetAsync(d, 0, 4 * sizeof(unsigned long long), b->stream);
+  int blocks = (b->n + 255) / 256;
+  k_pair_counts<<<blocks, 256, 0, b->stream>>>(P, b->pos_q, b->type, b->lj_eps, b->lj_sig,
+                                               b->nl_count, b->nl_ent, d);
+  cudaError_t e = cudaGetLastError();
+  unsigned long long h[4] = {0, 0, 0, 0};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  cudaFree(d);
+  if (e != cudaSuccess) return cuda_fail(e, "k_pair_counts");
+  for (int t = 0; t < 4; t++) out4[t] = (long long)h[t];
+  return FE_OK;
+}
+
 static double host_ref_erfc(double x) {
   // same function as ref_erfc (ewald.c:817-836), evaluated on the host once
   double z = fabs(x);

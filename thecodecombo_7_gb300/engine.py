@@ -55,7 +55,7 @@ EXPORTS = [
     "fe_mc_chains_collect", "fe_mc_chains_samples", "fe_mc_chains_train_surrogate",
     "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
-    "fe_go_get_stream", "fe_autotune",
+    "fe_go_get_stream", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -247,6 +247,12 @@ class Box:
         self._check(self.lib.fe_get_positions(self.h, _p(records), C.c_size_t(stride),
                                               C.c_size_t(off_x)))
 
+    def set_positions_nopbc_array(self, pos):
+        """Unwrapped positions (atnopbc) from an n x 3 array."""
+        a = _c(pos, np.float64).reshape(-1, 3)
+        self._check(self.lib.fe_set_positions_nopbc(self.h, _p(a), C.c_size_t(24),
+                                                    C.c_size_t(0)))
+
     def get_positions_nopbc(self):
         out = np.empty((self.n, 3))
         self._check(self.lib.fe_get_positions_nopbc(self.h, _p(out), C.c_size_t(24),
@@ -377,6 +383,13 @@ class Box:
         ub = self.sysm.n if ub is None else ub
         self._check(self.lib.fe_nl_check(self.h, int(lb), int(ub), C.byref(f)))
         return f.value
+
+    def pair_counts(self):
+        """FP64 boxes: (half-list entries, evaluated pairs within rc, those
+        with LJ, excluded pairs within rc)."""
+        v = np.zeros(4, np.int64)
+        self._check(self.lib.fe_pair_counts(self.h, _p(v)))
+        return tuple(int(x) for x in v)
 
     def inner_list_stats(self):
         """Mixed mode: (entries, longest row, prunes so far) of the inner list."""
@@ -537,6 +550,17 @@ class Batch:
         s = C.c_void_p()
         self._check(self.lib.fe_batch_get_stream(self.h, C.byref(s)))
         return s.value or 0
+
+
+def pipe_peak(which: int, device: int = 0) -> float:
+    """Measured FP32 FMA (which=0) or FP64 FMA (1) TFLOP/s, or ex2.approx
+    Tera-ops/s (2), of the device."""
+    lib = load_library()
+    v = C.c_double()
+    rc = lib.fe_pipe_peak(int(device), int(which), C.byref(v))
+    if rc != FE_OK:
+        raise FeError(rc, lib.fe_last_error().decode())
+    return v.value
 
 
 def tc_gemm_bf16(A_bits, B_bits, bias=None):

@@ -232,13 +232,14 @@ def _place_centres_fast(rng: np.random.Generator, n_mol: int, L: float, dmin: fl
 
 def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
               grid=None, T: float = 300.0, L: float | None = None,
-              dmin: float = 2.6, **params) -> System:
+              dmin: float = 2.6, helper: bool = True, **params) -> System:
     """The 3-site bent-molecule box of the configured workloads.
 
     ``density`` is sites per A^3 (0.1 gives L = 34.47 A at 1,365 molecules and
     L = 98.65 A at 32,000).  ``grid`` defaults to about 1 point/A: round(L)
     lowered to the nearest FFT-friendly size (32^3 and 96^3 for the two sizes
-    above).
+    above).  ``helper=False`` places the molecules with numpy only (same
+    result, no compiled helper loaded).
     """
     rng = np.random.default_rng(seed)
     n = 3 * n_mol
@@ -247,7 +248,7 @@ def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
     if grid is None:
         g = fft_friendly_below(int(round(L)))
         grid = (g, g, g)
-    centres = _place_centres_fast(rng, n_mol, L, dmin)
+    centres = _place_centres_fast(rng, n_mol, L, dmin) if helper else None
     if centres is None:
         centres = _place_centres(rng, n_mol, L, dmin)
     R = _random_rotations(rng, n_mol)
