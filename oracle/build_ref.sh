@@ -37,4 +37,10 @@ build ref_harness -std=gnu99 -O2 -ffp-contract=off
 build ref_harness_fast -std=c99 -D_POSIX_C_SOURCE=200809L -O3 -ffast-math -funroll-all-loops
 # the DLIST build (nl_check and the list-time snapshot, nblist.c:583-647)
 build ref_harness_dlist -std=gnu99 -O2 -ffp-contract=off -DDLIST
-echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast and $OUT/ref_harness_dlist"
+# the classic-Ewald Monte Carlo build (-DMC without SPME): enbnd_mc,
+# ewald_kspace_mc and ewald_rspace_mc (ewald_mc.c:42-641), strict IEEE
+gcc -std=gnu99 -O2 -ffp-contract=off -DNLIST -DEWALD -DMC -DSTYPE -I"$REF" -w \
+    -o "$OUT/ref_harness_mc" "$HERE/ref_harness.c" \
+    "$REF/nblist.c" "$REF/setlj.c" "$REF/ewald.c" "$REF/ewald_mc.c" "$REF/cplx.c" \
+    "$REF/enbnd_mc.c" -lm
+echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast, $OUT/ref_harness_dlist and $OUT/ref_harness_mc"

@@ -23,6 +23,7 @@ SRC = [os.path.join(HERE, "fe_oracle.c"), os.path.join(HERE, "fe_fft.c")]
 REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 REF_BIN_FAST = os.path.join(HERE, "_ref", "ref_harness_fast")
 REF_BIN_DLIST = os.path.join(HERE, "_ref", "ref_harness_dlist")
+REF_BIN_MC = os.path.join(HERE, "_ref", "ref_harness_mc")
 
 # strict IEEE: no FMA contraction, no fast-math, so results are reproducible
 # on x86-64 and aarch64 alike and match a strict build of the reference
@@ -367,6 +368,28 @@ def run_reference_nlcheck(sysm, cases, workdir):
                 f.write(struct.pack("<iddd", i, dx, dy, dz))
     subprocess.check_call([REF_BIN_DLIST, "nlcheck", sp, op, cp])
     return read_tagged(op)
+
+
+def run_reference_mc(sysm, kmax, max_k_square, moves, workdir):
+    """The reference's classic-Ewald MC energies (-DMC build): enbnd_mc
+    (ewald_kspace_mc + ewald_rspace_mc + LJ) of the whole box, then before
+    and after each move (lb, ub, new_positions[(ub - lb), 3]), each move undone
+    after.  Returns energy[(nmoves + 1), 16] (whole box in [0, :8]; per move
+    8 before, 8 after, enbnd_mc's energy[] order) and the move ranges."""
+    os.makedirs(workdir, exist_ok=True)
+    sp = os.path.join(workdir, "system.bin")
+    mp = os.path.join(workdir, "moves.bin")
+    op = os.path.join(workdir, "out_mc.bin")
+    write_system_file(sp, sysm)
+    with open(mp, "wb") as f:
+        f.write(struct.pack("<3i", kmax, max_k_square, len(moves)))
+        for lb, ub, new in moves:
+            f.write(struct.pack("<2i", lb, ub))
+            f.write(np.ascontiguousarray(new, "<f8").reshape(ub - lb, 3).tobytes())
+    subprocess.check_call([REF_BIN_MC, "mc", sp, op, mp])
+    r = read_tagged(op)
+    return dict(energy=r["mc_energy"].reshape(len(moves) + 1, 16),
+                ranges=r["mc_rng_idx"].reshape(len(moves) + 1, 2), nk=int(r["mc_nk"][0]))
 
 
 # ---- counter-based random numbers and replica exchange (no system needed) ----

@@ -26,6 +26,15 @@
  *                 positions plus the case's displacements, pbc_all, and
  *                 nl_check(lb, ub) (nblist.c:607-647); dumps the flags and
  *                 the checked positions
+ *   mode mc      (the -DMC classic-Ewald build, ref_harness_mc, feature flags
+ *                 -DNLIST -DEWALD -DMC -DSTYPE without SPME): <moves.bin>
+ *                 (4th argument) gives kmax, max_k_square and trial moves
+ *                 (site range and new positions); ewald_setup, nblist, then
+ *                 enbnd_mc(lb, ub) -- its ewald_kspace_mc and ewald_rspace_mc
+ *                 (ewald_mc.c:42-641) included -- on the configuration before
+ *                 and after each move (the move undone after), as
+ *                 forces_mc(lb, ub, 0|1) does around a trial move
+ *                 (forces_mc.c:90-573, mcmove_displ.c:70,117)
  */
 #define MAIN
 #include "defines.h"
@@ -35,6 +44,9 @@
 void setlj(void);
 void ewald_setup(int);
 void nblist(int);
+#ifdef MC
+void enbnd_mc(int, int, int, double *);
+#else
 void forces(int);
 void charge_grid(int);
 void pme_calc(int, double *);
@@ -43,11 +55,14 @@ void integrate_vverlet(int, double);
 void integrate_nhc(double, int);
 void kinet(int);
 void pbc_all(int);
+#endif
 #ifdef DLIST
 void nl_check(int, int, int);
 #endif
+#ifndef MC
 double cbond(int);
 double cbend(int);
+#endif
 
 static FILE *g_out;
 
@@ -112,6 +127,9 @@ static void load_system(const char *path) {
   box[k].hx = box[k].lx / 2.0; box[k].hy = box[k].ly / 2.0; box[k].hz = box[k].lz / 2.0;
   box[k].vol = box[k].lx * box[k].ly * box[k].lz;
   box[k].rc2 = sim.rc * sim.rc;
+  box[k].least_boxh = (box[k].lx < box[k].ly ? (box[k].lx < box[k].lz ? box[k].lx : box[k].lz)
+                                             : (box[k].ly < box[k].lz ? box[k].ly : box[k].lz)) /
+                      2.0;
   box[k].rc4 = box[k].rc2 * box[k].rc2;
   box[k].boxns = N;
   box[k].nfree = 3.0 * N - 3.0;
@@ -227,6 +245,7 @@ static void alloc_state(void) {
       ls[l]->xflag[i] = calloc(N, sizeof(int));
     }
   }
+#ifdef SPME
   /* allocate.c:446-505 */
   int ORDER = sim.order;
   int GX = sim.grid[0], GY = sim.grid[1], GZ = sim.grid[2];
@@ -247,6 +266,7 @@ static void alloc_state(void) {
   long ngrid = (long)(GX + 5) * (GY + 5) * (GZ + 5);
   qgrida = fftw_malloc(sizeof(fftw_complex) * ngrid);
   memset(qgrida, 0, sizeof(fftw_complex) * ngrid);
+#endif
 
   nhc[k].M = NHC_M > 0 ? NHC_M : 1;
   nhc[k].Nc = 1;
@@ -312,6 +332,68 @@ static void en_record(double *r) {
   r[9] = en[k].sewald; r[10] = en[k].iewald; r[11] = en[k].tewald;
 }
 
+#ifdef MC
+/* The classic-Ewald MC energies (enbnd_mc with ewald_kspace_mc and
+ * ewald_rspace_mc) before and after each trial move of <moves.bin>:
+ * int32 kmax, max_k_square, nmoves; per move int32 lb, ub, then (ub - lb)
+ * x 3 doubles of new positions. */
+static void run_mc(const char *moves_path) {
+  int k = 0;
+  FILE *mf = fopen(moves_path, "rb");
+  if (!mf) die("cannot open moves file");
+  int32_t h[3];
+  rd(h, 4, 3, mf);
+  sim.kmax[k][0] = sim.kmax[k][1] = sim.kmax[k][2] = h[0];
+  sim.max_k_square[k] = h[1];
+  /* allocate.c:207-230 (MC force accumulators), 506-516 (k-vectors) */
+  ffox = calloc(1, sizeof(double *));
+  ffoy = calloc(1, sizeof(double *));
+  ffoz = calloc(1, sizeof(double *));
+  ffox[k] = calloc(N, sizeof(double));
+  ffoy[k] = calloc(N, sizeof(double));
+  ffoz[k] = calloc(N, sizeof(double));
+  kvec = calloc(1, sizeof(double *));
+  kvec[k] = calloc((size_t)(h[0] + 1) * (2 * h[0] + 1) * (2 * h[0] + 1), sizeof(double));
+  total_k_vectors = calloc(1, sizeof(int));
+  setlj();
+  ewald_setup(k);
+  nblist(k);
+  int nm = h[2];
+  double *e = malloc(sizeof(double) * 16 * (size_t)(nm + 1));
+  int32_t *rng = malloc(sizeof(int32_t) * 2 * (size_t)(nm + 1));
+  enbnd_mc(0, N, k, e); /* the whole configuration */
+  rng[0] = 0;
+  rng[1] = N;
+  double tk = total_k_vectors[k];
+  for (int m = 0; m < nm; m++) {
+    int32_t r[2];
+    rd(r, 4, 2, mf);
+    int lb = r[0], ub = r[1];
+    if (lb < 0 || ub > N || ub <= lb || ub - lb > 64) die("bad move range");
+    double old[64][3], nw[64][3];
+    rd(nw, 8, 3 * (size_t)(ub - lb), mf);
+    enbnd_mc(lb, ub, k, e + 16 * (m + 1)); /* forces_mc(lb, ub, 0, k) */
+    for (int i = lb; i < ub; i++) {
+      old[i - lb][0] = atom[k][i].x; old[i - lb][1] = atom[k][i].y; old[i - lb][2] = atom[k][i].z;
+      atom[k][i].x = nw[i - lb][0]; atom[k][i].y = nw[i - lb][1]; atom[k][i].z = nw[i - lb][2];
+    }
+    enbnd_mc(lb, ub, k, e + 16 * (m + 1) + 8); /* forces_mc(lb, ub, 1, k) */
+    for (int i = lb; i < ub; i++) {
+      atom[k][i].x = old[i - lb][0]; atom[k][i].y = old[i - lb][1]; atom[k][i].z = old[i - lb][2];
+    }
+    rng[2 * (m + 1)] = lb;
+    rng[2 * (m + 1) + 1] = ub;
+  }
+  fclose(mf);
+  /* e[0..7]: enbnd_mc energy[] of the whole box; per move 8 before, 8 after */
+  dump_d("mc_energy", e, 16 * (int64_t)(nm + 1));
+  dump_i("mc_rng_idx", rng, 2 * (int64_t)(nm + 1));
+  dump_d("mc_nk", &tk, 1);
+  free(e);
+  free(rng);
+}
+#endif
+
 int main(int argc, char **argv) {
   if (argc < 4) die("usage: ref_harness <mode> <system.bin> <out.bin> [nsteps]");
   const char *mode = argv[1];
@@ -320,9 +402,16 @@ int main(int argc, char **argv) {
   g_out = fopen(argv[3], "wb");
   if (!g_out) die("cannot open output");
   int k = 0;
+#ifdef MC
+  if (strcmp(mode, "mc") != 0 || argc < 5) die("the MC build runs: mc <system> <out> <moves>");
+  run_mc(argv[4]);
+  fclose(g_out);
+  return 0;
+#endif
   setlj();
   ewald_setup(k);
 
+#ifndef MC
   if (strcmp(mode, "nblist") == 0) {
     nblist(k);
     dump_list("nl", &nlist[k]);
@@ -464,6 +553,7 @@ int main(int argc, char **argv) {
   } else {
     die("unknown mode");
   }
+#endif
   fclose(g_out);
   return 0;
 }

@@ -26,3 +26,9 @@ def golden600():
 def golden4095():
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, "water4095.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_mc():
+    import numpy as np
+    return dict(np.load(os.path.join(GOLDEN, "mc.npz")))

@@ -20,6 +20,14 @@ Fixtures:
                  600-site box: list-time positions, the positions of 10
                  displacement cases after the reference's pbc_all, the site
                  ranges and the reference's nl_flag for each
+  mc.npz         the classic-Ewald Monte Carlo energies (-DMC build): the
+                 reference's enbnd_mc (ewald_kspace_mc + ewald_rspace_mc + LJ)
+                 before and after fixed trial molecule moves, on a periodic
+                 600-site box (k-space 297 vectors; its real space carries
+                 the reference's minimum-image slip, ewald_mc.c:432-437, so
+                 only the k-space and LJ parts are compared there) and on a
+                 330-site cluster inside a larger box (no pair needs an
+                 image: every part is compared)
 """
 import hashlib
 import os
@@ -81,6 +89,7 @@ def main():
         out["forces_" + k] = fo[k]
     np.savez_compressed(os.path.join(HERE, "water4095.npz"), **out)
     make_nlcheck(tmp)
+    make_mc(tmp)
     print("golden fixtures written to", HERE)
 
 
@@ -106,6 +115,39 @@ def nlcheck_cases(s):
     ]
 
 
+def mc_moves(s, nmol, seed, count=8, delta=0.6):
+    """Rigid translations of random molecules, (u - 0.5) delta per axis
+    (mcmove_displ.c:92-94)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(count):
+        m = int(rng.integers(0, nmol))
+        new = s.pos[3 * m:3 * m + 3] + (rng.uniform(size=3) - 0.5) * delta
+        out.append((3 * m, 3 * m + 3, new))
+    return out
+
+
+def make_mc(tmp):
+    out = {}
+    # periodic box
+    s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27), helper=False)
+    mv = mc_moves(s, 200, 5)
+    r = O.run_reference_mc(s, 5, 25, mv, tmp)
+    out.update(per_pos=s.pos, per_L=s.L, per_q=s.q, per_kmax=5, per_mks=25,
+               per_energy=r["energy"], per_ranges=r["ranges"], per_nk=r["nk"],
+               per_new=np.stack([m[2] for m in mv]))
+    # cluster: molecules inside a 15 A cube, box 36 x 38 x 40 A
+    s = systems.water_box(110, L=15.0, seed=8, grid=(24, 24, 24), helper=False)
+    s.pos -= 15.0 * np.floor(s.pos / 15.0 + 0.5)
+    s.L = np.array([36.0, 38.0, 40.0])
+    mv = mc_moves(s, 110, 6)
+    r = O.run_reference_mc(s, 7, 49, mv, tmp)
+    out.update(clu_pos=s.pos, clu_L=s.L, clu_q=s.q, clu_kmax=7, clu_mks=49,
+               clu_energy=r["energy"], clu_ranges=r["ranges"], clu_nk=r["nk"],
+               clu_new=np.stack([m[2] for m in mv]))
+    np.savez_compressed(os.path.join(HERE, "mc.npz"), **out)
+
+
 def make_nlcheck(tmp):
     s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27))
     cases = nlcheck_cases(s)
@@ -118,9 +160,10 @@ def make_nlcheck(tmp):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] == ["nlcheck"]:  # this fixture alone
+    if sys.argv[1:] in (["nlcheck"], ["mc"]):  # this fixture alone
         if not O.build_reference():
             raise SystemExit("reference sources not available")
-        make_nlcheck(tempfile.mkdtemp(prefix="fe_golden_"))
+        {"nlcheck": make_nlcheck, "mc": make_mc}[sys.argv[1]](
+            tempfile.mkdtemp(prefix="fe_golden_"))
     else:
         main()

@@ -11,3 +11,28 @@ def system_from_golden(g, n_mol):
     s.vel = np.ascontiguousarray(g["vel"])
     s.nlist_freq = int(g["nlist_freq"])
     return s
+
+
+def mc_case(g, which):
+    """(System, kmax, max_k_square, moves, reference energies) of one box of
+    the Monte Carlo fixture: which = "per" (periodic 600-site box) or "clu"
+    (cluster inside a larger box).  moves are (lb, ub, new positions)."""
+    pos = np.ascontiguousarray(g[which + "_pos"])
+    n_mol = pos.shape[0] // 3
+    s = systems.water_box(n_mol, L=25.0, seed=0, grid=(24, 24, 24), helper=False)
+    s.pos = pos
+    s.L = np.ascontiguousarray(g[which + "_L"], dtype=np.float64)
+    rng = g[which + "_ranges"][1:]
+    new = g[which + "_new"]
+    moves = [(int(a), int(b), new[i]) for i, (a, b) in enumerate(rng)]
+    return s, int(g[which + "_kmax"]), int(g[which + "_mks"]), moves, g[which + "_energy"]
+
+
+def mc_reference_parts(e):
+    """(dE_kspace, dE_real, dE_lj) of each move from the reference's
+    enbnd_mc energy[] before (e[:8]) and after (e[8:]): k-space energy[4];
+    real space energy[7] - energy[6] (unshifted real minus intramolecular);
+    shifted LJ energy[1] - energy[7] + energy[6] - energy[4] + energy[5]."""
+    def parts(x):
+        return np.array([x[4], x[7] - x[6], x[1] - x[7] + x[6] - x[4] + x[5]])
+    return np.array([parts(r[8:]) - parts(r[:8]) for r in e[1:]])

@@ -250,3 +250,22 @@ def test_mc_delta_with_switch_matches_oracle():
             want, wparts = orc.mc_delta_energy(s.pos, pn, lb, ub, kmax=5, max_k_square=25)
             assert abs(de - want) <= 1e-8 * max(1.0, abs(want)), (de, want)
             np.testing.assert_allclose(parts, wparts, rtol=1e-8, atol=1e-8)
+
+
+def test_mc_delta_matches_reference_fixture(golden_mc):
+    """fe_mc_delta (the drop-in's forces_mc energy change) against the
+    reference's own -DMC enbnd_mc before and after the same trial moves
+    (tests/golden/mc.npz): every part on the cluster box, where no pair
+    needs an image; k-space and LJ on the periodic box (the reference's
+    real space there carries its minimum-image slip, ewald_mc.c:432-437)."""
+    from tests.helpers import mc_case, mc_reference_parts
+    for which in ("clu", "per"):
+        s, kmax, mks, moves, e = mc_case(golden_mc, which)
+        want = mc_reference_parts(e)
+        with _box(s) as b:
+            b.mc_setup(kmax=kmax, max_k_square=mks)
+            assert abs(b.mc_kspace_energy() - e[0, 4]) <= 1e-10 * abs(e[0, 4])
+            for (lb, ub, new), w in zip(moves, want):
+                de, parts = b.mc_delta(lb, ub, new)
+                cols = [0, 1, 2] if which == "clu" else [0, 2]
+                np.testing.assert_allclose(parts[cols], w[cols], rtol=1e-9, atol=1e-9)
