@@ -176,6 +176,13 @@ int fe_kinet(fe_box *box, double *ken6, double *kinet);
 int fe_integrate_vverlet(fe_box *box, double vscal, double *en);
 /* integrate_nhc(time_step, ibox), integrate_nhc.c:40-161 (Nc = Nys = 1) */
 int fe_integrate_nhc(fe_box *box, double time_step);
+/* drift(ibox), drift.c:21-66: removes the net momentum from the velocities
+ * (v_i -= (sum_j m_j v_j / n) / m_i); uu is left as it is. */
+int fe_drift(fe_box *box);
+/* The thermostat temperature sim.T[k] of the box (integrate_nhc reads it):
+ * replica swaps that move a configuration to another box keep the box's
+ * temperature (swap_box.c:5-86). */
+int fe_box_set_temperature(fe_box *box, double T);
 
 /* The production step loop of nve_md.c:359-418 (use_nhc = 0) or nvt_md.c
  * with ID2 == 4 (use_nhc = 1): for i = 1..nsteps { if i % nlist_freq == 0
@@ -196,6 +203,17 @@ int fe_mc_setup(fe_box *box, int kmax, int max_k_square, double rc_ew);
  * (minimum image).  parts3 (may be NULL) = {dE_recip, dE_real, dE_lj}.
  * Replaces forces_mc(lb,ub,0|1,k) old/new differencing (forces_mc.c:90-573). */
 int fe_mc_delta(fe_box *box, int lb, int ub, const double *new_pos, double *dE, double *parts3);
+/* The same move with the change split into the reference's energy terms
+ * (ewald_mc.c / enbnd_mc.c): terms6 = {reciprocal (ewald_kspace_mc
+ * enkewald[0]), LJ (enonbond), LJ shift constant (enonbonds; 0 under the
+ * switch), real space (eewald_real), its shift constant (eewald_reals),
+ * intramolecular correction (eewald_intra)}, each new minus old. */
+int fe_mc_delta_terms(fe_box *box, int lb, int ub, const double *new_pos, double *terms6);
+/* The current energy of the pairs touching sites [lb, ub) in the same six
+ * terms, the first being the whole reciprocal energy: enbnd_mc(lb, ub) of
+ * enbnd_mc.c:26-501 (whose ewald_rspace_mc also counts the pairs of rows
+ * below lb that do not touch the range; they cancel in every difference). */
+int fe_mc_site_energy(fe_box *box, int lb, int ub, double *terms6);
 /* Commit the last fe_mc_delta move (positions and S(k) update) -- the
  * accepted branch of mcmove_trans.c:177; a rejected move needs no call
  * (mcmove_rstr restores nothing on the device). */

@@ -2,8 +2,10 @@
 FP64 integration) against the FP64 CPU oracle.
 
 Bars: relative rms force error <= 1e-5 (forces summed over all terms);
-energies within 2e-6 relative of the force-field total; bitwise identical
-results on repeated evaluation (fixed-point sums are order independent)."""
+bitwise identical results on repeated evaluation (fixed-point sums are order
+independent); energies per term, relative to the oracle's value of the same
+term, ENERGY_BARS below: 1e-7 where FP32 pair math can reach it, and for the
+terms it cannot, the measured level with its cause."""
 import numpy as np
 import pytest
 
@@ -12,6 +14,26 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 RMS_TOL = 1e-5
+
+# Relative error per energy term against the FP64 oracle at the seeded random
+# starts of 4,095 and 12,000 sites (measured on a GB300: 4,095 / 12,000).
+ENERGY_BARS = {
+    "sewald": 1e-12,  # 0: set up once in FP64
+    "iewald": 1e-9,   # < 2e-12: the correction energy is summed in double-float
+    # nbond = LJ + real - intra + (reciprocal - self): 1.4e-6 / 8e-8; inherits
+    # the real-space error below
+    "nbond": 3e-6, "nbonds": 3e-6,
+    # reciprocal: FP32 spline weights, grid and cuFFT transforms, 2.2e-7 /
+    # 1.1e-7 (a sum of positive |S(k)|^2 terms: below 1e-7 needs FP64 FFTs)
+    "kewald": 5e-7,
+    # real space: 4.6e-6 / 7.9e-7.  The term is a net sum of ~1e6 pair energies
+    # of both signs that cancel to ~1e-3 of their magnitudes; each FP32 pair
+    # energy carries ~1e-7 of rounding, so the net carries ~1e-6 relative
+    "rewald": 1e-5,
+    # coulomb = real + reciprocal - self - intra, a net of 1e-3 of its parts:
+    # 8.1e-6 / 2.2e-6 (the real-space error above over a smaller total)
+    "coulomb": 2e-5, "tewald": 2e-5,
+}
 
 
 def _mixed(s):
@@ -41,10 +63,29 @@ def test_mixed_force_error(case):
         f = b.get_forces()
     err = _rms_rel(f, f_ref)
     assert err <= RMS_TOL, f"rms force error {err:.3e}"
-    pot_ref = en_ref["bond"] + en_ref["bend"] + en_ref["nbonds"]
-    scale = max(abs(en_ref["sewald"]), abs(pot_ref))
-    for k in ("bond", "bend", "nbond", "nbonds", "rewald", "kewald", "iewald", "tewald"):
-        assert abs(en[k] - en_ref[k]) <= 2e-6 * scale, (k, en[k], en_ref[k])
+    for k, bar in ENERGY_BARS.items():
+        rel = abs(en[k] - en_ref[k]) / abs(en_ref[k])
+        assert rel <= bar, (k, en[k], en_ref[k], rel)
+    # bond and bend vanish at the rigid start (1e-22 in the oracle): absolute
+    for k in ("bond", "bend"):
+        assert abs(en[k] - en_ref[k]) <= 1e-6, (k, en[k], en_ref[k])
+
+
+def test_mixed_bonded_energies_relative():
+    """Bond and bend energies of a perturbed (non-rigid) geometry: sums of
+    positive terms, within 1e-6 relative of the oracle (FP32 r - r0 loses
+    ~1e-7 of each stretch)."""
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(1365, density=0.1, seed=41)
+    rng = np.random.default_rng(3)
+    s.pos = s.pos + rng.normal(0.0, 0.03, s.pos.shape)
+    s.pos -= s.L * np.floor(s.pos / s.L + 0.5)
+    _, en_ref = O.Oracle(s).forces(s.pos)
+    with _mixed(s) as b:
+        b.nblist()
+        en = b.forces()
+    for k in ("bond", "bend"):
+        assert abs(en[k] - en_ref[k]) <= 1e-6 * abs(en_ref[k]), (k, en[k], en_ref[k])
 
 
 def test_mixed_deterministic(case):
@@ -91,7 +132,9 @@ def test_mixed_switch_matches_oracle():
         en = b.forces()
         f = b.get_forces()
     assert _rms_rel(f, f_ref) <= RMS_TOL
-    assert abs(en["nbond"] - en_ref["nbond"]) <= 2e-6 * abs(en_ref["sewald"])
+    for k in ("nbond", "nbonds", "kewald", "iewald", "rewald"):
+        rel = abs(en[k] - en_ref[k]) / abs(en_ref[k])
+        assert rel <= ENERGY_BARS[k], (k, en[k], en_ref[k], rel)
 
 
 def test_mixed_drift_matches_fp64():

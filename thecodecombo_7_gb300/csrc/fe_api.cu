@@ -893,6 +893,31 @@ int fe_mc_delta(fe_box *box, int lb, int ub, const double *new_pos, double *dE, 
   return mc_delta(&box->b, lb, ub, new_pos, dE, parts3);
 }
 
+int fe_mc_delta_terms(fe_box *box, int lb, int ub, const double *new_pos, double *terms6) {
+  if (!box || !new_pos || !terms6) return FE_ERR_ARG;
+  return mc_terms(&box->b, lb, ub, new_pos, terms6);
+}
+
+int fe_mc_site_energy(fe_box *box, int lb, int ub, double *terms6) {
+  if (!box || !terms6) return FE_ERR_ARG;
+  return mc_terms(&box->b, lb, ub, nullptr, terms6);
+}
+
+int fe_drift(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  return launch_drift(&box->b);
+}
+
+int fe_box_set_temperature(fe_box *box, double T) {
+  if (!box || !(T > 0.0)) return FE_ERR_ARG;
+  Box *b = &box->b;
+  b->p.T = T;
+  FE_CUDA(cudaMemcpyAsync(b->scal + SC_TEMP, &b->p.T, sizeof(double), cudaMemcpyHostToDevice,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
 int fe_mc_accept(fe_box *box) {
   if (!box) return FE_ERR_ARG;
   return mc_accept(&box->b);

@@ -217,6 +217,8 @@ int relaunch_kernel(Box *b, int which);
 // k_mc.cu
 int mc_setup(Box *b, int kmax, int mks, double rc_ew);
 int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, double *parts);
+int mc_terms(Box *b, int lb, int ub, const double *new_pos_host, double *terms6);
+int launch_drift(Box *b);
 int mc_accept(Box *b);
 int mc_kspace_energy(Box *b, double *e);
 void mc_free(Box *b);

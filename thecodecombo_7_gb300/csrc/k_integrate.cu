@@ -289,6 +289,44 @@ __global__ void k_kinet_fix(int n, const double *__restrict__ mass, const double
   }
 }
 
+// drift(ibox), drift.c:21-66: the net momentum P = sum m v divided by the
+// number of sites, then v_i -= (P / n) / m_i (velocities only, uu kept).
+__global__ void k_momentum(int n, const double *__restrict__ mass, const double *__restrict__ vv,
+                           double *__restrict__ partials) {
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    double m = mass[i];
+    v[0] += m * vv[3 * i];
+    v[1] += m * vv[3 * i + 1];
+    v[2] += m * vv[3 * i + 2];
+  }
+  block_partials<3>(v, partials);
+}
+
+__global__ void k_drift_remove(int n, const double *__restrict__ mass, const double *__restrict__ p,
+                               double *__restrict__ vv) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double ns = 1.0 * n;
+  double imass = 1.0 / mass[i];
+  vv[3 * i] -= (p[0] / ns) * imass;
+  vv[3 * i + 1] -= (p[1] / ns) * imass;
+  vv[3 * i + 2] -= (p[2] / ns) * imass;
+}
+
+int launch_drift(Box *b) {
+  int blocks = (b->n + 255) / 256;
+  if (blocks > 1024) blocks = 1024;
+  k_momentum<<<blocks, 256, 0, b->stream>>>(b->n, b->mass, b->vv, b->partials);
+  FE_LAUNCH_CHECK("k_momentum");
+  int rc = launch_reduce(b, b->partials, blocks, 3, SC_ENERGY3, 1.0);  // scratch slots
+  if (rc) return rc;
+  k_drift_remove<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->mass, b->scal + SC_ENERGY3,
+                                                           b->vv);
+  FE_LAUNCH_CHECK("k_drift_remove");
+  return FE_OK;
+}
+
 int launch_kinet(Box *b) {
   int blocks = (b->n + 255) / 256;
   if (blocks > 512) blocks = 512;

@@ -79,6 +79,7 @@ struct McPair {
   double3 L, H;
   double rc2, rce2, kappa, fconv, lj_shift_rc2;
   double ron2, sw_den;  // LJ switch (ron2 = 0: the reference's shift)
+  double erfc_rce;      // erfc(kappa rc_ew) / rc_ew
   int n, nt, lb, ub;
 };
 
@@ -90,14 +91,17 @@ __device__ __forceinline__ int mc_xflag(const int *__restrict__ xs, const int *_
   return f;
 }
 
-// one pair's shifted LJ (rc) + real-space Ewald (rc_ew) + excluded-pair
-// correction, as ewald_mc.c:390-606 / enbnd_mc.c with the minimum image of
-// cnonbond_nblist.c:167-172
-__device__ __forceinline__ void mc_pair_energy(const McPair &P, double3 pa, double qa, int ta,
-                                               double3 pb, double qb, int tb, int xflag,
-                                               const double *__restrict__ lj_eps,
-                                               const double *__restrict__ lj_sig, double &elj,
-                                               double &ereal) {
+// one pair's MC energy terms, as ewald_mc.c:390-606 / enbnd_mc.c with the
+// minimum image of cnonbond_nblist.c:167-172, added to t[5]:
+//   t[0] LJ within rc (switched when r_switch > 0), t[1] its shift constant
+//   eps (sr12s - 2 sr6s) (enonbonds; 0 under the switch), t[2] real-space
+//   Ewald qq erfc(kr)/r within rc_ew, t[3] its shift constant
+//   qq erfc(k rc_ew)/rc_ew (eewald_reals), t[4] the excluded-pair correction
+//   qq12 (1 - erfc(kr))/r (eewald_intra)
+__device__ __forceinline__ void mc_pair_terms(const McPair &P, double3 pa, double qa, int ta,
+                                              double3 pb, double qb, int tb, int xflag,
+                                              const double *__restrict__ lj_eps,
+                                              const double *__restrict__ lj_sig, double *t) {
   double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
   if (dx > P.H.x) dx -= P.L.x;
   else if (dx < -P.H.x) dx += P.L.x;
@@ -122,12 +126,13 @@ __device__ __forceinline__ void mc_pair_energy(const McPair &P, double3 pa, doub
           double c = P.rc2 - dr2;
           e *= c * c * (P.rc2 + 2.0 * dr2 - 3.0 * P.ron2) / P.sw_den;
         }
-        elj += e;
+        t[0] += e;
       } else {
         double sr2s = (sig * sig) / P.rc2;
         double sr6s = sr2s * sr2s * sr2s;
         double sr12s = sr6s * sr6s;
-        elj += eps * (sr12 - 2.0 * sr6) - eps * (sr12s - 2.0 * sr6s);
+        t[0] += eps * (sr12 - 2.0 * sr6);
+        t[1] += eps * (sr12s - 2.0 * sr6s);
       }
     }
   }
@@ -138,22 +143,28 @@ __device__ __forceinline__ void mc_pair_energy(const McPair &P, double3 pa, doub
   double dr = sqrt(dr2);
   double dri = 1.0 / dr;
   double erfckr = ref_erfc(P.kappa * dr);
-  if (qq != 0.0) ereal += qq * erfckr * dri;
+  if (qq != 0.0) {
+    t[2] += qq * erfckr * dri;
+    t[3] += qq * P.erfc_rce;
+  }
   if (xflag) {
     double qq12 = qqab;
     if (xflag == 4) qq12 *= (1.0 - kE14FAC);
-    ereal -= qq12 * (1.0 - erfckr) * dri;
+    t[4] += qq12 * (1.0 - erfckr) * dri;
   }
 }
 
-// grid-stride over (moved site j, partner b): new minus old pair energies
+// grid-stride over (moved site j, partner b): the pair terms of
+// mc_pair_terms, new minus old (DELTA) or of the current configuration
+// (the energy of the pairs touching sites [lb, ub))
+template <bool DELTA>
 __global__ void k_mc_pairs(McPair P, const double4 *__restrict__ pos, const int *__restrict__ type,
                            const double *__restrict__ newpos, const double *__restrict__ lj_eps,
                            const double *__restrict__ lj_sig, const int *__restrict__ xs,
                            const int *__restrict__ xp, const int *__restrict__ xf,
                            double *__restrict__ partials) {
   int m = P.ub - P.lb;
-  double dlj = 0.0, dre = 0.0;
+  double acc[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
   long total = (long)m * P.n;
   for (long t = (long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long)gridDim.x * blockDim.x) {
@@ -166,19 +177,24 @@ __global__ void k_mc_pairs(McPair P, const double4 *__restrict__ pos, const int 
     double4 A = pos[a], B = pos[b];
     int xflag = mc_xflag(xs, xp, xf, a, b);
     double3 ao = make_double3(A.x, A.y, A.z);
-    double3 an = make_double3(newpos[3 * j], newpos[3 * j + 1], newpos[3 * j + 2]);
     double3 bo = make_double3(B.x, B.y, B.z);
-    double3 bn = bmoved ? make_double3(newpos[3 * (b - P.lb)], newpos[3 * (b - P.lb) + 1],
-                                       newpos[3 * (b - P.lb) + 2])
-                        : bo;
-    double lo = 0.0, ro = 0.0, ln = 0.0, rn = 0.0;
-    mc_pair_energy(P, ao, A.w, type[a], bo, B.w, type[b], xflag, lj_eps, lj_sig, lo, ro);
-    mc_pair_energy(P, an, A.w, type[a], bn, B.w, type[b], xflag, lj_eps, lj_sig, ln, rn);
-    dlj += ln - lo;
-    dre += rn - ro;
+    double to[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    mc_pair_terms(P, ao, A.w, type[a], bo, B.w, type[b], xflag, lj_eps, lj_sig, to);
+    if (DELTA) {
+      double3 an = make_double3(newpos[3 * j], newpos[3 * j + 1], newpos[3 * j + 2]);
+      double3 bn = bmoved ? make_double3(newpos[3 * (b - P.lb)], newpos[3 * (b - P.lb) + 1],
+                                         newpos[3 * (b - P.lb) + 2])
+                          : bo;
+      double tn[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+      mc_pair_terms(P, an, A.w, type[a], bn, B.w, type[b], xflag, lj_eps, lj_sig, tn);
+#pragma unroll
+      for (int q = 0; q < 5; q++) acc[q] += tn[q] - to[q];
+    } else {
+#pragma unroll
+      for (int q = 0; q < 5; q++) acc[q] += to[q];
+    }
   }
-  double v[2] = {dlj, dre};
-  block_partials<2>(v, partials);
+  block_partials<5>(acc, partials);
 }
 
 __global__ void k_mc_commit(int nk, int lb, int m, const double *__restrict__ newpos,
@@ -260,27 +276,56 @@ int mc_setup(Box *b, int kmax, int mks, double rc_ew) {
   return FE_OK;
 }
 
-int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, double *parts) {
+static double host_erfc_nr(double x) {
+  // the reference's erfc fit (ewald.c:817-836), evaluated once on the host
+  double z = fabs(x);
+  double t = 1.0 / (1.0 + 0.5 * z);
+  double v = t * exp(-z * z + -1.26551223 +
+                     t * (1.00002368 + t * (0.37409196 + t * (0.09678418 +
+                     t * (-0.18628806 + t * (0.27886807 + t * (-1.13520398 +
+                     t * (1.48851587 + t * (-0.82215223 + t * 0.17087277)))))))));
+  return x < 0 ? 2.0 - v : v;
+}
+
+// Energy terms of the pairs touching sites [lb, ub): with new_pos_host, the
+// change when those sites move there (and the reciprocal change, dS kept for
+// fe_mc_accept); without, the current energies (and the whole reciprocal
+// energy).  terms[6] = {reciprocal, LJ, LJ shift constant, real space, its
+// shift constant, intramolecular correction} (see mc_pair_terms).
+int mc_terms(Box *b, int lb, int ub, const double *new_pos_host, double *terms) {
   if (!b->mc_S) {
-    set_error("fe_mc_delta before fe_mc_setup");
+    set_error("fe_mc_delta / fe_mc_site_energy before fe_mc_setup");
     return FE_ERR_STATE;
   }
   int m = ub - lb;
+  if (lb < 0 || ub > b->n || m < 1) {
+    set_error("fe_mc: site range outside the box");
+    return FE_ERR_ARG;
+  }
   if (m > kMcMaxMoved) {
     set_error("fe_mc_delta: at most 64 sites per move");
     return FE_ERR_SIZE;
   }
-  FE_CUDA(cudaMemcpyAsync(b->mc_newpos, new_pos_host, sizeof(double) * 3 * m,
-                          cudaMemcpyHostToDevice, b->stream));
-  double two_pi = 2.0 * kPI;
-  double3 tp = make_double3(two_pi * (1.0 / b->p.L[0]), two_pi * (1.0 / b->p.L[1]),
-                            two_pi * (1.0 / b->p.L[2]));
-  int kb = (b->mc_nk + 127) / 128;
-  k_mc_recip<<<kb, 128, 0, b->stream>>>(b->mc_nk, lb, m, tp, b->pos_q, b->mc_newpos, b->mc_kidx,
-                                        b->mc_kvec, b->mc_S, b->mc_dS, b->mc_part);
-  FE_LAUNCH_CHECK("k_mc_recip");
-  int rc = launch_reduce(b, b->mc_part, kb, 1, SC_ENERGY3, 1.0);  // scratch slot
-  if (rc) return rc;
+  const bool delta = new_pos_host != nullptr;
+  double h[6];
+  if (delta) {
+    FE_CUDA(cudaMemcpyAsync(b->mc_newpos, new_pos_host, sizeof(double) * 3 * m,
+                            cudaMemcpyHostToDevice, b->stream));
+    double two_pi = 2.0 * kPI;
+    double3 tp = make_double3(two_pi * (1.0 / b->p.L[0]), two_pi * (1.0 / b->p.L[1]),
+                              two_pi * (1.0 / b->p.L[2]));
+    int kb = (b->mc_nk + 127) / 128;
+    k_mc_recip<<<kb, 128, 0, b->stream>>>(b->mc_nk, lb, m, tp, b->pos_q, b->mc_newpos,
+                                          b->mc_kidx, b->mc_kvec, b->mc_S, b->mc_dS, b->mc_part);
+    FE_LAUNCH_CHECK("k_mc_recip");
+    int rc = launch_reduce(b, b->mc_part, kb, 1, SC_ENERGY3, 1.0);  // scratch slot
+    if (rc) return rc;
+    FE_CUDA(cudaMemcpyAsync(h, b->scal + SC_ENERGY3, sizeof(double), cudaMemcpyDeviceToHost,
+                            b->stream));
+  } else {
+    int rc = mc_kspace_energy(b, h);
+    if (rc) return rc;
+  }
   McPair P;
   P.L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   P.H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);
@@ -289,6 +334,7 @@ int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, dou
   P.sw_den = (P.rc2 - P.ron2) * (P.rc2 - P.ron2) * (P.rc2 - P.ron2);
   P.rce2 = b->mc_rc_ew * b->mc_rc_ew;
   P.kappa = b->p.kappa;
+  P.erfc_rce = host_erfc_nr(b->p.kappa * b->mc_rc_ew) / b->mc_rc_ew;
   P.fconv = (kELEC * kELEQ * kELEQ * kNA * 0.001);
   P.n = b->n;
   P.nt = b->nt;
@@ -297,27 +343,41 @@ int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, dou
   long total = (long)m * b->n;
   int pb = (int)((total + 255) / 256);
   if (pb > 1024) pb = 1024;
-  k_mc_pairs<<<pb, 256, 0, b->stream>>>(P, b->pos_q, b->type, b->mc_newpos, b->lj_eps, b->lj_sig,
-                                        b->x_start, b->x_partner, b->x_flag,
-                                        b->mc_part + kMaxPartialBlocks * kPartialTerms / 2);
+  double *part = b->mc_part + kMaxPartialBlocks * kPartialTerms / 2;
+  if (delta)
+    k_mc_pairs<true><<<pb, 256, 0, b->stream>>>(P, b->pos_q, b->type, b->mc_newpos, b->lj_eps,
+                                                b->lj_sig, b->x_start, b->x_partner, b->x_flag,
+                                                part);
+  else
+    k_mc_pairs<false><<<pb, 256, 0, b->stream>>>(P, b->pos_q, b->type, b->mc_newpos, b->lj_eps,
+                                                 b->lj_sig, b->x_start, b->x_partner, b->x_flag,
+                                                 part);
   FE_LAUNCH_CHECK("k_mc_pairs");
-  rc = launch_reduce(b, b->mc_part + kMaxPartialBlocks * kPartialTerms / 2, pb, 2, SC_ENERGY3 + 1,
-                     1.0);
+  int rc = launch_reduce(b, part, pb, 5, SC_ENERGY8, 1.0);  // scratch slots
   if (rc) return rc;
-  double h[3];
-  FE_CUDA(cudaMemcpyAsync(h, b->scal + SC_ENERGY3, sizeof(double) * 3, cudaMemcpyDeviceToHost,
+  FE_CUDA(cudaMemcpyAsync(h + 1, b->scal + SC_ENERGY8, sizeof(double) * 5, cudaMemcpyDeviceToHost,
                           b->stream));
   FE_CUDA(cudaStreamSynchronize(b->stream));
-  double dk = h[0], dlj = h[1], dreal = h[2];
+  for (int q = 0; q < 6; q++) terms[q] = h[q];
+  if (delta) {
+    b->mc_lb = lb;
+    b->mc_ub = ub;
+    b->mc_pending = 1;
+  }
+  return FE_OK;
+}
+
+int mc_delta(Box *b, int lb, int ub, const double *new_pos_host, double *dE, double *parts) {
+  double t[6];
+  int rc = mc_terms(b, lb, ub, new_pos_host, t);
+  if (rc) return rc;
+  double dk = t[0], dlj = t[1] - t[2], dreal = t[3] - t[5];
   if (dE) *dE = dk + dreal + dlj;
   if (parts) {
     parts[0] = dk;
     parts[1] = dreal;
     parts[2] = dlj;
   }
-  b->mc_lb = lb;
-  b->mc_ub = ub;
-  b->mc_pending = 1;
   return FE_OK;
 }
 

@@ -56,6 +56,7 @@ EXPORTS = [
     "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
     "fe_go_get_stream", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
+    "fe_mc_delta_terms", "fe_mc_site_energy", "fe_drift", "fe_box_set_temperature",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -196,6 +197,7 @@ class Box:
         p.nfree = 0.0
         self.params = p
         h = C.c_void_p()
+        self.lib.fe_box_set_temperature.argtypes = [C.c_void_p, C.c_double]
         self._check(self.lib.fe_box_create(C.byref(h), C.byref(p)))
         self.h = h
         self.n = sysm.n
@@ -415,6 +417,27 @@ class Box:
         self._check(self.lib.fe_mc_delta(self.h, int(lb), int(ub), _p(npos), C.byref(de),
                                          _p(parts)))
         return de.value, parts
+
+    def mc_delta_terms(self, lb, ub, new_pos):
+        """Change of the six MC energy terms (reciprocal, LJ, LJ shift,
+        real, real shift, intramolecular) for moving [lb, ub) to new_pos."""
+        npos = _c(new_pos, np.float64).reshape(-1, 3)
+        t = np.empty(6)
+        self._check(self.lib.fe_mc_delta_terms(self.h, int(lb), int(ub), _p(npos), _p(t)))
+        return t
+
+    def mc_site_energy(self, lb, ub):
+        """The six terms of the pairs touching [lb, ub) (whole reciprocal)."""
+        t = np.empty(6)
+        self._check(self.lib.fe_mc_site_energy(self.h, int(lb), int(ub), _p(t)))
+        return t
+
+    def drift(self):
+        """drift.c:21: remove the net momentum from the velocities."""
+        self._check(self.lib.fe_drift(self.h))
+
+    def set_temperature(self, T):
+        self._check(self.lib.fe_box_set_temperature(self.h, C.c_double(T)))
 
     def mc_accept(self):
         self._check(self.lib.fe_mc_accept(self.h))
