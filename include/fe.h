@@ -158,6 +158,10 @@ int fe_cnonbondnl(fe_box *box, double *energy8);
 /* pme_calc(k, energy), pme_calc.c:18-279 (charge_grid, FFTs, reciprocal
  * sum, pme_force with mean-force removal): accumulates into ff. */
 int fe_pme_calc(fe_box *box, double *energy3);
+/* fillspline(w, array, darray), pme_spline.c:10-49: B-spline weights
+ * array[1..order] and derivatives darray[1..order] at fraction w (host
+ * arithmetic, the reference's recursion; arrays of order + 1 doubles). */
+int fe_bspline(int order, double w, double *array, double *darray);
 /* charge_grid(k), pme_qgrid.c:13-121: spread charges; fe_get_charge_grid
  * copies the real grid (grid[0]*grid[1]*grid[2] doubles, x slowest). */
 int fe_charge_grid(fe_box *box);

@@ -13,7 +13,7 @@
 # Feature flags: -DNLIST -DEWALD -DSPME -DSTYPE.  FFTW3 is not installed, so
 # the five FFTW symbols come from oracle/fftw_shim (the oracle's own FFT).
 set -e
-REF=${REF:-/root/reference}
+REF=${REF_DIR:?set REF_DIR to the reference source tree}
 HERE=$(cd "$(dirname "$0")" && pwd)
 OUT="$HERE/_ref"
 if [ ! -f "$REF/defines.h" ]; then
@@ -23,7 +23,7 @@ fi
 mkdir -p "$OUT"
 SRCS="nblist cnonbond_nblist pme_qgrid pme_spline pme_setup pme_calc forces
       cbond cbend curey ctorsion cimproper integrate_vverlet pbc_all kinet
-      integrate_nhc setlj ewald"
+      integrate_nhc setlj ewald drift"
 FEAT="-DNLIST -DEWALD -DSPME -DSTYPE"
 build() {
   name=$1; shift

@@ -307,6 +307,29 @@ static void fillspline(int ORDER, double w, double *array, double *darray) {
   array[1] *= div * (1.0 - w);
 }
 
+void or_fillspline(int order, double w, double *array, double *darray) {
+  fillspline(order, w, array, darray);
+}
+
+/* drift.c:21-66: net momentum / n subtracted as (P / n) / m_i */
+void or_drift(const or_system *s, double *vv) {
+  double vvx = 0.0, vvy = 0.0, vvz = 0.0;
+  for (int i = 0; i < s->n; i++) {
+    vvx += s->mass[i] * vv[3 * i];
+    vvy += s->mass[i] * vv[3 * i + 1];
+    vvz += s->mass[i] * vv[3 * i + 2];
+  }
+  vvx /= (1.0 * s->n);
+  vvy /= (1.0 * s->n);
+  vvz /= (1.0 * s->n);
+  for (int i = 0; i < s->n; i++) {
+    double imass = 1.0 / s->mass[i];
+    vv[3 * i] -= vvx * imass;
+    vv[3 * i + 1] -= vvy * imass;
+    vv[3 * i + 2] -= vvz * imass;
+  }
+}
+
 static void dftmod(double *bmod, const double *barr, int grid) {
   /* pme_setup.c:110-130 */
   double twopi = 2.0 * PI_;

@@ -139,6 +139,11 @@ int or_run_md_timed(const or_system *s, int nsteps, int nlist_freq, int use_nhc,
                     int nhc_M, double nhc_Q, double *pos, double *pos_nopbc,
                     double *vv, double *ff, double *zeta, double *rec, double *tstamp);
 
+/* pme_spline.c:10-49 B-spline weights / derivatives, array[0..order] */
+void or_fillspline(int order, double w, double *array, double *darray);
+/* drift.c:21-66 momentum removal on vv (n x 3) */
+void or_drift(const or_system *s, double *vv);
+
 /* ---- classic-Ewald MC energy path (ewald.c:46-118, ewald_mc.c) ---- */
 
 /* number of k-vectors of ewald_setup's enumeration (ewald.c:104-118) */

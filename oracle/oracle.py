@@ -46,12 +46,25 @@ def build(force: bool = False, fast: bool = False) -> str:
     return lib
 
 
+def reference_dir():
+    """The reference's source tree: the directory named by the environment
+    variable FE_REFERENCE_DIR, or else a checkout named ``reference`` next to
+    this repository; None when neither holds its defines.h."""
+    cands = [os.environ.get("FE_REFERENCE_DIR"),
+             os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")]
+    for c in cands:
+        if c and os.path.exists(os.path.join(c, "defines.h")):
+            return c
+    return None
+
+
 def build_reference() -> bool:
     """Compile the reference's own routines into oracle/_ref (only where the
     reference sources exist).  Returns True when the binary is available."""
     script = os.path.join(HERE, "build_ref.sh")
-    if os.path.exists("/root/reference/defines.h"):
-        subprocess.check_call(["sh", script])
+    ref = reference_dir()
+    if ref:
+        subprocess.check_call(["sh", script], env=dict(os.environ, REF_DIR=ref))
     return os.path.exists(REF_BIN)
 
 
@@ -268,6 +281,11 @@ class Oracle:
             out["tstamp"] = ts
         return out
 
+    def drift(self, vel):
+        v = np.ascontiguousarray(vel, np.float64).copy()
+        self.lib.or_drift(self.sp, _p(v))
+        return v
+
     # ---- MC ----
     def ewald_kspace_energy(self, pos, kmax=7, max_k_square=49):
         pos = np.ascontiguousarray(pos, np.float64)
@@ -368,6 +386,15 @@ def run_reference_nlcheck(sysm, cases, workdir):
                 f.write(struct.pack("<iddd", i, dx, dy, dz))
     subprocess.check_call([REF_BIN_DLIST, "nlcheck", sp, op, cp])
     return read_tagged(op)
+
+
+def fillspline(order, w):
+    """or_fillspline: (array, darray) of order + 1 doubles each."""
+    L = C.CDLL(build())
+    a = np.zeros(order + 1)
+    d = np.zeros(order + 1)
+    L.or_fillspline(C.c_int(order), C.c_double(w), _p(a), _p(d))
+    return a, d
 
 
 def run_reference_mc(sysm, kmax, max_k_square, moves, workdir):

@@ -21,6 +21,7 @@
  *   mode forces : force/energy breakdown at the input configuration
  *   mode nve    : nsteps of NVE velocity Verlet (list rebuilt every nlist)
  *   mode nhc    : nsteps of NHC-VV (integrate_nhc / integrate_vverlet / integrate_nhc)
+ *   mode drift  : drift() (drift.c:21) on the input velocities
  *   mode nlcheck (the -DDLIST build, ref_harness_dlist): nblist, then per
  *                 case of <cases.bin> (the 4th argument) the snapshot
  *                 positions plus the case's displacements, pbc_all, and
@@ -58,6 +59,9 @@ void pbc_all(int);
 #endif
 #ifdef DLIST
 void nl_check(int, int, int);
+#endif
+#ifndef MC
+void drift(int);
 #endif
 #ifndef MC
 double cbond(int);
@@ -453,6 +457,11 @@ int main(int argc, char **argv) {
     kinet(k);
     en_record(r);
     dump_d("en", r, 12);
+  } else if (strcmp(mode, "drift") == 0) {
+    /* drift.c:21: net-momentum removal from the input velocities */
+    drift(k);
+    dump_xyz("vel", vv[k]);
+    dump_xyz("vel_uu", uu[k]);
   } else if (strcmp(mode, "nve") == 0 || strcmp(mode, "nhc") == 0) {
     int nsteps = argc > 4 ? atoi(argv[4]) : 10;
     int use_nhc = strcmp(mode, "nhc") == 0;

@@ -20,6 +20,8 @@ Fixtures:
                  600-site box: list-time positions, the positions of 10
                  displacement cases after the reference's pbc_all, the site
                  ranges and the reference's nl_flag for each
+  drift600.npz   drift() (drift.c:21) on velocities of the 600-site box given
+                 a net momentum: velocities before and after
   mc.npz         the classic-Ewald Monte Carlo energies (-DMC build): the
                  reference's enbnd_mc (ewald_kspace_mc + ewald_rspace_mc + LJ)
                  before and after fixed trial molecule moves, on a periodic
@@ -90,6 +92,7 @@ def main():
     np.savez_compressed(os.path.join(HERE, "water4095.npz"), **out)
     make_nlcheck(tmp)
     make_mc(tmp)
+    make_drift(tmp)
     print("golden fixtures written to", HERE)
 
 
@@ -148,6 +151,14 @@ def make_mc(tmp):
     np.savez_compressed(os.path.join(HERE, "mc.npz"), **out)
 
 
+def make_drift(tmp):
+    s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27), helper=False)
+    s.vel = s.vel + np.array([0.7, -0.4, 0.25])
+    r = O.run_reference("drift", s, tmp)
+    np.savez_compressed(os.path.join(HERE, "drift600.npz"), vel0=s.vel, mass=s.mass,
+                        vel=r["vel"].reshape(-1, 3), uu=r["vel_uu"].reshape(-1, 3))
+
+
 def make_nlcheck(tmp):
     s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27))
     cases = nlcheck_cases(s)
@@ -160,10 +171,10 @@ def make_nlcheck(tmp):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["nlcheck"], ["mc"]):  # this fixture alone
+    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"]):  # this fixture alone
         if not O.build_reference():
             raise SystemExit("reference sources not available")
-        {"nlcheck": make_nlcheck, "mc": make_mc}[sys.argv[1]](
+        {"nlcheck": make_nlcheck, "mc": make_mc, "drift": make_drift}[sys.argv[1]](
             tempfile.mkdtemp(prefix="fe_golden_"))
     else:
         main()

@@ -7,6 +7,8 @@ import subprocess
 import numpy as np
 import pytest
 
+from oracle import oracle as O
+
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
@@ -114,21 +116,34 @@ def test_water_box_recipe():
     assert systems.fft_friendly_below(99) == 96 and systems.fft_friendly_below(34) == 32
 
 
-@pytest.mark.skipif(not os.path.exists("/root/reference/makefile"),
-                    reason="reference sources not present")
+@pytest.mark.skipif(O.reference_dir() is None, reason="reference sources not present")
 def test_reference_program_links_against_the_engine(lib):
-    """The reference's own program, with the nine replaced routines taken out
-    of its SRCS and the drop-in shim added, compiles and links against
-    libfe.so; the replaced symbols resolve to the shim."""
+    """The reference's own program, with the replaced routines taken out of
+    its SRCS and the drop-in shim added, compiles and links against libfe.so
+    in both forms (MD with SPME, Monte Carlo with classic Ewald); the
+    replaced symbols resolve to the shim."""
     script = os.path.join(ROOT, "thecodecombo_7_gb300", "dropin", "build_reference_with_engine.sh")
-    subprocess.check_call(["sh", script], stdout=subprocess.DEVNULL)
+    subprocess.check_call(["sh", script], stdout=subprocess.DEVNULL,
+                          env=dict(os.environ, REF_DIR=O.reference_dir()))
     out = os.path.join(ROOT, "thecodecombo_7_gb300", "dropin", "_build")
-    assert os.path.exists(os.path.join(out, "spidey_gpu"))
-    syms = subprocess.run(["nm", "--defined-only", os.path.join(out, "fe_dropin.o")],
-                          capture_output=True, text=True).stdout
-    for name in ("nblist", "forces", "cnonbondnl", "pme_calc", "charge_grid",
-                 "integrate_vverlet", "integrate_nhc", "pbc_all", "kinet"):
-        assert re.search(rf"\bT {name}\b", syms), name
-    need = subprocess.run(["nm", "-u", os.path.join(out, "fe_dropin.o")], capture_output=True,
-                          text=True).stdout
-    assert "fe_forces" in need and "fe_box_create" in need
+    forms = {
+        "md": ("nblist", "forces", "cnonbondnl", "pme_calc", "charge_grid", "pme_init",
+               "pme_clean", "fillspline", "integrate_vverlet", "integrate_nhc", "pbc_all",
+               "kinet", "drift", "isokin", "swap_box"),
+        "mc": ("forces_mc", "enbnd_mc", "ewald_kspace_mc", "ewald_rspace_mc", "nblist_pivot",
+               "drift"),
+    }
+    for form, names in forms.items():
+        assert os.path.exists(os.path.join(out, form, "spidey_gpu")), form
+        obj = os.path.join(out, form, "fe_dropin.o")
+        syms = subprocess.run(["nm", "--defined-only", obj], capture_output=True, text=True).stdout
+        for name in names:
+            assert re.search(rf"\bT {name}\b", syms), (form, name)
+        need = subprocess.run(["nm", "-u", obj], capture_output=True, text=True).stdout
+        assert "fe_box_create" in need
+    need_md = subprocess.run(["nm", "-u", os.path.join(out, "md", "fe_dropin.o")],
+                             capture_output=True, text=True).stdout
+    assert "fe_forces" in need_md and "fe_drift" in need_md and "fe_bspline" in need_md
+    need_mc = subprocess.run(["nm", "-u", os.path.join(out, "mc", "fe_dropin.o")],
+                             capture_output=True, text=True).stdout
+    assert "fe_mc_delta_terms" in need_mc and "fe_mc_site_energy" in need_mc

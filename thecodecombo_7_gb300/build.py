@@ -29,7 +29,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "--expt-relaxed-constexpr", "-I", CSRC, "-I", INCLUDE]
 # translation unit -> extra flags
 UNITS = {
-    "fe_api.cu": [],
+    "fe_api.cu": ["-Xcompiler", "-ffp-contract=off"],
     "k_nblist.cu": ["-fmad=false"],
     "k_pair64.cu": ["-fmad=false"],
     "k_spme.cu": ["-fmad=false"],

@@ -903,6 +903,44 @@ int fe_mc_site_energy(fe_box *box, int lb, int ub, double *terms6) {
   return mc_terms(&box->b, lb, ub, nullptr, terms6);
 }
 
+// pme_spline.c:10-49: cardinal B-spline weights array[1..order] and their
+// derivatives darray[1..order] at fraction w, by the same recursion (and
+// operation order) as the reference; host arithmetic (the kernels have their
+// own device copies of it).
+int fe_bspline(int order, double w, double *array, double *darray) {
+  if (order < 3 || order > 16 || !array || !darray) {
+    set_error("fe_bspline: order in 3..16 and two arrays of order + 1 doubles");
+    return FE_ERR_ARG;
+  }
+  for (int i = 3; i <= order; i++) array[i] = 0.0;
+  array[2] = w;
+  array[1] = 1.0 - w;
+  array[0] = 0.0;
+  for (int i = 3; i <= order - 1; i++) {
+    double div = (double)(1.0 / (i - 1));
+    array[i] = div * w * array[i - 1];
+    double di = (double)(i);
+    for (int j = 1; j <= (i - 2); j++) {
+      double dj = (double)(j);
+      array[i - j] = div * ((w + dj) * array[i - j - 1] + (di - dj - w) * array[i - j]);
+    }
+    array[1] *= div * (1.0 - w);
+  }
+  darray[0] = 0.0;
+  darray[1] = -array[1];
+  for (int i = 2; i <= order; i++) darray[i] = array[i - 1] - array[i];
+  int kk = order;
+  double div = (double)(1.0 / (kk - 1));
+  array[kk] = div * w * array[kk - 1];
+  double dkk = (double)(kk);
+  for (int i = 1; i <= (kk - 2); i++) {
+    double di = (double)(i);
+    array[kk - i] = div * ((w + di) * array[kk - i - 1] + (dkk - di - w) * array[kk - i]);
+  }
+  array[1] *= div * (1.0 - w);
+  return FE_OK;
+}
+
 int fe_drift(fe_box *box) {
   if (!box) return FE_ERR_ARG;
   return launch_drift(&box->b);

@@ -57,6 +57,7 @@ EXPORTS = [
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
     "fe_go_get_stream", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
     "fe_mc_delta_terms", "fe_mc_site_energy", "fe_drift", "fe_box_set_temperature",
+    "fe_bspline",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
