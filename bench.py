@@ -73,6 +73,71 @@ def profile_traffic():
     return None
 
 
+class NvmlSampler:
+    """SM clock and clock-event reasons read through NVML (libnvidia-ml, read
+    only) every millisecond from a thread, so that timed regions shorter than
+    nvidia-smi's sampling period still get samples."""
+
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown",
+               0x40: "hw_thermal_slowdown", 0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, device: int):
+        import ctypes as C
+        import threading
+        self.C = C
+        self.samples = []
+        self.stop_ev = threading.Event()
+        self.thread = None
+        self.ok = False
+        try:
+            lib = C.CDLL("libnvidia-ml.so.1")
+            if lib.nvmlInit_v2() != 0:
+                return
+            h = C.c_void_p()
+            if lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(device), C.byref(h)) != 0:
+                return
+            self.lib, self.h = lib, h
+            mx = C.c_uint()
+            self.max_mhz = (float(mx.value) if lib.nvmlDeviceGetMaxClockInfo(h, 1, C.byref(mx)) == 0
+                            else None)
+            self.reasons_fn = getattr(lib, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+                getattr(lib, "nvmlDeviceGetCurrentClocksThrottleReasons")
+            self.ok = True
+        except (OSError, AttributeError):
+            self.ok = False
+
+    def _run(self):
+        C = self.C
+        clk = C.c_uint()
+        rs = C.c_ulonglong()
+        while not self.stop_ev.is_set():
+            if self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(clk)) == 0:
+                r = rs.value if self.reasons_fn(self.h, C.byref(rs)) == 0 else 0
+                self.samples.append((float(clk.value), int(r)))
+            time.sleep(0.001)
+
+    def start(self):
+        if self.ok:
+            import threading
+            self.thread = threading.Thread(target=self._run, daemon=True)
+            self.thread.start()
+
+    def stop(self):
+        if not self.ok or self.thread is None:
+            return None
+        self.stop_ev.set()
+        self.thread.join()
+        if not self.samples:
+            return None
+        reasons = set()
+        for _, r in self.samples:
+            for bit, nm in self.REASONS.items():
+                if r & bit:
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(c for c, _ in self.samples), "sm_max_mhz": self.max_mhz,
+                "samples": len(self.samples), "reasons": sorted(reasons), "source": "nvml 1 ms"}
+
+
 class ClockSampler:
     """nvidia-smi clocks and throttle reasons sampled during the timed region."""
 
@@ -254,13 +319,27 @@ def drift_study(local, n_mol, equil_steps, nve_steps, fp64=True, seed=SEED + 9):
     integrator scales as dt^2; drift from the force field's cutoffs does not."""
     from thecodecombo_7_gb300 import engine, systems
     s = systems.water_box(n_mol, density=0.1, seed=seed, r_switch=R_SWITCH)
-    out = {"sites": s.n, "equilibration": f"{equil_steps} NHC steps at 300 K (mixed)"}
+    nfree = 3 * s.n - 3
+    RG = 8.31441e-3  # kJ/mol/K
+    chunk = 500
+    out = {"sites": s.n,
+           "equilibration": f"{equil_steps} steps (mixed): NVE in chunks of {chunk} with the "
+                            "velocities rescaled to 300 K after each (the reference's isokin), "
+                            f"then {equil_steps // 4} Nose-Hoover steps at 300 K"}
     with engine.Box(s, precision=engine.FE_PREC_MIXED, device=local) as b:
         b.nblist()
         b.forces()
         b.kinet()
-        rec = b.run_md(equil_steps, first_step=1, use_nhc=True, record=True)
-        out["T_end_K"] = float(2.0 * rec[-1, 0] / ((3 * s.n - 3) * 8.31441e-3))
+        step = 1
+        for _ in range(max(equil_steps // chunk, 1)):
+            b.run_md(chunk, first_step=step, record=False)
+            step += chunk
+            kin, _ = b.kinet()
+            v, u = b.get_velocities()
+            f = np.sqrt(s.T / (2.0 * kin / (nfree * RG)))
+            b.set_velocities(v * f, u * f)
+        rec = b.run_md(equil_steps // 4, first_step=step, use_nhc=True, record=True)
+        out["T_end_K"] = float(2.0 * rec[-1, 0] / (nfree * RG))
         pos, nop = b.get_positions(), b.get_positions_nopbc()
         vel, _ = b.get_velocities()
     precs = [("mixed", engine.FE_PREC_MIXED)] + ([("fp64", engine.FE_PREC_FP64)] if fp64 else [])
@@ -526,7 +605,9 @@ def run_ours(args, world, rank, local):
     first = W + 1
     nl = sysm.nlist_freq
     clocks = ClockSampler(local)
+    nvml = NvmlSampler(local)
     clocks.start()
+    nvml.start()
     barrier(world)
     torch.cuda.synchronize()
     ev0 = torch.cuda.Event(enable_timing=True)
@@ -538,6 +619,9 @@ def run_ours(args, world, rank, local):
     torch.cuda.synchronize()
     barrier(world)
     clk = clocks.stop()
+    clk_nvml = nvml.stop()
+    if clk_nvml and (clk.get("samples") or 0) < 3:
+        clk = dict(clk_nvml, nvidia_smi_samples=clk.get("samples"))
     ms = ev0.elapsed_time(ev1)
     ms_max = allreduce_max(ms, world)
     value = world * n * K / (ms_max / 1000.0)
@@ -666,7 +750,7 @@ def run_ours(args, world, rank, local):
                      ("mc", lambda: mc_sample(local)), ("go_replicas", lambda: go_sample(local)),
                      ("config0_fp64", lambda: config0_sample(local)),
                      ("nve_drift_4095", lambda: drift_study(local, 1365, 20000, 10000)),
-                     ("nve_drift_96000", lambda: drift_study(local, N_MOL, 10000, 10000,
+                     ("nve_drift_96000", lambda: drift_study(local, N_MOL, 8000, 10000,
                                                              fp64=False))):
         try:
             extras[name] = fn()
@@ -726,7 +810,15 @@ def main():
     ap.add_argument("--steps", type=int, default=2500)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--drift-study", type=int, default=0, metavar="NVE_STEPS",
+                    help="only the NVE drift study of the 4,095-site box, NVE_STEPS steps at "
+                         "dt (twice as many at dt/2), FP64 and mixed; prints one JSON line")
     args = ap.parse_args()
+    if args.drift_study:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps({"nve_drift_4095": drift_study(0, 1365, 40000, args.drift_study)}))
+        return
     world, rank, local = dist_setup() if args.impl == "ours" else (
         int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("RANK", "0")), 0)
     if args.impl == "reference":
