@@ -136,3 +136,46 @@ def test_delayed_acceptance_chain_replay(trained):
             pos = pos_new
     assert acc == n_acc > 0
     assert np.array_equal(xyz, pos)
+
+
+def _mc_energy(s, pos):
+    """The chains' energy function at pos: classic-Ewald reciprocal (kmax 7)
+    + real space + shifted LJ of all pairs minus the intramolecular
+    correction, from the FP64 engine (the self energy is a constant)."""
+    from thecodecombo_7_gb300 import engine
+    with engine.Box(s, precision=engine.FE_PREC_FP64) as b:
+        b.set_positions(pos)
+        b.mc_setup(kmax=7)
+        t = b.mc_site_energy(0, s.n)
+    return t[0] + (t[1] - t[2]) + (t[3] - t[5])
+
+
+def test_delayed_acceptance_samples_the_exact_distribution(trained):
+    """64 exact-dE chains and 64 delayed-acceptance chains started from the
+    same equilibrated configuration, 40,000 moves each (about 30 moves per
+    molecule): the mean and the variance of the energy of their final states
+    agree within their statistical errors (4 standard errors for the means,
+    an F ratio inside [0.45, 2.2] for the variances).  Delayed acceptance
+    keeps the Boltzmann distribution of the exact energy, only its acceptance
+    per move is lower."""
+    s, box, net, train, held, hist = trained
+    # equilibrate one exact chain from the random start
+    box.mc_chains_setup(nchains=1, kmax=7, T=T, seed=2024)
+    box.mc_chains_run(300000)
+    x0, _, _ = box.mc_chains_state(0)
+    u = {}
+    for mode, seed in ((0, 501), (1, 502)):
+        box.set_positions(x0)
+        box.mc_chains_setup(nchains=64, kmax=7, T=T, seed=seed)
+        if mode:
+            box.mc_chains_set_surrogate(net)
+            box.mc_chains_set_mode(1)
+        box.mc_chains_run(40000)
+        u[mode] = np.array([_mc_energy(s, box.mc_chains_state(c)[0]) for c in range(64)])
+    m0, m1 = u[0].mean(), u[1].mean()
+    v0, v1 = u[0].var(ddof=1), u[1].var(ddof=1)
+    se = np.sqrt(v0 / 64 + v1 / 64)
+    print(f"<U> exact {m0:.2f} +- {np.sqrt(v0 / 64):.2f}, delayed {m1:.2f} +- "
+          f"{np.sqrt(v1 / 64):.2f} kJ/mol; Var ratio {v1 / v0:.3f}")
+    assert abs(m1 - m0) <= 4.0 * se
+    assert 0.45 <= v1 / v0 <= 2.2

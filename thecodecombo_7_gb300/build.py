@@ -35,10 +35,10 @@ UNITS = {
     "k_spme.cu": ["-fmad=false"],
     "k_integrate.cu": ["-fmad=false"],
     "k_mc.cu": ["-fmad=false"],
-    "k_mixed.cu": [],
+    "k_mixed.cu": ["-ftz=true"],
     "k_noalloc.cu": [],
     "k_replica.cu": ["-fmad=false"],
-    "k_mcrun.cu": [],
+    "k_mcrun.cu": ["-ftz=true"],
     "k_mlp.cu": [],
     "k_go.cu": [],
     "k_peaks.cu": [],

@@ -51,7 +51,7 @@ struct MccParams {
   float sLf[3];      // L / 2^32 per axis
   double sLd[3];
   float rc2, rce2, kappa, fconv;
-  float ron2, sw_den;  // LJ switch (ron2 = 0: the reference's shift, lj[2])
+  float ron2, inv_sw_den;  // LJ switch (ron2 = 0: the reference's shift, lj[2])
   double beta;       // 1 / kT [mol/kJ], kT = RG T / 1000 (read_sim.c:351)
   double delta;      // translation (u - 0.5) * delta per axis (mcmove_displ.c:92-94)
   double rot_max;    // rotation angle in [-rot_max, rot_max] about the centre of mass
@@ -138,7 +138,7 @@ __device__ __forceinline__ float mcc_pair(const MccParams &P, float r2, float qq
     float elj = lj[0] * (sr6 * sr6 - 2.f * sr6) - lj[2];
     if (r2 > P.ron2 && P.ron2 > 0.f) {
       float c = P.rc2 - r2;
-      elj *= c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) / P.sw_den;
+      elj *= c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) * P.inv_sw_den;
     }
     e += elj;
   }
@@ -741,7 +741,7 @@ static int mcc_setup(Box *b, int nchains, const int *mol_first, int nmol, int km
   {
     double ron2 = b->p.r_switch > 0.0 ? b->p.r_switch * b->p.r_switch : 0.0;
     P.ron2 = (float)ron2;
-    P.sw_den = (float)((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2));
+    P.inv_sw_den = (float)(1.0 / ((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2)));
   }
   P.kappa = (float)b->p.kappa;
   P.fconv = (float)fconv;

@@ -490,7 +490,7 @@ constexpr int kPairGrab = 2;  // rows a warp takes from the row counter at a tim
 struct MxPair {
   int n, nt, cap;
   float rc2, kappa, c2k, qfe;  // c2k = 2 kappa / sqrt(pi); qfe = QFACTOR / epsRF
-  float ron2, sw_den;
+  float ron2, inv_sw_den;  // switch start^2 and 1 / (rc^2 - ron^2)^3
   float3 sc;                   // L / 2^32 per axis
   // inner list: radius^2 (rc + skin)^2, and the squared displacement that
   // forces a prune ((skin / 2)^2, less a rounding margin)
@@ -548,8 +548,8 @@ __device__ __forceinline__ void mx_pair_core(const MxPair &P, float qi, int j, i
     if (P.ron2 > 0.f) {
       if (r2 > P.ron2) {
         float c = P.rc2 - r2;
-        float sw = c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) / P.sw_den;
-        float dsw = 12.f * c * (r2 - P.ron2) / P.sw_den;
+        float sw = c * c * (P.rc2 + 2.f * r2 - 3.f * P.ron2) * P.inv_sw_den;
+        float dsw = 12.f * c * (r2 - P.ron2) * P.inv_sw_den;
         flj = flj * sw + elj * dsw;
         elj = elj * sw;
       }
@@ -1563,7 +1563,7 @@ int launch_mx_pair_only(Box *b) {
   double ron2 = b->p.r_switch > 0.0 ? b->p.r_switch * b->p.r_switch : 0.0;
   double rc2 = b->p.rc * b->p.rc;
   P.ron2 = (float)ron2;
-  P.sw_den = ron2 > 0.0 ? (float)((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2)) : 0.f;
+  P.inv_sw_den = ron2 > 0.0 ? (float)(1.0 / ((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2))) : 0.f;
   P.sc = fix_scale(b);
   size_t shm = sizeof(float) * (b->nt * b->nt * 3);
   double rp = b->p.rc + M.skin, hs = 0.5 * M.skin - 1e-4;
