@@ -1,0 +1,62 @@
+"""A single box of the water workload stepped on the GPU, for timing and for
+profiling one kernel at a time (a small driver: it builds only the box it
+is asked for).
+
+    python -m thecodecombo_7_gb300.workloads [--molecules 32000] [--precision mixed]
+        [--steps 30] [--warmup 10] [--switch 8.0]
+
+Builds the seeded 3-site water box (0.1 sites/A^3, SPME grid ~1 point/A),
+picks the pair kernel's launch shape, runs the warm-up steps, then the timed
+steps of the production loop (list every 10 steps) with CUDA events, and
+prints one JSON line: ms per step and the mean device time of the pair,
+spreading and list kernels re-launched on the final state.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+
+from . import engine, systems
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--molecules", type=int, default=32000)
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--switch", type=float, default=8.0)
+    ap.add_argument("--seed", type=int, default=2025)
+    a = ap.parse_args(argv)
+    import torch
+    s = systems.water_box(a.molecules, density=0.1, seed=a.seed, r_switch=a.switch)
+    prec = engine.FE_PREC_MIXED if a.precision == "mixed" else engine.FE_PREC_FP64
+    stream = torch.cuda.Stream()
+    out = {"sites": s.n, "precision": a.precision, "grid": list(s.grid)}
+    with engine.Box(s, precision=prec) as b:
+        b.set_stream(stream.cuda_stream)
+        b.nblist()
+        b.forces()
+        b.kinet()
+        if prec == engine.FE_PREC_MIXED:
+            out["launch_shape"] = b.autotune()
+        b.run_md(a.warmup, first_step=1, record=False)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run_md(a.steps, first_step=a.warmup + 1, record=False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out["ms_per_step"] = e0.elapsed_time(e1) / a.steps
+        out["atom_steps_per_s"] = s.n * a.steps / (e0.elapsed_time(e1) * 1e-3)
+        for name, k in (("pair", engine.FE_KERNEL_PAIR), ("spread", engine.FE_KERNEL_SPREAD),
+                        ("list", engine.FE_KERNEL_LIST)):
+            out[f"{name}_us"] = b.time_kernel(k, reps=10)
+        out["list_entries"], out["max_row"] = b.list_stats()
+        if prec == engine.FE_PREC_MIXED:
+            out["inner_entries"] = b.inner_list_stats()[0]
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()
