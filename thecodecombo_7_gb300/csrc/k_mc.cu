@@ -302,11 +302,11 @@ int mc_terms(Box *b, int lb, int ub, const double *new_pos_host, double *terms) 
     set_error("fe_mc: site range outside the box");
     return FE_ERR_ARG;
   }
-  if (m > kMcMaxMoved) {
+  const bool delta = new_pos_host != nullptr;
+  if (delta && m > kMcMaxMoved) {
     set_error("fe_mc_delta: at most 64 sites per move");
     return FE_ERR_SIZE;
   }
-  const bool delta = new_pos_host != nullptr;
   double h[6];
   if (delta) {
     FE_CUDA(cudaMemcpyAsync(b->mc_newpos, new_pos_host, sizeof(double) * 3 * m,
@@ -342,7 +342,7 @@ int mc_terms(Box *b, int lb, int ub, const double *new_pos_host, double *terms) 
   P.ub = ub;
   long total = (long)m * b->n;
   int pb = (int)((total + 255) / 256);
-  if (pb > 1024) pb = 1024;
+  if (pb > 2048) pb = 2048;  // partial slots: kMaxPartialBlocks / 2
   double *part = b->mc_part + kMaxPartialBlocks * kPartialTerms / 2;
   if (delta)
     k_mc_pairs<true><<<pb, 256, 0, b->stream>>>(P, b->pos_q, b->type, b->mc_newpos, b->lj_eps,
