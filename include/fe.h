@@ -368,6 +368,14 @@ int fe_batch_get_stream(fe_batch *batch, void **stream);
 /* Own kernel launches in one step graph: [plain, list, exchange, list+exchange];
  * -1 for a variant not captured yet. */
 int fe_batch_step_launches(fe_batch *batch, int *launches4);
+/* Fused stepping (the default when every box is mixed precision with
+ * molecules as contiguous runs of sites): each kernel of the step runs once
+ * for all boxes, box r owning a contiguous range of its blocks, and the
+ * charge grids of boxes of equal shape are transformed by one batched FFT;
+ * list rebuilds stay per box.  on = 0 steps every box on its own stream
+ * (one graph branch per box).  Results are the same either way (fixed-point
+ * sums).  FE_ERR_ARG when on = 1 and a box does not allow it. */
+int fe_batch_set_fused(fe_batch *batch, int on);
 
 /* ---- batched replica exchange of Go-model chains ------------------------ */
 

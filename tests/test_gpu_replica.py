@@ -128,3 +128,46 @@ def test_batch_mixed_equals_single_boxes():
     for (p1, v1), (p2, v2) in zip(alone, together):
         assert np.array_equal(p1, p2)
         assert np.array_equal(v1, v2)
+
+
+def test_fused_batch_matches_box_by_box():
+    """The fused step (each kernel once for every box, batched FFTs per grid
+    shape) against the box-by-box graph on the same mixed-precision boxes of
+    uneven sizes and grids: Nose-Hoover steps with list rebuilds and replica
+    exchanges; the same slots and temperatures, positions to 1e-6 A (the
+    batched FFT may round differently in the last bit; forces are fixed-point
+    sums either way)."""
+    from thecodecombo_7_gb300 import engine, systems
+    specs = [(1365, 300.0), (2000, 310.0), (1365, 320.0), (2600, 330.0), (2000, 340.0)]
+    ss = [systems.water_box(n, density=0.1, seed=60 + k, T=T, r_switch=8.0)
+          for k, (n, T) in enumerate(specs)]
+    for s in ss:
+        s.nlist_freq = 10
+    out = {}
+    for fused in (False, True):
+        boxes = [engine.Box(s, precision=engine.FE_PREC_MIXED) for s in ss]
+        try:
+            for b in boxes:
+                b.nblist()
+                b.forces()
+            batch = engine.Batch(boxes, seed=5)
+            batch.set_fused(fused)
+            batch.run(40, nlist_freq=10, swap_freq=10, first_step=1, use_nhc=True)
+            st = batch.state()
+            out[fused] = (st, [(b.get_positions(), b.get_velocities()[0]) for b in boxes],
+                          batch.step_launches())
+            batch.close()
+        finally:
+            for b in boxes:
+                b.close()
+    (s0, x0, l0), (s1, x1, l1) = out[False], out[True]
+    assert np.array_equal(s0["slot_box"], s1["slot_box"])
+    assert np.array_equal(s0["T_box"], s1["T_box"])
+    assert st["attempts"] == 4
+    for (p0, v0), (p1, v1), s in zip(x0, x1, ss):
+        d = p1 - p0
+        d -= s.L * np.round(d / s.L)
+        assert np.abs(d).max() < 1e-6
+        assert np.abs(v1 - v0).max() < 1e-4 * np.abs(v0).max()
+    # one launch per kernel for all boxes: far fewer than box by box
+    assert 0 < l1[0] <= 20 and l1[0] < l0[0]

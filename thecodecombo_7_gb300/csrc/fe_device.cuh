@@ -11,6 +11,29 @@
 
 namespace fe {
 
+// A block's view of the grid it works in: its index and the block count of
+// its box.  A launch over one box is the whole grid; a launch over many boxes
+// (replica batches) gives each box a contiguous range of blocks and each
+// block finds its box from the range table, so one kernel body serves both.
+struct VBlk {
+  int id, n;
+};
+__device__ __forceinline__ VBlk vblk_self() { return {(int)blockIdx.x, (int)gridDim.x}; }
+// box r of this block in a many-box launch: off[r] <= blockIdx.x < off[r + 1]
+__device__ __forceinline__ int vblk_box(const int *__restrict__ off, int nbox) {
+  int lo = 0, hi = nbox, b = (int)blockIdx.x;
+  while (hi - lo > 1) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(off + mid) <= b) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+__device__ __forceinline__ VBlk vblk_of(const int *__restrict__ off, int r) {
+  int o = __ldg(off + r);
+  return {(int)blockIdx.x - o, __ldg(off + r + 1) - o};
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
@@ -21,7 +44,8 @@ __device__ __forceinline__ double warp_sum(double v) {
 // partials[blockIdx.x * kPartialTerms + t].  blockDim.x must be a multiple
 // of 32 and at most 1024.
 template <int NT>
-__device__ __forceinline__ void block_partials(double (&v)[NT], double *partials) {
+__device__ __forceinline__ void block_partials(double (&v)[NT], double *partials,
+                                               VBlk vb = vblk_self()) {
   __shared__ double sh[32][NT];
   int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
 #pragma unroll
@@ -36,7 +60,7 @@ __device__ __forceinline__ void block_partials(double (&v)[NT], double *partials
     for (int t = 0; t < NT; t++) {
       double s = lane < nw ? sh[lane][t] : 0.0;
       s = warp_sum(s);
-      if (lane == 0) partials[blockIdx.x * kPartialTerms + t] = s;
+      if (lane == 0) partials[vb.id * kPartialTerms + t] = s;
     }
   }
 }
@@ -47,19 +71,20 @@ __device__ __forceinline__ void block_partials(double (&v)[NT], double *partials
 // entry and left 0 on exit.  blockDim.x <= 256.
 template <int NT>
 __device__ __forceinline__ bool block_partials_final(double (&v)[NT], double *partials,
-                                                     unsigned *ticket, double *out) {
-  block_partials<NT>(v, partials);  // thread 0 writes this block's partials
+                                                     unsigned *ticket, double *out,
+                                                     VBlk vb = vblk_self()) {
+  block_partials<NT>(v, partials, vb);  // thread 0 writes this block's partials
   __shared__ bool last;
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) last = atomicAdd(ticket, 1u) == (unsigned)vb.n - 1;
   __syncthreads();
   if (!last) return false;
   __threadfence();
   __shared__ double red[256];
   for (int t = 0; t < NT; t++) {
     double s = 0.0;
-    for (int b = threadIdx.x; b < (int)gridDim.x; b += blockDim.x)
+    for (int b = threadIdx.x; b < vb.n; b += blockDim.x)
       s += ((volatile double *)partials)[b * kPartialTerms + t];
     for (int i = threadIdx.x; i < 256; i += blockDim.x) red[i] = 0.0;
     __syncthreads();
@@ -135,12 +160,12 @@ __device__ __forceinline__ void block_fix_add(const T (&v)[NT], int shift,
 template <int NT, typename T>
 __device__ __forceinline__ bool block_fix_final(const T (&v)[NT], int shift,
                                                 unsigned long long *acc, unsigned *ticket,
-                                                double *out) {
+                                                double *out, VBlk vb = vblk_self()) {
   __shared__ bool last_blk;
   block_fix_add<NT>(v, shift, acc);
   __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) last_blk = atomicAdd(ticket, 1u) == gridDim.x - 1;
+  if (threadIdx.x == 0) last_blk = atomicAdd(ticket, 1u) == (unsigned)vb.n - 1;
   __syncthreads();
   if (!last_blk) return false;
   __threadfence();
@@ -170,6 +195,58 @@ __device__ __forceinline__ double ref_erfc(double x) {
                      t * (-0.82215223 + t * 0.17087277)))))))));
   if (x < 0) return 2.0 - v;
   return v;
+}
+
+// The mixed path's partial sums combined into the reference's slots (the
+// pair, exclusion / intramolecular and bonded sums of k_mixed.cu).
+__device__ __forceinline__ void mixed_slots_dev(double *__restrict__ s, double erfc_rc_over_rc,
+                                                int fused) {
+  if (fused) {
+    for (int t = 0; t < 5; t++) s[SC_MX_EXCL + t] = s[SC_MX_INTRA + t];
+    s[SC_BOND] = s[SC_MX_INTRA + 5];
+    s[SC_BEND] = s[SC_MX_INTRA + 6];
+  }
+  s[SC_LJ] = s[SC_MX_PAIR + 0] + s[SC_MX_EXCL + 0];
+  s[SC_LJS] = s[SC_MX_PAIR + 1] + s[SC_MX_EXCL + 1];
+  s[SC_REAL] = s[SC_MX_PAIR + 2] + s[SC_MX_EXCL + 2];
+  s[SC_REALS] = (s[SC_MX_PAIR + 3] + s[SC_MX_EXCL + 3]) * erfc_rc_over_rc;
+  s[SC_INTRA] = s[SC_MX_EXCL + 4];
+}
+
+// energy[8] of cnonbondnl (cnonbond_nblist.c:613-620), pme_calc's energy[3]
+// (pme_calc.c:99-101) and, with_bonded, en[k] of forces() (forces.c:172-219)
+__device__ __forceinline__ void assemble_dev(double *__restrict__ s, double fan, double sewald,
+                                             int with_bonded) {
+  double ek0 = s[SC_ENREC] * fan;
+  double ek1 = sewald;
+  double ek2 = ek0 - ek1;
+  s[SC_ENERGY3 + 0] = ek0;
+  s[SC_ENERGY3 + 1] = ek1;
+  s[SC_ENERGY3 + 2] = ek2;
+  double er0 = s[SC_REAL], er1 = s[SC_REAL] - s[SC_REALS], er2 = s[SC_INTRA];
+  double e[8];
+  e[0] = s[SC_LJ] + er0 - er2 + ek2;
+  e[1] = e[0] - s[SC_LJS];
+  e[2] = er0 + ek2 - er2;
+  e[3] = er0 - er1;
+  e[4] = ek0;
+  e[5] = ek1;
+  e[6] = er2;
+  e[7] = er0;
+  for (int k = 0; k < 8; k++) s[SC_ENERGY8 + k] = e[k];
+  if (with_bonded) {
+    s[FE_EN_BOND] = s[SC_BOND];
+    s[FE_EN_BEND] = s[SC_BEND];
+    s[FE_EN_NBOND] = e[0];
+    s[FE_EN_NBONDS] = e[1];
+    s[FE_EN_COULOMB] = e[2];
+    s[FE_EN_TEWALD] = e[2];
+    s[FE_EN_REWALD] = e[7];
+    s[FE_EN_REWALDS] = e[3];
+    s[FE_EN_KEWALD] = e[4];
+    s[FE_EN_SEWALD] = e[5];
+    s[FE_EN_IEWALD] = e[6];
+  }
 }
 
 // qa * qb * QFACTOR in the reference's evaluation order (QFACTOR is an

@@ -160,6 +160,27 @@ struct Box {
   McChains *mcc = nullptr;     // device-resident Monte Carlo chains (k_mcrun.cu)
 };
 
+// Per-box arguments of the batched integrator kernels (k_integrate.cu): a
+// replica batch keeps one per box in device memory.
+struct BIntArgs {
+  int n, nhc_M;
+  double dt, dt_h, nhc_Q, nfree;
+  double3 L, H;
+  const double *mass, *imass100;
+  double *ff, *vv, *uu, *nopbc;
+  double4 *pos;
+  double *zeta, *scal;
+  unsigned long long *facc;
+  unsigned *ticket;
+  int *status;
+  double *rec;
+  long rec_cap;
+  int *rec_counter;
+  // energy assembly of forces()
+  double fan, sewald, erfc_rc_over_rc;
+  int mixed, mixed_fused;
+};
+
 // ---- error plumbing ----
 void set_error(const std::string &msg);
 int cuda_fail(cudaError_t e, const char *what);
@@ -207,6 +228,16 @@ int launch_kinet(Box *b);
 int launch_vv2_kinet(Box *b, double vscal);  // vv2 with the kinetic tensor folded in
 int launch_nhc(Box *b, double time_step);
 int launch_record(Box *b);
+// batched step, integrator side (every box of a batch per launch)
+BIntArgs make_bint_args(Box *b);
+void mixed_bint_fields(Box *b, BIntArgs *a);  // k_mixed.cu
+int launch_b_kinet_nhc(const BIntArgs *A, const int *off, int nbox, int blocks, cudaStream_t s);
+int launch_b_vv1(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
+                 cudaStream_t s);
+int launch_b_vv2(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
+                 cudaStream_t s);
+int launch_b_scale_kinet(const BIntArgs *A, const int *off, int nbox, int blocks,
+                         cudaStream_t s);
 // one MD step of the box on its stream (nve_md.c:359-418 / nvt_md.c:529-531)
 int step_body(Box *b, bool with_list, bool use_nhc);
 // packed xyz (3n doubles) <-> the double4 positions, on the box's stream

@@ -93,5 +93,10 @@ void mixed_counts(Box *b, const int **lj, const int **rest);  // device row coun
 void mixed_inner_counts(Box *b, const int **lj, const int **rest, bool *on);
 MxPruneState *mixed_prune_state(Box *b);
 void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaStream_t s);
+// replica batches: the force evaluation of every box in one launch per kernel
+struct BMxPlan;
+int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out);
+int mixed_batch_forces(BMxPlan *plan, cudaStream_t s);
+void mixed_batch_free(BMxPlan *plan);
 
 }  // namespace fe

@@ -4,6 +4,8 @@
 // forces.c:204-219), velocity Verlet (integrate_vverlet.c:36-103) with
 // pbc_all (pbc_all.c:23-88), kinet (kinet.c:18-68) and the Nose-Hoover chain
 // (integrate_nhc.c:40-161).  Compiled with -fmad=false.
+#include <cstring>
+
 #include "fe_device.cuh"
 
 namespace fe {
@@ -58,36 +60,7 @@ int launch_apply_pme(Box *b) {
 // energy[8] of cnonbondnl and en[k] of forces()
 __global__ void k_assemble(double *__restrict__ s, double fan, double sewald, int with_bonded) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
-  double ek0 = s[SC_ENREC] * fan;  // pme_calc.c:99-101
-  double ek1 = sewald;
-  double ek2 = ek0 - ek1;
-  s[SC_ENERGY3 + 0] = ek0;
-  s[SC_ENERGY3 + 1] = ek1;
-  s[SC_ENERGY3 + 2] = ek2;
-  double er0 = s[SC_REAL], er1 = s[SC_REAL] - s[SC_REALS], er2 = s[SC_INTRA];
-  double e[8];
-  e[0] = s[SC_LJ] + er0 - er2 + ek2;  // cnonbond_nblist.c:613-620
-  e[1] = e[0] - s[SC_LJS];
-  e[2] = er0 + ek2 - er2;
-  e[3] = er0 - er1;
-  e[4] = ek0;
-  e[5] = ek1;
-  e[6] = er2;
-  e[7] = er0;
-  for (int k = 0; k < 8; k++) s[SC_ENERGY8 + k] = e[k];
-  if (with_bonded) {
-    s[FE_EN_BOND] = s[SC_BOND];  // forces.c:172-219
-    s[FE_EN_BEND] = s[SC_BEND];
-    s[FE_EN_NBOND] = e[0];
-    s[FE_EN_NBONDS] = e[1];
-    s[FE_EN_COULOMB] = e[2];
-    s[FE_EN_TEWALD] = e[2];
-    s[FE_EN_REWALD] = e[7];
-    s[FE_EN_REWALDS] = e[3];
-    s[FE_EN_KEWALD] = e[4];
-    s[FE_EN_SEWALD] = e[5];
-    s[FE_EN_IEWALD] = e[6];
-  }
+  assemble_dev(s, fan, sewald, with_bonded);
 }
 
 int launch_assemble_energies(Box *b, int with_bonded) {
@@ -348,9 +321,8 @@ int launch_kinet(Box *b) {
 // integrate_nhc.c:57-147 (Nc = Nys = 1, w[0] = 1): the chain, one thread.
 // The temperature is read from s[SC_TEMP] so that replica exchanges can
 // change it on the device between graph replays.
-__global__ void k_nhc_chain(int M, double Q, double nfree, double time_step,
-                            double *__restrict__ zeta, double *__restrict__ s) {
-  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+__device__ __forceinline__ void nhc_chain_dev(int M, double Q, double nfree, double time_step,
+                                              double *__restrict__ zeta, double *__restrict__ s) {
   double T = s[SC_TEMP];
 #define ZR(j) zeta[3 * (j)]
 #define ZV(j) zeta[3 * (j) + 1]
@@ -383,6 +355,12 @@ __global__ void k_nhc_chain(int M, double Q, double nfree, double time_step,
 #undef ZR
 #undef ZV
 #undef ZG
+}
+
+__global__ void k_nhc_chain(int M, double Q, double nfree, double time_step,
+                            double *__restrict__ zeta, double *__restrict__ s) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  nhc_chain_dev(M, Q, nfree, time_step, zeta, s);
 }
 
 // integrate_nhc.c:152-159
@@ -452,6 +430,216 @@ int launch_xyz_scatter(Box *b, const double *xyz, bool to_pos, bool to_nopbc) {
 int launch_xyz_gather(Box *b, double *xyz) {
   k_xyz_gather<<<(b->n + 255) / 256, 256, 0, b->stream>>>(b->n, b->pos_q, xyz);
   FE_LAUNCH_CHECK("k_xyz_gather");
+  return FE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Integrator kernels of a batched step: every box of a replica batch in one
+// launch per kernel (blocks of box r: off[r] .. off[r+1]-1).  The arithmetic
+// is that of the single-box kernels above, site for site; the Nose-Hoover
+// velocity scale is applied inside the next per-site pass instead of in a
+// launch of its own, and the energy assembly rides on the second half kick.
+
+__device__ __forceinline__ void kinet_scalars(double *__restrict__ s) {
+  double f = (0.125) * (kNA * kAU * 10.0);  // kinet.c:50-65
+  for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
+  s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
+}
+
+__device__ __forceinline__ void record_dev(const double *__restrict__ s, double *__restrict__ rec,
+                                           long cap, int *__restrict__ counter) {
+  int c = *counter;
+  if (c < cap)
+    for (int t = 0; t < FE_EN_COUNT; t++) rec[(long)c * FE_EN_COUNT + t] = s[t];
+  *counter = c + 1;
+}
+
+// kinet (fixed point, as k_kinet_fix) and the first Nose-Hoover chain update
+__global__ void k_b_kinet_nhc(const BIntArgs *__restrict__ A, const int *__restrict__ off,
+                              int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BIntArgs &a = A[r];
+  const VBlk vb = vblk_of(off, r);
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n; i += vb.n * blockDim.x) {
+    double fac = a.mass[i];
+    double sx = a.vv[3 * i] + a.uu[3 * i];
+    double sy = a.vv[3 * i + 1] + a.uu[3 * i + 1];
+    double sz = a.vv[3 * i + 2] + a.uu[3 * i + 2];
+    k[0] += fac * sx * sx;
+    k[1] += fac * sy * sx;
+    k[2] += fac * sy * sy;
+    k[3] += fac * sz * sx;
+    k[4] += fac * sz * sy;
+    k[5] += fac * sz * sz;
+  }
+  if (block_fix_final<6>(k, 20, a.facc, a.ticket, a.scal + SC_KEN, vb) && threadIdx.x == 0) {
+    kinet_scalars(a.scal);
+    nhc_chain_dev(a.nhc_M, a.nhc_Q, a.nfree, a.dt, a.zeta, a.scal);
+  }
+}
+
+// [Nose-Hoover velocity scale, integrate_nhc.c:152-159] then the first half
+// kick, drift and pbc_all (integrate_vverlet.c:54-83, vscal = 1)
+__global__ void k_b_vv1(const BIntArgs *__restrict__ A, const int *__restrict__ off, int nbox,
+                        int nhc) {
+  const int r = vblk_box(off, nbox);
+  const BIntArgs &a = A[r];
+  const VBlk vb = vblk_of(off, r);
+  int i = vb.id * blockDim.x + threadIdx.x;
+  if (i >= a.n) return;
+  double v[3];
+  for (int c = 0; c < 3; c++) v[c] = a.vv[3 * i + c];
+  if (nhc) {
+    double scale = a.scal[SC_NHC_SCALE];
+    for (int c = 0; c < 3; c++) {
+      v[c] = v[c] * scale;
+      a.uu[3 * i + c] = a.uu[3 * i + c] * scale;
+    }
+  }
+  double imass = a.imass100[i];
+  for (int c = 0; c < 3; c++) {
+    v[c] = 1.0 * (v[c] + a.dt_h * imass * a.ff[3 * i + c]);
+    a.vv[3 * i + c] = v[c];
+  }
+  double ddx = a.dt * v[0], ddy = a.dt * v[1], ddz = a.dt * v[2];
+  a.nopbc[3 * i] += ddx;
+  a.nopbc[3 * i + 1] += ddy;
+  a.nopbc[3 * i + 2] += ddz;
+  double4 p = a.pos[i];
+  p.x += ddx;
+  p.y += ddy;
+  p.z += ddz;
+  int bad = 0;
+  p.x = pbc_wrap(p.x, a.H.x, a.L.x, &bad);
+  p.y = pbc_wrap(p.y, a.H.y, a.L.y, &bad);
+  p.z = pbc_wrap(p.z, a.H.z, a.L.z, &bad);
+  if (bad) atomicOr(a.status, ST_PBC_LOOP);
+  a.pos[i] = p;
+}
+
+// the energy assembly of forces() (block 0), the second half kick with uu =
+// vv and the kinetic tensor; then either the record (NVE) or the second
+// chain update (NHC)
+__global__ void k_b_vv2(const BIntArgs *__restrict__ A, const int *__restrict__ off, int nbox,
+                        int nhc) {
+  const int r = vblk_box(off, nbox);
+  const BIntArgs &a = A[r];
+  const VBlk vb = vblk_of(off, r);
+  if (vb.id == 0 && threadIdx.x == 0) {
+    if (a.mixed) mixed_slots_dev(a.scal, a.erfc_rc_over_rc, a.mixed_fused);
+    assemble_dev(a.scal, a.fan, a.sewald, 1);
+  }
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n; i += vb.n * blockDim.x) {
+    double imass = a.imass100[i];
+    double v[3];
+    for (int c = 0; c < 3; c++) {
+      v[c] = (a.vv[3 * i + c] + 1.0 * a.dt_h * imass * a.ff[3 * i + c]);
+      a.vv[3 * i + c] = v[c];
+      a.uu[3 * i + c] = v[c];
+    }
+    double fac = a.mass[i];
+    double sx = v[0] + v[0], sy = v[1] + v[1], sz = v[2] + v[2];
+    k[0] += fac * sx * sx;
+    k[1] += fac * sy * sx;
+    k[2] += fac * sy * sy;
+    k[3] += fac * sz * sx;
+    k[4] += fac * sz * sy;
+    k[5] += fac * sz * sz;
+  }
+  if (block_fix_final<6>(k, 20, a.facc, a.ticket, a.scal + SC_KEN, vb) && threadIdx.x == 0) {
+    kinet_scalars(a.scal);
+    if (nhc) nhc_chain_dev(a.nhc_M, a.nhc_Q, a.nfree, a.dt, a.zeta, a.scal);
+    else record_dev(a.scal, a.rec, a.rec_cap, a.rec_counter);
+  }
+}
+
+// NHC: the second velocity scale, kinet of the scaled velocities and the record
+__global__ void k_b_scale_kinet(const BIntArgs *__restrict__ A, const int *__restrict__ off,
+                                int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BIntArgs &a = A[r];
+  const VBlk vb = vblk_of(off, r);
+  double scale = a.scal[SC_NHC_SCALE];
+  double k[6] = {0, 0, 0, 0, 0, 0};
+  for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n; i += vb.n * blockDim.x) {
+    double v[3], u[3];
+    for (int c = 0; c < 3; c++) {
+      v[c] = a.vv[3 * i + c] * scale;
+      u[c] = a.uu[3 * i + c] * scale;
+      a.vv[3 * i + c] = v[c];
+      a.uu[3 * i + c] = u[c];
+    }
+    double fac = a.mass[i];
+    double sx = v[0] + u[0], sy = v[1] + u[1], sz = v[2] + u[2];
+    k[0] += fac * sx * sx;
+    k[1] += fac * sy * sx;
+    k[2] += fac * sy * sy;
+    k[3] += fac * sz * sx;
+    k[4] += fac * sz * sy;
+    k[5] += fac * sz * sz;
+  }
+  if (block_fix_final<6>(k, 20, a.facc, a.ticket, a.scal + SC_KEN, vb) && threadIdx.x == 0) {
+    kinet_scalars(a.scal);
+    record_dev(a.scal, a.rec, a.rec_cap, a.rec_counter);
+  }
+}
+
+BIntArgs make_bint_args(Box *b) {
+  BIntArgs a;
+  memset(&a, 0, sizeof a);
+  a.n = b->n;
+  a.nhc_M = b->nhc_M;
+  a.dt = b->p.dt;
+  a.dt_h = 0.5 * b->p.dt;
+  a.nhc_Q = b->nhc_Q;
+  a.nfree = b->nfree;
+  a.L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
+  a.H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);
+  a.mass = b->mass;
+  a.imass100 = b->imass100;
+  a.ff = b->ff;
+  a.vv = b->vv;
+  a.uu = b->uu;
+  a.nopbc = b->pos_nopbc;
+  a.pos = b->pos_q;
+  a.zeta = b->zeta;
+  a.scal = b->scal;
+  a.facc = b->facc;
+  a.ticket = b->ticket;
+  a.status = b->status;
+  a.rec = b->rec;
+  a.rec_cap = b->rec_cap;
+  a.rec_counter = b->rec_counter;
+  a.fan = 0.5 * kELEC * kELEQ * kELEQ * kNA * 1.0E-3 / b->p.epsRF;
+  a.sewald = b->sewald;
+  a.mixed = b->mx != nullptr;
+  mixed_bint_fields(b, &a);
+  return a;
+}
+
+int launch_b_kinet_nhc(const BIntArgs *A, const int *off, int nbox, int blocks, cudaStream_t s) {
+  k_b_kinet_nhc<<<blocks, 256, 0, s>>>(A, off, nbox);
+  FE_LAUNCH_CHECK("k_b_kinet_nhc");
+  return FE_OK;
+}
+int launch_b_vv1(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
+                 cudaStream_t s) {
+  k_b_vv1<<<blocks, 256, 0, s>>>(A, off, nbox, nhc);
+  FE_LAUNCH_CHECK("k_b_vv1");
+  return FE_OK;
+}
+int launch_b_vv2(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
+                 cudaStream_t s) {
+  k_b_vv2<<<blocks, 256, 0, s>>>(A, off, nbox, nhc);
+  FE_LAUNCH_CHECK("k_b_vv2");
+  return FE_OK;
+}
+int launch_b_scale_kinet(const BIntArgs *A, const int *off, int nbox, int blocks,
+                         cudaStream_t s) {
+  k_b_scale_kinet<<<blocks, 256, 0, s>>>(A, off, nbox);
+  FE_LAUNCH_CHECK("k_b_scale_kinet");
   return FE_OK;
 }
 

@@ -33,7 +33,9 @@
 // counter) with coalesced entry loads; the row's FP32 partial sums are added
 // over the warp in a fixed butterfly and converted once to the fixed-point
 // accumulators (2^32 per kJ/mol/A) -- deterministic.
+#include <algorithm>
 #include <climits>
+#include <cstring>
 #include <cmath>
 #include <vector>
 
@@ -134,11 +136,11 @@ __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ p
 // per step: sorted fixed-point coordinates and charge; with `snap`, also the
 // largest squared displacement (A^2) of any site since the inner list was
 // last pruned (float bits, atomicMax: non-negative floats order as integers)
-__global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *__restrict__ perm,
+__device__ __forceinline__ void k_mx_convert_body(VBlk vb_, int n, const double4 *__restrict__ pos, const int *__restrict__ perm,
                              double3 invL, int4 *__restrict__ posfx,
                              const int4 *__restrict__ snap, float3 sc,
                              unsigned *__restrict__ dmax2) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = vb_.id * blockDim.x + threadIdx.x;
   float d2 = 0.f;
   if (s < n) {
     double4 p = pos[perm[s]];
@@ -158,6 +160,13 @@ __global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *
     for (int o = 16; o; o >>= 1) d2 = fmaxf(d2, __shfl_xor_sync(0xffffffffu, d2, o));
     if ((threadIdx.x & 31) == 0 && d2 > 0.f) atomicMax(dmax2, __float_as_uint(d2));
   }
+}
+
+__global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *__restrict__ perm,
+                             double3 invL, int4 *__restrict__ posfx,
+                             const int4 *__restrict__ snap, float3 sc,
+                             unsigned *__restrict__ dmax2) {
+  k_mx_convert_body(vblk_self(), n, pos, perm, invL, posfx, snap, sc, dmax2);
 }
 
 __device__ __forceinline__ int mx_is_excluded(const int *__restrict__ xs, const int *__restrict__ xp,
@@ -645,8 +654,7 @@ __device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float
 // prune is due.  The plain variant walks the inner rows (nothing when the
 // PRUNE variant ran), finishes the energies and clears the state.
 template <int NW, int RW, bool PRUNE>
-__global__ void __launch_bounds__(NW * 32, RW / NW)
-k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
+__device__ __forceinline__ void k_mx_pair_body(VBlk vb_, MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
           const int *__restrict__ perm, const int *__restrict__ cnt_lj,
           const int *__restrict__ cnt_nl, const int *__restrict__ ent,
           int *__restrict__ icnt_lj, int *__restrict__ icnt_nl, int *__restrict__ ient,
@@ -665,7 +673,7 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   __syncthreads();
   int lane = threadIdx.x & 31;
   unsigned lt = (1u << lane) - 1u;
-  if (PRUNE && P.inner_on && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&ps->prunes, 1ull);
+  if (PRUNE && P.inner_on && vb_.id == 0 && threadIdx.x == 0) atomicAdd(&ps->prunes, 1ull);
   const int *rlj = PRUNE ? cnt_lj : icnt_lj;
   const int *rnl = PRUNE ? cnt_nl : icnt_nl;
   const int *rent = PRUNE ? ent : ient;
@@ -742,11 +750,24 @@ k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type
   }
   // the last block: both variants have read the prune state and every row
   // has been taken, clear both
-  if (block_fix_final<4>(eq, 32, facc, ticket, out) && threadIdx.x == 0) {
+  if (block_fix_final<4>(eq, 32, facc, ticket, out, vb_) && threadIdx.x == 0) {
     ps->need = 0;
     ps->dmax2 = 0u;
     ps->next_row = 0;
   }
+}
+
+template <int NW, int RW, bool PRUNE>
+__global__ void __launch_bounds__(NW * 32, RW / NW)
+k_mx_pair(MxPair P, const int4 *__restrict__ posfx, const int *__restrict__ type_s,
+          const int *__restrict__ perm, const int *__restrict__ cnt_lj,
+          const int *__restrict__ cnt_nl, const int *__restrict__ ent,
+          int *__restrict__ icnt_lj, int *__restrict__ icnt_nl, int *__restrict__ ient,
+          int4 *__restrict__ snap, MxPruneState *__restrict__ ps,
+          const float *__restrict__ lj_tab, unsigned long long *__restrict__ fix,
+          unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+          double *__restrict__ out, int *__restrict__ status) {
+  k_mx_pair_body<NW, RW, PRUNE>(vblk_self(), P, posfx, type_s, perm, cnt_lj, cnt_nl, ent, icnt_lj, icnt_nl, ient, snap, ps, lj_tab, fix, facc, ticket, out, status);
 }
 
 // qq (1 - erfc(kappa r)) / r of an excluded pair in double-float, from the
@@ -943,10 +964,10 @@ __device__ __forceinline__ void fillspline_f(int order, float w, float *array, f
 // weights, binning
 // B-spline weights and derivatives of every site and its integer spline
 // origin (floor of u G, exact from the 32-bit fraction)
-__global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ posfx,
+__device__ __forceinline__ void k_mx_splines_body(VBlk vb_, int n, int order, int3 G, const int4 *__restrict__ posfx,
                              int *__restrict__ floor3, float *__restrict__ sm,
                              float *__restrict__ sd) {
-  int s = blockIdx.x * blockDim.x + threadIdx.x;
+  int s = vb_.id * blockDim.x + threadIdx.x;
   if (s >= n) return;
   int4 p = posfx[s];
   unsigned u[3] = {(unsigned)p.x, (unsigned)p.y, (unsigned)p.z};
@@ -964,6 +985,12 @@ __global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ 
   }
 }
 
+__global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ posfx,
+                             int *__restrict__ floor3, float *__restrict__ sm,
+                             float *__restrict__ sd) {
+  k_mx_splines_body(vblk_self(), n, order, G, posfx, floor3, sm, sd);
+}
+
 // Spreading by fixed-point reductions: thread (site, mx) adds the
 // contributions q wx wy wz of its site's spline slab mx (order x order
 // points) to a 64-bit fixed-point grid (2^40 per unit) with fire-and-forget
@@ -973,10 +1000,10 @@ __global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ 
 constexpr float kSpRedFix = 1099511627776.0f;  // 2^40
 constexpr double kSpRedUnfix = 1.0 / 1099511627776.0;
 
-__global__ void k_mx_spread_red(int n, int order, int3 G, const int4 *__restrict__ posfx,
+__device__ __forceinline__ void k_mx_spread_red_body(VBlk vb_, int n, int order, int3 G, const int4 *__restrict__ posfx,
                                 const float *__restrict__ sm, const int *__restrict__ floor3,
                                 unsigned long long *__restrict__ gfix) {
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  int t = vb_.id * blockDim.x + threadIdx.x;
   int s = t / order, mx = t - s * order;
   if (s >= n) return;
   const float *w = sm + (size_t)s * order * 3;
@@ -998,31 +1025,42 @@ __global__ void k_mx_spread_red(int n, int order, int3 G, const int4 *__restrict
   }
 }
 
+__global__ void k_mx_spread_red(int n, int order, int3 G, const int4 *__restrict__ posfx,
+                                const float *__restrict__ sm, const int *__restrict__ floor3,
+                                unsigned long long *__restrict__ gfix) {
+  k_mx_spread_red_body(vblk_self(), n, order, G, posfx, sm, floor3, gfix);
+}
+
 // FP32 grid from the fixed-point sums; the sums are cleared for the next step
 // (two points per thread and iteration: 16-byte loads and stores)
-__global__ void k_mx_fix2grid(long K, unsigned long long *__restrict__ gfix,
+__device__ __forceinline__ void k_mx_fix2grid_body(VBlk vb_, long K, unsigned long long *__restrict__ gfix,
                               float *__restrict__ grid) {
   const long K2 = K >> 1;
   longlong2 *g2 = reinterpret_cast<longlong2 *>(gfix);
   float2 *o2 = reinterpret_cast<float2 *>(grid);
-  for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < K2;
-       i += (long)gridDim.x * blockDim.x) {
+  for (long i = (long)vb_.id * blockDim.x + threadIdx.x; i < K2;
+       i += (long)vb_.n * blockDim.x) {
     longlong2 v = g2[i];
     o2[i] = make_float2((float)((double)v.x * kSpRedUnfix), (float)((double)v.y * kSpRedUnfix));
     g2[i] = make_longlong2(0, 0);
   }
-  if ((K & 1) && blockIdx.x == 0 && threadIdx.x == 0) {
+  if ((K & 1) && vb_.id == 0 && threadIdx.x == 0) {
     grid[K - 1] = (float)((double)(long long)gfix[K - 1] * kSpRedUnfix);
     gfix[K - 1] = 0ull;
   }
 }
 
-__global__ void k_mx_recip(long Kh, const float *__restrict__ eterm, const float *__restrict__ kw,
+__global__ void k_mx_fix2grid(long K, unsigned long long *__restrict__ gfix,
+                              float *__restrict__ grid) {
+  k_mx_fix2grid_body(vblk_self(), K, gfix, grid);
+}
+
+__device__ __forceinline__ void k_mx_recip_body(VBlk vb_, long Kh, const float *__restrict__ eterm, const float *__restrict__ kw,
                            cufftComplex *__restrict__ gk, unsigned long long *__restrict__ facc,
                            unsigned *__restrict__ ticket, double *__restrict__ out) {
   float e = 0.f;
-  for (long h = (long)blockIdx.x * blockDim.x + threadIdx.x; h < Kh;
-       h += (long)gridDim.x * blockDim.x) {
+  for (long h = (long)vb_.id * blockDim.x + threadIdx.x; h < Kh;
+       h += (long)vb_.n * blockDim.x) {
     cufftComplex v = gk[h];
     float et = eterm[h];
     e = fmaf(kw[h] * et, v.x * v.x + v.y * v.y, e);
@@ -1031,10 +1069,16 @@ __global__ void k_mx_recip(long Kh, const float *__restrict__ eterm, const float
     gk[h] = v;
   }
   float vv[1] = {e};
-  block_fix_final<1>(vv, 24, facc, ticket, out);
+  block_fix_final<1>(vv, 24, facc, ticket, out, vb_);
 }
 
-__global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
+__global__ void k_mx_recip(long Kh, const float *__restrict__ eterm, const float *__restrict__ kw,
+                           cufftComplex *__restrict__ gk, unsigned long long *__restrict__ facc,
+                           unsigned *__restrict__ ticket, double *__restrict__ out) {
+  k_mx_recip_body(vblk_self(), Kh, eterm, kw, gk, facc, ticket, out);
+}
+
+__device__ __forceinline__ void k_mx_gather_body(VBlk vb_, int n, int order, int3 G, float3 gl, float qfe,
                             const int4 *__restrict__ posfx, const int *__restrict__ perm,
                             const int *__restrict__ floor3, const float *__restrict__ sm,
                             const float *__restrict__ sd, const float *__restrict__ grid,
@@ -1042,7 +1086,7 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
                             unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                             double *__restrict__ out) {
   long long sx = 0, sy = 0, sz = 0;
-  for (int s = blockIdx.x * blockDim.x + threadIdx.x; s < n; s += gridDim.x * blockDim.x) {
+  for (int s = vb_.id * blockDim.x + threadIdx.x; s < n; s += vb_.n * blockDim.x) {
     float fxi = 0.f, fyi = 0.f, fzi = 0.f;
     const float *m = sm + (size_t)s * order * 3;
     const float *dm = sd + (size_t)s * order * 3;
@@ -1078,18 +1122,33 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
     sz += qz;
   }
   long long v[3] = {sx, sy, sz};
-  block_fix_final<3>(v, 0, facc, ticket, out);
+  block_fix_final<3>(v, 0, facc, ticket, out, vb_);
+}
+
+__global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
+                            const int4 *__restrict__ posfx, const int *__restrict__ perm,
+                            const int *__restrict__ floor3, const float *__restrict__ sm,
+                            const float *__restrict__ sd, const float *__restrict__ grid,
+                            unsigned long long *__restrict__ fix,
+                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+                            double *__restrict__ out) {
+  k_mx_gather_body(vblk_self(), n, order, G, gl, qfe, posfx, perm, floor3, sm, sd, grid, fix, facc, ticket, out);
 }
 
 // FP64 forces from the fixed-point sums, minus the mean reciprocal force
-__global__ void k_mx_finalize(int n, const unsigned long long *__restrict__ fix,
+__device__ __forceinline__ void k_mx_finalize_body(VBlk vb_, int n, const unsigned long long *__restrict__ fix,
                               const double *__restrict__ scal, double *__restrict__ ff) {
   __shared__ double mean[3];
   if (threadIdx.x < 3) mean[threadIdx.x] = scal[SC_FMEAN + threadIdx.x] / kFixScale / (double)n;
   __syncthreads();
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = vb_.id * blockDim.x + threadIdx.x;
   if (i >= 3 * n) return;
   ff[i] = (double)(long long)fix[i] * (1.0 / kFixScale) - mean[i % 3];
+}
+
+__global__ void k_mx_finalize(int n, const unsigned long long *__restrict__ fix,
+                              const double *__restrict__ scal, double *__restrict__ ff) {
+  k_mx_finalize_body(vblk_self(), n, fix, scal, ff);
 }
 
 // All intramolecular terms of one molecule per thread: the exclusion
@@ -1120,7 +1179,7 @@ __device__ __forceinline__ void intra_add(float (&F)[NS][3], int a, float x, flo
 // NS: the largest molecule (sites) of the box, so that the molecule's
 // positions and forces stay in registers
 template <int NS>
-__global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
+__device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *__restrict__ mol_first,
                            const int *__restrict__ mol_x, const int *__restrict__ mol_xi,
                            const int *__restrict__ mol_b, const int *__restrict__ mol_bi,
                            const int *__restrict__ mol_a, const int *__restrict__ mol_ai,
@@ -1138,7 +1197,7 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
                            double *__restrict__ out) {
   float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, eb = 0.f, ea = 0.f;
   long long q_intra = 0;
-  for (int m = blockIdx.x * blockDim.x + threadIdx.x; m < nmol; m += gridDim.x * blockDim.x) {
+  for (int m = vb_.id * blockDim.x + threadIdx.x; m < nmol; m += vb_.n * blockDim.x) {
     const int lb = mol_first[m], ns = mol_first[m + 1] - lb;
     int4 P[NS];
     float F[NS][3];
@@ -1242,22 +1301,33 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
   }
   long long v[7] = {to_fixed(e_lj, 32), to_fixed(e_ljs, 32), to_fixed(e_real, 32),
                     to_fixed(qsum, 32), q_intra, to_fixed(eb, 32), to_fixed(ea, 32)};
-  block_fix_final<7>(v, 32, facc, ticket, out);
+  block_fix_final<7>(v, 32, facc, ticket, out, vb_);
+}
+
+template <int NS>
+__global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
+                           const int *__restrict__ mol_x, const int *__restrict__ mol_xi,
+                           const int *__restrict__ mol_b, const int *__restrict__ mol_bi,
+                           const int *__restrict__ mol_a, const int *__restrict__ mol_ai,
+                           const int *__restrict__ ab, const int *__restrict__ flag,
+                           const int *__restrict__ bond_ab, const double *__restrict__ bond_req,
+                           const double *__restrict__ bond_k, const int *__restrict__ bend_abc,
+                           const double *__restrict__ bend_t0, const double *__restrict__ bend_k,
+                           const int4 *__restrict__ posfx, const int *__restrict__ iperm,
+                           const int *__restrict__ type, float3 sL, int nt,
+                           const float *__restrict__ lj_tab, float rc2, float kappa, float c2k,
+                           float qf, float epsRF, const double4 *__restrict__ pos_q,
+                           const float2 *__restrict__ exptab, DfIntra D,
+                           unsigned long long *__restrict__ fix,
+                           unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+                           double *__restrict__ out) {
+  k_mx_intra_body<NS>(vblk_self(), nmol, mol_first, mol_x, mol_xi, mol_b, mol_bi, mol_a, mol_ai, ab, flag, bond_ab, bond_req, bond_k, bend_abc, bend_t0, bend_k, posfx, iperm, type, sL, nt, lj_tab, rc2, kappa, c2k, qf, epsRF, pos_q, exptab, D, fix, facc, ticket, out);
 }
 
 // combine the mixed kernels' sums into the reference's slots
 __global__ void k_mx_slots(double *__restrict__ s, double erfc_rc_over_rc, int fused) {
   if (threadIdx.x != 0) return;
-  if (fused) {
-    for (int t = 0; t < 5; t++) s[SC_MX_EXCL + t] = s[SC_MX_INTRA + t];
-    s[SC_BOND] = s[SC_MX_INTRA + 5];
-    s[SC_BEND] = s[SC_MX_INTRA + 6];
-  }
-  s[SC_LJ] = s[SC_MX_PAIR + 0] + s[SC_MX_EXCL + 0];
-  s[SC_LJS] = s[SC_MX_PAIR + 1] + s[SC_MX_EXCL + 1];
-  s[SC_REAL] = s[SC_MX_PAIR + 2] + s[SC_MX_EXCL + 2];
-  s[SC_REALS] = (s[SC_MX_PAIR + 3] + s[SC_MX_EXCL + 3]) * erfc_rc_over_rc;
-  s[SC_INTRA] = s[SC_MX_EXCL + 4];
+  mixed_slots_dev(s, erfc_rc_over_rc, fused);
 }
 
 // ---------------------------------------------------------------------------
@@ -1549,7 +1619,7 @@ static int pair_blocks(Box *b, int nw) {
   return blocks > 2048 ? 2048 : blocks;
 }
 
-int launch_mx_pair_only(Box *b) {
+MxPair mx_pair_params(Box *b) {
   Mixed &M = *b->mx;
   MxPair P;
   P.n = b->n;
@@ -1565,11 +1635,17 @@ int launch_mx_pair_only(Box *b) {
   P.ron2 = (float)ron2;
   P.inv_sw_den = ron2 > 0.0 ? (float)(1.0 / ((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2))) : 0.f;
   P.sc = fix_scale(b);
-  size_t shm = sizeof(float) * (b->nt * b->nt * 3);
   double rp = b->p.rc + M.skin, hs = 0.5 * M.skin - 1e-4;
   P.rp2 = (float)(rp * rp);
   P.thresh2 = (float)(hs * hs);
   P.inner_on = M.inner_on ? 1 : 0;
+  return P;
+}
+
+int launch_mx_pair_only(Box *b) {
+  Mixed &M = *b->mx;
+  MxPair P = mx_pair_params(b);
+  size_t shm = sizeof(float) * (b->nt * b->nt * 3);
   int nw = M.tune_nw, blocks = M.tune_blocks > 0 ? M.tune_blocks : pair_blocks(b, nw);
 #define FE_PAIR_ARGS                                                                          \
   P, M.posfx, M.type_s, M.perm, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl, M.ient, M.snap, \
@@ -1742,6 +1818,396 @@ int forces_mixed(Box *b) {
   k_mx_finalize<<<(3 * n + 255) / 256, 256, 0, b->stream>>>(n, M.fix, b->scal, b->ff);
   FE_LAUNCH_CHECK("k_mx_finalize");
   return launch_mixed_assemble(b);
+}
+
+// ---------------------------------------------------------------------------
+// Replica batches: every box's force evaluation in one launch per kernel.
+// Box r of a launch owns blocks off[r] .. off[r+1]-1 and runs the same kernel
+// body as its own launch would, on its own buffers (the per-box arguments
+// are kept in device memory); its reductions finish in its own last block.
+// The grids of boxes of equal shape sit side by side so that one batched
+// cuFFT plan transforms them all.
+
+struct BMxArgs {
+  int n, nt, nmol, order;
+  const double4 *pos;
+  const int *perm, *iperm, *type, *type_s;
+  double3 invL;
+  int4 *posfx;
+  int4 *snap;
+  float3 sc;
+  MxPruneState *ps;
+  unsigned long long *fix, *facc;
+  unsigned *ticket;
+  double *scal;
+  int *status;
+  // pair
+  MxPair P;
+  const int *cnt_lj, *cnt_nl, *ent;
+  int *icnt_lj, *icnt_nl, *ient;
+  const float *lj_tab;
+  // intramolecular
+  const int *mol_first, *mol_x, *mol_xi, *mol_b, *mol_bi, *mol_a, *mol_ai, *excl_ab, *excl_flag;
+  const int *bond_ab, *bend_abc;
+  const double *bond_req, *bond_k, *bend_t0, *bend_k;
+  float rc2, kappa, c2k, qf, epsRF;
+  const float2 *exptab;
+  DfIntra D;
+  // SPME
+  int3 G;
+  long K, Kh;
+  int *floor3;
+  float *sm, *sd;
+  unsigned long long *gfix;
+  float *grid32;
+  cufftComplex *grid32k;
+  const float *eterm32, *kw32;
+  float3 gl;
+  float qfe;
+  double *ff;
+};
+
+__global__ void k_b_mx_convert(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                               int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  const VBlk vb = vblk_of(off, r);
+  int s = vb.id * blockDim.x + threadIdx.x;
+  if (s < a.n) {  // the force sums start from zero (forces_mixed's memset)
+    a.fix[3 * s] = 0ull;
+    a.fix[3 * s + 1] = 0ull;
+    a.fix[3 * s + 2] = 0ull;
+  }
+  k_mx_convert_body(vb, a.n, a.pos, a.perm, a.invL, a.posfx,
+                    a.P.inner_on ? a.snap : nullptr, a.sc, &a.ps->dmax2);
+}
+
+template <bool PRUNE>
+__global__ void __launch_bounds__(256, PRUNE ? 4 : 6)
+k_b_mx_pair(const BMxArgs *__restrict__ A, const int *__restrict__ off, int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_pair_body<8, PRUNE ? 32 : 48, PRUNE>(
+      vblk_of(off, r), a.P, a.posfx, a.type_s, a.perm, a.cnt_lj, a.cnt_nl, a.ent, a.icnt_lj,
+      a.icnt_nl, a.ient, a.snap, a.ps, a.lj_tab, a.fix, a.facc, a.ticket, a.scal + SC_MX_PAIR,
+      a.status);
+}
+
+template <int NS>
+__global__ void k_b_mx_intra(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                             int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_intra_body<NS>(vblk_of(off, r), a.nmol, a.mol_first, a.mol_x, a.mol_xi, a.mol_b, a.mol_bi,
+                      a.mol_a, a.mol_ai, a.excl_ab, a.excl_flag, a.bond_ab, a.bond_req, a.bond_k,
+                      a.bend_abc, a.bend_t0, a.bend_k, a.posfx, a.iperm, a.type, a.sc, a.nt,
+                      a.lj_tab, a.rc2, a.kappa, a.c2k, a.qf, a.epsRF, a.pos, a.exptab, a.D, a.fix,
+                      a.facc, a.ticket, a.scal + SC_MX_INTRA);
+}
+
+__global__ void k_b_mx_splines(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                               int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_splines_body(vblk_of(off, r), a.n, a.order, a.G, a.posfx, a.floor3, a.sm, a.sd);
+}
+
+__global__ void k_b_mx_spread(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                              int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_spread_red_body(vblk_of(off, r), a.n, a.order, a.G, a.posfx, a.sm, a.floor3, a.gfix);
+}
+
+__global__ void k_b_mx_fix2grid(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                                int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_fix2grid_body(vblk_of(off, r), a.K, a.gfix, a.grid32);
+}
+
+__global__ void k_b_mx_recip(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                             int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_recip_body(vblk_of(off, r), a.Kh, a.eterm32, a.kw32, a.grid32k, a.facc, a.ticket,
+                  a.scal + SC_ENREC);
+}
+
+__global__ void k_b_mx_gather(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                              int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_gather_body(vblk_of(off, r), a.n, a.order, a.G, a.gl, a.qfe, a.posfx, a.perm, a.floor3,
+                   a.sm, a.sd, a.grid32, a.fix, a.facc, a.ticket, a.scal + SC_FMEAN);
+}
+
+__global__ void k_b_mx_finalize(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                                int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_finalize_body(vblk_of(off, r), a.n, a.fix, a.scal, a.ff);
+}
+
+struct BMxGroup {
+  int G[3];
+  int count = 0;
+  float *real = nullptr;
+  cufftComplex *cplx = nullptr;
+  cufftHandle r2c = 0, c2r = 0;
+  bool plans = false;
+};
+
+// block offsets of one kernel over the batch (device copy)
+struct BMxRange {
+  int *d_off = nullptr;
+  int total = 0;
+};
+
+struct BMxPlan {
+  int nbox = 0;
+  BMxArgs *d_args = nullptr;
+  BMxRange convert, prune, pair, intra, splines, spread, fix2grid, recip, gather, finalize;
+  int intra_ns = 3;
+  size_t pair_shm = 0;
+  std::vector<BMxGroup> groups;
+};
+
+static int bmx_range(BMxRange &R, const std::vector<int> &blocks) {
+  std::vector<int> off(blocks.size() + 1, 0);
+  for (size_t r = 0; r < blocks.size(); r++) off[r + 1] = off[r] + blocks[r];
+  R.total = off.back();
+  FE_CUDA(cudaMalloc(&R.d_off, sizeof(int) * off.size()));
+  FE_CUDA(cudaMemcpy(R.d_off, off.data(), sizeof(int) * off.size(), cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+
+void mixed_batch_free(BMxPlan *P) {
+  if (!P) return;
+  cudaFree(P->d_args);
+  BMxRange *rs[] = {&P->convert, &P->prune, &P->pair, &P->intra, &P->splines, &P->spread,
+                    &P->fix2grid, &P->recip, &P->gather, &P->finalize};
+  for (BMxRange *r : rs) cudaFree(r->d_off);
+  for (BMxGroup &g : P->groups) {
+    if (g.plans) {
+      cufftDestroy(g.r2c);
+      cufftDestroy(g.c2r);
+    }
+    cudaFree(g.real);
+    cudaFree(g.cplx);
+  }
+  delete P;
+}
+
+void mixed_bint_fields(Box *b, BIntArgs *a) {
+  if (!b->mx) return;
+  a->erfc_rc_over_rc = b->mx->erfc_rc_over_rc;
+  a->mixed_fused = b->mx->nmol > 0 ? 1 : 0;
+}
+
+// The batched force evaluation needs mixed-precision boxes whose molecules
+// are contiguous runs of sites (the fused intramolecular kernel); otherwise
+// FE_ERR_ARG and the batch steps box by box.
+int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
+  *out = nullptr;
+  for (int r = 0; r < nbox; r++)
+    if (!boxes[r]->mx || boxes[r]->mx->nmol == 0 || boxes[r]->mx->intra_maxs > kIntraMaxSites) {
+      set_error("batched force evaluation: mixed-precision boxes of contiguous molecules only");
+      return FE_ERR_ARG;
+    }
+  BMxPlan *P = new BMxPlan();
+  P->nbox = nbox;
+  std::vector<BMxArgs> args(nbox);
+  std::vector<int> bconv, bprune, bpair, bintra, bspl, bspr, bf2g, brec, bgat, bfin;
+  double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
+  int rc = FE_OK;
+  for (int r = 0; r < nbox && rc == FE_OK; r++) {
+    Box *b = boxes[r];
+    Mixed &M = *b->mx;
+    BMxArgs &a = args[r];
+    memset(&a, 0, sizeof a);
+    a.n = b->n;
+    a.nt = b->nt;
+    a.nmol = M.nmol;
+    a.order = b->order;
+    a.pos = b->pos_q;
+    a.perm = M.perm;
+    a.iperm = M.iperm;
+    a.type = b->type;
+    a.type_s = M.type_s;
+    a.invL = make_double3(1.0 / b->p.L[0], 1.0 / b->p.L[1], 1.0 / b->p.L[2]);
+    a.posfx = M.posfx;
+    a.snap = M.snap;
+    a.sc = fix_scale(b);
+    a.ps = M.ps;
+    a.fix = M.fix;
+    a.facc = b->facc;
+    a.ticket = b->ticket;
+    a.scal = b->scal;
+    a.status = b->status;
+    a.P = mx_pair_params(b);
+    a.cnt_lj = M.cnt_lj;
+    a.cnt_nl = M.cnt_nl;
+    a.ent = M.ent;
+    a.icnt_lj = M.icnt_lj;
+    a.icnt_nl = M.icnt_nl;
+    a.ient = M.ient;
+    a.lj_tab = M.lj_tab;
+    a.mol_first = M.mol_first;
+    a.mol_x = M.mol_x;
+    a.mol_xi = M.mol_xi;
+    a.mol_b = M.mol_b;
+    a.mol_bi = M.mol_bi;
+    a.mol_a = M.mol_a;
+    a.mol_ai = M.mol_ai;
+    a.excl_ab = M.excl_ab;
+    a.excl_flag = M.excl_flag;
+    a.bond_ab = b->bond_ab;
+    a.bend_abc = b->bend_abc;
+    a.bond_req = b->bond_req;
+    a.bond_k = b->bond_k;
+    a.bend_t0 = b->bend_t0;
+    a.bend_k = b->bend_k;
+    a.rc2 = (float)(b->p.rc * b->p.rc);
+    a.kappa = (float)b->p.kappa;
+    a.c2k = (float)(2.0 * b->p.kappa / sqrt(kPI));
+    a.qf = (float)qf;
+    a.epsRF = (float)b->p.epsRF;
+    a.exptab = M.exptab;
+    a.D = M.dfi;
+    a.G = make_int3(b->G[0], b->G[1], b->G[2]);
+    a.K = b->K;
+    a.Kh = b->Kh;
+    a.floor3 = M.floor3;
+    a.sm = M.sm;
+    a.sd = M.sd;
+    a.gfix = M.gfix;
+    a.eterm32 = M.eterm32;
+    a.kw32 = M.kw32;
+    a.gl = make_float3((float)(b->G[0] / b->p.L[0]), (float)(b->G[1] / b->p.L[1]),
+                       (float)(b->G[2] / b->p.L[2]));
+    a.qfe = (float)(qf / b->p.epsRF);
+    a.ff = b->ff;
+    // the grid of equal shapes side by side (the group buffers are set below)
+    int gi = -1;
+    for (size_t g = 0; g < P->groups.size(); g++)
+      if (P->groups[g].G[0] == b->G[0] && P->groups[g].G[1] == b->G[1] &&
+          P->groups[g].G[2] == b->G[2])
+        gi = (int)g;
+    if (gi < 0) {
+      P->groups.push_back(BMxGroup());
+      gi = (int)P->groups.size() - 1;
+      for (int d = 0; d < 3; d++) P->groups[gi].G[d] = b->G[d];
+    }
+    a.grid32 = reinterpret_cast<float *>((size_t)gi);                        // group index,
+    a.grid32k = reinterpret_cast<cufftComplex *>((size_t)P->groups[gi].count);  // slot in it
+    P->groups[gi].count++;
+    if (M.intra_maxs > P->intra_ns) P->intra_ns = M.intra_maxs;
+    size_t shm = sizeof(float) * (b->nt * b->nt * 3);
+    if (shm > P->pair_shm) P->pair_shm = shm;
+    int nsm = M.nsm > 0 ? M.nsm : 152;
+    bconv.push_back((b->n + 255) / 256);
+    bprune.push_back(std::max(1, std::min(4 * nsm, b->n / 160)));
+    bpair.push_back(std::max(1, std::min(2048, b->n / 80)));
+    bintra.push_back(std::min(2048, (M.nmol + 127) / 128));
+    bspl.push_back((b->n + 127) / 128);
+    bspr.push_back((int)(((long)b->n * b->order + 255) / 256));
+    bf2g.push_back((int)std::min<long>(8L * nsm, (b->K / 2 + 255) / 256 + 1));
+    brec.push_back((int)std::min<long>(1024L, (b->Kh + 255) / 256));
+    bgat.push_back(std::min(1024, (b->n + 127) / 128));
+    bfin.push_back((3 * b->n + 255) / 256);
+  }
+  // group buffers and batched plans; each box's grid points into its group
+  for (BMxGroup &g : P->groups) {
+    if (rc) break;
+    long K = (long)g.G[0] * g.G[1] * g.G[2], Kh = (long)g.G[0] * g.G[1] * (g.G[2] / 2 + 1);
+    if (cudaMalloc(&g.real, sizeof(float) * K * g.count) != cudaSuccess ||
+        cudaMalloc(&g.cplx, sizeof(cufftComplex) * Kh * g.count) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "batch grid buffers");
+      break;
+    }
+    int nn[3] = {g.G[0], g.G[1], g.G[2]};
+    cufftResult fr = cufftPlanMany(&g.r2c, 3, nn, nullptr, 1, (int)K, nullptr, 1, (int)Kh,
+                                   CUFFT_R2C, g.count);
+    if (fr == CUFFT_SUCCESS)
+      fr = cufftPlanMany(&g.c2r, 3, nn, nullptr, 1, (int)Kh, nullptr, 1, (int)K, CUFFT_C2R,
+                         g.count);
+    if (fr != CUFFT_SUCCESS) {
+      rc = cufft_fail(fr, "cufftPlanMany (batch)");
+      break;
+    }
+    g.plans = true;
+  }
+  if (rc == FE_OK)
+    for (int r = 0; r < nbox; r++) {
+      size_t gi = reinterpret_cast<size_t>(args[r].grid32);
+      size_t slot = reinterpret_cast<size_t>(args[r].grid32k);
+      BMxGroup &g = P->groups[gi];
+      long K = (long)g.G[0] * g.G[1] * g.G[2], Kh = (long)g.G[0] * g.G[1] * (g.G[2] / 2 + 1);
+      args[r].grid32 = g.real + slot * K;
+      args[r].grid32k = g.cplx + slot * Kh;
+    }
+  if (rc == FE_OK && cudaMalloc(&P->d_args, sizeof(BMxArgs) * nbox) != cudaSuccess)
+    rc = cuda_fail(cudaGetLastError(), "batch arguments");
+  if (rc == FE_OK &&
+      cudaMemcpy(P->d_args, args.data(), sizeof(BMxArgs) * nbox, cudaMemcpyHostToDevice) !=
+          cudaSuccess)
+    rc = cuda_fail(cudaGetLastError(), "batch arguments");
+  if (rc == FE_OK) rc = bmx_range(P->convert, bconv);
+  if (rc == FE_OK) rc = bmx_range(P->prune, bprune);
+  if (rc == FE_OK) rc = bmx_range(P->pair, bpair);
+  if (rc == FE_OK) rc = bmx_range(P->intra, bintra);
+  if (rc == FE_OK) rc = bmx_range(P->splines, bspl);
+  if (rc == FE_OK) rc = bmx_range(P->spread, bspr);
+  if (rc == FE_OK) rc = bmx_range(P->fix2grid, bf2g);
+  if (rc == FE_OK) rc = bmx_range(P->recip, brec);
+  if (rc == FE_OK) rc = bmx_range(P->gather, bgat);
+  if (rc == FE_OK) rc = bmx_range(P->finalize, bfin);
+  if (rc) {
+    mixed_batch_free(P);
+    return rc;
+  }
+  *out = P;
+  return FE_OK;
+}
+
+// One force evaluation of every box (forces_mixed for each, energies
+// assembled later by the batched second half kick).
+int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
+  const int nb = P->nbox;
+  k_b_mx_convert<<<P->convert.total, 256, 0, s>>>(P->d_args, P->convert.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_convert");
+  k_b_mx_pair<true><<<P->prune.total, 256, P->pair_shm, s>>>(P->d_args, P->prune.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_pair<prune>");
+  k_b_mx_pair<false><<<P->pair.total, 256, P->pair_shm, s>>>(P->d_args, P->pair.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_pair");
+  if (P->intra_ns <= 3) k_b_mx_intra<3><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
+  else if (P->intra_ns <= 4) k_b_mx_intra<4><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
+  else k_b_mx_intra<kIntraMaxSites><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_intra");
+  k_b_mx_splines<<<P->splines.total, 128, 0, s>>>(P->d_args, P->splines.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_splines");
+  k_b_mx_spread<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_spread");
+  k_b_mx_fix2grid<<<P->fix2grid.total, 256, 0, s>>>(P->d_args, P->fix2grid.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_fix2grid");
+  for (BMxGroup &g : P->groups) {
+    cufftResult r = cufftSetStream(g.r2c, s);
+    if (r == CUFFT_SUCCESS) r = cufftExecR2C(g.r2c, g.real, g.cplx);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C (batch)");
+  }
+  k_b_mx_recip<<<P->recip.total, 256, 0, s>>>(P->d_args, P->recip.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_recip");
+  for (BMxGroup &g : P->groups) {
+    cufftResult r = cufftSetStream(g.c2r, s);
+    if (r == CUFFT_SUCCESS) r = cufftExecC2R(g.c2r, g.cplx, g.real);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R (batch)");
+  }
+  k_b_mx_gather<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_gather");
+  k_b_mx_finalize<<<P->finalize.total, 256, 0, s>>>(P->d_args, P->finalize.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_finalize");
+  return FE_OK;
 }
 
 int launch_mixed_assemble(Box *b) {

@@ -26,6 +26,7 @@
 #include <vector>
 
 #include "fe_internal.h"
+#include "fe_mixed.h"
 #include "fe_rng.cuh"
 
 namespace fe {
@@ -57,6 +58,12 @@ struct Batch {
   cudaGraphExec_t g[4] = {nullptr, nullptr, nullptr, nullptr};  // bit 0 list, bit 1 exchange
   int launches[4] = {0, 0, 0, 0};
   int g_key = -1;
+  // fused step: every box in one launch per kernel (mixed-precision boxes)
+  bool fused = false;
+  BMxPlan *mx = nullptr;
+  BIntArgs *d_bint = nullptr;
+  int *d_off_red = nullptr, *d_off_site = nullptr;  // block ranges: reductions, per site
+  int tot_red = 0, tot_site = 0;
 };
 
 // Boltzmann energy in kJ/mol as read_sim.c:351 (sim.kT = RG * T * .001).
@@ -137,7 +144,79 @@ static int launch_exchange(Batch *B) {
   return FE_OK;
 }
 
+static void free_fused(Batch *B) {
+  if (B->mx) mixed_batch_free(B->mx);
+  B->mx = nullptr;
+  cudaFree(B->d_bint);
+  cudaFree(B->d_off_red);
+  cudaFree(B->d_off_site);
+  B->d_bint = nullptr;
+  B->d_off_red = B->d_off_site = nullptr;
+  B->fused = false;
+}
+
+// Sets up the fused step (all boxes per launch) when every box allows it.
+static int setup_fused(Batch *B) {
+  BMxPlan *plan = nullptr;
+  int rc = mixed_batch_plan(B->boxes.data(), B->R, &plan);
+  if (rc) return rc;
+  B->mx = plan;
+  std::vector<BIntArgs> args(B->R);
+  std::vector<int> ored(B->R + 1, 0), osite(B->R + 1, 0);
+  for (int r = 0; r < B->R; r++) {
+    Box *b = B->boxes[r];
+    args[r] = make_bint_args(b);
+    args[r].rec = nullptr;  // batches keep no per-step records
+    args[r].rec_cap = 0;
+    int nred = (b->n + 255) / 256;
+    ored[r + 1] = ored[r] + (nred > 512 ? 512 : nred);
+    osite[r + 1] = osite[r] + (b->n + 255) / 256;
+  }
+  B->tot_red = ored[B->R];
+  B->tot_site = osite[B->R];
+  FE_CUDA(cudaMalloc(&B->d_bint, sizeof(BIntArgs) * B->R));
+  FE_CUDA(cudaMalloc(&B->d_off_red, sizeof(int) * (B->R + 1)));
+  FE_CUDA(cudaMalloc(&B->d_off_site, sizeof(int) * (B->R + 1)));
+  FE_CUDA(cudaMemcpy(B->d_bint, args.data(), sizeof(BIntArgs) * B->R, cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemcpy(B->d_off_red, ored.data(), sizeof(int) * (B->R + 1), cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemcpy(B->d_off_site, osite.data(), sizeof(int) * (B->R + 1),
+                     cudaMemcpyHostToDevice));
+  B->fused = true;
+  return FE_OK;
+}
+
+// One step of every box as the fused kernels: list rebuilds per box on their
+// own streams (a tenth of the steps), then one launch per kernel for all
+// boxes -- [NHC] half kick, forces, half kick [NHC], as step_body.
+static int fused_step(Batch *B, bool with_list, bool use_nhc) {
+  int rc = FE_OK;
+  cudaStream_t s = B->main;
+  if (with_list) {
+    cudaError_t e = cudaEventRecord(B->fork, s);
+    for (int r = 0; r < B->R && rc == FE_OK && e == cudaSuccess; r++) {
+      Box *b = B->boxes[r];
+      e = cudaStreamWaitEvent(b->stream, B->fork, 0);
+      if (e != cudaSuccess) break;
+      rc = launch_mixed_list(b);
+      if (rc) break;
+      e = cudaEventRecord(B->join[r], b->stream);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, B->join[r], 0);
+    }
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "fused step (lists)");
+  }
+  const int nb = B->R, nhc = use_nhc ? 1 : 0;
+  if (use_nhc && (rc = launch_b_kinet_nhc(B->d_bint, B->d_off_red, nb, B->tot_red, s))) return rc;
+  if ((rc = launch_b_vv1(B->d_bint, B->d_off_site, nb, B->tot_site, nhc, s))) return rc;
+  if ((rc = mixed_batch_forces(B->mx, s))) return rc;
+  if ((rc = launch_b_vv2(B->d_bint, B->d_off_red, nb, B->tot_red, nhc, s))) return rc;
+  if (use_nhc && (rc = launch_b_scale_kinet(B->d_bint, B->d_off_red, nb, B->tot_red, s)))
+    return rc;
+  return FE_OK;
+}
+
 static void free_batch(Batch *B) {
+  free_fused(B);
   for (auto &g : B->g)
     if (g) cudaGraphExecDestroy(g);
   for (auto e : B->join)
@@ -161,16 +240,21 @@ static int capture_batch(Batch *B, bool with_list, bool exchange, bool use_nhc,
   FE_CUDA(cudaStreamBeginCapture(B->main, cudaStreamCaptureModeThreadLocal));
   long l0 = g_launches;
   int rc = FE_OK;
-  cudaError_t e = cudaEventRecord(B->fork, B->main);
-  for (int r = 0; r < B->R && rc == FE_OK && e == cudaSuccess; r++) {
-    Box *b = B->boxes[r];
-    e = cudaStreamWaitEvent(b->stream, B->fork, 0);
-    if (e != cudaSuccess) break;
-    rc = step_body(b, with_list, use_nhc);
-    if (rc) break;
-    e = cudaEventRecord(B->join[r], b->stream);
-    if (e != cudaSuccess) break;
-    e = cudaStreamWaitEvent(B->main, B->join[r], 0);
+  cudaError_t e = cudaSuccess;
+  if (B->fused) {
+    rc = fused_step(B, with_list, use_nhc);
+  } else {
+    e = cudaEventRecord(B->fork, B->main);
+    for (int r = 0; r < B->R && rc == FE_OK && e == cudaSuccess; r++) {
+      Box *b = B->boxes[r];
+      e = cudaStreamWaitEvent(b->stream, B->fork, 0);
+      if (e != cudaSuccess) break;
+      rc = step_body(b, with_list, use_nhc);
+      if (rc) break;
+      e = cudaEventRecord(B->join[r], b->stream);
+      if (e != cudaSuccess) break;
+      e = cudaStreamWaitEvent(B->main, B->join[r], 0);
+    }
   }
   if (rc == FE_OK && e == cudaSuccess && exchange) rc = launch_exchange(B);
   *nlaunch = (int)(g_launches - l0);
@@ -285,8 +369,29 @@ int fe_batch_create(fe_batch **out, fe_box *const *boxes, int nrep, uint64_t see
     delete fb;
     return rc;
   }
+  // the fused step where every box allows it (mixed precision, contiguous
+  // molecules); otherwise each box steps on its own stream
+  if (setup_fused(B) != FE_OK) free_fused(B);
   *out = fb;
   return FE_OK;
+}
+
+int fe_batch_set_fused(fe_batch *batch, int on) {
+  if (!batch) return FE_ERR_ARG;
+  Batch *B = &batch->B;
+  cudaStreamSynchronize(B->main);
+  for (int k = 0; k < 4; k++)
+    if (B->g[k]) {
+      cudaGraphExecDestroy(B->g[k]);
+      B->g[k] = nullptr;
+      B->launches[k] = -1;
+    }
+  B->g_key = -1;
+  free_fused(B);
+  if (!on) return FE_OK;
+  int rc = setup_fused(B);
+  if (rc) free_fused(B);
+  return rc;
 }
 
 void fe_batch_destroy(fe_batch *batch) {

@@ -57,7 +57,7 @@ EXPORTS = [
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
     "fe_go_get_stream", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
     "fe_mc_delta_terms", "fe_mc_site_energy", "fe_drift", "fe_box_set_temperature",
-    "fe_bspline",
+    "fe_bspline", "fe_batch_set_fused",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -568,6 +568,11 @@ class Batch:
         v = np.empty(4, np.int32)
         self._check(self.lib.fe_batch_step_launches(self.h, _p(v)))
         return v.tolist()
+
+    def set_fused(self, on: bool):
+        """All boxes per kernel launch (True, the default where allowed) or
+        one graph branch per box (False)."""
+        self._check(self.lib.fe_batch_set_fused(self.h, int(on)))
 
     def stream(self) -> int:
         """cudaStream_t (as an integer) the step graphs run on."""
