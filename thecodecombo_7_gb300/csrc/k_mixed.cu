@@ -2117,21 +2117,24 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
     bgat.push_back(std::min(1024, (b->n + 127) / 128));
     bfin.push_back((3 * b->n + 255) / 256);
   }
-  // group buffers and batched plans; each box's grid points into its group
+  // group buffers and batched plans; each box's grid points into its group.
+  // Real grids start every Kpad floats (K rounded up to 4: 16-byte aligned,
+  // as the grid kernels' paired float stores need for odd K).
   for (BMxGroup &g : P->groups) {
     if (rc) break;
     long K = (long)g.G[0] * g.G[1] * g.G[2], Kh = (long)g.G[0] * g.G[1] * (g.G[2] / 2 + 1);
-    if (cudaMalloc(&g.real, sizeof(float) * K * g.count) != cudaSuccess ||
+    long Kpad = (K + 3) / 4 * 4;
+    if (cudaMalloc(&g.real, sizeof(float) * Kpad * g.count) != cudaSuccess ||
         cudaMalloc(&g.cplx, sizeof(cufftComplex) * Kh * g.count) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "batch grid buffers");
       break;
     }
     int nn[3] = {g.G[0], g.G[1], g.G[2]};
-    cufftResult fr = cufftPlanMany(&g.r2c, 3, nn, nullptr, 1, (int)K, nullptr, 1, (int)Kh,
-                                   CUFFT_R2C, g.count);
+    int nh[3] = {g.G[0], g.G[1], g.G[2] / 2 + 1};
+    cufftResult fr = cufftPlanMany(&g.r2c, 3, nn, nn, 1, (int)Kpad, nh, 1, (int)Kh, CUFFT_R2C,
+                                   g.count);
     if (fr == CUFFT_SUCCESS)
-      fr = cufftPlanMany(&g.c2r, 3, nn, nullptr, 1, (int)Kh, nullptr, 1, (int)K, CUFFT_C2R,
-                         g.count);
+      fr = cufftPlanMany(&g.c2r, 3, nn, nh, 1, (int)Kh, nn, 1, (int)Kpad, CUFFT_C2R, g.count);
     if (fr != CUFFT_SUCCESS) {
       rc = cufft_fail(fr, "cufftPlanMany (batch)");
       break;
@@ -2144,7 +2147,8 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
       size_t slot = reinterpret_cast<size_t>(args[r].grid32k);
       BMxGroup &g = P->groups[gi];
       long K = (long)g.G[0] * g.G[1] * g.G[2], Kh = (long)g.G[0] * g.G[1] * (g.G[2] / 2 + 1);
-      args[r].grid32 = g.real + slot * K;
+      long Kpad = (K + 3) / 4 * 4;
+      args[r].grid32 = g.real + slot * Kpad;
       args[r].grid32k = g.cplx + slot * Kh;
     }
   if (rc == FE_OK && cudaMalloc(&P->d_args, sizeof(BMxArgs) * nbox) != cudaSuccess)
