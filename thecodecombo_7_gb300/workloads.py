@@ -4,6 +4,7 @@ is asked for).
 
     python -m thecodecombo_7_gb300.workloads [--molecules 32000] [--precision mixed]
         [--steps 30] [--warmup 10] [--switch 8.0]
+    python -m thecodecombo_7_gb300.workloads --batch [--replicas 32] [--unfused]
 
 Builds the seeded 3-site water box (0.1 sites/A^3, SPME grid ~1 point/A),
 picks the pair kernel's launch shape, runs the warm-up steps, then the timed
@@ -19,6 +20,42 @@ import json
 from . import engine, systems
 
 
+def batch_main(a):
+    """The uneven replica batch: 32 NHC boxes of 2,000-12,000 molecules (the
+    bench's batch leg), stepped together; prints one JSON line."""
+    import numpy as np
+    import torch
+    rng = np.random.default_rng(a.seed + 4)
+    nmol = rng.integers(2000, 12001, a.replicas)
+    temps = np.linspace(300.0, 400.0, a.replicas)
+    ss = [systems.water_box(int(m), density=0.1, seed=a.seed + 100 + k, T=float(temps[k]),
+                            r_switch=a.switch) for k, m in enumerate(nmol)]
+    boxes = [engine.Box(s, precision=engine.FE_PREC_MIXED) for s in ss]
+    out = {"replicas": a.replicas, "sites": int(sum(s.n for s in ss))}
+    try:
+        for b in boxes:
+            b.nblist()
+            b.forces()
+        batch = engine.Batch(boxes, seed=a.seed)
+        batch.set_fused(not a.unfused)
+        batch.run(a.warmup, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
+        st = torch.cuda.ExternalStream(batch.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        batch.run(a.steps, nlist_freq=10, swap_freq=500, first_step=a.warmup + 1, use_nhc=True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out.update(ms_per_step=ms / a.steps, atom_steps_per_s=out["sites"] * a.steps / (ms * 1e-3),
+                   launches=batch.step_launches(), fused=not a.unfused)
+        batch.close()
+    finally:
+        for b in boxes:
+            b.close()
+    print(json.dumps(out))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--molecules", type=int, default=32000)
@@ -27,7 +64,13 @@ def main(argv=None):
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--switch", type=float, default=8.0)
     ap.add_argument("--seed", type=int, default=2025)
+    ap.add_argument("--batch", action="store_true",
+                    help="the 32-replica uneven batch instead of one box")
+    ap.add_argument("--replicas", type=int, default=32)
+    ap.add_argument("--unfused", action="store_true", help="batch: box by box")
     a = ap.parse_args(argv)
+    if a.batch:
+        return batch_main(a)
     import torch
     s = systems.water_box(a.molecules, density=0.1, seed=a.seed, r_switch=a.switch)
     prec = engine.FE_PREC_MIXED if a.precision == "mixed" else engine.FE_PREC_FP64
