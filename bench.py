@@ -415,11 +415,22 @@ def batched_sample(local, steps):
             b.forces()
             shapes.append(b.autotune()[:3])  # per-box launch shape (uneven sizes)
         batch = engine.Batch(boxes, seed=SEED)
-        # warm up to step 480 so that the timed steps include the exchange at step 500
-        batch.run(480, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
+        # box by box (one graph branch per box) first, then the fused step
+        # (one launch per kernel for all boxes), continuing the same run
+        batch.set_fused(False)
+        batch.run(240, nlist_freq=10, swap_freq=500, first_step=1, use_nhc=True)
         st = torch.cuda.ExternalStream(batch.stream(), device=local)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        batch.run(100, nlist_freq=10, swap_freq=500, first_step=241, use_nhc=True)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms_unfused = e0.elapsed_time(e1) / 100
+        lv_unfused = batch.step_launches()
+        batch.set_fused(True)
+        # warm up to step 480 so that the timed steps include the exchange at step 500
+        batch.run(140, nlist_freq=10, swap_freq=500, first_step=341, use_nhc=True)
         first = 481
         e0.record(st)
         batch.run(steps, nlist_freq=10, swap_freq=500, first_step=first, use_nhc=True)
@@ -443,6 +454,12 @@ def batched_sample(local, steps):
             "exchange_attempts": int(state["attempts"]),
             "exchanges_in_timed_steps": n_ex, "list_steps": n_list,
             "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]},
+            "stepping": "fused: each kernel launched once for all 32 boxes (box ranges of "
+                        "blocks), batched FFTs per grid shape; list rebuilds per box",
+            "box_by_box": {"value": n_atoms / (ms_unfused * 1e-3), "ms_per_step": ms_unfused,
+                           "graph_launches_per_step": {"plain": lv_unfused[0],
+                                                       "list": lv_unfused[1]},
+                           "steps": 100},
             "pair_launch_shapes": sorted(set(tuple(x) for x in shapes))}
 
 
