@@ -328,7 +328,12 @@ int fe_mc_chains_train_surrogate(fe_box *box, fe_mlp *mlp, int epochs, int batch
                                  uint64_t seed, float *loss_hist);
 /* Copies the network into the chains (bf16 weights, FP32 arithmetic in the kernel). */
 int fe_mc_chains_set_surrogate(fe_box *box, fe_mlp *mlp);
-/* 0: exact dE in one stage; 1: delayed acceptance (after set_surrogate). */
+/* 0: exact dE in one stage; 1: delayed acceptance (after set_surrogate);
+ * 2 and 3: the same two with the reciprocal change recomputed from every site
+ * at every evaluation (S(k) before and after the move summed over all sites,
+ * FP64 sums) -- the cost of the reference's ewald_kspace_mc evaluation
+ * (ewald_mc.c:109-156, called before and after each trial by forces_mc), kept
+ * as the denominator of its delayed-acceptance comparison. */
 int fe_mc_chains_set_mode(fe_box *box, int mode);
 /* {moves, accepted, stage-1 accepted, exact reciprocal evaluations} of a chain. */
 int fe_mc_chains_stats(fe_box *box, int chain, int64_t *out4);

@@ -101,3 +101,29 @@ def test_mc_chains_independent_and_deterministic(system):
     assert np.array_equal(one[0][0], three[0][0]) and one[0][2] == three[0][2]
     assert not np.array_equal(three[0][0], three[1][0])
     assert all(c[1] == 300 for c in three)
+
+
+def test_full_recompute_mode_matches_incremental(system):
+    """Mode 2 (the reciprocal change recomputed from every site, the
+    reference's cost) gives the same reciprocal energy change as the
+    incremental structure factor, move for move, to 2e-3 kJ/mol (the same
+    draws, so the same trial moves while the decisions agree)."""
+    from thecodecombo_7_gb300 import engine
+    n = 60
+    recs = []
+    for mode in (0, 2):
+        with engine.Box(system, precision=engine.FE_PREC_FP64) as b:
+            b.mc_chains_setup(nchains=1, kmax=7, T=300.0, seed=77, log_cap=n)
+            b.mc_chains_set_mode(mode)
+            b.mc_chains_run(n)
+            rec, _ = b.mc_chains_log(n)
+            recs.append(rec)
+    r0, r2 = recs
+    same = 0
+    for t in range(n):
+        assert int(r0[t, 0]) == int(r2[t, 0])  # same proposal
+        assert abs(r0[t, 4] - r2[t, 4]) <= DE_TOL, (t, r0[t, 4], r2[t, 4])
+        same += 1
+        if r0[t, 2] != r2[t, 2]:  # a near-tie decided differently: paths part
+            break
+    assert same >= n // 2

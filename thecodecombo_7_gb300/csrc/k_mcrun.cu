@@ -59,6 +59,7 @@ struct MccParams {
   uint64_t seed;
   int log_cap;
   int mode;          // 0: exact dE; 1: delayed acceptance with the surrogate
+  int full;          // 1: the reciprocal change recomputed from every site (the reference's cost)
   int desc;          // descriptors computed (mode 1 or sample collection)
   int collect;       // store (descriptors, exact dE_k) samples in mode 0
   long long sample_cap;  // samples per chain
@@ -490,7 +491,31 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
     }
     const bool need_k = (P.mode == 0) || stage1;
     if (need_k) {
-      if (tid < P.nk) {
+      if (tid < P.nk && P.full) {
+        // the reference's evaluation (ewald_mc.c:109-156 before and after the
+        // move, forces_mc.c:90-573): S(k) of the old and of the new
+        // configuration summed over every site, in FP64
+        double sox = 0.0, soy = 0.0, snx = 0.0, sny = 0.0;
+        for (int j = 0; j < P.n; j++) {
+          int4 pj = sm_pos[j];
+          double q = (double)__int_as_float(pj.w);
+          float so, co;
+          phase_sincos((uint32_t)kx * (unsigned)pj.x + (uint32_t)ky * (unsigned)pj.y +
+                           (uint32_t)kz * (unsigned)pj.z,
+                       so, co);
+          sox += q * (double)co;
+          soy += q * (double)so;
+          if (j >= lb && j < lb + m) {
+            const unsigned *u = mv_new[j - lb];
+            phase_sincos((uint32_t)kx * u[0] + (uint32_t)ky * u[1] + (uint32_t)kz * u[2], so, co);
+          }
+          snx += q * (double)co;
+          sny += q * (double)so;
+        }
+        dSx = (float)(snx - sox);
+        dSy = (float)(sny - soy);
+        dk = (float)((double)ck * ((snx * snx + sny * sny) - (sox * sox + soy * soy)));
+      } else if (tid < P.nk) {
         for (int i = 0; i < m; i++) {
           uint32_t po = (uint32_t)kx * mv_old[i][0] + (uint32_t)ky * mv_old[i][1] +
                         (uint32_t)kz * mv_old[i][2];
@@ -781,6 +806,7 @@ static int mcc_setup(Box *b, int nchains, const int *mol_first, int nmol, int km
   FE_CUDA(cudaMalloc(&D.stats, sizeof(long long) * 2 * nchains));
   FE_CUDA(cudaMemset(D.stats, 0, sizeof(long long) * 2 * nchains));
   P.mode = 0;
+  P.full = 0;
   P.desc = 0;
   P.collect = 0;
   P.sample_cap = 0;
@@ -1062,15 +1088,16 @@ int fe_mc_chains_set_surrogate(fe_box *box, fe_mlp *mlp) {
 
 // 0: exact dE (one stage); 1: delayed acceptance (needs a surrogate)
 int fe_mc_chains_set_mode(fe_box *box, int mode) {
-  if (!box || !box->b.mcc || (mode != 0 && mode != 1)) return FE_ERR_ARG;
+  if (!box || !box->b.mcc || mode < 0 || mode > 3) return FE_ERR_ARG;
   McChains *M = box->b.mcc;
-  if (mode == 1 && !M->D.w1t) {
+  if ((mode & 1) && !M->D.w1t) {
     set_error("fe_mc_chains_set_mode: delayed acceptance needs fe_mc_chains_set_surrogate first");
     return FE_ERR_STATE;
   }
   MccParams P = M->P;
-  P.mode = mode;
-  P.desc = (mode == 1 || P.collect) ? 1 : 0;
+  P.mode = mode & 1;
+  P.full = mode >> 1;
+  P.desc = (P.mode == 1 || P.collect) ? 1 : 0;
   int rc = mcc_check_smem(P);
   if (rc) return rc;
   M->P = P;
