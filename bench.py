@@ -566,6 +566,32 @@ def mc_sample(local):
         out["da_over_exact_accepted_per_s"] = (
             out["delayed_acceptance_1_chain"]["accepted_moves_per_s"] /
             out["exact_1_chain"]["accepted_moves_per_s"])
+        # against the reference's exact evaluation: the reciprocal change
+        # recomputed from every site before and after each move (modes 2, 3)
+        for mode, name in ((2, "exact_full_recompute"), (3, "delayed_acceptance_full_recompute")):
+            box.mc_chains_setup(nchains=1, kmax=7, T=300.0, seed=SEED + 7)
+            if mode == 3:
+                box.mc_chains_set_surrogate(net)
+            box.mc_chains_set_mode(mode)
+            box.mc_chains_run(50)
+            a0 = box.mc_chains_stats(0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            moves = 1500
+            e0.record(stream)
+            box.mc_chains_run(moves)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            sec = e0.elapsed_time(e1) / 1000.0
+            a1 = box.mc_chains_stats(0)
+            acc = a1["accepted"] - a0["accepted"]
+            out[f"{name}_1_chain"] = {"accepted_moves_per_s": acc / sec, "moves_per_s": moves / sec,
+                                      "acceptance": acc / moves,
+                                      "stage1_acceptance": (a1["stage1"] - a0["stage1"]) / moves,
+                                      "us_per_move": 1e6 * sec / moves, "moves_per_chain": moves}
+        out["da_over_exact_full_recompute_accepted_per_s"] = (
+            out["delayed_acceptance_full_recompute_1_chain"]["accepted_moves_per_s"] /
+            out["exact_full_recompute_1_chain"]["accepted_moves_per_s"])
         # the reference's exact dE recomputes the whole structure factor twice
         # per move (ewald_mc.c:109-156 via forces_mc); its CPU restatement,
         # one thread, reference makefile flags, on 40 translation moves
