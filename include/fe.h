@@ -331,7 +331,7 @@ int fe_mc_chains_set_surrogate(fe_box *box, fe_mlp *mlp);
 /* 0: exact dE in one stage; 1: delayed acceptance (after set_surrogate);
  * 2 and 3: the same two with the reciprocal change recomputed from every site
  * at every evaluation (S(k) before and after the move summed over all sites,
- * FP64 sums) -- the cost of the reference's ewald_kspace_mc evaluation
+ * float-pair sums) -- the cost of the reference's ewald_kspace_mc evaluation
  * (ewald_mc.c:109-156, called before and after each trial by forces_mc), kept
  * as the denominator of its delayed-acceptance comparison. */
 int fe_mc_chains_set_mode(fe_box *box, int mode);

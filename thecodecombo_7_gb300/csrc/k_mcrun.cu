@@ -494,24 +494,27 @@ k_mcc_run(MccParams P, MccDev D, long long nmoves) {
       if (tid < P.nk && P.full) {
         // the reference's evaluation (ewald_mc.c:109-156 before and after the
         // move, forces_mc.c:90-573): S(k) of the old and of the new
-        // configuration summed over every site, in FP64
-        double sox = 0.0, soy = 0.0, snx = 0.0, sny = 0.0;
+        // configuration summed over every site (float-pair sums)
+        float soxh = 0.f, soxl = 0.f, soyh = 0.f, soyl = 0.f;
+        float snxh = 0.f, snxl = 0.f, snyh = 0.f, snyl = 0.f;
         for (int j = 0; j < P.n; j++) {
           int4 pj = sm_pos[j];
-          double q = (double)__int_as_float(pj.w);
+          float q = __int_as_float(pj.w);
           float so, co;
           phase_sincos((uint32_t)kx * (unsigned)pj.x + (uint32_t)ky * (unsigned)pj.y +
                            (uint32_t)kz * (unsigned)pj.z,
                        so, co);
-          sox += q * (double)co;
-          soy += q * (double)so;
+          ff_add(soxh, soxl, q * co);
+          ff_add(soyh, soyl, q * so);
           if (j >= lb && j < lb + m) {
             const unsigned *u = mv_new[j - lb];
             phase_sincos((uint32_t)kx * u[0] + (uint32_t)ky * u[1] + (uint32_t)kz * u[2], so, co);
           }
-          snx += q * (double)co;
-          sny += q * (double)so;
+          ff_add(snxh, snxl, q * co);
+          ff_add(snyh, snyl, q * so);
         }
+        double sox = (double)soxh + soxl, soy = (double)soyh + soyl;
+        double snx = (double)snxh + snxl, sny = (double)snyh + snyl;
         dSx = (float)(snx - sox);
         dSy = (float)(sny - soy);
         dk = (float)((double)ck * ((snx * snx + sny * sny) - (sox * sox + soy * soy)));
