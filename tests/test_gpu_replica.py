@@ -175,5 +175,8 @@ def test_fused_batch_matches_box_by_box():
         d -= s.L * np.round(d / s.L)
         assert np.abs(d).max() < 1e-6
         assert np.abs(v1 - v0).max() < 1e-4 * np.abs(v0).max()
-    # one launch per kernel for all boxes: far fewer than box by box
-    assert 0 < l1[0] <= 20 and l1[0] < l0[0]
+    # one launch per kernel for all boxes: far fewer than box by box; the
+    # list rebuild adds six launches and the exchange two (list steps here
+    # are exchange steps too)
+    assert 0 < l1[0] <= 14 and l1[0] < l0[0]
+    assert 0 < l1[3] <= 22 and l1[3] < l0[3]

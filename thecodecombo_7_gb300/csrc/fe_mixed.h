@@ -97,6 +97,7 @@ void k_cell_scan_ext(const int *count, int ncells, int *start, int *fill, cudaSt
 struct BMxPlan;
 int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out);
 int mixed_batch_forces(BMxPlan *plan, cudaStream_t s);
+int mixed_batch_list(BMxPlan *plan, cudaStream_t s);
 void mixed_batch_free(BMxPlan *plan);
 
 }  // namespace fe

@@ -70,9 +70,9 @@ __device__ __forceinline__ unsigned frac32(double x, double invL) {
 
 // cell of each site from the same 32-bit fractions the kernels see, so that
 // cell membership and fixed-point coordinates always agree
-__global__ void k_mx_cell(int n, const double4 *__restrict__ pos, double3 invL, int3 nc,
+__device__ __forceinline__ void k_mx_cell_body(VBlk vb_, int n, const double4 *__restrict__ pos, double3 invL, int3 nc,
                           int *__restrict__ cell_of, int *__restrict__ count) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = vb_.id * blockDim.x + threadIdx.x;
   if (i >= n) return;
   double4 p = pos[i];
   int cx = (int)(((unsigned long long)frac32(p.x, invL.x) * (unsigned)nc.x) >> 32);
@@ -83,22 +83,32 @@ __global__ void k_mx_cell(int n, const double4 *__restrict__ pos, double3 invL, 
   atomicAdd(&count[c], 1);
 }
 
-__global__ void k_mx_fill(int n, const int *__restrict__ cell_of, const int *__restrict__ start,
+__global__ void k_mx_cell(int n, const double4 *__restrict__ pos, double3 invL, int3 nc,
+                          int *__restrict__ cell_of, int *__restrict__ count) {
+  k_mx_cell_body(vblk_self(), n, pos, invL, nc, cell_of, count);
+}
+
+__device__ __forceinline__ void k_mx_fill_body(VBlk vb_, int n, const int *__restrict__ cell_of, const int *__restrict__ start,
                           int *__restrict__ fill, int *__restrict__ perm) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  int i = vb_.id * blockDim.x + threadIdx.x;
   if (i >= n) return;
   int c = cell_of[i];
   int s = atomicAdd(&fill[c], 1);
   perm[start[c] + s] = i;
 }
 
+__global__ void k_mx_fill(int n, const int *__restrict__ cell_of, const int *__restrict__ start,
+                          int *__restrict__ fill, int *__restrict__ perm) {
+  k_mx_fill_body(vblk_self(), n, cell_of, start, fill, perm);
+}
+
 // order each cell's sites by original index (deterministic layout)
-__global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ perm,
+__device__ __forceinline__ void k_mx_cellsort_body(VBlk vb_, const int *__restrict__ start, int *__restrict__ perm,
                               int *__restrict__ iperm, int *__restrict__ cell_s,
                               const int *__restrict__ type, int *__restrict__ type_s,
                               int *__restrict__ status) {
   __shared__ int buf[kMxMaxCellAtoms];
-  int c = blockIdx.x;
+  int c = vb_.id;
   int s0 = start[c], s1 = start[c + 1];
   int m = s1 - s0;
   if (m > kMxMaxCellAtoms) {
@@ -131,6 +141,13 @@ __global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ p
     cell_s[s0 + i] = c;
     type_s[s0 + i] = type[o];
   }
+}
+
+__global__ void k_mx_cellsort(const int *__restrict__ start, int *__restrict__ perm,
+                              int *__restrict__ iperm, int *__restrict__ cell_s,
+                              const int *__restrict__ type, int *__restrict__ type_s,
+                              int *__restrict__ status) {
+  k_mx_cellsort_body(vblk_self(), start, perm, iperm, cell_s, type, type_s, status);
 }
 
 // per step: sorted fixed-point coordinates and charge; with `snap`, also the
@@ -315,8 +332,7 @@ __device__ __forceinline__ void list_chunk(
 // q-th partner of site k and locates it among the candidates once per column
 // batch), so the per-pair test is a distance, a mask bit and a ballot.
 // Rows come out in a fixed (column, slot) order: deterministic.
-__global__ void __launch_bounds__(kMxWarps * 32, kListBlocksPerSM)
-k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
+__device__ __forceinline__ void k_mx_list_body(VBlk vb_, int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
           const int *__restrict__ iperm, const int *__restrict__ cell_s,
           const int *__restrict__ type_s, const int *__restrict__ cstart, int3 nc, float3 sc,
           float3 Lf, float rlist, int nt, const unsigned *__restrict__ lj_row,
@@ -335,7 +351,7 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
   float3 hc = make_float3(Lf.x / nc.x, Lf.y / nc.y, Lf.z / nc.z);
   float3 ihc = make_float3(nc.x / Lf.x, nc.y / Lf.y, nc.z / Lf.z);
   int nunits = (n + kListUnit - 1) / kListUnit;
-  for (int u = blockIdx.x * kMxWarps + wib; u < nunits; u += gridDim.x * kMxWarps) {
+  for (int u = vb_.id * kMxWarps + wib; u < nunits; u += vb_.n * kMxWarps) {
     int s0 = u * kListUnit, nk = min(kListUnit, n - s0);
     int sl = s0 + min(lane, nk - 1);  // lanes past the unit repeat its last site
     int4 pk = posfx[sl];
@@ -488,6 +504,17 @@ k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
     for (int k = 0; k < kListUnit; k++)
       if (k < nk) row_close(rc[k], cap, s0 + k, lane - k, cnt_lj, cnt_nl, status);
   }
+}
+
+__global__ void __launch_bounds__(kMxWarps * 32, kListBlocksPerSM)
+k_mx_list(int n, const int4 *__restrict__ posfx, const int *__restrict__ perm,
+          const int *__restrict__ iperm, const int *__restrict__ cell_s,
+          const int *__restrict__ type_s, const int *__restrict__ cstart, int3 nc, float3 sc,
+          float3 Lf, float rlist, int nt, const unsigned *__restrict__ lj_row,
+          const unsigned char *__restrict__ lj_on, const int *__restrict__ xs,
+          const int *__restrict__ xp, int cap, int *__restrict__ cnt_lj,
+          int *__restrict__ cnt_nl, int *__restrict__ ent, int *__restrict__ status) {
+  k_mx_list_body(vblk_self(), n, posfx, perm, iperm, cell_s, type_s, cstart, nc, sc, Lf, rlist, nt, lj_row, lj_on, xs, xp, cap, cnt_lj, cnt_nl, ent, status);
 }
 
 
@@ -1361,6 +1388,9 @@ int mixed_setup(Box *b) {
       return FE_ERR_ARG;
     }
   FE_CUDA(cudaMalloc(&M.cell_count, sizeof(int) * M.ncells));
+  // the counts are zero between list builds: each build clears them after
+  // its scan (launch_mixed_list, k_b_mx_scan)
+  FE_CUDA(cudaMemset(M.cell_count, 0, sizeof(int) * M.ncells));
   FE_CUDA(cudaMalloc(&M.cell_start, sizeof(int) * (M.ncells + 1)));
   FE_CUDA(cudaMalloc(&M.cell_fill, sizeof(int) * M.ncells));
   FE_CUDA(cudaMalloc(&M.cell_of, sizeof(int) * n));
@@ -1587,11 +1617,11 @@ int launch_mixed_list(Box *b) {
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   double3 invL = make_double3(1.0 / b->p.L[0], 1.0 / b->p.L[1], 1.0 / b->p.L[2]);
   int3 nc = make_int3(M.nc[0], M.nc[1], M.nc[2]);
-  FE_CUDA(cudaMemsetAsync(M.cell_count, 0, sizeof(int) * M.ncells, b->stream));
   k_mx_cell<<<(n + 255) / 256, 256, 0, b->stream>>>(n, b->pos_q, invL, nc, M.cell_of,
                                                     M.cell_count);
   FE_LAUNCH_CHECK("k_mx_cell");
   k_cell_scan_ext(M.cell_count, M.ncells, M.cell_start, M.cell_fill, b->stream);
+  FE_CUDA(cudaMemsetAsync(M.cell_count, 0, sizeof(int) * M.ncells, b->stream));
   k_mx_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.cell_of, M.cell_start, M.cell_fill, M.perm);
   FE_LAUNCH_CHECK("k_mx_fill");
   k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s,
@@ -1853,6 +1883,18 @@ struct BMxArgs {
   float rc2, kappa, c2k, qf, epsRF;
   const float2 *exptab;
   DfIntra D;
+  // list rebuild
+  int3 nc;
+  int ncells;
+  int *cell_count, *cell_start, *cell_fill, *cell_of, *cell_s;
+  int *perm_w, *iperm_w, *type_s_w;
+  float3 Lf;
+  float rlist;
+  const unsigned *lj_row;
+  const unsigned char *lj_on;
+  const int *x_start, *x_partner;
+  int cap;
+  int *cnt_lj_w, *cnt_nl_w, *ent_w;
   // SPME
   int3 G;
   long K, Kh;
@@ -1949,6 +1991,79 @@ __global__ void k_b_mx_finalize(const BMxArgs *__restrict__ A, const int *__rest
   k_mx_finalize_body(vblk_of(off, r), a.n, a.fix, a.scal, a.ff);
 }
 
+// list rebuild of every box: cells, scan, fill, sort within cells, the
+// fixed-point coordinates and the outer list (launch_mixed_list for each box)
+__global__ void k_b_mx_cell(const BMxArgs *__restrict__ A, const int *__restrict__ off, int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_cell_body(vblk_of(off, r), a.n, a.pos, a.invL, a.nc, a.cell_of, a.cell_count);
+}
+
+// exclusive prefix of the cell counts (one block of 1024 threads per box,
+// as k_cell_scan); fill counters cleared, counts cleared for the next build
+__global__ void __launch_bounds__(1024) k_b_mx_scan(const BMxArgs *__restrict__ A) {
+  const BMxArgs &a = A[blockIdx.x];
+  __shared__ int part[1024];
+  int t = threadIdx.x, T = blockDim.x;
+  int chunk = (a.ncells + T - 1) / T;
+  int lo = min(t * chunk, a.ncells), hi = min(lo + chunk, a.ncells);
+  int sum = 0;
+  for (int c = lo; c < hi; c++) sum += a.cell_count[c];
+  part[t] = sum;
+  __syncthreads();
+  if (t == 0) {
+    int acc = 0;
+    for (int k = 0; k < T; k++) {
+      int v = part[k];
+      part[k] = acc;
+      acc += v;
+    }
+    a.cell_start[a.ncells] = acc;
+  }
+  __syncthreads();
+  int acc = part[t];
+  for (int c = lo; c < hi; c++) {
+    a.cell_start[c] = acc;
+    a.cell_fill[c] = 0;
+    acc += a.cell_count[c];
+    a.cell_count[c] = 0;
+  }
+}
+
+__global__ void k_b_mx_fill(const BMxArgs *__restrict__ A, const int *__restrict__ off, int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_fill_body(vblk_of(off, r), a.n, a.cell_of, a.cell_start, a.cell_fill, a.perm_w);
+}
+
+__global__ void k_b_mx_cellsort(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                                int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  const VBlk vb = vblk_of(off, r);
+  // the inner list and its snapshot belong to the old sort: prune next
+  if (vb.id == 0 && threadIdx.x == 0) a.ps->need = 1;
+  k_mx_cellsort_body(vb, a.cell_start, a.perm_w, a.iperm_w, a.cell_s, a.type, a.type_s_w,
+                     a.status);
+}
+
+__global__ void k_b_mx_convert_only(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                                    int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_convert_body(vblk_of(off, r), a.n, a.pos, a.perm, a.invL, a.posfx,
+                    a.P.inner_on ? a.snap : nullptr, a.sc, &a.ps->dmax2);
+}
+
+__global__ void __launch_bounds__(kMxWarps * 32, kListBlocksPerSM)
+k_b_mx_list(const BMxArgs *__restrict__ A, const int *__restrict__ off, int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_list_body(vblk_of(off, r), a.n, a.posfx, a.perm, a.iperm, a.cell_s, a.type_s,
+                 a.cell_start, a.nc, a.sc, a.Lf, a.rlist, a.nt, a.lj_row, a.lj_on, a.x_start,
+                 a.x_partner, a.cap, a.cnt_lj_w, a.cnt_nl_w, a.ent_w, a.status);
+}
+
 struct BMxGroup {
   int G[3];
   int count = 0;
@@ -1968,6 +2083,7 @@ struct BMxPlan {
   int nbox = 0;
   BMxArgs *d_args = nullptr;
   BMxRange convert, prune, pair, intra, splines, spread, fix2grid, recip, gather, finalize;
+  BMxRange cell, fill, cellsort, list;
   int intra_ns = 3;
   size_t pair_shm = 0;
   std::vector<BMxGroup> groups;
@@ -1986,7 +2102,8 @@ void mixed_batch_free(BMxPlan *P) {
   if (!P) return;
   cudaFree(P->d_args);
   BMxRange *rs[] = {&P->convert, &P->prune, &P->pair, &P->intra, &P->splines, &P->spread,
-                    &P->fix2grid, &P->recip, &P->gather, &P->finalize};
+                    &P->fix2grid, &P->recip, &P->gather, &P->finalize, &P->cell, &P->fill,
+                    &P->cellsort, &P->list};
   for (BMxRange *r : rs) cudaFree(r->d_off);
   for (BMxGroup &g : P->groups) {
     if (g.plans) {
@@ -2019,6 +2136,7 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
   P->nbox = nbox;
   std::vector<BMxArgs> args(nbox);
   std::vector<int> bconv, bprune, bpair, bintra, bspl, bspr, bf2g, brec, bgat, bfin;
+  std::vector<int> bcell, bfill, bsort, blist;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
   int rc = FE_OK;
   for (int r = 0; r < nbox && rc == FE_OK; r++) {
@@ -2088,6 +2206,26 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
                        (float)(b->G[2] / b->p.L[2]));
     a.qfe = (float)(qf / b->p.epsRF);
     a.ff = b->ff;
+    a.nc = make_int3(M.nc[0], M.nc[1], M.nc[2]);
+    a.ncells = M.ncells;
+    a.cell_count = M.cell_count;
+    a.cell_start = M.cell_start;
+    a.cell_fill = M.cell_fill;
+    a.cell_of = M.cell_of;
+    a.cell_s = M.cell_s;
+    a.perm_w = M.perm;
+    a.iperm_w = M.iperm;
+    a.type_s_w = M.type_s;
+    a.Lf = make_float3((float)b->p.L[0], (float)b->p.L[1], (float)b->p.L[2]);
+    a.rlist = (float)(b->p.rclist < b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew);
+    a.lj_row = M.lj_row;
+    a.lj_on = M.lj_on;
+    a.x_start = b->x_start;
+    a.x_partner = b->x_partner;
+    a.cap = M.cap;
+    a.cnt_lj_w = M.cnt_lj;
+    a.cnt_nl_w = M.cnt_nl;
+    a.ent_w = M.ent;
     // the grid of equal shapes side by side (the group buffers are set below)
     int gi = -1;
     for (size_t g = 0; g < P->groups.size(); g++)
@@ -2116,6 +2254,12 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
     brec.push_back((int)std::min<long>(1024L, (b->Kh + 255) / 256));
     bgat.push_back(std::min(1024, (b->n + 127) / 128));
     bfin.push_back((3 * b->n + 255) / 256);
+    bcell.push_back((b->n + 255) / 256);
+    bfill.push_back((b->n + 255) / 256);
+    bsort.push_back(M.ncells);
+    int units = (b->n + kListUnit - 1) / kListUnit;
+    int lb = (units + kMxWarps - 1) / kMxWarps;
+    blist.push_back(std::max(1, std::min(lb, nsm * 8)));
   }
   // group buffers and batched plans; each box's grid points into its group.
   // Real grids start every Kpad floats (K rounded up to 4: 16-byte aligned,
@@ -2167,11 +2311,34 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
   if (rc == FE_OK) rc = bmx_range(P->recip, brec);
   if (rc == FE_OK) rc = bmx_range(P->gather, bgat);
   if (rc == FE_OK) rc = bmx_range(P->finalize, bfin);
+  if (rc == FE_OK) rc = bmx_range(P->cell, bcell);
+  if (rc == FE_OK) rc = bmx_range(P->fill, bfill);
+  if (rc == FE_OK) rc = bmx_range(P->cellsort, bsort);
+  if (rc == FE_OK) rc = bmx_range(P->list, blist);
   if (rc) {
     mixed_batch_free(P);
     return rc;
   }
   *out = P;
+  return FE_OK;
+}
+
+// The list rebuild of every box (launch_mixed_list for each); the cell
+// counts are zero on entry and left at zero by the scan.
+int mixed_batch_list(BMxPlan *P, cudaStream_t s) {
+  const int nb = P->nbox;
+  k_b_mx_cell<<<P->cell.total, 256, 0, s>>>(P->d_args, P->cell.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_cell");
+  k_b_mx_scan<<<nb, 1024, 0, s>>>(P->d_args);
+  FE_LAUNCH_CHECK("k_b_mx_scan");
+  k_b_mx_fill<<<P->fill.total, 256, 0, s>>>(P->d_args, P->fill.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_fill");
+  k_b_mx_cellsort<<<P->cellsort.total, 256, 0, s>>>(P->d_args, P->cellsort.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_cellsort");
+  k_b_mx_convert_only<<<P->convert.total, 256, 0, s>>>(P->d_args, P->convert.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_convert_only");
+  k_b_mx_list<<<P->list.total, kMxWarps * 32, 0, s>>>(P->d_args, P->list.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_list");
   return FE_OK;
 }
 

@@ -185,26 +185,13 @@ static int setup_fused(Batch *B) {
   return FE_OK;
 }
 
-// One step of every box as the fused kernels: list rebuilds per box on their
-// own streams (a tenth of the steps), then one launch per kernel for all
-// boxes -- [NHC] half kick, forces, half kick [NHC], as step_body.
+// One step of every box as the fused kernels, one launch per kernel for all
+// boxes: [list rebuild,] [NHC] half kick, forces, half kick [NHC], as
+// step_body.
 static int fused_step(Batch *B, bool with_list, bool use_nhc) {
   int rc = FE_OK;
   cudaStream_t s = B->main;
-  if (with_list) {
-    cudaError_t e = cudaEventRecord(B->fork, s);
-    for (int r = 0; r < B->R && rc == FE_OK && e == cudaSuccess; r++) {
-      Box *b = B->boxes[r];
-      e = cudaStreamWaitEvent(b->stream, B->fork, 0);
-      if (e != cudaSuccess) break;
-      rc = launch_mixed_list(b);
-      if (rc) break;
-      e = cudaEventRecord(B->join[r], b->stream);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(s, B->join[r], 0);
-    }
-    if (rc) return rc;
-    if (e != cudaSuccess) return cuda_fail(e, "fused step (lists)");
-  }
+  if (with_list && (rc = mixed_batch_list(B->mx, s))) return rc;
   const int nb = B->R, nhc = use_nhc ? 1 : 0;
   if (use_nhc && (rc = launch_b_kinet_nhc(B->d_bint, B->d_off_red, nb, B->tot_red, s))) return rc;
   if ((rc = launch_b_vv1(B->d_bint, B->d_off_site, nb, B->tot_site, nhc, s))) return rc;

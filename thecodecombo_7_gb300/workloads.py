@@ -6,6 +6,10 @@ is asked for).
         [--steps 30] [--warmup 10] [--switch 8.0]
     python -m thecodecombo_7_gb300.workloads --batch [--replicas 32] [--unfused]
 
+With --profile-range the timed steps alone are bracketed by
+cudaProfilerStart/Stop, so `ncu --profile-from-start off` lists the launches
+of the production steps without the set-up, autotuning and warm-up.
+
 Builds the seeded 3-site water box (0.1 sites/A^3, SPME grid ~1 point/A),
 picks the pair kernel's launch shape, runs the warm-up steps, then the timed
 steps of the production loop (list every 10 steps) with CUDA events, and
@@ -42,9 +46,13 @@ def batch_main(a):
         st = torch.cuda.ExternalStream(batch.stream())
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        if a.profile_range:
+            torch.cuda.profiler.start()
         e0.record(st)
         batch.run(a.steps, nlist_freq=10, swap_freq=500, first_step=a.warmup + 1, use_nhc=True)
         e1.record(st)
+        if a.profile_range:
+            torch.cuda.profiler.stop()
         torch.cuda.synchronize()
         ms = e0.elapsed_time(e1)
         out.update(ms_per_step=ms / a.steps, atom_steps_per_s=out["sites"] * a.steps / (ms * 1e-3),
@@ -68,6 +76,8 @@ def main(argv=None):
                     help="the 32-replica uneven batch instead of one box")
     ap.add_argument("--replicas", type=int, default=32)
     ap.add_argument("--unfused", action="store_true", help="batch: box by box")
+    ap.add_argument("--profile-range", action="store_true",
+                    help="bracket the timed steps with cudaProfilerStart/Stop")
     a = ap.parse_args(argv)
     if a.batch:
         return batch_main(a)
@@ -86,9 +96,13 @@ def main(argv=None):
         b.run_md(a.warmup, first_step=1, record=False)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
+        if a.profile_range:
+            torch.cuda.profiler.start()
         e0.record(stream)
         b.run_md(a.steps, first_step=a.warmup + 1, record=False)
         e1.record(stream)
+        if a.profile_range:
+            torch.cuda.profiler.stop()
         torch.cuda.synchronize()
         out["ms_per_step"] = e0.elapsed_time(e1) / a.steps
         out["atom_steps_per_s"] = s.n * a.steps / (e0.elapsed_time(e1) * 1e-3)
