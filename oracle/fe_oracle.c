@@ -666,6 +666,164 @@ double or_cbend(const or_system *s, const double *pos, double *ff) {
 }
 
 /* ------------------------------------------------------------------------ */
+/* minimum image of one separation, the branch form of cbond.c / ctorsion.c */
+static void or_min_image(const or_system *s, double *d) {
+  for (int c = 0; c < 3; c++) {
+    double l = s->L[c], h = l / 2.0;
+    if (d[c] > h) d[c] -= l;
+    else if (d[c] < -h) d[c] += l;
+  }
+}
+
+double or_curey(const or_system *s, const double *pos, int nurey, const int *ab,
+                const double *seq, const double *k, double *ff) {
+  /* curey.c:37-106: E = k (r - Seq)^2 on the 1-3 distance */
+  double eurey = 0.0;
+  for (int i = 0; i < nurey; i++) {
+    int ia = ab[2 * i], ib = ab[2 * i + 1];
+    double d[3];
+    for (int c = 0; c < 3; c++) d[c] = pos[3 * ib + c] - pos[3 * ia + c];
+    or_min_image(s, d);
+    double drr = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+    double dr = sqrt(drr);
+    double dri = 1.0 / dr;
+    double rr = dr - seq[i];
+    double fr = -k[i] * rr * 2.0;
+    eurey += -(fr * rr * 0.5);
+    for (int c = 0; c < 3; c++) {
+      double f = fr * dri * d[c];
+      ff[3 * ia + c] -= f;
+      ff[3 * ib + c] += f;
+    }
+  }
+  return eurey;
+}
+
+/* The dihedral of (a, b, c, d) and the force of a generalised force fr
+ * (-dE/dtau) on the four sites, in the operation order of ctorsion.c:80-246
+ * and cimproper.c (the two share it).  Returns tau. */
+static double or_dihedral(const or_system *s, const double *pos, int ia, int ib, int ic,
+                          int id, double (*fr_of)(double tau, const void *par, double *e),
+                          const void *par, double *e, double *ff) {
+  double dab[3], dbc[3], dcd[3];
+  for (int c = 0; c < 3; c++) {
+    dab[c] = pos[3 * ib + c] - pos[3 * ia + c];
+    dbc[c] = pos[3 * ic + c] - pos[3 * ib + c];
+    dcd[c] = pos[3 * id + c] - pos[3 * ic + c];
+  }
+  or_min_image(s, dab);
+  or_min_image(s, dbc);
+  or_min_image(s, dcd);
+  double rab = sqrt(dab[0] * dab[0] + dab[1] * dab[1] + dab[2] * dab[2]);
+  double irab = 1.0 / rab;
+  double eab[3] = {dab[0] * irab, dab[1] * irab, dab[2] * irab};
+  double rbc = sqrt(dbc[0] * dbc[0] + dbc[1] * dbc[1] + dbc[2] * dbc[2]);
+  double irbc = 1.0 / rbc;
+  double ebc[3] = {dbc[0] * irbc, dbc[1] * irbc, dbc[2] * irbc};
+  double rcd = sqrt(dcd[0] * dcd[0] + dcd[1] * dcd[1] + dcd[2] * dcd[2]);
+  double ircd = 1.0 / rcd;
+  double ecd[3] = {dcd[0] * ircd, dcd[1] * ircd, dcd[2] * ircd};
+  /* u = eab x ebc, w = ecd x ebc and the bend cosines at b and c */
+  double u[3] = {eab[1] * ebc[2] - eab[2] * ebc[1], eab[2] * ebc[0] - eab[0] * ebc[2],
+                 eab[0] * ebc[1] - eab[1] * ebc[0]};
+  double cosb = -(eab[0] * ebc[0] + eab[1] * ebc[1] + eab[2] * ebc[2]);
+  double isinb2 = 1.0 / (1.0 - cosb * cosb);
+  double isinb = sqrt(isinb2);
+  double w[3] = {ecd[1] * ebc[2] - ecd[2] * ebc[1], ecd[2] * ebc[0] - ecd[0] * ebc[2],
+                 ecd[0] * ebc[1] - ecd[1] * ebc[0]};
+  double cosc = -(ecd[0] * ebc[0] + ecd[1] * ebc[1] + ecd[2] * ebc[2]);
+  double isinc2 = 1.0 / (1.0 - cosc * cosc);
+  double isinc = sqrt(isinc2);
+  /* sign from (u x w) . ebc, angle from u . w */
+  double x0 = -(u[1] * w[2] - u[2] * w[1]);
+  double x1 = -(u[2] * w[0] - u[0] * w[2]);
+  double x2 = -(u[0] * w[1] - u[1] * w[0]);
+  double num = (x0 * ebc[0] + x1 * ebc[1] + x2 * ebc[2]);
+  double sgn = num >= 0.0 ? 1.0 : -1.0;
+  double costau = -(u[0] * w[0] + u[1] * w[1] + u[2] * w[2]) * isinb * isinc;
+  if (costau > 1.0) costau = 1.0;
+  if (costau < -1.0) costau = -1.0;
+  double tau = sgn * acos(costau);
+  double fr = fr_of(tau, par, e);
+  double fa = -fr * irab * isinb2;
+  double fb1 = fr * (rbc - rab * cosb) * irab * irbc * isinb2;
+  double fb2 = fr * cosc * irbc * isinc2;
+  double fc1 = fr * (rbc - rcd * cosc) * ircd * irbc * isinc2;
+  double fc2 = fr * cosb * irbc * isinb2;
+  double fd = -fr * ircd * isinc2;
+  for (int c = 0; c < 3; c++) {
+    ff[3 * ia + c] += fa * u[c];
+    ff[3 * ib + c] += (fb1 * u[c] + fb2 * w[c]);
+    ff[3 * ic + c] += fc1 * w[c] + fc2 * u[c];
+    ff[3 * id + c] += fd * w[c];
+  }
+  return tau;
+}
+
+typedef struct {
+  const double *kphi, *nphi, *delphi; /* 6 each */
+} or_tors_par;
+
+/* ctorsion.c:176-188: cosine series, stopping at the first zero kphi */
+static double or_tors_fr(double tau, const void *vp, double *e) {
+  const or_tors_par *p = (const or_tors_par *)vp;
+  double fr = 0.0, et = 0.0;
+  for (int t = 0; t < 6; t++) {
+    if (p->kphi[t] != 0.0) {
+      fr += p->kphi[t] * p->nphi[t] * (sin(p->nphi[t] * tau - p->delphi[t]));
+      et += p->kphi[t] * (1 + cos(p->nphi[t] * tau - p->delphi[t]));
+    } else {
+      break;
+    }
+  }
+  *e = et;
+  return fr;
+}
+
+double or_ctorsion(const or_system *s, const double *pos, int ntors, const int *abcd,
+                   const double *kphi, const double *nphi, const double *delphi, double *ff,
+                   double *tau_out) {
+  /* ctorsion.c:63-246 */
+  double etorsion = 0.0;
+  for (int i = 0; i < ntors; i++) {
+    or_tors_par p = {kphi + 6 * i, nphi + 6 * i, delphi + 6 * i};
+    double et = 0.0;
+    double tau = or_dihedral(s, pos, abcd[4 * i], abcd[4 * i + 1], abcd[4 * i + 2],
+                             abcd[4 * i + 3], or_tors_fr, &p, &et, ff);
+    etorsion += et;
+    if (tau_out) tau_out[i] = tau;
+  }
+  return etorsion;
+}
+
+typedef struct {
+  double k, eq;
+} or_impr_par;
+
+/* cimproper.c: E = kimpr (tau - angeq)^2, fr = -2 kimpr (tau - angeq) */
+static double or_impr_fr(double tau, const void *vp, double *e) {
+  const or_impr_par *p = (const or_impr_par *)vp;
+  double rr = tau - p->eq;
+  double fr = -2.0 * p->k * rr;
+  *e = -fr * rr * 0.5;
+  return fr;
+}
+
+double or_cimproper(const or_system *s, const double *pos, int nimpr, const int *abcd,
+                    const double *kimpr, const double *angeq, double *ff) {
+  /* cimproper.c:55-221 */
+  double eimproper = 0.0;
+  for (int i = 0; i < nimpr; i++) {
+    or_impr_par p = {kimpr[i], angeq[i]};
+    double ei = 0.0;
+    or_dihedral(s, pos, abcd[4 * i], abcd[4 * i + 1], abcd[4 * i + 2], abcd[4 * i + 3],
+                or_impr_fr, &p, &ei, ff);
+    eimproper += ei;
+  }
+  return eimproper;
+}
+
+/* ------------------------------------------------------------------------ */
 void or_forces(const or_system *s, const double *pos, const int *cnt,
                const int *idx, const int *flag, double sewald, double *ff,
                or_energy *en) {

@@ -101,6 +101,16 @@ double or_ewald_self(const or_system *s);
 /* cbond.c:27-180 and cbend.c:24-218 (accumulate into ff, return energy). */
 double or_cbond(const or_system *s, const double *pos, double *ff);
 double or_cbend(const or_system *s, const double *pos, double *ff);
+/* Urey-Bradley 1-3 terms (curey.c:37-106), proper torsions (ctorsion.c:63-246;
+ * tau_out, may be NULL, gets each torsion's angle) and improper torsions
+ * (cimproper.c:55-221); each adds its forces to ff and returns its energy. */
+double or_curey(const or_system *s, const double *pos, int nurey, const int *ab,
+                const double *seq, const double *k, double *ff);
+double or_ctorsion(const or_system *s, const double *pos, int ntors, const int *abcd,
+                   const double *kphi, const double *nphi, const double *delphi, double *ff,
+                   double *tau_out);
+double or_cimproper(const or_system *s, const double *pos, int nimpr, const int *abcd,
+                    const double *kimpr, const double *angeq, double *ff);
 
 /* forces.c:118-446: zero ff, bonded, cnonbondnl (+ pme_calc), energies. */
 void or_forces(const or_system *s, const double *pos, const int *cnt,

@@ -227,6 +227,42 @@ class Oracle:
         ea = self.lib.or_cbend(self.sp, _p(pos), _p(ff))
         return ff, eb, ea
 
+    def bonded_ext(self, pos):
+        """Urey-Bradley, torsion and improper terms (curey.c, ctorsion.c,
+        cimproper.c): a dict of forces (n, 3) and energies per term and the
+        torsion angles."""
+        sm = self.sysm
+        pos = np.ascontiguousarray(pos, np.float64)
+        L = self.lib
+        for f in (L.or_curey, L.or_ctorsion, L.or_cimproper):
+            f.restype = C.c_double
+        k = dict(ab=np.ascontiguousarray(sm.ureys, np.int32),
+                 seq=np.ascontiguousarray(sm.urey_seq, np.float64),
+                 uk=np.ascontiguousarray(sm.urey_k, np.float64),
+                 t=np.ascontiguousarray(sm.tors, np.int32),
+                 kp=np.ascontiguousarray(sm.tors_kphi, np.float64),
+                 np_=np.ascontiguousarray(sm.tors_nphi, np.float64),
+                 dp=np.ascontiguousarray(sm.tors_delphi, np.float64),
+                 m=np.ascontiguousarray(sm.impr, np.int32),
+                 mk=np.ascontiguousarray(sm.impr_k, np.float64),
+                 me=np.ascontiguousarray(sm.impr_eq, np.float64))
+        out = {}
+        f = np.zeros((sm.n, 3))
+        out["e_urey"] = L.or_curey(self.sp, _p(pos), C.c_int(len(k["ab"])), _p(k["ab"]),
+                                   _p(k["seq"]), _p(k["uk"]), _p(f))
+        out["f_urey"] = f
+        f = np.zeros((sm.n, 3))
+        tau = np.zeros(max(len(k["t"]), 1))
+        out["e_tors"] = L.or_ctorsion(self.sp, _p(pos), C.c_int(len(k["t"])), _p(k["t"]),
+                                      _p(k["kp"]), _p(k["np_"]), _p(k["dp"]), _p(f), _p(tau))
+        out["f_tors"] = f
+        out["tau"] = tau[:len(k["t"])]
+        f = np.zeros((sm.n, 3))
+        out["e_impr"] = L.or_cimproper(self.sp, _p(pos), C.c_int(len(k["m"])), _p(k["m"]),
+                                       _p(k["mk"]), _p(k["me"]), _p(f))
+        out["f_impr"] = f
+        return out
+
     def ewald_self(self):
         return self.lib.or_ewald_self(self.sp)
 
@@ -337,6 +373,26 @@ def write_system_file(path, sysm):
         x[:, :2] = sysm.excl
         x[:, 2] = sysm.excl_flag
         f.write(x.tobytes())
+        if getattr(sysm, "has_ext_bonded", False):
+            # trailer: Urey-Bradley, torsion and improper records
+            f.write(b"FEXT")
+            f.write(struct.pack("<3i", len(sysm.ureys), len(sysm.tors), len(sysm.impr)))
+            u = np.zeros(len(sysm.ureys), dtype=[("ab", "<i4", 2), ("p", "<f8", 2)])
+            u["ab"] = sysm.ureys
+            u["p"][:, 0] = sysm.urey_seq
+            u["p"][:, 1] = sysm.urey_k
+            f.write(u.tobytes())
+            t = np.zeros(len(sysm.tors), dtype=[("abcd", "<i4", 4), ("p", "<f8", 18)])
+            t["abcd"] = sysm.tors
+            t["p"][:, 0:6] = sysm.tors_kphi
+            t["p"][:, 6:12] = sysm.tors_nphi
+            t["p"][:, 12:18] = sysm.tors_delphi
+            f.write(t.tobytes())
+            m = np.zeros(len(sysm.impr), dtype=[("abcd", "<i4", 4), ("p", "<f8", 2)])
+            m["abcd"] = sysm.impr
+            m["p"][:, 0] = sysm.impr_k
+            m["p"][:, 1] = sysm.impr_eq
+            f.write(m.tobytes())
 
 
 def read_tagged(path):

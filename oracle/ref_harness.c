@@ -66,6 +66,9 @@ void drift(int);
 #ifndef MC
 double cbond(int);
 double cbend(int);
+double curey(int);
+double ctorsion(int);
+double cimproper(int);
 #endif
 
 static FILE *g_out;
@@ -195,16 +198,6 @@ static void load_system(const char *path) {
     bend[k][i].a = abc[0]; bend[k][i].b = abc[1]; bend[k][i].c = abc[2];
     bend[k][i].angeq = p[0]; bend[k][i].krbend = p[1];
   }
-  urey = calloc(1, sizeof(struct ureys *));
-  urey[k] = calloc(1, sizeof(struct ureys));
-  ureyN[k] = 0;
-  tors = calloc(1, sizeof(struct torsions *));
-  tors[k] = calloc(1, sizeof(struct torsions));
-  torsN[k] = 0;
-  impr = calloc(1, sizeof(struct impropers *));
-  impr[k] = calloc(1, sizeof(struct impropers));
-  imprN[k] = 0;
-
   xint = calloc(1, sizeof(struct excinter *));
   xint[k] = calloc(NX + 1, sizeof(struct excinter));
   xintN[k] = NX;
@@ -212,6 +205,54 @@ static void load_system(const char *path) {
     int32_t e[3];
     rd(e, 4, 3, f);
     xint[k][i].a = e[0]; xint[k][i].b = e[1]; xint[k][i].xflag = e[2];
+  }
+  /* optional trailer "FEXT": Urey-Bradley, torsion and improper records
+   * (read_topology.c fills urey[k], tors[k], impr[k]) */
+  int32_t next[3] = {0, 0, 0};
+  char tag[4];
+  if (fread(tag, 1, 4, f) == 4) {
+    if (memcmp(tag, "FEXT", 4) != 0) die("bad trailer");
+    rd(next, 4, 3, f);
+  }
+  urey = calloc(1, sizeof(struct ureys *));
+  urey[k] = calloc(next[0] + 1, sizeof(struct ureys));
+  ureyN[k] = next[0];
+  for (int i = 0; i < next[0]; i++) {
+    int32_t ab[2];
+    double p[2];
+    rd(ab, 4, 2, f);
+    rd(p, 8, 2, f);
+    urey[k][i].a = ab[0]; urey[k][i].b = ab[1];
+    urey[k][i].Seq = p[0]; urey[k][i].k = p[1];
+  }
+  tors = calloc(1, sizeof(struct torsions *));
+  tors[k] = calloc(next[1] + 1, sizeof(struct torsions));
+  torsN[k] = next[1];
+  for (int i = 0; i < next[1]; i++) {
+    int32_t abcd[4];
+    double p[18];
+    rd(abcd, 4, 4, f);
+    rd(p, 8, 18, f);
+    tors[k][i].a = abcd[0]; tors[k][i].b = abcd[1];
+    tors[k][i].c = abcd[2]; tors[k][i].d = abcd[3];
+    for (int t = 0; t < 6; t++) {
+      tors[k][i].kphi[t] = p[t];
+      tors[k][i].nphi[t] = p[6 + t];
+      tors[k][i].delphi[t] = p[12 + t];
+    }
+    tors[k][i].phitag = 1; /* every angle lands in .phi (ctorsion.c:172) */
+  }
+  impr = calloc(1, sizeof(struct impropers *));
+  impr[k] = calloc(next[2] + 1, sizeof(struct impropers));
+  imprN[k] = next[2];
+  for (int i = 0; i < next[2]; i++) {
+    int32_t abcd[4];
+    double p[2];
+    rd(abcd, 4, 4, f);
+    rd(p, 8, 2, f);
+    impr[k][i].a = abcd[0]; impr[k][i].b = abcd[1];
+    impr[k][i].c = abcd[2]; impr[k][i].d = abcd[3];
+    impr[k][i].kimpr = p[0]; impr[k][i].angeq = p[1];
   }
   fclose(f);
 
@@ -450,6 +491,24 @@ int main(int argc, char **argv) {
     eb[1] = cbend(k);
     dump_xyz("f_bonded", ff[k]);
     dump_d("e_bonded", eb, 2);
+    /* Urey-Bradley, torsions and impropers alone (forces.c:183-188) */
+    double e3[3];
+    memset(ff[k], 0, sizeof(struct veloc) * N);
+    e3[0] = curey(k);
+    dump_xyz("f_urey", ff[k]);
+    memset(ff[k], 0, sizeof(struct veloc) * N);
+    e3[1] = ctorsion(k);
+    dump_xyz("f_tors", ff[k]);
+    memset(ff[k], 0, sizeof(struct veloc) * N);
+    e3[2] = cimproper(k);
+    dump_xyz("f_impr", ff[k]);
+    dump_d("e_ext", e3, 3);
+    {
+      double *tau = malloc(sizeof(double) * (size_t)(torsN[k] + 1));
+      for (int i = 0; i < torsN[k]; i++) tau[i] = tors[k][i].phi;
+      dump_d("tau", tau, torsN[k]);
+      free(tau);
+    }
     /* full forces() (forces.c:118-446) */
     forces(k);
     dump_xyz("f_total", ff[k]);
@@ -457,6 +516,8 @@ int main(int argc, char **argv) {
     kinet(k);
     en_record(r);
     dump_d("en", r, 12);
+    double rx[3] = {en[k].urey, en[k].tors, en[k].impr};
+    dump_d("en_ext", rx, 3);
   } else if (strcmp(mode, "drift") == 0) {
     /* drift.c:21: net-momentum removal from the input velocities */
     drift(k);

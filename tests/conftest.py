@@ -32,3 +32,9 @@ def golden4095():
 def golden_mc():
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, "mc.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_chain():
+    import numpy as np
+    return dict(np.load(os.path.join(GOLDEN, "chain900.npz")))

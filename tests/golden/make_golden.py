@@ -22,6 +22,13 @@ Fixtures:
                  ranges and the reference's nl_flag for each
   drift600.npz   drift() (drift.c:21) on velocities of the 600-site box given
                  a net momentum: velocities before and after
+  chain900.npz   150 flexible 6-site chains (L = 31.07 A, grid 30^3): every
+                 bonded term of forces() -- bonds, bends, Urey-Bradley,
+                 proper torsions (cosine series, one stopping early) and
+                 impropers -- with 1-4 pairs (xflag 4); the topology, the
+                 forces of curey / ctorsion / cimproper alone, their energies
+                 and torsion angles, the full forces() and en[k], and a
+                 12-step NVE trajectory
   mc.npz         the classic-Ewald Monte Carlo energies (-DMC build): the
                  reference's enbnd_mc (ewald_kspace_mc + ewald_rspace_mc + LJ)
                  before and after fixed trial molecule moves, on a periodic
@@ -93,6 +100,7 @@ def main():
     make_nlcheck(tmp)
     make_mc(tmp)
     make_drift(tmp)
+    make_chain(tmp)
     print("golden fixtures written to", HERE)
 
 
@@ -151,6 +159,26 @@ def make_mc(tmp):
     np.savez_compressed(os.path.join(HERE, "mc.npz"), **out)
 
 
+CHAIN_KEYS = ("bonds", "bond_req", "bond_k", "bends", "bend_theta0", "bend_k", "excl",
+              "excl_flag", "type_eps_kcal", "type_rmin_half", "ureys", "urey_seq", "urey_k",
+              "tors", "tors_kphi", "tors_nphi", "tors_delphi", "impr", "impr_k", "impr_eq")
+
+
+def make_chain(tmp):
+    s = systems.chain_box(150, 6, seed=3)
+    s.nlist_freq = 5
+    fo = O.run_reference("forces", s, tmp)
+    nve = O.run_reference("nve", s, tmp, nsteps=12)
+    out = sys_arrays(s)
+    for k in CHAIN_KEYS:
+        out["top_" + k] = getattr(s, k)
+    for k, v in fo.items():
+        out["forces_" + k] = v
+    for k, v in nve.items():
+        out["nve_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "chain900.npz"), **out)
+
+
 def make_drift(tmp):
     s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27), helper=False)
     s.vel = s.vel + np.array([0.7, -0.4, 0.25])
@@ -171,10 +199,11 @@ def make_nlcheck(tmp):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"]):  # this fixture alone
+    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"]):  # this fixture alone
         if not O.build_reference():
             raise SystemExit("reference sources not available")
-        {"nlcheck": make_nlcheck, "mc": make_mc, "drift": make_drift}[sys.argv[1]](
+        {"nlcheck": make_nlcheck, "mc": make_mc, "drift": make_drift,
+         "chain": make_chain}[sys.argv[1]](
             tempfile.mkdtemp(prefix="fe_golden_"))
     else:
         main()

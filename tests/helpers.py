@@ -36,3 +36,21 @@ def mc_reference_parts(e):
     def parts(x):
         return np.array([x[4], x[7] - x[6], x[1] - x[7] + x[6] - x[4] + x[5]])
     return np.array([parts(r[8:]) - parts(r[:8]) for r in e[1:]])
+
+
+CHAIN_KEYS = ("bonds", "bond_req", "bond_k", "bends", "bend_theta0", "bend_k", "excl",
+              "excl_flag", "type_eps_kcal", "type_rmin_half", "ureys", "urey_seq", "urey_k",
+              "tors", "tors_kphi", "tors_nphi", "tors_delphi", "impr", "impr_k", "impr_eq")
+
+
+def chain_from_golden(g):
+    """The chain box of chain900.npz, topology and state from the fixture."""
+    L = np.ascontiguousarray(g["L"], dtype=np.float64)
+    kw = {k: np.ascontiguousarray(g["top_" + k]) for k in CHAIN_KEYS}
+    s = systems.System(L=L, pos=np.ascontiguousarray(g["pos"]), q=np.ascontiguousarray(g["q"]),
+                       mass=np.ascontiguousarray(g["mass"]),
+                       type=np.ascontiguousarray(g["type"], dtype=np.int32),
+                       vel=np.ascontiguousarray(g["vel"]),
+                       grid=tuple(int(x) for x in g["grid"]), **kw)
+    s.nlist_freq = int(g["nlist_freq"])
+    return s

@@ -112,3 +112,40 @@ def test_oracle_fft_matches_dft(shape):
         got = buf[..., 0] + 1j * buf[..., 1]
         want = np.fft.fftn(x) if sign == -1 else np.fft.ifftn(x) * x.size
         np.testing.assert_allclose(got, want, rtol=1e-12, atol=1e-11 * np.abs(want).max())
+
+
+def test_oracle_chain_terms_bit_exact(golden_chain):
+    """Urey-Bradley, torsions (with a series that stops at a zero term) and
+    impropers: the oracle's restatements equal the reference's curey,
+    ctorsion and cimproper bit for bit, torsion angles included; the
+    non-bonded forces with 1-4 pairs (xflag 4) too; the full forces() to
+    rounding (the oracle sums the terms in another order)."""
+    from helpers import chain_from_golden
+    g = golden_chain
+    s = chain_from_golden(g)
+    orc = O.Oracle(s)
+    x = orc.bonded_ext(s.pos)
+    for k in ("f_urey", "f_tors", "f_impr"):
+        np.testing.assert_array_equal(x[k].ravel(), g["forces_" + k], err_msg=k)
+    assert (x["e_urey"], x["e_tors"], x["e_impr"]) == tuple(g["forces_e_ext"])
+    np.testing.assert_array_equal(x["tau"], g["forces_tau"])
+    np.testing.assert_array_equal(g["forces_en_ext"], g["forces_e_ext"])
+    lst = orc.nblist(s.pos)
+    ff, en = orc.forces(s.pos, lst)
+    fb, eb, ea = orc.bonded(s.pos)
+    np.testing.assert_array_equal(fb.ravel(), g["forces_f_bonded"])
+    # cnonbondnl: the pair loop and pme_calc adding into one force array
+    import ctypes as C
+    cnt, idx, flg = lst
+    pos = np.ascontiguousarray(s.pos)
+    fnb, e5, e3 = np.zeros((s.n, 3)), np.zeros(5), np.zeros(3)
+    orc.lib.or_cnonbond_pairs(orc.sp, O._p(pos), O._p(cnt), O._p(idx), O._p(flg), O._p(fnb),
+                              O._p(e5))
+    orc.lib.or_pme_calc(orc.sp, O._p(pos), C.c_double(orc.ewald_self()), O._p(fnb), O._p(e3))
+    np.testing.assert_array_equal(fnb.ravel(), g["forces_f_nonbond"])
+    total = ff + x["f_urey"] + x["f_tors"] + x["f_impr"]
+    scale = np.abs(g["forces_f_total"]).max()
+    assert np.abs(total.ravel() - g["forces_f_total"]).max() < 1e-12 * scale
+    ref_en = dict(zip(O.EN_KEYS, g["forces_en"]))
+    for k in ("nbond", "nbonds", "coulomb", "rewald", "rewalds", "kewald", "sewald", "iewald"):
+        assert en[k] == ref_en[k], k

@@ -68,6 +68,20 @@ class System:
     nhc_M: int = 3
     nhc_Q: float = 1.0e-18
     seed: int = 0
+    # Urey-Bradley 1-3 terms (curey.c), E = k (r - Seq)^2
+    ureys: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 2), np.int32))
+    urey_seq: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0))
+    urey_k: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0))
+    # proper torsions (ctorsion.c): E = sum_t kphi (1 + cos(nphi tau - delphi)),
+    # six terms per torsion, the series ending at the first kphi == 0
+    tors: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 4), np.int32))
+    tors_kphi: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 6)))
+    tors_nphi: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 6)))
+    tors_delphi: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 6)))
+    # improper torsions (cimproper.c): E = kimpr (tau - angeq)^2
+    impr: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros((0, 4), np.int32))
+    impr_k: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0))
+    impr_eq: np.ndarray = dataclasses.field(default_factory=lambda: np.zeros(0))
 
     @property
     def n(self) -> int:
@@ -76,6 +90,11 @@ class System:
     @property
     def ntypes(self) -> int:
         return int(self.type_eps_kcal.shape[0])
+
+    @property
+    def has_ext_bonded(self) -> bool:
+        """Urey-Bradley, torsion or improper terms present."""
+        return bool(len(self.ureys) or len(self.tors) or len(self.impr))
 
     def lj_tables(self):
         """Mixed (eps [kJ/mol], R_min [A]) per type pair, setlj.c:181-191."""
@@ -292,6 +311,116 @@ def water_box(n_mol: int, density: float = 0.1, seed: int = 1234,
         bend_k=np.full(n_mol, 55.0 * KCAL),
         excl=excl.astype(np.int32), excl_flag=excl_flag,
         T=T, grid=tuple(int(x) for x in grid), seed=seed)
+    for k, v in params.items():
+        setattr(sysm, k, v)
+    return sysm
+
+
+def _grow_chain(rng, n_site, bond, theta, L):
+    """One chain grown site by site: bond lengths and bend angles around
+    (bond, theta) with a small spread, dihedrals uniform in (-pi, pi]."""
+    x = np.zeros((n_site, 3))
+    x[1] = [bond, 0.0, 0.0]
+    if n_site > 2:
+        th = theta + rng.normal(0.0, 0.05)
+        x[2] = x[1] + bond * np.array([-math.cos(th), math.sin(th), 0.0])
+    for k in range(3, n_site):
+        b = bond * (1.0 + rng.normal(0.0, 0.02))
+        th = theta + rng.normal(0.0, 0.05)
+        phi = rng.uniform(-math.pi, math.pi)
+        a, bb, c = x[k - 3], x[k - 2], x[k - 1]
+        bc = c - bb
+        bc /= np.linalg.norm(bc)
+        nrm = np.cross(bb - a, bc)
+        nrm /= np.linalg.norm(nrm)
+        m = np.stack([bc, np.cross(nrm, bc), nrm], 1)
+        d = np.array([-b * math.cos(th), b * math.sin(th) * math.cos(phi),
+                      b * math.sin(th) * math.sin(phi)])
+        x[k] = c + m @ d
+    return x - x.mean(0)
+
+
+def chain_box(n_mol: int = 150, n_site: int = 6, density: float = 0.03, seed: int = 0,
+              T: float = 300.0, L: float | None = None, dmin: float = 2.5, grid=None,
+              **params) -> System:
+    """Flexible united-atom chains with every bonded term of forces():
+    bonds, bends, Urey-Bradley 1-3 terms, proper torsions (three-term cosine
+    series; the first torsion of each chain has a zero second term, so its
+    series stops after one term) and one improper per chain; charges
+    +-0.25 / +-0.1 e (neutral chains), 1-2 / 1-3 pairs excluded (xflag 1 / 2)
+    and 1-4 pairs modified (xflag 4).  Chains are grown with random
+    dihedrals, rotated at random and placed one by one, rejecting any site
+    closer than ``dmin`` to a site of another chain."""
+    rng = np.random.default_rng(seed)
+    n = n_mol * n_site
+    if L is None:
+        L = (n / density) ** (1.0 / 3.0)
+    if grid is None:
+        g = fft_friendly_below(int(round(L)))
+        grid = (g, g, g)
+    bond, theta = 1.53, math.radians(111.0)
+    placed = np.zeros((0, 3))
+    chains = []
+    tries = 0
+    while len(chains) < n_mol:
+        tries += 1
+        if tries > 200 * n_mol:
+            raise RuntimeError(f"could not place {n_mol} chains at L={L:.2f}")
+        x = _grow_chain(rng, n_site, bond, theta, L)
+        dd = np.linalg.norm(x[:, None] - x[None], axis=-1)
+        if n_site > 4 and np.triu(dd < dmin, 4).any():  # the chain folds onto itself
+            continue
+        x = x @ _random_rotations(rng, 1)[0].T + rng.uniform(-L / 2, L / 2, 3)
+        x -= L * np.floor(x / L + 0.5)
+        if len(placed):
+            tree = cKDTree(np.mod(placed + L / 2, L), boxsize=L)
+            if np.isfinite(tree.query(np.mod(x + L / 2, L), distance_upper_bound=dmin)[0]).any():
+                continue
+        chains.append(x)
+        placed = np.concatenate([placed, x])
+    pos = np.concatenate(chains)
+    pattern_q = np.array([0.25, -0.25, 0.1, -0.1, 0.25, -0.25])
+    q = np.tile(np.resize(pattern_q, n_site), n_mol)
+    q -= np.repeat(q.reshape(n_mol, n_site).mean(1), n_site)  # neutral chains
+    typ1 = np.ones(n_site, np.int32)
+    typ1[0] = typ1[-1] = 0
+    typ = np.tile(typ1, n_mol)
+    mass = np.where(typ == 0, 15.0, 14.0)
+    sd = np.sqrt(KB * T / (mass * AU)) * 1.0e-2
+    vel = rng.normal(size=(n, 3)) * sd[:, None]
+    vel -= (vel * mass[:, None]).sum(0) / mass.sum()
+    base = n_site * np.arange(n_mol, dtype=np.int32)[:, None]
+    def idx(*offs):
+        ks = np.arange(n_site - max(offs), dtype=np.int32)
+        return np.stack([(base + ks[None, :] + o) for o in offs], -1).reshape(-1, len(offs))
+    bonds, bends, ureys, tors = idx(0, 1), idx(0, 1, 2), idx(0, 2), idx(0, 1, 2, 3)
+    nt = len(tors)
+    kphi = np.zeros((nt, 6))
+    nphi = np.zeros((nt, 6))
+    delphi = np.zeros((nt, 6))
+    kphi[:, :3] = np.array([0.20, 0.25, 0.40]) * KCAL
+    nphi[:, :3] = [1.0, 2.0, 3.0]
+    delphi[:, :3] = [0.0, math.pi, 0.0]
+    first = (np.arange(nt) % (n_site - 3)) == 0
+    kphi[first, 1] = 0.0  # the series stops here (ctorsion.c:178-186)
+    impr = (base[:, 0:1] + np.array([[1, 0, 2, 3]], np.int32)).astype(np.int32)
+    excl = np.concatenate([bonds, ureys, idx(0, 3)])
+    excl_flag = np.concatenate([np.ones(len(bonds), np.int32), 2 * np.ones(len(ureys), np.int32),
+                                4 * np.ones(len(tors), np.int32)])
+    sysm = System(
+        L=np.array([L, L, L], dtype=np.float64),
+        pos=np.ascontiguousarray(pos), q=q.astype(np.float64), mass=mass.astype(np.float64),
+        type=typ, vel=np.ascontiguousarray(vel),
+        type_eps_kcal=np.array([-0.175, -0.118]),
+        type_rmin_half=np.array([2.06, 2.20]),
+        bonds=bonds, bond_req=np.full(len(bonds), bond), bond_k=np.full(len(bonds), 222.5 * KCAL),
+        bends=bends, bend_theta0=np.full(len(bends), theta),
+        bend_k=np.full(len(bends), 58.35 * KCAL),
+        excl=excl.astype(np.int32), excl_flag=excl_flag,
+        T=T, grid=tuple(int(x) for x in grid), seed=seed,
+        ureys=ureys, urey_seq=np.full(len(ureys), 2.53), urey_k=np.full(len(ureys), 11.16 * KCAL),
+        tors=tors.astype(np.int32), tors_kphi=kphi, tors_nphi=nphi, tors_delphi=delphi,
+        impr=impr, impr_k=np.full(n_mol, 20.0 * KCAL), impr_eq=np.full(n_mol, math.radians(35.0)))
     for k, v in params.items():
         setattr(sysm, k, v)
     return sysm
