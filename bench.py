@@ -287,6 +287,8 @@ def nve_drift(rec, sysm, dt=None):
     fluctuation about the line (kJ/mol)."""
     dt = sysm.dt if dt is None else dt
     tot = rec[:, 0] + rec[:, 1] + rec[:, 2] + rec[:, 4]  # kinet + bond + bend + nbonds
+    if rec.shape[1] > 12:  # + urey + tors + impr (calcvalue.c:45-53)
+        tot = tot + rec[:, 12] + rec[:, 13] + rec[:, 14]
     t_ps = np.arange(len(tot)) * dt
     kT = 1.380662e-23 * 6.022045e23 * sysm.T * 1e-3
     nfree = 3 * sysm.n - 3
@@ -455,7 +457,7 @@ def batched_sample(local, steps):
             "exchanges_in_timed_steps": n_ex, "list_steps": n_list,
             "graph_launches_per_step": {"plain": lv[0], "list": lv[1], "list_exchange": lv[3]},
             "stepping": "fused: each kernel launched once for all 32 boxes (box ranges of "
-                        "blocks), batched FFTs per grid shape; list rebuilds per box",
+                        "blocks), batched FFTs per grid shape, list rebuilds of all boxes in six launches",
             "box_by_box": {"value": n_atoms / (ms_unfused * 1e-3), "ms_per_step": ms_unfused,
                            "graph_launches_per_step": {"plain": lv_unfused[0],
                                                        "list": lv_unfused[1]},

@@ -32,7 +32,7 @@
 extern "C" {
 #endif
 
-#define FE_ABI_VERSION 1
+#define FE_ABI_VERSION 2  /* 2: en[k] records carry urey, tors, impr */
 
 enum {
   FE_OK = 0,
@@ -55,7 +55,7 @@ enum {
 enum {
   FE_EN_KINET = 0, FE_EN_BOND, FE_EN_BEND, FE_EN_NBOND, FE_EN_NBONDS,
   FE_EN_COULOMB, FE_EN_REWALD, FE_EN_REWALDS, FE_EN_KEWALD, FE_EN_SEWALD,
-  FE_EN_IEWALD, FE_EN_TEWALD, FE_EN_COUNT
+  FE_EN_IEWALD, FE_EN_TEWALD, FE_EN_UREY, FE_EN_TORS, FE_EN_IMPR, FE_EN_COUNT
 };
 
 typedef struct fe_box fe_box;
@@ -168,6 +168,28 @@ int fe_charge_grid(fe_box *box);
 int fe_get_charge_grid(fe_box *box, double *grid);
 /* cbond + cbend energies into en2 (forces accumulated into ff). */
 int fe_bonded(fe_box *box, double *en2);
+
+/* ---- bonded terms beyond bonds and bends (read_topology.c fills urey[k],
+ * tors[k], impr[k]); each call replaces the box's set of that kind and
+ * forces() includes them from then on (FE_EN_UREY, FE_EN_TORS, FE_EN_IMPR). */
+/* Urey-Bradley 1-3 terms, curey.c:37-106: E = k (r_ab - seq)^2.
+ * ab: 2*n site indices; seq [A]; k [kJ/mol/A^2]. */
+int fe_set_ureys(fe_box *box, int n, const int *ab, const double *seq, const double *k);
+/* Proper torsions, ctorsion.c:63-246: E = sum_t kphi[t] (1 + cos(nphi[t] tau
+ * - delphi[t])) over t < 6, the series ending at the first kphi[t] == 0 (as the
+ * reference's loop); tau is the dihedral a-b-c-d.  abcd: 4*n; kphi, nphi,
+ * delphi: 6*n each (struct torsions' arrays) [kJ/mol, 1, rad]. */
+int fe_set_torsions(fe_box *box, int n, const int *abcd, const double *kphi,
+                    const double *nphi, const double *delphi);
+/* Improper torsions, cimproper.c:55-221: E = kimpr (tau - angeq)^2.
+ * abcd: 4*n; kimpr [kJ/mol/rad^2]; angeq [rad]. */
+int fe_set_impropers(fe_box *box, int n, const int *abcd, const double *kimpr,
+                     const double *angeq);
+/* The dihedral tau of every torsion at the last force evaluation
+ * (ctorsion.c:172-175 stores it in tors[k][i].phi / psi / theta by tag). */
+int fe_get_torsion_angles(fe_box *box, double *tau);
+/* curey + ctorsion + cimproper energies into en3 (forces accumulated into ff). */
+int fe_bonded_ext(fe_box *box, double *en3);
 /* zero ff (forces.c:126-130) */
 int fe_zero_forces(fe_box *box);
 

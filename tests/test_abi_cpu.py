@@ -61,7 +61,7 @@ def test_ctypes_signatures_match_header(lib):
 
 
 def test_abi_version(lib):
-    assert lib.fe_abi_version() == 1
+    assert lib.fe_abi_version() == 2
 
 
 def test_non_neutral_box_is_rejected_with_code_20(lib):

@@ -111,7 +111,7 @@ def test_swap_sequence_matches_oracle():
             md = o.run_md(4, use_nhc=True, pos=st[other]["pos"], vel=vel[k],
                           zeta=st[k]["zeta"], pos_nopbc=st[other]["nop"], T=T[k])
             want = md["en"][1:]
-            rel = np.abs(recs[k] - want).max() / np.abs(want).max()
+            rel = np.abs(recs[k][:, :want.shape[1]] - want).max() / np.abs(want).max()
             assert rel < 1e-10, (k, rel)
             np.testing.assert_allclose(boxes[k].get_positions(), md["pos"], rtol=0, atol=1e-10)
     finally:

@@ -292,6 +292,24 @@ def test_mixed_spme_small_and_ragged_grids(grid):
     assert abs(en["kewald"] - en_ref["kewald"]) <= 2e-6 * abs(en_ref["sewald"])
 
 
+@pytest.mark.parametrize("order", [3, 4, 6])
+def test_mixed_spline_orders(order):
+    """Order 4 computes its spline weights inside spreading and gathering;
+    other orders store them in a separate pass first: both against the FP64
+    oracle at the same order."""
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(600, density=0.1, seed=11, order=order)
+    f_ref, en_ref = O.Oracle(s).forces(s.pos)
+    with _mixed(s) as b:
+        b.nblist()
+        en = b.forces()
+        f = b.get_forces()
+    err = _rms_rel(f, f_ref)
+    assert err <= RMS_TOL, f"rms force error {err:.3e}"
+    assert abs(en["kewald"] - en_ref["kewald"]) <= 5e-7 * abs(en_ref["kewald"]) + 1e-9 * abs(
+        en_ref["sewald"])
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_nl_check_matches_oracle(precision):
     """fe_nl_check against the oracle's restatement of nl_check after moves

@@ -32,8 +32,10 @@ UNITS = {
     "fe_api.cu": ["-Xcompiler", "-ffp-contract=off"],
     "k_nblist.cu": ["-fmad=false"],
     "k_pair64.cu": ["-fmad=false"],
+    "k_bonded_ext.cu": ["-fmad=false"],
     "k_spme.cu": ["-fmad=false"],
     "k_integrate.cu": ["-fmad=false"],
+    "k_integrate_mx.cu": [],
     "k_mc.cu": ["-fmad=false"],
     "k_mixed.cu": ["-ftz=true"],
     "k_noalloc.cu": [],

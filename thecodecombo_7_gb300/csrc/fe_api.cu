@@ -86,6 +86,7 @@ static int forces_device(Box *b) {
   int rc;
   if ((rc = launch_zero_forces(b))) return rc;
   if ((rc = launch_bonded64(b))) return rc;
+  if ((rc = launch_bonded_ext(b, false))) return rc;
   if ((rc = launch_pair64(b))) return rc;
   if ((rc = launch_pme64(b))) return rc;
   if ((rc = launch_apply_pme(b))) return rc;
@@ -99,7 +100,8 @@ static void free_box(Box *b) {
                   b->cell_fill, b->cell_atoms, b->cell_of, b->nl_count, b->nl_ent, b->eterm,
                   b->kweight, b->grid, b->grid_k, b->spl_floor, b->spl_m, b->spl_d, b->fp,
                   b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->facc, b->xyz_dev, b->zeta, b->rec,
-                  b->rec_counter};
+                  b->rec_counter, b->urey_ab, b->urey_seq, b->urey_k, b->tors_abcd, b->tors_par,
+                  b->tors_tau, b->impr_abcd, b->impr_k, b->impr_eq};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   mc_free(b);
@@ -343,7 +345,14 @@ int step_body(Box *b, bool with_list, bool use_nhc) {
   if (with_list && (rc = launch_list(b))) return rc;
   if (use_nhc && (rc = launch_nhc(b, b->p.dt))) return rc;
   if ((rc = launch_vv1(b, 1.0))) return rc;
-  if ((rc = forces_device(b))) return rc;
+  // mixed NVE: the force finalisation, the energy assembly, the second half
+  // kick, kinet and the record in one launch
+  const bool tail = b->mx != nullptr && !use_nhc;
+  b->fold_tail = tail;
+  rc = forces_device(b);
+  b->fold_tail = false;
+  if (rc) return rc;
+  if (tail) return launch_vv2_mx_tail(b);
   if (use_nhc) {
     if ((rc = launch_vv2(b, 1.0))) return rc;
     if ((rc = launch_nhc(b, b->p.dt))) return rc;
@@ -647,6 +656,113 @@ int fe_bonded(fe_box *box, double *en2) {
     en2[0] = b->host_scal[SC_BOND];
     en2[1] = b->host_scal[SC_BEND];
   }
+  return FE_OK;
+}
+
+// the step graphs were captured without the changed terms: recapture
+static void drop_step_graphs(Box *b) {
+  if (b->g_step) cudaGraphExecDestroy(b->g_step);
+  if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
+  b->g_step = b->g_step_list = nullptr;
+  b->g_key = -1;
+}
+
+static bool sites_in_range(const int *idx, size_t count, int n) {
+  for (size_t i = 0; i < count; i++)
+    if (idx[i] < 0 || idx[i] >= n) return false;
+  return true;
+}
+
+static int replace_bytes(Box *b, void **dst, const void *src, size_t bytes) {
+  if (*dst) {
+    FE_CUDA(cudaStreamSynchronize(b->stream));
+    cudaFree(*dst);
+    *dst = nullptr;
+  }
+  if (bytes == 0) return FE_OK;
+  FE_CUDA(cudaMalloc(dst, bytes));
+  FE_CUDA(cudaMemcpy(*dst, src, bytes, cudaMemcpyHostToDevice));
+  return FE_OK;
+}
+#define replace_array(b, dst, src, count) \
+  replace_bytes((b), (void **)(dst), (const void *)(src), sizeof(**(dst)) * (count))
+
+int fe_set_ureys(fe_box *box, int n, const int *ab, const double *seq, const double *k) {
+  if (!box || n < 0 || (n > 0 && (!ab || !seq || !k))) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!sites_in_range(ab, 2 * (size_t)n, b->n)) {
+    set_error("fe_set_ureys: site index outside the box");
+    return FE_ERR_ARG;
+  }
+  int rc;
+  if ((rc = replace_array(b, &b->urey_ab, ab, 2 * (size_t)n))) return rc;
+  if ((rc = replace_array(b, &b->urey_seq, seq, (size_t)n))) return rc;
+  if ((rc = replace_array(b, &b->urey_k, k, (size_t)n))) return rc;
+  b->nurey = n;
+  drop_step_graphs(b);
+  return FE_OK;
+}
+
+int fe_set_torsions(fe_box *box, int n, const int *abcd, const double *kphi,
+                    const double *nphi, const double *delphi) {
+  if (!box || n < 0 || (n > 0 && (!abcd || !kphi || !nphi || !delphi))) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!sites_in_range(abcd, 4 * (size_t)n, b->n)) {
+    set_error("fe_set_torsions: site index outside the box");
+    return FE_ERR_ARG;
+  }
+  std::vector<double> par(18 * (size_t)n);
+  for (int i = 0; i < n; i++)
+    for (int t = 0; t < 6; t++) {
+      par[18 * (size_t)i + t] = kphi[6 * (size_t)i + t];
+      par[18 * (size_t)i + 6 + t] = nphi[6 * (size_t)i + t];
+      par[18 * (size_t)i + 12 + t] = delphi[6 * (size_t)i + t];
+    }
+  int rc;
+  if ((rc = replace_array(b, &b->tors_abcd, abcd, 4 * (size_t)n))) return rc;
+  if ((rc = replace_array(b, &b->tors_par, (const double *)par.data(), par.size()))) return rc;
+  std::vector<double> zero((size_t)n, 0.0);
+  if ((rc = replace_array(b, &b->tors_tau, (const double *)zero.data(), zero.size()))) return rc;
+  b->ntors = n;
+  drop_step_graphs(b);
+  return FE_OK;
+}
+
+int fe_set_impropers(fe_box *box, int n, const int *abcd, const double *kimpr,
+                     const double *angeq) {
+  if (!box || n < 0 || (n > 0 && (!abcd || !kimpr || !angeq))) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (!sites_in_range(abcd, 4 * (size_t)n, b->n)) {
+    set_error("fe_set_impropers: site index outside the box");
+    return FE_ERR_ARG;
+  }
+  int rc;
+  if ((rc = replace_array(b, &b->impr_abcd, abcd, 4 * (size_t)n))) return rc;
+  if ((rc = replace_array(b, &b->impr_k, kimpr, (size_t)n))) return rc;
+  if ((rc = replace_array(b, &b->impr_eq, angeq, (size_t)n))) return rc;
+  b->nimpr = n;
+  drop_step_graphs(b);
+  return FE_OK;
+}
+
+int fe_get_torsion_angles(fe_box *box, double *tau) {
+  if (!box || (!tau && box->b.ntors > 0)) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (b->ntors == 0) return FE_OK;
+  FE_CUDA(cudaMemcpyAsync(tau, b->tors_tau, sizeof(double) * b->ntors, cudaMemcpyDeviceToHost,
+                          b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_bonded_ext(fe_box *box, double *en3) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = launch_bonded_ext(b, false);
+  if (rc) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  if (en3)
+    for (int t = 0; t < 3; t++) en3[t] = b->nurey + b->ntors + b->nimpr ? b->host_scal[SC_UREY + t] : 0.0;
   return FE_OK;
 }
 

@@ -237,6 +237,9 @@ __device__ __forceinline__ void assemble_dev(double *__restrict__ s, double fan,
   if (with_bonded) {
     s[FE_EN_BOND] = s[SC_BOND];
     s[FE_EN_BEND] = s[SC_BEND];
+    s[FE_EN_UREY] = s[SC_UREY];
+    s[FE_EN_TORS] = s[SC_TORS];
+    s[FE_EN_IMPR] = s[SC_IMPR];
     s[FE_EN_NBOND] = e[0];
     s[FE_EN_NBONDS] = e[1];
     s[FE_EN_COULOMB] = e[2];
@@ -253,6 +256,36 @@ __device__ __forceinline__ void assemble_dev(double *__restrict__ s, double fan,
 // unparenthesised macro, defines.h:71).
 __device__ __forceinline__ double qfactor_mul(double x) {
   return ((((x * kELEC) * kELEQ) * kELEQ) * kNA) * 1.0E-3;
+}
+
+// pbc_all for one coordinate, bounded (the reference loops until inside)
+__device__ __forceinline__ double pbc_wrap(double d, double h, double l, int *bad) {
+  double pbc = 0.0;
+  int it = 0;
+  while (d < -h || d > h) {
+    if (d < -h) pbc = +l;
+    if (d > h) pbc = -l;
+    d += pbc;
+    if (++it > 64) {
+      *bad = 1;
+      break;
+    }
+  }
+  return d;
+}
+
+__device__ __forceinline__ void kinet_scalars(double *__restrict__ s) {
+  double f = (0.125) * (kNA * kAU * 10.0);  // kinet.c:50-65
+  for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
+  s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
+}
+
+__device__ __forceinline__ void record_dev(const double *__restrict__ s, double *__restrict__ rec,
+                                           long cap, int *__restrict__ counter) {
+  int c = *counter;
+  if (c < cap)
+    for (int t = 0; t < FE_EN_COUNT; t++) rec[(long)c * FE_EN_COUNT + t] = s[t];
+  *counter = c + 1;
 }
 
 }  // namespace fe

@@ -44,6 +44,7 @@ enum : int {
   SC_REALS,                        // eewald_reals
   SC_INTRA,                        // eewald_intra
   SC_BOND, SC_BEND,                // cbond, cbend
+  SC_UREY, SC_TORS, SC_IMPR,       // curey, ctorsion, cimproper
   SC_ENREC,                        // sum eterm * |S|^2 (before the fan factor)
   SC_FMEAN,                        // 3 slots: sum of the reciprocal forces
   SC_KEN = SC_FMEAN + 3,           // 6 slots: kinetic-energy tensor
@@ -87,6 +88,13 @@ struct Box {
   int nbond = 0, nbend = 0;
   int *bond_ab = nullptr, *bend_abc = nullptr;
   double *bond_req = nullptr, *bond_k = nullptr, *bend_t0 = nullptr, *bend_k = nullptr;
+  // Urey-Bradley, proper and improper torsions (fe_set_ureys / _torsions / _impropers)
+  int nurey = 0, ntors = 0, nimpr = 0;
+  int *urey_ab = nullptr, *tors_abcd = nullptr, *impr_abcd = nullptr;
+  double *urey_seq = nullptr, *urey_k = nullptr;
+  double *tors_par = nullptr;  // 18 per torsion: kphi[6], nphi[6], delphi[6]
+  double *tors_tau = nullptr;  // the angle of each torsion at the last evaluation
+  double *impr_k = nullptr, *impr_eq = nullptr;
 
   // cell grid for the list build
   int nc[3] = {1, 1, 1};
@@ -99,6 +107,9 @@ struct Box {
   int *nl_count = nullptr; // n
   int *nl_ent = nullptr;   // n * max_nb, entry = b * 8 + xflag
   bool have_list = false;
+  // set by step_body around a mixed NVE force evaluation: the force
+  // finalisation and the energy assembly run inside the second half kick
+  bool fold_tail = false;
 
   // SPME
   int G[3] = {0, 0, 0};
@@ -212,6 +223,9 @@ int launch_nl_check(Box *b, int lb, int ub, int *dflag);  // nblist.c:607-647
 int launch_pair64(Box *b);
 int pair_counts64(Box *b, long long *out4);  // instrumentation: half-list counts
 int launch_bonded64(Box *b);
+// Urey-Bradley, torsions, impropers: into ff (FP64 atomics) or the mixed
+// path's fixed-point sums (to_fixed); energies to SC_UREY..SC_IMPR
+int launch_bonded_ext(Box *b, bool to_fixed);
 // k_spme.cu
 int spme_setup(Box *b);
 int launch_charge_grid64(Box *b);
@@ -231,6 +245,10 @@ int launch_record(Box *b);
 // batched step, integrator side (every box of a batch per launch)
 BIntArgs make_bint_args(Box *b);
 void mixed_bint_fields(Box *b, BIntArgs *a);  // k_mixed.cu
+unsigned long long *mixed_force_sums(Box *b);  // k_mixed.cu: the fixed-point force sums
+// mixed NVE: force finalisation, energy assembly, second half kick, kinet, record
+int launch_vv2_mx_tail(Box *b);
+int launch_vv1_mx(Box *b, double vscal);  // k_integrate_mx.cu (mixed boxes)
 int launch_b_kinet_nhc(const BIntArgs *A, const int *off, int nbox, int blocks, cudaStream_t s);
 int launch_b_vv1(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
                  cudaStream_t s);

@@ -70,22 +70,6 @@ int launch_assemble_energies(Box *b, int with_bonded) {
   return FE_OK;
 }
 
-// pbc_all for one coordinate, bounded (the reference loops until inside)
-__device__ __forceinline__ double pbc_wrap(double d, double h, double l, int *bad) {
-  double pbc = 0.0;
-  int it = 0;
-  while (d < -h || d > h) {
-    if (d < -h) pbc = +l;
-    if (d > h) pbc = -l;
-    d += pbc;
-    if (++it > 64) {
-      *bad = 1;
-      break;
-    }
-  }
-  return d;
-}
-
 // integrate_vverlet.c:54-83: half kick, drift (atom and atnopbc), pbc_all
 __global__ void k_vv1(int n, double vscal, double dt, double dt_h, double3 L, double3 H,
                       const double *__restrict__ imass100, const double *__restrict__ ff,
@@ -117,6 +101,7 @@ __global__ void k_vv1(int n, double vscal, double dt, double dt_h, double3 L, do
 }
 
 int launch_vv1(Box *b, double vscal) {
+  if (b->mx) return launch_vv1_mx(b, vscal);
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   double3 H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);  // pbc_all.c hx
   double dt = b->p.dt, dt_h = 0.5 * b->p.dt;
@@ -440,19 +425,6 @@ int launch_xyz_gather(Box *b, double *xyz) {
 // velocity scale is applied inside the next per-site pass instead of in a
 // launch of its own, and the energy assembly rides on the second half kick.
 
-__device__ __forceinline__ void kinet_scalars(double *__restrict__ s) {
-  double f = (0.125) * (kNA * kAU * 10.0);  // kinet.c:50-65
-  for (int i = 0; i < 6; i++) s[SC_KEN + i] *= f;
-  s[FE_EN_KINET] = s[SC_KEN + 0] + s[SC_KEN + 2] + s[SC_KEN + 5];
-}
-
-__device__ __forceinline__ void record_dev(const double *__restrict__ s, double *__restrict__ rec,
-                                           long cap, int *__restrict__ counter) {
-  int c = *counter;
-  if (c < cap)
-    for (int t = 0; t < FE_EN_COUNT; t++) rec[(long)c * FE_EN_COUNT + t] = s[t];
-  *counter = c + 1;
-}
 
 // kinet (fixed point, as k_kinet_fix) and the first Nose-Hoover chain update
 __global__ void k_b_kinet_nhc(const BIntArgs *__restrict__ A, const int *__restrict__ off,

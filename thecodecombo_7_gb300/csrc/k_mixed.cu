@@ -179,10 +179,19 @@ __device__ __forceinline__ void k_mx_convert_body(VBlk vb_, int n, const double4
   }
 }
 
+// fix_zero (optional): the force sums to clear for the evaluation that follows
 __global__ void k_mx_convert(int n, const double4 *__restrict__ pos, const int *__restrict__ perm,
                              double3 invL, int4 *__restrict__ posfx,
                              const int4 *__restrict__ snap, float3 sc,
-                             unsigned *__restrict__ dmax2) {
+                             unsigned *__restrict__ dmax2, unsigned long long *__restrict__ fix_zero) {
+  if (fix_zero) {
+    int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s < n) {
+      fix_zero[3 * s] = 0ull;
+      fix_zero[3 * s + 1] = 0ull;
+      fix_zero[3 * s + 2] = 0ull;
+    }
+  }
   k_mx_convert_body(vblk_self(), n, pos, perm, invL, posfx, snap, sc, dmax2);
 }
 
@@ -528,6 +537,8 @@ struct MxPair {
   float rc2, kappa, c2k, qfe;  // c2k = 2 kappa / sqrt(pi); qfe = QFACTOR / epsRF
   float ron2, inv_sw_den;  // switch start^2 and 1 / (rc^2 - ron^2)^3
   float3 sc;                   // L / 2^32 per axis
+  int cubic;                   // Lx = Ly = Lz: distances formed in lattice units
+  float s2;                    // sc.x^2 (cubic boxes)
   // inner list: radius^2 (rc + skin)^2, and the squared displacement that
   // forces a prune ((skin / 2)^2, less a rounding margin)
   float rp2, thresh2;
@@ -551,6 +562,30 @@ __device__ __forceinline__ float erfc_nr_f(float z, float ex) {
   return t * ex * __expf(p);
 }
 
+// 2^x by the SFU's ex2.approx (PTX ISA): the exponential of the pair terms
+__device__ __forceinline__ float ex2_approx(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kLog2e = 1.44269504f;
+
+// the same fit as erfc_nr_f, erfc(z) = t exp(-z^2 + P(t)), with the two
+// exponents merged: t 2^(P(t) log2 e + q2), q2 = -z^2 log2 e given
+__device__ __forceinline__ float erfc_nr_q(float z, float q2) {
+  float t = __fdividef(1.0f, fmaf(0.5f, z, 1.0f));
+  float p = fmaf(t, 0.17087277f, -0.82215223f);
+  p = fmaf(t, p, 1.48851587f);
+  p = fmaf(t, p, -1.13520398f);
+  p = fmaf(t, p, 0.27886807f);
+  p = fmaf(t, p, -0.18628806f);
+  p = fmaf(t, p, 0.09678418f);
+  p = fmaf(t, p, 0.37409196f);
+  p = fmaf(t, p, 1.00002368f);
+  p = fmaf(t, p, -1.26551223f);
+  return t * ex2_approx(fmaf(p, kLog2e, q2));
+}
+
 struct PairAcc {
   float fx, fy, fz, e_lj, e_ljs, e_real, qsum;
 };
@@ -567,11 +602,13 @@ __device__ __forceinline__ void mx_pair_core(const MxPair &P, float qi, int j, i
   float r = r2 * rinv;
   float rinv2 = rinv * rinv;
   float qq = qi * __int_as_float(pj.w);
+  float qr = qq * rinv;
   float kr = P.kappa * r;
-  float ex = __expf(-kr * kr);
-  float erfckr = erfc_nr_f(kr, ex);
-  float F = qq * rinv * rinv2 * fmaf(P.c2k * r, ex, erfckr);
-  a.e_real = fmaf(qq * erfckr, rinv, a.e_real);
+  float q2 = (kr * -kLog2e) * kr;
+  float ex = ex2_approx(q2);  // exp(-(kappa r)^2)
+  float erfckr = erfc_nr_q(kr, q2);
+  float F = qr * rinv2 * fmaf(P.c2k * r, ex, erfckr);
+  a.e_real = fmaf(qr, erfckr, a.e_real);
   a.qsum += qq;
   if (WITH_LJ) {
     const float *lj = ljrow + type_s[j] * 3;
@@ -600,20 +637,38 @@ __device__ __forceinline__ void mx_pair_core(const MxPair &P, float qi, int j, i
   a.fz = fmaf(F, dz, a.fz);
 }
 
-template <bool WITH_LJ>
+// the separation of sites pi and pj: in A, or (CUBIC) in lattice units of
+// L / 2^32 with r2 in A^2 -- the force sums are then scaled once per row
+template <bool CUBIC>
+__device__ __forceinline__ float mx_sep(const MxPair &P, int4 pi, int4 pj, float &dx, float &dy,
+                                        float &dz) {
+  if (CUBIC) {
+    dx = __int2float_rn((int)((unsigned)pi.x - (unsigned)pj.x));
+    dy = __int2float_rn((int)((unsigned)pi.y - (unsigned)pj.y));
+    dz = __int2float_rn((int)((unsigned)pi.z - (unsigned)pj.z));
+    return P.s2 * fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  }
+  dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, P.sc.x);
+  dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, P.sc.y);
+  dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, P.sc.z);
+  return dx * dx + dy * dy + dz * dz;
+}
+
+template <bool WITH_LJ, bool CUBIC>
 __device__ __forceinline__ void mx_pair_one(const MxPair &P, int4 pi, float qi, int j, int4 pj,
                                             const float *__restrict__ ljrow,
                                             const int *__restrict__ type_s, PairAcc &a) {
-  float dx = fx_delta((unsigned)pi.x, (unsigned)pj.x, P.sc.x);
-  float dy = fx_delta((unsigned)pi.y, (unsigned)pj.y, P.sc.y);
-  float dz = fx_delta((unsigned)pi.z, (unsigned)pj.z, P.sc.z);
-  mx_pair_core<WITH_LJ>(P, qi, j, pj, dx, dy, dz, dx * dx + dy * dy + dz * dz, ljrow, type_s, a);
+  float dx, dy, dz;
+  float r2 = mx_sep<CUBIC>(P, pi, pj, dx, dy, dz);
+  mx_pair_core<WITH_LJ>(P, qi, j, pj, dx, dy, dz, r2, ljrow, type_s, a);
 }
 
 // Walks entries b0 + lane, b0 + lane + 32, ... of a row with a two-deep
 // software pipeline: the entry two iterations ahead and the j position one
-// iteration ahead are in flight while the current pair is computed.
-template <bool WITH_LJ>
+// iteration ahead are in flight while the current pair is computed.  The loop
+// body covers two entries, so the in-flight values change registers without
+// copies.
+template <bool WITH_LJ, bool CUBIC>
 __device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
                                            const int *__restrict__ row, int b0, int b1, int lane,
                                            const int4 *__restrict__ posfx,
@@ -621,19 +676,22 @@ __device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
                                            const int *__restrict__ type_s, PairAcc &a) {
   int i = b0 + lane;
   if (i >= b1) return;
-  int e_cur = row[i];
-  int e_nxt = i + 32 < b1 ? row[i + 32] : -1;
-  int4 p_cur = posfx[e_cur];
+  int e0 = row[i];
+  int e1 = i + 32 < b1 ? row[i + 32] : -1;
+  int4 p0 = posfx[e0];
   while (true) {
-    int e_nn = (e_nxt >= 0 && i + 64 < b1) ? row[i + 64] : -1;
-    int4 p_nxt = make_int4(0, 0, 0, 0);
-    if (e_nxt >= 0) p_nxt = posfx[e_nxt];
-    mx_pair_one<WITH_LJ>(P, pi, qi, e_cur, p_cur, ljrow, type_s, a);
-    if (e_nxt < 0) break;
-    e_cur = e_nxt;
-    p_cur = p_nxt;
-    e_nxt = e_nn;
-    i += 32;
+    int e2 = (e1 >= 0 && i + 64 < b1) ? row[i + 64] : -1;
+    int4 p1 = make_int4(0, 0, 0, 0);
+    if (e1 >= 0) p1 = posfx[e1];
+    mx_pair_one<WITH_LJ, CUBIC>(P, pi, qi, e0, p0, ljrow, type_s, a);
+    if (e1 < 0) break;
+    int e3 = (e2 >= 0 && i + 96 < b1) ? row[i + 96] : -1;
+    if (e2 >= 0) p0 = posfx[e2];
+    mx_pair_one<WITH_LJ, CUBIC>(P, pi, qi, e1, p1, ljrow, type_s, a);
+    if (e2 < 0) break;
+    e0 = e2;
+    e1 = e3;
+    i += 64;
   }
 }
 
@@ -643,7 +701,7 @@ __device__ __forceinline__ void mx_segment(const MxPair &P, int4 pi, float qi,
 // same two-deep pipeline), but the loop runs the warp's common trip count so
 // that the appends can use warp ballots; lanes past the row end compute
 // nothing and append nothing.
-template <bool WITH_LJ>
+template <bool WITH_LJ, bool CUBIC>
 __device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float qi,
                                                  const int *__restrict__ row, int b0, int b1,
                                                  int lane, unsigned lt,
@@ -660,10 +718,8 @@ __device__ __forceinline__ void mx_segment_prune(const MxPair &P, int4 pi, float
     int e_nn = i + 64 < b1 ? row[i + 64] : 0;
     int4 p_nxt = posfx[e_nxt];
     bool v = i < b1;
-    float dx = fx_delta((unsigned)pi.x, (unsigned)p_cur.x, P.sc.x);
-    float dy = fx_delta((unsigned)pi.y, (unsigned)p_cur.y, P.sc.y);
-    float dz = fx_delta((unsigned)pi.z, (unsigned)p_cur.z, P.sc.z);
-    float r2 = dx * dx + dy * dy + dz * dz;
+    float dx, dy, dz;
+    float r2 = mx_sep<CUBIC>(P, pi, p_cur, dx, dy, dz);
     if (v) mx_pair_core<WITH_LJ>(P, qi, e_cur, p_cur, dx, dy, dz, r2, ljrow, type_s, a);
     row_push_bf(v && r2 < P.rp2, WITH_LJ, e_cur, lt, P.cap, irow, rc);
     e_cur = e_nxt;
@@ -730,15 +786,29 @@ __device__ __forceinline__ void k_mx_pair_body(VBlk vb_, MxPair P, const int4 *_
     if (PRUNE && P.inner_on) {
       int *irow = ient + (size_t)s * P.cap;
       RowCursor rc = {0, 0};
-      mx_segment_prune<true>(P, pi, qi, row, 0, rlj[s], lane, lt, posfx, ljrow, type_s, irow, rc,
-                             a);
-      mx_segment_prune<false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, lt, posfx, ljrow,
-                              type_s, irow, rc, a);
+      if (P.cubic) {
+        mx_segment_prune<true, true>(P, pi, qi, row, 0, rlj[s], lane, lt, posfx, ljrow, type_s,
+                                     irow, rc, a);
+        mx_segment_prune<false, true>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, lt, posfx,
+                                      ljrow, type_s, irow, rc, a);
+      } else {
+        mx_segment_prune<true, false>(P, pi, qi, row, 0, rlj[s], lane, lt, posfx, ljrow, type_s,
+                                      irow, rc, a);
+        mx_segment_prune<false, false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, lt, posfx,
+                                       ljrow, type_s, irow, rc, a);
+      }
       row_close(rc, P.cap, s, lane, icnt_lj, icnt_nl, status);
       if (lane == 0) snap[s] = pi;
     } else {
-      mx_segment<true>(P, pi, qi, row, 0, rlj[s], lane, posfx, ljrow, type_s, a);
-      mx_segment<false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, posfx, ljrow, type_s, a);
+      if (P.cubic) {
+        mx_segment<true, true>(P, pi, qi, row, 0, rlj[s], lane, posfx, ljrow, type_s, a);
+        mx_segment<false, true>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, posfx, ljrow,
+                                type_s, a);
+      } else {
+        mx_segment<true, false>(P, pi, qi, row, 0, rlj[s], lane, posfx, ljrow, type_s, a);
+        mx_segment<false, false>(P, pi, qi, row, P.cap - rnl[s], P.cap, lane, posfx, ljrow,
+                                 type_s, a);
+      }
     }
     // the row's force: a fixed butterfly of FP32 partial sums (deterministic),
     // converted once to the fixed-point accumulators
@@ -748,6 +818,11 @@ __device__ __forceinline__ void k_mx_pair_body(VBlk vb_, MxPair P, const int4 *_
       fx += __shfl_xor_sync(0xffffffffu, fx, o);
       fy += __shfl_xor_sync(0xffffffffu, fy, o);
       fz += __shfl_xor_sync(0xffffffffu, fz, o);
+    }
+    if (P.cubic) {  // lattice units to A
+      fx *= P.sc.x;
+      fy *= P.sc.x;
+      fz *= P.sc.x;
     }
     // every pair is visited from both ends: half of each row's energy
     float e[4] = {0.5f * a.e_lj, 0.5f * a.e_ljs, 0.5f * a.e_real, 0.5f * a.qsum};
@@ -1058,6 +1133,54 @@ __global__ void k_mx_spread_red(int n, int order, int3 G, const int4 *__restrict
   k_mx_spread_red_body(vblk_self(), n, order, G, posfx, sm, floor3, gfix);
 }
 
+// Order 4 (the configured workloads): the spline weights are computed where
+// they are used, from the site's 32-bit fixed-point coordinate, instead of
+// being stored by a separate pass and read back (fillspline_f with a
+// constant order unrolls into registers).
+__device__ __forceinline__ void spline4_axis(unsigned u, int g, int &fl, float (&m)[5],
+                                             float (&dm)[5]) {
+  unsigned long long t = (unsigned long long)u * (unsigned)g;
+  fl = (int)(t >> 32);
+  fillspline_f(4, (float)(unsigned)(t & 0xffffffffull) * 0x1p-32f, m, dm);
+}
+
+__device__ __forceinline__ void k_mx_spread4_body(VBlk vb_, int n, int3 G,
+                                                  const int4 *__restrict__ posfx,
+                                                  unsigned long long *__restrict__ gfix) {
+  int t = vb_.id * blockDim.x + threadIdx.x;
+  int s = t >> 2, mx = t & 3;
+  if (s >= n) return;
+  int4 p = posfx[s];
+  float wx[5], wy[5], wz[5], dd[5];
+  int fx, fy, fz;
+  spline4_axis((unsigned)p.x, G.x, fx, wx, dd);
+  spline4_axis((unsigned)p.y, G.y, fy, wy, dd);
+  spline4_axis((unsigned)p.z, G.z, fz, wz, dd);
+  float w_mx = mx == 0 ? wx[1] : mx == 1 ? wx[2] : mx == 2 ? wx[3] : wx[4];
+  float qwx = __int_as_float(p.w) * w_mx;
+  int x = fx - 3 + mx, y0 = fy - 3, z0 = fz - 3;
+  if (x < 0) x += G.x;
+  unsigned long long *gx = gfix + (size_t)x * G.y * G.z;
+#pragma unroll
+  for (int my = 0; my < 4; my++) {
+    int y = y0 + my;
+    if (y < 0) y += G.y;
+    float v = qwx * wy[my + 1];
+    unsigned long long *gy = gx + (size_t)y * G.z;
+#pragma unroll
+    for (int mz = 0; mz < 4; mz++) {
+      int z = z0 + mz;
+      if (z < 0) z += G.z;
+      atomicAdd(gy + z, (unsigned long long)__float2ll_rn(v * wz[mz + 1] * kSpRedFix));
+    }
+  }
+}
+
+__global__ void k_mx_spread4(int n, int3 G, const int4 *__restrict__ posfx,
+                             unsigned long long *__restrict__ gfix) {
+  k_mx_spread4_body(vblk_self(), n, G, posfx, gfix);
+}
+
 // FP32 grid from the fixed-point sums; the sums are cleared for the next step
 // (two points per thread and iteration: 16-byte loads and stores)
 __device__ __forceinline__ void k_mx_fix2grid_body(VBlk vb_, long K, unsigned long long *__restrict__ gfix,
@@ -1160,6 +1283,70 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
                             unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                             double *__restrict__ out) {
   k_mx_gather_body(vblk_self(), n, order, G, gl, qfe, posfx, perm, floor3, sm, sd, grid, fix, facc, ticket, out);
+}
+
+// gather with the order-4 weights and derivatives computed in registers
+__device__ __forceinline__ void k_mx_gather4_body(VBlk vb_, int n, int3 G, float3 gl, float qfe,
+                                                  const int4 *__restrict__ posfx,
+                                                  const int *__restrict__ perm,
+                                                  const float *__restrict__ grid,
+                                                  unsigned long long *__restrict__ fix,
+                                                  unsigned long long *__restrict__ facc,
+                                                  unsigned *__restrict__ ticket,
+                                                  double *__restrict__ out) {
+  long long sx = 0, sy = 0, sz = 0;
+  for (int s = vb_.id * blockDim.x + threadIdx.x; s < n; s += vb_.n * blockDim.x) {
+    int4 p = posfx[s];
+    float m[3][5], dm[3][5];
+    int fl[3];
+    spline4_axis((unsigned)p.x, G.x, fl[0], m[0], dm[0]);
+    spline4_axis((unsigned)p.y, G.y, fl[1], m[1], dm[1]);
+    spline4_axis((unsigned)p.z, G.z, fl[2], m[2], dm[2]);
+    float fxi = 0.f, fyi = 0.f, fzi = 0.f;
+    int xo = fl[0] - 4, yo0 = fl[1] - 4, zo0 = fl[2] - 4;
+#pragma unroll
+    for (int xi = 1; xi <= 4; xi++) {
+      int x = wrap1(xo + xi, G.x);
+      float mx = m[0][xi], dmx = dm[0][xi];
+#pragma unroll
+      for (int yi = 1; yi <= 4; yi++) {
+        int y = wrap1(yo0 + yi, G.y);
+        float my = m[1][yi], dmy = dm[1][yi];
+        const float *row = grid + ((long)x * G.y + y) * G.z;
+#pragma unroll
+        for (int zi = 1; zi <= 4; zi++) {
+          int z = wrap1(zo0 + zi, G.z);
+          float mz = m[2][zi], dmz = dm[2][zi];
+          float term = row[z];
+          fxi -= dmx * my * mz * term;
+          fyi -= mx * dmy * mz * term;
+          fzi -= mx * my * dmz * term;
+        }
+      }
+    }
+    float fac = __int_as_float(p.w) * qfe;
+    fxi *= fac * gl.x;
+    fyi *= fac * gl.y;
+    fzi *= fac * gl.z;
+    int oi = perm[s];
+    long long qx = to_fix(fxi), qy = to_fix(fyi), qz = to_fix(fzi);
+    atomicAdd(&fix[3 * oi], (unsigned long long)qx);
+    atomicAdd(&fix[3 * oi + 1], (unsigned long long)qy);
+    atomicAdd(&fix[3 * oi + 2], (unsigned long long)qz);
+    sx += qx;
+    sy += qy;
+    sz += qz;
+  }
+  long long v[3] = {sx, sy, sz};
+  block_fix_final<3>(v, 0, facc, ticket, out, vb_);
+}
+
+__global__ void k_mx_gather4(int n, int3 G, float3 gl, float qfe, const int4 *__restrict__ posfx,
+                             const int *__restrict__ perm, const float *__restrict__ grid,
+                             unsigned long long *__restrict__ fix,
+                             unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
+                             double *__restrict__ out) {
+  k_mx_gather4_body(vblk_self(), n, G, gl, qfe, posfx, perm, grid, fix, facc, ticket, out);
 }
 
 // FP64 forces from the fixed-point sums, minus the mean reciprocal force
@@ -1599,12 +1786,12 @@ static float3 fix_scale(Box *b) {
                      (float)(b->p.L[2] / kFixScale));
 }
 
-static int launch_convert(Box *b) {
+static int launch_convert(Box *b, bool zero_forces = false) {
   Mixed &M = *b->mx;
   double3 invL = make_double3(1.0 / b->p.L[0], 1.0 / b->p.L[1], 1.0 / b->p.L[2]);
   k_mx_convert<<<(b->n + 255) / 256, 256, 0, b->stream>>>(
       b->n, b->pos_q, M.perm, invL, M.posfx, M.inner_on ? M.snap : nullptr, fix_scale(b),
-      &M.ps->dmax2);
+      &M.ps->dmax2, zero_forces ? M.fix : nullptr);
   FE_LAUNCH_CHECK("k_mx_convert");
   return FE_OK;
 }
@@ -1665,6 +1852,8 @@ MxPair mx_pair_params(Box *b) {
   P.ron2 = (float)ron2;
   P.inv_sw_den = ron2 > 0.0 ? (float)(1.0 / ((rc2 - ron2) * (rc2 - ron2) * (rc2 - ron2))) : 0.f;
   P.sc = fix_scale(b);
+  P.cubic = (b->p.L[0] == b->p.L[1] && b->p.L[1] == b->p.L[2]) ? 1 : 0;
+  P.s2 = P.sc.x * P.sc.x;
   double rp = b->p.rc + M.skin, hs = 0.5 * M.skin - 1e-4;
   P.rp2 = (float)(rp * rp);
   P.thresh2 = (float)(hs * hs);
@@ -1762,9 +1951,14 @@ int launch_mx_spread_only(Box *b) {
   Mixed &M = *b->mx;
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   long nt = (long)b->n * b->order;
-  k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, b->order, G, M.posfx,
-                                                                     M.sm, M.floor3, M.gfix);
-  FE_LAUNCH_CHECK("k_mx_spread_red");
+  if (b->order == 4) {
+    k_mx_spread4<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, G, M.posfx, M.gfix);
+    FE_LAUNCH_CHECK("k_mx_spread4");
+  } else {
+    k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(
+        b->n, b->order, G, M.posfx, M.sm, M.floor3, M.gfix);
+    FE_LAUNCH_CHECK("k_mx_spread_red");
+  }
   k_mx_fix2grid<<<M.nsm * 8, 256, 0, b->stream>>>(b->K, M.gfix, M.grid32);
   FE_LAUNCH_CHECK("k_mx_fix2grid");
   return FE_OK;
@@ -1774,8 +1968,7 @@ int forces_mixed(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
   int rc;
-  if ((rc = launch_convert(b))) return rc;
-  FE_CUDA(cudaMemsetAsync(M.fix, 0, sizeof(unsigned long long) * 3 * n, b->stream));
+  if ((rc = launch_convert(b, true))) return rc;  // also clears the force sums
   if ((rc = launch_mx_pair_only(b))) return rc;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
   // intramolecular terms: one thread per molecule when the topology allows,
@@ -1817,11 +2010,15 @@ int forces_mixed(Box *b) {
                                            b->scal + SC_BOND);
     FE_LAUNCH_CHECK("k_mx_bonded");
   }
+  // Urey-Bradley, torsions and impropers (FP64, into the fixed-point sums)
+  if ((rc = launch_bonded_ext(b, true))) return rc;
   // SPME
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
-  k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, M.posfx, M.floor3, M.sm,
-                                                       M.sd);
-  FE_LAUNCH_CHECK("k_mx_splines");
+  if (b->order != 4) {  // order 4 computes its weights inside spreading and gathering
+    k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, M.posfx, M.floor3,
+                                                         M.sm, M.sd);
+    FE_LAUNCH_CHECK("k_mx_splines");
+  }
   if ((rc = launch_mx_spread_only(b))) return rc;
   cufftResult r = cufftSetStream(M.plan_r2c, b->stream);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
@@ -1841,10 +2038,17 @@ int forces_mixed(Box *b) {
   int gb = (n + 127) / 128;
   if (gb > 1024) gb = 1024;
   float qfe = (float)(qf / b->p.epsRF);
-  k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3, M.sm,
-                                         M.sd, M.grid32, M.fix, b->facc, b->ticket,
-                                         b->scal + SC_FMEAN);
-  FE_LAUNCH_CHECK("k_mx_gather");
+  if (b->order == 4) {
+    k_mx_gather4<<<gb, 128, 0, b->stream>>>(n, G, gl, qfe, M.posfx, M.perm, M.grid32, M.fix,
+                                            b->facc, b->ticket, b->scal + SC_FMEAN);
+    FE_LAUNCH_CHECK("k_mx_gather4");
+  } else {
+    k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3,
+                                           M.sm, M.sd, M.grid32, M.fix, b->facc, b->ticket,
+                                           b->scal + SC_FMEAN);
+    FE_LAUNCH_CHECK("k_mx_gather");
+  }
+  if (b->fold_tail) return FE_OK;  // finalised inside the second half kick
   k_mx_finalize<<<(3 * n + 255) / 256, 256, 0, b->stream>>>(n, M.fix, b->scal, b->ff);
   FE_LAUNCH_CHECK("k_mx_finalize");
   return launch_mixed_assemble(b);
@@ -1959,6 +2163,21 @@ __global__ void k_b_mx_spread(const BMxArgs *__restrict__ A, const int *__restri
   const int r = vblk_box(off, nbox);
   const BMxArgs &a = A[r];
   k_mx_spread_red_body(vblk_of(off, r), a.n, a.order, a.G, a.posfx, a.sm, a.floor3, a.gfix);
+}
+
+__global__ void k_b_mx_spread4(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                               int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_spread4_body(vblk_of(off, r), a.n, a.G, a.posfx, a.gfix);
+}
+
+__global__ void k_b_mx_gather4(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+                               int nbox) {
+  const int r = vblk_box(off, nbox);
+  const BMxArgs &a = A[r];
+  k_mx_gather4_body(vblk_of(off, r), a.n, a.G, a.gl, a.qfe, a.posfx, a.perm, a.grid32, a.fix,
+                    a.facc, a.ticket, a.scal + SC_FMEAN);
 }
 
 __global__ void k_b_mx_fix2grid(const BMxArgs *__restrict__ A, const int *__restrict__ off,
@@ -2085,6 +2304,7 @@ struct BMxPlan {
   BMxRange convert, prune, pair, intra, splines, spread, fix2grid, recip, gather, finalize;
   BMxRange cell, fill, cellsort, list;
   int intra_ns = 3;
+  bool order4 = true;  // every box has B-spline order 4: weights computed in place
   size_t pair_shm = 0;
   std::vector<BMxGroup> groups;
 };
@@ -2116,6 +2336,8 @@ void mixed_batch_free(BMxPlan *P) {
   delete P;
 }
 
+unsigned long long *mixed_force_sums(Box *b) { return b->mx ? b->mx->fix : nullptr; }
+
 void mixed_bint_fields(Box *b, BIntArgs *a) {
   if (!b->mx) return;
   a->erfc_rc_over_rc = b->mx->erfc_rc_over_rc;
@@ -2130,6 +2352,12 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
   for (int r = 0; r < nbox; r++)
     if (!boxes[r]->mx || boxes[r]->mx->nmol == 0 || boxes[r]->mx->intra_maxs > kIntraMaxSites) {
       set_error("batched force evaluation: mixed-precision boxes of contiguous molecules only");
+      return FE_ERR_ARG;
+    }
+  for (int r = 0; r < nbox; r++)
+    if (boxes[r]->nurey + boxes[r]->ntors + boxes[r]->nimpr > 0) {
+      set_error("batched force evaluation: boxes with Urey-Bradley, torsion or improper terms "
+                "run box by box");
       return FE_ERR_ARG;
     }
   BMxPlan *P = new BMxPlan();
@@ -2254,6 +2482,7 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
     brec.push_back((int)std::min<long>(1024L, (b->Kh + 255) / 256));
     bgat.push_back(std::min(1024, (b->n + 127) / 128));
     bfin.push_back((3 * b->n + 255) / 256);
+    if (b->order != 4) P->order4 = false;
     bcell.push_back((b->n + 255) / 256);
     bfill.push_back((b->n + 255) / 256);
     bsort.push_back(M.ncells);
@@ -2356,10 +2585,15 @@ int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
   else if (P->intra_ns <= 4) k_b_mx_intra<4><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
   else k_b_mx_intra<kIntraMaxSites><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_intra");
-  k_b_mx_splines<<<P->splines.total, 128, 0, s>>>(P->d_args, P->splines.d_off, nb);
-  FE_LAUNCH_CHECK("k_b_mx_splines");
-  k_b_mx_spread<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
-  FE_LAUNCH_CHECK("k_b_mx_spread");
+  if (P->order4) {
+    k_b_mx_spread4<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_spread4");
+  } else {
+    k_b_mx_splines<<<P->splines.total, 128, 0, s>>>(P->d_args, P->splines.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_splines");
+    k_b_mx_spread<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_spread");
+  }
   k_b_mx_fix2grid<<<P->fix2grid.total, 256, 0, s>>>(P->d_args, P->fix2grid.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_fix2grid");
   for (BMxGroup &g : P->groups) {
@@ -2374,8 +2608,13 @@ int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
     if (r == CUFFT_SUCCESS) r = cufftExecC2R(g.c2r, g.cplx, g.real);
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R (batch)");
   }
-  k_b_mx_gather<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
-  FE_LAUNCH_CHECK("k_b_mx_gather");
+  if (P->order4) {
+    k_b_mx_gather4<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_gather4");
+  } else {
+    k_b_mx_gather<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_gather");
+  }
   k_b_mx_finalize<<<P->finalize.total, 256, 0, s>>>(P->d_args, P->finalize.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_finalize");
   return FE_OK;

@@ -71,8 +71,10 @@ __device__ __forceinline__ double rex_kT(double T) { return ((kKB * kNA) * T) * 
 
 // The reference's en[k].potens for the water force field (calcvalue.c:43):
 // bond + bend + nbonds (torsion, improper and Urey-Bradley terms are zero).
+// en[k].potens of calcvalue.c:45-53 (no GOLIK, no SASA, not NEUTRAL)
 __device__ __forceinline__ double rex_potens(const double *s) {
-  return s[FE_EN_BOND] + s[FE_EN_BEND] + s[FE_EN_NBONDS];
+  return s[FE_EN_BOND] + s[FE_EN_BEND] + s[FE_EN_TORS] + s[FE_EN_NBONDS] + s[FE_EN_IMPR] +
+         s[FE_EN_UREY];
 }
 
 __global__ void k_rex_decide(int R, const RexRep *__restrict__ rep, const double *__restrict__ Tslot,

@@ -42,6 +42,12 @@
  * (forces_mc.c:511-534).  The reference's MC forces (ffox ..) are not
  * produced: the moves use energies only.
  *
+ * Bonded terms: bonds and bends come with the box; Urey-Bradley (urey[k]),
+ * torsion (tors[k]) and improper (impr[k]) records are uploaded once with it
+ * (fe_set_ureys / fe_set_torsions / fe_set_impropers), forces() fills
+ * en[k].urey, .tors and .impr, and each torsion's angle goes back to
+ * tors[k][i].phi / psi / theta when the system tags any (ctorsion.c:172-175).
+ *
  * Errors print the engine's message and exit() with the reference's codes
  * (5: neighbour list over capacity, nblist.c:185-197; 20: non-neutral box,
  * ewald.c:185-194; 1 otherwise).  FE_PRECISION=mixed in the environment
@@ -82,22 +88,81 @@ static int env_on(const char *name) {
   return v && v[0] == '1';
 }
 
+/* Urey-Bradley (urey[k]), torsion (tors[k]) and improper (impr[k]) records
+ * of read_topology.c, uploaded once with the box. */
+static void set_ext_bonded(fe_box *b, int k) {
+#ifndef NEUTRAL
+  int nu = ureyN[k];
+  if (nu > 0) {
+    int *ab = malloc(sizeof(int) * 2 * nu);
+    double *seq = malloc(sizeof(double) * nu), *kk = malloc(sizeof(double) * nu);
+    for (int i = 0; i < nu; i++) {
+      ab[2 * i] = urey[k][i].a;
+      ab[2 * i + 1] = urey[k][i].b;
+      seq[i] = urey[k][i].Seq;
+      kk[i] = urey[k][i].k;
+    }
+    FE_OR_DIE(fe_set_ureys(b, nu, ab, seq, kk), "setup (ureys)");
+    free(ab); free(seq); free(kk);
+  }
+#endif
+  int nt = torsN[k];
+  if (nt > 0) {
+    int *abcd = malloc(sizeof(int) * 4 * nt);
+    double *kp = malloc(sizeof(double) * 6 * nt), *np = malloc(sizeof(double) * 6 * nt);
+    double *dp = malloc(sizeof(double) * 6 * nt);
+    for (int i = 0; i < nt; i++) {
+      abcd[4 * i] = tors[k][i].a;
+      abcd[4 * i + 1] = tors[k][i].b;
+      abcd[4 * i + 2] = tors[k][i].c;
+      abcd[4 * i + 3] = tors[k][i].d;
+      for (int t = 0; t < 6; t++) {
+        kp[6 * i + t] = tors[k][i].kphi[t];
+        np[6 * i + t] = tors[k][i].nphi[t];
+        dp[6 * i + t] = tors[k][i].delphi[t];
+      }
+    }
+    FE_OR_DIE(fe_set_torsions(b, nt, abcd, kp, np, dp), "setup (torsions)");
+    free(abcd); free(kp); free(np); free(dp);
+  }
+  int ni = imprN[k];
+  if (ni > 0) {
+    int *abcd = malloc(sizeof(int) * 4 * ni);
+    double *kk = malloc(sizeof(double) * ni), *eq = malloc(sizeof(double) * ni);
+    for (int i = 0; i < ni; i++) {
+      abcd[4 * i] = impr[k][i].a;
+      abcd[4 * i + 1] = impr[k][i].b;
+      abcd[4 * i + 2] = impr[k][i].c;
+      abcd[4 * i + 3] = impr[k][i].d;
+      kk[i] = impr[k][i].kimpr;
+      eq[i] = impr[k][i].angeq;
+    }
+    FE_OR_DIE(fe_set_impropers(b, ni, abcd, kk, eq), "setup (impropers)");
+    free(abcd); free(kk); free(eq);
+  }
+}
+
+/* ctorsion.c:172-175: each torsion's angle into phi / psi / theta by its tag */
+static void put_torsion_angles(fe_box *b, int k) {
+  int nt = torsN[k], tagged = 0;
+  for (int i = 0; i < nt && !tagged; i++)
+    tagged = tors[k][i].phitag == 1 || tors[k][i].psitag == 1 || tors[k][i].thetag == 1;
+  if (!tagged) return;
+  double *tau = malloc(sizeof(double) * nt);
+  FE_OR_DIE(fe_get_torsion_angles(b, tau), "torsion angles");
+  for (int i = 0; i < nt; i++) {
+    if (tors[k][i].phitag == 1) tors[k][i].phi = tau[i];
+    else if (tors[k][i].psitag == 1) tors[k][i].psi = tau[i];
+    else if (tors[k][i].thetag == 1) tors[k][i].theta = tau[i];
+  }
+  free(tau);
+}
+
 /* Builds the engine's box k from the reference's globals (sim, box[k],
  * pott[k], atom[k], ljset, bond[k], bend[k], xint[k], nhc[k]). */
 static fe_box *fe_of(int k) {
   if (g_fe[k]) return g_fe[k];
   int n = box[k].boxns;
-  if (torsN[k] > 0 || imprN[k] > 0
-#ifndef NEUTRAL
-      || ureyN[k] > 0
-#endif
-  ) {
-#ifdef FE_DROPIN_MD
-    fprintf(stdout, "GPU engine: torsions, impropers and Urey-Bradley terms are not on the "
-                    "device path; use the CPU build for this system\n");
-    exit(1);
-#endif
-  }
   double *q = malloc(sizeof(double) * n), *mass = malloc(sizeof(double) * n);
   int *type = malloc(sizeof(int) * n);
   for (int i = 0; i < n; i++) {
@@ -187,6 +252,7 @@ static fe_box *fe_of(int k) {
   free(q); free(mass); free(type); free(eps); free(sig); free(bab); free(aabc); free(breq);
   free(bk); free(at0); free(ak); free(xab); free(xfl);
   if (nhc[k].zeta) FE_OR_DIE(fe_set_nhc_state(g_fe[k], &nhc[k].zeta[0].r), "setup");
+  set_ext_bonded(g_fe[k], k);
   return g_fe[k];
 }
 
@@ -252,10 +318,11 @@ static void put_energies(int k, const double *e) {
   en[k].bond = e[FE_EN_BOND];
   en[k].bend = e[FE_EN_BEND];
 #ifndef NEUTRAL
-  en[k].urey = 0.0;
+  en[k].urey = e[FE_EN_UREY];
 #endif
-  en[k].tors = 0.0;
-  en[k].impr = 0.0;
+  en[k].tors = e[FE_EN_TORS];
+  en[k].impr = e[FE_EN_IMPR];
+  put_torsion_angles(g_fe[k], k);
   en[k].nbond = e[FE_EN_NBOND];
   en[k].nbonds = e[FE_EN_NBONDS];
   en[k].coulomb = e[FE_EN_COULOMB];

@@ -32,7 +32,7 @@ FE_ERR_SIZE = 32
 FE_PREC_FP64 = 0
 FE_PREC_MIXED = 1
 EN_KEYS = ["kinet", "bond", "bend", "nbond", "nbonds", "coulomb", "rewald", "rewalds",
-           "kewald", "sewald", "iewald", "tewald"]
+           "kewald", "sewald", "iewald", "tewald", "urey", "tors", "impr"]
 FE_EN_COUNT = len(EN_KEYS)
 
 # symbols of include/fe.h (checked by the tests against the built library)
@@ -57,7 +57,8 @@ EXPORTS = [
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
     "fe_go_get_stream", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
     "fe_mc_delta_terms", "fe_mc_site_energy", "fe_drift", "fe_box_set_temperature",
-    "fe_bspline", "fe_batch_set_fused",
+    "fe_bspline", "fe_batch_set_fused", "fe_set_ureys", "fe_set_torsions", "fe_set_impropers",
+    "fe_get_torsion_angles", "fe_bonded_ext",
 ]
 FE_KERNEL_PAIR = 0
 FE_KERNEL_SPREAD = 1
@@ -204,6 +205,8 @@ class Box:
         self.n = sysm.n
         self.set_positions(sysm.pos, nopbc=True)
         self.set_velocities(sysm.vel)
+        if getattr(sysm, "has_ext_bonded", False):
+            self.set_ext_bonded(sysm)
 
     # ---- plumbing ----
     def _check(self, rc):
@@ -331,6 +334,34 @@ class Box:
         e = np.empty(2)
         self._check(self.lib.fe_bonded(self.h, _p(e)))
         return e
+
+    def set_ext_bonded(self, sysm):
+        """Urey-Bradley, proper and improper torsion terms of sysm."""
+        ab = _c(sysm.ureys, np.int32)
+        self._check(self.lib.fe_set_ureys(self.h, ab.shape[0], _p(ab),
+                                          _p(_c(sysm.urey_seq, np.float64)),
+                                          _p(_c(sysm.urey_k, np.float64))))
+        t = _c(sysm.tors, np.int32)
+        self._check(self.lib.fe_set_torsions(self.h, t.shape[0], _p(t),
+                                             _p(_c(sysm.tors_kphi, np.float64)),
+                                             _p(_c(sysm.tors_nphi, np.float64)),
+                                             _p(_c(sysm.tors_delphi, np.float64))))
+        m = _c(sysm.impr, np.int32)
+        self._check(self.lib.fe_set_impropers(self.h, m.shape[0], _p(m),
+                                              _p(_c(sysm.impr_k, np.float64)),
+                                              _p(_c(sysm.impr_eq, np.float64))))
+        self.ntors = t.shape[0]
+
+    def bonded_ext(self):
+        """curey, ctorsion, cimproper energies (forces added into ff)."""
+        e = np.empty(3)
+        self._check(self.lib.fe_bonded_ext(self.h, _p(e)))
+        return e
+
+    def torsion_angles(self):
+        tau = np.empty(max(getattr(self, "ntors", 0), 1))
+        self._check(self.lib.fe_get_torsion_angles(self.h, _p(tau)))
+        return tau[:getattr(self, "ntors", 0)]
 
     def zero_forces(self):
         self._check(self.lib.fe_zero_forces(self.h))
