@@ -288,4 +288,43 @@ __device__ __forceinline__ void record_dev(const double *__restrict__ s, double 
   *counter = c + 1;
 }
 
+// integrate_nhc.c:57-147 (Nc = Nys = 1, w[0] = 1): the chain, one thread.
+// The temperature is read from s[SC_TEMP] so that replica exchanges can
+// change it on the device between graph replays.
+__device__ __forceinline__ void nhc_chain_dev(int M, double Q, double nfree, double time_step,
+                                              double *__restrict__ zeta, double *__restrict__ s) {
+  double T = s[SC_TEMP];
+#define ZR(j) zeta[3 * (j)]
+#define ZV(j) zeta[3 * (j) + 1]
+#define ZG(j) zeta[3 * (j) + 2]
+  int M1 = M - 1, M2 = M - 2;
+  double NkT = nfree * kKB * T * 1E-4;
+  double kT = kKB * T * 1E-4;
+  double akin = 2.0 * s[FE_EN_KINET] * 1000.0 * 1E-4 / kNA;
+  double scale = 1.0;
+  double dt = time_step * 1.0 / (double)1;
+  double dt2 = dt / 2.0, dt4 = dt / 4.0, dt8 = dt / 8.0;
+  double AA;
+  ZG(0) = (akin - NkT) / Q;
+  ZV(M1) += ZG(M1) * dt4;
+  for (int j = 0; j < M1; j++) {
+    AA = exp(-dt8 * ZV(M1 - j));
+    ZV(M2 - j) = ZV(M2 - j) * AA * AA + dt4 * ZG(M2 - j) * AA;
+  }
+  AA = exp(-dt2 * ZV(0));
+  scale = scale * AA;
+  for (int j = 0; j < M; j++) ZR(j) += ZV(j) * dt2;
+  ZG(0) = (scale * scale * akin - NkT) / Q;
+  for (int j = 0; j < M - 1; j++) {
+    AA = exp(-dt8 * ZV(j + 1));
+    ZV(j) = ZV(j) * AA * AA + dt4 * ZG(j) * AA;
+    ZG(j + 1) = (Q * ZV(j) * ZV(j) - kT) / Q;
+  }
+  ZV(M - 1) += ZG(M - 1) * dt4;
+  s[SC_NHC_SCALE] = scale;
+#undef ZR
+#undef ZV
+#undef ZG
+}
+
 }  // namespace fe

@@ -255,7 +255,7 @@ int launch_b_vv1(const BIntArgs *A, const int *off, int nbox, int blocks, int nh
 int launch_b_vv2(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
                  cudaStream_t s);
 int launch_b_scale_kinet(const BIntArgs *A, const int *off, int nbox, int blocks,
-                         cudaStream_t s);
+                         int chain_next, cudaStream_t s);
 // one MD step of the box on its stream (nve_md.c:359-418 / nvt_md.c:529-531)
 int step_body(Box *b, bool with_list, bool use_nhc);
 // packed xyz (3n doubles) <-> the double4 positions, on the box's stream

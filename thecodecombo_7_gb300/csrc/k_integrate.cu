@@ -303,44 +303,6 @@ int launch_kinet(Box *b) {
   return FE_OK;
 }
 
-// integrate_nhc.c:57-147 (Nc = Nys = 1, w[0] = 1): the chain, one thread.
-// The temperature is read from s[SC_TEMP] so that replica exchanges can
-// change it on the device between graph replays.
-__device__ __forceinline__ void nhc_chain_dev(int M, double Q, double nfree, double time_step,
-                                              double *__restrict__ zeta, double *__restrict__ s) {
-  double T = s[SC_TEMP];
-#define ZR(j) zeta[3 * (j)]
-#define ZV(j) zeta[3 * (j) + 1]
-#define ZG(j) zeta[3 * (j) + 2]
-  int M1 = M - 1, M2 = M - 2;
-  double NkT = nfree * kKB * T * 1E-4;
-  double kT = kKB * T * 1E-4;
-  double akin = 2.0 * s[FE_EN_KINET] * 1000.0 * 1E-4 / kNA;
-  double scale = 1.0;
-  double dt = time_step * 1.0 / (double)1;
-  double dt2 = dt / 2.0, dt4 = dt / 4.0, dt8 = dt / 8.0;
-  double AA;
-  ZG(0) = (akin - NkT) / Q;
-  ZV(M1) += ZG(M1) * dt4;
-  for (int j = 0; j < M1; j++) {
-    AA = exp(-dt8 * ZV(M1 - j));
-    ZV(M2 - j) = ZV(M2 - j) * AA * AA + dt4 * ZG(M2 - j) * AA;
-  }
-  AA = exp(-dt2 * ZV(0));
-  scale = scale * AA;
-  for (int j = 0; j < M; j++) ZR(j) += ZV(j) * dt2;
-  ZG(0) = (scale * scale * akin - NkT) / Q;
-  for (int j = 0; j < M - 1; j++) {
-    AA = exp(-dt8 * ZV(j + 1));
-    ZV(j) = ZV(j) * AA * AA + dt4 * ZG(j) * AA;
-    ZG(j + 1) = (Q * ZV(j) * ZV(j) - kT) / Q;
-  }
-  ZV(M - 1) += ZG(M - 1) * dt4;
-  s[SC_NHC_SCALE] = scale;
-#undef ZR
-#undef ZV
-#undef ZG
-}
 
 __global__ void k_nhc_chain(int M, double Q, double nfree, double time_step,
                             double *__restrict__ zeta, double *__restrict__ s) {
@@ -418,146 +380,6 @@ int launch_xyz_gather(Box *b, double *xyz) {
   return FE_OK;
 }
 
-// ---------------------------------------------------------------------------
-// Integrator kernels of a batched step: every box of a replica batch in one
-// launch per kernel (blocks of box r: off[r] .. off[r+1]-1).  The arithmetic
-// is that of the single-box kernels above, site for site; the Nose-Hoover
-// velocity scale is applied inside the next per-site pass instead of in a
-// launch of its own, and the energy assembly rides on the second half kick.
-
-
-// kinet (fixed point, as k_kinet_fix) and the first Nose-Hoover chain update
-__global__ void k_b_kinet_nhc(const BIntArgs *__restrict__ A, const int *__restrict__ off,
-                              int nbox) {
-  const int r = vblk_box(off, nbox);
-  const BIntArgs &a = A[r];
-  const VBlk vb = vblk_of(off, r);
-  double k[6] = {0, 0, 0, 0, 0, 0};
-  for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n; i += vb.n * blockDim.x) {
-    double fac = a.mass[i];
-    double sx = a.vv[3 * i] + a.uu[3 * i];
-    double sy = a.vv[3 * i + 1] + a.uu[3 * i + 1];
-    double sz = a.vv[3 * i + 2] + a.uu[3 * i + 2];
-    k[0] += fac * sx * sx;
-    k[1] += fac * sy * sx;
-    k[2] += fac * sy * sy;
-    k[3] += fac * sz * sx;
-    k[4] += fac * sz * sy;
-    k[5] += fac * sz * sz;
-  }
-  if (block_fix_final<6>(k, 20, a.facc, a.ticket, a.scal + SC_KEN, vb) && threadIdx.x == 0) {
-    kinet_scalars(a.scal);
-    nhc_chain_dev(a.nhc_M, a.nhc_Q, a.nfree, a.dt, a.zeta, a.scal);
-  }
-}
-
-// [Nose-Hoover velocity scale, integrate_nhc.c:152-159] then the first half
-// kick, drift and pbc_all (integrate_vverlet.c:54-83, vscal = 1)
-__global__ void k_b_vv1(const BIntArgs *__restrict__ A, const int *__restrict__ off, int nbox,
-                        int nhc) {
-  const int r = vblk_box(off, nbox);
-  const BIntArgs &a = A[r];
-  const VBlk vb = vblk_of(off, r);
-  int i = vb.id * blockDim.x + threadIdx.x;
-  if (i >= a.n) return;
-  double v[3];
-  for (int c = 0; c < 3; c++) v[c] = a.vv[3 * i + c];
-  if (nhc) {
-    double scale = a.scal[SC_NHC_SCALE];
-    for (int c = 0; c < 3; c++) {
-      v[c] = v[c] * scale;
-      a.uu[3 * i + c] = a.uu[3 * i + c] * scale;
-    }
-  }
-  double imass = a.imass100[i];
-  for (int c = 0; c < 3; c++) {
-    v[c] = 1.0 * (v[c] + a.dt_h * imass * a.ff[3 * i + c]);
-    a.vv[3 * i + c] = v[c];
-  }
-  double ddx = a.dt * v[0], ddy = a.dt * v[1], ddz = a.dt * v[2];
-  a.nopbc[3 * i] += ddx;
-  a.nopbc[3 * i + 1] += ddy;
-  a.nopbc[3 * i + 2] += ddz;
-  double4 p = a.pos[i];
-  p.x += ddx;
-  p.y += ddy;
-  p.z += ddz;
-  int bad = 0;
-  p.x = pbc_wrap(p.x, a.H.x, a.L.x, &bad);
-  p.y = pbc_wrap(p.y, a.H.y, a.L.y, &bad);
-  p.z = pbc_wrap(p.z, a.H.z, a.L.z, &bad);
-  if (bad) atomicOr(a.status, ST_PBC_LOOP);
-  a.pos[i] = p;
-}
-
-// the energy assembly of forces() (block 0), the second half kick with uu =
-// vv and the kinetic tensor; then either the record (NVE) or the second
-// chain update (NHC)
-__global__ void k_b_vv2(const BIntArgs *__restrict__ A, const int *__restrict__ off, int nbox,
-                        int nhc) {
-  const int r = vblk_box(off, nbox);
-  const BIntArgs &a = A[r];
-  const VBlk vb = vblk_of(off, r);
-  if (vb.id == 0 && threadIdx.x == 0) {
-    if (a.mixed) mixed_slots_dev(a.scal, a.erfc_rc_over_rc, a.mixed_fused);
-    assemble_dev(a.scal, a.fan, a.sewald, 1);
-  }
-  double k[6] = {0, 0, 0, 0, 0, 0};
-  for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n; i += vb.n * blockDim.x) {
-    double imass = a.imass100[i];
-    double v[3];
-    for (int c = 0; c < 3; c++) {
-      v[c] = (a.vv[3 * i + c] + 1.0 * a.dt_h * imass * a.ff[3 * i + c]);
-      a.vv[3 * i + c] = v[c];
-      a.uu[3 * i + c] = v[c];
-    }
-    double fac = a.mass[i];
-    double sx = v[0] + v[0], sy = v[1] + v[1], sz = v[2] + v[2];
-    k[0] += fac * sx * sx;
-    k[1] += fac * sy * sx;
-    k[2] += fac * sy * sy;
-    k[3] += fac * sz * sx;
-    k[4] += fac * sz * sy;
-    k[5] += fac * sz * sz;
-  }
-  if (block_fix_final<6>(k, 20, a.facc, a.ticket, a.scal + SC_KEN, vb) && threadIdx.x == 0) {
-    kinet_scalars(a.scal);
-    if (nhc) nhc_chain_dev(a.nhc_M, a.nhc_Q, a.nfree, a.dt, a.zeta, a.scal);
-    else record_dev(a.scal, a.rec, a.rec_cap, a.rec_counter);
-  }
-}
-
-// NHC: the second velocity scale, kinet of the scaled velocities and the record
-__global__ void k_b_scale_kinet(const BIntArgs *__restrict__ A, const int *__restrict__ off,
-                                int nbox) {
-  const int r = vblk_box(off, nbox);
-  const BIntArgs &a = A[r];
-  const VBlk vb = vblk_of(off, r);
-  double scale = a.scal[SC_NHC_SCALE];
-  double k[6] = {0, 0, 0, 0, 0, 0};
-  for (int i = vb.id * blockDim.x + threadIdx.x; i < a.n; i += vb.n * blockDim.x) {
-    double v[3], u[3];
-    for (int c = 0; c < 3; c++) {
-      v[c] = a.vv[3 * i + c] * scale;
-      u[c] = a.uu[3 * i + c] * scale;
-      a.vv[3 * i + c] = v[c];
-      a.uu[3 * i + c] = u[c];
-    }
-    double fac = a.mass[i];
-    double sx = v[0] + u[0], sy = v[1] + u[1], sz = v[2] + u[2];
-    k[0] += fac * sx * sx;
-    k[1] += fac * sy * sx;
-    k[2] += fac * sy * sy;
-    k[3] += fac * sz * sx;
-    k[4] += fac * sz * sy;
-    k[5] += fac * sz * sz;
-  }
-  if (block_fix_final<6>(k, 20, a.facc, a.ticket, a.scal + SC_KEN, vb) && threadIdx.x == 0) {
-    kinet_scalars(a.scal);
-    record_dev(a.scal, a.rec, a.rec_cap, a.rec_counter);
-  }
-}
-
 BIntArgs make_bint_args(Box *b) {
   BIntArgs a;
   memset(&a, 0, sizeof a);
@@ -589,30 +411,6 @@ BIntArgs make_bint_args(Box *b) {
   a.mixed = b->mx != nullptr;
   mixed_bint_fields(b, &a);
   return a;
-}
-
-int launch_b_kinet_nhc(const BIntArgs *A, const int *off, int nbox, int blocks, cudaStream_t s) {
-  k_b_kinet_nhc<<<blocks, 256, 0, s>>>(A, off, nbox);
-  FE_LAUNCH_CHECK("k_b_kinet_nhc");
-  return FE_OK;
-}
-int launch_b_vv1(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
-                 cudaStream_t s) {
-  k_b_vv1<<<blocks, 256, 0, s>>>(A, off, nbox, nhc);
-  FE_LAUNCH_CHECK("k_b_vv1");
-  return FE_OK;
-}
-int launch_b_vv2(const BIntArgs *A, const int *off, int nbox, int blocks, int nhc,
-                 cudaStream_t s) {
-  k_b_vv2<<<blocks, 256, 0, s>>>(A, off, nbox, nhc);
-  FE_LAUNCH_CHECK("k_b_vv2");
-  return FE_OK;
-}
-int launch_b_scale_kinet(const BIntArgs *A, const int *off, int nbox, int blocks,
-                         cudaStream_t s) {
-  k_b_scale_kinet<<<blocks, 256, 0, s>>>(A, off, nbox);
-  FE_LAUNCH_CHECK("k_b_scale_kinet");
-  return FE_OK;
 }
 
 int launch_record(Box *b) {

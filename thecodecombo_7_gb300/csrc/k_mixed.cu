@@ -28,7 +28,8 @@
 //     semantics);
 //   * SPME spreading adds every site's spline contributions to 64-bit
 //     fixed-point grid sums with integer reductions (order independent),
-//     converted once per step to the FP32 grid for cuFFT.
+//     converted once per step to the FP32 grid for cuFFT; at order 4 the
+//     spline weights are computed where they are used (spreading, gather).
 // In the pair kernel one warp walks a row (rows handed out from a device
 // counter) with coalesced entry loads; the row's FP32 partial sums are added
 // over the warp in a fixed butterfly and converted once to the fixed-point
@@ -1144,7 +1145,7 @@ __device__ __forceinline__ void spline4_axis(unsigned u, int g, int &fl, float (
   fillspline_f(4, (float)(unsigned)(t & 0xffffffffull) * 0x1p-32f, m, dm);
 }
 
-__device__ __forceinline__ void k_mx_spread4_body(VBlk vb_, int n, int3 G,
+__device__ __forceinline__ void k_mx_spread_o4_body(VBlk vb_, int n, int3 G,
                                                   const int4 *__restrict__ posfx,
                                                   unsigned long long *__restrict__ gfix) {
   int t = vb_.id * blockDim.x + threadIdx.x;
@@ -1176,9 +1177,9 @@ __device__ __forceinline__ void k_mx_spread4_body(VBlk vb_, int n, int3 G,
   }
 }
 
-__global__ void k_mx_spread4(int n, int3 G, const int4 *__restrict__ posfx,
+__global__ void k_mx_spread_o4(int n, int3 G, const int4 *__restrict__ posfx,
                              unsigned long long *__restrict__ gfix) {
-  k_mx_spread4_body(vblk_self(), n, G, posfx, gfix);
+  k_mx_spread_o4_body(vblk_self(), n, G, posfx, gfix);
 }
 
 // FP32 grid from the fixed-point sums; the sums are cleared for the next step
@@ -1286,7 +1287,7 @@ __global__ void k_mx_gather(int n, int order, int3 G, float3 gl, float qfe,
 }
 
 // gather with the order-4 weights and derivatives computed in registers
-__device__ __forceinline__ void k_mx_gather4_body(VBlk vb_, int n, int3 G, float3 gl, float qfe,
+__device__ __forceinline__ void k_mx_gather_o4_body(VBlk vb_, int n, int3 G, float3 gl, float qfe,
                                                   const int4 *__restrict__ posfx,
                                                   const int *__restrict__ perm,
                                                   const float *__restrict__ grid,
@@ -1341,12 +1342,12 @@ __device__ __forceinline__ void k_mx_gather4_body(VBlk vb_, int n, int3 G, float
   block_fix_final<3>(v, 0, facc, ticket, out, vb_);
 }
 
-__global__ void k_mx_gather4(int n, int3 G, float3 gl, float qfe, const int4 *__restrict__ posfx,
+__global__ void k_mx_gather_o4(int n, int3 G, float3 gl, float qfe, const int4 *__restrict__ posfx,
                              const int *__restrict__ perm, const float *__restrict__ grid,
                              unsigned long long *__restrict__ fix,
                              unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                              double *__restrict__ out) {
-  k_mx_gather4_body(vblk_self(), n, G, gl, qfe, posfx, perm, grid, fix, facc, ticket, out);
+  k_mx_gather_o4_body(vblk_self(), n, G, gl, qfe, posfx, perm, grid, fix, facc, ticket, out);
 }
 
 // FP64 forces from the fixed-point sums, minus the mean reciprocal force
@@ -1952,8 +1953,8 @@ int launch_mx_spread_only(Box *b) {
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   long nt = (long)b->n * b->order;
   if (b->order == 4) {
-    k_mx_spread4<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, G, M.posfx, M.gfix);
-    FE_LAUNCH_CHECK("k_mx_spread4");
+    k_mx_spread_o4<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, G, M.posfx, M.gfix);
+    FE_LAUNCH_CHECK("k_mx_spread_o4");
   } else {
     k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(
         b->n, b->order, G, M.posfx, M.sm, M.floor3, M.gfix);
@@ -2039,9 +2040,9 @@ int forces_mixed(Box *b) {
   if (gb > 1024) gb = 1024;
   float qfe = (float)(qf / b->p.epsRF);
   if (b->order == 4) {
-    k_mx_gather4<<<gb, 128, 0, b->stream>>>(n, G, gl, qfe, M.posfx, M.perm, M.grid32, M.fix,
+    k_mx_gather_o4<<<gb, 128, 0, b->stream>>>(n, G, gl, qfe, M.posfx, M.perm, M.grid32, M.fix,
                                             b->facc, b->ticket, b->scal + SC_FMEAN);
-    FE_LAUNCH_CHECK("k_mx_gather4");
+    FE_LAUNCH_CHECK("k_mx_gather_o4");
   } else {
     k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3,
                                            M.sm, M.sd, M.grid32, M.fix, b->facc, b->ticket,
@@ -2165,18 +2166,18 @@ __global__ void k_b_mx_spread(const BMxArgs *__restrict__ A, const int *__restri
   k_mx_spread_red_body(vblk_of(off, r), a.n, a.order, a.G, a.posfx, a.sm, a.floor3, a.gfix);
 }
 
-__global__ void k_b_mx_spread4(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+__global__ void k_b_mx_spread_o4(const BMxArgs *__restrict__ A, const int *__restrict__ off,
                                int nbox) {
   const int r = vblk_box(off, nbox);
   const BMxArgs &a = A[r];
-  k_mx_spread4_body(vblk_of(off, r), a.n, a.G, a.posfx, a.gfix);
+  k_mx_spread_o4_body(vblk_of(off, r), a.n, a.G, a.posfx, a.gfix);
 }
 
-__global__ void k_b_mx_gather4(const BMxArgs *__restrict__ A, const int *__restrict__ off,
+__global__ void k_b_mx_gather_o4(const BMxArgs *__restrict__ A, const int *__restrict__ off,
                                int nbox) {
   const int r = vblk_box(off, nbox);
   const BMxArgs &a = A[r];
-  k_mx_gather4_body(vblk_of(off, r), a.n, a.G, a.gl, a.qfe, a.posfx, a.perm, a.grid32, a.fix,
+  k_mx_gather_o4_body(vblk_of(off, r), a.n, a.G, a.gl, a.qfe, a.posfx, a.perm, a.grid32, a.fix,
                     a.facc, a.ticket, a.scal + SC_FMEAN);
 }
 
@@ -2586,8 +2587,8 @@ int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
   else k_b_mx_intra<kIntraMaxSites><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_intra");
   if (P->order4) {
-    k_b_mx_spread4<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_spread4");
+    k_b_mx_spread_o4<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_spread_o4");
   } else {
     k_b_mx_splines<<<P->splines.total, 128, 0, s>>>(P->d_args, P->splines.d_off, nb);
     FE_LAUNCH_CHECK("k_b_mx_splines");
@@ -2609,8 +2610,8 @@ int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
     if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R (batch)");
   }
   if (P->order4) {
-    k_b_mx_gather4<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_gather4");
+    k_b_mx_gather_o4<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_gather_o4");
   } else {
     k_b_mx_gather<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
     FE_LAUNCH_CHECK("k_b_mx_gather");

@@ -55,8 +55,10 @@ struct Batch {
   unsigned long long *d_attempt = nullptr;  // attempts made so far
   uint64_t seed = 0;
   int max_n3 = 0;
-  cudaGraphExec_t g[4] = {nullptr, nullptr, nullptr, nullptr};  // bit 0 list, bit 1 exchange
-  int launches[4] = {0, 0, 0, 0};
+  // step graphs: bit 0 list, bit 1 exchange, bit 2 last step of a run (fused
+  // Nose-Hoover: the last step leaves the next step's first chain update out)
+  cudaGraphExec_t g[8] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  int launches[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   int g_key = -1;
   // fused step: every box in one launch per kernel (mixed-precision boxes)
   bool fused = false;
@@ -188,18 +190,23 @@ static int setup_fused(Batch *B) {
 }
 
 // One step of every box as the fused kernels, one launch per kernel for all
-// boxes: [list rebuild,] [NHC] half kick, forces, half kick [NHC], as
-// step_body.
-static int fused_step(Batch *B, bool with_list, bool use_nhc) {
+// boxes: [list rebuild,] [NHC scale,] half kick, forces, half kick [NHC],
+// as step_body.  With Nose-Hoover the first chain update of a step needs the
+// kinetic energy of the velocities the previous step ended with, which the
+// previous step's last pass has just summed: that pass applies it
+// (chain_next) unless an exchange follows (which rescales velocities and
+// swaps temperatures: capture_batch recomputes it after the exchange) or the
+// step ends a run (fe_batch_run starts every run with the update).
+static int fused_step(Batch *B, bool with_list, bool use_nhc, bool chain_next) {
   int rc = FE_OK;
   cudaStream_t s = B->main;
   if (with_list && (rc = mixed_batch_list(B->mx, s))) return rc;
   const int nb = B->R, nhc = use_nhc ? 1 : 0;
-  if (use_nhc && (rc = launch_b_kinet_nhc(B->d_bint, B->d_off_red, nb, B->tot_red, s))) return rc;
   if ((rc = launch_b_vv1(B->d_bint, B->d_off_site, nb, B->tot_site, nhc, s))) return rc;
   if ((rc = mixed_batch_forces(B->mx, s))) return rc;
   if ((rc = launch_b_vv2(B->d_bint, B->d_off_red, nb, B->tot_red, nhc, s))) return rc;
-  if (use_nhc && (rc = launch_b_scale_kinet(B->d_bint, B->d_off_red, nb, B->tot_red, s)))
+  if (use_nhc && (rc = launch_b_scale_kinet(B->d_bint, B->d_off_red, nb, B->tot_red,
+                                             chain_next ? 1 : 0, s)))
     return rc;
   return FE_OK;
 }
@@ -223,7 +230,7 @@ static void free_batch(Batch *B) {
   if (B->main) cudaStreamDestroy(B->main);
 }
 
-static int capture_batch(Batch *B, bool with_list, bool exchange, bool use_nhc,
+static int capture_batch(Batch *B, bool with_list, bool exchange, bool last, bool use_nhc,
                          cudaGraphExec_t *out, int *nlaunch) {
   cudaGraph_t g = nullptr;
   FE_CUDA(cudaStreamBeginCapture(B->main, cudaStreamCaptureModeThreadLocal));
@@ -231,7 +238,7 @@ static int capture_batch(Batch *B, bool with_list, bool exchange, bool use_nhc,
   int rc = FE_OK;
   cudaError_t e = cudaSuccess;
   if (B->fused) {
-    rc = fused_step(B, with_list, use_nhc);
+    rc = fused_step(B, with_list, use_nhc, use_nhc && !exchange && !last);
   } else {
     e = cudaEventRecord(B->fork, B->main);
     for (int r = 0; r < B->R && rc == FE_OK && e == cudaSuccess; r++) {
@@ -246,6 +253,10 @@ static int capture_batch(Batch *B, bool with_list, bool exchange, bool use_nhc,
     }
   }
   if (rc == FE_OK && e == cudaSuccess && exchange) rc = launch_exchange(B);
+  // fused Nose-Hoover: the next step's first chain update, from the
+  // velocities as the exchange left them
+  if (rc == FE_OK && e == cudaSuccess && exchange && B->fused && use_nhc && !last)
+    rc = launch_b_kinet_nhc(B->d_bint, B->d_off_red, B->R, B->tot_red, B->main);
   *nlaunch = (int)(g_launches - l0);
   cudaError_t ee = cudaStreamEndCapture(B->main, &g);
   if (rc) {
@@ -369,7 +380,7 @@ int fe_batch_set_fused(fe_batch *batch, int on) {
   if (!batch) return FE_ERR_ARG;
   Batch *B = &batch->B;
   cudaStreamSynchronize(B->main);
-  for (int k = 0; k < 4; k++)
+  for (int k = 0; k < 8; k++)
     if (B->g[k]) {
       cudaGraphExecDestroy(B->g[k]);
       B->g[k] = nullptr;
@@ -411,10 +422,18 @@ int fe_batch_run(fe_batch *batch, int nsteps, int nlist_freq, int swap_freq, lon
   }
   // work queued on the boxes' own streams comes first
   for (Box *b : B->boxes) FE_CUDA(cudaStreamSynchronize(b->stream));
-  for (long i = first_step; i < first_step + nsteps; i++) {
-    int v = (i % nlist_freq == 0 ? 1 : 0) | (swap_freq > 0 && i % swap_freq == 0 ? 2 : 0);
+  // fused Nose-Hoover: the first step's first chain update, from the current
+  // velocities (every run ends without it)
+  if (B->fused && use_nhc &&
+      (rc = launch_b_kinet_nhc(B->d_bint, B->d_off_red, B->R, B->tot_red, B->main)))
+    return rc;
+  const long end = first_step + nsteps;
+  for (long i = first_step; i < end; i++) {
+    int v = (i % nlist_freq == 0 ? 1 : 0) | (swap_freq > 0 && i % swap_freq == 0 ? 2 : 0) |
+            (B->fused && use_nhc && i == end - 1 ? 4 : 0);
     if (!B->g[v]) {
-      if ((rc = capture_batch(B, v & 1, v & 2, use_nhc != 0, &B->g[v], &B->launches[v]))) return rc;
+      if ((rc = capture_batch(B, v & 1, v & 2, v & 4, use_nhc != 0, &B->g[v], &B->launches[v])))
+        return rc;
       B->g_key = key;
     }
     FE_CUDA(cudaGraphLaunch(B->g[v], B->main));
