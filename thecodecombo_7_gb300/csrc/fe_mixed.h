@@ -23,7 +23,24 @@ struct MxPruneState {
   int pad;
 };
 
+// The topology of a box whose molecules are all alike (same size, terms and
+// site types at the same positions, consecutive from site 0): the fused
+// intramolecular kernel then reads it from the launch parameters instead of
+// following per-molecule index lists.
+constexpr int kTplTerms = 16;
+struct IntraTpl {
+  int ns, nx, nb, na;
+  int xa[kTplTerms], xb[kTplTerms], xf[kTplTerms];
+  int ba[kTplTerms], bb[kTplTerms];
+  float breq[kTplTerms], bk[kTplTerms];
+  int aa[kTplTerms], ab[kTplTerms], ac[kTplTerms];
+  float at0[kTplTerms], ak[kTplTerms];
+  int type[kIntraMaxSites];
+};
+
 struct Mixed {
+  bool uniform = false;  // all molecules alike: tpl holds their topology
+  IntraTpl tpl;
   // cell grid (edge >= rlist / 3) used to sort sites and enumerate candidates
   int nc[3] = {1, 1, 1};
   double h[3] = {0, 0, 0};

@@ -1391,9 +1391,20 @@ __device__ __forceinline__ void intra_add(float (&F)[NS][3], int a, float x, flo
     }
 }
 
+template <int NS>
+__device__ __forceinline__ int intra_pick_i(const int (&v)[kIntraMaxSites], int a) {
+  int r = v[0];
+#pragma unroll
+  for (int i = 1; i < NS; i++)
+    if (a == i) r = v[i];
+  return r;
+}
+
 // NS: the largest molecule (sites) of the box, so that the molecule's
 // positions and forces stay in registers
-template <int NS>
+// UNI: every molecule is T (its terms read from T, unrolled), else the
+// per-molecule index lists
+template <int NS, bool UNI = false>
 __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *__restrict__ mol_first,
                            const int *__restrict__ mol_x, const int *__restrict__ mol_xi,
                            const int *__restrict__ mol_b, const int *__restrict__ mol_bi,
@@ -1409,11 +1420,12 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
                            const float2 *__restrict__ exptab, DfIntra D,
                            unsigned long long *__restrict__ fix,
                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
-                           double *__restrict__ out) {
+                           double *__restrict__ out, const IntraTpl &T = IntraTpl()) {
   float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, eb = 0.f, ea = 0.f;
   long long q_intra = 0;
   for (int m = vb_.id * blockDim.x + threadIdx.x; m < nmol; m += vb_.n * blockDim.x) {
-    const int lb = mol_first[m], ns = mol_first[m + 1] - lb;
+    const int lb = UNI ? m * T.ns : mol_first[m];
+    const int ns = UNI ? T.ns : mol_first[m + 1] - lb;
     int4 P[NS];
     float F[NS][3];
 #pragma unroll
@@ -1421,9 +1433,21 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
       P[i] = i < ns ? posfx[iperm[lb + i]] : make_int4(0, 0, 0, 0);
       F[i][0] = F[i][1] = F[i][2] = 0.f;
     }
-    for (int t = mol_x[m]; t < mol_x[m + 1]; t++) {
-      int x = mol_xi[t];
-      int a = ab[2 * x] - lb, bq = ab[2 * x + 1] - lb, xf = flag[x];
+    const int tx0 = UNI ? 0 : mol_x[m], tx1 = UNI ? kTplTerms : mol_x[m + 1];
+#pragma unroll
+    for (int t = tx0; t < tx1; t++) {
+      int a, bq, xf;
+      if (UNI) {
+        if (t >= T.nx) break;
+        a = T.xa[t];
+        bq = T.xb[t];
+        xf = T.xf[t];
+      } else {
+        int x = mol_xi[t];
+        a = ab[2 * x] - lb;
+        bq = ab[2 * x + 1] - lb;
+        xf = flag[x];
+      }
       if (xf == 0) continue;
       const int4 Pa = intra_pick(P, a), Pb = intra_pick(P, bq);
       float dx = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
@@ -1443,7 +1467,9 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
         Fs += qq * rinv * rinv2 * (erfckr + c2k * r * ex);
         e_real += qq * erfckr * rinv;
         qsum += qq;
-        const float *lj = lj_tab + (type[lb + a] * nt + type[lb + bq]) * 3;
+        const int ta = UNI ? intra_pick_i<NS>(T.type, a) : type[lb + a];
+        const int tb = UNI ? intra_pick_i<NS>(T.type, bq) : type[lb + bq];
+        const float *lj = lj_tab + (ta * nt + tb) * 3;
         if (lj[0] != 0.f) {
           float sr2 = lj[1] * rinv2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
           Fs += 12.f * lj[0] * rinv2 * (sr12 - sr6);
@@ -1460,24 +1486,56 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
       intra_add(F, a, Fs * dx, Fs * dy, Fs * dz);
       intra_add(F, bq, -Fs * dx, -Fs * dy, -Fs * dz);
     }
-    for (int t = mol_b[m]; t < mol_b[m + 1]; t++) {
-      int u = mol_bi[t];
-      int ia = bond_ab[2 * u] - lb, ib = bond_ab[2 * u + 1] - lb;
+    const int tb0 = UNI ? 0 : mol_b[m], tb1 = UNI ? kTplTerms : mol_b[m + 1];
+#pragma unroll
+    for (int t = tb0; t < tb1; t++) {
+      int ia, ib;
+      float req, kb;
+      if (UNI) {
+        if (t >= T.nb) break;
+        ia = T.ba[t];
+        ib = T.bb[t];
+        req = T.breq[t];
+        kb = T.bk[t];
+      } else {
+        int u = mol_bi[t];
+        ia = bond_ab[2 * u] - lb;
+        ib = bond_ab[2 * u + 1] - lb;
+        req = (float)bond_req[u];
+        kb = (float)bond_k[u];
+      }
       const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib);
       float dx = fx_delta((unsigned)Pb.x, (unsigned)Pa.x, sL.x);
       float dy = fx_delta((unsigned)Pb.y, (unsigned)Pa.y, sL.y);
       float dz = fx_delta((unsigned)Pb.z, (unsigned)Pa.z, sL.z);
       float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-      float rr = dr - (float)bond_req[u];
-      float fr = -(float)bond_k[u] * rr * 2.f;
+      float rr = dr - req;
+      float fr = -kb * rr * 2.f;
       eb += -(fr * rr * 0.5f);
       float sc = fr / dr;
       intra_add(F, ia, -sc * dx, -sc * dy, -sc * dz);
       intra_add(F, ib, sc * dx, sc * dy, sc * dz);
     }
-    for (int t = mol_a[m]; t < mol_a[m + 1]; t++) {
-      int u = mol_ai[t];
-      int ia = bend_abc[3 * u] - lb, ib = bend_abc[3 * u + 1] - lb, ic = bend_abc[3 * u + 2] - lb;
+    const int ta0 = UNI ? 0 : mol_a[m], ta1 = UNI ? kTplTerms : mol_a[m + 1];
+#pragma unroll
+    for (int t = ta0; t < ta1; t++) {
+      int ia, ib, ic;
+      float t0, ka;
+      if (UNI) {
+        if (t >= T.na) break;
+        ia = T.aa[t];
+        ib = T.ab[t];
+        ic = T.ac[t];
+        t0 = T.at0[t];
+        ka = T.ak[t];
+      } else {
+        int u = mol_ai[t];
+        ia = bend_abc[3 * u] - lb;
+        ib = bend_abc[3 * u + 1] - lb;
+        ic = bend_abc[3 * u + 2] - lb;
+        t0 = (float)bend_t0[u];
+        ka = (float)bend_k[u];
+      }
       const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib), Pc = intra_pick(P, ic);
       float dax = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
       float day = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
@@ -1493,8 +1551,8 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
       cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
       float phi = acosf(cosphi);
       float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
-      float rr = phi - (float)bend_t0[u];
-      float fr = -(float)bend_k[u] * rr * 2.f;
+      float rr = phi - t0;
+      float fr = -ka * rr * 2.f;
       ea += -fr * rr * 0.5f;
       float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
       float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
@@ -1537,6 +1595,24 @@ __global__ void k_mx_intra(int nmol, const int *__restrict__ mol_first,
                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                            double *__restrict__ out) {
   k_mx_intra_body<NS>(vblk_self(), nmol, mol_first, mol_x, mol_xi, mol_b, mol_bi, mol_a, mol_ai, ab, flag, bond_ab, bond_req, bond_k, bend_abc, bend_t0, bend_k, posfx, iperm, type, sL, nt, lj_tab, rc2, kappa, c2k, qf, epsRF, pos_q, exptab, D, fix, facc, ticket, out);
+}
+
+// the same for a box of identical molecules (their topology in T)
+template <int NS>
+__global__ void k_mx_intra_uni(int nmol, IntraTpl T, const int4 *__restrict__ posfx,
+                               const int *__restrict__ iperm, float3 sL, int nt,
+                               const float *__restrict__ lj_tab, float rc2, float kappa,
+                               float c2k, float qf, float epsRF,
+                               const double4 *__restrict__ pos_q,
+                               const float2 *__restrict__ exptab, DfIntra D,
+                               unsigned long long *__restrict__ fix,
+                               unsigned long long *__restrict__ facc,
+                               unsigned *__restrict__ ticket, double *__restrict__ out) {
+  k_mx_intra_body<NS, true>(vblk_self(), nmol, nullptr, nullptr, nullptr, nullptr, nullptr,
+                            nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+                            nullptr, nullptr, nullptr, posfx, iperm, nullptr, sL, nt, lj_tab,
+                            rc2, kappa, c2k, qf, epsRF, pos_q, exptab, D, fix, facc, ticket, out,
+                            T);
 }
 
 // combine the mixed kernels' sums into the reference's slots
@@ -1700,6 +1776,70 @@ int mixed_setup(Box *b) {
       M.intra_maxs = 1;
       for (int m = 0; m < nm; m++)
         if (first[m + 1] - first[m] > M.intra_maxs) M.intra_maxs = first[m + 1] - first[m];
+      // all molecules alike?  (same size and, at the same relative sites,
+      // the same exclusions, bonds, bends and site types)
+      IntraTpl &T = M.tpl;
+      memset(&T, 0, sizeof T);
+      const int ns0 = first[1] - first[0];
+      bool uni = xo[1] - xo[0] <= kTplTerms && bo[1] - bo[0] <= kTplTerms &&
+                 ao[1] - ao[0] <= kTplTerms;
+      T.ns = ns0;
+      T.nx = xo[1] - xo[0];
+      T.nb = bo[1] - bo[0];
+      T.na = ao[1] - ao[0];
+      for (int m = 0; m < nm && uni; m++) {
+        const int lb = first[m];
+        if (first[m + 1] - lb != ns0 || lb != m * ns0 || xo[m + 1] - xo[m] != T.nx ||
+            bo[m + 1] - bo[m] != T.nb || ao[m + 1] - ao[m] != T.na) {
+          uni = false;
+          break;
+        }
+        for (int i = 0; i < ns0 && uni; i++) {
+          if (m == 0) T.type[i] = pp.type[lb + i];
+          else if (pp.type[lb + i] != T.type[i]) uni = false;
+        }
+        for (int k = 0; k < T.nx && uni; k++) {
+          int x = xi[xo[m] + k];
+          int a = pp.excl_ab[2 * x] - lb, c = pp.excl_ab[2 * x + 1] - lb, f = pp.excl_flag[x];
+          if (m == 0) {
+            T.xa[k] = a;
+            T.xb[k] = c;
+            T.xf[k] = f;
+          } else if (a != T.xa[k] || c != T.xb[k] || f != T.xf[k]) {
+            uni = false;
+          }
+        }
+        for (int k = 0; k < T.nb && uni; k++) {
+          int u = bi[bo[m] + k];
+          int a = pp.bond_ab[2 * u] - lb, c = pp.bond_ab[2 * u + 1] - lb;
+          float req = (float)pp.bond_req[u], kk = (float)pp.bond_k[u];
+          if (m == 0) {
+            T.ba[k] = a;
+            T.bb[k] = c;
+            T.breq[k] = req;
+            T.bk[k] = kk;
+          } else if (a != T.ba[k] || c != T.bb[k] || req != T.breq[k] || kk != T.bk[k]) {
+            uni = false;
+          }
+        }
+        for (int k = 0; k < T.na && uni; k++) {
+          int u = ai[ao[m] + k];
+          int a = pp.bend_abc[3 * u] - lb, c = pp.bend_abc[3 * u + 1] - lb,
+              d = pp.bend_abc[3 * u + 2] - lb;
+          float t0 = (float)pp.bend_theta0[u], kk = (float)pp.bend_k[u];
+          if (m == 0) {
+            T.aa[k] = a;
+            T.ab[k] = c;
+            T.ac[k] = d;
+            T.at0[k] = t0;
+            T.ak[k] = kk;
+          } else if (a != T.aa[k] || c != T.ab[k] || d != T.ac[k] || t0 != T.at0[k] ||
+                     kk != T.ak[k]) {
+            uni = false;
+          }
+        }
+      }
+      M.uniform = uni;
     }
   }
 
@@ -1985,7 +2125,13 @@ int forces_mixed(Box *b) {
       M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),                 \
       (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,     \
       b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA
-    if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
+    if (M.uniform && M.tpl.ns == 3)
+      k_mx_intra_uni<3><<<mb, 128, 0, b->stream>>>(
+          M.nmol, M.tpl, M.posfx, M.iperm, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),
+          (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
+          (float)b->p.epsRF, b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket,
+          b->scal + SC_MX_INTRA);
+    else if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
     else if (M.intra_maxs <= 4) k_mx_intra<4><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
     else k_mx_intra<kIntraMaxSites><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
 #undef FE_INTRA_ARGS
