@@ -1101,7 +1101,6 @@ __global__ void k_mx_splines(int n, int order, int3 G, const int4 *__restrict__ 
 // additions, so the grid is bitwise reproducible; sites in sorted (spatial)
 // order keep neighbouring threads on neighbouring grid lines.
 constexpr float kSpRedFix = 1099511627776.0f;  // 2^40
-constexpr double kSpRedUnfix = 1.0 / 1099511627776.0;
 
 __device__ __forceinline__ void k_mx_spread_red_body(VBlk vb_, int n, int order, int3 G, const int4 *__restrict__ posfx,
                                 const float *__restrict__ sm, const int *__restrict__ floor3,
@@ -1182,6 +1181,16 @@ __global__ void k_mx_spread_o4(int n, int3 G, const int4 *__restrict__ posfx,
   k_mx_spread_o4_body(vblk_self(), n, G, posfx, gfix);
 }
 
+// A grid sum (2^40 per unit) as FP32 without the FP64 pipe: the upper 32
+// bits hold value x 2^8 and convert exactly while |value| < 2^16 (a grid
+// point's charge sum is a few e), the lower 32 bits with one rounding, and
+// one fused multiply-add joins them.
+__device__ __forceinline__ float grid_fix_to_f32(long long v) {
+  int hi = (int)(v >> 32);
+  unsigned lo = (unsigned)(v & 0xffffffffll);
+  return fmaf((float)hi, 0x1p-8f, __uint2float_rn(lo) * 0x1p-40f);
+}
+
 // FP32 grid from the fixed-point sums; the sums are cleared for the next step
 // (two points per thread and iteration: 16-byte loads and stores)
 __device__ __forceinline__ void k_mx_fix2grid_body(VBlk vb_, long K, unsigned long long *__restrict__ gfix,
@@ -1192,11 +1201,11 @@ __device__ __forceinline__ void k_mx_fix2grid_body(VBlk vb_, long K, unsigned lo
   for (long i = (long)vb_.id * blockDim.x + threadIdx.x; i < K2;
        i += (long)vb_.n * blockDim.x) {
     longlong2 v = g2[i];
-    o2[i] = make_float2((float)((double)v.x * kSpRedUnfix), (float)((double)v.y * kSpRedUnfix));
+    o2[i] = make_float2(grid_fix_to_f32(v.x), grid_fix_to_f32(v.y));
     g2[i] = make_longlong2(0, 0);
   }
   if ((K & 1) && vb_.id == 0 && threadIdx.x == 0) {
-    grid[K - 1] = (float)((double)(long long)gfix[K - 1] * kSpRedUnfix);
+    grid[K - 1] = grid_fix_to_f32((long long)gfix[K - 1]);
     gfix[K - 1] = 0ull;
   }
 }
@@ -1404,6 +1413,105 @@ __device__ __forceinline__ int intra_pick_i(const int (&v)[kIntraMaxSites], int 
 // positions and forces stay in registers
 // UNI: every molecule is T (its terms read from T, unrolled), else the
 // per-molecule index lists
+// The three kinds of intramolecular term, each adding to the molecule's
+// force registers F and the thread's energy sums A.
+struct IntraAcc {
+  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, eb = 0.f, ea = 0.f;
+  long long q_intra = 0;
+};
+
+// excluded (xf 1-3) or 1-4 (xf 4) pair a-bq: the intra correction, and for
+// 1-4 pairs the scaled real-space term and LJ (cnonbond_nblist.c:245-263,
+// 416-437); qa, qb the FP64 charges, type_a / type_b the site types
+template <int NS>
+__device__ __forceinline__ void intra_excl(const int4 (&P)[NS], float (&F)[NS][3], int a, int bq,
+                                           int xf, double qa, double qb, int type_a, int type_b,
+                                           float3 sL, int nt, const float *__restrict__ lj_tab,
+                                           float rc2, float kappa, float c2k, float qf,
+                                           float epsRF, const float2 *__restrict__ exptab,
+                                           const DfIntra &D, IntraAcc &A) {
+  const int4 Pa = intra_pick(P, a), Pb = intra_pick(P, bq);
+  float dx = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
+  float dy = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
+  float dz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
+  float r2 = dx * dx + dy * dy + dz * dz;
+  if (r2 > rc2) return;
+  float rinv = rsqrtf(r2), r = r2 * rinv, rinv2 = rinv * rinv;
+  float kr = kappa * r;
+  float ex = __expf(-kr * kr);
+  float erfckr = erfc_nr_f(kr, ex);
+  float qqab = __int_as_float(Pa.w) * __int_as_float(Pb.w) * qf;
+  float Fs = 0.f;
+  float qcorr = qqab;
+  if (xf == 4) {
+    float qq = qqab * (float)kE14FAC / epsRF;
+    Fs += qq * rinv * rinv2 * (erfckr + c2k * r * ex);
+    A.e_real += qq * erfckr * rinv;
+    A.qsum += qq;
+    const float *lj = lj_tab + (type_a * nt + type_b) * 3;
+    if (lj[0] != 0.f) {
+      float sr2 = lj[1] * rinv2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+      Fs += 12.f * lj[0] * rinv2 * (sr12 - sr6);
+      A.e_lj += lj[0] * (sr12 - 2.f * sr6);
+      A.e_ljs += lj[0] * lj[2];
+    }
+    qcorr *= (1.f - (float)kE14FAC);
+  }
+  float erfkr = 1.f - erfckr;
+  A.q_intra += df_to_fixed(
+      intra_energy_df(D, Pa, Pb, qa, qb, xf == 4 ? (float)(1.0 - kE14FAC) : 1.f, exptab), 32);
+  Fs -= qcorr * rinv * rinv2 * (erfkr - c2k * r * ex);
+  intra_add(F, a, Fs * dx, Fs * dy, Fs * dz);
+  intra_add(F, bq, -Fs * dx, -Fs * dy, -Fs * dz);
+}
+
+template <int NS>
+__device__ __forceinline__ void intra_bond(const int4 (&P)[NS], float (&F)[NS][3], int ia, int ib,
+                                           float req, float kb, float3 sL, IntraAcc &A) {
+  const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib);
+  float dx = fx_delta((unsigned)Pb.x, (unsigned)Pa.x, sL.x);
+  float dy = fx_delta((unsigned)Pb.y, (unsigned)Pa.y, sL.y);
+  float dz = fx_delta((unsigned)Pb.z, (unsigned)Pa.z, sL.z);
+  float dr = sqrtf(dx * dx + dy * dy + dz * dz);
+  float rr = dr - req;
+  float fr = -kb * rr * 2.f;
+  A.eb += -(fr * rr * 0.5f);
+  float sc = fr / dr;
+  intra_add(F, ia, -sc * dx, -sc * dy, -sc * dz);
+  intra_add(F, ib, sc * dx, sc * dy, sc * dz);
+}
+
+template <int NS>
+__device__ __forceinline__ void intra_bend(const int4 (&P)[NS], float (&F)[NS][3], int ia, int ib,
+                                           int ic, float t0, float ka, float3 sL, IntraAcc &A) {
+  const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib), Pc = intra_pick(P, ic);
+  float dax = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
+  float day = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
+  float daz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
+  float dcx = fx_delta((unsigned)Pc.x, (unsigned)Pb.x, sL.x);
+  float dcy = fx_delta((unsigned)Pc.y, (unsigned)Pb.y, sL.y);
+  float dcz = fx_delta((unsigned)Pc.z, (unsigned)Pb.z, sL.z);
+  float drai = rsqrtf(dax * dax + day * day + daz * daz);
+  float erax = dax * drai, eray = day * drai, eraz = daz * drai;
+  float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+  float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
+  float cosphi = erax * ercx + eray * ercy + eraz * ercz;
+  cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
+  float phi = acosf(cosphi);
+  float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
+  float rr = phi - t0;
+  float fr = -ka * rr * 2.f;
+  A.ea += -fr * rr * 0.5f;
+  float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
+  float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
+        fza = (eraz * cosphi - ercz) * irasin;
+  float fxc = (ercx * cosphi - erax) * ircsin, fyc = (ercy * cosphi - eray) * ircsin,
+        fzc = (ercz * cosphi - eraz) * ircsin;
+  intra_add(F, ia, fxa, fya, fza);
+  intra_add(F, ic, fxc, fyc, fzc);
+  intra_add(F, ib, -(fxa + fxc), -(fya + fyc), -(fza + fzc));
+}
+
 template <int NS, bool UNI = false>
 __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *__restrict__ mol_first,
                            const int *__restrict__ mol_x, const int *__restrict__ mol_xi,
@@ -1421,8 +1529,7 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
                            unsigned long long *__restrict__ fix,
                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                            double *__restrict__ out, const IntraTpl &T = IntraTpl()) {
-  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, eb = 0.f, ea = 0.f;
-  long long q_intra = 0;
+  IntraAcc A;
   for (int m = vb_.id * blockDim.x + threadIdx.x; m < nmol; m += vb_.n * blockDim.x) {
     const int lb = UNI ? m * T.ns : mol_first[m];
     const int ns = UNI ? T.ns : mol_first[m + 1] - lb;
@@ -1449,42 +1556,10 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
         xf = flag[x];
       }
       if (xf == 0) continue;
-      const int4 Pa = intra_pick(P, a), Pb = intra_pick(P, bq);
-      float dx = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
-      float dy = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
-      float dz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
-      float r2 = dx * dx + dy * dy + dz * dz;
-      if (r2 > rc2) continue;
-      float rinv = rsqrtf(r2), r = r2 * rinv, rinv2 = rinv * rinv;
-      float kr = kappa * r;
-      float ex = __expf(-kr * kr);
-      float erfckr = erfc_nr_f(kr, ex);
-      float qqab = __int_as_float(Pa.w) * __int_as_float(Pb.w) * qf;
-      float Fs = 0.f;
-      float qcorr = qqab;
-      if (xf == 4) {
-        float qq = qqab * (float)kE14FAC / epsRF;
-        Fs += qq * rinv * rinv2 * (erfckr + c2k * r * ex);
-        e_real += qq * erfckr * rinv;
-        qsum += qq;
-        const int ta = UNI ? intra_pick_i<NS>(T.type, a) : type[lb + a];
-        const int tb = UNI ? intra_pick_i<NS>(T.type, bq) : type[lb + bq];
-        const float *lj = lj_tab + (ta * nt + tb) * 3;
-        if (lj[0] != 0.f) {
-          float sr2 = lj[1] * rinv2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
-          Fs += 12.f * lj[0] * rinv2 * (sr12 - sr6);
-          e_lj += lj[0] * (sr12 - 2.f * sr6);
-          e_ljs += lj[0] * lj[2];
-        }
-        qcorr *= (1.f - (float)kE14FAC);
-      }
-      float erfkr = 1.f - erfckr;
-      q_intra += df_to_fixed(intra_energy_df(D, Pa, Pb, pos_q[lb + a].w, pos_q[lb + bq].w,
-                                             xf == 4 ? (float)(1.0 - kE14FAC) : 1.f, exptab),
-                             32);
-      Fs -= qcorr * rinv * rinv2 * (erfkr - c2k * r * ex);
-      intra_add(F, a, Fs * dx, Fs * dy, Fs * dz);
-      intra_add(F, bq, -Fs * dx, -Fs * dy, -Fs * dz);
+      intra_excl<NS>(P, F, a, bq, xf, pos_q[lb + a].w, pos_q[lb + bq].w,
+                     UNI ? intra_pick_i<NS>(T.type, a) : type[lb + a],
+                     UNI ? intra_pick_i<NS>(T.type, bq) : type[lb + bq], sL, nt, lj_tab, rc2,
+                     kappa, c2k, qf, epsRF, exptab, D, A);
     }
     const int tb0 = UNI ? 0 : mol_b[m], tb1 = UNI ? kTplTerms : mol_b[m + 1];
 #pragma unroll
@@ -1504,17 +1579,7 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
         req = (float)bond_req[u];
         kb = (float)bond_k[u];
       }
-      const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib);
-      float dx = fx_delta((unsigned)Pb.x, (unsigned)Pa.x, sL.x);
-      float dy = fx_delta((unsigned)Pb.y, (unsigned)Pa.y, sL.y);
-      float dz = fx_delta((unsigned)Pb.z, (unsigned)Pa.z, sL.z);
-      float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-      float rr = dr - req;
-      float fr = -kb * rr * 2.f;
-      eb += -(fr * rr * 0.5f);
-      float sc = fr / dr;
-      intra_add(F, ia, -sc * dx, -sc * dy, -sc * dz);
-      intra_add(F, ib, sc * dx, sc * dy, sc * dz);
+      intra_bond<NS>(P, F, ia, ib, req, kb, sL, A);
     }
     const int ta0 = UNI ? 0 : mol_a[m], ta1 = UNI ? kTplTerms : mol_a[m + 1];
 #pragma unroll
@@ -1536,32 +1601,7 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
         t0 = (float)bend_t0[u];
         ka = (float)bend_k[u];
       }
-      const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib), Pc = intra_pick(P, ic);
-      float dax = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
-      float day = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
-      float daz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
-      float dcx = fx_delta((unsigned)Pc.x, (unsigned)Pb.x, sL.x);
-      float dcy = fx_delta((unsigned)Pc.y, (unsigned)Pb.y, sL.y);
-      float dcz = fx_delta((unsigned)Pc.z, (unsigned)Pb.z, sL.z);
-      float drai = rsqrtf(dax * dax + day * day + daz * daz);
-      float erax = dax * drai, eray = day * drai, eraz = daz * drai;
-      float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
-      float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
-      float cosphi = erax * ercx + eray * ercy + eraz * ercz;
-      cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
-      float phi = acosf(cosphi);
-      float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
-      float rr = phi - t0;
-      float fr = -ka * rr * 2.f;
-      ea += -fr * rr * 0.5f;
-      float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
-      float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
-            fza = (eraz * cosphi - ercz) * irasin;
-      float fxc = (ercx * cosphi - erax) * ircsin, fyc = (ercy * cosphi - eray) * ircsin,
-            fzc = (ercz * cosphi - eraz) * ircsin;
-      intra_add(F, ia, fxa, fya, fza);
-      intra_add(F, ic, fxc, fyc, fzc);
-      intra_add(F, ib, -(fxa + fxc), -(fya + fyc), -(fza + fzc));
+      intra_bend<NS>(P, F, ia, ib, ic, t0, ka, sL, A);
     }
 #pragma unroll
     for (int i = 0; i < NS; i++)
@@ -1572,8 +1612,8 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
           *q = *q + (unsigned long long)to_fix(F[i][c]);
         }
   }
-  long long v[7] = {to_fixed(e_lj, 32), to_fixed(e_ljs, 32), to_fixed(e_real, 32),
-                    to_fixed(qsum, 32), q_intra, to_fixed(eb, 32), to_fixed(ea, 32)};
+  long long v[7] = {to_fixed(A.e_lj, 32), to_fixed(A.e_ljs, 32), to_fixed(A.e_real, 32),
+                    to_fixed(A.qsum, 32), A.q_intra, to_fixed(A.eb, 32), to_fixed(A.ea, 32)};
   block_fix_final<7>(v, 32, facc, ticket, out, vb_);
 }
 
@@ -2125,12 +2165,13 @@ int forces_mixed(Box *b) {
       M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),                 \
       (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,     \
       b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA
-    if (M.uniform && M.tpl.ns == 3)
+    if (M.uniform && M.tpl.ns == 3) {
       k_mx_intra_uni<3><<<mb, 128, 0, b->stream>>>(
           M.nmol, M.tpl, M.posfx, M.iperm, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),
           (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
           (float)b->p.epsRF, b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket,
           b->scal + SC_MX_INTRA);
+    }
     else if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
     else if (M.intra_maxs <= 4) k_mx_intra<4><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
     else k_mx_intra<kIntraMaxSites><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
