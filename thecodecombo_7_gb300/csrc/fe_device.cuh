@@ -327,4 +327,35 @@ __device__ __forceinline__ void nhc_chain_dev(int M, double Q, double nfree, dou
 #undef ZG
 }
 
+// Exclusive prefix sum of one int per thread over a block of up to 1024
+// threads (warp shuffles, then the warp totals); *total gets the block's sum.
+__device__ __forceinline__ int block_exclusive_scan(int v, int *total) {
+  __shared__ int wsum[32];
+  __shared__ int wtot;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[w] = x;
+  __syncthreads();
+  if (w == 0) {
+    int y = lane < nw ? wsum[lane] : 0, z = y;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int q = __shfl_up_sync(0xffffffffu, z, o);
+      if (lane >= o) z += q;
+    }
+    wsum[lane] = z - y;
+    if (lane == 31) wtot = z;  // the block total (nw <= 32)
+  }
+  __syncthreads();
+  int base = wsum[w];
+  *total = wtot;
+  __syncthreads();
+  return base + x - v;
+}
+
 }  // namespace fe

@@ -103,7 +103,8 @@ __global__ void k_mx_fill(int n, const int *__restrict__ cell_of, const int *__r
   k_mx_fill_body(vblk_self(), n, cell_of, start, fill, perm);
 }
 
-// order each cell's sites by original index (deterministic layout)
+// order each cell's sites by original index (deterministic layout): cells of up
+// to 32 sites by rank within one warp, larger ones by a bitonic sort
 __device__ __forceinline__ void k_mx_cellsort_body(VBlk vb_, const int *__restrict__ start, int *__restrict__ perm,
                               int *__restrict__ iperm, int *__restrict__ cell_s,
                               const int *__restrict__ type, int *__restrict__ type_s,
@@ -115,6 +116,21 @@ __device__ __forceinline__ void k_mx_cellsort_body(VBlk vb_, const int *__restri
   if (m > kMxMaxCellAtoms) {
     if (threadIdx.x == 0) atomicOr(status, ST_CELL_OVERFLOW);
     m = kMxMaxCellAtoms;
+  }
+  if (m <= 32 && blockDim.x == 32) {
+    // one site per lane: its rank among the cell's original indices
+    const int lane = threadIdx.x;
+    int v = lane < m ? perm[s0 + lane] : INT_MAX;
+    int rank = 0;
+#pragma unroll
+    for (int src = 0; src < 32; src++) rank += __shfl_sync(0xffffffffu, v, src) < v ? 1 : 0;
+    if (lane < m) {
+      perm[s0 + rank] = v;
+      iperm[v] = s0 + rank;
+      cell_s[s0 + rank] = c;
+      type_s[s0 + rank] = type[v];
+    }
+    return;
   }
   int P = 1;
   while (P < m) P <<= 1;
@@ -251,7 +267,7 @@ constexpr int kListUnit = 8;  // consecutive sorted sites one warp lists togethe
 // make fewer, longer contiguous ranges; 3 measured fastest of 2, 3, 4
 constexpr double kListCellsPerReach = 3.0;
 constexpr int kListExcl = 4;  // excluded partners per site handled by lane masks
-constexpr int kListBlocksPerSM = 2;  // register budget of the list build (no spills)
+constexpr int kListBlocksPerSM = 3;  // register budget of the list build (no spills at 74)
 static_assert(kListUnit * kListExcl == 32, "one lane per (site, excluded partner)");
 
 __device__ __forceinline__ float warp_fmin(float v) {
@@ -1992,7 +2008,7 @@ int launch_mixed_list(Box *b) {
   FE_CUDA(cudaMemsetAsync(M.cell_count, 0, sizeof(int) * M.ncells, b->stream));
   k_mx_fill<<<(n + 255) / 256, 256, 0, b->stream>>>(n, M.cell_of, M.cell_start, M.cell_fill, M.perm);
   FE_LAUNCH_CHECK("k_mx_fill");
-  k_mx_cellsort<<<M.ncells, 256, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s,
+  k_mx_cellsort<<<M.ncells, 32, 0, b->stream>>>(M.cell_start, M.perm, M.iperm, M.cell_s,
                                                  b->type, M.type_s, b->status);
   FE_LAUNCH_CHECK("k_mx_cellsort");
   int rc = launch_convert(b);
@@ -2410,25 +2426,14 @@ __global__ void k_b_mx_cell(const BMxArgs *__restrict__ A, const int *__restrict
 // as k_cell_scan); fill counters cleared, counts cleared for the next build
 __global__ void __launch_bounds__(1024) k_b_mx_scan(const BMxArgs *__restrict__ A) {
   const BMxArgs &a = A[blockIdx.x];
-  __shared__ int part[1024];
   int t = threadIdx.x, T = blockDim.x;
   int chunk = (a.ncells + T - 1) / T;
   int lo = min(t * chunk, a.ncells), hi = min(lo + chunk, a.ncells);
   int sum = 0;
   for (int c = lo; c < hi; c++) sum += a.cell_count[c];
-  part[t] = sum;
-  __syncthreads();
-  if (t == 0) {
-    int acc = 0;
-    for (int k = 0; k < T; k++) {
-      int v = part[k];
-      part[k] = acc;
-      acc += v;
-    }
-    a.cell_start[a.ncells] = acc;
-  }
-  __syncthreads();
-  int acc = part[t];
+  int total;
+  int acc = block_exclusive_scan(sum, &total);
+  if (t == 0) a.cell_start[a.ncells] = total;
   for (int c = lo; c < hi; c++) {
     a.cell_start[c] = acc;
     a.cell_fill[c] = 0;
@@ -2750,7 +2755,7 @@ int mixed_batch_list(BMxPlan *P, cudaStream_t s) {
   FE_LAUNCH_CHECK("k_b_mx_scan");
   k_b_mx_fill<<<P->fill.total, 256, 0, s>>>(P->d_args, P->fill.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_fill");
-  k_b_mx_cellsort<<<P->cellsort.total, 256, 0, s>>>(P->d_args, P->cellsort.d_off, nb);
+  k_b_mx_cellsort<<<P->cellsort.total, 32, 0, s>>>(P->d_args, P->cellsort.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_cellsort");
   k_b_mx_convert_only<<<P->convert.total, 256, 0, s>>>(P->d_args, P->convert.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_convert_only");

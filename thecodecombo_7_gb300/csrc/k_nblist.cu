@@ -38,25 +38,14 @@ __global__ void k_cell_count(const double4 *__restrict__ pos, int n, double3 L, 
 // exclusive scan of cell_count into cell_start[0..ncells] (one block)
 __global__ void k_cell_scan(const int *__restrict__ count, int ncells, int *__restrict__ start,
                             int *__restrict__ fill) {
-  __shared__ int part[1024];
   int t = threadIdx.x, T = blockDim.x;
   int chunk = (ncells + T - 1) / T;
   int lo = min(t * chunk, ncells), hi = min(lo + chunk, ncells);
   int s = 0;
   for (int c = lo; c < hi; c++) s += count[c];
-  part[t] = s;
-  __syncthreads();
-  if (t == 0) {
-    int acc = 0;
-    for (int k = 0; k < T; k++) {
-      int v = part[k];
-      part[k] = acc;
-      acc += v;
-    }
-    start[ncells] = acc;
-  }
-  __syncthreads();
-  int acc = part[t];
+  int total;
+  int acc = block_exclusive_scan(s, &total);
+  if (t == 0) start[ncells] = total;
   for (int c = lo; c < hi; c++) {
     start[c] = acc;
     fill[c] = 0;
