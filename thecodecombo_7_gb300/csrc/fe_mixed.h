@@ -62,6 +62,12 @@ struct Mixed {
   int4 *snap = nullptr;           // posfx at the last prune
   MxPruneState *ps = nullptr;
   unsigned long long *fix = nullptr;  // 3n fixed-point forces (2^32 per kJ/mol/A)
+  // the reciprocal-space branch runs on its own stream beside the pair
+  // kernel, with its own last-block reduction slots
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
+  unsigned long long *facc2 = nullptr;
+  unsigned *ticket2 = nullptr;
   float *lj_tab = nullptr;        // nt*nt x (eps, sig^2, shift constant)
   unsigned char *lj_on = nullptr; // nt*nt: pair type has an LJ term
   unsigned *lj_row = nullptr;     // nt <= 32: bit t of lj_row[t'] = lj_on[t][t']

@@ -1625,7 +1625,7 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
 #pragma unroll
         for (int c = 0; c < 3; c++) {
           unsigned long long *q = fix + 3 * (size_t)(lb + i) + c;
-          *q = *q + (unsigned long long)to_fix(F[i][c]);
+          atomicAdd(q, (unsigned long long)to_fix(F[i][c]));
         }
   }
   long long v[7] = {to_fixed(A.e_lj, 32), to_fixed(A.e_ljs, 32), to_fixed(A.e_real, 32),
@@ -1691,6 +1691,13 @@ int mixed_setup(Box *b) {
   Mixed &M = *b->mx;
   int n = b->n;
   FE_CUDA(cudaDeviceGetAttribute(&M.nsm, cudaDevAttrMultiProcessorCount, b->dev));
+  FE_CUDA(cudaStreamCreateWithFlags(&M.s2, cudaStreamNonBlocking));
+  FE_CUDA(cudaEventCreateWithFlags(&M.ev_fork, cudaEventDisableTiming));
+  FE_CUDA(cudaEventCreateWithFlags(&M.ev_join, cudaEventDisableTiming));
+  FE_CUDA(cudaMalloc(&M.facc2, sizeof(unsigned long long) * kFaccSlots));
+  FE_CUDA(cudaMemset(M.facc2, 0, sizeof(unsigned long long) * kFaccSlots));
+  FE_CUDA(cudaMalloc(&M.ticket2, sizeof(unsigned)));
+  FE_CUDA(cudaMemset(M.ticket2, 0, sizeof(unsigned)));
   // cell grid of edge >= rlist / kListCellsPerReach
   double edge = (b->p.rclist > b->p.rclist_ew ? b->p.rclist : b->p.rclist_ew) / kListCellsPerReach;
   M.ncells = 1;
@@ -1954,9 +1961,12 @@ void mixed_free(Box *b) {
                   M.type_s, M.posfx, M.cnt_lj, M.cnt_nl, M.ent, M.icnt_lj, M.icnt_nl,
                   M.ient, M.snap, M.ps, M.fix, M.lj_tab, M.lj_on, M.lj_row, M.excl_ab, M.excl_flag, M.eterm32, M.kw32,
                   M.grid32, M.grid32k, M.floor3, M.gfix, M.sm, M.sd, M.mol_first, M.mol_x,
-                  M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai, M.exptab};
+                  M.mol_xi, M.mol_b, M.mol_bi, M.mol_a, M.mol_ai, M.exptab, M.facc2, M.ticket2};
   for (void *p : ptrs)
     if (p) cudaFree(p);
+  if (M.ev_fork) cudaEventDestroy(M.ev_fork);
+  if (M.ev_join) cudaEventDestroy(M.ev_join);
+  if (M.s2) cudaStreamDestroy(M.s2);
   if (M.plans) {
     cufftDestroy(M.plan_r2c);
     cufftDestroy(M.plan_c2r);
@@ -2144,20 +2154,68 @@ int mixed_autotune(Box *b, int *nw_out, int *rw_out, int *blocks_out, double *us
   return FE_OK;
 }
 
-int launch_mx_spread_only(Box *b) {
+static int spread_on(Box *b, cudaStream_t st) {
   Mixed &M = *b->mx;
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   long nt = (long)b->n * b->order;
   if (b->order == 4) {
-    k_mx_spread_o4<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(b->n, G, M.posfx, M.gfix);
+    k_mx_spread_o4<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(b->n, G, M.posfx, M.gfix);
     FE_LAUNCH_CHECK("k_mx_spread_o4");
   } else {
-    k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, b->stream>>>(
+    k_mx_spread_red<<<(unsigned)((nt + 255) / 256), 256, 0, st>>>(
         b->n, b->order, G, M.posfx, M.sm, M.floor3, M.gfix);
     FE_LAUNCH_CHECK("k_mx_spread_red");
   }
-  k_mx_fix2grid<<<M.nsm * 8, 256, 0, b->stream>>>(b->K, M.gfix, M.grid32);
+  k_mx_fix2grid<<<M.nsm * 8, 256, 0, st>>>(b->K, M.gfix, M.grid32);
   FE_LAUNCH_CHECK("k_mx_fix2grid");
+  return FE_OK;
+}
+
+int launch_mx_spread_only(Box *b) { return spread_on(b, b->stream); }
+
+// The reciprocal-space forces and energy (pme_calc's work) on stream st with
+// the reduction slots facc / ticket: [splines,] spreading, FFT, convolution,
+// inverse FFT, gather.  It reads the fixed-point coordinates and adds to the
+// force sums with integer atomics, so it may run beside the pair kernel.
+static int spme_on(Box *b, cudaStream_t st, unsigned long long *facc, unsigned *ticket) {
+  Mixed &M = *b->mx;
+  const int n = b->n;
+  int rc;
+  int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
+  if (b->order != 4) {  // order 4 computes its weights inside spreading and gathering
+    k_mx_splines<<<(n + 127) / 128, 128, 0, st>>>(n, b->order, G, M.posfx, M.floor3, M.sm,
+                                                  M.sd);
+    FE_LAUNCH_CHECK("k_mx_splines");
+  }
+  if ((rc = spread_on(b, st))) return rc;
+  cufftResult r = cufftSetStream(M.plan_r2c, st);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
+  r = cufftExecR2C(M.plan_r2c, M.grid32, M.grid32k);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
+  int kb = (int)((b->Kh + 255) / 256);
+  if (kb > 1024) kb = 1024;
+  k_mx_recip<<<kb, 256, 0, st>>>(b->Kh, M.eterm32, M.kw32, M.grid32k, facc, ticket,
+                                 b->scal + SC_ENREC);
+  FE_LAUNCH_CHECK("k_mx_recip");
+  r = cufftSetStream(M.plan_c2r, st);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
+  r = cufftExecC2R(M.plan_c2r, M.grid32k, M.grid32);
+  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R");
+  double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
+  float3 gl = make_float3((float)(b->G[0] / b->p.L[0]), (float)(b->G[1] / b->p.L[1]),
+                          (float)(b->G[2] / b->p.L[2]));
+  int gb = (n + 127) / 128;
+  if (gb > 1024) gb = 1024;
+  float qfe = (float)(qf / b->p.epsRF);
+  if (b->order == 4) {
+    k_mx_gather_o4<<<gb, 128, 0, st>>>(n, G, gl, qfe, M.posfx, M.perm, M.grid32, M.fix, facc,
+                                       ticket, b->scal + SC_FMEAN);
+    FE_LAUNCH_CHECK("k_mx_gather_o4");
+  } else {
+    k_mx_gather<<<gb, 128, 0, st>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3, M.sm,
+                                    M.sd, M.grid32, M.fix, facc, ticket, b->scal + SC_FMEAN);
+    FE_LAUNCH_CHECK("k_mx_gather");
+  }
   return FE_OK;
 }
 
@@ -2166,6 +2224,11 @@ int forces_mixed(Box *b) {
   int n = b->n;
   int rc;
   if ((rc = launch_convert(b, true))) return rc;  // also clears the force sums
+  // reciprocal space on the second stream, beside the pair kernel
+  FE_CUDA(cudaEventRecord(M.ev_fork, b->stream));
+  FE_CUDA(cudaStreamWaitEvent(M.s2, M.ev_fork, 0));
+  if ((rc = spme_on(b, M.s2, M.facc2, M.ticket2))) return rc;
+  FE_CUDA(cudaEventRecord(M.ev_join, M.s2));
   if ((rc = launch_mx_pair_only(b))) return rc;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
   // intramolecular terms: one thread per molecule when the topology allows,
@@ -2216,42 +2279,7 @@ int forces_mixed(Box *b) {
   }
   // Urey-Bradley, torsions and impropers (FP64, into the fixed-point sums)
   if ((rc = launch_bonded_ext(b, true))) return rc;
-  // SPME
-  int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
-  if (b->order != 4) {  // order 4 computes its weights inside spreading and gathering
-    k_mx_splines<<<(n + 127) / 128, 128, 0, b->stream>>>(n, b->order, G, M.posfx, M.floor3,
-                                                         M.sm, M.sd);
-    FE_LAUNCH_CHECK("k_mx_splines");
-  }
-  if ((rc = launch_mx_spread_only(b))) return rc;
-  cufftResult r = cufftSetStream(M.plan_r2c, b->stream);
-  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
-  r = cufftExecR2C(M.plan_r2c, M.grid32, M.grid32k);
-  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C");
-  int kb = (int)((b->Kh + 255) / 256);
-  if (kb > 1024) kb = 1024;
-  k_mx_recip<<<kb, 256, 0, b->stream>>>(b->Kh, M.eterm32, M.kw32, M.grid32k, b->facc,
-                                        b->ticket, b->scal + SC_ENREC);
-  FE_LAUNCH_CHECK("k_mx_recip");
-  r = cufftSetStream(M.plan_c2r, b->stream);
-  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
-  r = cufftExecC2R(M.plan_c2r, M.grid32k, M.grid32);
-  if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R");
-  float3 gl = make_float3((float)(b->G[0] / b->p.L[0]), (float)(b->G[1] / b->p.L[1]),
-                          (float)(b->G[2] / b->p.L[2]));
-  int gb = (n + 127) / 128;
-  if (gb > 1024) gb = 1024;
-  float qfe = (float)(qf / b->p.epsRF);
-  if (b->order == 4) {
-    k_mx_gather_o4<<<gb, 128, 0, b->stream>>>(n, G, gl, qfe, M.posfx, M.perm, M.grid32, M.fix,
-                                            b->facc, b->ticket, b->scal + SC_FMEAN);
-    FE_LAUNCH_CHECK("k_mx_gather_o4");
-  } else {
-    k_mx_gather<<<gb, 128, 0, b->stream>>>(n, b->order, G, gl, qfe, M.posfx, M.perm, M.floor3,
-                                           M.sm, M.sd, M.grid32, M.fix, b->facc, b->ticket,
-                                           b->scal + SC_FMEAN);
-    FE_LAUNCH_CHECK("k_mx_gather");
-  }
+  FE_CUDA(cudaStreamWaitEvent(b->stream, M.ev_join, 0));
   if (b->fold_tail) return FE_OK;  // finalised inside the second half kick
   k_mx_finalize<<<(3 * n + 255) / 256, 256, 0, b->stream>>>(n, M.fix, b->scal, b->ff);
   FE_LAUNCH_CHECK("k_mx_finalize");
