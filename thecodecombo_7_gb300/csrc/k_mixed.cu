@@ -2219,17 +2219,12 @@ static int spme_on(Box *b, cudaStream_t st, unsigned long long *facc, unsigned *
   return FE_OK;
 }
 
-int forces_mixed(Box *b) {
+// The intramolecular terms (exclusion corrections, 1-4 pairs, bonds, bends)
+// on stream st with the reduction slots facc / ticket: one thread per
+// molecule when the topology allows, else kernels over the exclusion and
+// bonded lists.  Integer atomics into the force sums.
+static int intra_on(Box *b, cudaStream_t st, unsigned long long *facc, unsigned *ticket) {
   Mixed &M = *b->mx;
-  int n = b->n;
-  int rc;
-  if ((rc = launch_convert(b, true))) return rc;  // also clears the force sums
-  // reciprocal space on the second stream, beside the pair kernel
-  FE_CUDA(cudaEventRecord(M.ev_fork, b->stream));
-  FE_CUDA(cudaStreamWaitEvent(M.s2, M.ev_fork, 0));
-  if ((rc = spme_on(b, M.s2, M.facc2, M.ticket2))) return rc;
-  FE_CUDA(cudaEventRecord(M.ev_join, M.s2));
-  if ((rc = launch_mx_pair_only(b))) return rc;
   double qf = kELEC * kELEQ * kELEQ * kNA * 1.0E-3;
   // intramolecular terms: one thread per molecule when the topology allows,
   // else the exclusion and bonded kernels
@@ -2243,40 +2238,56 @@ int forces_mixed(Box *b) {
       M.excl_flag, b->bond_ab, b->bond_req, b->bond_k, b->bend_abc, b->bend_t0, b->bend_k,        \
       M.posfx, M.iperm, b->type, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),                 \
       (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf, (float)b->p.epsRF,     \
-      b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket, b->scal + SC_MX_INTRA
+      b->pos_q, M.exptab, dfi, M.fix, facc, ticket, b->scal + SC_MX_INTRA
     if (M.uniform && M.tpl.ns == 3) {
-      k_mx_intra_uni<3><<<mb, 128, 0, b->stream>>>(
+      k_mx_intra_uni<3><<<mb, 128, 0, st>>>(
           M.nmol, M.tpl, M.posfx, M.iperm, sL, b->nt, M.lj_tab, (float)(b->p.rc * b->p.rc),
           (float)b->p.kappa, (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
-          (float)b->p.epsRF, b->pos_q, M.exptab, dfi, M.fix, b->facc, b->ticket,
+          (float)b->p.epsRF, b->pos_q, M.exptab, dfi, M.fix, facc, ticket,
           b->scal + SC_MX_INTRA);
     }
-    else if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
-    else if (M.intra_maxs <= 4) k_mx_intra<4><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
-    else k_mx_intra<kIntraMaxSites><<<mb, 128, 0, b->stream>>>(FE_INTRA_ARGS);
+    else if (M.intra_maxs <= 3) k_mx_intra<3><<<mb, 128, 0, st>>>(FE_INTRA_ARGS);
+    else if (M.intra_maxs <= 4) k_mx_intra<4><<<mb, 128, 0, st>>>(FE_INTRA_ARGS);
+    else k_mx_intra<kIntraMaxSites><<<mb, 128, 0, st>>>(FE_INTRA_ARGS);
 #undef FE_INTRA_ARGS
     FE_LAUNCH_CHECK("k_mx_intra");
   } else {
     int xb = (M.nexcl + 255) / 256;
     if (xb > 1024) xb = 1024;
     if (xb < 1) xb = 1;
-    k_mx_excl<<<xb, 256, 0, b->stream>>>(M.nexcl, M.excl_ab, M.excl_flag, M.posfx, M.iperm,
+    k_mx_excl<<<xb, 256, 0, st>>>(M.nexcl, M.excl_ab, M.excl_flag, M.posfx, M.iperm,
                                          b->type, sL, b->nt, M.lj_tab,
                                          (float)(b->p.rc * b->p.rc), (float)b->p.kappa,
                                          (float)(2.0 * b->p.kappa / sqrt(kPI)), (float)qf,
                                          (float)b->p.epsRF, b->pos_q, M.exptab, dfi, M.fix,
-                                         b->facc, b->ticket, b->scal + SC_MX_EXCL);
+                                         facc, ticket, b->scal + SC_MX_EXCL);
     FE_LAUNCH_CHECK("k_mx_excl");
     int tot = b->nbond + b->nbend;
     int bb = (tot + 255) / 256;
     if (bb > 1024) bb = 1024;
     if (bb < 1) bb = 1;
-    k_mx_bonded<<<bb, 256, 0, b->stream>>>(b->nbond, b->nbend, sL, M.posfx, M.iperm, b->bond_ab,
+    k_mx_bonded<<<bb, 256, 0, st>>>(b->nbond, b->nbend, sL, M.posfx, M.iperm, b->bond_ab,
                                            b->bond_req, b->bond_k, b->bend_abc, b->bend_t0,
-                                           b->bend_k, M.fix, b->facc, b->ticket,
+                                           b->bend_k, M.fix, facc, ticket,
                                            b->scal + SC_BOND);
     FE_LAUNCH_CHECK("k_mx_bonded");
   }
+  return FE_OK;
+}
+
+int forces_mixed(Box *b) {
+  Mixed &M = *b->mx;
+  int n = b->n;
+  int rc;
+  if ((rc = launch_convert(b, true))) return rc;  // also clears the force sums
+  // reciprocal space on the second stream, beside the pair kernel (the
+  // intramolecular terms there measured slower: they follow the pair kernel)
+  FE_CUDA(cudaEventRecord(M.ev_fork, b->stream));
+  FE_CUDA(cudaStreamWaitEvent(M.s2, M.ev_fork, 0));
+  if ((rc = spme_on(b, M.s2, M.facc2, M.ticket2))) return rc;
+  FE_CUDA(cudaEventRecord(M.ev_join, M.s2));
+  if ((rc = launch_mx_pair_only(b))) return rc;
+  if ((rc = intra_on(b, b->stream, b->facc, b->ticket))) return rc;
   // Urey-Bradley, torsions and impropers (FP64, into the fixed-point sums)
   if ((rc = launch_bonded_ext(b, true))) return rc;
   FE_CUDA(cudaStreamWaitEvent(b->stream, M.ev_join, 0));
@@ -2303,8 +2314,8 @@ struct BMxArgs {
   int4 *snap;
   float3 sc;
   MxPruneState *ps;
-  unsigned long long *fix, *facc;
-  unsigned *ticket;
+  unsigned long long *fix, *facc, *facc2;  // facc2 / ticket2: the reciprocal branch's
+  unsigned *ticket, *ticket2;
   double *scal;
   int *status;
   // pair
@@ -2409,7 +2420,7 @@ __global__ void k_b_mx_gather_o4(const BMxArgs *__restrict__ A, const int *__res
   const int r = vblk_box(off, nbox);
   const BMxArgs &a = A[r];
   k_mx_gather_o4_body(vblk_of(off, r), a.n, a.G, a.gl, a.qfe, a.posfx, a.perm, a.grid32, a.fix,
-                    a.facc, a.ticket, a.scal + SC_FMEAN);
+                    a.facc2, a.ticket2, a.scal + SC_FMEAN);
 }
 
 __global__ void k_b_mx_fix2grid(const BMxArgs *__restrict__ A, const int *__restrict__ off,
@@ -2423,7 +2434,7 @@ __global__ void k_b_mx_recip(const BMxArgs *__restrict__ A, const int *__restric
                              int nbox) {
   const int r = vblk_box(off, nbox);
   const BMxArgs &a = A[r];
-  k_mx_recip_body(vblk_of(off, r), a.Kh, a.eterm32, a.kw32, a.grid32k, a.facc, a.ticket,
+  k_mx_recip_body(vblk_of(off, r), a.Kh, a.eterm32, a.kw32, a.grid32k, a.facc2, a.ticket2,
                   a.scal + SC_ENREC);
 }
 
@@ -2432,7 +2443,7 @@ __global__ void k_b_mx_gather(const BMxArgs *__restrict__ A, const int *__restri
   const int r = vblk_box(off, nbox);
   const BMxArgs &a = A[r];
   k_mx_gather_body(vblk_of(off, r), a.n, a.order, a.G, a.gl, a.qfe, a.posfx, a.perm, a.floor3,
-                   a.sm, a.sd, a.grid32, a.fix, a.facc, a.ticket, a.scal + SC_FMEAN);
+                   a.sm, a.sd, a.grid32, a.fix, a.facc2, a.ticket2, a.scal + SC_FMEAN);
 }
 
 __global__ void k_b_mx_finalize(const BMxArgs *__restrict__ A, const int *__restrict__ off,
@@ -2526,6 +2537,9 @@ struct BMxPlan {
   BMxRange cell, fill, cellsort, list;
   int intra_ns = 3;
   bool order4 = true;  // every box has B-spline order 4: weights computed in place
+  // the reciprocal branch's stream and its fork / join events
+  cudaStream_t s2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   size_t pair_shm = 0;
   std::vector<BMxGroup> groups;
 };
@@ -2546,6 +2560,9 @@ void mixed_batch_free(BMxPlan *P) {
                     &P->fix2grid, &P->recip, &P->gather, &P->finalize, &P->cell, &P->fill,
                     &P->cellsort, &P->list};
   for (BMxRange *r : rs) cudaFree(r->d_off);
+  if (P->ev_fork) cudaEventDestroy(P->ev_fork);
+  if (P->ev_join) cudaEventDestroy(P->ev_join);
+  if (P->s2) cudaStreamDestroy(P->s2);
   for (BMxGroup &g : P->groups) {
     if (g.plans) {
       cufftDestroy(g.r2c);
@@ -2583,6 +2600,9 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
     }
   BMxPlan *P = new BMxPlan();
   P->nbox = nbox;
+  FE_CUDA(cudaStreamCreateWithFlags(&P->s2, cudaStreamNonBlocking));
+  FE_CUDA(cudaEventCreateWithFlags(&P->ev_fork, cudaEventDisableTiming));
+  FE_CUDA(cudaEventCreateWithFlags(&P->ev_join, cudaEventDisableTiming));
   std::vector<BMxArgs> args(nbox);
   std::vector<int> bconv, bprune, bpair, bintra, bspl, bspr, bf2g, brec, bgat, bfin;
   std::vector<int> bcell, bfill, bsort, blist;
@@ -2610,6 +2630,8 @@ int mixed_batch_plan(Box *const *boxes, int nbox, BMxPlan **out) {
     a.fix = M.fix;
     a.facc = b->facc;
     a.ticket = b->ticket;
+    a.facc2 = M.facc2;
+    a.ticket2 = M.ticket2;
     a.scal = b->scal;
     a.status = b->status;
     a.P = mx_pair_params(b);
@@ -2798,6 +2820,42 @@ int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
   const int nb = P->nbox;
   k_b_mx_convert<<<P->convert.total, 256, 0, s>>>(P->d_args, P->convert.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_convert");
+  // reciprocal space of every box on the second stream, beside the pair kernel
+  cudaStream_t s2 = P->s2;
+  FE_CUDA(cudaEventRecord(P->ev_fork, s));
+  FE_CUDA(cudaStreamWaitEvent(s2, P->ev_fork, 0));
+  if (P->order4) {
+    k_b_mx_spread_o4<<<P->spread.total, 256, 0, s2>>>(P->d_args, P->spread.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_spread_o4");
+  } else {
+    k_b_mx_splines<<<P->splines.total, 128, 0, s2>>>(P->d_args, P->splines.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_splines");
+    k_b_mx_spread<<<P->spread.total, 256, 0, s2>>>(P->d_args, P->spread.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_spread");
+  }
+  k_b_mx_fix2grid<<<P->fix2grid.total, 256, 0, s2>>>(P->d_args, P->fix2grid.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_fix2grid");
+  for (BMxGroup &g : P->groups) {
+    cufftResult r = cufftSetStream(g.r2c, s2);
+    if (r == CUFFT_SUCCESS) r = cufftExecR2C(g.r2c, g.real, g.cplx);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C (batch)");
+  }
+  k_b_mx_recip<<<P->recip.total, 256, 0, s2>>>(P->d_args, P->recip.d_off, nb);
+  FE_LAUNCH_CHECK("k_b_mx_recip");
+  for (BMxGroup &g : P->groups) {
+    cufftResult r = cufftSetStream(g.c2r, s2);
+    if (r == CUFFT_SUCCESS) r = cufftExecC2R(g.c2r, g.cplx, g.real);
+    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R (batch)");
+  }
+  if (P->order4) {
+    k_b_mx_gather_o4<<<P->gather.total, 128, 0, s2>>>(P->d_args, P->gather.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_gather_o4");
+  } else {
+    k_b_mx_gather<<<P->gather.total, 128, 0, s2>>>(P->d_args, P->gather.d_off, nb);
+    FE_LAUNCH_CHECK("k_b_mx_gather");
+  }
+  FE_CUDA(cudaEventRecord(P->ev_join, s2));
+  // real space and the intramolecular terms
   k_b_mx_pair<true><<<P->prune.total, 256, P->pair_shm, s>>>(P->d_args, P->prune.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_pair<prune>");
   k_b_mx_pair<false><<<P->pair.total, 256, P->pair_shm, s>>>(P->d_args, P->pair.d_off, nb);
@@ -2806,36 +2864,7 @@ int mixed_batch_forces(BMxPlan *P, cudaStream_t s) {
   else if (P->intra_ns <= 4) k_b_mx_intra<4><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
   else k_b_mx_intra<kIntraMaxSites><<<P->intra.total, 128, 0, s>>>(P->d_args, P->intra.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_intra");
-  if (P->order4) {
-    k_b_mx_spread_o4<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_spread_o4");
-  } else {
-    k_b_mx_splines<<<P->splines.total, 128, 0, s>>>(P->d_args, P->splines.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_splines");
-    k_b_mx_spread<<<P->spread.total, 256, 0, s>>>(P->d_args, P->spread.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_spread");
-  }
-  k_b_mx_fix2grid<<<P->fix2grid.total, 256, 0, s>>>(P->d_args, P->fix2grid.d_off, nb);
-  FE_LAUNCH_CHECK("k_b_mx_fix2grid");
-  for (BMxGroup &g : P->groups) {
-    cufftResult r = cufftSetStream(g.r2c, s);
-    if (r == CUFFT_SUCCESS) r = cufftExecR2C(g.r2c, g.real, g.cplx);
-    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecR2C (batch)");
-  }
-  k_b_mx_recip<<<P->recip.total, 256, 0, s>>>(P->d_args, P->recip.d_off, nb);
-  FE_LAUNCH_CHECK("k_b_mx_recip");
-  for (BMxGroup &g : P->groups) {
-    cufftResult r = cufftSetStream(g.c2r, s);
-    if (r == CUFFT_SUCCESS) r = cufftExecC2R(g.c2r, g.cplx, g.real);
-    if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecC2R (batch)");
-  }
-  if (P->order4) {
-    k_b_mx_gather_o4<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_gather_o4");
-  } else {
-    k_b_mx_gather<<<P->gather.total, 128, 0, s>>>(P->d_args, P->gather.d_off, nb);
-    FE_LAUNCH_CHECK("k_b_mx_gather");
-  }
+  FE_CUDA(cudaStreamWaitEvent(s, P->ev_join, 0));
   k_b_mx_finalize<<<P->finalize.total, 256, 0, s>>>(P->d_args, P->finalize.d_off, nb);
   FE_LAUNCH_CHECK("k_b_mx_finalize");
   return FE_OK;
