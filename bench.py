@@ -488,6 +488,7 @@ def go_sample(local):
         torch.cuda.synchronize()
         sec = e0.elapsed_time(e1) / 1000.0
         s = b.state()
+        lay = b.layout()
     finally:
         b.close()
     nb = int(g.nbeads.sum())
@@ -499,6 +500,8 @@ def go_sample(local):
             "steps": 5000, "us_per_step": 1e6 * sec / 5000,
             "exchange_attempts": int(s["attempted"].sum()),
             "exchanges_accepted": int(s["accepted"].sum()),
+            "ctas": lay["ncta"], "resident_ctas": lay["slots"],
+            "chains_by_ctas": {str(k): int((lay["parts"] == k).sum()) for k in (1, 2, 3, 4)},
             "workload": "64 Go-model C-alpha chains (60-400 beads), bonds 3.8 A k=100 "
                         "kcal/mol/A^2, natives 12-10 eps=1 kcal/mol, non-native (4 A/r)^12, "
                         "BAOAB Langevin dt 10 fs gamma 1/ps, T 280-450 K geometric, exchange "

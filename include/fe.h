@@ -446,6 +446,10 @@ int fe_go_forces(fe_go *go, double *f, double *epot);
 int fe_go_state(fe_go *go, double *pos, double *vel, double *T, double *epot, int *slot_rep,
                 int64_t *accepted, int64_t *attempted, uint64_t *steps);
 int fe_go_get_stream(fe_go *go, void **stream);
+/* The launch's load-balance plan: *ncta CTAs (clusters of four), *slots the
+ * CTAs the GPU holds at once, parts[r] (nrep ints, may be NULL) the CTAs
+ * that share replica r's chain (1 to 4). */
+int fe_go_layout(fe_go *go, int *ncta, int *slots, int *parts);
 
 /* ---- launch-shape autotuning (no counterpart in the reference) --------- */
 

@@ -82,3 +82,34 @@ def test_go_reproducible(chains):
             b.close()
     assert np.array_equal(out[0]["pos"], out[1]["pos"])
     assert np.array_equal(out[0]["slot_rep"], out[1]["slot_rep"])
+
+
+def test_go_split_plan_and_forces():
+    """48 chains of 20-120 beads: the plan mixes chains on one CTA with chains
+    split over several CTAs of a cluster; every kind matches the oracle's
+    forces and a short trajectory."""
+    from thecodecombo_7_gb300 import engine, systems
+    g = systems.go_chains(48, nmin=20, nmax=120, seed=19)
+    b = engine.GoBatch(g, seed=2)
+    try:
+        lay = b.layout()
+        f, e = b.forces()
+        b.run(10)
+        s = b.state()
+    finally:
+        b.close()
+    parts = lay["parts"]
+    assert lay["ncta"] % 4 == 0 and parts.sum() <= lay["ncta"]
+    assert set(parts.tolist()) <= {1, 2, 3, 4}
+    assert len(set(parts.tolist())) > 1, parts
+    assert lay["ncta"] <= lay["slots"] or parts.max() == 1
+    st = g.start
+    for r in range(len(g.nbeads)):
+        fr, er = O.go_forces(g, r)
+        fg = f[st[r]:st[r + 1]]
+        rms = np.sqrt(((fg - fr) ** 2).sum() / (fr ** 2).sum())
+        assert rms <= 1e-5, (r, parts[r], rms)
+        assert abs(e[r] - er) <= 1e-5 * g.eps * g.nbeads[r], (r, parts[r], e[r], er)
+        x, v, eo = O.go_baoab(g, r, 10, seed=2)
+        assert np.abs(s["pos"][st[r]:st[r + 1]] - x).max() < 1e-4, (r, parts[r])
+        assert np.abs(s["vel"][st[r]:st[r + 1]] - v).max() < 1e-2, (r, parts[r])

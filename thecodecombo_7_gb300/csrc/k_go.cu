@@ -1,6 +1,7 @@
 // k_go.cu -- batched replica exchange of C-alpha Go-model chains: one
 // persistent launch runs a whole exchange segment (thousands of Langevin
-// steps) of every replica, one CTA per replica and one thread per bead.
+// steps) of every replica, one to four CTAs per replica and one to sixteen
+// threads per bead.
 //
 // The reference's Go pair loop (cnbnd_golik, cgolik.c:644-948) walks the
 // Verlet list with a dense N x N native-contact matrix (golik[k].contact)
@@ -16,17 +17,34 @@
 //   - the native contacts as a bitmask (N^2 bits per replica, in shared
 //     memory) plus a CSR list of (partner, r0^2) for the attraction;
 //   - forces in FP32, all pairs of the chain per bead (<= 1024 beads), split
-//     over 1-8 adjacent threads per bead and summed by warp shuffles; no
+//     over 1-16 adjacent threads per bead and summed by warp shuffles; no
 //     atomics, fixed order;
+//   - load balance over the SMs: the launch runs clusters of four CTAs, and a
+//     long chain is split over 2 to 4 CTAs of one cluster (each owns a
+//     contiguous slice of beads and computes their forces from all beads of
+//     the chain).  Every CTA holds the whole chain's FP32 positions in two
+//     shared-memory buffers; after each update a CTA stores its slice into
+//     the next buffer of every CTA of its chain (distributed shared memory)
+//     and one cluster barrier per step orders the stores before the reads.
+//     Shorter chains take one CTA each; the split of each chain is planned
+//     on the host to level the partners each thread walks per step over the
+//     CTAs the GPU holds at once;
+//   - the FP64 state update by one thread per bead, apart from the force
+//     layout, so that each warp's FP64 instructions carry 32 beads; the
+//     pair energies are summed only in the last force evaluation of a
+//     segment (the exchange needs no other);
 //   - positions and velocities in FP64 registers of the owning thread for
 //     the whole segment; BAOAB Langevin (Leimkuhler & Matthews 2013) with the
-//     O step v = c1 v + c2 sqrt(kT/m) xi in FP64, xi Gaussian by Box-Muller
-//     from Philox4x32-10 draws keyed by (bead, step);
+//     O step v = c1 v + c2 sqrt(kT/m) xi in FP64 (the noise term itself
+//     formed in FP32), xi Gaussian by Box-Muller from Philox4x32-10 draws
+//     keyed by (bead, step); the closing B of one step and the opening B of
+//     the next are one kick of 2 (dt/2) f / m;
 //   - after the segment, one exchange kernel: adjacent temperature slots as
 //     swap_box does (pairs alternate between attempts), acceptance
 //     exp((1/kT_s - 1/kT_s+1)(U_s - U_s+1)) > u, velocity rescale by
 //     sqrt(T_s/T_s+1); it also advances the device step counter, so the
 //     pair (segment, exchange) is captured once as a CUDA graph and replayed.
+#include <algorithm>
 #include <cmath>
 #include <vector>
 
@@ -36,20 +54,33 @@
 namespace fe {
 
 constexpr int kGoMaxBeads = 1024;
+constexpr int kGoBlock = 1024;   // threads per CTA
+constexpr int kGoCluster = 4;    // CTAs per cluster; a chain takes 1 to 4 of them
+constexpr int kGoMaxTpb = 16;    // threads per bead at most
 constexpr uint32_t kRngTagGo = 0x474F4C31u;  // "GOL1"
+
+// What one CTA of the launch does: beads [lo, lo + nb) of replica `rep`
+// with `tpb` threads per bead; its chain is shared by the cluster ranks
+// [peer0, peer0 + npeer).  rep < 0: a padding CTA that only joins the
+// cluster barriers.
+struct GoCta {
+  int rep, lo, nb, tpb, peer0, npeer;
+};
 
 struct GoK {
   float eps, sig2, rc2, e_shift, kb, r0b;
+  float c12, f12;   // eps sigma^12 and 12 eps sigma^12 of the repulsion
   double acc_fac;   // 100 / m: kJ/mol/A per amu -> A/ps^2
   double dt, c1, c2;
   double vscale;    // sqrt(100 / m): sqrt(kT [kJ/mol]) -> A/ps
   int min_sep;
   int nrep;
-  int tpb;          // threads per bead (power of two)
+  int maxN;         // longest chain: the stride of the two position buffers
   uint64_t seed;
 };
 
 struct GoD {
+  const GoCta *cta;      // one per CTA of the launch
   const int *start;      // nrep + 1: first bead of each replica
   const int *maskoff;    // nrep: first mask word of each replica
   const unsigned *mask;  // native bitmask rows (N words of ceil(N/32) per replica)
@@ -70,35 +101,50 @@ struct GoD {
 
 // Force on bead i of a chain of N (positions in shared memory) from the
 // partners j = sub, sub + T, sub + 2T, ... (T threads per bead, sub its
-// index); natives and bonds are added by sub 0 only.  Returns this thread's
-// share of the potential energy (pairs and bonds split in half).
-__device__ __forceinline__ float go_force(const GoK &K, const GoD &D, const float4 *__restrict__ p,
-                                          const unsigned *__restrict__ mrow, int N, int i, int sub,
-                                          int T, int gbase, float &fx, float &fy, float &fz) {
-  float4 pi = p[i];
+// index); natives likewise over the bead's CSR row, bonds by sub 0 only.
+// The partners of one 32-bead word are taken in groups of up to four whose
+// positions are loaded together.  Returns this thread's share of the
+// potential energy (pairs and bonds split in half).
+template <int T, bool WITH_E>
+__device__ __forceinline__ float go_force_t(const GoK &K, const GoD &D, const float4 *__restrict__ p,
+                                            const unsigned *__restrict__ mrow, int N, int i,
+                                            int sub, int gbase, float &fx, float &fy, float &fz) {
+  constexpr int PER = 32 / T;           // this thread's partners per word
+  constexpr int G = PER < 4 ? PER : 4;  // loads in flight
+  const float4 pi = p[i];
   float e = 0.f;
   fx = fy = fz = 0.f;
-  for (int j = sub; j < N; j += T) {
-    int sep = i > j ? i - j : j - i;
-    if (sep < K.min_sep) continue;
-    if ((mrow[j >> 5] >> (j & 31)) & 1u) continue;  // native: below
-    float4 pj = p[j];
-    float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
-    float r2 = dx * dx + dy * dy + dz * dz;
-    if (r2 >= K.rc2) continue;
-    float ri2 = __fdividef(1.f, r2);
-    float s2 = K.sig2 * ri2;
-    float s6 = s2 * s2 * s2;
-    float s12 = s6 * s6;
-    e += 0.5f * (K.eps * s12 - K.e_shift);
-    float fs = 12.f * K.eps * s12 * ri2;
-    fx = fmaf(fs, dx, fx);
-    fy = fmaf(fs, dy, fy);
-    fz = fmaf(fs, dz, fz);
+  // the row's bits mark the pairs the repulsion skips: natives (below) and
+  // |i - j| < min_sep, the bead itself included
+  const int nw = (N + 31) >> 5;
+  for (int w = 0; w < nw; w++) {
+    const unsigned skip = mrow[w];
+    const int base = w << 5;
+#pragma unroll
+    for (int k0 = 0; k0 < PER; k0 += G) {
+      float4 pj[G];
+#pragma unroll
+      for (int k = 0; k < G; k++) pj[k] = p[min(base + sub + (k0 + k) * T, N - 1)];
+#pragma unroll
+      for (int k = 0; k < G; k++) {
+        const int b = sub + (k0 + k) * T;
+        const float dx = pi.x - pj[k].x, dy = pi.y - pj[k].y, dz = pi.z - pj[k].z;
+        const float r2 = dx * dx + dy * dy + dz * dz;
+        if (base + b < N && !((skip >> b) & 1u) && r2 < K.rc2) {
+          const float ri2 = __fdividef(1.f, r2);
+          const float ri6 = ri2 * ri2 * ri2;
+          const float ri12 = ri6 * ri6;
+          if (WITH_E) e += 0.5f * fmaf(K.c12, ri12, -K.e_shift);
+          const float fs = K.f12 * ri12 * ri2;
+          fx = fmaf(fs, dx, fx);
+          fy = fmaf(fs, dy, fy);
+          fz = fmaf(fs, dz, fz);
+        }
+      }
+    }
   }
-  if (sub != 0) return e;
-  int g = gbase + i;
-  for (int q = D.nat_start[g]; q < D.nat_start[g + 1]; q++) {
+  const int g = gbase + i;
+  for (int q = D.nat_start[g] + sub; q < D.nat_start[g + 1]; q += T) {
     int j = D.nat_j[q] - gbase;
     float4 pj = p[j];
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
@@ -107,12 +153,13 @@ __device__ __forceinline__ float go_force(const GoK &K, const GoD &D, const floa
     float s2 = D.nat_r02[q] * ri2;
     float s10 = s2 * s2 * s2 * s2 * s2;
     float s12 = s10 * s2;
-    e += 0.5f * K.eps * (5.f * s12 - 6.f * s10);
+    if (WITH_E) e += 0.5f * K.eps * (5.f * s12 - 6.f * s10);
     float fs = 60.f * K.eps * (s12 - s10) * ri2;
     fx = fmaf(fs, dx, fx);
     fy = fmaf(fs, dy, fy);
     fz = fmaf(fs, dz, fz);
   }
+  if (sub != 0) return e;
   for (int nb = -1; nb <= 1; nb += 2) {
     int j = i + nb;
     if (j < 0 || j >= N) continue;
@@ -120,13 +167,26 @@ __device__ __forceinline__ float go_force(const GoK &K, const GoD &D, const floa
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     float r = sqrtf(dx * dx + dy * dy + dz * dz);
     float dr = r - K.r0b;
-    e += 0.5f * K.kb * dr * dr;
+    if (WITH_E) e += 0.5f * K.kb * dr * dr;
     float fs = -2.f * K.kb * dr / r;
     fx = fmaf(fs, dx, fx);
     fy = fmaf(fs, dy, fy);
     fz = fmaf(fs, dz, fz);
   }
   return e;
+}
+
+template <bool WITH_E>
+__device__ __forceinline__ float go_force(const GoK &K, const GoD &D, const float4 *__restrict__ p,
+                                          const unsigned *__restrict__ mrow, int N, int i, int sub,
+                                          int T, int gbase, float &fx, float &fy, float &fz) {
+  switch (T) {
+    case 1: return go_force_t<1, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 2: return go_force_t<2, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 4: return go_force_t<4, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 8: return go_force_t<8, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    default: return go_force_t<16, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+  }
 }
 
 // sum over the T adjacent lanes of one bead (T a power of two <= 32)
@@ -172,85 +232,151 @@ __device__ __forceinline__ double go_block_sum(double v, double *red) {
   return red[32];
 }
 
+// Distributed shared memory and the cluster barrier (PTX ISA: mapa,
+// st.shared::cluster, barrier.cluster).
+__device__ __forceinline__ uint32_t go_cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+__device__ __forceinline__ uint32_t go_peer_addr(const void *p, uint32_t rank) {
+  uint32_t a = (uint32_t)__cvta_generic_to_shared(p), d;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(rank));
+  return d;
+}
+__device__ __forceinline__ void go_st_peer(uint32_t a, float4 v) {
+  asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v.x), "f"(v.y),
+               "f"(v.z), "f"(v.w)
+               : "memory");
+}
+__device__ __forceinline__ void go_st_peer(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+// every thread of the cluster: stores before it are seen by loads after it
+__device__ __forceinline__ void go_cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release;\n\tbarrier.cluster.wait.acquire;" ::: "memory");
+}
+
+// bead i's FP32 position into buffer slot i of every CTA of the chain
+__device__ __forceinline__ void go_publish(const GoCta &c, float4 *buf, int i, double x0, double x1,
+                                           double x2) {
+  const float4 p = make_float4((float)x0, (float)x1, (float)x2, 0.f);
+  for (int q = 0; q < c.npeer; q++) go_st_peer(go_peer_addr(buf + i, (uint32_t)(c.peer0 + q)), p);
+}
+
 // One segment of nsteps BAOAB steps of every replica (mode 0), or a single
-// force evaluation into D.f (mode 1).
-__global__ void __launch_bounds__(kGoMaxBeads, 1) k_go_segment(GoK K, GoD D, int nsteps, int mode) {
-  extern __shared__ float4 go_pos[];
-  const int r = blockIdx.x, T = K.tpb;
-  const int i = threadIdx.x / T, sub = threadIdx.x % T;
-  const int gbase = D.start[r], N = D.start[r + 1] - gbase;
-  const int W = (N + 31) >> 5;
-  unsigned *mask = (unsigned *)(go_pos + N);
+// force evaluation into D.f (mode 1).  Launched in clusters of kGoCluster
+// CTAs; every thread of every CTA runs the same barriers.  Forces use T
+// threads per bead; the FP64 state update uses one thread per bead (thread
+// t integrates bead lo + t), so each warp's FP64 instructions carry 32
+// beads — the FP64 pipe is narrow on this part.  The forces pass between
+// the two layouts through shared memory.
+__global__ void __launch_bounds__(kGoBlock, 1) k_go_segment(GoK K, GoD D, int nsteps, int mode) {
+  extern __shared__ float4 go_pos[];  // two buffers of K.maxN, then the skip rows
   __shared__ double red[33];
-  for (int t = threadIdx.x; t < N * W; t += blockDim.x) mask[t] = D.mask[D.maskoff[r] + t];
-  const bool bead = i < N;          // this thread works on a bead
-  const bool own = bead && sub == 0;  // ... and owns its coordinates
+  __shared__ double epart[kGoCluster];
+  __shared__ float4 fsh[kGoBlock];    // the lane-summed force of each bead of the slice
+  const GoCta c = D.cta[blockIdx.x];
+  const bool live = c.rep >= 0;
+  const int T = live ? c.tpb : 1;
+  const int il = threadIdx.x / T, sub = threadIdx.x % T;
+  const int gbase = live ? D.start[c.rep] : 0;
+  const int N = live ? D.start[c.rep + 1] - gbase : 0;
+  const int W = (N + 31) >> 5;
+  unsigned *rows = (unsigned *)(go_pos + 2 * K.maxN);
+  const bool bead = live && il < c.nb;  // this thread computes forces on bead lo + il
+  const int i = c.lo + il;
+  const bool integ = live && (int)threadIdx.x < c.nb;  // ... integrates bead lo + tid
+  const int ib = c.lo + (int)threadIdx.x;
+  if (live) {
+    const unsigned *src = D.mask + D.maskoff[c.rep] + (size_t)c.lo * W;
+    for (int t = threadIdx.x; t < c.nb * W; t += blockDim.x) rows[t] = src[t];
+  }
+  __syncthreads();
+  const unsigned *mrow = rows + (bead ? il : 0) * W;
+  if (bead && sub == 0) {
+    unsigned *row = rows + il * W;
+    for (int j = max(0, i - K.min_sep + 1); j <= min(N - 1, i + K.min_sep - 1); j++)
+      row[j >> 5] |= 1u << (j & 31);
+  }
   double x0 = 0, x1 = 0, x2 = 0, v0 = 0, v1 = 0, v2 = 0;
-  if (own) {
-    const double *xp = D.x + 3 * (size_t)(gbase + i), *vp = D.v + 3 * (size_t)(gbase + i);
+  if (integ) {
+    const double *xp = D.x + 3 * (size_t)(gbase + ib), *vp = D.v + 3 * (size_t)(gbase + ib);
     x0 = xp[0];
     x1 = xp[1];
     x2 = xp[2];
     v0 = vp[0];
     v1 = vp[1];
     v2 = vp[2];
-    go_pos[i] = make_float4((float)x0, (float)x1, (float)x2, 0.f);
   }
-  __syncthreads();
-  const unsigned *mrow = mask + (bead ? i : 0) * W;
+  go_cluster_sync();  // every CTA of the cluster runs: its shared memory may be written
+  if (integ) go_publish(c, go_pos, ib, x0, x1, x2);
+  go_cluster_sync();
   float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
-  if (bead) e = go_force(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
+  if (bead) {
+    if (mode == 1 || nsteps == 0) e = go_force<true>(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
+    else go_force<false>(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
+  }
   fx = go_lane_sum(fx, T);
   fy = go_lane_sum(fy, T);
   fz = go_lane_sum(fz, T);
+  if (bead && sub == 0) fsh[il] = make_float4(fx, fy, fz, 0.f);
+  __syncthreads();
   if (mode == 1) {
-    if (own) {
-      float *fp = D.f + 3 * (size_t)(gbase + i);
-      fp[0] = fx;
-      fp[1] = fy;
-      fp[2] = fz;
+    if (integ) {
+      const float4 f = fsh[threadIdx.x];
+      float *fp = D.f + 3 * (size_t)(gbase + ib);
+      fp[0] = f.x;
+      fp[1] = f.y;
+      fp[2] = f.z;
     }
-    double et = go_block_sum(bead ? (double)e : 0.0, red);
-    if (threadIdx.x == 0) D.epot[r] = et;
-    return;
+    nsteps = 0;
   }
   const unsigned long long step0 = *D.step;
-  const double kT = ((kKB * kNA) * D.T[r]) * .001;  // read_sim.c:351, kJ/mol
-  const double sv = K.vscale * sqrt(kT) * K.c2;
+  const double kT = live ? ((kKB * kNA) * D.T[c.rep]) * .001 : 0.0;  // read_sim.c:351, kJ/mol
+  const float svf = (float)(K.vscale * sqrt(kT) * K.c2);  // the noise amplitude
   const double hdt = 0.5 * K.dt, ha = 0.5 * K.dt * K.acc_fac;
   for (int s = 0; s < nsteps; s++) {
-    if (own) {
-      // B, A, O, A
-      v0 += ha * fx;
-      v1 += ha * fy;
-      v2 += ha * fz;
+    float4 *nxt = go_pos + ((s + 1) & 1) * K.maxN;
+    if (integ) {
+      const float4 f = fsh[threadIdx.x];
+      // the closing B of step s - 1 (s > 0) and the B of step s, then A, O, A
+      const double k = s > 0 ? 2.0 * ha : ha;
+      v0 += k * f.x;
+      v1 += k * f.y;
+      v2 += k * f.z;
       x0 += hdt * v0;
       x1 += hdt * v1;
       x2 += hdt * v2;
       float z0, z1, z2;
-      go_normals(K.seed, (uint32_t)(gbase + i), step0 + s, z0, z1, z2);
-      v0 = K.c1 * v0 + sv * z0;
-      v1 = K.c1 * v1 + sv * z1;
-      v2 = K.c1 * v2 + sv * z2;
+      go_normals(K.seed, (uint32_t)(gbase + ib), step0 + s, z0, z1, z2);
+      v0 = K.c1 * v0 + (double)(svf * z0);
+      v1 = K.c1 * v1 + (double)(svf * z1);
+      v2 = K.c1 * v2 + (double)(svf * z2);
       x0 += hdt * v0;
       x1 += hdt * v1;
       x2 += hdt * v2;
+      // every CTA of the chain read this buffer last in step s - 1, before
+      // the barrier that ended that step
+      go_publish(c, nxt, ib, x0, x1, x2);
     }
-    __syncthreads();  // everyone is done reading the old positions
-    if (own) go_pos[i] = make_float4((float)x0, (float)x1, (float)x2, 0.f);
-    __syncthreads();
-    if (bead) e = go_force(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
+    go_cluster_sync();  // also: fsh was read above before it is written below
+    if (bead) {  // the energy of the last step only
+      if (s == nsteps - 1) e = go_force<true>(K, D, nxt, mrow, N, i, sub, T, gbase, fx, fy, fz);
+      else go_force<false>(K, D, nxt, mrow, N, i, sub, T, gbase, fx, fy, fz);
+    }
     fx = go_lane_sum(fx, T);
     fy = go_lane_sum(fy, T);
     fz = go_lane_sum(fz, T);
-    if (own) {
-      v0 += ha * fx;  // B
-      v1 += ha * fy;
-      v2 += ha * fz;
-    }
+    if (bead && sub == 0) fsh[il] = make_float4(fx, fy, fz, 0.f);
+    __syncthreads();
   }
-  if (own) {
-    double *xp = D.x + 3 * (size_t)(gbase + i), *vp = D.v + 3 * (size_t)(gbase + i);
+  if (integ && nsteps > 0) {
+    const float4 f = fsh[threadIdx.x];
+    v0 += ha * f.x;  // the closing B of the last step
+    v1 += ha * f.y;
+    v2 += ha * f.z;
+    double *xp = D.x + 3 * (size_t)(gbase + ib), *vp = D.v + 3 * (size_t)(gbase + ib);
     xp[0] = x0;
     xp[1] = x1;
     xp[2] = x2;
@@ -258,8 +384,17 @@ __global__ void __launch_bounds__(kGoMaxBeads, 1) k_go_segment(GoK K, GoD D, int
     vp[1] = v1;
     vp[2] = v2;
   }
-  double et = go_block_sum(bead ? (double)e : 0.0, red);
-  if (threadIdx.x == 0) D.epot[r] = et;
+  // the chain's potential energy: each CTA's block sum into the slot of its
+  // part in the first CTA of the chain, summed there in part order
+  const double et = go_block_sum(bead ? (double)e : 0.0, red);
+  const int part = (int)go_cluster_rank() - c.peer0;
+  if (threadIdx.x == 0 && live) go_st_peer(go_peer_addr(&epart[part], (uint32_t)c.peer0), et);
+  go_cluster_sync();
+  if (threadIdx.x == 0 && live && part == 0) {
+    double sum = 0.0;
+    for (int q = 0; q < c.npeer; q++) sum += epart[q];
+    D.epot[c.rep] = sum;
+  }
 }
 
 // Advances the step counter by nsteps; when `exchange`, one swap_box attempt
@@ -309,6 +444,9 @@ __global__ void k_go_exchange(GoD D, int nrep, int nsteps, int exchange, uint64_
 
 struct GoBatch {
   int nrep = 0, total = 0, maxN = 0, dev = 0;
+  int ncta = 0;     // CTAs of the launch (a multiple of kGoCluster)
+  int slots = 0;    // CTAs resident at once, as planned for
+  std::vector<int> parts;  // CTAs per replica
   GoK K{};
   GoD D{};
   size_t smem = 0;
@@ -333,18 +471,100 @@ static int go_upload(GoBatch *G, T **dst, const T *src, size_t n) {
   return FE_OK;
 }
 
-// threads per bead: as many as fit the longest chain into 1024 threads (a
-// power of two, at most 8); the block is rounded up to whole warps
-static int go_tpb(int maxN) {
+// threads per bead for a slice of nb beads: as many as fit the CTA (a
+// power of two, at most kGoMaxTpb)
+static int go_tpb(int nb) {
   int t = 1;
-  while (t < 8 && 2 * t * maxN <= kGoMaxBeads) t *= 2;
+  while (t < kGoMaxTpb && 2 * t * nb <= kGoBlock) t *= 2;
   return t;
 }
-static int go_threads(const GoBatch *G) { return ((G->maxN * G->K.tpb + 31) / 32) * 32; }
+
+// The cost of one CTA holding a slice of nb beads of a chain of N: the
+// partners each of its threads walks per step.
+static int go_cost(int N, int parts) {
+  const int nb = (N + parts - 1) / parts;
+  return (N + go_tpb(nb) - 1) / go_tpb(nb);
+}
+
+// Clusters that chains split into `parts` CTAs pack into: a 4-way chain
+// fills one, a 3-way chain takes one with room for a single-CTA chain, 2-way
+// chains pair up or share with single-CTA chains.
+static int go_clusters(const std::vector<int> &parts) {
+  int n[5] = {0, 0, 0, 0, 0};
+  for (int p : parts) n[p]++;
+  const int ones = std::max(0, n[1] - n[3]);
+  return n[4] + n[3] + (2 * n[2] + ones + kGoCluster - 1) / kGoCluster;
+}
+
+// Splits each chain over 1 to 4 CTAs of one cluster: starting from one each,
+// the chain whose CTA has the highest cost takes the fewest more CTAs that
+// lower it, while the clusters needed fit the `slots` CTAs the GPU holds at
+// once; then packs the chains into clusters (no chain crosses a cluster)
+// and pads the last one.
+static std::vector<GoCta> go_plan(const std::vector<int> &nb, int slots) {
+  const int n = (int)nb.size();
+  std::vector<int> parts(n, 1);
+  for (;;) {
+    int r = 0;
+    for (int q = 1; q < n; q++)
+      if (go_cost(nb[q], parts[q]) > go_cost(nb[r], parts[r])) r = q;
+    int P = parts[r] + 1;
+    while (P <= kGoCluster && go_cost(nb[r], P) >= go_cost(nb[r], parts[r])) P++;
+    if (P > kGoCluster) break;
+    std::vector<int> trial = parts;
+    trial[r] = P;
+    if (go_clusters(trial) * kGoCluster > slots) break;
+    parts = trial;
+  }
+  std::vector<GoCta> t;
+  auto add = [&](int r) {
+    const int base = (int)t.size(), P = parts[r];
+    for (int p = 0; p < P; p++) {
+      int lo = (int)((long long)p * nb[r] / P), hi = (int)((long long)(p + 1) * nb[r] / P);
+      t.push_back(GoCta{r, lo, hi - lo, go_tpb(hi - lo), base % kGoCluster, P});
+    }
+  };
+  const GoCta pad{-1, 0, 0, 1, 0, 0};
+  std::vector<int> ones;
+  for (int r = 0; r < n; r++)
+    if (parts[r] == 1) ones.push_back(r);
+  size_t next1 = 0;
+  for (int r = 0; r < n; r++)
+    if (parts[r] == 4) add(r);
+  for (int r = 0; r < n; r++)
+    if (parts[r] == 3) {
+      add(r);
+      if (next1 < ones.size()) add(ones[next1++]);
+      else t.push_back(pad);
+    }
+  for (int r = 0; r < n; r++)
+    if (parts[r] == 2) add(r);
+  for (; next1 < ones.size(); next1++) add(ones[next1]);
+  while (t.size() % kGoCluster) t.push_back(pad);
+  return t;
+}
+
+static int go_launch(GoBatch *G, int nsteps, int mode) {
+  cudaLaunchConfig_t cfg = {};
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kGoCluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.gridDim = dim3((unsigned)G->ncta);
+  cfg.blockDim = dim3(kGoBlock);
+  cfg.dynamicSmemBytes = G->smem;
+  cfg.stream = G->st;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaError_t e = cudaLaunchKernelEx(&cfg, k_go_segment, G->K, G->D, nsteps, mode);
+  if (e != cudaSuccess) return cuda_fail(e, "k_go_segment");
+  return FE_OK;
+}
 
 static int go_launch_segment(GoBatch *G, int nsteps, int exchange) {
-  k_go_segment<<<G->nrep, go_threads(G), G->smem, G->st>>>(G->K, G->D, nsteps, 0);
-  FE_LAUNCH_CHECK("k_go_segment");
+  int rc = go_launch(G, nsteps, 0);
+  if (rc) return rc;
   k_go_exchange<<<1, 256, 0, G->st>>>(G->D, G->nrep, nsteps, exchange, G->seed);
   FE_LAUNCH_CHECK("k_go_exchange");
   return FE_OK;
@@ -413,6 +633,11 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
   K.rc2 = (float)(p->rc_rep * p->rc_rep);
   double sr = p->sigma_rep / p->rc_rep, sr6 = sr * sr * sr * sr * sr * sr;
   K.e_shift = (float)(p->eps * sr6 * sr6);
+  {
+    double s2 = p->sigma_rep * p->sigma_rep, s12 = s2 * s2 * s2 * s2 * s2 * s2;
+    K.c12 = (float)(p->eps * s12);
+    K.f12 = (float)(12.0 * p->eps * s12);
+  }
   K.kb = (float)p->k_bond;
   K.r0b = (float)p->r_bond;
   K.acc_fac = 100.0 / p->mass;
@@ -422,7 +647,7 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
   K.c2 = sqrt(1.0 - K.c1 * K.c1);
   K.min_sep = p->min_sep < 1 ? 1 : p->min_sep;
   K.nrep = nrep;
-  K.tpb = go_tpb(maxN);
+  K.maxN = maxN;
   K.seed = seed;
   int rc = FE_OK;
   std::vector<int> slot(nrep);
@@ -456,12 +681,48 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
     unsigned long long zero = 0;
     if ((rc = go_upload(G, &D.step, &zero, 1))) break;
     if ((rc = go_upload(G, &D.attempt, &zero, 1))) break;
-    G->smem = sizeof(float4) * (size_t)maxN + sizeof(unsigned) * (size_t)maxN * ((maxN + 31) / 32);
+    // two position buffers of the longest chain, and the skip rows of the
+    // largest slice (sized for one CTA per chain, which bounds any split)
+    size_t rowsz = 0;
+    for (int r = 0; r < nrep; r++)
+      rowsz = std::max(rowsz, (size_t)nbeads[r] * ((nbeads[r] + 31) / 32));
+    G->smem = 2 * sizeof(float4) * (size_t)maxN + sizeof(unsigned) * rowsz;
     if (cudaFuncSetAttribute(k_go_segment, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)G->smem) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute");
       break;
     }
+    // CTAs resident at once: whole clusters of this kernel's shape
+    int nsm = 0, nclu = 0;
+    if (cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, G->dev) != cudaSuccess) {
+      rc = cuda_fail(cudaGetLastError(), "cudaDeviceGetAttribute");
+      break;
+    }
+    {
+      cudaLaunchConfig_t cfg = {};
+      cudaLaunchAttribute at[1];
+      at[0].id = cudaLaunchAttributeClusterDimension;
+      at[0].val.clusterDim.x = kGoCluster;
+      at[0].val.clusterDim.y = 1;
+      at[0].val.clusterDim.z = 1;
+      cfg.gridDim = dim3((unsigned)(kGoCluster * ((nsm + kGoCluster - 1) / kGoCluster)));
+      cfg.blockDim = dim3(kGoBlock);
+      cfg.dynamicSmemBytes = G->smem;
+      cfg.attrs = at;
+      cfg.numAttrs = 1;
+      if (cudaOccupancyMaxActiveClusters(&nclu, k_go_segment, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        nclu = nsm / kGoCluster;
+      }
+    }
+    std::vector<int> nbv(nbeads, nbeads + nrep);
+    G->slots = std::max(1, std::min(nclu, nsm / kGoCluster)) * kGoCluster;
+    std::vector<GoCta> plan = go_plan(nbv, G->slots);
+    G->ncta = (int)plan.size();
+    G->parts.assign(nrep, 0);
+    for (const GoCta &c : plan)
+      if (c.rep >= 0 && c.lo == 0) G->parts[c.rep] = c.npeer;
+    if ((rc = go_upload(G, (GoCta **)&D.cta, plan.data(), plan.size()))) break;
   } while (0);
   if (rc) {
     go_free(G);
@@ -512,8 +773,8 @@ int fe_go_run(fe_go *h, int64_t nsteps, int swap_freq) {
 int fe_go_forces(fe_go *h, double *f, double *epot) {
   if (!h) return FE_ERR_ARG;
   GoBatch *G = &h->G;
-  k_go_segment<<<G->nrep, go_threads(G), G->smem, G->st>>>(G->K, G->D, 0, 1);
-  FE_LAUNCH_CHECK("k_go_segment");
+  int rc = go_launch(G, 0, 1);
+  if (rc) return rc;
   FE_CUDA(cudaStreamSynchronize(G->st));
   if (f) {
     std::vector<float> t(3 * (size_t)G->total);
@@ -541,6 +802,16 @@ int fe_go_state(fe_go *h, double *pos, double *vel, double *T, double *epot, int
   if (attempted)
     FE_CUDA(cudaMemcpy(attempted, G->D.att, sizeof(long long) * G->nrep, cudaMemcpyDeviceToHost));
   if (steps) FE_CUDA(cudaMemcpy(steps, G->D.step, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  return FE_OK;
+}
+
+int fe_go_layout(fe_go *h, int *ncta, int *slots, int *parts) {
+  if (!h) return FE_ERR_ARG;
+  const GoBatch *G = &h->G;
+  if (ncta) *ncta = G->ncta;
+  if (slots) *slots = G->slots;
+  if (parts)
+    for (int r = 0; r < G->nrep; r++) parts[r] = G->parts[r];
   return FE_OK;
 }
 

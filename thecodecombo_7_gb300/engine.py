@@ -55,7 +55,7 @@ EXPORTS = [
     "fe_mc_chains_collect", "fe_mc_chains_samples", "fe_mc_chains_train_surrogate",
     "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
-    "fe_go_get_stream", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
+    "fe_go_get_stream", "fe_go_layout", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
     "fe_mc_delta_terms", "fe_mc_site_energy", "fe_drift", "fe_box_set_temperature",
     "fe_bspline", "fe_batch_set_fused", "fe_set_ureys", "fe_set_torsions", "fe_set_impropers",
     "fe_get_torsion_angles", "fe_bonded_ext",
@@ -763,3 +763,11 @@ class GoBatch:
         s = C.c_void_p()
         self._check(self.lib.fe_go_get_stream(self.h, C.byref(s)))
         return s.value or 0
+
+    def layout(self):
+        """The launch's load-balance plan: CTAs launched, CTAs resident at
+        once, and the CTAs that share each replica's chain."""
+        ncta, slots = C.c_int(), C.c_int()
+        parts = np.empty(len(self.g.nbeads), np.int32)
+        self._check(self.lib.fe_go_layout(self.h, C.byref(ncta), C.byref(slots), _p(parts)))
+        return dict(ncta=ncta.value, slots=slots.value, parts=parts)

@@ -5,6 +5,7 @@ is asked for).
     python -m thecodecombo_7_gb300.workloads [--molecules 32000] [--precision mixed]
         [--steps 30] [--warmup 10] [--switch 8.0]
     python -m thecodecombo_7_gb300.workloads --batch [--replicas 32] [--unfused]
+    python -m thecodecombo_7_gb300.workloads --go [--replicas 64] [--steps 1000]
 
 With --profile-range the timed steps alone are bracketed by
 cudaProfilerStart/Stop, so `ncu --profile-from-start off` lists the launches
@@ -64,6 +65,38 @@ def batch_main(a):
     print(json.dumps(out))
 
 
+def go_main(a):
+    """Go-model replica exchange: 64 chains of 60-400 beads (the bench's Go
+    leg), one persistent launch per exchange segment of --steps steps; times
+    --warmup segments untimed and then 5 segments; prints one JSON line."""
+    import torch
+    g = systems.go_chains(a.replicas, seed=a.seed)
+    b = engine.GoBatch(g, seed=a.seed)
+    try:
+        b.run(a.warmup * a.steps, swap_freq=a.steps)
+        st = torch.cuda.ExternalStream(b.stream())
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        if a.profile_range:
+            torch.cuda.profiler.start()
+        e0.record(st)
+        b.run(5 * a.steps, swap_freq=a.steps)
+        e1.record(st)
+        if a.profile_range:
+            torch.cuda.profiler.stop()
+        torch.cuda.synchronize()
+        us = 1e3 * e0.elapsed_time(e1) / (5 * a.steps)
+        lay = b.layout()
+    finally:
+        b.close()
+    nb = int(g.nbeads.sum())
+    print(json.dumps({"replicas": a.replicas, "beads": nb, "us_per_step": us,
+                      "bead_steps_per_s": nb / (us * 1e-6), "ctas": lay["ncta"],
+                      "resident_ctas": lay["slots"],
+                      "chains_by_ctas": {str(k): int((lay["parts"] == k).sum())
+                                         for k in (1, 2, 3, 4)}}))
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
     ap.add_argument("--molecules", type=int, default=32000)
@@ -74,12 +107,19 @@ def main(argv=None):
     ap.add_argument("--seed", type=int, default=2025)
     ap.add_argument("--batch", action="store_true",
                     help="the 32-replica uneven batch instead of one box")
-    ap.add_argument("--replicas", type=int, default=32)
+    ap.add_argument("--go", action="store_true",
+                    help="the Go-model replica exchange instead of water")
+    ap.add_argument("--replicas", type=int, default=None,
+                    help="batch: 32 boxes; go: 64 chains")
     ap.add_argument("--unfused", action="store_true", help="batch: box by box")
     ap.add_argument("--profile-range", action="store_true",
                     help="bracket the timed steps with cudaProfilerStart/Stop")
     a = ap.parse_args(argv)
+    if a.go:
+        a.replicas = a.replicas or 64
+        return go_main(a)
     if a.batch:
+        a.replicas = a.replicas or 32
         return batch_main(a)
     import torch
     s = systems.water_box(a.molecules, density=0.1, seed=a.seed, r_switch=a.switch)
