@@ -202,6 +202,22 @@ int fe_kinet(fe_box *box, double *ken6, double *kinet);
 int fe_integrate_vverlet(fe_box *box, double vscal, double *en);
 /* integrate_nhc(time_step, ibox), integrate_nhc.c:40-161 (Nc = Nys = 1) */
 int fe_integrate_nhc(fe_box *box, double time_step);
+/* RESPA multiple time stepping (FP64 boxes; FE_ERR_STATE for mixed):
+ * force_short(ibox), force_short.c:46-137: cbond + cbend + curey into
+ * ff_short (ff holds them after the call, en's bond/bend/urey updated). */
+int fe_force_short(fe_box *box, double *en);
+/* force_long(ibox), force_long.c:46-145: ctorsion + cimproper + cnonbondnl
+ * (with SPME) into ff and ff_long; en's other terms updated. */
+int fe_force_long(fe_box *box, double *en);
+/* integrate_mts(ibox, vscal), integrate_mts.c:37-140: one long step of
+ * nshort short steps (sim.nsteps; the long step dt * nshort, init.c:314),
+ * pbc_all and both force classes inside; uu = vv after; `en` may be NULL.
+ * ff_short and ff_long start at zero as the reference's arrays do: call
+ * fe_force_short and fe_force_long first (nve_md.c:298-304). */
+int fe_integrate_mts(fe_box *box, double vscal, int nshort, double *en);
+/* The ff_short / ff_long arrays (either pointer may be NULL). */
+int fe_get_forces_mts(fe_box *box, double *ff_short, double *ff_long);
+int fe_set_forces_mts(fe_box *box, const double *ff_short, const double *ff_long);
 /* drift(ibox), drift.c:21-66: removes the net momentum from the velocities
  * (v_i -= (sum_j m_j v_j / n) / m_i); uu is left as it is. */
 int fe_drift(fe_box *box);

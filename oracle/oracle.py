@@ -413,14 +413,17 @@ def read_tagged(path):
     return out
 
 
-def run_reference(mode, sysm, workdir, nsteps=None, fast=False):
-    """Run the reference's own routines (oracle/_ref) on sysm."""
+def run_reference(mode, sysm, workdir, nsteps=None, fast=False, extra=()):
+    """Run the reference's own routines (oracle/_ref) on sysm; `extra` are
+    further integer arguments of the mode (mts: the short steps per long
+    step)."""
     binp = REF_BIN_FAST if fast else REF_BIN
     os.makedirs(workdir, exist_ok=True)
     sp = os.path.join(workdir, "system.bin")
     op = os.path.join(workdir, f"out_{mode}.bin")
     write_system_file(sp, sysm)
     cmd = [binp, mode, sp, op] + ([str(nsteps)] if nsteps is not None else [])
+    cmd += [str(x) for x in extra]
     subprocess.check_call(cmd)
     return read_tagged(op)
 

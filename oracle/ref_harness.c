@@ -22,6 +22,10 @@
  *   mode nve    : nsteps of NVE velocity Verlet (list rebuilt every nlist)
  *   mode nhc    : nsteps of NHC-VV (integrate_nhc / integrate_vverlet / integrate_nhc)
  *   mode drift  : drift() (drift.c:21) on the input velocities
+ *   mode mts    : nsteps long steps of RESPA (integrate_mts.c:37) with
+ *                 nshort short steps each (argv[5]; init.c:314 sets
+ *                 dtlong = dt * nshort); force_short / force_long /
+ *                 forces / kinet before the loop as nve_md.c:298-304 does
  *   mode nlcheck (the -DDLIST build, ref_harness_dlist): nblist, then per
  *                 case of <cases.bin> (the 4th argument) the snapshot
  *                 positions plus the case's displacements, pbc_all, and
@@ -53,6 +57,9 @@ void charge_grid(int);
 void pme_calc(int, double *);
 void cnonbondnl(int, double *);
 void integrate_vverlet(int, double);
+void integrate_mts(int, double);
+void force_short(int);
+void force_long(int);
 void integrate_nhc(double, int);
 void kinet(int);
 void pbc_all(int);
@@ -268,6 +275,10 @@ static void alloc_state(void) {
   vv = calloc(1, sizeof(struct veloc *));
   uu = calloc(1, sizeof(struct veloc *));
   ff[k] = calloc(N, sizeof(struct veloc));
+  ff_short = calloc(1, sizeof(struct veloc *));
+  ff_long = calloc(1, sizeof(struct veloc *));
+  ff_short[k] = calloc(N, sizeof(struct veloc));
+  ff_long[k] = calloc(N, sizeof(struct veloc));
   vv[k] = calloc(N, sizeof(struct veloc));
   uu[k] = calloc(N, sizeof(struct veloc));
   for (int i = 0; i < N; i++) {
@@ -559,6 +570,35 @@ int main(int argc, char **argv) {
       }
       dump_d("zeta", z, 3 * (int64_t)M);
     }
+    free(rec);
+  } else if (strcmp(mode, "mts") == 0) {
+    int nsteps = argc > 4 ? atoi(argv[4]) : 6;
+    sim.nsteps = argc > 5 ? atoi(argv[5]) : 4;
+    sim.dtlong = sim.dt * sim.nsteps; /* init.c:314 */
+    nblist(k);
+    force_short(k); /* nve_md.c:298-304 */
+    force_long(k);
+    forces(k);
+    kinet(k);
+    double *rec = malloc(sizeof(double) * 15 * (size_t)(nsteps + 1));
+    en_record(rec);
+    rec[12] = en[k].urey; rec[13] = en[k].tors; rec[14] = en[k].impr;
+    for (int i = 1; i <= nsteps; i++) {
+      if (i % sim.nlist == 0) nblist(k);
+      integrate_mts(k, 1.0); /* nve_md.c:412 */
+      kinet(k);
+      en_record(rec + 15 * i);
+      rec[15 * i + 12] = en[k].urey; rec[15 * i + 13] = en[k].tors;
+      rec[15 * i + 14] = en[k].impr;
+    }
+    dump_d("en_steps", rec, 15 * (int64_t)(nsteps + 1));
+    dump_pos("pos", atom[k]);
+    dump_pos("pos_nopbc", atnopbc[k]);
+    dump_xyz("vel", vv[k]);
+    dump_xyz("vel_uu", uu[k]);
+    dump_xyz("force", ff[k]);
+    dump_xyz("f_short", ff_short[k]);
+    dump_xyz("f_long", ff_long[k]);
     free(rec);
 #ifdef DLIST
   } else if (strcmp(mode, "nlcheck") == 0) {

@@ -35,6 +35,12 @@ def golden_mc():
 
 
 @pytest.fixture(scope="session")
+def golden_mts600():
+    import numpy as np
+    return dict(np.load(os.path.join(GOLDEN, "mts_water600.npz")))
+
+
+@pytest.fixture(scope="session")
 def golden_chain():
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, "chain900.npz")))

@@ -101,6 +101,7 @@ def main():
     make_mc(tmp)
     make_drift(tmp)
     make_chain(tmp)
+    make_mts_water(tmp)
     print("golden fixtures written to", HERE)
 
 
@@ -169,7 +170,11 @@ def make_chain(tmp):
     s.nlist_freq = 5
     fo = O.run_reference("forces", s, tmp)
     nve = O.run_reference("nve", s, tmp, nsteps=12)
+    # RESPA (integrate_mts.c): 6 long steps of 4 short steps
+    mts = O.run_reference("mts", s, tmp, nsteps=6, extra=(4,))
     out = sys_arrays(s)
+    for k, v in mts.items():
+        out["mts_" + k] = v
     for k in CHAIN_KEYS:
         out["top_" + k] = getattr(s, k)
     for k, v in fo.items():
@@ -177,6 +182,17 @@ def make_chain(tmp):
     for k, v in nve.items():
         out["nve_" + k] = v
     np.savez_compressed(os.path.join(HERE, "chain900.npz"), **out)
+
+
+def make_mts_water(tmp):
+    """RESPA on the 600-site water box: 8 long steps of 4 short steps."""
+    s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27))
+    s.nlist_freq = 5
+    r = O.run_reference("mts", s, tmp, nsteps=8, extra=(4,))
+    out = sys_arrays(s)
+    for k, v in r.items():
+        out["mts_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "mts_water600.npz"), **out)
 
 
 def make_drift(tmp):
@@ -199,11 +215,11 @@ def make_nlcheck(tmp):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"]):  # this fixture alone
+    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"], ["mts"]):  # this fixture alone
         if not O.build_reference():
             raise SystemExit("reference sources not available")
         {"nlcheck": make_nlcheck, "mc": make_mc, "drift": make_drift,
-         "chain": make_chain}[sys.argv[1]](
+         "chain": make_chain, "mts": make_mts_water}[sys.argv[1]](
             tempfile.mkdtemp(prefix="fe_golden_"))
     else:
         main()

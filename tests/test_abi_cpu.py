@@ -129,7 +129,8 @@ def test_reference_program_links_against_the_engine(lib):
     forms = {
         "md": ("nblist", "forces", "cnonbondnl", "pme_calc", "charge_grid", "pme_init",
                "pme_clean", "fillspline", "integrate_vverlet", "integrate_nhc", "pbc_all",
-               "kinet", "drift", "isokin", "swap_box"),
+               "kinet", "drift", "isokin", "swap_box", "force_short", "force_long",
+               "integrate_mts"),
         "mc": ("forces_mc", "enbnd_mc", "ewald_kspace_mc", "ewald_rspace_mc", "nblist_pivot",
                "drift"),
     }
@@ -144,6 +145,7 @@ def test_reference_program_links_against_the_engine(lib):
     need_md = subprocess.run(["nm", "-u", os.path.join(out, "md", "fe_dropin.o")],
                              capture_output=True, text=True).stdout
     assert "fe_forces" in need_md and "fe_drift" in need_md and "fe_bspline" in need_md
+    assert "fe_integrate_mts" in need_md and "fe_set_forces_mts" in need_md
     need_mc = subprocess.run(["nm", "-u", os.path.join(out, "mc", "fe_dropin.o")],
                              capture_output=True, text=True).stdout
     assert "fe_mc_delta_terms" in need_mc and "fe_mc_site_energy" in need_mc

@@ -149,3 +149,17 @@ def test_oracle_chain_terms_bit_exact(golden_chain):
     ref_en = dict(zip(O.EN_KEYS, g["forces_en"]))
     for k in ("nbond", "nbonds", "coulomb", "rewald", "rewalds", "kewald", "sewald", "iewald"):
         assert en[k] == ref_en[k], k
+
+
+def test_respa_fixtures_semantics(golden_chain, golden_mts600):
+    """The reference's RESPA runs (integrate_mts.c) as committed: ff ends as
+    force_long's forces (ff_long = ff, force_long.c:139-143), uu = vv after
+    the last kick (integrate_mts.c:133-135), and the water box's total energy
+    stays within 1 % over 8 long steps of 2 fs."""
+    for g, nlong in ((golden_chain, 6), (golden_mts600, 8)):
+        assert np.array_equal(g["mts_force"], g["mts_f_long"])
+        assert np.array_equal(g["mts_vel"], g["mts_vel_uu"])
+        assert g["mts_en_steps"].shape == (15 * (nlong + 1),)
+    e = golden_mts600["mts_en_steps"].reshape(-1, 15)
+    tot = e[:, 0] + e[:, 1] + e[:, 2] + e[:, 3] + e[:, 12] + e[:, 13] + e[:, 14]
+    assert np.abs(tot - tot[0]).max() < 0.01 * abs(tot[0])

@@ -36,6 +36,7 @@ UNITS = {
     "k_spme.cu": ["-fmad=false"],
     "k_integrate.cu": ["-fmad=false"],
     "k_integrate_mx.cu": [],
+    "k_respa.cu": ["-fmad=false"],
     "k_mc.cu": ["-fmad=false"],
     "k_mixed.cu": ["-ftz=true"],
     "k_noalloc.cu": [],

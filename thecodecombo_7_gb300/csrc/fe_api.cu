@@ -101,7 +101,7 @@ static void free_box(Box *b) {
                   b->kweight, b->grid, b->grid_k, b->spl_floor, b->spl_m, b->spl_d, b->fp,
                   b->gbin_count, b->gbin_atoms, b->partials, b->scal, b->status, b->ticket, b->facc, b->xyz_dev, b->zeta, b->rec,
                   b->rec_counter, b->urey_ab, b->urey_seq, b->urey_k, b->tors_abcd, b->tors_par,
-                  b->tors_tau, b->impr_abcd, b->impr_k, b->impr_eq};
+                  b->tors_tau, b->impr_abcd, b->impr_k, b->impr_eq, b->ff_short, b->ff_long};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   mc_free(b);
@@ -795,6 +795,87 @@ int fe_integrate_vverlet(fe_box *box, double vscal, double *en) {
   if ((rc = sync_scal(b))) return rc;
   if (en)
     for (int i = 0; i < FE_EN_COUNT; i++) en[i] = b->host_scal[i];
+  return FE_OK;
+}
+
+// RESPA runs on the FP64 drop-in: the mixed path folds the bonded terms and
+// the exclusion corrections into one fixed-point pass
+static int respa_check(Box *b, const char *what) {
+  if (b->mx) {
+    set_error(std::string(what) + ": RESPA runs on the FP64 engine (FE_PREC_FP64)");
+    return FE_ERR_STATE;
+  }
+  if (!b->have_list) {
+    set_error(std::string(what) + " requested before a neighbour list was built");
+    return FE_ERR_STATE;
+  }
+  return FE_OK;
+}
+
+static void copy_en(const Box *b, double *en) {
+  if (en)
+    for (int i = 0; i < FE_EN_COUNT; i++) en[i] = b->host_scal[i];
+}
+
+int fe_force_short(fe_box *box, double *en) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc;
+  if ((rc = respa_check(b, "fe_force_short"))) return rc;
+  if ((rc = respa_force_short(b))) return rc;
+  // force_short.c leaves ff holding the fast forces
+  FE_CUDA(cudaMemcpyAsync(b->ff, b->ff_short, sizeof(double) * 3 * (size_t)b->n,
+                          cudaMemcpyDeviceToDevice, b->stream));
+  if ((rc = launch_assemble_energies(b, 1))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  copy_en(b, en);
+  return FE_OK;
+}
+
+int fe_force_long(fe_box *box, double *en) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc;
+  if ((rc = respa_check(b, "fe_force_long"))) return rc;
+  if ((rc = respa_force_long(b))) return rc;
+  if ((rc = launch_assemble_energies(b, 1))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  copy_en(b, en);
+  return FE_OK;
+}
+
+int fe_integrate_mts(fe_box *box, double vscal, int nshort, double *en) {
+  if (!box || nshort < 1) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc;
+  if ((rc = respa_check(b, "fe_integrate_mts"))) return rc;
+  if ((rc = respa_step(b, vscal, nshort))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  copy_en(b, en);
+  return FE_OK;
+}
+
+int fe_get_forces_mts(fe_box *box, double *ff_short, double *ff_long) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = respa_alloc(b);
+  if (rc) return rc;
+  const size_t bytes = sizeof(double) * 3 * (size_t)b->n;
+  if (ff_short) FE_CUDA(cudaMemcpyAsync(ff_short, b->ff_short, bytes, cudaMemcpyDeviceToHost, b->stream));
+  if (ff_long) FE_CUDA(cudaMemcpyAsync(ff_long, b->ff_long, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+int fe_set_forces_mts(fe_box *box, const double *ff_short, const double *ff_long) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc = respa_alloc(b);
+  if (rc) return rc;
+  const size_t bytes = sizeof(double) * 3 * (size_t)b->n;
+  if (ff_short) FE_CUDA(cudaMemcpyAsync(b->ff_short, ff_short, bytes, cudaMemcpyHostToDevice, b->stream));
+  if (ff_long) FE_CUDA(cudaMemcpyAsync(b->ff_long, ff_long, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaStreamSynchronize(b->stream));
   return FE_OK;
 }
 

@@ -55,7 +55,8 @@ enum : int {
   SC_MX_EXCL = SC_MX_PAIR + 4,     // 5 slots: mixed exclusion sums (.., intra)
   SC_TEMP = SC_MX_EXCL + 5,        // thermostat temperature [K] (sim.T[k]); exchanges rewrite it
   SC_MX_INTRA,                     // 7 slots: fused intramolecular sums (5 exclusion, bond, bend)
-  SC_COUNT = SC_MX_INTRA + 7
+  SC_EXT_TMP = SC_MX_INTRA + 7,    // 3 slots: curey/ctorsion/cimproper sums of a subset of the kinds
+  SC_COUNT = SC_EXT_TMP + 3
 };
 
 // Largest number of blocks a partial-sum kernel may use.
@@ -77,6 +78,7 @@ struct Box {
   double4 *pos_list0 = nullptr; // n: wrapped positions at the last list build (nl_check)
   int *nl_dev = nullptr;        // 1: nl_check's flag
   double *vv = nullptr, *uu = nullptr, *ff = nullptr;  // 3n, struct veloc layout
+  double *ff_short = nullptr, *ff_long = nullptr;      // 3n each, RESPA's fast and slow forces
   double *mass = nullptr;
   double *imass100 = nullptr;  // 100 / mass (integrate_vverlet.c:56), one division at setup
   int *type = nullptr;
@@ -225,7 +227,12 @@ int pair_counts64(Box *b, long long *out4);  // instrumentation: half-list count
 int launch_bonded64(Box *b);
 // Urey-Bradley, torsions, impropers: into ff (FP64 atomics) or the mixed
 // path's fixed-point sums (to_fixed); energies to SC_UREY..SC_IMPR
-int launch_bonded_ext(Box *b, bool to_fixed);
+int launch_bonded_ext(Box *b, bool to_fixed, int kinds = 7);  // kinds: 1 urey, 2 torsion, 4 improper
+// k_respa.cu (FP64 drop-in): force_short.c, force_long.c, integrate_mts.c
+int respa_alloc(Box *b);
+int respa_force_short(Box *b);
+int respa_force_long(Box *b);
+int respa_step(Box *b, double vscal, int nshort);
 // k_spme.cu
 int spme_setup(Box *b);
 int launch_charge_grid64(Box *b);

@@ -48,6 +48,11 @@ struct ExtArgs {
   double *tors_tau;
   const int *impr_abcd;
   const double *impr_k, *impr_eq;
+  // the terms evaluated: [t0, t1) of urey, then torsion, then improper
+  // order; `kinds` (bit 0 urey, 1 torsion, 2 improper) are the energies
+  // written to fin[0..2] when not all three are evaluated
+  int t0, t1, kinds;
+  double *fin;
 };
 
 // the dihedral (a, b, c, d) and its generalised force fr = -dE/dtau applied
@@ -126,8 +131,8 @@ k_bonded_ext(ExtArgs a, const double4 *__restrict__ pos, double *__restrict__ ff
              unsigned long long *__restrict__ fix, unsigned long long *__restrict__ facc,
              unsigned *__restrict__ ticket, double *__restrict__ out) {
   double e[3] = {0.0, 0.0, 0.0};  // urey, torsion, improper
-  const int tot = a.nurey + a.ntors + a.nimpr;
-  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < tot; t += gridDim.x * blockDim.x) {
+  for (int t = a.t0 + blockIdx.x * blockDim.x + threadIdx.x; t < a.t1;
+       t += gridDim.x * blockDim.x) {
     if (t < a.nurey) {
       int ia = a.urey_ab[2 * t], ib = a.urey_ab[2 * t + 1];
       double4 A = pos[ia], B = pos[ib];
@@ -171,13 +176,25 @@ k_bonded_ext(ExtArgs a, const double4 *__restrict__ pos, double *__restrict__ ff
       dihedral_force<FIXED>(D, fr, q[0], q[1], q[2], q[3], ff, fix);
     }
   }
-  block_fix_final<3>(e, 32, facc, ticket, out);
+  const bool last = block_fix_final<3>(e, 32, facc, ticket, out);
+  // a subset of the kinds: only their energies leave the scratch slots
+  if (last && a.kinds != 7 && threadIdx.x < 3 && ((a.kinds >> threadIdx.x) & 1))
+    a.fin[threadIdx.x] = out[threadIdx.x];
 }
 
-int launch_bonded_ext(Box *b, bool to_fixed) {
+int launch_bonded_ext(Box *b, bool to_fixed, int kinds) {
   const int tot = b->nurey + b->ntors + b->nimpr;
-  if (tot == 0) return FE_OK;
   ExtArgs a;
+  a.t0 = (kinds & 1) ? 0 : (kinds & 2) ? b->nurey : b->nurey + b->ntors;
+  a.t1 = (kinds & 4) ? tot : (kinds & 2) ? b->nurey + b->ntors : b->nurey;
+  a.kinds = kinds;
+  a.fin = b->scal + SC_UREY;
+  if (tot == 0) return FE_OK;
+  if (a.t1 <= a.t0) {  // none of these kinds: their energies are zero
+    for (int k = 0; k < 3; k++)
+      if ((kinds >> k) & 1) FE_CUDA(cudaMemsetAsync(b->scal + SC_UREY + k, 0, sizeof(double), b->stream));
+    return FE_OK;
+  }
   a.L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   a.H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);
   a.nurey = b->nurey;
@@ -192,7 +209,7 @@ int launch_bonded_ext(Box *b, bool to_fixed) {
   a.impr_abcd = b->impr_abcd;
   a.impr_k = b->impr_k;
   a.impr_eq = b->impr_eq;
-  int blocks = (tot + 255) / 256;
+  int blocks = (a.t1 - a.t0 + 255) / 256;
   if (blocks > 1024) blocks = 1024;
   if (to_fixed) {
     if (!b->mx) {
@@ -202,8 +219,9 @@ int launch_bonded_ext(Box *b, bool to_fixed) {
     k_bonded_ext<true><<<blocks, 256, 0, b->stream>>>(a, b->pos_q, nullptr, b->mx->fix, b->facc,
                                                       b->ticket, b->scal + SC_UREY);
   } else {
-    k_bonded_ext<false><<<blocks, 256, 0, b->stream>>>(a, b->pos_q, b->ff, nullptr, b->facc,
-                                                       b->ticket, b->scal + SC_UREY);
+    k_bonded_ext<false><<<blocks, 256, 0, b->stream>>>(
+        a, b->pos_q, b->ff, nullptr, b->facc, b->ticket,
+        b->scal + (kinds == 7 ? SC_UREY : SC_EXT_TMP));
   }
   FE_LAUNCH_CHECK("k_bonded_ext");
   return FE_OK;

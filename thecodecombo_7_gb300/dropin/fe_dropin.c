@@ -7,7 +7,8 @@
  *   MD form (-DNLIST -DEWALD -DSPME -DSTYPE): replaces nblist.c,
  *     cnonbond_nblist.c, pme_qgrid.c, pme_calc.c, pme_setup.c, pme_spline.c,
  *     integrate_vverlet.c, integrate_nhc.c, pbc_all.c, kinet.c, forces.c,
- *     drift.c, isokin.c and swap_box.c.
+ *     drift.c, isokin.c, swap_box.c and, for RESPA (sim.ID2 == 3, FP64
+ *     engine), integrate_mts.c, force_short.c and force_long.c.
  *   MC form (-DNLIST -DEWALD -DMC -DSTYPE, classic Ewald, no SPME): replaces
  *     forces_mc.c, enbnd_mc.c, ewald_mc.c, nblist_pivot.c, drift.c.
  *
@@ -457,6 +458,63 @@ void integrate_vverlet(int ibox, double vscal) {
   get_atoms(b, ibox, 1);
   FE_OR_DIE(fe_get_velocities(b, &vv[ibox][0].x, &uu[ibox][0].x), "integrate_vverlet");
   FE_OR_DIE(fe_get_forces(b, &ff[ibox][0].x), "integrate_vverlet");
+  put_energies(ibox, e);
+}
+
+/* force_short.c:46: bonds, bends, Urey-Bradley into ff and ff_short;
+ * en[k].bond / bend / urey */
+void force_short(int ibox) {
+  fe_box *b = fe_of(ibox);
+  double e[FE_EN_COUNT];
+  put_atoms(b, ibox, 0);
+  FE_OR_DIE(fe_force_short(b, e), "force_short");
+  FE_OR_DIE(fe_get_forces(b, &ff[ibox][0].x), "force_short");
+  FE_OR_DIE(fe_get_forces_mts(b, &ff_short[ibox][0].x, NULL), "force_short");
+  g_ok[ibox].ff = 1;
+  en[ibox].bond = e[FE_EN_BOND];
+  en[ibox].bend = e[FE_EN_BEND];
+#ifndef NEUTRAL
+  en[ibox].urey = e[FE_EN_UREY];
+#endif
+}
+
+/* force_long.c:46: torsions, impropers and cnonbondnl into ff and ff_long;
+ * the other en[k] terms as force_long.c:94-116 sets them */
+void force_long(int ibox) {
+  fe_box *b = fe_of(ibox);
+  double e[FE_EN_COUNT];
+  put_atoms(b, ibox, 0);
+  FE_OR_DIE(fe_force_long(b, e), "force_long");
+  FE_OR_DIE(fe_get_forces(b, &ff[ibox][0].x), "force_long");
+  FE_OR_DIE(fe_get_forces_mts(b, NULL, &ff_long[ibox][0].x), "force_long");
+  g_ok[ibox].ff = 1;
+  double bond = en[ibox].bond, bend = en[ibox].bend;
+#ifndef NEUTRAL
+  double ur = en[ibox].urey;
+#endif
+  put_energies(ibox, e);
+  en[ibox].bond = bond;
+  en[ibox].bend = bend;
+#ifndef NEUTRAL
+  en[ibox].urey = ur;
+#endif
+}
+
+/* integrate_mts.c:37: one RESPA long step of sim.nsteps short steps
+ * (dtlong = dt * nsteps, init.c:314); reads atom, atnopbc, vv, ff_short and
+ * ff_long, writes them back with uu, ff and the energies of both classes */
+void integrate_mts(int ibox, double vscal) {
+  fe_box *b = fe_of(ibox);
+  double e[FE_EN_COUNT];
+  put_atoms(b, ibox, 1);
+  put_vel(b, ibox);
+  FE_OR_DIE(fe_set_forces_mts(b, &ff_short[ibox][0].x, &ff_long[ibox][0].x), "integrate_mts");
+  FE_OR_DIE(fe_integrate_mts(b, vscal, sim.nsteps, e), "integrate_mts");
+  get_atoms(b, ibox, 1);
+  FE_OR_DIE(fe_get_velocities(b, &vv[ibox][0].x, &uu[ibox][0].x), "integrate_mts");
+  FE_OR_DIE(fe_get_forces(b, &ff[ibox][0].x), "integrate_mts");
+  FE_OR_DIE(fe_get_forces_mts(b, &ff_short[ibox][0].x, &ff_long[ibox][0].x), "integrate_mts");
+  g_ok[ibox].ff = 1;
   put_energies(ibox, e);
 }
 

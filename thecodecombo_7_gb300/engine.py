@@ -43,6 +43,8 @@ EXPORTS = [
     "fe_get_nhc_state", "fe_nblist", "fe_nblist_download", "fe_forces", "fe_cnonbondnl",
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
+    "fe_force_short", "fe_force_long", "fe_integrate_mts", "fe_get_forces_mts",
+    "fe_set_forces_mts",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats", "fe_nl_check",
     "fe_ewald_kspace_energy_noalloc",
@@ -379,6 +381,32 @@ class Box:
         en = np.empty(FE_EN_COUNT)
         self._check(self.lib.fe_integrate_vverlet(self.h, C.c_double(vscal), _p(en)))
         return dict(zip(EN_KEYS, en.tolist()))
+
+    def force_short(self):
+        """force_short.c: bonds, bends and Urey-Bradley terms into ff_short
+        (and ff); returns the energies."""
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_force_short(self.h, _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
+
+    def force_long(self):
+        """force_long.c: torsions, impropers and the non-bonded terms with
+        SPME into ff_long (and ff); returns the energies."""
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_force_long(self.h, _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
+
+    def integrate_mts(self, nshort, vscal=1.0):
+        """integrate_mts.c: one RESPA long step of `nshort` short steps."""
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_integrate_mts(self.h, C.c_double(vscal), int(nshort), _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
+
+    def forces_mts(self):
+        """(ff_short, ff_long) as two (n, 3) arrays."""
+        fs, fl = np.empty((self.n, 3)), np.empty((self.n, 3))
+        self._check(self.lib.fe_get_forces_mts(self.h, _p(fs), _p(fl)))
+        return fs, fl
 
     def integrate_nhc(self, time_step=None):
         ts = self.sysm.dt if time_step is None else time_step
