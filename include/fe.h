@@ -215,6 +215,12 @@ int fe_force_long(fe_box *box, double *en);
  * ff_short and ff_long start at zero as the reference's arrays do: call
  * fe_force_short and fe_force_long first (nve_md.c:298-304). */
 int fe_integrate_mts(fe_box *box, double vscal, int nshort, double *en);
+/* integrate_mts_nhc(ibox, vscal), integrate_mts_nhc.c:37-162: RESPA with
+ * the Nose-Hoover chain of fe_integrate_nhc applied over half a long step at
+ * both ends of the long step (xrespa = sim.xRESPA = 0) or over half a short
+ * step at both ends of every short step (xrespa = 1); the kicks carry no
+ * vscal, as there. */
+int fe_integrate_mts_nhc(fe_box *box, int nshort, int xrespa, double *en);
 /* The ff_short / ff_long arrays (either pointer may be NULL). */
 int fe_get_forces_mts(fe_box *box, double *ff_short, double *ff_long);
 int fe_set_forces_mts(fe_box *box, const double *ff_short, const double *ff_long);

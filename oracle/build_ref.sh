@@ -23,7 +23,7 @@ fi
 mkdir -p "$OUT"
 SRCS="nblist cnonbond_nblist pme_qgrid pme_spline pme_setup pme_calc forces
       cbond cbend curey ctorsion cimproper integrate_vverlet pbc_all kinet
-      integrate_nhc setlj ewald drift integrate_mts force_short force_long"
+      integrate_nhc setlj ewald drift integrate_mts integrate_mts_nhc force_short force_long"
 FEAT="-DNLIST -DEWALD -DSPME -DSTYPE"
 build() {
   name=$1; shift

@@ -22,6 +22,9 @@
  *   mode nve    : nsteps of NVE velocity Verlet (list rebuilt every nlist)
  *   mode nhc    : nsteps of NHC-VV (integrate_nhc / integrate_vverlet / integrate_nhc)
  *   mode drift  : drift() (drift.c:21) on the input velocities
+ *   mode mtsnhc : as mts with integrate_mts_nhc.c:37 (nvt_md.c:552) and
+ *                 sim.xRESPA = argv[6] (0: thermostat per long step, 1:
+ *                 per short step)
  *   mode mts    : nsteps long steps of RESPA (integrate_mts.c:37) with
  *                 nshort short steps each (argv[5]; init.c:314 sets
  *                 dtlong = dt * nshort); force_short / force_long /
@@ -58,6 +61,7 @@ void pme_calc(int, double *);
 void cnonbondnl(int, double *);
 void integrate_vverlet(int, double);
 void integrate_mts(int, double);
+void integrate_mts_nhc(int, double);
 void force_short(int);
 void force_long(int);
 void integrate_nhc(double, int);
@@ -571,9 +575,11 @@ int main(int argc, char **argv) {
       dump_d("zeta", z, 3 * (int64_t)M);
     }
     free(rec);
-  } else if (strcmp(mode, "mts") == 0) {
+  } else if (strcmp(mode, "mts") == 0 || strcmp(mode, "mtsnhc") == 0) {
     int nsteps = argc > 4 ? atoi(argv[4]) : 6;
+    int use_nhc = strcmp(mode, "mtsnhc") == 0;
     sim.nsteps = argc > 5 ? atoi(argv[5]) : 4;
+    sim.xRESPA[k] = argc > 6 ? atoi(argv[6]) : 0;
     sim.dtlong = sim.dt * sim.nsteps; /* init.c:314 */
     nblist(k);
     force_short(k); /* nve_md.c:298-304 */
@@ -585,7 +591,8 @@ int main(int argc, char **argv) {
     rec[12] = en[k].urey; rec[13] = en[k].tors; rec[14] = en[k].impr;
     for (int i = 1; i <= nsteps; i++) {
       if (i % sim.nlist == 0) nblist(k);
-      integrate_mts(k, 1.0); /* nve_md.c:412 */
+      if (use_nhc) integrate_mts_nhc(k, 1.0); /* nvt_md.c:552 */
+      else integrate_mts(k, 1.0);             /* nve_md.c:412 */
       kinet(k);
       en_record(rec + 15 * i);
       rec[15 * i + 12] = en[k].urey; rec[15 * i + 13] = en[k].tors;
@@ -599,6 +606,16 @@ int main(int argc, char **argv) {
     dump_xyz("force", ff[k]);
     dump_xyz("f_short", ff_short[k]);
     dump_xyz("f_long", ff_long[k]);
+    if (use_nhc) {
+      double z[3 * 16];
+      int M = nhc[k].M < 16 ? nhc[k].M : 16;
+      for (int j = 0; j < M; j++) {
+        z[3 * j] = nhc[k].zeta[j].r;
+        z[3 * j + 1] = nhc[k].zeta[j].v;
+        z[3 * j + 2] = nhc[k].zeta[j].G;
+      }
+      dump_d("zeta", z, 3 * (int64_t)M);
+    }
     free(rec);
 #ifdef DLIST
   } else if (strcmp(mode, "nlcheck") == 0) {

@@ -192,6 +192,12 @@ def make_mts_water(tmp):
     out = sys_arrays(s)
     for k, v in r.items():
         out["mts_" + k] = v
+    # integrate_mts_nhc.c with the thermostat per long step (xRESPA 0) and
+    # per short step (xRESPA 1)
+    for x in (0, 1):
+        r = O.run_reference("mtsnhc", s, tmp, nsteps=8, extra=(4, x))
+        for k, v in r.items():
+            out[f"mtsnhc{x}_" + k] = v
     np.savez_compressed(os.path.join(HERE, "mts_water600.npz"), **out)
 
 

@@ -130,7 +130,7 @@ def test_reference_program_links_against_the_engine(lib):
         "md": ("nblist", "forces", "cnonbondnl", "pme_calc", "charge_grid", "pme_init",
                "pme_clean", "fillspline", "integrate_vverlet", "integrate_nhc", "pbc_all",
                "kinet", "drift", "isokin", "swap_box", "force_short", "force_long",
-               "integrate_mts"),
+               "integrate_mts", "integrate_mts_nhc"),
         "mc": ("forces_mc", "enbnd_mc", "ewald_kspace_mc", "ewald_rspace_mc", "nblist_pivot",
                "drift"),
     }

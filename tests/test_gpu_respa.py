@@ -1,8 +1,9 @@
 """RESPA multiple time stepping on the FP64 engine (integrate_mts.c,
-force_short.c, force_long.c) against the reference's own runs: the 900-site
-chain box (every bonded kind: bonds, bends and Urey-Bradley terms fast;
-torsions, impropers and the non-bonded terms with SPME slow; 6 long steps of
-4 short steps) and the 600-site water box (8 long steps of 4).
+integrate_mts_nhc.c, force_short.c, force_long.c) against the reference's
+own runs: the 900-site chain box (every bonded kind: bonds, bends and
+Urey-Bradley terms fast; torsions, impropers and the non-bonded terms with
+SPME slow; 6 long steps of 4 short steps) and the 600-site water box (8 long
+steps of 4, plain and with the Nose-Hoover chain at either placement).
 
 Bars as for the velocity-Verlet trajectories: energies of every long step to
 1e-9 of their size, positions to 1e-10 A, velocities to 1e-8 A/ps, the
@@ -25,8 +26,9 @@ def _close_f(got, want, tol=1e-9):
     assert err <= tol * scale, f"max force error {err:.3e} (scale {scale:.3e})"
 
 
-def _run(s, g, nlong, nshort):
-    """nve_md.c:298-304 before the loop, then its RESPA branch (:400-418)."""
+def _run(s, g, nlong, nshort, xrespa=None):
+    """nve_md.c:298-304 before the loop, then its RESPA branch (:400-418), or
+    nvt_md.c's integrate_mts_nhc branch (:552) when xrespa is 0 or 1."""
     from thecodecombo_7_gb300 import engine
     rec = np.zeros((nlong + 1, 15))
     with engine.Box(s, precision=engine.FE_PREC_FP64) as b:
@@ -39,31 +41,37 @@ def _run(s, g, nlong, nshort):
         for i in range(1, nlong + 1):
             if i % s.nlist_freq == 0:
                 b.nblist()
-            en = b.integrate_mts(nshort)
+            en = (b.integrate_mts(nshort) if xrespa is None
+                  else b.integrate_mts_nhc(nshort, xrespa))
             rec[i] = [b.kinet()[0]] + [en[k] for k in O.EN_KEYS[1:12]] + [
                 en["urey"], en["tors"], en["impr"]]
         out = dict(rec=rec, pos=b.get_positions(), pos_nopbc=b.get_positions_nopbc(),
                    force=b.get_forces())
         out["vel"], out["uu"] = b.get_velocities()
         out["f_short"], out["f_long"] = b.forces_mts()
+        out["zeta"] = b.get_nhc_state()
     return out
 
 
-def _check(out, g, nlong):
-    want = g["mts_en_steps"].reshape(-1, 15)
+def _check(out, g, nlong, pre="mts_"):
+    g = {k[len(pre):]: v for k, v in g.items() if k.startswith(pre)}
+    want = g["en_steps"].reshape(-1, 15)
     assert want.shape[0] == nlong + 1
     keys = list(O.EN_KEYS[:12]) + ["urey", "tors", "impr"]
     for i in range(nlong + 1):
         for k in range(15):
             assert abs(out["rec"][i, k] - want[i, k]) <= ETOL * max(1.0, abs(want[i, k])), \
                 (i, keys[k], out["rec"][i, k], want[i, k])
-    np.testing.assert_allclose(out["pos"].ravel(), g["mts_pos"], rtol=0, atol=1e-10)
-    np.testing.assert_allclose(out["pos_nopbc"].ravel(), g["mts_pos_nopbc"], rtol=0, atol=1e-10)
-    np.testing.assert_allclose(out["vel"].ravel(), g["mts_vel"], rtol=0, atol=1e-8)
-    np.testing.assert_allclose(out["uu"].ravel(), g["mts_vel_uu"], rtol=0, atol=1e-8)
-    _close_f(out["force"].ravel(), g["mts_force"])
-    _close_f(out["f_short"].ravel(), g["mts_f_short"])
-    _close_f(out["f_long"].ravel(), g["mts_f_long"])
+    np.testing.assert_allclose(out["pos"].ravel(), g["pos"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(out["pos_nopbc"].ravel(), g["pos_nopbc"], rtol=0, atol=1e-10)
+    np.testing.assert_allclose(out["vel"].ravel(), g["vel"], rtol=0, atol=1e-8)
+    np.testing.assert_allclose(out["uu"].ravel(), g["vel_uu"], rtol=0, atol=1e-8)
+    _close_f(out["force"].ravel(), g["force"])
+    _close_f(out["f_short"].ravel(), g["f_short"])
+    _close_f(out["f_long"].ravel(), g["f_long"])
+    if "zeta" in g:
+        z = g["zeta"].reshape(-1, 3)
+        np.testing.assert_allclose(out["zeta"][:len(z)], z, rtol=1e-9, atol=1e-15)
 
 
 def test_respa_chain_vs_reference(golden_chain):
@@ -74,6 +82,14 @@ def test_respa_chain_vs_reference(golden_chain):
 def test_respa_water_vs_reference(golden_mts600):
     g = golden_mts600
     _check(_run(system_from_golden(g, 200), g, 8, 4), g, 8)
+
+
+@pytest.mark.parametrize("xrespa", [0, 1])
+def test_respa_nhc_water_vs_reference(golden_mts600, xrespa):
+    """integrate_mts_nhc.c with the chain per long step (xRESPA 0) or per
+    short step (xRESPA 1): trajectory, energies and the chain's state."""
+    g = golden_mts600
+    _check(_run(system_from_golden(g, 200), g, 8, 4, xrespa), g, 8, f"mtsnhc{xrespa}_")
 
 
 def test_respa_one_short_step_is_velocity_verlet(golden600):

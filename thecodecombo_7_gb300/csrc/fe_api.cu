@@ -849,7 +849,18 @@ int fe_integrate_mts(fe_box *box, double vscal, int nshort, double *en) {
   Box *b = &box->b;
   int rc;
   if ((rc = respa_check(b, "fe_integrate_mts"))) return rc;
-  if ((rc = respa_step(b, vscal, nshort))) return rc;
+  if ((rc = respa_step(b, vscal, nshort, -1))) return rc;
+  if ((rc = sync_scal(b))) return rc;
+  copy_en(b, en);
+  return FE_OK;
+}
+
+int fe_integrate_mts_nhc(fe_box *box, int nshort, int xrespa, double *en) {
+  if (!box || nshort < 1 || (xrespa != 0 && xrespa != 1)) return FE_ERR_ARG;
+  Box *b = &box->b;
+  int rc;
+  if ((rc = respa_check(b, "fe_integrate_mts_nhc"))) return rc;
+  if ((rc = respa_step(b, 1.0, nshort, xrespa))) return rc;
   if ((rc = sync_scal(b))) return rc;
   copy_en(b, en);
   return FE_OK;

@@ -232,7 +232,7 @@ int launch_bonded_ext(Box *b, bool to_fixed, int kinds = 7);  // kinds: 1 urey, 
 int respa_alloc(Box *b);
 int respa_force_short(Box *b);
 int respa_force_long(Box *b);
-int respa_step(Box *b, double vscal, int nshort);
+int respa_step(Box *b, double vscal, int nshort, int xrespa);  // xrespa < 0: no thermostat
 // k_spme.cu
 int spme_setup(Box *b);
 int launch_charge_grid64(Box *b);

@@ -7,7 +7,11 @@
 //   - one long step: a half kick with the slow forces, nsteps short steps
 //     (half kick with the fast forces, drift of atom and atnopbc, pbc_all,
 //     fast forces, half kick), the slow forces, a half kick with them, and
-//     uu = vv.
+//     uu = vv;
+//   - the Nose-Hoover form (integrate_mts_nhc.c:37-162): integrate_nhc over
+//     half a long step at both ends of the long step (sim.xRESPA = 0) or over
+//     half a short step at both ends of every short step (sim.xRESPA = 1);
+//     its kicks carry no vscal.
 // Compiled with -fmad=false; every kick keeps the reference's operation
 // order (left to right: dt * imass * f, vscal applied where it applies it).
 // Kernels fuse what runs site by site in a row: the opening slow kick with
@@ -53,9 +57,9 @@ __global__ void k_mts_drift(int n, int lead, int nkick, double vscal, double dt_
   pos[i] = p;
 }
 
-// the last fast half kick (integrate_mts.c:111-115), the slow one
-// (:128-132) and uu = vv (:133-135)
-__global__ void k_mts_close(int n, double vs_dt_shorth, double vs_dt_longh,
+// a closing fast half kick (integrate_mts.c:111-115); on the last short
+// step (`last`) also the slow one (:128-132) and uu = vv (:133-135)
+__global__ void k_mts_close(int n, int last, double vs_dt_shorth, double vs_dt_longh,
                             const double *__restrict__ imass100,
                             const double *__restrict__ f_short, const double *__restrict__ f_long,
                             double *__restrict__ vv, double *__restrict__ uu) {
@@ -64,9 +68,11 @@ __global__ void k_mts_close(int n, double vs_dt_shorth, double vs_dt_longh,
   const double imass = imass100[i / 3];
   double w = vv[i];
   w = w + vs_dt_shorth * imass * f_short[i];
-  w = w + vs_dt_longh * imass * f_long[i];
+  if (last) {
+    w = w + vs_dt_longh * imass * f_long[i];
+    uu[i] = w;
+  }
   vv[i] = w;
-  uu[i] = w;
 }
 
 // ff_short and ff_long on first use, zeroed as the reference's allocation
@@ -106,29 +112,41 @@ int respa_force_long(Box *b) {
   return FE_OK;
 }
 
-// integrate_mts.c:37-140, one long step of nshort short steps
-int respa_step(Box *b, double vscal, int nshort) {
+// integrate_mts.c:37-140 (xrespa < 0) or integrate_mts_nhc.c:37-162 with
+// sim.xRESPA = xrespa (0 or 1): one long step of nshort short steps
+int respa_step(Box *b, double vscal, int nshort, int xrespa) {
   int rc = respa_alloc(b);
   if (rc) return rc;
+  if (xrespa >= 0) vscal = 1.0;  // integrate_mts_nhc.c kicks without it
   const double dt = b->p.dt;
   const double dtlong = dt * nshort;  // init.c:314, sim.dtlong = sim.dt * sim.nsteps
   const double dt_shorth = 0.5 * dt, dt_longh = 0.5 * dtlong;
   const double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   const double3 H = make_double3(b->p.L[0] / 2.0, b->p.L[1] / 2.0, b->p.L[2] / 2.0);
-  const int blocks = (b->n + 255) / 256;
+  const int blocks = (b->n + 255) / 256, blocks3 = (3 * b->n + 255) / 256;
+  if (xrespa == 0 && (rc = launch_nhc(b, dt_longh))) return rc;
   for (int j = 0; j < nshort; j++) {
-    k_mts_drift<<<blocks, 256, 0, b->stream>>>(b->n, j == 0, j == 0 ? 1 : 2, vscal, dt_longh,
+    if (xrespa == 1 && (rc = launch_nhc(b, dt_shorth))) return rc;
+    // the closing kick of the previous short step joins this one's opening
+    // kick unless a thermostat pass runs between them
+    const int nkick = (j > 0 && xrespa != 1) ? 2 : 1;
+    k_mts_drift<<<blocks, 256, 0, b->stream>>>(b->n, j == 0, nkick, vscal, dt_longh,
                                                vscal * dt_shorth, dt, L, H, b->imass100,
                                                b->ff_long, b->ff_short, b->vv, b->pos_q,
                                                b->pos_nopbc, b->status);
     FE_LAUNCH_CHECK("k_mts_drift");
     if ((rc = respa_force_short(b))) return rc;
+    const bool last = j == nshort - 1;
+    if (last && (rc = respa_force_long(b))) return rc;
+    if (last || xrespa == 1) {
+      k_mts_close<<<blocks3, 256, 0, b->stream>>>(b->n, last, vscal * dt_shorth,
+                                                  vscal * dt_longh, b->imass100, b->ff_short,
+                                                  b->ff_long, b->vv, b->uu);
+      FE_LAUNCH_CHECK("k_mts_close");
+    }
+    if (xrespa == 1 && (rc = launch_nhc(b, dt_shorth))) return rc;
   }
-  if ((rc = respa_force_long(b))) return rc;
-  k_mts_close<<<(3 * b->n + 255) / 256, 256, 0, b->stream>>>(b->n, vscal * dt_shorth,
-                                                             vscal * dt_longh, b->imass100,
-                                                             b->ff_short, b->ff_long, b->vv, b->uu);
-  FE_LAUNCH_CHECK("k_mts_close");
+  if (xrespa == 0 && (rc = launch_nhc(b, dt_longh))) return rc;
   return launch_assemble_energies(b, 1);
 }
 

@@ -39,6 +39,6 @@ link() {
   echo "linked $OUT/spidey_gpu"
 }
 link md "-DNLIST -DEWALD -DSPME -DSTYPE" \
-  "nblist.c cnonbond_nblist.c pme_qgrid.c pme_calc.c pme_setup.c pme_spline.c integrate_vverlet.c integrate_nhc.c pbc_all.c kinet.c forces.c drift.c isokin.c swap_box.c integrate_mts.c force_short.c force_long.c"
+  "nblist.c cnonbond_nblist.c pme_qgrid.c pme_calc.c pme_setup.c pme_spline.c integrate_vverlet.c integrate_nhc.c pbc_all.c kinet.c forces.c drift.c isokin.c swap_box.c integrate_mts.c integrate_mts_nhc.c force_short.c force_long.c"
 link mc "-DNLIST -DEWALD -DMC -DSTYPE" \
   "forces_mc.c enbnd_mc.c ewald_mc.c nblist_pivot.c drift.c"

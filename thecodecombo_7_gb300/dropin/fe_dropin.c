@@ -7,8 +7,8 @@
  *   MD form (-DNLIST -DEWALD -DSPME -DSTYPE): replaces nblist.c,
  *     cnonbond_nblist.c, pme_qgrid.c, pme_calc.c, pme_setup.c, pme_spline.c,
  *     integrate_vverlet.c, integrate_nhc.c, pbc_all.c, kinet.c, forces.c,
- *     drift.c, isokin.c, swap_box.c and, for RESPA (sim.ID2 == 3, FP64
- *     engine), integrate_mts.c, force_short.c and force_long.c.
+ *     drift.c, isokin.c, swap_box.c and, for RESPA (FP64 engine),
+ *     integrate_mts.c, integrate_mts_nhc.c, force_short.c and force_long.c.
  *   MC form (-DNLIST -DEWALD -DMC -DSTYPE, classic Ewald, no SPME): replaces
  *     forces_mc.c, enbnd_mc.c, ewald_mc.c, nblist_pivot.c, drift.c.
  *
@@ -514,6 +514,26 @@ void integrate_mts(int ibox, double vscal) {
   FE_OR_DIE(fe_get_velocities(b, &vv[ibox][0].x, &uu[ibox][0].x), "integrate_mts");
   FE_OR_DIE(fe_get_forces(b, &ff[ibox][0].x), "integrate_mts");
   FE_OR_DIE(fe_get_forces_mts(b, &ff_short[ibox][0].x, &ff_long[ibox][0].x), "integrate_mts");
+  g_ok[ibox].ff = 1;
+  put_energies(ibox, e);
+}
+
+/* integrate_mts_nhc.c:37 (nvt_md.c:552): RESPA with the chain of
+ * integrate_nhc placed by sim.xRESPA[k]; nhc[k].zeta goes both ways */
+void integrate_mts_nhc(int ibox, double vscal) {
+  fe_box *b = fe_of(ibox);
+  double e[FE_EN_COUNT];
+  (void)vscal;  /* integrate_mts_nhc.c does not apply it */
+  put_atoms(b, ibox, 1);
+  put_vel(b, ibox);
+  FE_OR_DIE(fe_set_forces_mts(b, &ff_short[ibox][0].x, &ff_long[ibox][0].x), "integrate_mts_nhc");
+  FE_OR_DIE(fe_set_nhc_state(b, &nhc[ibox].zeta[0].r), "integrate_mts_nhc");
+  FE_OR_DIE(fe_integrate_mts_nhc(b, sim.nsteps, sim.xRESPA[ibox], e), "integrate_mts_nhc");
+  get_atoms(b, ibox, 1);
+  FE_OR_DIE(fe_get_velocities(b, &vv[ibox][0].x, &uu[ibox][0].x), "integrate_mts_nhc");
+  FE_OR_DIE(fe_get_forces(b, &ff[ibox][0].x), "integrate_mts_nhc");
+  FE_OR_DIE(fe_get_forces_mts(b, &ff_short[ibox][0].x, &ff_long[ibox][0].x), "integrate_mts_nhc");
+  FE_OR_DIE(fe_get_nhc_state(b, &nhc[ibox].zeta[0].r), "integrate_mts_nhc");
   g_ok[ibox].ff = 1;
   put_energies(ibox, e);
 }

@@ -44,7 +44,7 @@ EXPORTS = [
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_force_short", "fe_force_long", "fe_integrate_mts", "fe_get_forces_mts",
-    "fe_set_forces_mts",
+    "fe_set_forces_mts", "fe_integrate_mts_nhc",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats", "fe_nl_check",
     "fe_ewald_kspace_energy_noalloc",
@@ -400,6 +400,13 @@ class Box:
         """integrate_mts.c: one RESPA long step of `nshort` short steps."""
         en = np.empty(FE_EN_COUNT)
         self._check(self.lib.fe_integrate_mts(self.h, C.c_double(vscal), int(nshort), _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
+
+    def integrate_mts_nhc(self, nshort, xrespa=0):
+        """integrate_mts_nhc.c: one RESPA long step with the Nose-Hoover chain
+        per long step (xrespa 0) or per short step (xrespa 1)."""
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_integrate_mts_nhc(self.h, int(nshort), int(xrespa), _p(en)))
         return dict(zip(EN_KEYS, en.tolist()))
 
     def forces_mts(self):
