@@ -11,9 +11,11 @@ sums, FP64 integration).  Synthetic seeded input (no dataset is involved).
 
 Prints one JSON line.  ``value`` is atom-steps/s with all state resident on
 the GPU (steps timed with CUDA events on the engine's stream); ``e2e`` is the
-same metric through the C ABI with host buffers (positions and velocities
-uploaded and positions, velocities and forces read back every step, as a
-drop-in integrate_vverlet called from the reference's host loop would).
+same metric through the C ABI with host buffers: every step uploads the
+state integrate_vverlet reads (atom, atnopbc, vv, ff from pinned host
+arrays) and reads back what it writes (those, uu and the energies),
+in one fe_integrate_vverlet_host call per step, then kinet, as the
+reference's host loop (nve_md.c) calls them.
 Under torchrun each rank runs its own replica (the single-box path does not
 shard: replicas only) and the slowest rank's time is used.
 ``--impl reference`` times the reference's CPU implementation of the path
@@ -736,22 +738,21 @@ def run_ours(args, world, rank, local):
     def ptr(a):
         return a.ctypes.data_as(C.c_void_p)
 
+    ff_h[:] = box.get_forces()
     en = np.empty(engine.FE_EN_COUNT)
+    io = engine.FeMdIo(pos_h.ctypes.data, 24, 0, nop_h.ctypes.data, 24, 0, vv_h.ctypes.data,
+                       uu_h.ctypes.data, ff_h.ctypes.data)
     barrier(world)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for i in range(first + K, first + K + ke):
-        box._check(lib.fe_set_positions(box.h, ptr(pos_h), C.c_size_t(24), C.c_size_t(0), 0))
-        box._check(lib.fe_set_positions_nopbc(box.h, ptr(nop_h), C.c_size_t(24), C.c_size_t(0)))
-        box._check(lib.fe_set_velocities(box.h, ptr(vv_h), ptr(uu_h)))
+        # nve_md.c's loop: the list when due, integrate_vverlet with the host
+        # state it reads (atom, atnopbc, vv, ff: uploaded before the step)
+        # and writes (those and uu: read back after it), kinet
         if i % nl == 0:
             box._check(lib.fe_nblist(box.h))
-        box._check(lib.fe_integrate_vverlet(box.h, C.c_double(1.0), ptr(en)))
+        box._check(lib.fe_integrate_vverlet_host(box.h, C.c_double(1.0), C.byref(io), ptr(en)))
         box._check(lib.fe_kinet(box.h, None, None))
-        box._check(lib.fe_get_positions(box.h, ptr(pos_h), C.c_size_t(24), C.c_size_t(0)))
-        box._check(lib.fe_get_positions_nopbc(box.h, ptr(nop_h), C.c_size_t(24), C.c_size_t(0)))
-        box._check(lib.fe_get_velocities(box.h, ptr(vv_h), ptr(uu_h)))
-        box._check(lib.fe_get_forces(box.h, ptr(ff_h)))
     torch.cuda.synchronize()
     t_e2e = allreduce_max(time.perf_counter() - t0, world)
     e2e = world * n * ke / t_e2e

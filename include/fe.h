@@ -200,6 +200,26 @@ int fe_kinet(fe_box *box, double *ken6, double *kinet);
 /* integrate_vverlet(ibox, vscal), integrate_vverlet.c:36-103 (includes
  * pbc_all and forces); `en` as for fe_forces, may be NULL. */
 int fe_integrate_vverlet(fe_box *box, double vscal, double *en);
+/* Host arrays of one integrate_vverlet call as the drop-in makes it: the
+ * wrapped positions (struct atoms records by stride/offset, as
+ * fe_set_positions), the unwrapped ones (atnopbc), vv, uu and ff (3n
+ * doubles each); all are read before the step and written after it. */
+typedef struct fe_md_io {
+  void *atoms;
+  size_t atoms_stride, atoms_off;
+  void *nopbc;
+  size_t nopbc_stride, nopbc_off;
+  double *vv, *uu, *ff;
+} fe_md_io;
+/* integrate_vverlet with its host state in one call: the uploads of atom,
+ * atnopbc, vv and ff (uu is only written, integrate_vverlet.c:95-97), the
+ * step, the downloads of all five and `en`.  With every array in pinned host
+ * memory and 24-byte strides the copies are queued around the step (the
+ * positions' download on a second stream while the forces are evaluated)
+ * and the call synchronises once; otherwise it makes the separate calls
+ * (fe_set_positions .. fe_get_forces) with their own synchronisations.
+ * Same results either way. */
+int fe_integrate_vverlet_host(fe_box *box, double vscal, const fe_md_io *io, double *en);
 /* integrate_nhc(time_step, ibox), integrate_nhc.c:40-161 (Nc = Nys = 1) */
 int fe_integrate_nhc(fe_box *box, double time_step);
 /* RESPA multiple time stepping (FP64 boxes; FE_ERR_STATE for mixed):

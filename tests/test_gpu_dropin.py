@@ -117,3 +117,55 @@ def test_swap_sequence_matches_oracle():
     finally:
         for b in boxes:
             b.close()
+
+
+def test_integrate_vverlet_host_equals_separate_calls(golden600):
+    """fe_integrate_vverlet_host with pinned arrays (copies queued around the
+    step, one synchronisation) and with plain numpy arrays (the separate
+    upload / step / download calls) gives the results of the separate calls:
+    bit for bit in mixed precision (fixed-point force sums), and to the
+    run-to-run spread of the FP64 atomic force sums in FP64."""
+    import torch
+    from thecodecombo_7_gb300 import engine
+    from tests.helpers import system_from_golden
+    s = system_from_golden(golden600, 200)
+    for prec in (engine.FE_PREC_FP64, engine.FE_PREC_MIXED):
+        outs = []
+        for mode in ("pinned", "numpy", "calls"):
+            with engine.Box(s, precision=prec) as b:
+                b.nblist()
+                b.forces()
+                arrs = [b.get_positions(), b.get_positions_nopbc(), *b.get_velocities(),
+                        b.get_forces()]
+                if mode == "pinned":
+                    pinned = []
+                    for a in arrs:
+                        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+                        t[:] = a
+                        pinned.append(t)
+                    arrs = pinned
+                for i in range(1, 7):
+                    if i % s.nlist_freq == 0:
+                        b.nblist()
+                    if mode == "calls":
+                        b.set_positions(arrs[0])
+                        b.set_positions_nopbc_array(arrs[1])
+                        b.set_velocities(arrs[2], arrs[3])
+                        b.set_forces(arrs[4])
+                        en = b.integrate_vverlet()
+                        arrs = [b.get_positions(), b.get_positions_nopbc(), *b.get_velocities(),
+                                b.get_forces()]
+                    else:
+                        en = b.integrate_vverlet_host(*arrs)
+                outs.append(([a.copy() for a in arrs], en))
+        for other in outs[1:]:
+            for k, (a, c) in enumerate(zip(outs[0][0], other[0])):
+                if prec == engine.FE_PREC_MIXED:
+                    assert np.array_equal(a, c), k
+                else:
+                    assert np.abs(a - c).max() <= 1e-10 * max(1.0, np.abs(a).max()), k
+            for key, v in outs[0][1].items():
+                if prec == engine.FE_PREC_MIXED:
+                    assert v == other[1][key], key
+                else:
+                    assert abs(v - other[1][key]) <= 1e-10 * max(1.0, abs(v)), key

@@ -116,6 +116,9 @@ static void free_box(Box *b) {
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  if (b->s_io) cudaStreamDestroy(b->s_io);
+  if (b->ev_io_pos) cudaEventDestroy(b->ev_io_pos);
+  if (b->ev_io_done) cudaEventDestroy(b->ev_io_done);
 }
 
 static int create(Box *b, const fe_box_params *p) {
@@ -887,6 +890,69 @@ int fe_set_forces_mts(fe_box *box, const double *ff_short, const double *ff_long
   if (ff_short) FE_CUDA(cudaMemcpyAsync(b->ff_short, ff_short, bytes, cudaMemcpyHostToDevice, b->stream));
   if (ff_long) FE_CUDA(cudaMemcpyAsync(b->ff_long, ff_long, bytes, cudaMemcpyHostToDevice, b->stream));
   FE_CUDA(cudaStreamSynchronize(b->stream));
+  return FE_OK;
+}
+
+// the gather of the wrapped positions into xyz_dev on stream `s`
+static int k_xyz_gather_on(Box *b, cudaStream_t s) {
+  cudaStream_t keep = b->stream;
+  b->stream = s;
+  int rc = launch_xyz_gather(b, b->xyz_dev);
+  b->stream = keep;
+  return rc;
+}
+
+int fe_integrate_vverlet_host(fe_box *box, double vscal, const fe_md_io *io, double *en) {
+  if (!box || !io || !io->atoms || !io->nopbc || !io->vv || !io->uu || !io->ff) {
+    set_error("fe_integrate_vverlet_host: null argument");
+    return FE_ERR_ARG;
+  }
+  Box *b = &box->b;
+  char *ap = (char *)io->atoms + io->atoms_off, *np = (char *)io->nopbc + io->nopbc_off;
+  const bool queued = io->atoms_stride == 24 && io->nopbc_stride == 24 && pinned_host(ap) &&
+                      pinned_host(np) && pinned_host(io->vv) && pinned_host(io->uu) &&
+                      pinned_host(io->ff);
+  int rc;
+  if (!queued) {
+    if ((rc = fe_set_positions(box, io->atoms, io->atoms_stride, io->atoms_off, 0))) return rc;
+    if ((rc = fe_set_positions_nopbc(box, io->nopbc, io->nopbc_stride, io->nopbc_off))) return rc;
+    if ((rc = fe_set_velocities(box, io->vv, io->uu))) return rc;
+    if ((rc = fe_set_forces(box, io->ff))) return rc;
+    if ((rc = fe_integrate_vverlet(box, vscal, en))) return rc;
+    if ((rc = fe_get_positions(box, io->atoms, io->atoms_stride, io->atoms_off))) return rc;
+    if ((rc = fe_get_positions_nopbc(box, io->nopbc, io->nopbc_stride, io->nopbc_off))) return rc;
+    if ((rc = fe_get_velocities(box, io->vv, io->uu))) return rc;
+    return fe_get_forces(box, io->ff);
+  }
+  if (!b->s_io) {
+    FE_CUDA(cudaStreamCreateWithFlags(&b->s_io, cudaStreamNonBlocking));
+    FE_CUDA(cudaEventCreateWithFlags(&b->ev_io_pos, cudaEventDisableTiming));
+    FE_CUDA(cudaEventCreateWithFlags(&b->ev_io_done, cudaEventDisableTiming));
+  }
+  const size_t bytes = sizeof(double) * 3 * (size_t)b->n;
+  // uu is written by the step, not read (integrate_vverlet.c:95-97)
+  FE_CUDA(cudaMemcpyAsync(b->xyz_dev, ap, bytes, cudaMemcpyHostToDevice, b->stream));
+  if ((rc = launch_xyz_scatter(b, b->xyz_dev, true, false))) return rc;
+  FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, np, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaMemcpyAsync(b->vv, io->vv, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaMemcpyAsync(b->ff, io->ff, bytes, cudaMemcpyHostToDevice, b->stream));
+  if ((rc = launch_vv1(b, vscal))) return rc;
+  // the positions are final after the drift: their download runs on the
+  // copy stream while the forces are evaluated
+  FE_CUDA(cudaEventRecord(b->ev_io_pos, b->stream));
+  FE_CUDA(cudaStreamWaitEvent(b->s_io, b->ev_io_pos, 0));
+  if ((rc = k_xyz_gather_on(b, b->s_io))) return rc;
+  FE_CUDA(cudaMemcpyAsync(ap, b->xyz_dev, bytes, cudaMemcpyDeviceToHost, b->s_io));
+  FE_CUDA(cudaMemcpyAsync(np, b->pos_nopbc, bytes, cudaMemcpyDeviceToHost, b->s_io));
+  FE_CUDA(cudaEventRecord(b->ev_io_done, b->s_io));
+  if ((rc = forces_device(b))) return rc;
+  if ((rc = launch_vv2(b, vscal))) return rc;
+  FE_CUDA(cudaMemcpyAsync(io->vv, b->vv, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(io->uu, b->uu, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(io->ff, b->ff, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamWaitEvent(b->stream, b->ev_io_done, 0));
+  if ((rc = sync_scal(b))) return rc;
+  copy_en(b, en);
   return FE_OK;
 }
 

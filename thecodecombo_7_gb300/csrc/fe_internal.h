@@ -70,6 +70,10 @@ struct Box {
   int dev = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
+  // fe_integrate_vverlet_host: a copy stream for the positions' download,
+  // which overlaps the force evaluation (created on first use)
+  cudaStream_t s_io = nullptr;
+  cudaEvent_t ev_io_pos = nullptr, ev_io_done = nullptr;
   int prec = FE_PREC_FP64;
 
   // sites

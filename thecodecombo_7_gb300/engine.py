@@ -44,7 +44,7 @@ EXPORTS = [
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_force_short", "fe_force_long", "fe_integrate_mts", "fe_get_forces_mts",
-    "fe_set_forces_mts", "fe_integrate_mts_nhc",
+    "fe_set_forces_mts", "fe_integrate_mts_nhc", "fe_integrate_vverlet_host",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats", "fe_nl_check",
     "fe_ewald_kspace_energy_noalloc",
@@ -71,6 +71,13 @@ class FeError(RuntimeError):
     def __init__(self, code: int, msg: str):
         super().__init__(f"[fe error {code}] {msg}")
         self.code = code
+
+
+class FeMdIo(C.Structure):
+    """fe_md_io: the host arrays of one fe_integrate_vverlet_host call."""
+    _fields_ = [("atoms", C.c_void_p), ("atoms_stride", C.c_size_t), ("atoms_off", C.c_size_t),
+                ("nopbc", C.c_void_p), ("nopbc_stride", C.c_size_t), ("nopbc_off", C.c_size_t),
+                ("vv", C.c_void_p), ("uu", C.c_void_p), ("ff", C.c_void_p)]
 
 
 class FeBoxParams(C.Structure):
@@ -414,6 +421,21 @@ class Box:
         fs, fl = np.empty((self.n, 3)), np.empty((self.n, 3))
         self._check(self.lib.fe_get_forces_mts(self.h, _p(fs), _p(fl)))
         return fs, fl
+
+    def integrate_vverlet_host(self, pos, pos_nopbc, vv, uu, ff, vscal=1.0):
+        """integrate_vverlet with its host state in one call: the five (n, 3)
+        float64 arrays are read before the step and overwritten after it
+        (one synchronisation when they are in pinned memory)."""
+        arrs = (pos, pos_nopbc, vv, uu, ff)
+        for a in arrs:
+            if a.dtype != np.float64 or not a.flags.c_contiguous or a.size != 3 * self.n:
+                raise ValueError("integrate_vverlet_host needs contiguous float64 (n, 3) arrays")
+        io = FeMdIo(pos.ctypes.data, 24, 0, pos_nopbc.ctypes.data, 24, 0, vv.ctypes.data,
+                    uu.ctypes.data, ff.ctypes.data)
+        en = np.empty(FE_EN_COUNT)
+        self._check(self.lib.fe_integrate_vverlet_host(self.h, C.c_double(vscal), C.byref(io),
+                                                       _p(en)))
+        return dict(zip(EN_KEYS, en.tolist()))
 
     def integrate_nhc(self, time_step=None):
         ts = self.sysm.dt if time_step is None else time_step
