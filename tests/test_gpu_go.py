@@ -113,3 +113,29 @@ def test_go_split_plan_and_forces():
         x, v, eo = O.go_baoab(g, r, 10, seed=2)
         assert np.abs(s["pos"][st[r]:st[r + 1]] - x).max() < 1e-4, (r, parts[r])
         assert np.abs(s["vel"][st[r]:st[r + 1]] - v).max() < 1e-2, (r, parts[r])
+
+
+@pytest.mark.parametrize("nrep,nb", [(1, 1024), (3, 2), (2, 5)])
+def test_go_extreme_chain_lengths(nrep, nb):
+    """The limits of the batch: one chain of the maximum 1,024 beads (split
+    over the CTAs of a cluster, the largest shared-memory rows), chains of two
+    beads (a bond and nothing else) and of five (one non-native pair)."""
+    from thecodecombo_7_gb300 import engine, systems
+    g = systems.go_chains(nrep, nmin=nb, nmax=nb, seed=23)
+    b = engine.GoBatch(g, seed=4)
+    try:
+        f, e = b.forces()
+        b.run(10)
+        s = b.state()
+    finally:
+        b.close()
+    st = g.start
+    for r in range(nrep):
+        fr, er = O.go_forces(g, r)
+        fg = f[st[r]:st[r + 1]]
+        scale = np.sqrt((fr ** 2).sum())
+        assert np.sqrt(((fg - fr) ** 2).sum()) <= 1e-5 * max(scale, 1e-3), r
+        assert abs(e[r] - er) <= 1e-5 * g.eps * max(g.nbeads[r], 10), (r, e[r], er)
+        x, v, eo = O.go_baoab(g, r, 10, seed=4)
+        assert np.abs(s["pos"][st[r]:st[r + 1]] - x).max() < 1e-4, r
+        assert np.abs(s["vel"][st[r]:st[r + 1]] - v).max() < 1e-2, r

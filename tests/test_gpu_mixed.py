@@ -88,6 +88,27 @@ def test_mixed_bonded_energies_relative():
         assert abs(en[k] - en_ref[k]) <= 1e-6 * abs(en_ref[k]), (k, en[k], en_ref[k])
 
 
+def test_mixed_bonded_energies_thermal():
+    """Bond and bend energies of a thermalised box (400 NVE steps from the
+    rigid start) against the FP64 oracle on the same coordinates: within
+    1e-7, the energy bar (the stretch and the angle carry no FP32 bias: theta0
+    and r0 as two floats, the length scale's rounding corrected, correctly
+    rounded lengths)."""
+    from thecodecombo_7_gb300 import systems
+    s = systems.water_box(1365, density=0.1, seed=43)
+    with _mixed(s) as b:
+        b.nblist()
+        b.forces()
+        b.kinet()
+        b.run_md(400, nlist_freq=10, record=False)
+        pos = b.get_positions()
+        b.nblist()
+        en = b.forces()
+    _, en_ref = O.Oracle(s).forces(pos)
+    for k in ("bond", "bend"):
+        assert abs(en[k] - en_ref[k]) <= 1e-7 * abs(en_ref[k]), (k, en[k], en_ref[k])
+
+
 def test_mixed_deterministic(case):
     s, _, _ = case
     with _mixed(s) as b:

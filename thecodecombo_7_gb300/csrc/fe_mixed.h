@@ -32,9 +32,9 @@ struct IntraTpl {
   int ns, nx, nb, na;
   int xa[kTplTerms], xb[kTplTerms], xf[kTplTerms];
   int ba[kTplTerms], bb[kTplTerms];
-  float breq[kTplTerms], bk[kTplTerms];
+  float breq[kTplTerms], breq_lo[kTplTerms], bk[kTplTerms];  // r0 as hi + lo floats
   int aa[kTplTerms], ab[kTplTerms], ac[kTplTerms];
-  float at0[kTplTerms], ak[kTplTerms];
+  float at0[kTplTerms], at0_lo[kTplTerms], ak[kTplTerms];       // theta0 as hi + lo floats
   int type[kIntraMaxSites];
 };
 

@@ -687,8 +687,13 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
     for (int r = 0; r < nrep; r++)
       rowsz = std::max(rowsz, (size_t)nbeads[r] * ((nbeads[r] + 31) / 32));
     G->smem = 2 * sizeof(float4) * (size_t)maxN + sizeof(unsigned) * rowsz;
+    // the kernel's limit set once for the largest batch any handle can hold
+    // (1,024 beads), so that handles of different sizes never lower it
+    // under one another's launches
+    const int smem_cap = (int)(2 * sizeof(float4) * kGoMaxBeads +
+                               sizeof(unsigned) * kGoMaxBeads * (kGoMaxBeads / 32));
     if (cudaFuncSetAttribute(k_go_segment, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)G->smem) != cudaSuccess) {
+                             smem_cap) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute");
       break;
     }

@@ -977,8 +977,11 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
   block_fix_final<5>(v, 32, facc, ticket, out);
 }
 
-// bonded terms in FP32 from the fixed-point coordinates (cbond.c, cbend.c)
-__global__ void k_mx_bonded(int nbond, int nbend, float3 sL, const int4 *__restrict__ posfx,
+// bonded terms in FP32 from the fixed-point coordinates (cbond.c, cbend.c),
+// without the FP32 biases intra_bond / intra_bend take out (rho: the length
+// scale's rounding per axis)
+__global__ void k_mx_bonded(int nbond, int nbend, float3 sL, float3 rho,
+                            const int4 *__restrict__ posfx,
                             const int *__restrict__ iperm,
                             const int *__restrict__ bond_ab, const double *__restrict__ bond_req,
                             const double *__restrict__ bond_k, const int *__restrict__ bend_abc,
@@ -996,7 +999,9 @@ __global__ void k_mx_bonded(int nbond, int nbend, float3 sL, const int4 *__restr
       float dy = fx_delta((unsigned)B.y, (unsigned)A.y, sL.y);
       float dz = fx_delta((unsigned)B.z, (unsigned)A.z, sL.z);
       float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-      float rr = dr - (float)bond_req[t];
+      const double r0 = bond_req[t];
+      const float req = (float)r0, req_lo = (float)(r0 - (double)req);
+      float rr = (dr - req) - req_lo + (dx * dx * rho.x + dy * dy * rho.y + dz * dz * rho.z) / dr;
       float fr = -(float)bond_k[t] * rr * 2.f;
       eb += -(fr * rr * 0.5f);
       float s = fr / dr;
@@ -1017,15 +1022,17 @@ __global__ void k_mx_bonded(int nbond, int nbend, float3 sL, const int4 *__restr
       float dcx = fx_delta((unsigned)Cc.x, (unsigned)B.x, sL.x);
       float dcy = fx_delta((unsigned)Cc.y, (unsigned)B.y, sL.y);
       float dcz = fx_delta((unsigned)Cc.z, (unsigned)B.z, sL.z);
-      float drai = rsqrtf(dax * dax + day * day + daz * daz);
+      float drai = 1.f / sqrtf(dax * dax + day * day + daz * daz);
       float erax = dax * drai, eray = day * drai, eraz = daz * drai;
-      float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+      float drci = 1.f / sqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
       float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
       float cosphi = erax * ercx + eray * ercy + eraz * ercz;
       cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
       float phi = acosf(cosphi);
       float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
-      float rr = phi - (float)bend_t0[u];
+      const double th0 = bend_t0[u];
+      const float t0 = (float)th0;
+      float rr = (phi - t0) - (float)(th0 - (double)t0);
       float fr = -(float)bend_k[u] * rr * 2.f;
       ea += -fr * rr * 0.5f;
       float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
@@ -1483,13 +1490,17 @@ __device__ __forceinline__ void intra_excl(const int4 (&P)[NS], float (&F)[NS][3
 
 template <int NS>
 __device__ __forceinline__ void intra_bond(const int4 (&P)[NS], float (&F)[NS][3], int ia, int ib,
-                                           float req, float kb, float3 sL, IntraAcc &A) {
+                                           float req, float req_lo, float kb, float3 sL,
+                                           float3 rho, IntraAcc &A) {
   const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib);
   float dx = fx_delta((unsigned)Pb.x, (unsigned)Pa.x, sL.x);
   float dy = fx_delta((unsigned)Pb.y, (unsigned)Pa.y, sL.y);
   float dz = fx_delta((unsigned)Pb.z, (unsigned)Pa.z, sL.z);
   float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-  float rr = dr - req;
+  // the stretch r - r0 carries no bias of FP32 roundings: the length scale
+  // per axis is L / 2^32 = sL (1 + rho) and r0 = req + req_lo, so r - r0 =
+  // (dr - req) - req_lo + sum(d^2 rho) / dr to first order in rho
+  float rr = (dr - req) - req_lo + (dx * dx * rho.x + dy * dy * rho.y + dz * dz * rho.z) / dr;
   float fr = -kb * rr * 2.f;
   A.eb += -(fr * rr * 0.5f);
   float sc = fr / dr;
@@ -1499,7 +1510,8 @@ __device__ __forceinline__ void intra_bond(const int4 (&P)[NS], float (&F)[NS][3
 
 template <int NS>
 __device__ __forceinline__ void intra_bend(const int4 (&P)[NS], float (&F)[NS][3], int ia, int ib,
-                                           int ic, float t0, float ka, float3 sL, IntraAcc &A) {
+                                           int ic, float t0, float t0_lo, float ka, float3 sL,
+                                           IntraAcc &A) {
   const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib), Pc = intra_pick(P, ic);
   float dax = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
   float day = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
@@ -1507,15 +1519,18 @@ __device__ __forceinline__ void intra_bend(const int4 (&P)[NS], float (&F)[NS][3
   float dcx = fx_delta((unsigned)Pc.x, (unsigned)Pb.x, sL.x);
   float dcy = fx_delta((unsigned)Pc.y, (unsigned)Pb.y, sL.y);
   float dcz = fx_delta((unsigned)Pc.z, (unsigned)Pb.z, sL.z);
-  float drai = rsqrtf(dax * dax + day * day + daz * daz);
+  // correctly rounded lengths (the approximate reciprocal square root biases
+  // the angle by ~1e-7 rad, which the energy, a sum of (phi - t0)^2 terms of
+  // one sign of bias, does not average away)
+  float drai = 1.f / sqrtf(dax * dax + day * day + daz * daz);
   float erax = dax * drai, eray = day * drai, eraz = daz * drai;
-  float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+  float drci = 1.f / sqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
   float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
   float cosphi = erax * ercx + eray * ercy + eraz * ercz;
   cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
   float phi = acosf(cosphi);
   float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
-  float rr = phi - t0;
+  float rr = (phi - t0) - t0_lo;  // theta0 = t0 + t0_lo
   float fr = -ka * rr * 2.f;
   A.ea += -fr * rr * 0.5f;
   float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
@@ -1546,6 +1561,9 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                            double *__restrict__ out, const IntraTpl &T = IntraTpl()) {
   IntraAcc A;
+  // relative rounding of the FP32 length scale per axis (L / 2^32 = hi + lo)
+  const float3 rho = make_float3(D.sl[0].y / D.sl[0].x, D.sl[1].y / D.sl[1].x,
+                                 D.sl[2].y / D.sl[2].x);
   for (int m = vb_.id * blockDim.x + threadIdx.x; m < nmol; m += vb_.n * blockDim.x) {
     const int lb = UNI ? m * T.ns : mol_first[m];
     const int ns = UNI ? T.ns : mol_first[m + 1] - lb;
@@ -1581,43 +1599,49 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
 #pragma unroll
     for (int t = tb0; t < tb1; t++) {
       int ia, ib;
-      float req, kb;
+      float req, req_lo, kb;
       if (UNI) {
         if (t >= T.nb) break;
         ia = T.ba[t];
         ib = T.bb[t];
         req = T.breq[t];
+        req_lo = T.breq_lo[t];
         kb = T.bk[t];
       } else {
         int u = mol_bi[t];
         ia = bond_ab[2 * u] - lb;
         ib = bond_ab[2 * u + 1] - lb;
-        req = (float)bond_req[u];
+        const double r0 = bond_req[u];
+        req = (float)r0;
+        req_lo = (float)(r0 - (double)req);
         kb = (float)bond_k[u];
       }
-      intra_bond<NS>(P, F, ia, ib, req, kb, sL, A);
+      intra_bond<NS>(P, F, ia, ib, req, req_lo, kb, sL, rho, A);
     }
     const int ta0 = UNI ? 0 : mol_a[m], ta1 = UNI ? kTplTerms : mol_a[m + 1];
 #pragma unroll
     for (int t = ta0; t < ta1; t++) {
       int ia, ib, ic;
-      float t0, ka;
+      float t0, t0_lo, ka;
       if (UNI) {
         if (t >= T.na) break;
         ia = T.aa[t];
         ib = T.ab[t];
         ic = T.ac[t];
         t0 = T.at0[t];
+        t0_lo = T.at0_lo[t];
         ka = T.ak[t];
       } else {
         int u = mol_ai[t];
         ia = bend_abc[3 * u] - lb;
         ib = bend_abc[3 * u + 1] - lb;
         ic = bend_abc[3 * u + 2] - lb;
-        t0 = (float)bend_t0[u];
+        const double th0 = bend_t0[u];
+        t0 = (float)th0;
+        t0_lo = (float)(th0 - (double)t0);
         ka = (float)bend_k[u];
       }
-      intra_bend<NS>(P, F, ia, ib, ic, t0, ka, sL, A);
+      intra_bend<NS>(P, F, ia, ib, ic, t0, t0_lo, ka, sL, A);
     }
 #pragma unroll
     for (int i = 0; i < NS; i++)
@@ -1876,12 +1900,15 @@ int mixed_setup(Box *b) {
           int u = bi[bo[m] + k];
           int a = pp.bond_ab[2 * u] - lb, c = pp.bond_ab[2 * u + 1] - lb;
           float req = (float)pp.bond_req[u], kk = (float)pp.bond_k[u];
+          float req_lo = (float)(pp.bond_req[u] - (double)req);
           if (m == 0) {
             T.ba[k] = a;
             T.bb[k] = c;
             T.breq[k] = req;
+            T.breq_lo[k] = req_lo;
             T.bk[k] = kk;
-          } else if (a != T.ba[k] || c != T.bb[k] || req != T.breq[k] || kk != T.bk[k]) {
+          } else if (a != T.ba[k] || c != T.bb[k] || req != T.breq[k] ||
+                     req_lo != T.breq_lo[k] || kk != T.bk[k]) {
             uni = false;
           }
         }
@@ -1890,14 +1917,16 @@ int mixed_setup(Box *b) {
           int a = pp.bend_abc[3 * u] - lb, c = pp.bend_abc[3 * u + 1] - lb,
               d = pp.bend_abc[3 * u + 2] - lb;
           float t0 = (float)pp.bend_theta0[u], kk = (float)pp.bend_k[u];
+          float t0_lo = (float)(pp.bend_theta0[u] - (double)t0);
           if (m == 0) {
             T.aa[k] = a;
             T.ab[k] = c;
             T.ac[k] = d;
             T.at0[k] = t0;
+            T.at0_lo[k] = t0_lo;
             T.ak[k] = kk;
           } else if (a != T.aa[k] || c != T.ab[k] || d != T.ac[k] || t0 != T.at0[k] ||
-                     kk != T.ak[k]) {
+                     t0_lo != T.at0_lo[k] || kk != T.ak[k]) {
             uni = false;
           }
         }
@@ -2266,7 +2295,9 @@ static int intra_on(Box *b, cudaStream_t st, unsigned long long *facc, unsigned 
     int bb = (tot + 255) / 256;
     if (bb > 1024) bb = 1024;
     if (bb < 1) bb = 1;
-    k_mx_bonded<<<bb, 256, 0, st>>>(b->nbond, b->nbend, sL, M.posfx, M.iperm, b->bond_ab,
+    const float3 rho = make_float3(dfi.sl[0].y / dfi.sl[0].x, dfi.sl[1].y / dfi.sl[1].x,
+                                   dfi.sl[2].y / dfi.sl[2].x);
+    k_mx_bonded<<<bb, 256, 0, st>>>(b->nbond, b->nbend, sL, rho, M.posfx, M.iperm, b->bond_ab,
                                            b->bond_req, b->bond_k, b->bend_abc, b->bend_t0,
                                            b->bend_k, M.fix, facc, ticket,
                                            b->scal + SC_BOND);
