@@ -158,6 +158,12 @@ int fe_cnonbondnl(fe_box *box, double *energy8);
 /* pme_calc(k, energy), pme_calc.c:18-279 (charge_grid, FFTs, reciprocal
  * sum, pme_force with mean-force removal): accumulates into ff. */
 int fe_pme_calc(fe_box *box, double *energy3);
+/* pme_force(k), pme_calc.c:122-279: the reciprocal forces from the grid as
+ * the last fe_pme_calc left it (convolved, back in real space) and the
+ * splines of the last charge_grid, mean force removed, accumulated into ff
+ * (pme_calc calls it at its end; the drop-in exports it for callers of its
+ * own). */
+int fe_pme_force(fe_box *box);
 /* fillspline(w, array, darray), pme_spline.c:10-49: B-spline weights
  * array[1..order] and derivatives darray[1..order] at fraction w (host
  * arithmetic, the reference's recursion; arrays of order + 1 doubles). */

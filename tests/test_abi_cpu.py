@@ -127,7 +127,7 @@ def test_reference_program_links_against_the_engine(lib):
                           env=dict(os.environ, REF_DIR=O.reference_dir()))
     out = os.path.join(ROOT, "thecodecombo_7_gb300", "dropin", "_build")
     forms = {
-        "md": ("nblist", "forces", "cnonbondnl", "pme_calc", "charge_grid", "pme_init",
+        "md": ("nblist", "forces", "cnonbondnl", "pme_calc", "pme_force", "charge_grid", "pme_init",
                "pme_clean", "fillspline", "integrate_vverlet", "integrate_nhc", "pbc_all",
                "kinet", "drift", "isokin", "swap_box", "force_short", "force_long",
                "integrate_mts", "integrate_mts_nhc"),

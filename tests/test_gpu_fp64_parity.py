@@ -269,3 +269,19 @@ def test_mc_delta_matches_reference_fixture(golden_mc):
                 de, parts = b.mc_delta(lb, ub, new)
                 cols = [0, 1, 2] if which == "clu" else [0, 2]
                 np.testing.assert_allclose(parts[cols], w[cols], rtol=1e-9, atol=1e-9)
+
+
+def test_pme_force_alone(golden600):
+    """pme_force (pme_calc.c:122) after pme_calc: the same reciprocal forces
+    from the grid pme_calc left, which are the reference's own f_pme."""
+    g = golden600
+    s = system_from_golden(g, 200)
+    with _box(s) as b:
+        b.zero_forces()
+        b.pme_calc()
+        f1 = b.get_forces()
+        b.zero_forces()
+        b.pme_force()
+        f2 = b.get_forces()
+    assert np.array_equal(f1, f2)
+    _close_f(f2.ravel(), g["forces_f_pme"])

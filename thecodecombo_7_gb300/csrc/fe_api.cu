@@ -634,6 +634,19 @@ int fe_pme_calc(fe_box *box, double *energy3) {
   return FE_OK;
 }
 
+int fe_pme_force(fe_box *box) {
+  if (!box) return FE_ERR_ARG;
+  Box *b = &box->b;
+  if (b->mx) {
+    set_error("fe_pme_force is the FP64 drop-in entry; the mixed path evaluates fe_forces");
+    return FE_ERR_STATE;
+  }
+  int rc;
+  if ((rc = launch_pme_gather64(b))) return rc;
+  if ((rc = launch_apply_pme(b))) return rc;
+  return check_status(b);
+}
+
 int fe_charge_grid(fe_box *box) {
   if (!box) return FE_ERR_ARG;
   int rc = launch_charge_grid64(&box->b);

@@ -241,6 +241,7 @@ int respa_step(Box *b, double vscal, int nshort, int xrespa);  // xrespa < 0: no
 int spme_setup(Box *b);
 int launch_charge_grid64(Box *b);
 int launch_pme64(Box *b);  // spread .. gather; fp and SC_FMEAN, SC_ENREC
+int launch_pme_gather64(Box *b);  // the gather alone from the convolved grid
 // k_integrate.cu
 int launch_reduce(Box *b, const double *partials, int nblocks, int nterms, int slot, double scale);
 int launch_zero_forces(Box *b);

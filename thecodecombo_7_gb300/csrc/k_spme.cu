@@ -329,6 +329,13 @@ int launch_pme64(Box *b) {
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftSetStream");
   r = cufftExecZ2D(b->plan_c2r, b->grid_k, b->grid);
   if (r != CUFFT_SUCCESS) return cufft_fail(r, "cufftExecZ2D");
+  return launch_pme_gather64(b);
+}
+
+// pme_force (pme_calc.c:122-206): the reciprocal forces into fp from the
+// convolved grid and the splines of the last charge_grid, their sum into
+// SC_FMEAN (the mean removal is launch_apply_pme)
+int launch_pme_gather64(Box *b) {
   int3 G = make_int3(b->G[0], b->G[1], b->G[2]);
   double3 L = make_double3(b->p.L[0], b->p.L[1], b->p.L[2]);
   int gb = (b->n + 127) / 128;

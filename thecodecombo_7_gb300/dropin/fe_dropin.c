@@ -413,6 +413,15 @@ void pme_calc(int k, double *energy) {
   FE_OR_DIE(fe_get_forces(b, &ff[k][0].x), "pme_calc");
 }
 
+/* pme_calc.c:122 (accumulates into ff like the original, from the grid of
+ * the last pme_calc) */
+void pme_force(int k) {
+  fe_box *b = fe_of(k);
+  put_ff(b, k);
+  FE_OR_DIE(fe_pme_force(b), "pme_force");
+  FE_OR_DIE(fe_get_forces(b, &ff[k][0].x), "pme_force");
+}
+
 /* pme_qgrid.c:13: fills qgrida (real part, imaginary zero) */
 void charge_grid(int k) {
   fe_box *b = fe_of(k);

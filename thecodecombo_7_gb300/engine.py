@@ -44,7 +44,7 @@ EXPORTS = [
     "fe_pme_calc", "fe_charge_grid", "fe_get_charge_grid", "fe_bonded", "fe_zero_forces",
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_force_short", "fe_force_long", "fe_integrate_mts", "fe_get_forces_mts",
-    "fe_set_forces_mts", "fe_integrate_mts_nhc", "fe_integrate_vverlet_host",
+    "fe_set_forces_mts", "fe_integrate_mts_nhc", "fe_integrate_vverlet_host", "fe_pme_force",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats", "fe_nl_check",
     "fe_ewald_kspace_energy_noalloc",
@@ -322,6 +322,11 @@ class Box:
         en = np.empty(FE_EN_COUNT)
         self._check(self.lib.fe_forces(self.h, _p(en)))
         return dict(zip(EN_KEYS, en.tolist()))
+
+    def pme_force(self):
+        """pme_force (pme_calc.c:122): reciprocal forces from the grid of the
+        last pme_calc, accumulated into ff."""
+        self._check(self.lib.fe_pme_force(self.h))
 
     def cnonbondnl(self):
         e = np.empty(8)
