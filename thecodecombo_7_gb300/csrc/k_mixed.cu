@@ -61,6 +61,12 @@ __device__ __forceinline__ float fx_delta(unsigned a, unsigned b, float scale) {
   return __int2float_rn((int)(a - b)) * scale;
 }
 
+// a fixed-point coordinate difference in A, in FP64 (the integer difference
+// is exact; sd = L / 2^32 in double)
+__device__ __forceinline__ double fx_delta_d(unsigned a, unsigned b, double sd) {
+  return (double)(int)(a - b) * sd;
+}
+
 // ---------------------------------------------------------------------------
 // sorting by cells
 
@@ -977,10 +983,10 @@ __global__ void k_mx_excl(int nexcl, const int *__restrict__ ab, const int *__re
   block_fix_final<5>(v, 32, facc, ticket, out);
 }
 
-// bonded terms in FP32 from the fixed-point coordinates (cbond.c, cbend.c),
-// without the FP32 biases intra_bond / intra_bend take out (rho: the length
-// scale's rounding per axis)
-__global__ void k_mx_bonded(int nbond, int nbend, float3 sL, float3 rho,
+// bonded terms from the fixed-point coordinates (cbond.c, cbend.c): the
+// stretch, the angle and the energies in FP64 as in intra_bond / intra_bend,
+// the forces in FP32 (sd: the length scale L / 2^32 in FP64)
+__global__ void k_mx_bonded(int nbond, int nbend, float3 sL, double3 sd,
                             const int4 *__restrict__ posfx,
                             const int *__restrict__ iperm,
                             const int *__restrict__ bond_ab, const double *__restrict__ bond_req,
@@ -989,7 +995,7 @@ __global__ void k_mx_bonded(int nbond, int nbend, float3 sL, float3 rho,
                             unsigned long long *__restrict__ fix,
                             unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                             double *__restrict__ out) {
-  float eb = 0.f, ea = 0.f;
+  double eb = 0.0, ea = 0.0;
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < nbond + nbend;
        t += gridDim.x * blockDim.x) {
     if (t < nbond) {
@@ -999,11 +1005,12 @@ __global__ void k_mx_bonded(int nbond, int nbend, float3 sL, float3 rho,
       float dy = fx_delta((unsigned)B.y, (unsigned)A.y, sL.y);
       float dz = fx_delta((unsigned)B.z, (unsigned)A.z, sL.z);
       float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-      const double r0 = bond_req[t];
-      const float req = (float)r0, req_lo = (float)(r0 - (double)req);
-      float rr = (dr - req) - req_lo + (dx * dx * rho.x + dy * dy * rho.y + dz * dz * rho.z) / dr;
-      float fr = -(float)bond_k[t] * rr * 2.f;
-      eb += -(fr * rr * 0.5f);
+      const double ex = fx_delta_d((unsigned)B.x, (unsigned)A.x, sd.x);
+      const double ey = fx_delta_d((unsigned)B.y, (unsigned)A.y, sd.y);
+      const double ez = fx_delta_d((unsigned)B.z, (unsigned)A.z, sd.z);
+      const double rrd = sqrt(ex * ex + ey * ey + ez * ez) - bond_req[t];
+      eb += bond_k[t] * rrd * rrd;
+      float fr = -(float)bond_k[t] * (float)rrd * 2.f;
       float s = fr / dr;
       long long fxq = to_fix(s * dx), fyq = to_fix(s * dy), fzq = to_fix(s * dz);
       atomicAdd(&fix[3 * ia], (unsigned long long)(-fxq));
@@ -1022,19 +1029,24 @@ __global__ void k_mx_bonded(int nbond, int nbend, float3 sL, float3 rho,
       float dcx = fx_delta((unsigned)Cc.x, (unsigned)B.x, sL.x);
       float dcy = fx_delta((unsigned)Cc.y, (unsigned)B.y, sL.y);
       float dcz = fx_delta((unsigned)Cc.z, (unsigned)B.z, sL.z);
-      float drai = 1.f / sqrtf(dax * dax + day * day + daz * daz);
+      float drai = rsqrtf(dax * dax + day * day + daz * daz);
       float erax = dax * drai, eray = day * drai, eraz = daz * drai;
-      float drci = 1.f / sqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+      float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
       float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
-      float cosphi = erax * ercx + eray * ercy + eraz * ercz;
-      cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
-      float phi = acosf(cosphi);
+      const double pax = fx_delta_d((unsigned)A.x, (unsigned)B.x, sd.x);
+      const double pay = fx_delta_d((unsigned)A.y, (unsigned)B.y, sd.y);
+      const double paz = fx_delta_d((unsigned)A.z, (unsigned)B.z, sd.z);
+      const double pcx = fx_delta_d((unsigned)Cc.x, (unsigned)B.x, sd.x);
+      const double pcy = fx_delta_d((unsigned)Cc.y, (unsigned)B.y, sd.y);
+      const double pcz = fx_delta_d((unsigned)Cc.z, (unsigned)B.z, sd.z);
+      double cosd = (pax * pcx + pay * pcy + paz * pcz) /
+                    sqrt((pax * pax + pay * pay + paz * paz) * (pcx * pcx + pcy * pcy + pcz * pcz));
+      cosd = fmin(fmax(cosd, -1.0), 1.0);
+      const double rrd = acos(cosd) - bend_t0[u];
+      ea += bend_k[u] * rrd * rrd;
+      float cosphi = (float)cosd;
       float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
-      const double th0 = bend_t0[u];
-      const float t0 = (float)th0;
-      float rr = (phi - t0) - (float)(th0 - (double)t0);
-      float fr = -(float)bend_k[u] * rr * 2.f;
-      ea += -fr * rr * 0.5f;
+      float fr = -(float)bend_k[u] * (float)rrd * 2.f;
       float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
       float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
             fza = (eraz * cosphi - ercz) * irasin;
@@ -1053,7 +1065,7 @@ __global__ void k_mx_bonded(int nbond, int nbend, float3 sL, float3 rho,
       atomicAdd(&fix[3 * ic + 2], (unsigned long long)cz);
     }
   }
-  float v[2] = {eb, ea};
+  double v[2] = {eb, ea};
   block_fix_final<2>(v, 32, facc, ticket, out);
 }
 
@@ -1439,9 +1451,11 @@ __device__ __forceinline__ int intra_pick_i(const int (&v)[kIntraMaxSites], int 
 // The three kinds of intramolecular term, each adding to the molecule's
 // force registers F and the thread's energy sums A.
 struct IntraAcc {
-  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f, eb = 0.f, ea = 0.f;
+  float e_lj = 0.f, e_ljs = 0.f, e_real = 0.f, qsum = 0.f;
+  double eb = 0.0, ea = 0.0;  // bond and bend energies (FP64 geometry)
   long long q_intra = 0;
 };
+
 
 // excluded (xf 1-3) or 1-4 (xf 4) pair a-bq: the intra correction, and for
 // 1-4 pairs the scaled real-space term and LJ (cnonbond_nblist.c:245-263,
@@ -1488,51 +1502,61 @@ __device__ __forceinline__ void intra_excl(const int4 (&P)[NS], float (&F)[NS][3
   intra_add(F, bq, -Fs * dx, -Fs * dy, -Fs * dz);
 }
 
+// cbond.c:27: E = k (r - r0)^2.  The stretch and the energy in FP64 from
+// the exact fixed-point differences (a sum of ~1e5 small positive terms
+// keeps 1e-7 only if each stretch does: FP32 lengths carry ~1e-7 of r, a
+// few 1e-6 of r - r0); the force in FP32 along the FP32 bond vector.
 template <int NS>
 __device__ __forceinline__ void intra_bond(const int4 (&P)[NS], float (&F)[NS][3], int ia, int ib,
-                                           float req, float req_lo, float kb, float3 sL,
-                                           float3 rho, IntraAcc &A) {
+                                           double req, float kb, float3 sL, double3 sd,
+                                           IntraAcc &A) {
   const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib);
+  const double ex = fx_delta_d((unsigned)Pb.x, (unsigned)Pa.x, sd.x);
+  const double ey = fx_delta_d((unsigned)Pb.y, (unsigned)Pa.y, sd.y);
+  const double ez = fx_delta_d((unsigned)Pb.z, (unsigned)Pa.z, sd.z);
+  const double rr = sqrt(ex * ex + ey * ey + ez * ez) - req;
+  A.eb += (double)kb * rr * rr;
   float dx = fx_delta((unsigned)Pb.x, (unsigned)Pa.x, sL.x);
   float dy = fx_delta((unsigned)Pb.y, (unsigned)Pa.y, sL.y);
   float dz = fx_delta((unsigned)Pb.z, (unsigned)Pa.z, sL.z);
   float dr = sqrtf(dx * dx + dy * dy + dz * dz);
-  // the stretch r - r0 carries no bias of FP32 roundings: the length scale
-  // per axis is L / 2^32 = sL (1 + rho) and r0 = req + req_lo, so r - r0 =
-  // (dr - req) - req_lo + sum(d^2 rho) / dr to first order in rho
-  float rr = (dr - req) - req_lo + (dx * dx * rho.x + dy * dy * rho.y + dz * dz * rho.z) / dr;
-  float fr = -kb * rr * 2.f;
-  A.eb += -(fr * rr * 0.5f);
+  float fr = -kb * (float)rr * 2.f;
   float sc = fr / dr;
   intra_add(F, ia, -sc * dx, -sc * dy, -sc * dz);
   intra_add(F, ib, sc * dx, sc * dy, sc * dz);
 }
 
+// cbend.c:24: E = k (theta - theta0)^2.  The angle and the energy in FP64
+// (as the stretch above); the force in FP32 from the FP32 unit vectors.
 template <int NS>
 __device__ __forceinline__ void intra_bend(const int4 (&P)[NS], float (&F)[NS][3], int ia, int ib,
-                                           int ic, float t0, float t0_lo, float ka, float3 sL,
+                                           int ic, double t0, float ka, float3 sL, double3 sd,
                                            IntraAcc &A) {
   const int4 Pa = intra_pick(P, ia), Pb = intra_pick(P, ib), Pc = intra_pick(P, ic);
+  const double ax = fx_delta_d((unsigned)Pa.x, (unsigned)Pb.x, sd.x);
+  const double ay = fx_delta_d((unsigned)Pa.y, (unsigned)Pb.y, sd.y);
+  const double az = fx_delta_d((unsigned)Pa.z, (unsigned)Pb.z, sd.z);
+  const double cx = fx_delta_d((unsigned)Pc.x, (unsigned)Pb.x, sd.x);
+  const double cy = fx_delta_d((unsigned)Pc.y, (unsigned)Pb.y, sd.y);
+  const double cz = fx_delta_d((unsigned)Pc.z, (unsigned)Pb.z, sd.z);
+  double cosd = (ax * cx + ay * cy + az * cz) /
+                sqrt((ax * ax + ay * ay + az * az) * (cx * cx + cy * cy + cz * cz));
+  cosd = fmin(fmax(cosd, -1.0), 1.0);
+  const double rr = acos(cosd) - t0;
+  A.ea += (double)ka * rr * rr;
   float dax = fx_delta((unsigned)Pa.x, (unsigned)Pb.x, sL.x);
   float day = fx_delta((unsigned)Pa.y, (unsigned)Pb.y, sL.y);
   float daz = fx_delta((unsigned)Pa.z, (unsigned)Pb.z, sL.z);
   float dcx = fx_delta((unsigned)Pc.x, (unsigned)Pb.x, sL.x);
   float dcy = fx_delta((unsigned)Pc.y, (unsigned)Pb.y, sL.y);
   float dcz = fx_delta((unsigned)Pc.z, (unsigned)Pb.z, sL.z);
-  // correctly rounded lengths (the approximate reciprocal square root biases
-  // the angle by ~1e-7 rad, which the energy, a sum of (phi - t0)^2 terms of
-  // one sign of bias, does not average away)
-  float drai = 1.f / sqrtf(dax * dax + day * day + daz * daz);
+  float drai = rsqrtf(dax * dax + day * day + daz * daz);
   float erax = dax * drai, eray = day * drai, eraz = daz * drai;
-  float drci = 1.f / sqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+  float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
   float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
-  float cosphi = erax * ercx + eray * ercy + eraz * ercz;
-  cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
-  float phi = acosf(cosphi);
+  float cosphi = (float)cosd;
   float isinphi = rsqrtf(fmaxf(1.f - cosphi * cosphi, 1e-20f));
-  float rr = (phi - t0) - t0_lo;  // theta0 = t0 + t0_lo
-  float fr = -ka * rr * 2.f;
-  A.ea += -fr * rr * 0.5f;
+  float fr = -ka * (float)rr * 2.f;
   float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
   float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
         fza = (eraz * cosphi - ercz) * irasin;
@@ -1561,9 +1585,10 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
                            unsigned long long *__restrict__ facc, unsigned *__restrict__ ticket,
                            double *__restrict__ out, const IntraTpl &T = IntraTpl()) {
   IntraAcc A;
-  // relative rounding of the FP32 length scale per axis (L / 2^32 = hi + lo)
-  const float3 rho = make_float3(D.sl[0].y / D.sl[0].x, D.sl[1].y / D.sl[1].x,
-                                 D.sl[2].y / D.sl[2].x);
+  // the length scale per axis, L / 2^32, in FP64 (hi + lo)
+  const double3 sd = make_double3((double)D.sl[0].x + (double)D.sl[0].y,
+                                  (double)D.sl[1].x + (double)D.sl[1].y,
+                                  (double)D.sl[2].x + (double)D.sl[2].y);
   for (int m = vb_.id * blockDim.x + threadIdx.x; m < nmol; m += vb_.n * blockDim.x) {
     const int lb = UNI ? m * T.ns : mol_first[m];
     const int ns = UNI ? T.ns : mol_first[m + 1] - lb;
@@ -1599,49 +1624,45 @@ __device__ __forceinline__ void k_mx_intra_body(VBlk vb_, int nmol, const int *_
 #pragma unroll
     for (int t = tb0; t < tb1; t++) {
       int ia, ib;
-      float req, req_lo, kb;
+      double req;
+      float kb;
       if (UNI) {
         if (t >= T.nb) break;
         ia = T.ba[t];
         ib = T.bb[t];
-        req = T.breq[t];
-        req_lo = T.breq_lo[t];
+        req = (double)T.breq[t] + (double)T.breq_lo[t];
         kb = T.bk[t];
       } else {
         int u = mol_bi[t];
         ia = bond_ab[2 * u] - lb;
         ib = bond_ab[2 * u + 1] - lb;
-        const double r0 = bond_req[u];
-        req = (float)r0;
-        req_lo = (float)(r0 - (double)req);
+        req = bond_req[u];
         kb = (float)bond_k[u];
       }
-      intra_bond<NS>(P, F, ia, ib, req, req_lo, kb, sL, rho, A);
+      intra_bond<NS>(P, F, ia, ib, req, kb, sL, sd, A);
     }
     const int ta0 = UNI ? 0 : mol_a[m], ta1 = UNI ? kTplTerms : mol_a[m + 1];
 #pragma unroll
     for (int t = ta0; t < ta1; t++) {
       int ia, ib, ic;
-      float t0, t0_lo, ka;
+      double t0;
+      float ka;
       if (UNI) {
         if (t >= T.na) break;
         ia = T.aa[t];
         ib = T.ab[t];
         ic = T.ac[t];
-        t0 = T.at0[t];
-        t0_lo = T.at0_lo[t];
+        t0 = (double)T.at0[t] + (double)T.at0_lo[t];
         ka = T.ak[t];
       } else {
         int u = mol_ai[t];
         ia = bend_abc[3 * u] - lb;
         ib = bend_abc[3 * u + 1] - lb;
         ic = bend_abc[3 * u + 2] - lb;
-        const double th0 = bend_t0[u];
-        t0 = (float)th0;
-        t0_lo = (float)(th0 - (double)t0);
+        t0 = bend_t0[u];
         ka = (float)bend_k[u];
       }
-      intra_bend<NS>(P, F, ia, ib, ic, t0, t0_lo, ka, sL, A);
+      intra_bend<NS>(P, F, ia, ib, ic, t0, ka, sL, sd, A);
     }
 #pragma unroll
     for (int i = 0; i < NS; i++)
@@ -2295,9 +2316,10 @@ static int intra_on(Box *b, cudaStream_t st, unsigned long long *facc, unsigned 
     int bb = (tot + 255) / 256;
     if (bb > 1024) bb = 1024;
     if (bb < 1) bb = 1;
-    const float3 rho = make_float3(dfi.sl[0].y / dfi.sl[0].x, dfi.sl[1].y / dfi.sl[1].x,
-                                   dfi.sl[2].y / dfi.sl[2].x);
-    k_mx_bonded<<<bb, 256, 0, st>>>(b->nbond, b->nbend, sL, rho, M.posfx, M.iperm, b->bond_ab,
+    const double3 sd = make_double3((double)dfi.sl[0].x + (double)dfi.sl[0].y,
+                                    (double)dfi.sl[1].x + (double)dfi.sl[1].y,
+                                    (double)dfi.sl[2].x + (double)dfi.sl[2].y);
+    k_mx_bonded<<<bb, 256, 0, st>>>(b->nbond, b->nbend, sL, sd, M.posfx, M.iperm, b->bond_ab,
                                            b->bond_req, b->bond_k, b->bend_abc, b->bend_t0,
                                            b->bend_k, M.fix, facc, ticket,
                                            b->scal + SC_BOND);
