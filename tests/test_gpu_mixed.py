@@ -73,8 +73,9 @@ def test_mixed_force_error(case):
 
 def test_mixed_bonded_energies_relative():
     """Bond and bend energies of a perturbed (non-rigid) geometry: sums of
-    positive terms, within 1e-6 relative of the oracle (FP32 r - r0 loses
-    ~1e-7 of each stretch)."""
+    positive terms, within 1e-7 relative of the oracle (the stretch and the
+    angle are formed in FP64 from the fixed-point coordinates, whose
+    2e-8 A resolution is all that separates them from the oracle's)."""
     from thecodecombo_7_gb300 import systems
     s = systems.water_box(1365, density=0.1, seed=41)
     rng = np.random.default_rng(3)
@@ -85,15 +86,14 @@ def test_mixed_bonded_energies_relative():
         b.nblist()
         en = b.forces()
     for k in ("bond", "bend"):
-        assert abs(en[k] - en_ref[k]) <= 1e-6 * abs(en_ref[k]), (k, en[k], en_ref[k])
+        assert abs(en[k] - en_ref[k]) <= 1e-7 * abs(en_ref[k]), (k, en[k], en_ref[k])
 
 
 def test_mixed_bonded_energies_thermal():
     """Bond and bend energies of a thermalised box (400 NVE steps from the
     rigid start) against the FP64 oracle on the same coordinates: within
-    1e-7, the energy bar (the stretch and the angle carry no FP32 bias: theta0
-    and r0 as two floats, the length scale's rounding corrected, correctly
-    rounded lengths)."""
+    1e-7, the energy bar (stretch and angle in FP64 from the fixed-point
+    coordinates)."""
     from thecodecombo_7_gb300 import systems
     s = systems.water_box(1365, density=0.1, seed=43)
     with _mixed(s) as b:
