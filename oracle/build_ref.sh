@@ -9,6 +9,7 @@
 #   ref_harness_fast  the reference makefile's own flags (makefile:84-88:
 #                     -O3 -ffast-math -funroll-all-loops -std=c99), for timing
 #   ref_harness_dlist the strict build with -DDLIST (nl_check)
+#   ref_harness_go    the Go-model routines of cgolik.c (-DGOLIK)
 #
 # Feature flags: -DNLIST -DEWALD -DSPME -DSTYPE.  FFTW3 is not installed, so
 # the five FFTW symbols come from oracle/fftw_shim (the oracle's own FFT).
@@ -43,4 +44,8 @@ gcc -std=gnu99 -O2 -ffp-contract=off -DNLIST -DEWALD -DMC -DSTYPE -I"$REF" -w \
     -o "$OUT/ref_harness_mc" "$HERE/ref_harness.c" \
     "$REF/nblist.c" "$REF/setlj.c" "$REF/ewald.c" "$REF/ewald_mc.c" "$REF/cplx.c" \
     "$REF/enbnd_mc.c" -lm
-echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast, $OUT/ref_harness_dlist and $OUT/ref_harness_mc"
+# the reference's own Go model (-DGOLIK, no STYPE: cgolik.c reads the
+# per-box pair table ljset[k].pot[a][b]), strict IEEE
+gcc -std=gnu99 -O2 -ffp-contract=off -DGOLIK -DNLIST -I"$REF" -w \
+    -o "$OUT/ref_harness_go" "$HERE/ref_harness_go.c" "$REF/cgolik.c" -lm
+echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast, $OUT/ref_harness_dlist, $OUT/ref_harness_mc and $OUT/ref_harness_go"

@@ -1437,3 +1437,165 @@ double or_go_baoab(int N, double *pos, double *vel, int gbase, const int *nat_st
   free(f);
   return e;
 }
+
+/* ---- the reference's own Go model (cgolik.c) ---- */
+
+double or_go_hc_term(int N, const double *pos, int gbase, const int *nat_start, const int *nat_j,
+                     const double *nat_r0, const or_go_hc_params *p, const double *bond_r0,
+                     const double *bend_t0, int term, double *f, double *e2) {
+  const double eps = p->eps;
+  double e = 0.0;
+  for (int i = 0; i < 3 * N; i++) f[i] = 0.0;
+  if (term == 0) {  /* cbb_golik, cgolik.c:56-104 */
+    double k1 = -eps;
+    double k2 = k1 * 100;
+    for (int i = 0; i + 1 < N; i++) {
+      int ia = i, ib = i + 1;
+      double dx = pos[3 * ib] - pos[3 * ia];
+      double dy = pos[3 * ib + 1] - pos[3 * ia + 1];
+      double dz = pos[3 * ib + 2] - pos[3 * ia + 2];
+      double drr = dx * dx + dy * dy + dz * dz;
+      double dr = sqrt(drr);
+      double dri = 1.0 / dr;
+      double rr = dr - bond_r0[i];
+      double rr2 = rr * rr;
+      double fr1 = k1 * rr * 2.0;
+      double fr2 = k2 * rr * rr2 * 4.0;
+      e += -rr * (fr1 * 0.5 + fr2 * 0.25);
+      double fr = fr1 + fr2;
+      double fx = fr * dri * dx, fy = fr * dri * dy, fz = fr * dri * dz;
+      f[3 * ia] -= fx; f[3 * ia + 1] -= fy; f[3 * ia + 2] -= fz;
+      f[3 * ib] += fx; f[3 * ib + 1] += fy; f[3 * ib + 2] += fz;
+    }
+  } else if (term == 1) {  /* cba_golik, cgolik.c:204-296 (k_theta = -10 eps) */
+    double k_theta = -10.0 * eps;
+    for (int i = 0; i + 2 < N; i++) {
+      int ia = i, ib = i + 1, ic = i + 2;
+      double dax = pos[3 * ia] - pos[3 * ib], day = pos[3 * ia + 1] - pos[3 * ib + 1],
+             daz = pos[3 * ia + 2] - pos[3 * ib + 2];
+      double dcx = pos[3 * ic] - pos[3 * ib], dcy = pos[3 * ic + 1] - pos[3 * ib + 1],
+             dcz = pos[3 * ic + 2] - pos[3 * ib + 2];
+      double drai = 1.0 / sqrt(dax * dax + day * day + daz * daz);
+      double erax = dax * drai, eray = day * drai, eraz = daz * drai;
+      double drci = 1.0 / sqrt(dcx * dcx + dcy * dcy + dcz * dcz);
+      double ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
+      double cosphi = erax * ercx + eray * ercy + eraz * ercz;
+      double phi = acos(cosphi);
+      double isinphi = 1.0 / sqrt(1.0 - cosphi * cosphi);
+      double rr = phi - bend_t0[i];
+      double fr = k_theta * rr * 2.0;
+      e += -fr * rr * 0.5;
+      double irasin = drai * isinphi * fr;
+      double ircsin = drci * isinphi * fr;
+      double fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
+             fza = (eraz * cosphi - ercz) * irasin;
+      double fxc = (ercx * cosphi - erax) * ircsin, fyc = (ercy * cosphi - eray) * ircsin,
+             fzc = (ercz * cosphi - eraz) * ircsin;
+      f[3 * ia] += fxa; f[3 * ia + 1] += fya; f[3 * ia + 2] += fza;
+      f[3 * ib] += -(fxa + fxc); f[3 * ib + 1] += -(fya + fyc); f[3 * ib + 2] += -(fza + fzc);
+      f[3 * ic] += fxc; f[3 * ic + 1] += fyc; f[3 * ic + 2] += fzc;
+    }
+  } else if (term == 2) {  /* cda_golik, cgolik.c:399-610 (k_phi = 0.2 eps, 3-fold) */
+    double k_phi = 0.2 * eps;
+    for (int i = 0; i + 3 < N; i++) {
+      int ia = i, ib = i + 1, ic = i + 2, id = i + 3;
+      double dabx = pos[3 * ib] - pos[3 * ia], daby = pos[3 * ib + 1] - pos[3 * ia + 1],
+             dabz = pos[3 * ib + 2] - pos[3 * ia + 2];
+      double dbcx = pos[3 * ic] - pos[3 * ib], dbcy = pos[3 * ic + 1] - pos[3 * ib + 1],
+             dbcz = pos[3 * ic + 2] - pos[3 * ib + 2];
+      double dcdx = pos[3 * id] - pos[3 * ic], dcdy = pos[3 * id + 1] - pos[3 * ic + 1],
+             dcdz = pos[3 * id + 2] - pos[3 * ic + 2];
+      double rab = sqrt(dabx * dabx + daby * daby + dabz * dabz);
+      double irab = 1.0 / rab;
+      double erabx = dabx * irab, eraby = daby * irab, erabz = dabz * irab;
+      double rbc = sqrt(dbcx * dbcx + dbcy * dbcy + dbcz * dbcz);
+      double irbc = 1.0 / rbc;
+      double erbcx = dbcx * irbc, erbcy = dbcy * irbc, erbcz = dbcz * irbc;
+      double rcd = sqrt(dcdx * dcdx + dcdy * dcdy + dcdz * dcdz);
+      double ircd = 1.0 / rcd;
+      double ercdx = dcdx * ircd, ercdy = dcdy * ircd, ercdz = dcdz * ircd;
+      double abbcx = eraby * erbcz - erabz * erbcy;
+      double abbcy = erabz * erbcx - erabx * erbcz;
+      double abbcz = erabx * erbcy - eraby * erbcx;
+      double cosb = -(erabx * erbcx + eraby * erbcy + erabz * erbcz);
+      double isinb2 = 1.0 / (1.0 - cosb * cosb);
+      double isinb = sqrt(isinb2);
+      double dccbx = ercdy * erbcz - ercdz * erbcy;
+      double dccby = ercdz * erbcx - ercdx * erbcz;
+      double dccbz = ercdx * erbcy - ercdy * erbcx;
+      double cosc = -(ercdx * erbcx + ercdy * erbcy + ercdz * erbcz);
+      double isinc2 = 1.0 / (1.0 - cosc * cosc);
+      double isinc = sqrt(isinc2);
+      double abcdx = -(abbcy * dccbz - abbcz * dccby);
+      double abcdy = -(abbcz * dccbx - abbcx * dccbz);
+      double abcdz = -(abbcx * dccby - abbcy * dccbx);
+      double num = (abcdx * erbcx + abcdy * erbcy + abcdz * erbcz);
+      double signum = num >= 0.0 ? 1.0 : -1.0;
+      double costau = -(abbcx * dccbx + abbcy * dccby + abbcz * dccbz) * isinb * isinc;
+      if (costau > 1.0) costau = 1.0;
+      if (costau < -1.0) costau = -1.0;
+      double tau = signum * acos(costau);
+      double fr = k_phi * 3.0 * (sin(3.0 * tau - 0.0));
+      e += k_phi * (1 + cos(3.0 * tau - 0.0));
+      double fa = -fr * irab * isinb2;
+      f[3 * ia] += fa * abbcx; f[3 * ia + 1] += fa * abbcy; f[3 * ia + 2] += fa * abbcz;
+      double fb1 = fr * (rbc - rab * cosb) * irab * irbc * isinb2;
+      double fb2 = fr * cosc * irbc * isinc2;
+      f[3 * ib] += (fb1 * abbcx + fb2 * dccbx);
+      f[3 * ib + 1] += (fb1 * abbcy + fb2 * dccby);
+      f[3 * ib + 2] += (fb1 * abbcz + fb2 * dccbz);
+      double fc1 = fr * (rbc - rcd * cosc) * ircd * irbc * isinc2;
+      double fc2 = fr * cosb * irbc * isinb2;
+      f[3 * ic] += fc1 * dccbx + fc2 * abbcx;
+      f[3 * ic + 1] += fc1 * dccby + fc2 * abbcy;
+      f[3 * ic + 2] += fc1 * dccbz + fc2 * abbcz;
+      double fd = -fr * ircd * isinc2;
+      f[3 * id] += fd * dccbx; f[3 * id + 1] += fd * dccby; f[3 * id + 2] += fd * dccbz;
+    }
+  } else {  /* cnbnd_golik, cgolik.c:644-948 (protein sites, no solvent) */
+    const double factor = pow(2.0, -(1.0 / 6.0));
+    double rc2 = p->rc * p->rc, rc2_rep = p->d_rep * p->d_rep;
+    double enonbond = 0.0, enonbonds = 0.0, enonnative = 0.0;
+    for (int a = 0; a < N - 1; a++) {
+      double fxa = 0.0, fya = 0.0, fza = 0.0;
+      double ax = pos[3 * a], ay = pos[3 * a + 1], az = pos[3 * a + 2];
+      for (int b = a + 1; b < N; b++) {
+        double dx = ax - pos[3 * b], dy = ay - pos[3 * b + 1], dz = az - pos[3 * b + 2];
+        double dr2 = dx * dx + dy * dy + dz * dz;
+        if (dr2 > rc2) continue;
+        int flag = 0;
+        double sig = factor * p->d_rep, pe = eps;
+        for (int q = nat_start[gbase + a]; q < nat_start[gbase + a + 1]; q++)
+          if (nat_j[q] == gbase + b) { flag = 1; sig = factor * nat_r0[q]; }
+        if (b == a + 1) { flag = 0; sig = 0.0; pe = 0.0; }  /* read_golik.c:99-110 */
+        if (flag == 0 && dr2 > rc2_rep) continue;
+        double force = 0.0;
+        if ((pe * sig) != 0.0) {
+          double sr2 = (sig * sig) / dr2, sr6 = sr2 * sr2 * sr2, sr12 = sr6 * sr6;
+          double sr2s = (sig * sig) / rc2, sr6s = sr2s * sr2s * sr2s, sr12s = sr6s * sr6s;
+          force = (48.0 * pe / dr2) * (sr12 - 0.5 * sr6);
+          double enbnd = 4.0 * pe * (sr12 - sr6);
+          double enbnds = 4.0 * pe * (sr12s - sr6s);
+          if (flag == 0) {
+            enonnative += (enbnd + pe);
+          } else {
+            enonbond += enbnd;
+            enonbonds += enbnds;
+          }
+        }
+        if (force != 0.0) {
+          double fx = force * dx, fy = force * dy, fz = force * dz;
+          fxa += fx; fya += fy; fza += fz;
+          f[3 * b] -= fx; f[3 * b + 1] -= fy; f[3 * b + 2] -= fz;
+        }
+      }
+      f[3 * a] += fxa; f[3 * a + 1] += fya; f[3 * a + 2] += fza;
+    }
+    if (e2) {
+      e2[0] = enonbond + enonnative;
+      e2[1] = enonbond - enonbonds + enonnative;
+    }
+    e = enonbond - enonbonds + enonnative;
+  }
+  return e;
+}

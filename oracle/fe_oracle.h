@@ -221,6 +221,25 @@ double or_go_baoab(int N, double *pos, double *vel, int gbase, const int *nat_st
                    const int *nat_j, const double *nat_r0, const or_go_params *p, double T,
                    uint64_t seed, uint64_t step0, int nsteps);
 
+/* The reference's own Go model (cgolik.c, GOLIK build, protein sites only,
+ * no periodic images): bonds E = eps dr^2 + 100 eps dr^4 (cbb_golik,
+ * cgolik.c:25-174), bends E = 10 eps (theta - theta0)^2 (cba_golik,
+ * :176-367), torsions E = 0.2 eps (1 + cos 3 tau) (cda_golik, :369-641, GOBT
+ * phases zero), natives 4 eps [(s/r)^12 - (s/r)^6] with s = 2^(-1/6) r0
+ * shifted at rc, non-natives the same with s = 2^(-1/6) d_rep cut at d_rep
+ * and lifted by eps (cnbnd_golik, :644-948); bonded pairs excluded.
+ * term: 0 bonds, 1 bends, 2 torsions, 3 pairs (then e2 = {energy[0],
+ * energy[1]} of cnbnd_golik: unshifted and shifted).  Forces into f (3N,
+ * overwritten); returns the term's energy (shifted for pairs). */
+typedef struct {
+  double eps;    /* kJ/mol */
+  double d_rep;  /* non-native cut [A] */
+  double rc;     /* native cutoff [A] */
+} or_go_hc_params;
+double or_go_hc_term(int N, const double *pos, int gbase, const int *nat_start, const int *nat_j,
+                     const double *nat_r0, const or_go_hc_params *p, const double *bond_r0,
+                     const double *bend_t0, int term, double *f, double *e2);
+
 #ifdef __cplusplus
 }
 #endif

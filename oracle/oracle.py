@@ -24,6 +24,7 @@ REF_BIN = os.path.join(HERE, "_ref", "ref_harness")
 REF_BIN_FAST = os.path.join(HERE, "_ref", "ref_harness_fast")
 REF_BIN_DLIST = os.path.join(HERE, "_ref", "ref_harness_dlist")
 REF_BIN_MC = os.path.join(HERE, "_ref", "ref_harness_mc")
+REF_BIN_GO = os.path.join(HERE, "_ref", "ref_harness_go")
 
 # strict IEEE: no FMA contraction, no fast-math, so results are reproducible
 # on x86-64 and aarch64 alike and match a strict build of the reference
@@ -587,3 +588,77 @@ def nl_check(pos, pos0, L, rclist, rc, lb=0, ub=None):
         if d[0] * d[0] + d[1] * d[1] + d[2] * d[2] > rcut * rcut:
             return 1
     return 0
+
+
+# ---- the reference's own Go model (cgolik.c) ----
+
+class OrGoHcParams(C.Structure):
+    _fields_ = [("eps", C.c_double), ("d_rep", C.c_double), ("rc", C.c_double)]
+
+
+def go_native_geometry(g, r):
+    """Bond lengths (N-1) and bend angles (N-2) of replica r's native
+    structure (its starting coordinates), as set_go_params takes them
+    (read_golik.c:300-355 with GOBT)."""
+    a, b = int(g.start[r]), int(g.start[r + 1])
+    x = np.asarray(g.pos[a:b], np.float64)
+    d = x[1:] - x[:-1]
+    r0 = np.sqrt((d * d).sum(axis=1))
+    u, v = -d[:-1], d[1:]
+    cos = (u * v).sum(axis=1) / np.sqrt((u * u).sum(axis=1) * (v * v).sum(axis=1))
+    return r0, np.arccos(cos)
+
+
+def go_hc_terms(g, r, hc, pos=None):
+    """The four terms of the reference's Go model (or_go_hc_term) of replica
+    r: dict of forces (N, 3) and energies per term (pairs: shifted, and
+    e_nb2 = (unshifted, shifted))."""
+    L = _go_lib()
+    L.or_go_hc_term.restype = C.c_double
+    a, b = int(g.start[r]), int(g.start[r + 1])
+    x = np.ascontiguousarray(g.pos[a:b] if pos is None else pos, np.float64)
+    ns = np.ascontiguousarray(g.nat_start, np.int32)
+    nj = np.ascontiguousarray(g.nat_j, np.int32)
+    r0 = np.ascontiguousarray(g.nat_r0, np.float64)
+    br0, bt0 = (np.ascontiguousarray(v) for v in go_native_geometry(g, r))
+    p = OrGoHcParams(*hc)
+    out = {}
+    for t, name in enumerate(("bond", "bend", "tors", "nb")):
+        f = np.zeros((b - a, 3))
+        e2 = np.zeros(2)
+        out["e_" + name] = L.or_go_hc_term(b - a, _p(x), a, _p(ns), _p(nj), _p(r0), C.byref(p),
+                                           _p(br0), _p(bt0), t, _p(f), _p(e2))
+        out["f_" + name] = f
+        if name == "nb":
+            out["e_nb2"] = e2
+    return out
+
+
+def run_reference_go(g, r, hc, workdir, pos=None, L_box=1.0e4):
+    """The reference's own cbb_golik / cba_golik / cda_golik / cnbnd_golik
+    (oracle/_ref/ref_harness_go) on replica r with parameters hc = (eps,
+    d_rep, rc), at pos (default: the native structure, whose geometry sets
+    the bond lengths and bend angles either way)."""
+    os.makedirs(workdir, exist_ok=True)
+    a, b = int(g.start[r]), int(g.start[r + 1])
+    N = b - a
+    br0, bt0 = go_native_geometry(g, r)
+    pairs = []
+    for i in range(N):
+        for q in range(int(g.nat_start[a + i]), int(g.nat_start[a + i + 1])):
+            j = int(g.nat_j[q]) - a
+            if j > i:
+                pairs.append((i, j, float(g.nat_r0[q])))
+    sp = os.path.join(workdir, "go.bin")
+    op = os.path.join(workdir, "out_go.bin")
+    with open(sp, "wb") as f:
+        f.write(struct.pack("<i", N))
+        f.write(struct.pack("<4d", L_box, hc[0], hc[1], hc[2]))
+        f.write(np.ascontiguousarray(g.pos[a:b] if pos is None else pos, "<f8").tobytes())
+        f.write(np.ascontiguousarray(br0, "<f8").tobytes())
+        f.write(np.ascontiguousarray(bt0, "<f8").tobytes())
+        f.write(struct.pack("<i", len(pairs)))
+        for i, j, r0 in pairs:
+            f.write(struct.pack("<iid", i, j, r0))
+    subprocess.check_call([REF_BIN_GO, sp, op])
+    return read_tagged(op)

@@ -41,6 +41,12 @@ def golden_mts600():
 
 
 @pytest.fixture(scope="session")
+def golden_go_hc():
+    import numpy as np
+    return dict(np.load(os.path.join(GOLDEN, "go_hc.npz")))
+
+
+@pytest.fixture(scope="session")
 def golden_chain():
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, "chain900.npz")))

@@ -102,6 +102,7 @@ def main():
     make_drift(tmp)
     make_chain(tmp)
     make_mts_water(tmp)
+    make_go_hc(tmp)
     print("golden fixtures written to", HERE)
 
 
@@ -201,6 +202,24 @@ def make_mts_water(tmp):
     np.savez_compressed(os.path.join(HERE, "mts_water600.npz"), **out)
 
 
+def make_go_hc(tmp):
+    """The reference's own Go model (cgolik.c) on three chains of 60-150
+    beads at perturbed coordinates: forces and energies per term."""
+    g = systems.go_chains(3, nmin=60, nmax=150, seed=31)
+    rng = np.random.default_rng(8)
+    hc = (g.eps, 4.0, 12.0)  # eps, d_repulsive, rc
+    out = dict(nbeads=g.nbeads, pos0=g.pos, nat_start=g.nat_start, nat_j=g.nat_j,
+               nat_r0=g.nat_r0, hc=np.array(hc))
+    pos = g.pos + rng.normal(0.0, 0.15, g.pos.shape)
+    out["pos"] = pos
+    for r in range(len(g.nbeads)):
+        a, b = int(g.start[r]), int(g.start[r + 1])
+        ref = O.run_reference_go(g, r, hc, tmp, pos=pos[a:b])
+        for k, v in ref.items():
+            out[f"r{r}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, "go_hc.npz"), **out)
+
+
 def make_drift(tmp):
     s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27), helper=False)
     s.vel = s.vel + np.array([0.7, -0.4, 0.25])
@@ -221,11 +240,11 @@ def make_nlcheck(tmp):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"], ["mts"]):  # this fixture alone
+    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"], ["mts"], ["go"]):  # alone
         if not O.build_reference():
             raise SystemExit("reference sources not available")
         {"nlcheck": make_nlcheck, "mc": make_mc, "drift": make_drift,
-         "chain": make_chain, "mts": make_mts_water}[sys.argv[1]](
+         "chain": make_chain, "mts": make_mts_water, "go": make_go_hc}[sys.argv[1]](
             tempfile.mkdtemp(prefix="fe_golden_"))
     else:
         main()

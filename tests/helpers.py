@@ -54,3 +54,17 @@ def chain_from_golden(g):
                        grid=tuple(int(x) for x in g["grid"]), **kw)
     s.nlist_freq = int(g["nlist_freq"])
     return s
+
+
+def go_from_golden(g):
+    """The chains of go_hc.npz (native structure as the starting coordinates,
+    velocities zero, temperatures 300 K) and the perturbed coordinates the
+    reference's terms were evaluated at."""
+    nb = np.asarray(g["nbeads"], np.int32)
+    n = int(nb.sum())
+    chains = systems.GoChains(nbeads=nb, pos=np.ascontiguousarray(g["pos0"]),
+                              vel=np.zeros((n, 3)), nat_start=np.asarray(g["nat_start"], np.int32),
+                              nat_j=np.asarray(g["nat_j"], np.int32),
+                              nat_r0=np.asarray(g["nat_r0"], np.float64),
+                              T=np.full(len(nb), 300.0))
+    return chains, np.ascontiguousarray(g["pos"]), tuple(float(x) for x in g["hc"])

@@ -68,3 +68,23 @@ def test_go_oracle_verlet_limit_is_second_order():
         x, v, e1 = O.go_baoab(g, 1, int(round(0.2 / dt)), seed=1)
         errs.append(abs(e1 + ke(v) - e0))
     assert errs[1] < errs[0] / 3.0, errs
+
+
+def test_reference_go_model_pinned(golden_go_hc):
+    """The restatement of the reference's own Go model (or_go_hc_term:
+    cbb_golik, cba_golik, cda_golik, cnbnd_golik of cgolik.c) against the
+    reference's routines run on the same chains (tests/golden/go_hc.npz):
+    forces and energies of every term bit for bit."""
+    from oracle import oracle as O
+    from tests.helpers import go_from_golden
+    g = golden_go_hc
+    chains, pos, hc = go_from_golden(g)
+    for r in range(len(chains.nbeads)):
+        a, b = int(chains.start[r]), int(chains.start[r + 1])
+        mine = O.go_hc_terms(chains, r, hc, pos=pos[a:b])
+        for name in ("bond", "bend", "tors", "nb"):
+            np.testing.assert_array_equal(mine["f_" + name].ravel(), g[f"r{r}_f_{name}"])
+        en = g[f"r{r}_en"]
+        assert mine["e_bond"] == en[0] and mine["e_bend"] == en[1] and mine["e_tors"] == en[2]
+        assert mine["e_nb2"][0] == en[3] and mine["e_nb2"][1] == en[4]
+        assert np.abs(g[f"r{r}_f_bond"]).max() > 0 and np.abs(g[f"r{r}_f_bend"]).max() > 0
