@@ -494,6 +494,16 @@ int fe_go_forces(fe_go *go, double *f, double *epot);
 int fe_go_state(fe_go *go, double *pos, double *vel, double *T, double *epot, int *slot_rep,
                 int64_t *accepted, int64_t *attempted, uint64_t *steps);
 int fe_go_get_stream(fe_go *go, void **stream);
+/* Switches the batch to the reference's own Go model (cgolik.c): bonds
+ * eps dr^2 + 100 eps dr^4 with bond_r0[i] the length of bond (i, i+1)
+ * (global bead index; the last bead of a chain unused), bends
+ * 10 eps (theta - theta0)^2 with bend_t0[i] the angle centred at bead i,
+ * torsions 0.2 eps (1 + cos 3 tau), natives 4 eps [(s/r)^12 - (s/r)^6] with
+ * s = 2^(-1/6) r0 within rc (energy shifted to zero there), non-natives the
+ * same with s = 2^(-1/6) d_rep within d_rep, lifted by eps; only bonded
+ * pairs excluded. */
+int fe_go_set_reference_form(fe_go *go, const double *bond_r0, const double *bend_t0,
+                             double d_rep, double rc);
 /* The launch's load-balance plan: *ncta CTAs (clusters of four), *slots the
  * CTAs the GPU holds at once, parts[r] (nrep ints, may be NULL) the CTAs
  * that share replica r's chain (1 to 4). */

@@ -1599,3 +1599,48 @@ double or_go_hc_term(int N, const double *pos, int gbase, const int *nat_start, 
   }
   return e;
 }
+
+static double go_hc_all(int N, const double *pos, int gbase, const int *nat_start,
+                        const int *nat_j, const double *nat_r0, const or_go_hc_params *hc,
+                        const double *bond_r0, const double *bend_t0, double *f) {
+  double *t = (double *)malloc(sizeof(double) * 3 * (size_t)N);
+  double e = 0.0;
+  for (int i = 0; i < 3 * N; i++) f[i] = 0.0;
+  for (int term = 0; term < 4; term++) {
+    e += or_go_hc_term(N, pos, gbase, nat_start, nat_j, nat_r0, hc, bond_r0, bend_t0, term, t,
+                       NULL);
+    for (int i = 0; i < 3 * N; i++) f[i] += t[i];
+  }
+  free(t);
+  return e;
+}
+
+double or_go_baoab_hc(int N, double *pos, double *vel, int gbase, const int *nat_start,
+                      const int *nat_j, const double *nat_r0, const or_go_params *p,
+                      const or_go_hc_params *hc, const double *bond_r0, const double *bend_t0,
+                      double T, uint64_t seed, uint64_t step0, int nsteps) {
+  /* the B A O A B sequence of or_go_baoab with these forces */
+  double *f = (double *)malloc(sizeof(double) * 3 * (size_t)N);
+  double e = go_hc_all(N, pos, gbase, nat_start, nat_j, nat_r0, hc, bond_r0, bend_t0, f);
+  double c1 = exp(-p->gamma * p->dt), c2 = sqrt(1.0 - c1 * c1);
+  double kT = ((KB_ * NA_) * T) * .001;
+  double sv = sqrt(100.0 / p->mass) * sqrt(kT) * c2;
+  double hdt = 0.5 * p->dt, ha = 0.5 * p->dt * (100.0 / p->mass);
+  for (int s = 0; s < nsteps; s++) {
+    for (int i = 0; i < N; i++) {
+      double z[3];
+      go_normals(seed, (uint32_t)(gbase + i), step0 + (uint64_t)s, z);
+      for (int a = 0; a < 3; a++) {
+        double v = vel[3 * i + a] + ha * f[3 * i + a];
+        double x = pos[3 * i + a] + hdt * v;
+        v = c1 * v + sv * z[a];
+        pos[3 * i + a] = x + hdt * v;
+        vel[3 * i + a] = v;
+      }
+    }
+    e = go_hc_all(N, pos, gbase, nat_start, nat_j, nat_r0, hc, bond_r0, bend_t0, f);
+    for (int i = 0; i < 3 * N; i++) vel[i] += ha * f[i];
+  }
+  free(f);
+  return e;
+}

@@ -239,6 +239,13 @@ typedef struct {
 double or_go_hc_term(int N, const double *pos, int gbase, const int *nat_start, const int *nat_j,
                      const double *nat_r0, const or_go_hc_params *p, const double *bond_r0,
                      const double *bend_t0, int term, double *f, double *e2);
+/* or_go_baoab with the forces of the reference's Go model (the sum of the
+ * four terms above; the potential energy returned is that sum, pairs
+ * shifted). */
+double or_go_baoab_hc(int N, double *pos, double *vel, int gbase, const int *nat_start,
+                      const int *nat_j, const double *nat_r0, const or_go_params *p,
+                      const or_go_hc_params *hc, const double *bond_r0, const double *bend_t0,
+                      double T, uint64_t seed, uint64_t step0, int nsteps);
 
 #ifdef __cplusplus
 }

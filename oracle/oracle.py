@@ -662,3 +662,29 @@ def run_reference_go(g, r, hc, workdir, pos=None, L_box=1.0e4):
             f.write(struct.pack("<iid", i, j, r0))
     subprocess.check_call([REF_BIN_GO, sp, op])
     return read_tagged(op)
+
+
+def go_hc_forces(g, r, hc, pos=None):
+    """(forces (N, 3), potential energy) of replica r under the reference's
+    Go model: the sum of the four terms."""
+    t = go_hc_terms(g, r, hc, pos)
+    f = t["f_bond"] + t["f_bend"] + t["f_tors"] + t["f_nb"]
+    return f, t["e_bond"] + t["e_bend"] + t["e_tors"] + t["e_nb"]
+
+
+def go_hc_baoab(g, r, hc, nsteps, seed, step0=0):
+    """nsteps Langevin steps of replica r under the reference's Go model;
+    returns (pos, vel, final potential)."""
+    L = _go_lib()
+    L.or_go_baoab_hc.restype = C.c_double
+    a, b = int(g.start[r]), int(g.start[r + 1])
+    x = np.ascontiguousarray(g.pos[a:b], np.float64).copy()
+    v = np.ascontiguousarray(g.vel[a:b], np.float64).copy()
+    ns = np.ascontiguousarray(g.nat_start, np.int32)
+    nj = np.ascontiguousarray(g.nat_j, np.int32)
+    r0 = np.ascontiguousarray(g.nat_r0, np.float64)
+    br0, bt0 = (np.ascontiguousarray(w) for w in go_native_geometry(g, r))
+    e = L.or_go_baoab_hc(b - a, _p(x), _p(v), a, _p(ns), _p(nj), _p(r0), C.byref(_go_params(g)),
+                         C.byref(OrGoHcParams(*hc)), _p(br0), _p(bt0), C.c_double(g.T[r]),
+                         C.c_uint64(seed), C.c_uint64(step0), int(nsteps))
+    return x, v, e

@@ -139,3 +139,58 @@ def test_go_extreme_chain_lengths(nrep, nb):
         x, v, eo = O.go_baoab(g, r, 10, seed=4)
         assert np.abs(s["pos"][st[r]:st[r + 1]] - x).max() < 1e-4, r
         assert np.abs(s["vel"][st[r]:st[r + 1]] - v).max() < 1e-2, r
+
+
+
+def test_reference_form_vs_reference(golden_go_hc):
+    """The reference's own Go model on the device (fe_go_set_reference_form)
+    against the reference's cgolik.c routines run on the same chains at the
+    same perturbed coordinates (tests/golden/go_hc.npz): forces (FP32) to
+    1e-5 rms, energy to 1e-5."""
+    import dataclasses
+    from thecodecombo_7_gb300 import engine
+    from tests.helpers import go_from_golden
+    g = golden_go_hc
+    chains, pos, hc = go_from_golden(g)
+    moved = dataclasses.replace(chains, pos=pos)
+    b = engine.GoBatch(moved, seed=1)
+    try:
+        b.set_reference_form(d_rep=hc[1], rc=hc[2], native=chains.pos)
+        f, e = b.forces()
+    finally:
+        b.close()
+    st = chains.start
+    for r in range(len(chains.nbeads)):
+        want = sum(g[f"r{r}_f_{t}"] for t in ("bond", "bend", "tors", "nb")).reshape(-1, 3)
+        got = f[st[r]:st[r + 1]]
+        rms = np.sqrt(((got - want) ** 2).sum() / (want ** 2).sum())
+        assert rms <= 1e-5, (r, rms)
+        en = g[f"r{r}_en"]
+        e_ref = en[0] + en[1] + en[2] + en[4]
+        assert abs(e[r] - e_ref) <= 1e-5 * max(abs(e_ref), 1.0), (r, e[r], e_ref)
+
+
+def test_reference_form_trajectory_matches_oracle():
+    """10 BAOAB steps under the reference's Go model against the oracle's
+    (pinned to cgolik.c) with the same Philox draws (measured: positions
+    within 1.8e-5 A, velocities 3.8e-4 A/ps, energies 4e-7).  Over 25 steps
+    one of these chains passes a nearly straight torsion, where the FP32
+    torsion force (~3e-5 of the force elsewhere) departs further and moves
+    the chain 3e-3 A from the FP64 trajectory; the other chains stay within
+    4e-5 A."""
+    from thecodecombo_7_gb300 import engine, systems
+    g = systems.go_chains(5, nmin=40, nmax=160, seed=12)
+    hc = (g.eps, 4.0, 12.0)
+    b = engine.GoBatch(g, seed=6)
+    try:
+        b.set_reference_form(d_rep=hc[1], rc=hc[2])
+        b.run(10)
+        s = b.state()
+    finally:
+        b.close()
+    st = g.start
+    for r in range(len(g.nbeads)):
+        x, v, e = O.go_hc_baoab(g, r, hc, 10, seed=6)
+        assert np.abs(s["pos"][st[r]:st[r + 1]] - x).max() < 1e-4, r
+        assert np.abs(s["vel"][st[r]:st[r + 1]] - v).max() < 2e-3, r
+        assert abs(s["epot"][r] - e) <= 1e-5 * max(abs(e), 1.0), (r, s["epot"][r], e)

@@ -39,6 +39,11 @@
 //     formed in FP32), xi Gaussian by Box-Muller from Philox4x32-10 draws
 //     keyed by (bead, step); the closing B of one step and the opening B of
 //     the next are one kick of 2 (dt/2) f / m;
+//   - a second energy function, the reference's own Go model (cgolik.c,
+//     fe_go_set_reference_form): bonds eps dr^2 + 100 eps dr^4, bends
+//     10 eps (theta - theta0)^2, three-fold torsions, natives 12-6 cut and
+//     shifted at rc, non-natives WCA within d_rep; each bead computes the
+//     bends and torsions that move it (the kernel is a template on the form);
 //   - after the segment, one exchange kernel: adjacent temperature slots as
 //     swap_box does (pairs alternate between attempts), acceptance
 //     exp((1/kT_s - 1/kT_s+1)(U_s - U_s+1)) > u, velocity rescale by
@@ -69,7 +74,15 @@ struct GoCta {
 
 struct GoK {
   float eps, sig2, rc2, e_shift, kb, r0b;
-  float c12, f12;   // eps sigma^12 and 12 eps sigma^12 of the repulsion
+  // the non-native pair within rc2: E = c12/r^12 - c6/r^6 + e0, force
+  // (f12/r^12 - f6/r^6)/r^2 along the separation
+  float c12, f12, c6, f6, e0;
+  // form 1, the reference's own model (cgolik.c): natives 12-6 with
+  // sigma^2 = 2^(-1/3) r0^2 cut and shifted at rc2n; bonds with a quartic
+  // term kq (r - r0)^4 and per-bond r0; bends kth (theta - theta0)^2;
+  // torsions kph (1 + cos 3 tau)
+  int form;
+  float rc2n, kq, kth, kph;
   double acc_fac;   // 100 / m: kJ/mol/A per amu -> A/ps^2
   double dt, c1, c2;
   double vscale;    // sqrt(100 / m): sqrt(kT [kJ/mol]) -> A/ps
@@ -87,6 +100,8 @@ struct GoD {
   const int *nat_start;  // total + 1 (CSR over global bead index)
   const int *nat_j;      // global partner index
   const float *nat_r02;  // native distance squared
+  const float *bond_r0;  // form 1: length of bond (i, i+1) per global bead i
+  const float *bend_t0;  // form 1: angle centred at global bead i
   double *x, *v;         // 3 * total
   float *f;              // 3 * total (fe_go_forces)
   double *T;             // nrep: current temperature of each replica
@@ -99,13 +114,107 @@ struct GoD {
   unsigned long long *attempt;
 };
 
+// The bend (c - 1, c, c + 1) of the reference's Go model (cba_golik,
+// cgolik.c:204-296: E = kth (theta - theta0)^2): the force on its site
+// `which` (0, 1, 2) added to f, the energy returned.
+__device__ __forceinline__ float go_bend(const float4 *__restrict__ p, int c, float t0, float kth,
+                                         int which, float &fx, float &fy, float &fz) {
+  const float4 A = p[c - 1], B = p[c], C = p[c + 1];
+  const float dax = A.x - B.x, day = A.y - B.y, daz = A.z - B.z;
+  const float dcx = C.x - B.x, dcy = C.y - B.y, dcz = C.z - B.z;
+  const float drai = rsqrtf(dax * dax + day * day + daz * daz);
+  const float erax = dax * drai, eray = day * drai, eraz = daz * drai;
+  const float drci = rsqrtf(dcx * dcx + dcy * dcy + dcz * dcz);
+  const float ercx = dcx * drci, ercy = dcy * drci, ercz = dcz * drci;
+  float cosphi = erax * ercx + eray * ercy + eraz * ercz;
+  cosphi = fminf(fmaxf(cosphi, -1.f), 1.f);
+  // sin from the cross product of the unit vectors: accurate in FP32 also
+  // where the three sites are nearly collinear (1 - cos^2 is not)
+  const float qx = eray * ercz - eraz * ercy, qy = eraz * ercx - erax * ercz,
+              qz = erax * ercy - eray * ercx;
+  const float sin2 = fmaxf(qx * qx + qy * qy + qz * qz, 1e-20f);
+  const float rr = atan2f(sqrtf(sin2), cosphi) - t0;
+  const float isinphi = rsqrtf(sin2);
+  const float fr = -2.f * kth * rr;
+  const float irasin = drai * isinphi * fr, ircsin = drci * isinphi * fr;
+  const float fxa = (erax * cosphi - ercx) * irasin, fya = (eray * cosphi - ercy) * irasin,
+              fza = (eraz * cosphi - ercz) * irasin;
+  const float fxc = (ercx * cosphi - erax) * ircsin, fyc = (ercy * cosphi - eray) * ircsin,
+              fzc = (ercz * cosphi - eraz) * ircsin;
+  if (which == 0) {
+    fx += fxa; fy += fya; fz += fza;
+  } else if (which == 2) {
+    fx += fxc; fy += fyc; fz += fzc;
+  } else {
+    fx -= fxa + fxc; fy -= fya + fyc; fz -= fza + fzc;
+  }
+  return kth * rr * rr;
+}
+
+// The torsion (a, a + 1, a + 2, a + 3) of the reference's Go model
+// (cda_golik, cgolik.c:399-610, three-fold, phase zero: E = kph (1 +
+// cos 3 tau)): the force on its site `which` (0..3) added, the energy
+// returned.
+__device__ __forceinline__ float go_tors(const float4 *__restrict__ p, int a, float kph,
+                                         int which, float &fx, float &fy, float &fz) {
+  const float4 A = p[a], B = p[a + 1], C = p[a + 2], Dd = p[a + 3];
+  const float dabx = B.x - A.x, daby = B.y - A.y, dabz = B.z - A.z;
+  const float dbcx = C.x - B.x, dbcy = C.y - B.y, dbcz = C.z - B.z;
+  const float dcdx = Dd.x - C.x, dcdy = Dd.y - C.y, dcdz = Dd.z - C.z;
+  const float rab = sqrtf(dabx * dabx + daby * daby + dabz * dabz), irab = 1.f / rab;
+  const float erabx = dabx * irab, eraby = daby * irab, erabz = dabz * irab;
+  const float rbc = sqrtf(dbcx * dbcx + dbcy * dbcy + dbcz * dbcz), irbc = 1.f / rbc;
+  const float erbcx = dbcx * irbc, erbcy = dbcy * irbc, erbcz = dbcz * irbc;
+  const float rcd = sqrtf(dcdx * dcdx + dcdy * dcdy + dcdz * dcdz), ircd = 1.f / rcd;
+  const float ercdx = dcdx * ircd, ercdy = dcdy * ircd, ercdz = dcdz * ircd;
+  const float abbcx = eraby * erbcz - erabz * erbcy, abbcy = erabz * erbcx - erabx * erbcz,
+              abbcz = erabx * erbcy - eraby * erbcx;
+  const float cosb = -(erabx * erbcx + eraby * erbcy + erabz * erbcz);
+  // 1 / sin^2 of the two bends from the cross products (1 - cos^2 loses its
+  // digits in FP32 where a bend is nearly straight)
+  const float isinb2 = 1.f / fmaxf(abbcx * abbcx + abbcy * abbcy + abbcz * abbcz, 1e-20f),
+              isinb = sqrtf(isinb2);
+  const float dccbx = ercdy * erbcz - ercdz * erbcy, dccby = ercdz * erbcx - ercdx * erbcz,
+              dccbz = ercdx * erbcy - ercdy * erbcx;
+  const float cosc = -(ercdx * erbcx + ercdy * erbcy + ercdz * erbcz);
+  const float isinc2 = 1.f / fmaxf(dccbx * dccbx + dccby * dccby + dccbz * dccbz, 1e-20f),
+              isinc = sqrtf(isinc2);
+  const float abcdx = -(abbcy * dccbz - abbcz * dccby), abcdy = -(abbcz * dccbx - abbcx * dccbz),
+              abcdz = -(abbcx * dccby - abbcy * dccbx);
+  // tau as the reference defines it (sign of num, angle between the two
+  // plane normals) but from atan2 of the normals' cross and dot products,
+  // accurate near 0 and pi where acos is not
+  const float num = abcdx * erbcx + abcdy * erbcy + abcdz * erbcz;
+  const float ctau = -(abbcx * dccbx + abbcy * dccby + abbcz * dccbz);
+  const float tau = atan2f(num, ctau);
+  float s3, c3;
+  sincosf(3.f * tau, &s3, &c3);
+  const float fr = 3.f * kph * s3;
+  if (which == 0) {
+    const float fa = -fr * irab * isinb2;
+    fx += fa * abbcx; fy += fa * abbcy; fz += fa * abbcz;
+  } else if (which == 1) {
+    const float fb1 = fr * (rbc - rab * cosb) * irab * irbc * isinb2;
+    const float fb2 = fr * cosc * irbc * isinc2;
+    fx += fb1 * abbcx + fb2 * dccbx; fy += fb1 * abbcy + fb2 * dccby; fz += fb1 * abbcz + fb2 * dccbz;
+  } else if (which == 2) {
+    const float fc1 = fr * (rbc - rcd * cosc) * ircd * irbc * isinc2;
+    const float fc2 = fr * cosb * irbc * isinb2;
+    fx += fc1 * dccbx + fc2 * abbcx; fy += fc1 * dccby + fc2 * abbcy; fz += fc1 * dccbz + fc2 * abbcz;
+  } else {
+    const float fd = -fr * ircd * isinc2;
+    fx += fd * dccbx; fy += fd * dccby; fz += fd * dccbz;
+  }
+  return kph * (1.f + c3);
+}
+
 // Force on bead i of a chain of N (positions in shared memory) from the
 // partners j = sub, sub + T, sub + 2T, ... (T threads per bead, sub its
 // index); natives likewise over the bead's CSR row, bonds by sub 0 only.
 // The partners of one 32-bead word are taken in groups of up to four whose
 // positions are loaded together.  Returns this thread's share of the
 // potential energy (pairs and bonds split in half).
-template <int T, bool WITH_E>
+template <int T, bool WITH_E, int FORM>
 __device__ __forceinline__ float go_force_t(const GoK &K, const GoD &D, const float4 *__restrict__ p,
                                             const unsigned *__restrict__ mrow, int N, int i,
                                             int sub, int gbase, float &fx, float &fy, float &fz) {
@@ -134,8 +243,9 @@ __device__ __forceinline__ float go_force_t(const GoK &K, const GoD &D, const fl
           const float ri2 = __fdividef(1.f, r2);
           const float ri6 = ri2 * ri2 * ri2;
           const float ri12 = ri6 * ri6;
-          if (WITH_E) e += 0.5f * fmaf(K.c12, ri12, -K.e_shift);
-          const float fs = K.f12 * ri12 * ri2;
+          if (WITH_E)
+            e += 0.5f * (FORM == 0 ? fmaf(K.c12, ri12, K.e0) : fmaf(K.c12, ri12, -K.c6 * ri6) + K.e0);
+          const float fs = (FORM == 0 ? K.f12 * ri12 : fmaf(K.f12, ri12, -K.f6 * ri6)) * ri2;
           fx = fmaf(fs, dx, fx);
           fy = fmaf(fs, dy, fy);
           fz = fmaf(fs, dz, fz);
@@ -150,11 +260,23 @@ __device__ __forceinline__ float go_force_t(const GoK &K, const GoD &D, const fl
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     float r2 = dx * dx + dy * dy + dz * dz;
     float ri2 = __fdividef(1.f, r2);
-    float s2 = D.nat_r02[q] * ri2;
-    float s10 = s2 * s2 * s2 * s2 * s2;
-    float s12 = s10 * s2;
-    if (WITH_E) e += 0.5f * K.eps * (5.f * s12 - 6.f * s10);
-    float fs = 60.f * K.eps * (s12 - s10) * ri2;
+    float fs;
+    if (FORM == 0) {
+      float s2 = D.nat_r02[q] * ri2;
+      float s10 = s2 * s2 * s2 * s2 * s2;
+      float s12 = s10 * s2;
+      if (WITH_E) e += 0.5f * K.eps * (5.f * s12 - 6.f * s10);
+      fs = 60.f * K.eps * (s12 - s10) * ri2;
+    } else {
+      if (r2 > K.rc2n) continue;
+      const float sg2 = 0.79370052598409973738f * D.nat_r02[q];  // (2^(-1/6) r0)^2
+      float s2 = sg2 * ri2, s6 = s2 * s2 * s2, s12 = s6 * s6;
+      if (WITH_E) {
+        float c2 = sg2 / K.rc2n, c6 = c2 * c2 * c2;
+        e += 0.5f * 4.f * K.eps * ((s12 - s6) - (c6 * c6 - c6));
+      }
+      fs = 48.f * K.eps * ri2 * (s12 - 0.5f * s6);
+    }
     fx = fmaf(fs, dx, fx);
     fy = fmaf(fs, dy, fy);
     fz = fmaf(fs, dz, fz);
@@ -166,26 +288,48 @@ __device__ __forceinline__ float go_force_t(const GoK &K, const GoD &D, const fl
     float4 pj = p[j];
     float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     float r = sqrtf(dx * dx + dy * dy + dz * dz);
-    float dr = r - K.r0b;
-    if (WITH_E) e += 0.5f * K.kb * dr * dr;
-    float fs = -2.f * K.kb * dr / r;
+    float dr = r - (FORM == 0 ? K.r0b : D.bond_r0[g + min(nb, 0)]);
+    float fs;
+    if (FORM == 0) {
+      if (WITH_E) e += 0.5f * K.kb * dr * dr;
+      fs = -2.f * K.kb * dr / r;
+    } else {
+      if (WITH_E) e += 0.5f * dr * dr * fmaf(K.kq, dr * dr, K.kb);
+      fs = -dr * fmaf(4.f * K.kq, dr * dr, 2.f * K.kb) / r;
+    }
     fx = fmaf(fs, dx, fx);
     fy = fmaf(fs, dy, fy);
     fz = fmaf(fs, dz, fz);
   }
+  if (FORM == 1) {
+    // the bends and torsions that move this bead: each computed whole, this
+    // bead's share of the force kept, its energy split over its beads
+#pragma unroll
+    for (int c = i - 1; c <= i + 1; c++)
+      if (c >= 1 && c + 1 < N) {
+        const float eb = go_bend(p, c, D.bend_t0[gbase + c], K.kth, i - (c - 1), fx, fy, fz);
+        if (WITH_E) e += eb * (1.f / 3.f);
+      }
+#pragma unroll
+    for (int a = i - 3; a <= i; a++)
+      if (a >= 0 && a + 3 < N) {
+        const float et = go_tors(p, a, K.kph, i - a, fx, fy, fz);
+        if (WITH_E) e += 0.25f * et;
+      }
+  }
   return e;
 }
 
-template <bool WITH_E>
+template <bool WITH_E, int FORM>
 __device__ __forceinline__ float go_force(const GoK &K, const GoD &D, const float4 *__restrict__ p,
                                           const unsigned *__restrict__ mrow, int N, int i, int sub,
                                           int T, int gbase, float &fx, float &fy, float &fz) {
   switch (T) {
-    case 1: return go_force_t<1, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
-    case 2: return go_force_t<2, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
-    case 4: return go_force_t<4, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
-    case 8: return go_force_t<8, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
-    default: return go_force_t<16, WITH_E>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 1: return go_force_t<1, WITH_E, FORM>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 2: return go_force_t<2, WITH_E, FORM>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 4: return go_force_t<4, WITH_E, FORM>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    case 8: return go_force_t<8, WITH_E, FORM>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
+    default: return go_force_t<16, WITH_E, FORM>(K, D, p, mrow, N, i, sub, gbase, fx, fy, fz);
   }
 }
 
@@ -271,6 +415,7 @@ __device__ __forceinline__ void go_publish(const GoCta &c, float4 *buf, int i, d
 // t integrates bead lo + t), so each warp's FP64 instructions carry 32
 // beads — the FP64 pipe is narrow on this part.  The forces pass between
 // the two layouts through shared memory.
+template <int FORM>
 __global__ void __launch_bounds__(kGoBlock, 1) k_go_segment(GoK K, GoD D, int nsteps, int mode) {
   extern __shared__ float4 go_pos[];  // two buffers of K.maxN, then the skip rows
   __shared__ double red[33];
@@ -314,8 +459,8 @@ __global__ void __launch_bounds__(kGoBlock, 1) k_go_segment(GoK K, GoD D, int ns
   go_cluster_sync();
   float fx = 0.f, fy = 0.f, fz = 0.f, e = 0.f;
   if (bead) {
-    if (mode == 1 || nsteps == 0) e = go_force<true>(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
-    else go_force<false>(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
+    if (mode == 1 || nsteps == 0) e = go_force<true, FORM>(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
+    else go_force<false, FORM>(K, D, go_pos, mrow, N, i, sub, T, gbase, fx, fy, fz);
   }
   fx = go_lane_sum(fx, T);
   fy = go_lane_sum(fy, T);
@@ -362,8 +507,8 @@ __global__ void __launch_bounds__(kGoBlock, 1) k_go_segment(GoK K, GoD D, int ns
     }
     go_cluster_sync();  // also: fsh was read above before it is written below
     if (bead) {  // the energy of the last step only
-      if (s == nsteps - 1) e = go_force<true>(K, D, nxt, mrow, N, i, sub, T, gbase, fx, fy, fz);
-      else go_force<false>(K, D, nxt, mrow, N, i, sub, T, gbase, fx, fy, fz);
+      if (s == nsteps - 1) e = go_force<true, FORM>(K, D, nxt, mrow, N, i, sub, T, gbase, fx, fy, fz);
+      else go_force<false, FORM>(K, D, nxt, mrow, N, i, sub, T, gbase, fx, fy, fz);
     }
     fx = go_lane_sum(fx, T);
     fy = go_lane_sum(fy, T);
@@ -557,7 +702,9 @@ static int go_launch(GoBatch *G, int nsteps, int mode) {
   cfg.stream = G->st;
   cfg.attrs = at;
   cfg.numAttrs = 1;
-  cudaError_t e = cudaLaunchKernelEx(&cfg, k_go_segment, G->K, G->D, nsteps, mode);
+  cudaError_t e = G->K.form == 0
+                      ? cudaLaunchKernelEx(&cfg, k_go_segment<0>, G->K, G->D, nsteps, mode)
+                      : cudaLaunchKernelEx(&cfg, k_go_segment<1>, G->K, G->D, nsteps, mode);
   if (e != cudaSuccess) return cuda_fail(e, "k_go_segment");
   return FE_OK;
 }
@@ -638,6 +785,11 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
     K.c12 = (float)(p->eps * s12);
     K.f12 = (float)(12.0 * p->eps * s12);
   }
+  K.c6 = K.f6 = 0.f;
+  K.e0 = -K.e_shift;
+  K.form = 0;
+  K.kq = K.kth = K.kph = 0.f;
+  K.rc2n = 0.f;
   K.kb = (float)p->k_bond;
   K.r0b = (float)p->r_bond;
   K.acc_fac = 100.0 / p->mass;
@@ -692,7 +844,9 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
     // under one another's launches
     const int smem_cap = (int)(2 * sizeof(float4) * kGoMaxBeads +
                                sizeof(unsigned) * kGoMaxBeads * (kGoMaxBeads / 32));
-    if (cudaFuncSetAttribute(k_go_segment, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    if (cudaFuncSetAttribute(k_go_segment<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             smem_cap) != cudaSuccess ||
+        cudaFuncSetAttribute(k_go_segment<1>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              smem_cap) != cudaSuccess) {
       rc = cuda_fail(cudaGetLastError(), "cudaFuncSetAttribute");
       break;
@@ -715,7 +869,7 @@ int fe_go_create(fe_go **out, int nrep, const int *nbeads, const double *pos, co
       cfg.dynamicSmemBytes = G->smem;
       cfg.attrs = at;
       cfg.numAttrs = 1;
-      if (cudaOccupancyMaxActiveClusters(&nclu, k_go_segment, &cfg) != cudaSuccess) {
+      if (cudaOccupancyMaxActiveClusters(&nclu, k_go_segment<1>, &cfg) != cudaSuccess) {
         cudaGetLastError();
         nclu = nsm / kGoCluster;
       }
@@ -807,6 +961,52 @@ int fe_go_state(fe_go *h, double *pos, double *vel, double *T, double *epot, int
   if (attempted)
     FE_CUDA(cudaMemcpy(attempted, G->D.att, sizeof(long long) * G->nrep, cudaMemcpyDeviceToHost));
   if (steps) FE_CUDA(cudaMemcpy(steps, G->D.step, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+  return FE_OK;
+}
+
+int fe_go_set_reference_form(fe_go *h, const double *bond_r0, const double *bend_t0,
+                             double d_rep, double rc) {
+  if (!h || !bond_r0 || !bend_t0 || !(d_rep > 0.0) || !(rc > d_rep)) {
+    set_error("fe_go_set_reference_form: invalid argument");
+    return FE_ERR_ARG;
+  }
+  GoBatch *G = &h->G;
+  FE_CUDA(cudaStreamSynchronize(G->st));
+  std::vector<float> br(G->total), bt(G->total);
+  for (int i = 0; i < G->total; i++) {
+    br[i] = (float)bond_r0[i];
+    bt[i] = (float)bend_t0[i];
+  }
+  int rc_ = FE_OK;
+  if (!G->D.bond_r0 && (rc_ = go_upload(G, (float **)&G->D.bond_r0, br.data(), br.size())))
+    return rc_;
+  if (!G->D.bend_t0 && (rc_ = go_upload(G, (float **)&G->D.bend_t0, bt.data(), bt.size())))
+    return rc_;
+  FE_CUDA(cudaMemcpy((void *)G->D.bond_r0, br.data(), sizeof(float) * br.size(),
+                     cudaMemcpyHostToDevice));
+  FE_CUDA(cudaMemcpy((void *)G->D.bend_t0, bt.data(), sizeof(float) * bt.size(),
+                     cudaMemcpyHostToDevice));
+  GoK &K = G->K;
+  const double eps = K.eps;  // kJ/mol
+  const double factor = pow(2.0, -1.0 / 6.0);  // read_golik.c:38
+  const double sg = factor * d_rep, s6 = pow(sg, 6.0), s12 = s6 * s6;
+  // non-natives: 4 eps [(s/r)^12 - (s/r)^6] + eps within d_rep (cgolik.c:780-800)
+  K.rc2 = (float)(d_rep * d_rep);
+  K.c12 = (float)(4.0 * eps * s12);
+  K.c6 = (float)(4.0 * eps * s6);
+  K.f12 = (float)(48.0 * eps * s12);
+  K.f6 = (float)(24.0 * eps * s6);
+  K.e0 = (float)eps;
+  K.rc2n = (float)(rc * rc);
+  K.kb = (float)eps;           // cbb_golik: -k1 = eps, -k2 = 100 eps
+  K.kq = (float)(100.0 * eps);
+  K.kth = (float)(10.0 * eps);  // cba_golik: k_theta = -10 eps
+  K.kph = (float)(0.2 * eps);   // cda_golik: k_phi = 0.2 eps
+  K.min_sep = 2;                // only bonded pairs are excluded (read_golik.c:99-110)
+  K.form = 1;
+  if (G->g) cudaGraphExecDestroy(G->g);  // recaptured with the new parameters
+  G->g = nullptr;
+  G->g_len = -1;
   return FE_OK;
 }
 

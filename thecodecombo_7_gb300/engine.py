@@ -57,7 +57,7 @@ EXPORTS = [
     "fe_mc_chains_collect", "fe_mc_chains_samples", "fe_mc_chains_train_surrogate",
     "fe_mc_chains_set_surrogate", "fe_mc_chains_set_mode", "fe_mc_chains_stats",
     "fe_go_create", "fe_go_destroy", "fe_go_run", "fe_go_forces", "fe_go_state",
-    "fe_go_get_stream", "fe_go_layout", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
+    "fe_go_get_stream", "fe_go_layout", "fe_go_set_reference_form", "fe_autotune", "fe_pipe_peak", "fe_pair_counts",
     "fe_mc_delta_terms", "fe_mc_site_energy", "fe_drift", "fe_box_set_temperature",
     "fe_bspline", "fe_batch_set_fused", "fe_set_ureys", "fe_set_torsions", "fe_set_impropers",
     "fe_get_torsion_angles", "fe_bonded_ext",
@@ -825,6 +825,27 @@ class GoBatch:
         s = C.c_void_p()
         self._check(self.lib.fe_go_get_stream(self.h, C.byref(s)))
         return s.value or 0
+
+    def set_reference_form(self, d_rep=4.0, rc=12.0, native=None):
+        """Switches to the reference's own Go model (cgolik.c) with the bond
+        lengths and bend angles of each chain's native structure (`native`,
+        (total, 3); default the starting coordinates), non-native cut d_rep
+        and native cutoff rc."""
+        g = self.g
+        st = g.start
+        nat = g.pos if native is None else native
+        br, bt = np.zeros(int(st[-1])), np.zeros(int(st[-1]))
+        for r in range(len(g.nbeads)):
+            a, b = int(st[r]), int(st[r + 1])
+            x = np.asarray(nat[a:b], np.float64)
+            d = x[1:] - x[:-1]
+            br[a:b - 1] = np.sqrt((d * d).sum(axis=1))
+            u, v = -d[:-1], d[1:]
+            bt[a + 1:b - 1] = np.arccos((u * v).sum(axis=1) / np.sqrt(
+                (u * u).sum(axis=1) * (v * v).sum(axis=1)))
+        self._keep.update(br=br, bt=bt)
+        self._check(self.lib.fe_go_set_reference_form(self.h, _p(br), _p(bt), C.c_double(d_rep),
+                                                       C.c_double(rc)))
 
     def layout(self):
         """The launch's load-balance plan: CTAs launched, CTAs resident at
