@@ -158,6 +158,12 @@ int fe_cnonbondnl(fe_box *box, double *energy8);
 /* pme_calc(k, energy), pme_calc.c:18-279 (charge_grid, FFTs, reciprocal
  * sum, pme_force with mean-force removal): accumulates into ff. */
 int fe_pme_calc(fe_box *box, double *energy3);
+/* The LJ form of the pair loop, as the reference's build chooses it: 0 its
+ * default eps[(R/r)^12 - 2(R/r)^6]; 2 its BGO build (cnonbond_nblist.c:
+ * 294-307), eps[13(R/r)^12 - 18(R/r)^10 + 4(R/r)^6] with the shifted energy
+ * at rc likewise.  FP64 boxes without the LJ switch (FE_ERR_STATE
+ * otherwise). */
+int fe_box_set_lj_form(fe_box *box, int form);
 /* pme_force(k), pme_calc.c:122-279: the reciprocal forces from the grid as
  * the last fe_pme_calc left it (convolved, back in real space) and the
  * splines of the last charge_grid, mean force removed, accumulated into ff

@@ -9,6 +9,7 @@
 #   ref_harness_fast  the reference makefile's own flags (makefile:84-88:
 #                     -O3 -ffast-math -funroll-all-loops -std=c99), for timing
 #   ref_harness_dlist the strict build with -DDLIST (nl_check)
+#   ref_harness_bgo   the strict build with -DBGO (the 12-10-6 pair form)
 #   ref_harness_go    the Go-model routines of cgolik.c (-DGOLIK)
 #
 # Feature flags: -DNLIST -DEWALD -DSPME -DSTYPE.  FFTW3 is not installed, so
@@ -44,8 +45,12 @@ gcc -std=gnu99 -O2 -ffp-contract=off -DNLIST -DEWALD -DMC -DSTYPE -I"$REF" -w \
     -o "$OUT/ref_harness_mc" "$HERE/ref_harness.c" \
     "$REF/nblist.c" "$REF/setlj.c" "$REF/ewald.c" "$REF/ewald_mc.c" "$REF/cplx.c" \
     "$REF/enbnd_mc.c" -lm
+# the Brooks Go model's pair form (-DBGO: cnonbond_nblist.c:294-307), strict;
+# -fcommon: defines.h declares a global of that build without extern, as the
+# compilers of the reference's time merged (common symbols)
+build ref_harness_bgo -std=gnu99 -O2 -ffp-contract=off -fcommon -DBGO
 # the reference's own Go model (-DGOLIK, no STYPE: cgolik.c reads the
 # per-box pair table ljset[k].pot[a][b]), strict IEEE
 gcc -std=gnu99 -O2 -ffp-contract=off -DGOLIK -DNLIST -I"$REF" -w \
     -o "$OUT/ref_harness_go" "$HERE/ref_harness_go.c" "$REF/cgolik.c" -lm
-echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast, $OUT/ref_harness_dlist, $OUT/ref_harness_mc and $OUT/ref_harness_go"
+echo "build_ref: built $OUT/ref_harness, $OUT/ref_harness_fast, $OUT/ref_harness_dlist, $OUT/ref_harness_mc, $OUT/ref_harness_bgo and $OUT/ref_harness_go"

@@ -220,7 +220,13 @@ void or_cnonbond_pairs(const or_system *s, const double *pos, const int *cnt,
         double sr12s = sr6s * sr6s;
         double flj = (12.0 * eps / dr2) * (sr12 - sr6);
         double elj = eps * (sr12 - 2.0 * sr6);
-        if (ron2 > 0.0) {
+        if (s->lj_form == 2) { /* the BGO build, cnonbond_nblist.c:294-307 */
+          double sr10 = sr6 * sr2 * sr2;
+          double sr10s = sr6s * sr2s * sr2s;
+          force = eps / dr2 * (156.0 * sr12 - 180.0 * sr10 + 24.0 * sr6);
+          enonbond += eps * (13.0 * sr12 - 18.0 * sr10 + 4.0 * sr6);
+          enonbonds += eps * (13.0 * sr12s - 18.0 * sr10s + 4.0 * sr6s);
+        } else if (ron2 > 0.0) {
           if (dr2 > ron2) {
             double c = rc2 - dr2;
             double sw = c * c * (rc2 + 2.0 * dr2 - 3.0 * ron2) / sw_den;

@@ -51,6 +51,8 @@ typedef struct {
   int nexcl;
   const int *excl_ab;      /* 2*nexcl (xint[k][i].a/b) */
   const int *excl_flag;    /* nexcl (xint[k][i].xflag: 1 bond 2 bend 3 exNB 4 1-4) */
+  int lj_form;             /* 0 CHARMM eps[(R/r)^12 - 2(R/r)^6]; 2 the BGO build's
+                              eps[13(R/r)^12 - 18(R/r)^10 + 4(R/r)^6] (cnonbond_nblist.c:294-307) */
 } or_system;
 
 /* Energy record in the reference's en[k] vocabulary (forces.c:204-219). */

@@ -25,6 +25,7 @@ REF_BIN_FAST = os.path.join(HERE, "_ref", "ref_harness_fast")
 REF_BIN_DLIST = os.path.join(HERE, "_ref", "ref_harness_dlist")
 REF_BIN_MC = os.path.join(HERE, "_ref", "ref_harness_mc")
 REF_BIN_GO = os.path.join(HERE, "_ref", "ref_harness_go")
+REF_BIN_BGO = os.path.join(HERE, "_ref", "ref_harness_bgo")
 
 # strict IEEE: no FMA contraction, no fast-math, so results are reproducible
 # on x86-64 and aarch64 alike and match a strict build of the reference
@@ -83,6 +84,7 @@ class OrSystem(C.Structure):
         ("nbend", C.c_int), ("bend_abc", C.c_void_p),
         ("bend_theta0", C.c_void_p), ("bend_k", C.c_void_p),
         ("nexcl", C.c_int), ("excl_ab", C.c_void_p), ("excl_flag", C.c_void_p),
+        ("lj_form", C.c_int),
     ]
 
 
@@ -152,6 +154,7 @@ class Oracle:
         s.bend_abc, s.bend_theta0, s.bend_k = _p(k["bend_abc"]), _p(k["bend_t0"]), _p(k["bend_k"])
         s.nexcl = k["excl_ab"].shape[0]
         s.excl_ab, s.excl_flag = _p(k["excl_ab"]), _p(k["excl_flag"])
+        s.lj_form = int(getattr(sysm, "lj_form", 0))
         self.s = s
         self.sp = C.byref(s)
 
@@ -414,11 +417,11 @@ def read_tagged(path):
     return out
 
 
-def run_reference(mode, sysm, workdir, nsteps=None, fast=False, extra=()):
+def run_reference(mode, sysm, workdir, nsteps=None, fast=False, extra=(), binary=None):
     """Run the reference's own routines (oracle/_ref) on sysm; `extra` are
     further integer arguments of the mode (mts: the short steps per long
-    step)."""
-    binp = REF_BIN_FAST if fast else REF_BIN
+    step); `binary` another build of the harness (REF_BIN_BGO)."""
+    binp = binary or (REF_BIN_FAST if fast else REF_BIN)
     os.makedirs(workdir, exist_ok=True)
     sp = os.path.join(workdir, "system.bin")
     op = os.path.join(workdir, f"out_{mode}.bin")

@@ -47,6 +47,12 @@ def golden_go_hc():
 
 
 @pytest.fixture(scope="session")
+def golden_bgo600():
+    import numpy as np
+    return dict(np.load(os.path.join(GOLDEN, "bgo600.npz")))
+
+
+@pytest.fixture(scope="session")
 def golden_chain():
     import numpy as np
     return dict(np.load(os.path.join(GOLDEN, "chain900.npz")))

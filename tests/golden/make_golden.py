@@ -103,6 +103,7 @@ def main():
     make_chain(tmp)
     make_mts_water(tmp)
     make_go_hc(tmp)
+    make_bgo(tmp)
     print("golden fixtures written to", HERE)
 
 
@@ -220,6 +221,17 @@ def make_go_hc(tmp):
     np.savez_compressed(os.path.join(HERE, "go_hc.npz"), **out)
 
 
+def make_bgo(tmp):
+    """The BGO build's pair form (cnonbond_nblist.c:294-307) on the 600-site
+    water box: forces() and its breakdown from the reference's -DBGO build."""
+    s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27))
+    fo = O.run_reference("forces", s, tmp, binary=O.REF_BIN_BGO)
+    out = sys_arrays(s)
+    for k, v in fo.items():
+        out["forces_" + k] = v
+    np.savez_compressed(os.path.join(HERE, "bgo600.npz"), **out)
+
+
 def make_drift(tmp):
     s = systems.water_box(200, L=25.0, seed=7, grid=(24, 25, 27), helper=False)
     s.vel = s.vel + np.array([0.7, -0.4, 0.25])
@@ -240,11 +252,12 @@ def make_nlcheck(tmp):
 
 
 if __name__ == "__main__":
-    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"], ["mts"], ["go"]):  # alone
+    if sys.argv[1:] in (["nlcheck"], ["mc"], ["drift"], ["chain"], ["mts"], ["go"], ["bgo"]):
         if not O.build_reference():
             raise SystemExit("reference sources not available")
         {"nlcheck": make_nlcheck, "mc": make_mc, "drift": make_drift,
-         "chain": make_chain, "mts": make_mts_water, "go": make_go_hc}[sys.argv[1]](
+         "chain": make_chain, "mts": make_mts_water, "go": make_go_hc,
+         "bgo": make_bgo}[sys.argv[1]](
             tempfile.mkdtemp(prefix="fe_golden_"))
     else:
         main()

@@ -285,3 +285,22 @@ def test_pme_force_alone(golden600):
         f2 = b.get_forces()
     assert np.array_equal(f1, f2)
     _close_f(f2.ravel(), g["forces_f_pme"])
+
+
+
+def test_bgo_pair_form_vs_reference(golden_bgo600):
+    """The pair loop's BGO form (fe_box_set_lj_form 2) against the
+    reference's own -DBGO build (tests/golden/bgo600.npz): forces and every
+    energy term to 1e-10."""
+    g = golden_bgo600
+    s = system_from_golden(g, 200)
+    with _box(s) as b:
+        b.set_lj_form(2)
+        b.nblist()
+        en = b.forces()
+        f = b.get_forces()
+    _close_f(f.ravel(), g["forces_f_total"])
+    ref = dict(zip(O.EN_KEYS, g["forces_en"]))
+    for k in ("bond", "bend", "nbond", "nbonds", "coulomb", "rewald", "rewalds", "kewald",
+              "sewald", "iewald", "tewald"):
+        _close_e(en[k], ref[k])

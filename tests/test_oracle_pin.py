@@ -163,3 +163,19 @@ def test_respa_fixtures_semantics(golden_chain, golden_mts600):
     e = golden_mts600["mts_en_steps"].reshape(-1, 15)
     tot = e[:, 0] + e[:, 1] + e[:, 2] + e[:, 3] + e[:, 12] + e[:, 13] + e[:, 14]
     assert np.abs(tot - tot[0]).max() < 0.01 * abs(tot[0])
+
+
+def test_oracle_bgo_pair_form_bit_exact(golden_bgo600):
+    """The BGO build's pair form (cnonbond_nblist.c:294-307: eps [13 (R/r)^12
+    - 18 (R/r)^10 + 4 (R/r)^6]) against the reference's own -DBGO build
+    (oracle/_ref/ref_harness_bgo, fixture tests/golden/bgo600.npz): the full
+    forces() and every energy term bit for bit."""
+    g = golden_bgo600
+    s = system_from_golden(g, 200)
+    s.lj_form = 2
+    orc = O.Oracle(s)
+    ff, en = orc.forces(s.pos, orc.nblist(s.pos))
+    np.testing.assert_array_equal(ff.ravel(), g["forces_f_total"])
+    ref_en = dict(zip(O.EN_KEYS, g["forces_en"]))
+    for k, v in en.items():
+        assert v == ref_en[k], k

@@ -634,6 +634,21 @@ int fe_pme_calc(fe_box *box, double *energy3) {
   return FE_OK;
 }
 
+int fe_box_set_lj_form(fe_box *box, int form) {
+  if (!box || (form != 0 && form != 2)) {
+    set_error("fe_box_set_lj_form: form is 0 (CHARMM) or 2 (BGO)");
+    return FE_ERR_ARG;
+  }
+  Box *b = &box->b;
+  if (form == 2 && (b->mx || b->p.r_switch > 0.0)) {
+    set_error("fe_box_set_lj_form: the BGO form is the FP64 drop-in's, without the LJ switch");
+    return FE_ERR_STATE;
+  }
+  b->lj_form = form;
+  b->g_key = -1;  // step graphs are recaptured
+  return FE_OK;
+}
+
 int fe_pme_force(fe_box *box) {
   if (!box) return FE_ERR_ARG;
   Box *b = &box->b;

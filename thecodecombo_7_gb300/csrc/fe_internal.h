@@ -75,6 +75,7 @@ struct Box {
   cudaStream_t s_io = nullptr;
   cudaEvent_t ev_io_pos = nullptr, ev_io_done = nullptr;
   int prec = FE_PREC_FP64;
+  int lj_form = 0;  // the pair loop's LJ form: 0 CHARMM, 2 the reference's BGO build
 
   // sites
   double4 *pos_q = nullptr;   // x, y, z (wrapped), q

@@ -14,6 +14,7 @@ struct PairParams {
   double3 L, H;
   double rc, rc2, kappa, kpi, epsRF, erfc_rc;
   double ron2, sw_den;  // optional CHARMM switch (ron2 = 0: off)
+  int lj_form;          // 0 CHARMM (the reference's default build); 2 its BGO build
   int n, nt, max_nb;
 };
 
@@ -68,7 +69,18 @@ k_pair64(PairParams P, const double4 *__restrict__ pos, const int *__restrict__ 
         double sr12 = sr6 * sr6;
         double flj = (12.0 * eps / dr2) * (sr12 - sr6);
         double elj = eps * (sr12 - 2.0 * sr6);
-        if (P.ron2 > 0.0) {
+        if (P.lj_form == 2) {
+          // the BGO build (cnonbond_nblist.c:294-307): eps [13 (R/r)^12 -
+          // 18 (R/r)^10 + 4 (R/r)^6], shifted sum at rc as the default form
+          double sr10 = sr6 * sr2 * sr2;
+          double sr2s = (sig * sig) / P.rc2;
+          double sr6s = sr2s * sr2s * sr2s;
+          double sr12s = sr6s * sr6s;
+          double sr10s = sr6s * sr2s * sr2s;
+          force = eps / dr2 * (156.0 * sr12 - 180.0 * sr10 + 24.0 * sr6);
+          e_lj += eps * (13.0 * sr12 - 18.0 * sr10 + 4.0 * sr6);
+          e_ljs += eps * (13.0 * sr12s - 18.0 * sr10s + 4.0 * sr6s);
+        } else if (P.ron2 > 0.0) {
           if (dr2 > P.ron2) {
             double c = P.rc2 - dr2;
             double sw = c * c * (P.rc2 + 2.0 * dr2 - 3.0 * P.ron2) / P.sw_den;
@@ -290,6 +302,7 @@ int launch_pair64(Box *b) {
   P.erfc_rc = host_ref_erfc(b->p.kappa * b->p.rc);
   P.ron2 = b->p.r_switch > 0.0 ? b->p.r_switch * b->p.r_switch : 0.0;
   P.sw_den = P.ron2 > 0.0 ? (P.rc2 - P.ron2) * (P.rc2 - P.ron2) * (P.rc2 - P.ron2) : 0.0;
+  P.lj_form = b->lj_form;
   P.n = b->n;
   P.nt = b->nt;
   P.max_nb = b->max_nb;

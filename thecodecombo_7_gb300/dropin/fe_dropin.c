@@ -49,6 +49,9 @@
  * en[k].urey, .tors and .impr, and each torsion's angle goes back to
  * tors[k][i].phi / psi / theta when the system tags any (ctorsion.c:172-175).
  *
+ * A -DBGO build of the reference gets the engine's BGO pair form (its
+ * 12-10-6 LJ term, cnonbond_nblist.c:294-307) on every box.
+ *
  * Errors print the engine's message and exit() with the reference's codes
  * (5: neighbour list over capacity, nblist.c:185-197; 20: non-neutral box,
  * ewald.c:185-194; 1 otherwise).  FE_PRECISION=mixed in the environment
@@ -254,6 +257,10 @@ static fe_box *fe_of(int k) {
   free(bk); free(at0); free(ak); free(xab); free(xfl);
   if (nhc[k].zeta) FE_OR_DIE(fe_set_nhc_state(g_fe[k], &nhc[k].zeta[0].r), "setup");
   set_ext_bonded(g_fe[k], k);
+#ifdef BGO
+  /* the build's pair form, cnonbond_nblist.c:294-307 */
+  FE_OR_DIE(fe_box_set_lj_form(g_fe[k], 2), "setup");
+#endif
   return g_fe[k];
 }
 

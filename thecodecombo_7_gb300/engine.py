@@ -45,6 +45,7 @@ EXPORTS = [
     "fe_pbc_all", "fe_kinet", "fe_integrate_vverlet", "fe_integrate_nhc", "fe_run_md",
     "fe_force_short", "fe_force_long", "fe_integrate_mts", "fe_get_forces_mts",
     "fe_set_forces_mts", "fe_integrate_mts_nhc", "fe_integrate_vverlet_host", "fe_pme_force",
+    "fe_box_set_lj_form",
     "fe_mc_setup", "fe_mc_delta", "fe_mc_accept", "fe_mc_kspace_energy",
     "fe_time_kernel", "fe_step_launches", "fe_list_stats", "fe_inner_list_stats", "fe_nl_check",
     "fe_ewald_kspace_energy_noalloc",
@@ -322,6 +323,11 @@ class Box:
         en = np.empty(FE_EN_COUNT)
         self._check(self.lib.fe_forces(self.h, _p(en)))
         return dict(zip(EN_KEYS, en.tolist()))
+
+    def set_lj_form(self, form):
+        """The pair loop's LJ form: 0 the reference's default, 2 its BGO
+        build (eps [13 (R/r)^12 - 18 (R/r)^10 + 4 (R/r)^6])."""
+        self._check(self.lib.fe_box_set_lj_form(self.h, int(form)))
 
     def pme_force(self):
         """pme_force (pme_calc.c:122): reciprocal forces from the grid of the
