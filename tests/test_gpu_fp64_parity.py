@@ -304,3 +304,63 @@ def test_bgo_pair_form_vs_reference(golden_bgo600):
     for k in ("bond", "bend", "nbond", "nbonds", "coulomb", "rewald", "rewalds", "kewald",
               "sewald", "iewald", "tewald"):
         _close_e(en[k], ref[k])
+
+
+def _slab_box(n_mol, Lxyz, seed):
+    """Whole molecules of a cubic water box cut to an orthorhombic box, with a
+    1.5 A gap left at every face (no close contacts across the new faces),
+    then four molecules moved so that one site sits exactly on -L/2 of each
+    axis (and one on -L/2 of all three): the wrap edges of the cell walk."""
+    from thecodecombo_7_gb300 import systems
+    Lxyz = np.asarray(Lxyz, dtype=float)
+    s = systems.water_box(n_mol, density=0.1, seed=seed, L=float(Lxyz.max()))
+    o = s.pos[0::3]
+    keep = np.all(np.abs(o) < Lxyz / 2 - 1.5, axis=1)
+    keep[:4] = True
+    m = np.flatnonzero(keep)
+    sites = (3 * m[:, None] + np.arange(3)).ravel()
+    t = systems.water_box(len(m), density=0.1, seed=seed, L=float(Lxyz.max()))
+    pos = s.pos[sites].copy()
+    for k, axes in enumerate(([0], [1], [2], [0, 1, 2])):
+        for a in axes:
+            pos[3 * k:3 * k + 3, a] += -Lxyz[a] / 2 - pos[3 * k, a]
+    pos -= Lxyz * np.floor(pos / Lxyz + 0.5)
+    t.pos = pos
+    t.L = Lxyz
+    t.grid = (40, 48, 36)
+    return t
+
+
+@pytest.mark.parametrize("case", ["cubic_3cells", "orthorhombic_faces"])
+def test_nblist_and_forces_on_larger_grids(case):
+    """The golden boxes (L = 25 and 34.5 A, list radius 12 A) have two cells
+    per axis; these boxes have three and more (9,000 sites, L = 44.8 A; and
+    an orthorhombic 40 x 52 x 37 A box with sites exactly on -L/2): the pair
+    lists bit-exact against the pinned oracle, forces and energies to 1e-10
+    (the Coulomb total to 1e-10 of the Ewald terms it is summed from)."""
+    from thecodecombo_7_gb300 import systems
+    if case == "cubic_3cells":
+        s = systems.water_box(3000, density=0.1, seed=31)
+    else:
+        s = _slab_box(2600, (40.0, 52.0, 37.0), seed=17)
+    orc = O.Oracle(s)
+    wcnt, widx, wflg = orc.nblist(s.pos)
+    wf, wen = orc.forces(s.pos, (wcnt, widx, wflg))
+    with _box(s) as b:
+        b.nblist()
+        cnt, idx, flg = b.nblist_download()
+        en = b.forces()
+        f = b.get_forces()
+    np.testing.assert_array_equal(cnt, wcnt)
+    np.testing.assert_array_equal(idx, widx)
+    np.testing.assert_array_equal(flg, wflg)
+    _close_f(f.ravel(), wf.ravel())
+    for k in ("bond", "bend", "nbond", "nbonds", "rewald", "rewalds", "kewald", "sewald",
+              "iewald"):
+        _close_e(en[k], wen[k], k)
+    # the Coulomb total is what is left of Ewald terms of 1e5-1e6 kJ/mol
+    # that nearly cancel (-7 kJ/mol on the 9,000-site box): its bar scales
+    # with the terms it is summed from
+    parts = sum(abs(wen[k]) for k in ("rewald", "kewald", "sewald", "iewald"))
+    for k in ("coulomb", "tewald"):
+        assert abs(en[k] - wen[k]) <= ETOL * parts, (k, en[k], wen[k], parts)
