@@ -228,7 +228,9 @@ typedef struct fe_md_io {
  * step, the downloads of all five and `en`.  With every array in pinned host
  * memory and 24-byte strides the copies are queued around the step (the
  * positions' download on a second stream while the forces are evaluated)
- * and the call synchronises once; otherwise it makes the separate calls
+ * and the call synchronises once (copies and kernels are captured as one
+ * graph on the first call with a given set of arrays and vscal, and
+ * replayed while they stay the same); otherwise it makes the separate calls
  * (fe_set_positions .. fe_get_forces) with their own synchronisations.
  * Same results either way. */
 int fe_integrate_vverlet_host(fe_box *box, double vscal, const fe_md_io *io, double *en);

@@ -119,13 +119,23 @@ def test_swap_sequence_matches_oracle():
             b.close()
 
 
+def _pinned_copies(arrs):
+    import torch
+    out = []
+    for a in arrs:
+        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
+        t[:] = a
+        out.append(t)
+    return out
+
+
 def test_integrate_vverlet_host_equals_separate_calls(golden600):
-    """fe_integrate_vverlet_host with pinned arrays (copies queued around the
-    step, one synchronisation) and with plain numpy arrays (the separate
-    upload / step / download calls) gives the results of the separate calls:
+    """fe_integrate_vverlet_host with pinned arrays (copies and kernels of
+    the step in one graph per set of host arrays, replayed; a new set midway
+    is captured anew) and with plain numpy arrays (the separate upload /
+    step / download calls) gives the results of the separate calls:
     bit for bit in mixed precision (fixed-point force sums), and to the
     run-to-run spread of the FP64 atomic force sums in FP64."""
-    import torch
     from thecodecombo_7_gb300 import engine
     from tests.helpers import system_from_golden
     s = system_from_golden(golden600, 200)
@@ -138,15 +148,13 @@ def test_integrate_vverlet_host_equals_separate_calls(golden600):
                 arrs = [b.get_positions(), b.get_positions_nopbc(), *b.get_velocities(),
                         b.get_forces()]
                 if mode == "pinned":
-                    pinned = []
-                    for a in arrs:
-                        t = torch.empty(a.shape, dtype=torch.float64, pin_memory=True).numpy()
-                        t[:] = a
-                        pinned.append(t)
-                    arrs = pinned
+                    arrs = _pinned_copies(arrs)
                 for i in range(1, 7):
                     if i % s.nlist_freq == 0:
                         b.nblist()
+                    if mode == "pinned" and i == 4:
+                        # other host arrays: the step's graph is captured anew
+                        arrs = _pinned_copies(arrs)
                     if mode == "calls":
                         b.set_positions(arrs[0])
                         b.set_positions_nopbc_array(arrs[1])

@@ -116,6 +116,7 @@ static void free_box(Box *b) {
   if (b->g_step) cudaGraphExecDestroy(b->g_step);
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
   if (b->own_stream && b->stream) cudaStreamDestroy(b->stream);
+  if (b->g_io) cudaGraphExecDestroy(b->g_io);
   if (b->s_io) cudaStreamDestroy(b->s_io);
   if (b->ev_io_pos) cudaEventDestroy(b->ev_io_pos);
   if (b->ev_io_done) cudaEventDestroy(b->ev_io_done);
@@ -381,6 +382,11 @@ int relaunch_kernel(Box *b, int which) {
   return FE_ERR_ARG;
 }
 
+static void drop_io_graph(Box *b) {
+  if (b->g_io) cudaGraphExecDestroy(b->g_io);
+  b->g_io = nullptr;
+}
+
 static int capture(Box *b, bool with_list, bool use_nhc, cudaGraphExec_t *out) {
   cudaGraph_t g;
   FE_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
@@ -449,6 +455,7 @@ int fe_box_set_stream(fe_box *box, void *stream) {
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
   b->g_step = b->g_step_list = nullptr;
   b->g_key = -1;
+  drop_io_graph(b);
   return FE_OK;
 }
 
@@ -646,6 +653,7 @@ int fe_box_set_lj_form(fe_box *box, int form) {
   }
   b->lj_form = form;
   b->g_key = -1;  // step graphs are recaptured
+  drop_io_graph(b);
   return FE_OK;
 }
 
@@ -696,6 +704,7 @@ static void drop_step_graphs(Box *b) {
   if (b->g_step_list) cudaGraphExecDestroy(b->g_step_list);
   b->g_step = b->g_step_list = nullptr;
   b->g_key = -1;
+  drop_io_graph(b);
 }
 
 static bool sites_in_range(const int *idx, size_t count, int n) {
@@ -930,6 +939,37 @@ static int k_xyz_gather_on(Box *b, cudaStream_t s) {
   return rc;
 }
 
+// The host-buffer step's copies and kernels: uploads of the step's inputs,
+// the first half kick and drift, the positions' download on the copy
+// stream beside the force evaluation, the second half kick and the
+// downloads of velocities and forces; joined back into b->stream.
+static int io_step_body(Box *b, double vscal, const fe_md_io *io, char *ap, char *np) {
+  int rc;
+  const size_t bytes = sizeof(double) * 3 * (size_t)b->n;
+  // uu is written by the step, not read (integrate_vverlet.c:95-97)
+  FE_CUDA(cudaMemcpyAsync(b->xyz_dev, ap, bytes, cudaMemcpyHostToDevice, b->stream));
+  if ((rc = launch_xyz_scatter(b, b->xyz_dev, true, false))) return rc;
+  FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, np, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaMemcpyAsync(b->vv, io->vv, bytes, cudaMemcpyHostToDevice, b->stream));
+  FE_CUDA(cudaMemcpyAsync(b->ff, io->ff, bytes, cudaMemcpyHostToDevice, b->stream));
+  if ((rc = launch_vv1(b, vscal))) return rc;
+  // the positions are final after the drift: their download runs on the
+  // copy stream while the forces are evaluated
+  FE_CUDA(cudaEventRecord(b->ev_io_pos, b->stream));
+  FE_CUDA(cudaStreamWaitEvent(b->s_io, b->ev_io_pos, 0));
+  if ((rc = k_xyz_gather_on(b, b->s_io))) return rc;
+  FE_CUDA(cudaMemcpyAsync(ap, b->xyz_dev, bytes, cudaMemcpyDeviceToHost, b->s_io));
+  FE_CUDA(cudaMemcpyAsync(np, b->pos_nopbc, bytes, cudaMemcpyDeviceToHost, b->s_io));
+  FE_CUDA(cudaEventRecord(b->ev_io_done, b->s_io));
+  if ((rc = forces_device(b))) return rc;
+  if ((rc = launch_vv2(b, vscal))) return rc;
+  FE_CUDA(cudaMemcpyAsync(io->vv, b->vv, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(io->uu, b->uu, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaMemcpyAsync(io->ff, b->ff, bytes, cudaMemcpyDeviceToHost, b->stream));
+  FE_CUDA(cudaStreamWaitEvent(b->stream, b->ev_io_done, 0));
+  return FE_OK;
+}
+
 int fe_integrate_vverlet_host(fe_box *box, double vscal, const fe_md_io *io, double *en) {
   if (!box || !io || !io->atoms || !io->nopbc || !io->vv || !io->uu || !io->ff) {
     set_error("fe_integrate_vverlet_host: null argument");
@@ -957,28 +997,30 @@ int fe_integrate_vverlet_host(fe_box *box, double vscal, const fe_md_io *io, dou
     FE_CUDA(cudaEventCreateWithFlags(&b->ev_io_pos, cudaEventDisableTiming));
     FE_CUDA(cudaEventCreateWithFlags(&b->ev_io_done, cudaEventDisableTiming));
   }
-  const size_t bytes = sizeof(double) * 3 * (size_t)b->n;
-  // uu is written by the step, not read (integrate_vverlet.c:95-97)
-  FE_CUDA(cudaMemcpyAsync(b->xyz_dev, ap, bytes, cudaMemcpyHostToDevice, b->stream));
-  if ((rc = launch_xyz_scatter(b, b->xyz_dev, true, false))) return rc;
-  FE_CUDA(cudaMemcpyAsync(b->pos_nopbc, np, bytes, cudaMemcpyHostToDevice, b->stream));
-  FE_CUDA(cudaMemcpyAsync(b->vv, io->vv, bytes, cudaMemcpyHostToDevice, b->stream));
-  FE_CUDA(cudaMemcpyAsync(b->ff, io->ff, bytes, cudaMemcpyHostToDevice, b->stream));
-  if ((rc = launch_vv1(b, vscal))) return rc;
-  // the positions are final after the drift: their download runs on the
-  // copy stream while the forces are evaluated
-  FE_CUDA(cudaEventRecord(b->ev_io_pos, b->stream));
-  FE_CUDA(cudaStreamWaitEvent(b->s_io, b->ev_io_pos, 0));
-  if ((rc = k_xyz_gather_on(b, b->s_io))) return rc;
-  FE_CUDA(cudaMemcpyAsync(ap, b->xyz_dev, bytes, cudaMemcpyDeviceToHost, b->s_io));
-  FE_CUDA(cudaMemcpyAsync(np, b->pos_nopbc, bytes, cudaMemcpyDeviceToHost, b->s_io));
-  FE_CUDA(cudaEventRecord(b->ev_io_done, b->s_io));
-  if ((rc = forces_device(b))) return rc;
-  if ((rc = launch_vv2(b, vscal))) return rc;
-  FE_CUDA(cudaMemcpyAsync(io->vv, b->vv, bytes, cudaMemcpyDeviceToHost, b->stream));
-  FE_CUDA(cudaMemcpyAsync(io->uu, b->uu, bytes, cudaMemcpyDeviceToHost, b->stream));
-  FE_CUDA(cudaMemcpyAsync(io->ff, b->ff, bytes, cudaMemcpyDeviceToHost, b->stream));
-  FE_CUDA(cudaStreamWaitEvent(b->stream, b->ev_io_done, 0));
+  // one graph per set of host arrays and velocity scale: a caller that
+  // keeps its arrays (the reference's atom, atnopbc, vv, uu, ff) replays it
+  const void *key[5] = {ap, np, io->vv, io->uu, io->ff};
+  if (!b->g_io || b->io_vscal != vscal || memcmp(key, b->io_key, sizeof key) != 0) {
+    drop_io_graph(b);
+    cudaGraph_t g;
+    FE_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    rc = io_step_body(b, vscal, io, ap, np);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc) {
+      if (e == cudaSuccess) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture (host-buffer step)");
+    e = cudaGraphInstantiate(&b->g_io, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+      b->g_io = nullptr;
+      return cuda_fail(e, "cudaGraphInstantiate (host-buffer step)");
+    }
+    memcpy(b->io_key, key, sizeof key);
+    b->io_vscal = vscal;
+  }
+  FE_CUDA(cudaGraphLaunch(b->g_io, b->stream));
   if ((rc = sync_scal(b))) return rc;
   copy_en(b, en);
   return FE_OK;
@@ -1053,6 +1095,7 @@ int fe_autotune(fe_box *box, int *choice3, double *us) {
     choice3[2] = blocks;
   }
   b->g_key = -1;  // step graphs are recaptured with the new shape
+  drop_io_graph(b);
   return forces_device(b);
 }
 

@@ -74,6 +74,11 @@ struct Box {
   // which overlaps the force evaluation (created on first use)
   cudaStream_t s_io = nullptr;
   cudaEvent_t ev_io_pos = nullptr, ev_io_done = nullptr;
+  // graph of the host-buffer step, captured for one set of host arrays and
+  // one velocity scale; dropped with the step graphs when the box changes
+  cudaGraphExec_t g_io = nullptr;
+  const void *io_key[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  double io_vscal = 0.0;
   int prec = FE_PREC_FP64;
   int lj_form = 0;  // the pair loop's LJ form: 0 CHARMM, 2 the reference's BGO build
 
